@@ -1,0 +1,194 @@
+/*
+ * mbir_gb300.h -- C ABI of the GB300-native MBIR reconstruction engine (HAADF/BF electron
+ * tomography).  Plain pointers and sizes only; no C++ or CUDA types cross this boundary.
+ *
+ * Reference interface each entry point replaces (paths relative to the OpenMBIR-TEM root):
+ *   HAADF_ReconstructionEngine::New / set{TomoInputs,Sinogram,Geometry,AdvParams,ForwardModel}
+ *     -> mbir_params_default + mbir_create + mbir_set_sinogram / mbir_load_sinogram_mrc
+ *        (Code/MBIRLib/HAADF/HAADF_ReconstructionEngine.h:67-99; wiring in
+ *         Code/MBIRLib/HAADF/HAADF_MultiResolutionReconstruction.cpp:392-437)
+ *   HAADF_ReconstructionEngine::execute -> mbir_run  (HAADF_ReconstructionEngine.cpp:327-913)
+ *   AbstractFilter::setCancel / getErrorCondition -> mbir_cancel / return codes + mbir_last_error
+ *     (Code/MBIRLib/Common/AbstractFilter.h:46-82, Observable.h:65-101)
+ *   Geometry->Object read-out, HAADF_ForwardModel::getI_0/getMu/getAlpha
+ *     -> mbir_get_volume / mbir_get_nuisance (HAADF_ForwardModel.h:70-90)
+ *   HAADF_ForwardModel::writeMRCFile / writeReconstructionFile / writeNuisanceParameters
+ *     -> mbir_write_outputs (HAADF_ForwardModel.cpp:34-245)
+ * The step-wise entry points (mbir_prepare, mbir_sweep, mbir_joint_estimation,
+ * mbir_update_weights, mbir_compute_cost, mbir_forward_project) expose the phases execute()
+ * runs internally (forward projection :655-691, updateVoxels :739-740, jointEstimation :774,
+ * updateWeights :784, computeCost :1147) so callers can drive or check them one at a time.
+ *
+ * Threading: mbir_run blocks; mbir_cancel and mbir_status may be called from another thread.
+ * Engines are independent.  Every function returns MBIR_OK (0) or a negative MBIR_E* code;
+ * no C++ exception crosses this boundary.
+ */
+#ifndef MBIR_GB300_H_
+#define MBIR_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MBIR_OK 0
+#define MBIR_EINVAL (-1)     /* bad argument or parameter */
+#define MBIR_ENOMEM (-2)     /* device or host allocation failed */
+#define MBIR_EDEVICE (-3)    /* CUDA error / no usable device */
+#define MBIR_EIO (-4)        /* file could not be read or written */
+#define MBIR_ESTATE (-5)     /* call made in the wrong order */
+#define MBIR_ETIMEOUT (-6)   /* a bounded device wait gave up */
+#define MBIR_ENOTSUP (-7)    /* configuration this build does not run */
+#define MBIR_ECANCELLED (-999) /* the reference's cancel code (HAADF_ReconstructionEngine.cpp:401) */
+
+#define MBIR_MODALITY_HAADF 0
+#define MBIR_MODALITY_BF 1
+
+#define MBIR_ORDER_PARALLEL 0  /* red/black y-slices x conflict-free voxel sets (GPU order) */
+#define MBIR_ORDER_REFERENCE 1 /* the reference's single-task random line order, y sequential */
+
+/* Parameter set: the reference CLI/pipeline inputs (HAADFReconstructionArgsParser.cpp:143-211,
+ * BFReconstructionArgsParser.cpp:145-226), the AdvancedParameters
+ * (ReconstructionStructures.h:164-187, defaults HAADF_ReconstructionEngine.cpp:244-259), the
+ * QGGMRF constants (HAADF_QGGMRFPriorModel.cpp:10-21) and the engine's own switches.
+ * mbir_params_default fills every field; unset fields are zero. */
+typedef struct mbir_params {
+  int32_t struct_size;        /* sizeof(mbir_params), checked by mbir_create */
+  int32_t modality;           /* MBIR_MODALITY_HAADF / MBIR_MODALITY_BF */
+  /* pipeline / TomoInputs */
+  double sample_thickness;    /* --thickness (nm) */
+  double diffuseness;         /* --diffuseness; prior q = diffuseness + 1 */
+  double sigma_x;             /* --sigma_x */
+  double stop_threshold;      /* --stop_threshold */
+  int32_t num_resolutions;    /* --num_resolutions */
+  int32_t final_resolution;   /* --final_resolution */
+  int32_t level;              /* resolution level this engine runs (0 = coarsest); -1 = finest */
+  double target_gain;         /* --target_gain */
+  int32_t outer_iterations;   /* --outer_iterations */
+  int32_t inner_iterations;   /* --inner_iterations */
+  double default_offset;      /* --default_offset */
+  int32_t use_default_offset; /* --use_default_offset */
+  double default_variance;    /* --default_variance */
+  double default_recon_value; /* --default_recon_value */
+  int32_t extend_object;      /* --extend_object */
+  int32_t interpolate_initial_recon; /* --interpolate_initial_recon */
+  int32_t tilt_selection;     /* --tilt_selection: 0 = a-tilt, 1 = b-tilt */
+  int32_t use_subvolume;      /* --subvolume given */
+  int32_t subvolume[6];       /* xmin,ymin,zmin,xmax,ymax,zmax */
+  double default_pixel_size;  /* nm; used when the MRC has no FEI extended header */
+  int32_t n_excluded_views;   /* --exclude_views */
+  int32_t excluded_views[256];
+  /* AdvancedParameters */
+  double x_shrink_factor;     /* 0.6 */
+  int32_t z_stretch;          /* 2 */
+  int32_t detector_response_bins; /* 64 */
+  int32_t profile_resolution; /* 1536 */
+  int32_t beam_resolution;    /* 512 */
+  int32_t joint_estimation;   /* 1 */
+  int32_t zero_skipping;      /* 1 */
+  int32_t noise_model;        /* 1 */
+  int32_t noise_estimation;   /* 0 (never set by the reference; zero-initialised here) */
+  int32_t estimate_prior;     /* 0 */
+  double threshold_reduction_factor; /* 1 */
+  /* QGGMRF prior rho(d) = (|d|^P/s^P) / (c + |d|^(P-Q)/s^(P-Q)) */
+  double qggmrf_p;            /* 2 */
+  double qggmrf_q;            /* 0 -> diffuseness + 1 */
+  double qggmrf_c;            /* 0.001 HAADF, 0.01 BF */
+  double qggmrf_alpha;        /* 1.5 over-relaxation */
+  /* bright field */
+  double bragg_threshold, bragg_delta, bf_offset, default_dosage;
+  /* engine switches */
+  int32_t order_mode;         /* MBIR_ORDER_PARALLEL / MBIR_ORDER_REFERENCE */
+  uint32_t seed;              /* visit-order seed (reference mode: mt19937 seed per sweep) */
+  int32_t compat_double_angle;/* 1: HAADF voxel profile from deg*(pi/180)^2, as the reference */
+  int32_t cost_every_sweep;   /* 1: evaluate the FP64 MAP cost after every sweep */
+  int32_t device;             /* CUDA device ordinal */
+  int32_t verbose;
+} mbir_params;
+
+typedef struct mbir_status {
+  int32_t state;          /* 0 created, 1 sinogram set, 2 prepared, 3 running, 4 done, <0 error */
+  int32_t outer_iter, inner_iter;
+  int32_t sweeps_done;
+  double last_cost;       /* NaN when not computed */
+  double last_rel_update; /* sum|dx| / sum|x| over the ROI from the last sweep */
+  double icd_ms_total;    /* device time in the ICD kernels */
+  double total_ms;        /* wall time of mbir_run */
+  int64_t voxels_visited; /* voxel visits in ICD sweeps (updated + zero-skipped) */
+  int64_t voxels_updated; /* voxel updates (not zero-skipped) */
+  int64_t footprint_entries; /* sum over voxel lines (z,x) of the A-column nonzeros */
+  int32_t t_rows;         /* detector rows touched by one voxel slice (voxel-line response) */
+  int32_t stride;         /* x stride of the conflict-free voxel sets */
+  int32_t staged;         /* 1: voxel slices staged in shared memory, 0: slices read from HBM */
+  int32_t reserved;
+} mbir_status;
+
+typedef struct mbir_engine mbir_engine;
+
+/* defaults of InitializeAdvancedParams + the CLI defaults for the modality */
+void mbir_params_default(mbir_params* p, int32_t modality);
+
+mbir_engine* mbir_create(const mbir_params* p);
+void mbir_destroy(mbir_engine* e);
+const char* mbir_last_error(const mbir_engine* e);
+
+/* Sinogram already cut to the region of interest: counts[theta][r][t] (t fastest), tilts in
+ * degrees (one per view), pixel pitch in nm.  Replaces MRCSinogramInitializer's result. */
+int32_t mbir_set_sinogram(mbir_engine* e, const float* counts, const float* tilts_deg,
+                          int32_t n_theta, int32_t n_r, int32_t n_t, double delta_r,
+                          double delta_t);
+/* MRC modes 0/1/2/6 with FEI extended header; honours use_subvolume/subvolume,
+ * excluded_views and tilt_selection exactly as the reference reader. */
+int32_t mbir_load_sinogram_mrc(mbir_engine* e, const char* path);
+
+/* Optional initial volume [z][x][y] (y fastest), sized as mbir_get_dims reports. */
+int32_t mbir_set_initial_volume(mbir_engine* e, const float* vol, int64_t n);
+/* Optional initial nuisance vectors (length n_theta each; NULL keeps the default). */
+int32_t mbir_set_initial_nuisance(mbir_engine* e, const double* gains, const double* offsets,
+                                  const double* variances);
+
+/* dims[0..2] = N_z, N_x, N_y of the volume; dims[3..5] = N_theta, N_r, N_t */
+int32_t mbir_get_dims(mbir_engine* e, int32_t* dims);
+
+/* execute(): prepare + outer/inner loop + nuisance updates; blocking. */
+int32_t mbir_run(mbir_engine* e);
+
+/* Step-wise phases of execute() */
+int32_t mbir_prepare(mbir_engine* e);
+int32_t mbir_sweep(mbir_engine* e, int32_t outer, int32_t inner, double* stats4);
+int32_t mbir_joint_estimation(mbir_engine* e);
+int32_t mbir_update_weights(mbir_engine* e);
+int32_t mbir_compute_cost(mbir_engine* e, double* parts3, double* total);
+int32_t mbir_forward_project(mbir_engine* e);
+
+/* Read-outs (host buffers owned by the caller) */
+int32_t mbir_get_volume(mbir_engine* e, float* out, int64_t n);          /* [z][x][y] */
+int32_t mbir_get_error_sinogram(mbir_engine* e, float* out, int64_t n);  /* [theta][r][t] */
+int32_t mbir_get_projection(mbir_engine* e, float* out, int64_t n);      /* last forward projection [theta][r][t] */
+int32_t mbir_get_nuisance(mbir_engine* e, double* gains, double* offsets, double* variances);
+/* detector response H [n_theta][bins] and t-response H_t [bins] (FP64 as built) */
+int32_t mbir_get_tables(mbir_engine* e, double* H, double* Ht);
+/* parallel-mode schedule: row order of sweep `sweep` (N_z entries) and the x stride */
+int32_t mbir_get_schedule(mbir_engine* e, int32_t sweep, int32_t* row_order, int32_t* stride);
+int32_t mbir_status_get(mbir_engine* e, mbir_status* st);
+void mbir_cancel(mbir_engine* e);
+
+/* ReconstructedVolume MRC (float32, z reversed, x cropped as the reference), ReconstructedObject.bin
+ * (double, y-x-z), Final{Gain,Offset}Parameters.bin and FinalVariances.bin (double[N_theta]). */
+int32_t mbir_write_outputs(mbir_engine* e, const char* dir, const char* mrc_path);
+
+/* Multi-resolution pipeline (HAADF_MultiResolutionReconstruction::execute,
+ * HAADF_MultiResolutionReconstruction.cpp:175-485): coarse-to-fine levels with sigma_x scaling
+ * and 2x voxel replication hand-off; writes the final volume to out ([z][x][y], n floats). */
+int32_t mbir_run_multires(const mbir_params* p, const float* counts, const float* tilts_deg,
+                          int32_t n_theta, int32_t n_r, int32_t n_t, double delta_r,
+                          double delta_t, float* out, int64_t n, int32_t* dims_out);
+
+/* Library version string */
+const char* mbir_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,91 @@
+"""Build libmbir_gb300.so (sm_103a) in-tree with nvcc; no cmake, no torch extension.
+
+    python openmbir-tem_gb300/build.py            # build if sources are newer than the .so
+    python openmbir-tem_gb300/build.py --force
+
+Translation units compile in parallel; the shared library lands next to this file.
+"""
+import argparse
+import concurrent.futures as cf
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libmbir_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+SOURCES = ["mbir_kernels.cu", "mbir_engine.cu", "mrc_io.cpp", "mbir_capi.cpp"]
+HEADERS = ["mbir_internal.h", "mbir_engine.h"]
+
+
+def nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.sep not in cand or os.path.exists(cand)):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _stale():
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    deps = [os.path.join(CSRC, s) for s in SOURCES + HEADERS]
+    deps.append(os.path.join(ROOT, "include", "mbir_gb300.h"))
+    deps.append(os.path.abspath(__file__))
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _compile(src, verbose=False, ptxas_v=False):
+    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+    cmd = [nvcc(), "-std=c++17", "-O3", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+           "-I", CSRC, "-I", os.path.join(ROOT, "include"), "-c", os.path.join(CSRC, src),
+           "-o", obj]
+    if src.endswith(".cu"):
+        cmd[1:1] = ARCH + ["-lineinfo", "--expt-relaxed-constexpr"]
+        if ptxas_v:
+            cmd.insert(1, "-Xptxas=-v")
+    else:
+        cmd[1:1] = ["-x", "c++"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed for {src}:\n{r.stdout}\n{r.stderr}")
+    return obj, r.stderr
+
+
+def build(force=False, verbose=False, ptxas_v=False):
+    """Compile the CUDA engine into openmbir-tem_gb300/libmbir_gb300.so; returns its path."""
+    if not force and not _stale():
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        results = list(ex.map(lambda s: _compile(s, verbose, ptxas_v), SOURCES))
+    objs = [o for o, _ in results]
+    if ptxas_v:
+        for _, log in results:
+            if log:
+                print(log)
+    tmp = LIB + ".tmp"
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static", "-lrt", "-ldl",
+                                                             "-lpthread"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("--verbose", action="store_true")
+    ap.add_argument("--ptxas-v", action="store_true")
+    a = ap.parse_args()
+    print(build(force=a.force or a.ptxas_v, verbose=a.verbose, ptxas_v=a.ptxas_v))
+    sys.exit(0)

@@ -1,0 +1,184 @@
+// mbir_engine.h -- host side of the GB300 MBIR engine (C++17).  One Engine = one
+// reconstruction resident on one GPU: sinogram, error sinogram, volume and nuisance state
+// stay in HBM from prepare() to destruction.
+#pragma once
+
+#include <atomic>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/mbir_gb300.h"
+#include "mbir_internal.h"
+
+namespace mbir {
+
+// Geometry of one resolution level, FP64, as the reference derives it
+// (InitialReconstructionInitializer.cpp:98-167, MRCSinogramInitializer.cpp:302-305).
+struct Geometry {
+  int n_theta = 0, n_r = 0, n_t = 0;
+  double delta_r = 1, delta_t = 1, R0 = 0, RMax = 0, T0 = 0, TMax = 0;
+  int n_x = 0, n_y = 0, n_z = 0;
+  double delta_xz = 1, delta_xy = 1, x0 = 0, y0 = 0, z0 = 0;
+  double length_x = 0, length_y = 0, length_z = 0;
+  double offset_r = 0, offset_t = 0;
+};
+
+// Tables built once per level (FP64, mirrors of the reference's setup).
+struct Tables {
+  std::vector<double> cosv, sinv;        // [n_theta]
+  std::vector<double> H;                 // [n_theta][bins]
+  std::vector<double> Ht;                // [bins]
+  std::vector<int> t_first, t_count;     // [n_y]
+  std::vector<double> hval;              // [n_y][kMaxTRows]
+  std::vector<uint8_t> line_nonempty;    // [n_z][n_x]
+};
+
+// mt19937 (Matsumoto & Nishimura 1998), the generator behind the reference's boost::mt19937.
+class MT19937 {
+ public:
+  explicit MT19937(uint32_t seed) { this->seed(seed); }
+  void seed(uint32_t s);
+  uint32_t next();
+
+ private:
+  uint32_t mt_[624];
+  int idx_ = 624;
+};
+
+// visit order of UpdateYSlice::execute (HAADF_ReconstructionEngine_UpdateVoxels.cpp:151-241)
+void reference_visit_order(uint32_t seed, int n_z, int n_x, std::vector<int32_t>& out);
+
+class Engine {
+ public:
+  explicit Engine(const mbir_params& p);
+  ~Engine();
+
+  int set_sinogram(const float* counts, const float* tilts_deg, int n_theta, int n_r, int n_t,
+                   double delta_r, double delta_t);
+  int load_mrc(const char* path);
+  int set_initial_volume(const float* vol, int64_t n);
+  int set_initial_nuisance(const double* g, const double* o, const double* v);
+  int dims(int32_t* d) const;
+
+  int prepare();
+  int sweep(int outer, int inner, double* stats4);
+  int joint_estimation();
+  int update_weights();
+  int compute_cost(double* parts3, double* total);
+  int forward_project();
+  int run();
+
+  int get_volume(float* out, int64_t n);
+  int get_error(float* out, int64_t n);
+  int get_projection(float* out, int64_t n);
+  int get_nuisance(double* g, double* o, double* v);
+  int get_tables(double* H, double* Ht);
+  int get_schedule(int sweep, int32_t* row_order, int32_t* stride);
+  int status(mbir_status* st) const;
+  void cancel() { cancel_.store(1); }
+  int write_outputs(const char* dir, const char* mrc_path);
+
+  const char* last_error() const { return err_.c_str(); }
+  int fail(int code, const std::string& msg);
+
+  const Geometry& geometry() const { return g_; }
+
+ private:
+  int build_host();  // geometry, tables, stride, initial nuisance: no GPU needed
+  int build_geometry();
+  int build_tables();
+  int compute_stride();
+  int init_nuisance_host();
+  int alloc_device();
+  int upload_views();  // (gain, weight) pairs and mu/gain doubles
+  int check_device_error();
+  void row_order_for_sweep(int sweep, std::vector<int32_t>& order) const;
+  int cuda_check(int code, const char* what);
+  void release();
+
+  mbir_params p_;
+  std::string err_;
+  std::atomic<int> cancel_{0};
+  int state_ = 0;
+  bool host_ready_ = false;
+
+  // host inputs
+  std::vector<float> counts_;     // [theta][r][t]
+  std::vector<double> tilts_;     // degrees
+  std::vector<float> init_vol_;   // optional [z][x][y]
+  std::vector<double> user_gain_, user_offset_, user_var_;
+
+  Geometry g_;
+  Tables tab_;
+  int bins_ = 64;
+  int nb_ = 3;        // candidate bins per view (2*half_width + 1)
+  int n_rp_ = 0;      // HBM row stride
+  int n_rs_ = 0;      // shared-memory row stride
+  int t_rows_ = 1;    // max t rows per voxel slice
+  int stride_ = 2;    // conflict-free x stride
+  bool stage_ = true; // slice fits in shared memory
+  size_t smem_bytes_ = 0;
+  DevFilter flt_{};
+  DevGeom dg_{};
+
+  // nuisance state (FP64, host copy is authoritative)
+  std::vector<double> I_, mu_, alpha_, w_;
+  std::vector<double> init_gain_, init_offset_, init_var_;
+
+  // device buffers
+  float* d_y_ = nullptr;
+  float* d_e_ = nullptr;
+  float* d_yest_ = nullptr;
+  float* d_x_ = nullptr;
+  float* d_stage_ = nullptr;  // host-layout staging buffer for transposes
+  float* d_H_ = nullptr;
+  float2* d_bx_ = nullptr;
+  double* d_u0_ = nullptr;
+  double* d_bz_ = nullptr;
+  float2* d_gw_ = nullptr;
+  int* d_tfirst_ = nullptr;
+  int* d_tcount_ = nullptr;
+  float* d_hval_ = nullptr;
+  int* d_rows_ = nullptr;
+  int* d_lines_ = nullptr;
+  double* d_stats_ = nullptr;   // [max slices][4]
+  double* d_stat4_ = nullptr;   // [4]
+  double* d_mu_ = nullptr;      // [n_theta]
+  double* d_gain_ = nullptr;
+  double* d_mu2_ = nullptr;
+  double* d_gain2_ = nullptr;
+  double* d_wv_ = nullptr;
+  double* d_partial_ = nullptr; // view sums partials
+  double* d_vsum_ = nullptr;    // [n_theta*6]
+  int* d_err_ = nullptr;
+  void* stream_ = nullptr;
+  void* ev0_ = nullptr;
+  void* ev1_ = nullptr;
+  int n_chunk_ = 8;
+  int prior_blocks_ = 152 * 4;
+
+  // progress
+  int sweeps_done_ = 0;
+  int outer_ = 0, inner_ = 0;
+  double last_cost_ = 0.0 / 0.0;
+  double last_rel_ = 0.0;
+  double icd_ms_ = 0.0;
+  double total_ms_ = 0.0;
+  int64_t visited_ = 0, updated_ = 0;
+  int64_t footprint_entries_ = 0;
+};
+
+// MRC I/O (mrc_io.cpp)
+struct MrcVolume {
+  int nx = 0, ny = 0, nz = 0, mode = 0;
+  bool has_fei = false;
+  std::vector<float> a_tilt, b_tilt, pixel_size;  // per section from the FEI extended header
+  std::vector<float> data;                         // sub-volume as float, [z][y][x]
+};
+int mrc_read(const std::string& path, const int* vmin, const int* vmax, MrcVolume& out,
+             bool header_only, std::string& err);
+int mrc_write_volume(const std::string& path, const float* zxy, int n_z, int n_x, int n_y,
+                     int x_start, int x_end, double length_x, std::string& err);
+
+}  // namespace mbir

@@ -1,0 +1,320 @@
+// mrc_io.cpp -- MRC tilt-series reader and volume writer, byte-compatible with the
+// reference's MRCReader / MRCWriter (Code/MBIRLib/IOFilters/MRCReader.cpp:99-368,
+// MRCWriter.cpp:90-290; header layout MRCHeader.h:46-212).  Fields are read and written at
+// their fixed byte offsets, little-endian, so no struct packing is assumed.
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "mbir_engine.h"
+
+namespace mbir {
+
+namespace {
+constexpr int kHeaderBytes = 1024;
+constexpr int kFeiBytes = 128;  // FEIHeader: 14 floats + 72 unused bytes
+
+int32_t rd_i32(const unsigned char* b, int off) {
+  int32_t v;
+  std::memcpy(&v, b + off, 4);
+  return v;
+}
+float rd_f32(const unsigned char* b, int off) {
+  float v;
+  std::memcpy(&v, b + off, 4);
+  return v;
+}
+void wr_i32(unsigned char* b, int off, int32_t v) { std::memcpy(b + off, &v, 4); }
+void wr_f32(unsigned char* b, int off, float v) { std::memcpy(b + off, &v, 4); }
+void wr_i16(unsigned char* b, int off, int16_t v) { std::memcpy(b + off, &v, 2); }
+}  // namespace
+
+int mrc_read(const std::string& path, const int* vmin, const int* vmax, MrcVolume& out,
+             bool header_only, std::string& err) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) {
+    err = "cannot open MRC file '" + path + "'";
+    return MBIR_EIO;
+  }
+  unsigned char h[kHeaderBytes];
+  if (std::fread(h, 1, kHeaderBytes, f) != kHeaderBytes) {
+    std::fclose(f);
+    err = "MRC header truncated";
+    return MBIR_EIO;
+  }
+  out.nx = rd_i32(h, 0);
+  out.ny = rd_i32(h, 4);
+  out.nz = rd_i32(h, 8);
+  out.mode = rd_i32(h, 12);
+  const int32_t next = rd_i32(h, 92);
+  if (out.nx <= 0 || out.ny <= 0 || out.nz <= 0 || next < 0) {
+    std::fclose(f);
+    err = "MRC header has invalid dimensions";
+    return MBIR_EINVAL;
+  }
+  std::vector<unsigned char> ext(static_cast<size_t>(next));
+  if (next > 0 && std::fread(ext.data(), 1, ext.size(), f) != ext.size()) {
+    std::fclose(f);
+    err = "MRC extended header truncated";
+    return MBIR_EIO;
+  }
+  // FEI extended header is recognised by the first label (MRCReader.cpp:121-165)
+  const std::string label0(reinterpret_cast<const char*>(h + 224), 80);
+  out.has_fei = (label0.find("Fei Company") != std::string::npos ||
+                 label0.find("EIC project") != std::string::npos ||
+                 label0.find("MCAP project, MDG, Copyright 2013") != std::string::npos);
+  if (label0.find("tif2mrc: Converted to MRC format") != std::string::npos) out.has_fei = false;
+  out.a_tilt.clear();
+  out.b_tilt.clear();
+  out.pixel_size.clear();
+  if (out.has_fei) {
+    if (static_cast<int64_t>(next) < static_cast<int64_t>(kFeiBytes) * out.nz) {
+      std::fclose(f);
+      err = "FEI extended header shorter than nz entries";
+      return MBIR_EINVAL;
+    }
+    for (int z = 0; z < out.nz; z++) {
+      const unsigned char* e = ext.data() + static_cast<size_t>(z) * kFeiBytes;
+      out.a_tilt.push_back(rd_f32(e, 0));
+      out.b_tilt.push_back(rd_f32(e, 4));
+      out.pixel_size.push_back(rd_f32(e, 44));
+    }
+  }
+  if (header_only) {
+    std::fclose(f);
+    return MBIR_OK;
+  }
+  size_t tsize = 0;
+  switch (out.mode) {
+    case 0: tsize = 1; break;
+    case 1: tsize = 2; break;
+    case 2: tsize = 4; break;
+    case 6: tsize = 2; break;
+    default:
+      std::fclose(f);
+      err = "unsupported MRC mode";
+      return MBIR_EINVAL;
+  }
+  int lo[3] = {0, 0, 0}, hi[3] = {out.nx - 1, out.ny - 1, out.nz - 1};
+  if (vmin && vmax)
+    for (int i = 0; i < 3; i++) {
+      lo[i] = vmin[i];
+      hi[i] = vmax[i];
+    }
+  const int dims[3] = {out.nx, out.ny, out.nz};
+  for (int i = 0; i < 3; i++)
+    if (lo[i] < 0 || hi[i] >= dims[i] || lo[i] > hi[i]) {
+      std::fclose(f);
+      err = "MRC sub-volume out of range";
+      return MBIR_EINVAL;
+    }
+  const long data_start = kHeaderBytes + next;
+  const int sx = hi[0] - lo[0] + 1, sy = hi[1] - lo[1] + 1, sz = hi[2] - lo[2] + 1;
+  out.data.assign(static_cast<size_t>(sx) * sy * sz, 0.f);
+  std::vector<unsigned char> row(static_cast<size_t>(sx) * tsize);
+  size_t o = 0;
+  // readPartialVolume (MRCReader.cpp:331-362): one x-run per (z, y)
+  for (int z = lo[2]; z <= hi[2]; ++z)
+    for (int y = lo[1]; y <= hi[1]; ++y) {
+      const long long off = (static_cast<long long>(out.nx) * out.ny * z +
+                             static_cast<long long>(out.nx) * y + lo[0]) *
+                            static_cast<long long>(tsize);
+      if (std::fseek(f, data_start + static_cast<long>(off), SEEK_SET) != 0 ||
+          std::fread(row.data(), 1, row.size(), f) != row.size()) {
+        std::fclose(f);
+        err = "MRC data truncated";
+        return MBIR_EIO;
+      }
+      for (int x = 0; x < sx; ++x) {
+        float v;
+        const unsigned char* p = row.data() + static_cast<size_t>(x) * tsize;
+        switch (out.mode) {
+          case 0: v = static_cast<float>(p[0]); break;
+          case 1: {
+            int16_t s;
+            std::memcpy(&s, p, 2);
+            v = static_cast<float>(s);
+            break;
+          }
+          case 2: std::memcpy(&v, p, 4); break;
+          default: {
+            uint16_t s;
+            std::memcpy(&s, p, 2);
+            v = static_cast<float>(s);
+            break;
+          }
+        }
+        out.data[o++] = v;
+      }
+    }
+  std::fclose(f);
+  return MBIR_OK;
+}
+
+// MRCWriter::initializeMRCHeader + write (MRCWriter.cpp:90-290): float32 volume, sections
+// written from z = N_z-1 down to 0, each section [y][x] over x in [x_start, x_end).
+int mrc_write_volume(const std::string& path, const float* zxy, int n_z, int n_x, int n_y,
+                     int x_start, int x_end, double length_x, std::string& err) {
+  if (x_start < 0) x_start = 0;
+  if (x_end > n_x) x_end = n_x;
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) {
+    err = "cannot open '" + path + "' for writing";
+    return MBIR_EIO;
+  }
+  unsigned char h[kHeaderBytes];
+  std::memset(h, 0, sizeof(h));
+  const int nx = x_end - x_start, ny = n_y, nz = n_z;
+  wr_i32(h, 0, nx);
+  wr_i32(h, 4, ny);
+  wr_i32(h, 8, nz);
+  wr_i32(h, 12, 2);
+  wr_i32(h, 28, nx);
+  wr_i32(h, 32, ny);
+  wr_i32(h, 36, nz);
+  wr_f32(h, 40, static_cast<float>(nx));
+  wr_f32(h, 44, static_cast<float>(ny));
+  wr_f32(h, 48, static_cast<float>(nz));
+  wr_f32(h, 52, 90.f);
+  wr_f32(h, 56, 90.f);
+  wr_f32(h, 60, 90.f);
+  wr_i32(h, 64, 1);
+  wr_i32(h, 68, 2);
+  wr_i32(h, 72, 3);
+  wr_i16(h, 88, 0);
+  wr_i32(h, 92, kFeiBytes * nz);
+  std::memcpy(h + 208, "MAP ", 4);
+  h[212] = 68;
+  h[213] = 65;
+  wr_i32(h, 220, 3);
+  std::snprintf(reinterpret_cast<char*>(h + 224), 80, "Fei Company (C) Copyright 2003");
+  std::snprintf(reinterpret_cast<char*>(h + 304), 80, "Reconstruction by OpenMBIR");
+  std::snprintf(reinterpret_cast<char*>(h + 384), 80,
+                "OpenMBIR code developed by Purdue University & BlueQuartz Software");
+  std::fwrite(h, 1, kHeaderBytes, f);
+  unsigned char fei[kFeiBytes];
+  for (int i = 0; i < nz; ++i) {
+    std::memset(fei, 0, sizeof(fei));
+    wr_f32(fei, 44, static_cast<float>(length_x));
+    std::fwrite(fei, 1, kFeiBytes, f);
+  }
+  std::vector<float> slice(static_cast<size_t>(nx) * ny);
+  float mean = 0.0f;
+  size_t count = 0;
+  float dmax = static_cast<float>(std::numeric_limits<double>::min());
+  float dmin = static_cast<float>(std::numeric_limits<double>::max());
+  for (int z = n_z - 1; z >= 0; z--) {
+    size_t idx = 0;
+    for (int y = 0; y < ny; ++y)
+      for (int x = x_start; x < x_end; ++x) {
+        const float d = zxy[(static_cast<size_t>(z) * n_x + x) * n_y + y];
+        slice[idx] = d;
+        mean += slice[idx];
+        count++;
+        if (d > dmax) dmax = d;
+        if (d < dmin) dmin = d;
+        ++idx;
+      }
+    std::fwrite(slice.data(), sizeof(float), slice.size(), f);
+  }
+  mean = count ? mean / count : 0.f;
+  std::fseek(f, 76, SEEK_SET);
+  std::fwrite(&dmin, 4, 1, f);
+  std::fwrite(&dmax, 4, 1, f);
+  std::fwrite(&mean, 4, 1, f);
+  std::fclose(f);
+  return MBIR_OK;
+}
+
+// MRCSinogramInitializer::execute (MRCSinogramInitializer.cpp:79-339) plus the tilt read of
+// the CLI (HAADFReconstructionArgsParser.cpp:296-322).
+int Engine::load_mrc(const char* path) {
+  if (!path) return fail(MBIR_EINVAL, "load_mrc: null path");
+  MrcVolume hdr;
+  std::string err;
+  int rc = mrc_read(path, nullptr, nullptr, hdr, true, err);
+  if (rc) return fail(rc, err);
+  if (hdr.mode != 1 && hdr.mode != 2 && hdr.mode != 6)
+    return fail(MBIR_EINVAL,
+                "The data type of the MRC file was not either 1 (signed 16 Bit Ints), 2 (32 bit "
+                "floats) or 6 (unsigned 16 Bit Ints)");
+  if (!hdr.has_fei) return fail(MBIR_EINVAL, "MRC file carries no FEI tilt angles");
+  int vmin[3] = {0, 0, 0}, vmax[3] = {hdr.nx - 1, hdr.ny - 1, hdr.nz - 1};
+  if (p_.use_subvolume) {
+    const int levels = p_.num_resolutions > 0 ? p_.num_resolutions : 1;
+    const int interp = (1 << (levels - 1)) * (p_.final_resolution > 0 ? p_.final_resolution : 1);
+    int xs = p_.subvolume[0], ys = p_.subvolume[1], zs = p_.subvolume[2];
+    int xe = p_.subvolume[3], ye = p_.subvolume[4], ze = p_.subvolume[5];
+    vmin[0] = xs;
+    vmin[1] = ys;
+    vmin[2] = zs;
+    vmax[0] = xe;
+    vmax[1] = ye;
+    vmax[2] = ze;
+    const double cor = hdr.nx / 2;  // integer division as in the reference
+    double left = cor - vmin[0];
+    double right = vmax[0] - cor + 1;
+    if (left < 0) {
+      vmin[0] = static_cast<int>(cor + left);
+      left *= -1;
+    }
+    if (right < 0) {
+      vmax[0] = static_cast<int>(cor - right);
+      right *= -1;
+    }
+    if (left != right) {
+      if (left < right) {
+        double tx = cor + left - 1;
+        if (tx >= hdr.nx) tx = hdr.nx - 1;
+        vmax[0] = static_cast<int>(tx);
+      } else {
+        double tx = cor - right;
+        if (tx < 0) tx = 0;
+        vmin[0] = static_cast<int>(tx);
+      }
+    }
+    const int16_t disty = static_cast<int16_t>(ye - ys + 1);
+    const int16_t rem = static_cast<int16_t>(disty % (interp * 3));
+    if (rem != 0) {
+      const int16_t remainder = static_cast<int16_t>(interp * 3 - rem);
+      if (ye + remainder < hdr.ny)
+        ye += remainder;
+      else
+        ye = hdr.ny - 1;
+    }
+    vmax[1] = ye;
+  }
+  const int n_r = vmax[0] - vmin[0] + 1, n_t = vmax[1] - vmin[1] + 1;
+  double dr = p_.default_pixel_size > 0 ? p_.default_pixel_size : 1.0;
+  if (hdr.has_fei) dr = static_cast<double>(hdr.pixel_size[0]) * 1.0e9;
+  std::vector<int> good;
+  for (int i = vmin[2]; i <= vmax[2]; ++i) {
+    bool keep = true;
+    for (int j = 0; j < p_.n_excluded_views && j < 256; ++j)
+      if (p_.excluded_views[j] == i) keep = false;
+    if (keep) good.push_back(i);
+  }
+  if (good.empty()) return fail(MBIR_EINVAL, "no views left after exclusion");
+  MrcVolume vol;
+  rc = mrc_read(path, vmin, vmax, vol, false, err);
+  if (rc) return fail(rc, err);
+  const int n_theta = static_cast<int>(good.size());
+  std::vector<float> counts(static_cast<size_t>(n_theta) * n_r * n_t);
+  std::vector<float> tilts(n_theta);
+  const std::vector<float>& src_tilts = p_.tilt_selection == 0 ? hdr.a_tilt : hdr.b_tilt;
+  for (int z = 0; z < n_theta; z++) {
+    const int dz = good[z] - vmin[2];
+    // the reference indexes the tilt list by the kept-view position, not the file section
+    // (MRCSinogramInitializer.cpp:271)
+    tilts[z] = src_tilts[z];
+    for (int y = 0; y < n_t; y++)
+      for (int x = 0; x < n_r; x++)
+        counts[(static_cast<size_t>(z) * n_r + x) * n_t + y] =
+            vol.data[static_cast<size_t>(dz) * n_r * n_t + static_cast<size_t>(y) * n_r + x];
+  }
+  return set_sinogram(counts.data(), tilts.data(), n_theta, n_r, n_t, dr, dr);
+}
+
+}  // namespace mbir

@@ -1,0 +1,318 @@
+"""ctypes binding of libmbir_gb300.so (the C ABI in include/mbir_gb300.h).
+
+This is a thin host-side wrapper for Python callers, tests and the benchmark.  It loads the
+in-tree CUDA library and raises if it is missing: there is no CPU fallback.
+
+    import mbir
+    p = mbir.default_params()
+    p.sample_thickness = 32; p.diffuseness = 0.1; p.sigma_x = 0.2; p.num_resolutions = 1
+    eng = mbir.Engine(p)
+    eng.set_sinogram(counts, tilts_deg, delta_r=1.0, delta_t=1.0)   # counts[theta][r][t]
+    eng.run()
+    vol = eng.volume()                                              # [z][x][y]
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmbir_gb300.so")
+
+MBIR_OK = 0
+ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "EDEVICE", -4: "EIO", -5: "ESTATE", -6: "ETIMEOUT",
+          -7: "ENOTSUP", -999: "ECANCELLED"}
+HAADF, BF = 0, 1
+ORDER_PARALLEL, ORDER_REFERENCE = 0, 1
+
+
+class MbirParams(C.Structure):
+    """Mirror of struct mbir_params (include/mbir_gb300.h); field order and types must match."""
+    _fields_ = [
+        ("struct_size", C.c_int32),
+        ("modality", C.c_int32),
+        ("sample_thickness", C.c_double),
+        ("diffuseness", C.c_double),
+        ("sigma_x", C.c_double),
+        ("stop_threshold", C.c_double),
+        ("num_resolutions", C.c_int32),
+        ("final_resolution", C.c_int32),
+        ("level", C.c_int32),
+        ("target_gain", C.c_double),
+        ("outer_iterations", C.c_int32),
+        ("inner_iterations", C.c_int32),
+        ("default_offset", C.c_double),
+        ("use_default_offset", C.c_int32),
+        ("default_variance", C.c_double),
+        ("default_recon_value", C.c_double),
+        ("extend_object", C.c_int32),
+        ("interpolate_initial_recon", C.c_int32),
+        ("tilt_selection", C.c_int32),
+        ("use_subvolume", C.c_int32),
+        ("subvolume", C.c_int32 * 6),
+        ("default_pixel_size", C.c_double),
+        ("n_excluded_views", C.c_int32),
+        ("excluded_views", C.c_int32 * 256),
+        ("x_shrink_factor", C.c_double),
+        ("z_stretch", C.c_int32),
+        ("detector_response_bins", C.c_int32),
+        ("profile_resolution", C.c_int32),
+        ("beam_resolution", C.c_int32),
+        ("joint_estimation", C.c_int32),
+        ("zero_skipping", C.c_int32),
+        ("noise_model", C.c_int32),
+        ("noise_estimation", C.c_int32),
+        ("estimate_prior", C.c_int32),
+        ("threshold_reduction_factor", C.c_double),
+        ("qggmrf_p", C.c_double),
+        ("qggmrf_q", C.c_double),
+        ("qggmrf_c", C.c_double),
+        ("qggmrf_alpha", C.c_double),
+        ("bragg_threshold", C.c_double),
+        ("bragg_delta", C.c_double),
+        ("bf_offset", C.c_double),
+        ("default_dosage", C.c_double),
+        ("order_mode", C.c_int32),
+        ("seed", C.c_uint32),
+        ("compat_double_angle", C.c_int32),
+        ("cost_every_sweep", C.c_int32),
+        ("device", C.c_int32),
+        ("verbose", C.c_int32),
+    ]
+
+
+class MbirStatus(C.Structure):
+    _fields_ = [
+        ("state", C.c_int32), ("outer_iter", C.c_int32), ("inner_iter", C.c_int32),
+        ("sweeps_done", C.c_int32), ("last_cost", C.c_double), ("last_rel_update", C.c_double),
+        ("icd_ms_total", C.c_double), ("total_ms", C.c_double), ("voxels_visited", C.c_int64),
+        ("voxels_updated", C.c_int64), ("footprint_entries", C.c_int64), ("t_rows", C.c_int32),
+        ("stride", C.c_int32), ("staged", C.c_int32), ("reserved", C.c_int32),
+    ]
+
+
+_lib = None
+
+_F = C.POINTER(C.c_float)
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int32)
+
+SIGNATURES = {
+    "mbir_version": (C.c_char_p, []),
+    "mbir_params_default": (None, [C.POINTER(MbirParams), C.c_int32]),
+    "mbir_create": (C.c_void_p, [C.POINTER(MbirParams)]),
+    "mbir_destroy": (None, [C.c_void_p]),
+    "mbir_last_error": (C.c_char_p, [C.c_void_p]),
+    "mbir_set_sinogram": (C.c_int32, [C.c_void_p, _F, _F, C.c_int32, C.c_int32, C.c_int32,
+                                      C.c_double, C.c_double]),
+    "mbir_load_sinogram_mrc": (C.c_int32, [C.c_void_p, C.c_char_p]),
+    "mbir_set_initial_volume": (C.c_int32, [C.c_void_p, _F, C.c_int64]),
+    "mbir_set_initial_nuisance": (C.c_int32, [C.c_void_p, _D, _D, _D]),
+    "mbir_get_dims": (C.c_int32, [C.c_void_p, _I]),
+    "mbir_run": (C.c_int32, [C.c_void_p]),
+    "mbir_prepare": (C.c_int32, [C.c_void_p]),
+    "mbir_sweep": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, _D]),
+    "mbir_joint_estimation": (C.c_int32, [C.c_void_p]),
+    "mbir_update_weights": (C.c_int32, [C.c_void_p]),
+    "mbir_compute_cost": (C.c_int32, [C.c_void_p, _D, _D]),
+    "mbir_forward_project": (C.c_int32, [C.c_void_p]),
+    "mbir_get_volume": (C.c_int32, [C.c_void_p, _F, C.c_int64]),
+    "mbir_get_error_sinogram": (C.c_int32, [C.c_void_p, _F, C.c_int64]),
+    "mbir_get_projection": (C.c_int32, [C.c_void_p, _F, C.c_int64]),
+    "mbir_get_nuisance": (C.c_int32, [C.c_void_p, _D, _D, _D]),
+    "mbir_get_tables": (C.c_int32, [C.c_void_p, _D, _D]),
+    "mbir_get_schedule": (C.c_int32, [C.c_void_p, C.c_int32, _I, _I]),
+    "mbir_status_get": (C.c_int32, [C.c_void_p, C.POINTER(MbirStatus)]),
+    "mbir_cancel": (None, [C.c_void_p]),
+    "mbir_write_outputs": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_char_p]),
+    "mbir_run_multires": (C.c_int32, [C.POINTER(MbirParams), _F, _F, C.c_int32, C.c_int32,
+                                      C.c_int32, C.c_double, C.c_double, _F, C.c_int64, _I]),
+}
+
+
+def lib():
+    """Load libmbir_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with openmbir-tem_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def default_params(modality=HAADF):
+    p = MbirParams()
+    lib().mbir_params_default(C.byref(p), modality)
+    if p.struct_size != C.sizeof(MbirParams):
+        raise RuntimeError("mbir_params layout mismatch between the binding and the library")
+    return p
+
+
+def _fp(a):
+    return a.ctypes.data_as(_F)
+
+
+def _dp(a):
+    return a.ctypes.data_as(_D) if a is not None else None
+
+
+class MbirError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Engine:
+    """One reconstruction on one GPU (mbir_engine*)."""
+
+    def __init__(self, params):
+        self._h = lib().mbir_create(C.byref(params))
+        if not self._h:
+            raise MbirError(-1, lib().mbir_last_error(None).decode())
+        self.params = params
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mbir_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != MBIR_OK:
+            raise MbirError(rc, lib().mbir_last_error(self._h).decode())
+        return rc
+
+    def set_sinogram(self, counts, tilts_deg, delta_r=1.0, delta_t=1.0):
+        counts = np.ascontiguousarray(counts, dtype=np.float32)
+        tilts = np.ascontiguousarray(tilts_deg, dtype=np.float32)
+        nt, nr, ntt = counts.shape
+        self._counts = counts
+        return self._check(lib().mbir_set_sinogram(self._h, _fp(counts), _fp(tilts), nt, nr, ntt,
+                                                   delta_r, delta_t))
+
+    def load_mrc(self, path):
+        return self._check(lib().mbir_load_sinogram_mrc(self._h, str(path).encode()))
+
+    def dims(self):
+        d = np.zeros(6, np.int32)
+        self._check(lib().mbir_get_dims(self._h, d.ctypes.data_as(_I)))
+        return tuple(int(v) for v in d)
+
+    def set_initial_volume(self, vol):
+        vol = np.ascontiguousarray(vol, dtype=np.float32)
+        return self._check(lib().mbir_set_initial_volume(self._h, _fp(vol), vol.size))
+
+    def set_initial_nuisance(self, gains=None, offsets=None, variances=None):
+        g = None if gains is None else np.ascontiguousarray(gains, np.float64)
+        o = None if offsets is None else np.ascontiguousarray(offsets, np.float64)
+        v = None if variances is None else np.ascontiguousarray(variances, np.float64)
+        return self._check(lib().mbir_set_initial_nuisance(self._h, _dp(g), _dp(o), _dp(v)))
+
+    def prepare(self):
+        return self._check(lib().mbir_prepare(self._h))
+
+    def run(self):
+        return self._check(lib().mbir_run(self._h))
+
+    def sweep(self, outer=0, inner=0):
+        st = np.zeros(4, np.float64)
+        self._check(lib().mbir_sweep(self._h, outer, inner, _dp(st)))
+        return st
+
+    def joint_estimation(self):
+        return self._check(lib().mbir_joint_estimation(self._h))
+
+    def update_weights(self):
+        return self._check(lib().mbir_update_weights(self._h))
+
+    def cost(self):
+        parts = np.zeros(3, np.float64)
+        tot = C.c_double()
+        self._check(lib().mbir_compute_cost(self._h, _dp(parts), C.byref(tot)))
+        return tot.value, parts
+
+    def forward_project(self):
+        return self._check(lib().mbir_forward_project(self._h))
+
+    def volume(self):
+        nz, nx, ny = self.dims()[:3]
+        out = np.empty((nz, nx, ny), np.float32)
+        self._check(lib().mbir_get_volume(self._h, _fp(out), out.size))
+        return out
+
+    def _sino(self, fn):
+        _, _, _, nt, nr, ntt = self.dims()
+        out = np.empty((nt, nr, ntt), np.float32)
+        self._check(fn(self._h, _fp(out), out.size))
+        return out
+
+    def error_sinogram(self):
+        return self._sino(lib().mbir_get_error_sinogram)
+
+    def projection(self):
+        return self._sino(lib().mbir_get_projection)
+
+    def nuisance(self):
+        nt = self.dims()[3]
+        g, o, v = (np.zeros(nt) for _ in range(3))
+        self._check(lib().mbir_get_nuisance(self._h, _dp(g), _dp(o), _dp(v)))
+        return g, o, v
+
+    def tables(self):
+        nt = self.dims()[3]
+        bins = self.params.detector_response_bins
+        H = np.zeros((nt, bins))
+        Ht = np.zeros(bins)
+        self._check(lib().mbir_get_tables(self._h, _dp(H), _dp(Ht)))
+        return H, Ht
+
+    def schedule(self, sweep=0):
+        nz = self.dims()[0]
+        rows = np.zeros(nz, np.int32)
+        stride = C.c_int32()
+        self._check(lib().mbir_get_schedule(self._h, sweep, rows.ctypes.data_as(_I),
+                                            C.byref(stride)))
+        return rows, stride.value
+
+    def status(self):
+        st = MbirStatus()
+        self._check(lib().mbir_status_get(self._h, C.byref(st)))
+        return st
+
+    def cancel(self):
+        lib().mbir_cancel(self._h)
+
+    def write_outputs(self, directory, mrc_path=""):
+        return self._check(lib().mbir_write_outputs(self._h, str(directory).encode(),
+                                                    str(mrc_path).encode()))
+
+
+def run_multires(params, counts, tilts_deg, delta_r=1.0, delta_t=1.0):
+    counts = np.ascontiguousarray(counts, np.float32)
+    tilts = np.ascontiguousarray(tilts_deg, np.float32)
+    nt, nr, ntt = counts.shape
+    finest = MbirParams.from_buffer_copy(params)
+    finest.level = -1
+    with Engine(finest) as probe:
+        probe.set_sinogram(counts, tilts, delta_r, delta_t)
+        nz, nx, ny = probe.dims()[:3]
+    dims = np.zeros(3, np.int32)
+    out = np.empty((nz, nx, ny), np.float32)
+    rc = lib().mbir_run_multires(C.byref(params), _fp(counts), _fp(tilts), nt, nr, ntt, delta_r,
+                                 delta_t, _fp(out), out.size, dims.ctypes.data_as(_I))
+    if rc != MBIR_OK:
+        raise MbirError(rc, "multires")
+    return out

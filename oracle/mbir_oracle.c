@@ -1,0 +1,911 @@
+/*
+ * mbir_oracle.c -- CPU restatement (FP64) of OpenMBIR-TEM's HAADF reconstruction path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the GB300 engine.  Loaded by tests/, by
+ * __graft_entry__.smoke() and by the cpu_baseline leg of bench.py; never by the product.
+ *
+ * All paths below are relative to the reference project root (Code/MBIRLib/...).
+ * Arithmetic is FP64 throughout, in the reference's loop order, so that the restatement
+ * reproduces the reference to rounding; it is pinned against the reference's own sources
+ * (oracle/ref_harness.cpp, tests/test_oracle_pin.py).
+ */
+#include "mbir_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+#define M_PI_2_ (M_PI / 2.0)
+#define M_PI_4_ (M_PI / 4.0)
+
+#define IDX3(i, j, k) (9 * (i) + 3 * (j) + (k))
+
+/* 26-neighbour prior weights, indexed [dy+1][dz+1][dx+1]
+ * (HAADF/HAADF_ReconstructionEngine.cpp:266-294, same table in _UpdateVoxels.cpp:556-585). */
+static const double k_filter[27] = {
+  0.0302, 0.0370, 0.0302, 0.0370, 0.0523, 0.0370, 0.0302, 0.0370, 0.0302,
+  0.0370, 0.0523, 0.0370, 0.0523, 0.0000, 0.0523, 0.0370, 0.0523, 0.0370,
+  0.0302, 0.0370, 0.0302, 0.0370, 0.0523, 0.0370, 0.0302, 0.0370, 0.0302};
+
+struct orc_ctx {
+  orc_params p;
+  int n_theta, n_r, n_t;
+  double delta_r, delta_t, R0, RMax, T0, TMax;
+  int n_x, n_y, n_z;
+  double delta_xz, delta_xy, x0, y0, z0, length_x, length_y, length_z;
+  double offset_r, offset_t;
+  double* angles_deg;
+  double* cosv;
+  double* sinv;
+  double* profile;
+  double* beam;
+  double* H;
+  double* Ht;
+  int* vlr_first;
+  int* vlr_count;
+  double* vlr_val; /* [n_y][vlr_cap] */
+  int vlr_cap;
+  int* col_start;
+  int* col_count;
+  int* col_index;
+  double* col_val;
+  double* counts;
+  double* x;
+  double* e;
+  double* w;
+  double* yest;
+  double* I;
+  double* mu;
+  double* alpha;
+  double* init_gain;
+  double* init_offset;
+  double* init_var;
+  unsigned char* mask;
+  double* mag_map;
+  double sig_p, sig_pq, sig_q;
+};
+
+/* ---------------------------------------------------------------------------------------
+ * QGGMRF prior (Reconstruction/QGGMRF_Functions.cpp:82-206)
+ * ------------------------------------------------------------------------------------- */
+static double q_value(const orc_ctx* c, double delta) {
+  /* QGGMRF_Functions.cpp:82-85 */
+  return (pow(fabs(delta), c->p.mrf_p) / c->sig_p) /
+         (c->p.mrf_c + pow(fabs(delta), c->p.mrf_p - c->p.mrf_q) / c->sig_pq);
+}
+
+static double q_derivative(const orc_ctx* c, double delta) {
+  /* QGGMRF_Functions.cpp:90-104 */
+  double P = c->p.mrf_p, Q = c->p.mrf_q;
+  double t1 = pow(fabs(delta), P - Q) / c->sig_pq;
+  double t2 = pow(fabs(delta), P - 1);
+  double t3 = c->p.mrf_c + t1;
+  if (delta < 0) return ((-1 * t2 / (t3 * c->sig_p)) * (P - ((P - Q) * t1) / (t3)));
+  return ((t2 / (t3 * c->sig_p)) * (P - ((P - Q) * t1) / (t3)));
+}
+
+static double q_second_at_zero(const orc_ctx* c) {
+  /* QGGMRF_Functions.cpp:109-112 */
+  return c->p.mrf_p / (c->sig_p * c->p.mrf_c);
+}
+
+static double clip(double x, double a, double b) { return (x < a) ? a : ((x > b) ? b : x); }
+
+/* QGGMRF::FunctionalSubstitution with QGGMRF_ITER = 1 (QGGMRF_Functions.cpp:153-206);
+ * ComputeParameters inlined (:118-147).  umin is NOT clamped at zero: POSITIVITY_CONSTRAINT
+ * is not visible in that translation unit. */
+static double q_substitution(const orc_ctx* c, double umin, double umax, double V,
+                             const unsigned char* bf, const double* nb, double theta1,
+                             double theta2) {
+  double ref = V, temp1 = 0, temp2 = 0;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      for (int k = 0; k < 3; k++) {
+        int id = IDX3(i, j, k);
+        if ((i != 1 || j != 1 || k != 1) && bf[id] == 1) {
+          double d0 = ref - nb[id];
+          double prm = (d0 != 0) ? q_derivative(c, d0) / d0 : q_second_at_zero(c);
+          double tc = k_filter[id] * prm;
+          temp1 += tc * nb[id];
+          temp2 += tc;
+        }
+      }
+  double u = (temp1 + (theta2 * V) - theta1) / (temp2 + theta2);
+  return clip(ref + c->p.mrf_alpha * (u - ref), umin, umax);
+}
+
+/* ---------------------------------------------------------------------------------------
+ * Geometry and tables
+ * ------------------------------------------------------------------------------------- */
+
+/* GenericFilters/InitialReconstructionInitializer.cpp:98-167 (non-FORWARD_PROJECT_MODE) and
+ * the sinogram extents of GenericFilters/MRCSinogramInitializer.cpp:302-305. */
+static void geometry_init(orc_ctx* c) {
+  const orc_params* p = &c->p;
+  c->R0 = -(c->n_r * c->delta_r) / 2;
+  c->RMax = (c->n_r * c->delta_r) / 2;
+  c->T0 = -(c->n_t * c->delta_t) / 2;
+  c->TMax = (c->n_t * c->delta_t) / 2;
+
+  c->delta_xz = c->delta_r * p->delta_xz_factor;
+  c->delta_xy = c->delta_xz;
+  double mx = fabs(c->angles_deg[0]);
+  for (int i = 1; i < c->n_theta; i++)
+    if (fabs(c->angles_deg[i]) > mx) mx = fabs(c->angles_deg[i]);
+  if (mx > 75.0) mx = 75.0; /* ReconstructionConstants.h:80 k_MaxAngleStretch */
+  mx = mx * M_PI / 180.0;
+  double lz = p->length_z;
+  lz *= p->z_stretch;
+  lz /= (p->interpolate_factor * c->delta_r);
+  lz = floor(lz + 0.5) * p->interpolate_factor * c->delta_r;
+  c->length_z = lz;
+  c->length_x = c->n_r * c->delta_r;
+  if (p->extend_object) {
+    double lx = p->x_shrink_factor * ((c->n_r * c->delta_r) / cos(mx)) + lz * tan(mx);
+    lx /= (p->interpolate_factor * c->delta_r);
+    c->length_x = floor(lx + 0.5) * p->interpolate_factor * c->delta_r;
+  }
+  c->length_y = c->n_t * c->delta_t; /* (yEnd - yStart + 1) * delta_t */
+  c->n_x = (int)(uint16_t)floor(c->length_x / c->delta_xz);
+  c->n_z = (int)(uint16_t)floor(lz / c->delta_xz);
+  c->n_y = (int)(uint16_t)floor(c->length_y / c->delta_xy);
+  c->x0 = -c->length_x / 2;
+  c->z0 = -lz / 2;
+  c->y0 = -c->length_y / 2;
+}
+
+/* HAADF_ReconstructionEngine::calculateVoxelProfile (HAADF_ReconstructionEngine.cpp:957-1029)
+ * for one view with the angle (radians) the profile is built from. */
+static void voxel_profile_row(const orc_ctx* c, double angle, double* out) {
+  double mvli;
+  while (angle > M_PI_2_) angle -= M_PI_2_;
+  while (angle < 0) angle += M_PI_2_;
+  if (angle <= M_PI_4_)
+    mvli = c->delta_xz / cos(angle);
+  else
+    mvli = c->delta_xz / cos(M_PI_2_ - angle);
+  double temp = cos(M_PI_4_);
+  double dist1 = temp * cos((M_PI_4_ - angle));
+  double dist2 = temp * fabs((cos((M_PI_4_ + angle))));
+  double lc = 1 - dist1, ln = 1 - dist2, rn = 1 + dist2, rc = 1 + dist1;
+  int PR = c->p.profile_resolution;
+  for (int j = 0; j < PR; j++) {
+    double t = 2.0 * j / PR;
+    double v;
+    if (t <= lc || t >= rc)
+      v = 0;
+    else if (t > rn)
+      v = mvli * (rc - t) / (rc - rn);
+    else if (t >= ln)
+      v = mvli;
+    else
+      v = mvli * (t - lc) / (ln - lc);
+    out[j] = v;
+  }
+}
+
+static void tables_init(orc_ctx* c) {
+  int nt = c->n_theta, bins = c->p.response_bins, PR = c->p.profile_resolution,
+      BR = c->p.beam_resolution;
+  /* angles: the engine converts to radians in place once before calculateSinCos
+   * (HAADF_ReconstructionEngine.cpp:464-471) and, in the HAADF engine, a second time before
+   * the profile that feeds DetectorResponse (:499, :978). */
+  c->cosv = (double*)calloc(nt, sizeof(double));
+  c->sinv = (double*)calloc(nt, sizeof(double));
+  c->profile = (double*)calloc((size_t)nt * PR, sizeof(double));
+  for (int i = 0; i < nt; i++) {
+    double rad = c->angles_deg[i] * (M_PI / 180.0);
+    c->cosv[i] = cos(rad); /* DetectorParameters.cpp:60-73 */
+    c->sinv[i] = sin(rad);
+    double prof_angle = c->p.compat_double_angle ? rad * (M_PI / 180.0) : rad;
+    voxel_profile_row(c, prof_angle, c->profile + (size_t)i * PR);
+  }
+  /* HAADF_ReconstructionEngine.cpp:467-470 */
+  c->offset_r = ((c->delta_xz / sqrt(3.0)) + c->delta_r / 2) / bins;
+  c->offset_t = ((c->delta_xz / 2) + c->delta_t / 2) / bins;
+  double beam_width = c->delta_r;
+  /* DetectorParameters::initializeBeamProfile (DetectorParameters.cpp:78-100) */
+  c->beam = (double*)calloc(BR, sizeof(double));
+  double sum = 0;
+  for (int i = 0; i < BR; i++) {
+    c->beam[i] = 0.54 - 0.46 * cos((2.0 * M_PI / BR) * i);
+    sum = sum + c->beam[i];
+  }
+  for (int i = 0; i < BR; i++) {
+    c->beam[i] /= sum;
+    c->beam[i] /= c->delta_t;
+  }
+  /* DetectorResponse::execute (GenericFilters/DetectorResponse.cpp:66-127) */
+  c->H = (double*)calloc((size_t)nt * bins, sizeof(double));
+  double r0 = -(beam_width) / 2;
+  double step = beam_width / BR;
+  double tc = (PR) / (2 * c->delta_xz);
+  for (int k = 0; k < nt; k++) {
+    for (int i = 0; i < bins; i++) {
+      double pcr = i * c->offset_r;
+      double rmin = pcr - c->delta_xz;
+      double s = 0;
+      for (int pp = 0; pp < BR; pp++) {
+        double r = r0 + pp * step;
+        if (r < rmin) continue;
+        int pi = (int)floor((r - rmin) * tc);
+        if (pi < 0) pi = 0;
+        if (pi >= PR) pi = PR - 1;
+        s += c->profile[(size_t)k * PR + pi] * c->beam[pp];
+      }
+      c->H[(size_t)k * bins + i] = s;
+    }
+  }
+  /* HAADF_ForwardModel::initializeHt (HAADF/HAADF_ForwardModel.cpp:408-451); identical for
+   * every view, so one row is kept. */
+  c->Ht = (double*)calloc(bins, sizeof(double));
+  for (int i = 0; i < bins; i++) {
+    double pct = i * c->offset_t, v;
+    if (c->delta_xy >= c->delta_t) {
+      if (pct <= ((c->delta_xy / 2) - (c->delta_t / 2)))
+        v = c->delta_t;
+      else
+        v = -1 * pct + (c->delta_xy / 2) + c->delta_t / 2;
+    } else {
+      if (pct <= c->delta_t / 2 - c->delta_xy / 2)
+        v = c->delta_xy;
+      else
+        v = -pct + (c->delta_xy / 2) + c->delta_t / 2;
+    }
+    if (v < 0) v = 0;
+    c->Ht[i] = v;
+  }
+  /* storeVoxelResponse (HAADF_ReconstructionEngine_Extra.cpp:329-404) */
+  c->vlr_cap = (int)(c->delta_xy / c->delta_t) + 2;
+  c->vlr_first = (int*)calloc(c->n_y, sizeof(int));
+  c->vlr_count = (int*)calloc(c->n_y, sizeof(int));
+  c->vlr_val = (double*)calloc((size_t)c->n_y * c->vlr_cap, sizeof(double));
+  for (int i = 0; i < c->n_y; i++) {
+    double y = ((double)i + 0.5) * c->delta_xy + c->y0;
+    double t = y;
+    double tmin = (t - c->delta_xy / 2) > c->T0 ? t - c->delta_xy / 2 : c->T0;
+    double tmax = (t + c->delta_xy / 2) <= c->TMax ? t + c->delta_xy / 2 : c->TMax;
+    int smin = (int16_t)(uint16_t)floor((tmin - c->T0) / c->delta_t);
+    int smax = (int16_t)(uint16_t)floor((tmax - c->T0) / c->delta_t);
+    if (smin < 0) smin = 0;
+    if (smax >= c->n_t) smax = c->n_t - 1;
+    c->vlr_first[i] = -1;
+    for (int it = smin; it <= smax; it++) {
+      double ct = ((double)it + 0.5) * c->delta_t + c->T0;
+      double dt = fabs(ct - t);
+      int idt = (uint16_t)floor(dt / c->offset_t);
+      double pt;
+      if (idt < bins) {
+        double w3 = dt - (double)(idt)*c->offset_t;
+        double w4 = ((double)idt + 1) * c->offset_t - dt;
+        int tt = idt + 1 < bins ? idt + 1 : bins - 1;
+        pt = (w4 / c->offset_t) * c->Ht[idt] + (w3 / c->offset_t) * c->Ht[tt];
+      } else {
+        pt = 0;
+      }
+      if (pt != 0 && c->vlr_count[i] < c->vlr_cap) {
+        if (c->vlr_count[i] == 0) c->vlr_first[i] = it;
+        c->vlr_val[(size_t)i * c->vlr_cap + c->vlr_count[i]] = pt;
+        c->vlr_count[i]++;
+      }
+    }
+    if (c->vlr_first[i] < 0) c->vlr_first[i] = 0;
+  }
+}
+
+/* AMatrixCol::calculateAMatrixColumnPartial (Common/AMatrixCol.cpp:82-239, duplicated at
+ * HAADF_ReconstructionEngine.cpp:1369-1524), AREA_WEIGHTED branch.  The t-direction part of
+ * that loop does not change the value (index_delta_t is fixed at 0), so it is omitted. */
+int orc_amatrix_column(const orc_ctx* c, int row, int col, int32_t* index, double* value,
+                       int cap) {
+  int bins = c->p.response_bins, count = 0;
+  double x = c->x0 + ((double)col + 0.5) * c->delta_xz;
+  double z = c->z0 + ((double)row + 0.5) * c->delta_xz;
+  for (int i = 0; i < c->n_theta; i++) {
+    double r = x * c->cosv[i] - z * c->sinv[i];
+    double rmin = r - c->delta_xz, rmax = r + c->delta_xz;
+    if (rmax < c->R0 || rmin > c->RMax) continue;
+    int imin = (int)floor(((rmin - c->R0) / c->delta_r));
+    int imax = (int)floor((rmax - c->R0) / c->delta_r);
+    if (imax >= c->n_r) imax = c->n_r - 1;
+    if (imin < 0) imin = 0;
+    for (int j = imin; j <= imax; j++) {
+      double rc = (c->R0 + (((double)j) + 0.5) * (c->delta_r));
+      double dr = fabs(r - rc);
+      int idr = (int)floor((dr / c->offset_r));
+      if (idr >= 0 && idr < bins) {
+        double w1 = dr - idr * c->offset_r;
+        double w2 = (idr + 1) * c->offset_r - dr;
+        int ii = idr + 1 < bins ? idr + 1 : bins - 1;
+        double f1 = (w2 / c->offset_r) * c->H[(size_t)i * bins + idr] +
+                    (w1 / c->offset_r) * c->H[(size_t)i * bins + ii];
+        if (f1 > 0 && count < cap) {
+          index[count] = i * c->n_r + j;
+          value[count] = f1;
+          count++;
+        }
+      }
+    }
+  }
+  return count;
+}
+
+int orc_voxel_line_response(const orc_ctx* c, int y, int32_t* t_first, double* value, int cap) {
+  int n = c->vlr_count[y];
+  *t_first = c->vlr_first[y];
+  for (int i = 0; i < n && i < cap; i++) value[i] = c->vlr_val[(size_t)y * c->vlr_cap + i];
+  return n;
+}
+
+static void columns_init(orc_ctx* c) {
+  int nl = c->n_z * c->n_x;
+  int cap = 3 * c->n_theta * ((int)ceil(3 * c->delta_xz / c->delta_r) + 1);
+  int32_t* ti = (int32_t*)malloc(sizeof(int32_t) * cap);
+  double* tv = (double*)malloc(sizeof(double) * cap);
+  c->col_start = (int*)calloc(nl + 1, sizeof(int));
+  c->col_count = (int*)calloc(nl, sizeof(int));
+  size_t total = 0, alloc = (size_t)nl * 2 * c->n_theta + 16;
+  c->col_index = (int*)malloc(sizeof(int) * alloc);
+  c->col_val = (double*)malloc(sizeof(double) * alloc);
+  for (int z = 0; z < c->n_z; z++)
+    for (int x = 0; x < c->n_x; x++) {
+      int l = z * c->n_x + x;
+      int n = orc_amatrix_column(c, z, x, ti, tv, cap);
+      if (total + n > alloc) {
+        alloc = (total + n) * 2;
+        c->col_index = (int*)realloc(c->col_index, sizeof(int) * alloc);
+        c->col_val = (double*)realloc(c->col_val, sizeof(double) * alloc);
+      }
+      c->col_start[l] = (int)total;
+      c->col_count[l] = n;
+      for (int q = 0; q < n; q++) {
+        c->col_index[total + q] = ti[q];
+        c->col_val[total + q] = tv[q];
+      }
+      total += n;
+    }
+  c->col_start[nl] = (int)total;
+  free(ti);
+  free(tv);
+}
+
+#define X3(c, zz, xx, yy) ((c)->x[((size_t)(zz) * (c)->n_x + (xx)) * (c)->n_y + (yy)])
+#define S3(c, arr, th_, r_, t_) ((c)->arr[((size_t)(th_) * (c)->n_r + (r_)) * (c)->n_t + (t_)])
+
+orc_ctx* orc_create(const orc_params* p, const double* counts, const double* tilts_deg,
+                    int n_theta, int n_r, int n_t, double delta_r, double delta_t) {
+  orc_ctx* c = (orc_ctx*)calloc(1, sizeof(orc_ctx));
+  c->p = *p;
+  c->n_theta = n_theta;
+  c->n_r = n_r;
+  c->n_t = n_t;
+  c->delta_r = delta_r;
+  c->delta_t = delta_t;
+  c->angles_deg = (double*)malloc(sizeof(double) * n_theta);
+  memcpy(c->angles_deg, tilts_deg, sizeof(double) * n_theta);
+  size_t ns = (size_t)n_theta * n_r * n_t;
+  c->counts = (double*)malloc(sizeof(double) * ns);
+  memcpy(c->counts, counts, sizeof(double) * ns);
+  geometry_init(c);
+  tables_init(c);
+  columns_init(c);
+  size_t nv = (size_t)c->n_z * c->n_x * c->n_y;
+  c->x = (double*)calloc(nv, sizeof(double));
+  c->e = (double*)calloc(ns, sizeof(double));
+  c->w = (double*)calloc(ns, sizeof(double));
+  c->yest = (double*)calloc(ns, sizeof(double));
+  c->I = (double*)calloc(n_theta, sizeof(double));
+  c->mu = (double*)calloc(n_theta, sizeof(double));
+  c->alpha = (double*)calloc(n_theta, sizeof(double));
+  c->init_gain = (double*)calloc(n_theta, sizeof(double));
+  c->init_offset = (double*)calloc(n_theta, sizeof(double));
+  c->init_var = (double*)calloc(n_theta, sizeof(double));
+  c->mag_map = (double*)calloc((size_t)c->n_z * c->n_x, sizeof(double));
+  c->mask = (unsigned char*)calloc((size_t)c->n_z * c->n_x, 1);
+  /* HAADF_QGGMRFPriorModel.cpp:10-21 (c, P and alpha come from params) */
+  c->sig_p = pow(p->sigma_x, p->mrf_p);
+  c->sig_pq = pow(p->sigma_x, (p->mrf_p - p->mrf_q));
+  c->sig_q = pow(p->sigma_x, p->mrf_q);
+  /* initializeROIMask (HAADF_ReconstructionEngine_Extra.cpp:227-248) */
+  for (int i = 0; i < c->n_z; i++)
+    for (int j = 0; j < c->n_x; j++) {
+      double x = c->x0 + ((double)j + 0.5) * c->delta_xz;
+      double z = c->z0 + ((double)i + 0.5) * c->delta_xz;
+      c->mask[(size_t)i * c->n_x + j] =
+          (x >= -(c->n_r * c->delta_r) / 2 && x <= (c->n_r * c->delta_r) / 2 &&
+           z >= -c->length_z / 2 && z <= c->length_z / 2)
+              ? 1
+              : 0;
+    }
+  return c;
+}
+
+void orc_destroy(orc_ctx* c) {
+  if (!c) return;
+  void* ptrs[] = {c->angles_deg, c->cosv,     c->sinv,       c->profile,     c->beam,
+                  c->H,          c->Ht,       c->vlr_first,  c->vlr_count,   c->vlr_val,
+                  c->col_start,  c->col_count, c->col_index, c->col_val,     c->counts,
+                  c->x,          c->e,        c->w,          c->yest,        c->I,
+                  c->mu,         c->alpha,    c->init_gain,  c->init_offset, c->init_var,
+                  c->mask,       c->mag_map};
+  for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) free(ptrs[i]);
+  free(c);
+}
+
+void orc_dims(const orc_ctx* c, int32_t* dims, double* geo) {
+  dims[0] = c->n_z;
+  dims[1] = c->n_x;
+  dims[2] = c->n_y;
+  if (geo) {
+    geo[0] = c->delta_xz;
+    geo[1] = c->delta_xy;
+    geo[2] = c->x0;
+    geo[3] = c->y0;
+    geo[4] = c->z0;
+    geo[5] = c->length_x;
+    geo[6] = c->length_y;
+    geo[7] = c->length_z;
+  }
+}
+void orc_offsets(const orc_ctx* c, double* o) {
+  o[0] = c->offset_r;
+  o[1] = c->offset_t;
+}
+double* orc_volume(orc_ctx* c) { return c->x; }
+double* orc_error(orc_ctx* c) { return c->e; }
+double* orc_weight(orc_ctx* c) { return c->w; }
+double* orc_yest(orc_ctx* c) { return c->yest; }
+double* orc_gain(orc_ctx* c) { return c->I; }
+double* orc_offset(orc_ctx* c) { return c->mu; }
+double* orc_variance(orc_ctx* c) { return c->alpha; }
+const double* orc_detector_response(const orc_ctx* c) { return c->H; }
+const double* orc_ht(const orc_ctx* c) { return c->Ht; }
+const double* orc_voxel_profile(const orc_ctx* c) { return c->profile; }
+const double* orc_mag_map(const orc_ctx* c) { return c->mag_map; }
+
+/* InitialReconstructionInitializer::initializeData (:74-90), then the zeroing of voxel lines
+ * with an empty A column (HAADF_ReconstructionEngine.cpp:614-625). */
+void orc_init_volume(orc_ctx* c, const double* vol) {
+  size_t nv = (size_t)c->n_z * c->n_x * c->n_y;
+  if (vol)
+    memcpy(c->x, vol, sizeof(double) * nv);
+  else
+    for (size_t i = 0; i < nv; i++) c->x[i] = c->p.default_recon_value;
+  for (int z = 0; z < c->n_z; z++)
+    for (int x = 0; x < c->n_x; x++)
+      if (c->col_count[z * c->n_x + x] == 0)
+        for (int y = 0; y < c->n_y; y++) X3(c, z, x, y) = 0.0;
+}
+
+/* createInitialGainsData / createInitialOffsetsData / createInitialVariancesData
+ * (HAADF/HAADF_ForwardModel.cpp:248-402), ComputeInitialOffsets::execute
+ * (GenericFilters/ComputeInitialOffsets.cpp:58-186) and gainAndOffsetInitialization
+ * (HAADF_ReconstructionEngine_Extra.cpp:280-307). */
+int orc_init_nuisance(orc_ctx* c) {
+  int nt = c->n_theta;
+  for (int i = 0; i < nt; i++) c->init_gain[i] = c->p.target_gain;
+  if (c->p.use_default_offset) {
+    for (int i = 0; i < nt; i++) c->init_offset[i] = c->p.default_offset;
+  } else {
+    double* avg = (double*)calloc(nt, sizeof(double));
+    double* tg = (double*)calloc(nt, sizeof(double));
+    for (int th = 0; th < nt; th++) {
+      double sum = 0;
+      for (int r = 0; r < c->n_r; r++)
+        for (int t = 0; t < c->n_t; t++) sum += S3(c, counts, th, r, t);
+      sum /= (c->n_r * c->n_t);
+      avg[th] = sum;
+      tg[th] = 1.0 / cos(c->angles_deg[th] * M_PI / 180);
+    }
+    double pm[2][2];
+    for (int i = 0; i < 2; i++)
+      for (int j = 0; j < 2; j++) {
+        pm[i][j] = 0;
+        for (int k = 0; k < nt; k++) {
+          double a = (i == 0) ? tg[k] : 1.0, b = (j == 0) ? tg[k] : 1.0;
+          pm[i][j] += a * b;
+        }
+      }
+    double det = pm[0][0] * pm[1][1] - (pm[0][1] * pm[0][1]);
+    double inv[2][2];
+    inv[0][0] = pm[1][1] / det;
+    inv[1][1] = pm[0][0] / det;
+    inv[0][1] = -pm[1][0] / det;
+    inv[1][0] = -pm[0][1] / det;
+    double tv[2] = {0, 0};
+    for (int j = 0; j < 2; j++)
+      for (int k = 0; k < nt; k++) tv[j] += ((j == 0) ? tg[k] : 1.0) * avg[k];
+    double est[2] = {0, 0};
+    for (int i = 0; i < 2; i++)
+      for (int k = 0; k < 2; k++) est[i] += inv[i][k] * tv[k];
+    for (int i = 0; i < nt; i++) c->init_offset[i] = est[1];
+    free(avg);
+    free(tg);
+  }
+  for (int i = 0; i < nt; i++) c->init_var[i] = c->p.default_variance;
+  double sum = 0;
+  for (int k = 0; k < nt; k++) {
+    c->I[k] = c->init_gain[k];
+    c->mu[k] = c->init_offset[k];
+    sum += c->I[k];
+  }
+  sum /= nt;
+  if (sum - c->p.target_gain > 1e-5) {
+    double t = c->p.target_gain / sum;
+    for (int k = 0; k < nt; k++) c->I[k] = c->init_gain[k] * t;
+  }
+  return 0;
+}
+
+/* HAADF_ForwardProject::operator() (HAADF/HAADF_ForwardProject.cpp:80-120), run serially
+ * over z in order so that the FP64 sum is deterministic. */
+void orc_forward_project(orc_ctx* c) {
+  size_t ns = (size_t)c->n_theta * c->n_r * c->n_t;
+  memset(c->yest, 0, sizeof(double) * ns);
+  for (int j = 0; j < c->n_z; j++)
+    for (int k = 0; k < c->n_x; k++) {
+      int l = j * c->n_x + k;
+      if (c->col_count[l] <= 0) continue;
+      for (int i = 0; i < c->n_y; i++)
+        for (int q = 0; q < c->col_count[l]; q++) {
+          int id = c->col_index[c->col_start[l] + q];
+          int th = id / c->n_r, r = id % c->n_r;
+          int t0 = c->vlr_first[i];
+          for (int a = 0; a < c->vlr_count[i]; a++) {
+            double tt = (c->I[th] * (c->col_val[c->col_start[l] + q] *
+                                     c->vlr_val[(size_t)i * c->vlr_cap + a] * X3(c, j, k, i)));
+            S3(c, yest, th, r, t0 + a) += tt;
+          }
+        }
+    }
+}
+
+/* calculateMeasurementWeight (HAADF_ReconstructionEngine_Extra.cpp:693-771) with
+ * IDENTITY_NOISE_MODEL (HAADFConstants.h:56) and no bright-field data. */
+void orc_measurement_weight(orc_ctx* c) {
+  for (int th = 0; th < c->n_theta; th++) {
+    if (c->p.noise_model) c->alpha[th] = c->init_var[th];
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = 0; t < c->n_t; t++) {
+        S3(c, e, th, r, t) = S3(c, counts, th, r, t) - S3(c, yest, th, r, t) - c->mu[th];
+        double w = 1.0;
+        if (c->p.noise_model) w /= c->alpha[th];
+        S3(c, w, th, r, t) = w;
+      }
+  }
+}
+
+/* One voxel of UpdateYSlice::execute (HAADF_ReconstructionEngine_UpdateVoxels.cpp:265-460). */
+static void update_voxel(orc_ctx* c, int jn, int kn, int i, int outer, int inner, double* stats) {
+  double nb[27];
+  unsigned char bf[27];
+  memset(nb, 0, sizeof(nb));
+  memset(bf, 0, sizeof(bf));
+  for (int p = -1; p <= 1; p++)
+    for (int q = -1; q <= 1; q++)
+      for (int r = -1; r <= 1; r++)
+        if (i + p >= 0 && i + p < c->n_y && jn + q >= 0 && jn + q < c->n_z && kn + r >= 0 &&
+            kn + r < c->n_x) {
+          nb[IDX3(p + 1, q + 1, r + 1)] = X3(c, q + jn, r + kn, p + i);
+          bf[IDX3(p + 1, q + 1, r + 1)] = 1;
+        }
+  nb[IDX3(1, 1, 1)] = 0.0;
+  double V = X3(c, jn, kn, i);
+  /* zero skipping :310-338 */
+  int zs = 0;
+  if (c->p.zero_skipping == 1 && V == 0.0 && (inner > 0 || outer > 0)) {
+    zs = 1;
+    for (int a = 0; a < 27; a++)
+      if (nb[a] > 0.0) zs = 0;
+  }
+  if (zs) {
+    stats[2] += 1;
+    return;
+  }
+  int l = jn * c->n_x + kn;
+  int base = c->col_start[l], cnt = c->col_count[l];
+  int t0 = c->vlr_first[i], tc = c->vlr_count[i];
+  const double* hv = c->vlr_val + (size_t)i * c->vlr_cap;
+  double th1 = 0.0, th2 = 0.0;
+  for (int q = 0; q < cnt; q++) {
+    int id = c->col_index[base + q];
+    int th = id / c->n_r, r = id % c->n_r;
+    double k0 = c->I[th] * (c->col_val[base + q]);
+    for (int a = 0; a < tc; a++) {
+      size_t ei = ((size_t)th * c->n_r + r) * c->n_t + (t0 + a);
+      double pe = k0 * hv[a];
+      th2 += (pe * pe * c->w[ei]);
+      th1 += (c->e[ei] * pe * c->w[ei]);
+    }
+  }
+  th1 *= -1;
+  /* find_min_max (:47-63) over all 27 entries (centre and out-of-range entries are 0) */
+  double low = nb[0], high = nb[0];
+  for (int a = 0; a < 27; a++) {
+    if (nb[a] < low) low = nb[a];
+    if (nb[a] > high) high = nb[a];
+  }
+  if (th2 != 0) {
+    low = (low > (V - (th1 / th2)) ? (V - (th1 / th2)) : low);
+    high = (high < (V - (th1 / th2)) ? (V - (th1 / th2)) : high);
+  }
+  double nv = q_substitution(c, low, high, V, bf, nb, th1, th2);
+  if (nv < 0.0) nv = 0.0; /* POSITIVITY_CONSTRAINT :394-400 */
+  X3(c, jn, kn, i) = nv;
+  c->mag_map[l] += fabs(nv - V);
+  if (c->mask[l] == 1) {
+    stats[0] += fabs(nv - V);
+    stats[1] += fabs(V);
+  }
+  stats[3] += 1;
+  for (int q = 0; q < cnt; q++) {
+    int id = c->col_index[base + q];
+    int th = id / c->n_r, r = id % c->n_r;
+    for (int a = 0; a < tc; a++) {
+      size_t ei = ((size_t)th * c->n_r + r) * c->n_t + (t0 + a);
+      double k2 = (c->I[th] * (c->col_val[base + q] * hv[a] * (nv - V)));
+      c->e[ei] -= k2;
+    }
+  }
+}
+
+/* ---------------------------------------------------------------------------------------
+ * MT19937 (Matsumoto & Nishimura 1998), the generator behind boost::mt19937; restated here
+ * from the published algorithm.
+ * ------------------------------------------------------------------------------------- */
+typedef struct {
+  uint32_t mt[624];
+  int idx;
+} mt_state;
+
+static void mt_seed(mt_state* s, uint32_t seed) {
+  s->mt[0] = seed;
+  for (int i = 1; i < 624; i++)
+    s->mt[i] = 1812433253u * (s->mt[i - 1] ^ (s->mt[i - 1] >> 30)) + (uint32_t)i;
+  s->idx = 624;
+}
+
+static uint32_t mt_next(mt_state* s) {
+  if (s->idx >= 624) {
+    for (int i = 0; i < 624; i++) {
+      uint32_t y = (s->mt[i] & 0x80000000u) | (s->mt[(i + 1) % 624] & 0x7fffffffu);
+      s->mt[i] = s->mt[(i + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+    }
+    s->idx = 0;
+  }
+  uint32_t y = s->mt[s->idx++];
+  y ^= (y >> 11);
+  y ^= (y << 7) & 0x9d2c5680u;
+  y ^= (y << 15) & 0xefc60000u;
+  y ^= (y >> 18);
+  return y;
+}
+
+/* Visit order of UpdateYSlice::execute (HAADF_ReconstructionEngine_UpdateVoxels.cpp:151-241):
+ * uniform_int over the full uint32 range returns the raw generator output; each draw picks
+ * Counter[draw % remaining] and moves the last entry into its place. */
+void orc_visit_order(uint32_t seed, int n_z, int n_x, int32_t* out) {
+  int size = n_z * n_x;
+  int32_t* counter = (int32_t*)malloc(sizeof(int32_t) * size);
+  for (int j = 0; j < size; j++) counter[j] = j;
+  mt_state s;
+  mt_seed(&s, seed);
+  int n = 0;
+  for (int j = 0; j < n_z; j++)
+    for (int k = 0; k < n_x; k++) {
+      uint32_t index = mt_next(&s) % (uint32_t)size;
+      int kn = counter[index] % n_x;
+      int jn = counter[index] / n_x;
+      counter[index] = counter[size - 1];
+      size--;
+      out[n++] = jn * n_x + kn;
+    }
+  free(counter);
+}
+
+void orc_icd_sweep_lines(orc_ctx* c, const int32_t* lines, int n_lines, int outer, int inner,
+                         double* stats) {
+  stats[0] = stats[1] = stats[2] = stats[3] = 0;
+  for (size_t i = 0; i < (size_t)c->n_z * c->n_x; i++) c->mag_map[i] = 0;
+  for (int n = 0; n < n_lines; n++) {
+    int l = lines[n];
+    if (c->col_count[l] <= 0) continue;
+    int jn = l / c->n_x, kn = l % c->n_x;
+    for (int i = 0; i < c->n_y; i++) update_voxel(c, jn, kn, i, outer, inner, stats);
+  }
+}
+
+void orc_icd_sweep_reference(orc_ctx* c, uint32_t seed, int outer, int inner, double* stats) {
+  int nl = c->n_z * c->n_x;
+  int32_t* order = (int32_t*)malloc(sizeof(int32_t) * nl);
+  orc_visit_order(seed, c->n_z, c->n_x, order);
+  orc_icd_sweep_lines(c, order, nl, outer, inner, stats);
+  free(order);
+}
+
+void orc_icd_sweep_slices(orc_ctx* c, const int32_t* row_order, int stride, int outer, int inner,
+                          double* stats) {
+  stats[0] = stats[1] = stats[2] = stats[3] = 0;
+  for (size_t i = 0; i < (size_t)c->n_z * c->n_x; i++) c->mag_map[i] = 0;
+  for (int colour = 0; colour < 2; colour++)
+    for (int i = colour; i < c->n_y; i += 2)
+      for (int rr = 0; rr < c->n_z; rr++) {
+        int z = row_order[rr];
+        for (int k = 0; k < stride; k++)
+          for (int x = k; x < c->n_x; x += stride)
+            if (c->col_count[z * c->n_x + x] > 0) update_voxel(c, z, x, i, outer, inner, stats);
+      }
+}
+
+/* jointEstimation, gain+offset branch (HAADF_ReconstructionEngine_Extra.cpp:419-636). */
+int orc_joint_estimation(orc_ctx* c) {
+  int nt = c->n_theta;
+  double* Qk = (double*)calloc((size_t)nt * 3, sizeof(double));
+  double* bk = (double*)calloc((size_t)nt * 2, sizeof(double));
+  double* d1 = (double*)calloc(nt, sizeof(double));
+  double* d2 = (double*)calloc(nt, sizeof(double));
+  for (int th = 0; th < nt; th++)
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = 0; t < c->n_t; t++) {
+        double v = S3(c, counts, th, r, t) - S3(c, e, th, r, t) - c->mu[th];
+        S3(c, yest, th, r, t) = v / c->I[th];
+      }
+  for (int th = 0; th < nt; th++) {
+    double a = 0, b = 0, cc = 0, d = 0, num = 0, den = 0;
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = 0; t < c->n_t; t++) {
+        double y = S3(c, counts, th, r, t), w = S3(c, w, th, r, t), ye = S3(c, yest, th, r, t);
+        num += (y * w);
+        den += (w);
+        a += (ye * w);
+        b += (ye * w * y);
+        cc += (y * y * w);
+        d += (ye * ye * w);
+      }
+    bk[th * 2 + 1] = num;
+    bk[th * 2 + 0] = b;
+    Qk[th * 3 + 2] = den;
+    Qk[th * 3 + 1] = a;
+    Qk[th * 3 + 0] = d;
+    d1[th] = num / den;
+    d2[th] = a / den;
+    (void)cc;
+  }
+  double sum1 = 0, sum2 = 0;
+  for (int th = 0; th < nt; th++) {
+    sum1 += (1.0 / (Qk[th * 3 + 0] - Qk[th * 3 + 1] * d2[th]));
+    sum2 += ((bk[th * 2 + 0] - Qk[th * 3 + 1] * d1[th]) / (Qk[th * 3 + 0] - Qk[th * 3 + 1] * d2[th]));
+  }
+  double lm = (-nt * c->p.target_gain + sum2) / sum1;
+  for (int th = 0; th < nt; th++) {
+    double ni = (-1 * lm - Qk[th * 3 + 1] * d1[th] + bk[th * 2 + 0]) /
+                (Qk[th * 3 + 0] - Qk[th * 3 + 1] * d2[th]);
+    c->I[th] = ni;
+    c->mu[th] = d1[th] - d2[th] * c->I[th];
+  }
+  for (int th = 0; th < nt; th++)
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = 0; t < c->n_t; t++)
+        S3(c, e, th, r, t) =
+            S3(c, counts, th, r, t) - c->mu[th] - (c->I[th] * S3(c, yest, th, r, t));
+  free(Qk);
+  free(bk);
+  free(d1);
+  free(d2);
+  return 0;
+}
+
+/* updateWeights (HAADF_ReconstructionEngine_Extra.cpp:795-881), IDENTITY_NOISE_MODEL. */
+void orc_update_weights(orc_ctx* c) {
+  for (int th = 0; th < c->n_theta; th++) {
+    double sum = 0;
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = 0; t < c->n_t; t++) S3(c, w, th, r, t) = 1.0;
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = 0; t < c->n_t; t++) {
+        double e = S3(c, e, th, r, t);
+        sum += (e * e * S3(c, w, th, r, t));
+      }
+    sum /= (c->n_r * c->n_t);
+    c->alpha[th] = sum;
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = 0; t < c->n_t; t++) S3(c, w, th, r, t) = 1.0 / c->alpha[th];
+  }
+}
+
+/* computeCost, QGGMRF branch (HAADF_ReconstructionEngine.cpp:1147-1364). */
+double orc_cost(const orc_ctx* c, double* parts) {
+  double cost = 0, temp = 0;
+  for (int i = 0; i < c->n_theta; i++)
+    for (int j = 0; j < c->n_r; j++)
+      for (int k = 0; k < c->n_t; k++) {
+        double ev = S3(c, e, i, j, k);
+        cost += (ev * ev * S3(c, w, i, j, k));
+      }
+  cost /= 2;
+  double data = cost;
+#define XV(zz, xx, yy) X3(c, zz, xx, yy)
+#define ACC(fi, z2, x2, y2) temp += k_filter[fi] * q_value(c, XV(i, j, k) - XV(z2, x2, y2))
+  for (int i = 0; i < c->n_z; i++)
+    for (int j = 0; j < c->n_x; j++)
+      for (int k = 0; k < c->n_y; k++) {
+        if (k + 1 < c->n_y) ACC(IDX3(2, 1, 1), i, j, k + 1);
+        if (j + 1 < c->n_x) {
+          if (k - 1 >= 0) ACC(IDX3(0, 1, 2), i, j + 1, k - 1);
+          ACC(IDX3(1, 1, 2), i, j + 1, k);
+          if (k + 1 < c->n_y) ACC(IDX3(2, 1, 2), i, j + 1, k + 1);
+        }
+        if (i + 1 < c->n_z) {
+          if (j - 1 >= 0) ACC(IDX3(1, 2, 0), i + 1, j - 1, k);
+          ACC(IDX3(1, 2, 1), i + 1, j, k);
+          if (j + 1 < c->n_x) ACC(IDX3(1, 2, 2), i + 1, j + 1, k);
+          if (j - 1 >= 0) {
+            if (k - 1 >= 0) ACC(IDX3(0, 2, 0), i + 1, j - 1, k - 1);
+            if (k + 1 < c->n_y) ACC(IDX3(2, 2, 0), i + 1, j - 1, k + 1);
+          }
+          if (k - 1 >= 0) ACC(IDX3(0, 2, 1), i + 1, j, k - 1);
+          if (j + 1 < c->n_x) {
+            if (k - 1 >= 0) ACC(IDX3(0, 2, 2), i + 1, j + 1, k - 1);
+            if (k + 1 < c->n_y) ACC(IDX3(2, 2, 2), i + 1, j + 1, k + 1);
+          }
+          if (k + 1 < c->n_y) ACC(IDX3(2, 2, 1), i + 1, j, k + 1);
+        }
+      }
+#undef ACC
+#undef XV
+  cost += temp;
+  double noise = 0;
+  if (c->p.noise_model) {
+    double tn = 0;
+    for (int i = 0; i < c->n_theta; i++)
+      for (int j = 0; j < c->n_r; j++)
+        for (int k = 0; k < c->n_t; k++) {
+          double w = S3(c, w, i, j, k);
+          if (w != 0) tn += log(2 * M_PI * (1.0 / w));
+        }
+    tn /= 2;
+    noise = tn;
+    cost += tn;
+  }
+  if (parts) {
+    parts[0] = data;
+    parts[1] = temp;
+    parts[2] = noise;
+  }
+  return cost;
+}
+
+/* HAADF_ReconstructionEngine::execute outer/inner loops (HAADF_ReconstructionEngine.cpp:706-815)
+ * with RegularRandomOrderUpdate and the ROI stop rule of updateVoxels (_UpdateVoxels.cpp:765-787). */
+int orc_run(orc_ctx* c, uint32_t seed, double* cost_log, int n_cost) {
+  int sweeps = 0;
+  double stop = c->p.stop_threshold;
+  int num_iter = c->p.inner_iterations;
+  for (int outer = 0; outer < c->p.outer_iterations; outer++) {
+    if (outer != 0) num_iter = 1;
+    int status = 1;
+    for (int inner = 0; inner < num_iter; inner++) {
+      double st[4];
+      orc_icd_sweep_reference(c, seed, outer, inner, st);
+      if (cost_log && sweeps < n_cost) cost_log[sweeps] = orc_cost(c, NULL);
+      sweeps++;
+      status = 1;
+      if (st[1] > 0 && (st[0] / st[1]) < stop) {
+        stop *= c->p.threshold_reduction_factor;
+        status = 0;
+        break;
+      }
+    }
+    if (c->p.joint_estimation) orc_joint_estimation(c);
+    if (c->p.noise_model) {
+      orc_update_weights(c);
+      if (status == 0 && outer >= 1) break;
+    } else if (status == 0 && outer >= 1) {
+      break;
+    }
+  }
+  return sweeps;
+}

@@ -1,0 +1,254 @@
+"""ctypes binding of the FP64 CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and by the
+cpu_baseline / reference leg of bench.py, always as the checker or the timed CPU baseline,
+never as a product path.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+SRC = os.path.join(HERE, "mbir_oracle.c")
+
+
+class OrcParams(C.Structure):
+    _fields_ = [
+        ("delta_xz_factor", C.c_double), ("interpolate_factor", C.c_double),
+        ("length_z", C.c_double), ("extend_object", C.c_int32), ("x_shrink_factor", C.c_double),
+        ("z_stretch", C.c_int32), ("response_bins", C.c_int32),
+        ("profile_resolution", C.c_int32), ("beam_resolution", C.c_int32),
+        ("compat_double_angle", C.c_int32), ("sigma_x", C.c_double), ("mrf_p", C.c_double),
+        ("mrf_q", C.c_double), ("mrf_c", C.c_double), ("mrf_alpha", C.c_double),
+        ("target_gain", C.c_double), ("default_offset", C.c_double),
+        ("default_variance", C.c_double), ("default_recon_value", C.c_double),
+        ("use_default_offset", C.c_int32), ("joint_estimation", C.c_int32),
+        ("noise_model", C.c_int32), ("zero_skipping", C.c_int32), ("stop_threshold", C.c_double),
+        ("outer_iterations", C.c_int32), ("inner_iterations", C.c_int32),
+        ("threshold_reduction_factor", C.c_double),
+    ]
+
+
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int32)
+_lib = None
+
+
+def build(force=False):
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        subprocess.check_call(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-o", LIB, SRC,
+                               "-lm"])
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        sig = {
+            "orc_create": (C.c_void_p, [C.POINTER(OrcParams), _D, _D, C.c_int, C.c_int, C.c_int,
+                                        C.c_double, C.c_double]),
+            "orc_destroy": (None, [C.c_void_p]),
+            "orc_dims": (None, [C.c_void_p, _I, _D]),
+            "orc_offsets": (None, [C.c_void_p, _D]),
+            "orc_volume": (_D, [C.c_void_p]), "orc_error": (_D, [C.c_void_p]),
+            "orc_weight": (_D, [C.c_void_p]), "orc_yest": (_D, [C.c_void_p]),
+            "orc_gain": (_D, [C.c_void_p]), "orc_offset": (_D, [C.c_void_p]),
+            "orc_variance": (_D, [C.c_void_p]),
+            "orc_detector_response": (_D, [C.c_void_p]), "orc_ht": (_D, [C.c_void_p]),
+            "orc_voxel_profile": (_D, [C.c_void_p]), "orc_mag_map": (_D, [C.c_void_p]),
+            "orc_amatrix_column": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _I, _D, C.c_int]),
+            "orc_voxel_line_response": (C.c_int, [C.c_void_p, C.c_int, _I, _D, C.c_int]),
+            "orc_init_volume": (None, [C.c_void_p, _D]),
+            "orc_init_nuisance": (C.c_int, [C.c_void_p]),
+            "orc_forward_project": (None, [C.c_void_p]),
+            "orc_measurement_weight": (None, [C.c_void_p]),
+            "orc_icd_sweep_reference": (None, [C.c_void_p, C.c_uint32, C.c_int, C.c_int, _D]),
+            "orc_icd_sweep_slices": (None, [C.c_void_p, _I, C.c_int, C.c_int, C.c_int, _D]),
+            "orc_icd_sweep_lines": (None, [C.c_void_p, _I, C.c_int, C.c_int, C.c_int, _D]),
+            "orc_joint_estimation": (C.c_int, [C.c_void_p]),
+            "orc_update_weights": (None, [C.c_void_p]),
+            "orc_cost": (C.c_double, [C.c_void_p, _D]),
+            "orc_visit_order": (None, [C.c_uint32, C.c_int, C.c_int, _I]),
+            "orc_run": (C.c_int, [C.c_void_p, C.c_uint32, _D, C.c_int]),
+        }
+        for n, (r, a) in sig.items():
+            f = getattr(L, n)
+            f.restype = r
+            f.argtypes = a
+        _lib = L
+    return _lib
+
+
+def params_from_mbir(p):
+    """Map the engine's mbir_params (CLI-level) onto one oracle level."""
+    o = OrcParams()
+    levels = max(p.num_resolutions, 1)
+    lvl = levels - 1 if (p.level < 0 or p.level >= levels) else p.level
+    fres = max(p.final_resolution, 1)
+    o.delta_xz_factor = 2.0 ** (levels - 1 - lvl) * fres
+    o.interpolate_factor = 2.0 ** (levels - 1) * fres
+    o.length_z = p.sample_thickness
+    o.extend_object = p.extend_object
+    o.x_shrink_factor = p.x_shrink_factor
+    o.z_stretch = p.z_stretch
+    o.response_bins = p.detector_response_bins
+    o.profile_resolution = p.profile_resolution
+    o.beam_resolution = p.beam_resolution
+    o.compat_double_angle = p.compat_double_angle
+    o.sigma_x = p.sigma_x
+    o.mrf_p = p.qggmrf_p
+    o.mrf_q = p.qggmrf_q if p.qggmrf_q != 0 else p.diffuseness + 1.0
+    o.mrf_c = p.qggmrf_c
+    o.mrf_alpha = p.qggmrf_alpha
+    o.target_gain = p.target_gain
+    o.default_offset = p.default_offset
+    o.default_variance = p.default_variance
+    o.default_recon_value = p.default_recon_value
+    o.use_default_offset = p.use_default_offset
+    o.joint_estimation = p.joint_estimation
+    o.noise_model = p.noise_model
+    o.zero_skipping = p.zero_skipping
+    o.stop_threshold = p.stop_threshold
+    o.outer_iterations = p.outer_iterations
+    o.inner_iterations = p.inner_iterations
+    o.threshold_reduction_factor = p.threshold_reduction_factor
+    return o
+
+
+class Oracle:
+    def __init__(self, oparams, counts, tilts_deg, delta_r=1.0, delta_t=1.0):
+        counts = np.ascontiguousarray(counts, np.float64)
+        tilts = np.ascontiguousarray(tilts_deg, np.float64)
+        self.shape = counts.shape
+        self.params = oparams
+        self._h = lib().orc_create(C.byref(oparams), counts.ctypes.data_as(_D),
+                                   tilts.ctypes.data_as(_D), *counts.shape, delta_r, delta_t)
+        d = np.zeros(3, np.int32)
+        geo = np.zeros(8)
+        lib().orc_dims(self._h, d.ctypes.data_as(_I), geo.ctypes.data_as(_D))
+        self.nz, self.nx, self.ny = (int(v) for v in d)
+        self.geo = geo
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_destroy(self._h)
+            self._h = None
+
+    def _view(self, fn, shape):
+        p = fn(self._h)
+        return np.ctypeslib.as_array(p, shape=shape)
+
+    def volume(self):
+        return self._view(lib().orc_volume, (self.nz, self.nx, self.ny))
+
+    def error(self):
+        return self._view(lib().orc_error, self.shape)
+
+    def weight(self):
+        return self._view(lib().orc_weight, self.shape)
+
+    def yest(self):
+        return self._view(lib().orc_yest, self.shape)
+
+    def gain(self):
+        return self._view(lib().orc_gain, (self.shape[0],))
+
+    def offset(self):
+        return self._view(lib().orc_offset, (self.shape[0],))
+
+    def variance(self):
+        return self._view(lib().orc_variance, (self.shape[0],))
+
+    def detector_response(self):
+        return self._view(lib().orc_detector_response, (self.shape[0], self.params.response_bins))
+
+    def ht(self):
+        return self._view(lib().orc_ht, (self.params.response_bins,))
+
+    def offsets(self):
+        o = np.zeros(2)
+        lib().orc_offsets(self._h, o.ctypes.data_as(_D))
+        return o
+
+    def amatrix_column(self, z, x):
+        cap = 64 * self.shape[0]
+        idx = np.zeros(cap, np.int32)
+        val = np.zeros(cap)
+        n = lib().orc_amatrix_column(self._h, z, x, idx.ctypes.data_as(_I),
+                                     val.ctypes.data_as(_D), cap)
+        return idx[:n].copy(), val[:n].copy()
+
+    def voxel_line_response(self, y):
+        val = np.zeros(16)
+        t0 = C.c_int32()
+        n = lib().orc_voxel_line_response(self._h, y, C.byref(t0), val.ctypes.data_as(_D), 16)
+        return t0.value, val[:n].copy()
+
+    def init_volume(self, vol=None):
+        if vol is None:
+            lib().orc_init_volume(self._h, None)
+        else:
+            v = np.ascontiguousarray(vol, np.float64)
+            lib().orc_init_volume(self._h, v.ctypes.data_as(_D))
+
+    def init_nuisance(self):
+        return lib().orc_init_nuisance(self._h)
+
+    def prepare(self, vol=None):
+        """volume init, nuisance init, forward projection, weights (execute() up to :691)."""
+        self.init_volume(vol)
+        self.init_nuisance()
+        lib().orc_forward_project(self._h)
+        lib().orc_measurement_weight(self._h)
+
+    def forward_project(self):
+        lib().orc_forward_project(self._h)
+
+    def measurement_weight(self):
+        lib().orc_measurement_weight(self._h)
+
+    def sweep_reference(self, seed, outer=0, inner=0):
+        st = np.zeros(4)
+        lib().orc_icd_sweep_reference(self._h, seed, outer, inner, st.ctypes.data_as(_D))
+        return st
+
+    def sweep_slices(self, row_order, stride, outer=0, inner=0):
+        rows = np.ascontiguousarray(row_order, np.int32)
+        st = np.zeros(4)
+        lib().orc_icd_sweep_slices(self._h, rows.ctypes.data_as(_I), stride, outer, inner,
+                                   st.ctypes.data_as(_D))
+        return st
+
+    def sweep_lines(self, lines, outer=0, inner=0):
+        ln = np.ascontiguousarray(lines, np.int32)
+        st = np.zeros(4)
+        lib().orc_icd_sweep_lines(self._h, ln.ctypes.data_as(_I), len(ln), outer, inner,
+                                  st.ctypes.data_as(_D))
+        return st
+
+    def joint_estimation(self):
+        return lib().orc_joint_estimation(self._h)
+
+    def update_weights(self):
+        lib().orc_update_weights(self._h)
+
+    def cost(self):
+        parts = np.zeros(3)
+        c = lib().orc_cost(self._h, parts.ctypes.data_as(_D))
+        return c, parts
+
+    def run(self, seed, n_cost=0):
+        log = np.zeros(max(n_cost, 1))
+        n = lib().orc_run(self._h, seed, log.ctypes.data_as(_D) if n_cost else None, n_cost)
+        return n, log[:min(n, n_cost)]
+
+
+def visit_order(seed, nz, nx):
+    out = np.zeros(nz * nx, np.int32)
+    lib().orc_visit_order(seed, nz, nx, out.ctypes.data_as(_I))
+    return out
