@@ -48,6 +48,9 @@ extern "C" {
 #define MBIR_ORDER_PARALLEL 0  /* red/black y-slices x conflict-free voxel sets (GPU order) */
 #define MBIR_ORDER_REFERENCE 1 /* the reference's single-task random line order, y sequential */
 
+#define MBIR_PRECISION_FP32 0  /* volume, error sinogram and footprints in FP32 (reductions FP64) */
+#define MBIR_PRECISION_FP64 1  /* everything in FP64, the reference's Real_t */
+
 /* Parameter set: the reference CLI/pipeline inputs (HAADFReconstructionArgsParser.cpp:143-211,
  * BFReconstructionArgsParser.cpp:145-226), the AdvancedParameters
  * (ReconstructionStructures.h:164-187, defaults HAADF_ReconstructionEngine.cpp:244-259), the
@@ -100,6 +103,7 @@ typedef struct mbir_params {
   double bragg_threshold, bragg_delta, bf_offset, default_dosage;
   /* engine switches */
   int32_t order_mode;         /* MBIR_ORDER_PARALLEL / MBIR_ORDER_REFERENCE */
+  int32_t precision;          /* MBIR_PRECISION_FP32 / MBIR_PRECISION_FP64 */
   uint32_t seed;              /* visit-order seed (reference mode: mt19937 seed per sweep) */
   int32_t compat_double_angle;/* 1: HAADF voxel profile from deg*(pi/180)^2, as the reference */
   int32_t cost_every_sweep;   /* 1: evaluate the FP64 MAP cost after every sweep */

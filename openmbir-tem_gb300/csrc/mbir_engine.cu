@@ -22,15 +22,19 @@ namespace {
 constexpr double kPi = 3.14159265358979323846;
 
 // prior weights [dy+1][dz+1][dx+1] (HAADF_ReconstructionEngine.cpp:266-294)
-constexpr float kFilter[27] = {0.0302f, 0.0370f, 0.0302f, 0.0370f, 0.0523f, 0.0370f, 0.0302f,
-                               0.0370f, 0.0302f, 0.0370f, 0.0523f, 0.0370f, 0.0523f, 0.0000f,
-                               0.0523f, 0.0370f, 0.0523f, 0.0370f, 0.0302f, 0.0370f, 0.0302f,
-                               0.0370f, 0.0523f, 0.0370f, 0.0302f, 0.0370f, 0.0302f};
+constexpr double kFilter[27] = {0.0302, 0.0370, 0.0302, 0.0370, 0.0523, 0.0370, 0.0302,
+                                0.0370, 0.0302, 0.0370, 0.0523, 0.0370, 0.0523, 0.0000,
+                                0.0523, 0.0370, 0.0523, 0.0370, 0.0302, 0.0370, 0.0302,
+                                0.0370, 0.0523, 0.0370, 0.0302, 0.0370, 0.0302};
 
 template <typename T>
 int dmalloc(T** p, size_t n) {
   if (n == 0) n = 1;
   return cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T)) == cudaSuccess ? 0 : MBIR_ENOMEM;
+}
+int dmalloc_bytes(void** p, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  return cudaMalloc(p, bytes) == cudaSuccess ? 0 : MBIR_ENOMEM;
 }
 template <typename T>
 void dfree(T*& p) {
@@ -80,6 +84,8 @@ void reference_visit_order(uint32_t seed, int n_z, int n_x, std::vector<int32_t>
 // ---- Engine -------------------------------------------------------------------------------
 Engine::Engine(const mbir_params& p) : p_(p) {
   if (p_.qggmrf_q == 0.0) p_.qggmrf_q = p_.diffuseness + 1.0;
+  fp64_ = p_.precision == MBIR_PRECISION_FP64 ? 1 : 0;
+  rb_ = fp64_ ? sizeof(double) : sizeof(float);
   bins_ = p_.detector_response_bins > 0 ? p_.detector_response_bins : 64;
 }
 
@@ -93,6 +99,7 @@ void Engine::release() {
   dfree(d_stage_);
   dfree(d_H_);
   dfree(d_bx_);
+  dfree(d_bxd_);
   dfree(d_u0_);
   dfree(d_bz_);
   dfree(d_gw_);
@@ -470,26 +477,27 @@ int Engine::alloc_device() {
   n_rs_ = (n_rp_ % 32 == 0) ? n_rp_ + 4 : n_rp_;
   int max_smem = 0;
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, p_.device);
-  smem_bytes_ = sweep_smem_bytes(g.n_theta, n_rs_, t_rows_, bins_);
+  smem_bytes_ = sweep_smem_bytes(g.n_theta, n_rs_, t_rows_, bins_, fp64_);
   stage_ = smem_bytes_ <= static_cast<size_t>(max_smem);
-  if (!stage_) smem_bytes_ = sweep_smem_bytes(g.n_theta, 0, t_rows_, bins_);
+  if (!stage_) smem_bytes_ = sweep_smem_bytes(g.n_theta, 0, t_rows_, bins_, fp64_);
   const size_t ns = static_cast<size_t>(g.n_t) * g.n_theta * n_rp_;
   const size_t nh = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;
   const size_t nv = static_cast<size_t>(g.n_z) * g.n_x * g.n_y;
   int rc = 0;
-  rc |= dmalloc(&d_y_, ns);
-  rc |= dmalloc(&d_e_, ns);
-  rc |= dmalloc(&d_yest_, ns);
-  rc |= dmalloc(&d_x_, nv);
+  rc |= dmalloc_bytes(&d_y_, ns * rb_);
+  rc |= dmalloc_bytes(&d_e_, ns * rb_);
+  rc |= dmalloc_bytes(&d_yest_, ns * rb_);
+  rc |= dmalloc_bytes(&d_x_, nv * rb_);
   rc |= dmalloc(&d_stage_, std::max(nh, nv));
-  rc |= dmalloc(&d_H_, static_cast<size_t>(g.n_theta) * (bins_ + 1));
+  rc |= dmalloc_bytes(&d_H_, static_cast<size_t>(g.n_theta) * (bins_ + 1) * rb_);
   rc |= dmalloc(&d_bx_, g.n_theta);
+  rc |= dmalloc(&d_bxd_, g.n_theta);
   rc |= dmalloc(&d_u0_, g.n_theta);
   rc |= dmalloc(&d_bz_, g.n_theta);
-  rc |= dmalloc(&d_gw_, g.n_theta);
+  rc |= dmalloc_bytes(&d_gw_, static_cast<size_t>(g.n_theta) * 2 * rb_);
   rc |= dmalloc(&d_tfirst_, g.n_y);
   rc |= dmalloc(&d_tcount_, g.n_y);
-  rc |= dmalloc(&d_hval_, static_cast<size_t>(g.n_y) * kMaxTRows);
+  rc |= dmalloc_bytes(&d_hval_, static_cast<size_t>(g.n_y) * kMaxTRows * rb_);
   rc |= dmalloc(&d_rows_, g.n_z);
   rc |= dmalloc(&d_lines_, static_cast<size_t>(g.n_z) * g.n_x);
   rc |= dmalloc(&d_stats_, static_cast<size_t>((g.n_y + 1) / 2 + 1) * kStatSlots * 2);
@@ -520,10 +528,18 @@ int Engine::alloc_device() {
 
 int Engine::upload_views() {
   const int nt = g_.n_theta;
-  std::vector<float2> gw(nt);
-  for (int v = 0; v < nt; v++) gw[v] = make_float2(static_cast<float>(I_[v]), static_cast<float>(w_[v]));
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
-  cudaMemcpyAsync(d_gw_, gw.data(), sizeof(float2) * nt, cudaMemcpyHostToDevice, s);
+  std::vector<float2> gw(nt);
+  std::vector<double2> gwd(nt);
+  for (int v = 0; v < nt; v++) {
+    gw[v] = make_float2(static_cast<float>(I_[v]), static_cast<float>(w_[v]));
+    gwd[v] = make_double2(I_[v], w_[v]);
+  }
+  if (fp64_)
+    cudaMemcpyAsync(d_gw_, gwd.data(), sizeof(double2) * nt, cudaMemcpyHostToDevice, s);
+  else
+    cudaMemcpyAsync(d_gw_, gw.data(), sizeof(float2) * nt, cudaMemcpyHostToDevice, s);
+  cudaStreamSynchronize(s);  // host vectors go out of scope
   cudaMemcpyAsync(d_mu_, mu_.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(d_gain_, I_.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(d_wv_, w_.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, s);
@@ -585,18 +601,32 @@ int Engine::prepare() {
   }
   std::vector<float> hv(tab_.hval.size());
   for (size_t i = 0; i < hv.size(); i++) hv[i] = static_cast<float>(tab_.hval[i]);
-  cudaMemcpyAsync(d_H_, Hf.data(), sizeof(float) * Hf.size(), cudaMemcpyHostToDevice, s);
+  std::vector<double> Hd(Hf.size()), bxd(g.n_theta);
+  for (int v = 0; v < g.n_theta; v++) {
+    for (int i = 0; i <= bins_; i++)
+      Hd[static_cast<size_t>(v) * (bins_ + 1) + i] =
+          tab_.H[static_cast<size_t>(v) * bins_ + std::min(i, bins_ - 1)];
+    bxd[v] = g.delta_xz * tab_.cosv[v] / g.delta_r;
+  }
+  if (fp64_) {
+    cudaMemcpyAsync(d_H_, Hd.data(), sizeof(double) * Hd.size(), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_hval_, tab_.hval.data(), sizeof(double) * tab_.hval.size(),
+                    cudaMemcpyHostToDevice, s);
+  } else {
+    cudaMemcpyAsync(d_H_, Hf.data(), sizeof(float) * Hf.size(), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_hval_, hv.data(), sizeof(float) * hv.size(), cudaMemcpyHostToDevice, s);
+  }
+  cudaMemcpyAsync(d_bxd_, bxd.data(), sizeof(double) * bxd.size(), cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(d_bx_, bx.data(), sizeof(float2) * bx.size(), cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(d_u0_, u0.data(), sizeof(double) * u0.size(), cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(d_bz_, bz.data(), sizeof(double) * bz.size(), cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(d_tfirst_, tab_.t_first.data(), sizeof(int) * g.n_y, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(d_tcount_, tab_.t_count.data(), sizeof(int) * g.n_y, cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(d_hval_, hv.data(), sizeof(float) * hv.size(), cudaMemcpyHostToDevice, s);
 
   // measured sinogram -> [t][theta][r_pad]
   const size_t nh = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;
   cudaMemcpyAsync(d_stage_, counts_.data(), sizeof(float) * nh, cudaMemcpyHostToDevice, s);
-  if ((rc = launch_sino_to_dev(d_stage_, d_y_, g.n_theta, g.n_r, n_rp_, g.n_t, s)))
+  if ((rc = launch_sino_to_dev(d_stage_, d_y_, g.n_theta, g.n_r, n_rp_, g.n_t, fp64_, s)))
     return cuda_check(rc, "sinogram upload");
 
   // initial volume (InitialReconstructionInitializer::initializeData, :74-90)
@@ -613,7 +643,7 @@ int Engine::prepare() {
       if (!tab_.line_nonempty[static_cast<size_t>(z) * g.n_x + x])
         for (int y = 0; y < g.n_y; y++) vol[(static_cast<size_t>(z) * g.n_x + x) * g.n_y + y] = 0.f;
   cudaMemcpyAsync(d_stage_, vol.data(), sizeof(float) * nv, cudaMemcpyHostToDevice, s);
-  if ((rc = launch_vol_to_dev(d_stage_, d_x_, g.n_z, g.n_x, g.n_y, s)))
+  if ((rc = launch_vol_to_dev(d_stage_, d_x_, g.n_z, g.n_x, g.n_y, fp64_, s)))
     return cuda_check(rc, "volume upload");
   if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "prepare sync");
 
@@ -648,12 +678,12 @@ int Engine::prepare() {
     }
   }
   for (int i = 0; i < 27; i++) flt_.f[i] = kFilter[i];
-  flt_.mrf_p = static_cast<float>(p_.qggmrf_p);
-  flt_.mrf_q = static_cast<float>(p_.qggmrf_q);
-  flt_.mrf_c = static_cast<float>(p_.qggmrf_c);
-  flt_.mrf_alpha = static_cast<float>(p_.qggmrf_alpha);
-  flt_.sig_p = static_cast<float>(std::pow(p_.sigma_x, p_.qggmrf_p));
-  flt_.sig_pq = static_cast<float>(std::pow(p_.sigma_x, p_.qggmrf_p - p_.qggmrf_q));
+  flt_.mrf_p = p_.qggmrf_p;
+  flt_.mrf_q = p_.qggmrf_q;
+  flt_.mrf_c = p_.qggmrf_c;
+  flt_.mrf_alpha = p_.qggmrf_alpha;
+  flt_.sig_p = std::pow(p_.sigma_x, p_.qggmrf_p);
+  flt_.sig_pq = std::pow(p_.sigma_x, p_.qggmrf_p - p_.qggmrf_q);
 
   if ((rc = upload_views())) return rc;
   state_ = 2;
@@ -668,19 +698,20 @@ int Engine::forward_project() {
   const Geometry& g = g_;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
   const size_t ns = static_cast<size_t>(g.n_t) * g.n_theta * n_rp_;
-  if (!stage_) cudaMemsetAsync(d_yest_, 0, sizeof(float) * ns, s);
+  if (!stage_) cudaMemsetAsync(d_yest_, 0, rb_ * ns, s);
   std::vector<int32_t> rows(g.n_z);
   for (int i = 0; i < g.n_z; i++) rows[i] = i;
   cudaMemcpyAsync(d_rows_, rows.data(), sizeof(int) * g.n_z, cudaMemcpyHostToDevice, s);
   SweepArgs a{};
   a.g = dg_;
-  a.tab = DevTables{d_H_, d_bx_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_};
+  a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_};
   a.flt = flt_;
   a.x = d_x_;
   a.e = d_yest_;
   a.row_order = d_rows_;
   a.stride = stride_;
   a.mode = kModeProject;
+  a.fp64 = fp64_;
   a.smem_rows = stage_ ? 1 : 0;
   a.n_rs = stage_ ? n_rs_ : 0;
   a.stats = nullptr;
@@ -693,7 +724,7 @@ int Engine::forward_project() {
     if (rc) return cuda_check(rc, "forward projection launch");
   }
   int rc = launch_error_from_projection(d_y_, d_yest_, d_e_, d_mu_, g.n_theta, n_rp_, g.n_r,
-                                        g.n_t, s);
+                                        g.n_t, fp64_, s);
   if (rc) return cuda_check(rc, "error sinogram");
   if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "forward projection");
   return check_device_error();
@@ -724,7 +755,7 @@ int Engine::sweep(int outer, int inner, double* stats4) {
     cudaMemcpyAsync(d_lines_, lines.data(), sizeof(int32_t) * lines.size(), cudaMemcpyHostToDevice, s);
     RefOrderArgs a{};
     a.g = dg_;
-    a.tab = DevTables{d_H_, d_bx_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_};
+    a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_};
     a.flt = flt_;
     a.x = d_x_;
     a.e = d_e_;
@@ -732,6 +763,7 @@ int Engine::sweep(int outer, int inner, double* stats4) {
     a.n_lines = static_cast<int>(lines.size());
     a.iter_nonzero = iter_nonzero;
     a.zero_skipping = p_.zero_skipping;
+    a.fp64 = fp64_;
     a.stats = d_stat4_;
     if ((rc = launch_ref_order(a, nb_, s))) return cuda_check(rc, "reference-order sweep");
   } else {
@@ -740,13 +772,14 @@ int Engine::sweep(int outer, int inner, double* stats4) {
     cudaMemcpyAsync(d_rows_, rows.data(), sizeof(int) * g.n_z, cudaMemcpyHostToDevice, s);
     SweepArgs a{};
     a.g = dg_;
-    a.tab = DevTables{d_H_, d_bx_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_};
+    a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_};
     a.flt = flt_;
     a.x = d_x_;
     a.e = d_e_;
     a.row_order = d_rows_;
     a.stride = stride_;
     a.mode = kModeICD;
+    a.fp64 = fp64_;
     a.iter_nonzero = iter_nonzero;
     a.zero_skipping = p_.zero_skipping;
     a.smem_rows = stage_ ? 1 : 0;
@@ -789,7 +822,7 @@ int Engine::joint_estimation() {
   const int nt = g.n_theta;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
   int rc = launch_view_sums(0, d_y_, d_e_, d_mu_, d_gain_, d_wv_, d_partial_, d_vsum_, nt, n_rp_,
-                            g.n_r, g.n_t, n_chunk_, s);
+                            g.n_r, g.n_t, n_chunk_, fp64_, s);
   if (rc) return cuda_check(rc, "joint estimation sums");
   std::vector<double> vs(static_cast<size_t>(nt) * 6);
   cudaMemcpyAsync(vs.data(), d_vsum_, sizeof(double) * vs.size(), cudaMemcpyDeviceToHost, s);
@@ -817,7 +850,8 @@ int Engine::joint_estimation() {
   }
   cudaMemcpyAsync(d_mu2_, Mn.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(d_gain2_, In.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, s);
-  rc = launch_rebuild_error(d_y_, d_e_, d_mu_, d_gain_, d_mu2_, d_gain2_, nt, n_rp_, g.n_r, g.n_t, s);
+  rc = launch_rebuild_error(d_y_, d_e_, d_mu_, d_gain_, d_mu2_, d_gain2_, nt, n_rp_, g.n_r, g.n_t,
+                            fp64_, s);
   if (rc) return cuda_check(rc, "rebuild error sinogram");
   I_ = In;
   mu_ = Mn;
@@ -831,7 +865,7 @@ int Engine::update_weights() {
   const int nt = g.n_theta;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
   int rc = launch_view_sums(1, d_y_, d_e_, d_mu_, d_gain_, d_wv_, d_partial_, d_vsum_, nt, n_rp_,
-                            g.n_r, g.n_t, n_chunk_, s);
+                            g.n_r, g.n_t, n_chunk_, fp64_, s);
   if (rc) return cuda_check(rc, "variance sums");
   std::vector<double> vs(nt);
   cudaMemcpyAsync(vs.data(), d_vsum_, sizeof(double) * nt, cudaMemcpyDeviceToHost, s);
@@ -850,10 +884,11 @@ int Engine::compute_cost(double* parts3, double* total) {
   const int nt = g.n_theta;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
   int rc = launch_view_sums(1, d_y_, d_e_, d_mu_, d_gain_, d_wv_, d_partial_, d_vsum_, nt, n_rp_,
-                            g.n_r, g.n_t, n_chunk_, s);
+                            g.n_r, g.n_t, n_chunk_, fp64_, s);
   if (rc) return cuda_check(rc, "cost data term");
   double* prior_partial = d_partial_ + static_cast<size_t>(nt) * n_chunk_ * 6;
-  rc = launch_prior_cost(d_x_, flt_, g.n_z, g.n_x, g.n_y, prior_partial, prior_blocks_, s);
+  rc = launch_prior_cost(d_x_, flt_, g.n_z, g.n_x, g.n_y, prior_partial, prior_blocks_, fp64_,
+                         s);
   if (rc) return cuda_check(rc, "cost prior term");
   std::vector<double> vs(nt), pp(prior_blocks_);
   cudaMemcpyAsync(vs.data(), d_vsum_, sizeof(double) * nt, cudaMemcpyDeviceToHost, s);
@@ -937,18 +972,18 @@ int Engine::get_volume(float* out, int64_t n) {
   const size_t nv = static_cast<size_t>(g.n_z) * g.n_x * g.n_y;
   if (!out || n < static_cast<int64_t>(nv)) return fail(MBIR_EINVAL, "get_volume: buffer too small");
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
-  int rc = launch_vol_to_host(d_x_, d_stage_, g.n_z, g.n_x, g.n_y, s);
+  int rc = launch_vol_to_host(d_x_, d_stage_, g.n_z, g.n_x, g.n_y, fp64_, s);
   if (rc) return cuda_check(rc, "volume read-out");
   cudaMemcpyAsync(out, d_stage_, sizeof(float) * nv, cudaMemcpyDeviceToHost, s);
   return cudaStreamSynchronize(s) == cudaSuccess ? 0 : cuda_check(MBIR_EDEVICE, "volume read-out");
 }
 
-static int sino_readout(Engine* eng, const float* dsrc, float* stage, float* out, int64_t n,
-                        const Geometry& g, int n_rp, void* stream) {
+static int sino_readout(Engine* eng, const void* dsrc, float* stage, float* out, int64_t n,
+                        const Geometry& g, int n_rp, int fp64, void* stream) {
   const size_t nh = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;
   if (!out || n < static_cast<int64_t>(nh)) return eng->fail(MBIR_EINVAL, "buffer too small");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (launch_sino_to_host(dsrc, stage, g.n_theta, g.n_r, n_rp, g.n_t, s))
+  if (launch_sino_to_host(dsrc, stage, g.n_theta, g.n_r, n_rp, g.n_t, fp64, s))
     return eng->fail(MBIR_EDEVICE, "sinogram read-out");
   cudaMemcpyAsync(out, stage, sizeof(float) * nh, cudaMemcpyDeviceToHost, s);
   return cudaStreamSynchronize(s) == cudaSuccess ? 0 : eng->fail(MBIR_EDEVICE, "sinogram read-out");
@@ -956,11 +991,11 @@ static int sino_readout(Engine* eng, const float* dsrc, float* stage, float* out
 
 int Engine::get_error(float* out, int64_t n) {
   if (state_ < 2) return fail(MBIR_ESTATE, "get_error: call prepare first");
-  return sino_readout(this, d_e_, d_stage_, out, n, g_, n_rp_, stream_);
+  return sino_readout(this, d_e_, d_stage_, out, n, g_, n_rp_, fp64_, stream_);
 }
 int Engine::get_projection(float* out, int64_t n) {
   if (state_ < 2) return fail(MBIR_ESTATE, "get_projection: call prepare first");
-  return sino_readout(this, d_yest_, d_stage_, out, n, g_, n_rp_, stream_);
+  return sino_readout(this, d_yest_, d_stage_, out, n, g_, n_rp_, fp64_, stream_);
 }
 
 int Engine::get_nuisance(double* gg, double* o, double* v) {

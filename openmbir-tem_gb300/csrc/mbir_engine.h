@@ -126,20 +126,23 @@ class Engine {
   std::vector<double> I_, mu_, alpha_, w_;
   std::vector<double> init_gain_, init_offset_, init_var_;
 
-  // device buffers
-  float* d_y_ = nullptr;
-  float* d_e_ = nullptr;
-  float* d_yest_ = nullptr;
-  float* d_x_ = nullptr;
-  float* d_stage_ = nullptr;  // host-layout staging buffer for transposes
-  float* d_H_ = nullptr;
+  // device buffers; "Real" arrays hold float (FP32 engine) or double (FP64 engine)
+  int fp64_ = 0;
+  size_t rb_ = 4;             // bytes per Real
+  void* d_y_ = nullptr;       // Real [n_t][n_theta][n_rp]
+  void* d_e_ = nullptr;
+  void* d_yest_ = nullptr;
+  void* d_x_ = nullptr;       // Real [n_y][n_z][n_x]
+  float* d_stage_ = nullptr;  // host-layout staging buffer for transposes (float)
+  void* d_H_ = nullptr;       // Real [n_theta][bins+1]
   float2* d_bx_ = nullptr;
+  double* d_bxd_ = nullptr;
   double* d_u0_ = nullptr;
   double* d_bz_ = nullptr;
-  float2* d_gw_ = nullptr;
+  void* d_gw_ = nullptr;      // Real2 [n_theta]
   int* d_tfirst_ = nullptr;
   int* d_tcount_ = nullptr;
-  float* d_hval_ = nullptr;
+  void* d_hval_ = nullptr;    // Real [n_y][kMaxTRows]
   int* d_rows_ = nullptr;
   int* d_lines_ = nullptr;
   double* d_stats_ = nullptr;   // [max slices][4]

@@ -1,9 +1,9 @@
 // mbir_internal.h -- structures shared by the host engine and the sm_103a kernels.
 //
-// HBM layout (all FP32 unless noted):
+// HBM layout (FP32 by default; FP64 when the engine runs in double precision):
 //   sinogram-shaped arrays (measured y, error e, projection yest): [t][theta][r_pad]
 //     -- one detector row t (a y-slice of the tilt series) is one contiguous block of
-//        n_theta * n_rp floats, so a voxel slice's footprint rows are a single TMA bulk copy;
+//        n_theta * n_rp values, so a voxel slice's footprint rows are a single TMA bulk copy;
 //   volume x: [y][z][x] -- one voxel slice is contiguous;
 //   per-view tables: detector response H [theta][bins+1], (gain, weight) pairs, projection
 //     coefficients; per-slice t-response (first row, count, values).
@@ -22,27 +22,29 @@ constexpr int kStatSlots = 4;         // sum|dx| (ROI), sum|x| (ROI), zero-skipp
 struct DevGeom {
   int n_theta, n_r, n_rp, n_t;
   int n_x, n_y, n_z;
-  int bins;          // detector response bins (64)
-  float kr;          // delta_r / OffsetR: detector-bin distance -> response-table index
-  float half_width;  // delta_xz / delta_r: footprint half width in detector bins
+  int bins;            // detector response bins (64)
+  double kr;           // delta_r / OffsetR: detector-bin distance -> response-table index
+  double half_width;   // delta_xz / delta_r: footprint half width in detector bins
   int roi_x0, roi_x1, roi_z0, roi_z1;  // ROI mask as index ranges [x0,x1] x [z0,z1]
 };
 
+// Type-erased table pointers: Real = float or double according to the engine precision.
 struct DevTables {
-  const float* H;        // [n_theta][bins+1], last entry repeats bins-1
-  const float2* bx;      // [n_theta] (hi, lo) of delta_xz*cos/delta_r
+  const void* H;         // Real [n_theta][bins+1], last entry repeats bins-1
+  const float2* bx;      // [n_theta] (hi, lo) of delta_xz*cos/delta_r   (FP32 path)
+  const double* bxd;     // [n_theta] delta_xz*cos/delta_r               (FP64 path)
   const double* u0;      // [n_theta] detector coordinate (bins) of voxel (0,0)
   const double* bz;      // [n_theta] delta_xz*sin/delta_r
-  const float2* gw;      // [n_theta] (gain I_theta, weight 1/alpha_theta)
+  const void* gw;        // Real2 [n_theta] (gain I_theta, weight 1/alpha_theta)
   const int* t_first;    // [n_y]
   const int* t_count;    // [n_y]
-  const float* hval;     // [n_y][kMaxTRows]
+  const void* hval;      // Real [n_y][kMaxTRows]
 };
 
 struct DevFilter {
-  float f[27];           // prior weights [dy+1][dz+1][dx+1]
-  float mrf_p, mrf_q, mrf_c, mrf_alpha;
-  float sig_p, sig_pq;   // sigma^P, sigma^(P-Q)
+  double f[27];          // prior weights [dy+1][dz+1][dx+1]
+  double mrf_p, mrf_q, mrf_c, mrf_alpha;
+  double sig_p, sig_pq;  // sigma^P, sigma^(P-Q)
 };
 
 enum SweepMode : int { kModeICD = 0, kModeProject = 1 };
@@ -51,8 +53,8 @@ struct SweepArgs {
   DevGeom g;
   DevTables tab;
   DevFilter flt;
-  float* x;              // [n_y][n_z][n_x]
-  float* e;              // [n_t][n_theta][n_rp]  (ICD: error; project: accumulated yest)
+  void* x;               // Real [n_y][n_z][n_x]
+  void* e;               // Real [n_t][n_theta][n_rp]  (ICD: error; project: accumulated yest)
   const int* row_order;  // [n_z]
   int stride;            // x stride of a conflict-free class
   int colour;            // y parity of the slices in this launch
@@ -61,7 +63,8 @@ struct SweepArgs {
   int iter_nonzero;      // zero skipping active (not the first sweep)
   int zero_skipping;
   int smem_rows;         // 1: stage the slice in shared memory
-  int n_rs;              // shared-memory row stride (floats)
+  int n_rs;              // shared-memory row stride (values)
+  int fp64;              // 1: Real = double
   double* stats;         // [gridDim.x][kStatSlots]
   int* err;              // device error word
 };
@@ -70,36 +73,40 @@ struct RefOrderArgs {
   DevGeom g;
   DevTables tab;
   DevFilter flt;
-  float* x;
-  float* e;
+  void* x;
+  void* e;
   const int* lines;      // visit order: z*n_x + x
   int n_lines;
   int iter_nonzero;
   int zero_skipping;
+  int fp64;
   double* stats;         // [kStatSlots]
 };
 
-// launchers (mbir_kernels.cu)
+// launchers (mbir_kernels.cu); fp64 selects Real = double for the void* arrays
 int launch_sweep(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_ref_order(const RefOrderArgs& a, int nb, void* stream);
-size_t sweep_smem_bytes(int n_theta, int n_rs, int t_rows, int bins);
-int launch_sino_to_dev(const float* host_layout_dev, float* dev_layout, int n_theta, int n_r,
-                       int n_rp, int n_t, void* stream);
-int launch_sino_to_host(const float* dev_layout, float* host_layout, int n_theta, int n_r,
-                        int n_rp, int n_t, void* stream);
-int launch_vol_to_dev(const float* zxy, float* yzx, int n_z, int n_x, int n_y, void* stream);
-int launch_vol_to_host(const float* yzx, float* zxy, int n_z, int n_x, int n_y, void* stream);
-int launch_error_from_projection(const float* y, const float* yest, float* e, const double* mu,
-                                 int n_theta, int n_rp, int n_r, int n_t, void* stream);
+size_t sweep_smem_bytes(int n_theta, int n_rs, int t_rows, int bins, int fp64);
+int launch_sino_to_dev(const float* host_layout, void* dev_layout, int n_theta, int n_r, int n_rp,
+                       int n_t, int fp64, void* stream);
+int launch_sino_to_host(const void* dev_layout, float* host_layout, int n_theta, int n_r,
+                        int n_rp, int n_t, int fp64, void* stream);
+int launch_vol_to_dev(const float* zxy, void* yzx, int n_z, int n_x, int n_y, int fp64,
+                      void* stream);
+int launch_vol_to_host(const void* yzx, float* zxy, int n_z, int n_x, int n_y, int fp64,
+                       void* stream);
+int launch_error_from_projection(const void* y, const void* yest, void* e, const double* mu,
+                                 int n_theta, int n_rp, int n_r, int n_t, int fp64, void* stream);
 // per-view FP64 sums; kind 0: joint-estimation sums (6), kind 1: sum e^2 (1)
-int launch_view_sums(int kind, const float* y, const float* e, const double* mu,
+int launch_view_sums(int kind, const void* y, const void* e, const double* mu,
                      const double* gain, const double* wv, double* partial, double* out,
-                     int n_theta, int n_rp, int n_r, int n_t, int n_chunk, void* stream);
-int launch_rebuild_error(const float* y, float* e, const double* mu_old, const double* gain_old,
+                     int n_theta, int n_rp, int n_r, int n_t, int n_chunk, int fp64,
+                     void* stream);
+int launch_rebuild_error(const void* y, void* e, const double* mu_old, const double* gain_old,
                          const double* mu_new, const double* gain_new, int n_theta, int n_rp,
-                         int n_r, int n_t, void* stream);
-int launch_prior_cost(const float* x, const DevFilter& f, int n_z, int n_x, int n_y,
-                      double* partial, int n_blocks, void* stream);
+                         int n_r, int n_t, int fp64, void* stream);
+int launch_prior_cost(const void* x, const DevFilter& f, int n_z, int n_x, int n_y,
+                      double* partial, int n_blocks, int fp64, void* stream);
 int launch_reduce_stats(const double* in, int n_rows, int n_cols, double* out, void* stream);
 
 }  // namespace mbir

@@ -14,12 +14,16 @@
 //                     with the error sinogram in HBM; one warp, used for order-exact parity.
 //   view_sums_kernel  FP64 per-view reductions for gain/offset and variance estimation.
 //   prior_cost_kernel FP64 accumulation of the QGGMRF prior term of the MAP cost.
+// Every kernel is instantiated for Real = float (production) and Real = double (the
+// reference's own precision, for order-exact parity and precision studies).
 //
 // Reference semantics follow Code/MBIRLib/HAADF/HAADF_ReconstructionEngine_UpdateVoxels.cpp
 // (UpdateYSlice::execute :149-484), Code/MBIRLib/Common/AMatrixCol.cpp:82-239 (A-column),
 // Code/MBIRLib/Reconstruction/QGGMRF_Functions.cpp:82-206 (prior), and
 // HAADF_ReconstructionEngine_Extra.cpp:419-881 / HAADF_ReconstructionEngine.cpp:1147-1364.
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "mbir_internal.h"
 
@@ -29,6 +33,17 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr uint32_t kWaitLimit = 1u << 24;  // bounded mbarrier polls before giving up
+
+template <typename Real>
+struct V2;
+template <>
+struct V2<float> {
+  using type = float2;
+};
+template <>
+struct V2<double> {
+  using type = double2;
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -85,36 +100,47 @@ __device__ __forceinline__ void bulk_wait_all() {
 }
 
 // ---- warp reductions ------------------------------------------------------------------
-__device__ __forceinline__ float warp_sum(float v) {
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
   return v;
 }
-__device__ __forceinline__ float warp_min(float v) {
+template <typename T>
+__device__ __forceinline__ T warp_min(T v) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(kFull, v, o));
+  for (int o = 16; o > 0; o >>= 1) {
+    const T w = __shfl_xor_sync(kFull, v, o);
+    v = w < v ? w : v;
+  }
   return v;
 }
-__device__ __forceinline__ float warp_max(float v) {
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, o));
-  return v;
-}
-__device__ __forceinline__ double warp_sum_d(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  for (int o = 16; o > 0; o >>= 1) {
+    const T w = __shfl_xor_sync(kFull, v, o);
+    v = w > v ? w : v;
+  }
   return v;
 }
 
-// Detector coordinate of a voxel row at one view, split as integer + fraction so that the
-// per-voxel position keeps ~1e-7 bin accuracy in FP32.
-struct RowBase {
+// Detector coordinate of a voxel row at one view.  FP32: integer + fraction so that the
+// per-voxel position keeps ~1e-7 bin accuracy; FP64: the coordinate itself.
+struct RowBaseF {
   int ib;
   float fb;
 };
+struct RowBaseD {
+  double base;
+};
+template <typename Real>
+using RowBase = typename std::conditional<std::is_same<Real, float>::value, RowBaseF,
+                                          RowBaseD>::type;
 
 // u = j0 + f (f in [0,1)) for voxel column x: u = base(z) + x * bx with bx given as hi+lo.
-__device__ __forceinline__ void detector_pos(int x, RowBase rb, float2 bx, int& j0, float& f) {
+__device__ __forceinline__ void detector_pos(int x, RowBaseF rb, float2 bx, double, int& j0,
+                                             float& f) {
   const float xf = static_cast<float>(x);
   const float p = xf * bx.x;
   const float pe = fmaf(xf, bx.x, -p);  // exact rounding error of x*bx.hi
@@ -125,96 +151,126 @@ __device__ __forceinline__ void detector_pos(int x, RowBase rb, float2 bx, int& 
   j0 = rb.ib + static_cast<int>(jp) + static_cast<int>(jf);
   f = ff;
 }
+__device__ __forceinline__ void detector_pos(int x, RowBaseD rb, float2, double bxd, int& j0,
+                                             double& f) {
+  const double u = fma(static_cast<double>(x), bxd, rb.base);
+  const double fl = floor(u);
+  j0 = static_cast<int>(fl);
+  f = u - fl;
+}
+
+template <typename Real>
+__device__ __forceinline__ void compute_row_base(const DevTables& tab, int n_theta, int z,
+                                                 RowBase<Real>* rb, int tid, int nthreads) {
+  for (int v = tid; v < n_theta; v += nthreads) {
+    const double b = tab.u0[v] - static_cast<double>(z) * tab.bz[v];
+    if constexpr (std::is_same<Real, float>::value) {
+      const double fl = floor(b);
+      rb[v].ib = static_cast<int>(fl);
+      rb[v].fb = static_cast<float>(b - fl);
+    } else {
+      rb[v].base = b;
+    }
+  }
+}
 
 // A-matrix entries of one voxel at one view (AMatrixCol.cpp:148-232): bins j in
 // [floor(u-d), floor(u+d)] on the detector, value = linear interpolation of the detector
 // response at |u - (j+0.5)|, kept when > 0.
-template <int NB>
-__device__ __forceinline__ void view_footprint(const DevGeom& g, const float* __restrict__ hrow,
-                                               int j0, float f, int& jlo, float (&a)[NB]) {
-  const int lo = j0 + static_cast<int>(floorf(f - g.half_width));
-  const int hi = j0 + static_cast<int>(floorf(f + g.half_width));
+template <typename Real, int NB>
+__device__ __forceinline__ void view_footprint(const DevGeom& g, const Real* __restrict__ hrow,
+                                               int j0, Real f, int& jlo, Real (&a)[NB]) {
+  const Real hw = static_cast<Real>(g.half_width);
+  const Real kr = static_cast<Real>(g.kr);
+  const int lo = j0 + static_cast<int>(floor(f - hw));
+  const int hi = j0 + static_cast<int>(floor(f + hw));
   jlo = lo;
 #pragma unroll
   for (int b = 0; b < NB; ++b) {
     const int j = lo + b;
-    float v = 0.f;
+    Real v = Real(0);
     if (j <= hi && j >= 0 && j < g.n_r) {
-      const float delta = fabsf(static_cast<float>(j0 - j) + f - 0.5f);
-      const float xr = delta * g.kr;
+      const Real delta = fabs(static_cast<Real>(j0 - j) + f - Real(0.5));
+      const Real xr = delta * kr;
       const int idx = static_cast<int>(xr);
       if (idx < g.bins) {
-        const float t = xr - static_cast<float>(idx);
-        v = (1.f - t) * hrow[idx] + t * hrow[idx + 1];
+        const Real t = xr - static_cast<Real>(idx);
+        v = (Real(1) - t) * hrow[idx] + t * hrow[idx + 1];
       }
     }
-    a[b] = v > 0.f ? v : 0.f;
+    a[b] = v > Real(0) ? v : Real(0);
   }
 }
 
 // rho'(d)/d of the QGGMRF prior (QGGMRF_Functions.cpp:90-104 divided by d), or rho''(0)
 // (:109-112) when d == 0.
-__device__ __forceinline__ float qggmrf_coef(const DevFilter& q, float d0) {
-  if (d0 == 0.f) return q.mrf_p / (q.sig_p * q.mrf_c);
-  const float ad = fabsf(d0);
-  const float t1 = powf(ad, q.mrf_p - q.mrf_q) / q.sig_pq;
-  const float t3 = q.mrf_c + t1;
-  float r = (q.mrf_p - ((q.mrf_p - q.mrf_q) * t1) / t3) / (t3 * q.sig_p);
-  if (q.mrf_p != 2.f) r *= powf(ad, q.mrf_p - 2.f);
+template <typename Real>
+__device__ __forceinline__ Real qggmrf_coef(const DevFilter& q, Real d0) {
+  const Real P = static_cast<Real>(q.mrf_p), Q = static_cast<Real>(q.mrf_q);
+  const Real c = static_cast<Real>(q.mrf_c), sp = static_cast<Real>(q.sig_p);
+  if (d0 == Real(0)) return P / (sp * c);
+  const Real ad = fabs(d0);
+  const Real t1 = pow(ad, P - Q) / static_cast<Real>(q.sig_pq);
+  const Real t3 = c + t1;
+  Real r = (P - ((P - Q) * t1) / t3) / (t3 * sp);
+  if (P != Real(2)) r *= pow(ad, P - Real(2));
   return r;
 }
 
 // One voxel (z, x, y) processed by one warp.  es points at the first detector row of slice y
-// (row stride rs floats between views, plane stride ps between t rows).  Returns in wst
+// (row stride rs values between views, plane stride ps between t rows).  Returns in wst
 // (lane 0): ROI sum|dx|, ROI sum|x|, zero-skipped, updated.
-template <int NB>
+template <typename Real, int NB>
 __device__ __forceinline__ void voxel_step(const DevGeom& g, const DevFilter& q,
-                                           float* __restrict__ vol, float* es, int rs, int ps,
-                                           const RowBase* rb, const float* sH,
-                                           const float2* sbx, const float2* sgw, int z, int x,
-                                           int y, int tcount, const float* hv, int mode,
+                                           Real* __restrict__ vol, Real* es, int rs, int ps,
+                                           const RowBase<Real>* rb, const Real* sH,
+                                           const float2* sbx, const double* sbxd,
+                                           const typename V2<Real>::type* sgw, int z, int x,
+                                           int y, int tcount, const Real* hv, int mode,
                                            int iter_nonzero, int zero_skipping, int lane,
                                            double* wst) {
+  using R2 = typename V2<Real>::type;
   const size_t plane = static_cast<size_t>(g.n_z) * g.n_x;
   const size_t vidx = static_cast<size_t>(y) * plane + static_cast<size_t>(z) * g.n_x + x;
-  const float V = vol[vidx];
+  const Real V = vol[vidx];
+  const Real hw = static_cast<Real>(g.half_width);
 
   int jlo[kMaxViewsPerLane];
-  float a[kMaxViewsPerLane][NB];
+  Real a[kMaxViewsPerLane][NB];
   bool any = false;
 #pragma unroll
   for (int i = 0; i < kMaxViewsPerLane; ++i) {
     const int v = lane + 32 * i;
     jlo[i] = 0;
 #pragma unroll
-    for (int b = 0; b < NB; ++b) a[i][b] = 0.f;
+    for (int b = 0; b < NB; ++b) a[i][b] = Real(0);
     if (v < g.n_theta) {
       int j0;
-      float f;
-      detector_pos(x, rb[v], sbx[v], j0, f);
-      const float u = static_cast<float>(j0) + f;
-      if (!(u + g.half_width < 0.f || u - g.half_width > static_cast<float>(g.n_r))) {
-        view_footprint<NB>(g, sH + v * (g.bins + 1), j0, f, jlo[i], a[i]);
+      Real f;
+      detector_pos(x, rb[v], sbx ? sbx[v] : float2{0.f, 0.f}, sbxd ? sbxd[v] : 0.0, j0, f);
+      const Real u = static_cast<Real>(j0) + f;
+      if (!(u + hw < Real(0) || u - hw > static_cast<Real>(g.n_r))) {
+        view_footprint<Real, NB>(g, sH + v * (g.bins + 1), j0, f, jlo[i], a[i]);
 #pragma unroll
-        for (int b = 0; b < NB; ++b) any |= (a[i][b] > 0.f);
+        for (int b = 0; b < NB; ++b) any |= (a[i][b] > Real(0));
       }
     }
   }
   if (!__any_sync(kFull, any)) return;  // empty A-column: the line is never visited
 
   if (mode == kModeProject) {
-    if (V != 0.f) {
+    if (V != Real(0)) {
 #pragma unroll
       for (int i = 0; i < kMaxViewsPerLane; ++i) {
         const int v = lane + 32 * i;
         if (v >= g.n_theta) continue;
-        const float gain = sgw[v].x;
+        const Real gain = sgw[v].x;
         for (int tr = 0; tr < tcount; ++tr) {
-          const float hh = hv[tr];
-          float* row = es + tr * ps + v * rs + jlo[i];
+          const Real hh = hv[tr];
+          Real* row = es + tr * ps + v * rs + jlo[i];
 #pragma unroll
           for (int b = 0; b < NB; ++b)
-            if (a[i][b] > 0.f) row[b] += gain * (a[i][b] * hh * V);
+            if (a[i][b] > Real(0)) row[b] += gain * (a[i][b] * hh * V);
         }
       }
     }
@@ -222,7 +278,7 @@ __device__ __forceinline__ void voxel_step(const DevGeom& g, const DevFilter& q,
   }
 
   // 26-neighbourhood, one neighbour per lane (UpdateVoxels.cpp:283-306)
-  float nb = 0.f;
+  Real nb = Real(0);
   bool nvalid = false;
   if (lane < 27) {
     const int dy = lane / 9 - 1, dz = (lane / 3) % 3 - 1, dx = lane % 3 - 1;
@@ -233,69 +289,69 @@ __device__ __forceinline__ void voxel_step(const DevGeom& g, const DevFilter& q,
     }
   }
   // zero skipping (UpdateVoxels.cpp:310-338)
-  if (zero_skipping && iter_nonzero && V == 0.f) {
-    if (!__any_sync(kFull, nb > 0.f)) {
+  if (zero_skipping && iter_nonzero && V == Real(0)) {
+    if (!__any_sync(kFull, nb > Real(0))) {
       if (lane == 0) wst[2] += 1.0;
       return;
     }
   }
   // theta1 / theta2 (UpdateVoxels.cpp:343-369)
-  float t1 = 0.f, t2 = 0.f;
+  Real t1 = Real(0), t2 = Real(0);
 #pragma unroll
   for (int i = 0; i < kMaxViewsPerLane; ++i) {
     const int v = lane + 32 * i;
     if (v >= g.n_theta) continue;
-    const float2 gw = sgw[v];
+    const R2 gw = sgw[v];
     for (int tr = 0; tr < tcount; ++tr) {
-      const float hh = hv[tr];
-      const float* row = es + tr * ps + v * rs + jlo[i];
+      const Real hh = hv[tr];
+      const Real* row = es + tr * ps + v * rs + jlo[i];
 #pragma unroll
       for (int b = 0; b < NB; ++b) {
-        if (a[i][b] > 0.f) {
-          const float pe = gw.x * a[i][b] * hh;
+        if (a[i][b] > Real(0)) {
+          const Real pe = gw.x * a[i][b] * hh;
           t2 += pe * pe * gw.y;
           t1 += row[b] * pe * gw.y;
         }
       }
     }
   }
-  const float theta1 = -warp_sum(t1);
-  const float theta2 = warp_sum(t2);
+  const Real theta1 = -warp_sum(t1);
+  const Real theta2 = warp_sum(t2);
   // bracket (find_min_max, UpdateVoxels.cpp:47-63): over all 27 entries, centre and
   // out-of-range entries count as 0
-  float lo = warp_min(nb), hi = warp_max(nb);
-  if (theta2 != 0.f) {
-    const float cand = V - theta1 / theta2;
+  Real lo = warp_min(nb), hi = warp_max(nb);
+  if (theta2 != Real(0)) {
+    const Real cand = V - theta1 / theta2;
     lo = lo > cand ? cand : lo;
     hi = hi < cand ? cand : hi;
   }
   // QGGMRF surrogate, one iteration (QGGMRF_Functions.cpp:153-206)
-  float s1 = 0.f, s2 = 0.f;
+  Real s1 = Real(0), s2 = Real(0);
   if (nvalid) {
-    const float tc = q.f[lane] * qggmrf_coef(q, V - nb);
+    const Real tc = static_cast<Real>(q.f[lane]) * qggmrf_coef<Real>(q, V - nb);
     s1 = tc * nb;
     s2 = tc;
   }
   s1 = warp_sum(s1);
   s2 = warp_sum(s2);
-  const float u = (s1 + theta2 * V - theta1) / (s2 + theta2);
-  float nv = V + q.mrf_alpha * (u - V);
+  const Real u = (s1 + theta2 * V - theta1) / (s2 + theta2);
+  Real nv = V + static_cast<Real>(q.mrf_alpha) * (u - V);
   nv = (nv < lo) ? lo : ((nv > hi) ? hi : nv);
-  if (nv < 0.f) nv = 0.f;  // positivity (UpdateVoxels.cpp:394-400)
-  const float dlt = nv - V;
+  if (nv < Real(0)) nv = Real(0);  // positivity (UpdateVoxels.cpp:394-400)
+  const Real dlt = nv - V;
   // error-sinogram scatter (UpdateVoxels.cpp:423-449)
-  if (dlt != 0.f) {
+  if (dlt != Real(0)) {
 #pragma unroll
     for (int i = 0; i < kMaxViewsPerLane; ++i) {
       const int v = lane + 32 * i;
       if (v >= g.n_theta) continue;
-      const float gain = sgw[v].x;
+      const Real gain = sgw[v].x;
       for (int tr = 0; tr < tcount; ++tr) {
-        const float hh = hv[tr];
-        float* row = es + tr * ps + v * rs + jlo[i];
+        const Real hh = hv[tr];
+        Real* row = es + tr * ps + v * rs + jlo[i];
 #pragma unroll
         for (int b = 0; b < NB; ++b)
-          if (a[i][b] > 0.f) row[b] -= gain * (a[i][b] * hh * dlt);
+          if (a[i][b] > Real(0)) row[b] -= gain * (a[i][b] * hh * dlt);
       }
     }
   }
@@ -309,24 +365,14 @@ __device__ __forceinline__ void voxel_step(const DevGeom& g, const DevFilter& q,
   }
 }
 
-__device__ __forceinline__ void compute_row_base(const DevTables& tab, int n_theta, int z,
-                                                 RowBase* rb, int tid, int nthreads) {
-  for (int v = tid; v < n_theta; v += nthreads) {
-    const double b = tab.u0[v] - static_cast<double>(z) * tab.bz[v];
-    const double fl = floor(b);
-    rb[v].ib = static_cast<int>(fl);
-    rb[v].fb = static_cast<float>(b - fl);
-  }
-}
-
 struct SmemLayout {
-  size_t bar, stats, rb, bx, gw, H, hv, es, total;
+  size_t bar, stats, rb, bx, bxd, gw, H, hv, es, total;
 };
 
 __host__ __device__ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 __host__ __device__ inline SmemLayout smem_layout(int n_theta, int n_rs, int t_rows, int bins,
-                                                  bool stage) {
+                                                  bool stage, size_t real_bytes) {
   SmemLayout L;
   size_t o = 0;
   L.bar = o;
@@ -334,23 +380,26 @@ __host__ __device__ inline SmemLayout smem_layout(int n_theta, int n_rs, int t_r
   L.stats = o;
   o += sizeof(double) * kWarps * kStatSlots;
   L.rb = o;
-  o = align_up(o + sizeof(RowBase) * n_theta, 16);
+  o = align_up(o + 8 * static_cast<size_t>(n_theta), 16);
   L.bx = o;
   o = align_up(o + sizeof(float2) * n_theta, 16);
+  L.bxd = o;
+  o = align_up(o + sizeof(double) * n_theta, 16);
   L.gw = o;
-  o = align_up(o + sizeof(float2) * n_theta, 16);
+  o = align_up(o + 2 * real_bytes * n_theta, 16);
   L.H = o;
-  o = align_up(o + sizeof(float) * n_theta * (bins + 1), 16);
+  o = align_up(o + real_bytes * n_theta * (bins + 1), 16);
   L.hv = o;
-  o = align_up(o + sizeof(float) * kMaxTRows, 128);
+  o = align_up(o + real_bytes * kMaxTRows, 128);
   L.es = o;
-  if (stage) o += sizeof(float) * static_cast<size_t>(t_rows) * n_theta * n_rs;
+  if (stage) o += real_bytes * static_cast<size_t>(t_rows) * n_theta * n_rs;
   L.total = align_up(o, 16);
   return L;
 }
 
-template <int NB, bool STAGE>
+template <typename Real, int NB, bool STAGE>
 __global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
+  using R2 = typename V2<Real>::type;
   extern __shared__ __align__(128) unsigned char smem[];
   const DevGeom& g = A.g;
   const int y = A.colour + 2 * static_cast<int>(blockIdx.x);
@@ -358,33 +407,41 @@ __global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
   const int tid = threadIdx.x, nthreads = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31;
   const int tcount = A.tab.t_count[y], tfirst = A.tab.t_first[y];
-  const SmemLayout L = smem_layout(g.n_theta, A.n_rs, tcount, g.bins, STAGE);
+  const SmemLayout L = smem_layout(g.n_theta, A.n_rs, tcount, g.bins, STAGE, sizeof(Real));
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L.bar);
   double* sstat = reinterpret_cast<double*>(smem + L.stats);
-  RowBase* rb = reinterpret_cast<RowBase*>(smem + L.rb);
+  RowBase<Real>* rb = reinterpret_cast<RowBase<Real>*>(smem + L.rb);
   float2* sbx = reinterpret_cast<float2*>(smem + L.bx);
-  float2* sgw = reinterpret_cast<float2*>(smem + L.gw);
-  float* sH = reinterpret_cast<float*>(smem + L.H);
-  float* shv = reinterpret_cast<float*>(smem + L.hv);
+  double* sbxd = reinterpret_cast<double*>(smem + L.bxd);
+  R2* sgw = reinterpret_cast<R2*>(smem + L.gw);
+  Real* sH = reinterpret_cast<Real*>(smem + L.H);
+  Real* shv = reinterpret_cast<Real*>(smem + L.hv);
+  const Real* gH = static_cast<const Real*>(A.tab.H);
+  const R2* ggw = static_cast<const R2*>(A.tab.gw);
+  const Real* ghv = static_cast<const Real*>(A.tab.hval);
+  Real* const ge = static_cast<Real*>(A.e);
+  Real* const gx = static_cast<Real*>(A.x);
+  constexpr bool kF32 = std::is_same<Real, float>::value;
 
-  for (int i = tid; i < g.n_theta * (g.bins + 1); i += nthreads) sH[i] = A.tab.H[i];
+  for (int i = tid; i < g.n_theta * (g.bins + 1); i += nthreads) sH[i] = gH[i];
   for (int v = tid; v < g.n_theta; v += nthreads) {
-    sbx[v] = A.tab.bx[v];
-    sgw[v] = A.tab.gw[v];
+    if (kF32) sbx[v] = A.tab.bx[v];
+    else sbxd[v] = A.tab.bxd[v];
+    sgw[v] = ggw[v];
   }
-  if (tid < kMaxTRows) shv[tid] = A.tab.hval[y * kMaxTRows + tid];
+  if (tid < kMaxTRows) shv[tid] = ghv[y * kMaxTRows + tid];
 
   const size_t sino_plane = static_cast<size_t>(g.n_theta) * g.n_rp;
-  float* es;
+  Real* es;
   int rs, ps;
   const int rows = tcount * g.n_theta;
-  const uint32_t row_bytes = static_cast<uint32_t>(g.n_rp * sizeof(float));
+  const uint32_t row_bytes = static_cast<uint32_t>(g.n_rp * sizeof(Real));
   if (STAGE) {
-    es = reinterpret_cast<float*>(smem + L.es);
+    es = reinterpret_cast<Real*>(smem + L.es);
     rs = A.n_rs;
     ps = g.n_theta * A.n_rs;
     if (A.mode == kModeProject) {
-      for (int i = tid; i < tcount * ps; i += nthreads) es[i] = 0.f;
+      for (int i = tid; i < tcount * ps; i += nthreads) es[i] = Real(0);
       __syncthreads();
     } else {
       if (tid == 0) {
@@ -396,8 +453,9 @@ __global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
       __syncthreads();
       for (int r = tid; r < rows; r += nthreads) {
         const int tr = r / g.n_theta, v = r % g.n_theta;
-        bulk_g2s(es + tr * ps + v * rs, A.e + (static_cast<size_t>(tfirst + tr)) * sino_plane +
-                                            static_cast<size_t>(v) * g.n_rp,
+        bulk_g2s(es + tr * ps + v * rs,
+                 ge + (static_cast<size_t>(tfirst + tr)) * sino_plane +
+                     static_cast<size_t>(v) * g.n_rp,
                  row_bytes, bar);
       }
       const bool ok = mbar_wait(bar, 0);
@@ -408,7 +466,7 @@ __global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
       }
     }
   } else {
-    es = A.e + static_cast<size_t>(tfirst) * sino_plane;
+    es = ge + static_cast<size_t>(tfirst) * sino_plane;
     rs = g.n_rp;
     ps = static_cast<int>(sino_plane);
   }
@@ -417,12 +475,13 @@ __global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
   for (int rr = 0; rr < g.n_z; ++rr) {
     const int z = A.row_order[rr];
     __syncthreads();
-    compute_row_base(A.tab, g.n_theta, z, rb, tid, nthreads);
+    compute_row_base<Real>(A.tab, g.n_theta, z, rb, tid, nthreads);
     __syncthreads();
     for (int k = 0; k < A.stride; ++k) {
       for (int x = k + A.stride * warp; x < g.n_x; x += A.stride * kWarps)
-        voxel_step<NB>(g, A.flt, A.x, es, rs, ps, rb, sH, sbx, sgw, z, x, y, tcount, shv, A.mode,
-                       A.iter_nonzero, A.zero_skipping, lane, wst);
+        voxel_step<Real, NB>(g, A.flt, gx, es, rs, ps, rb, sH, kF32 ? sbx : nullptr,
+                             kF32 ? nullptr : sbxd, sgw, z, x, y, tcount, shv, A.mode,
+                             A.iter_nonzero, A.zero_skipping, lane, wst);
       __syncthreads();
     }
   }
@@ -432,7 +491,7 @@ __global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
     __syncthreads();
     for (int r = tid; r < rows; r += nthreads) {
       const int tr = r / g.n_theta, v = r % g.n_theta;
-      bulk_s2g(A.e + (static_cast<size_t>(tfirst + tr)) * sino_plane +
+      bulk_s2g(ge + (static_cast<size_t>(tfirst + tr)) * sino_plane +
                    static_cast<size_t>(v) * g.n_rp,
                es + tr * ps + v * rs, row_bytes);
     }
@@ -451,20 +510,29 @@ __global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
   }
 }
 
-template <int NB>
+template <typename Real, int NB>
 __global__ void __launch_bounds__(32, 1) ref_order_kernel(RefOrderArgs A) {
+  using R2 = typename V2<Real>::type;
   extern __shared__ __align__(128) unsigned char smem[];
   const DevGeom& g = A.g;
   const int lane = threadIdx.x;
-  const SmemLayout L = smem_layout(g.n_theta, 0, 0, g.bins, false);
-  RowBase* rb = reinterpret_cast<RowBase*>(smem + L.rb);
+  const SmemLayout L = smem_layout(g.n_theta, 0, 0, g.bins, false, sizeof(Real));
+  RowBase<Real>* rb = reinterpret_cast<RowBase<Real>*>(smem + L.rb);
   float2* sbx = reinterpret_cast<float2*>(smem + L.bx);
-  float2* sgw = reinterpret_cast<float2*>(smem + L.gw);
-  float* sH = reinterpret_cast<float*>(smem + L.H);
-  for (int i = lane; i < g.n_theta * (g.bins + 1); i += 32) sH[i] = A.tab.H[i];
+  double* sbxd = reinterpret_cast<double*>(smem + L.bxd);
+  R2* sgw = reinterpret_cast<R2*>(smem + L.gw);
+  Real* sH = reinterpret_cast<Real*>(smem + L.H);
+  const Real* gH = static_cast<const Real*>(A.tab.H);
+  const R2* ggw = static_cast<const R2*>(A.tab.gw);
+  const Real* ghv = static_cast<const Real*>(A.tab.hval);
+  Real* const ge = static_cast<Real*>(A.e);
+  Real* const gx = static_cast<Real*>(A.x);
+  constexpr bool kF32 = std::is_same<Real, float>::value;
+  for (int i = lane; i < g.n_theta * (g.bins + 1); i += 32) sH[i] = gH[i];
   for (int v = lane; v < g.n_theta; v += 32) {
-    sbx[v] = A.tab.bx[v];
-    sgw[v] = A.tab.gw[v];
+    if (kF32) sbx[v] = A.tab.bx[v];
+    else sbxd[v] = A.tab.bxd[v];
+    sgw[v] = ggw[v];
   }
   __syncwarp();
   const size_t sino_plane = static_cast<size_t>(g.n_theta) * g.n_rp;
@@ -473,13 +541,14 @@ __global__ void __launch_bounds__(32, 1) ref_order_kernel(RefOrderArgs A) {
     const int l = A.lines[n];
     const int z = l / g.n_x, x = l % g.n_x;
     __syncwarp();
-    compute_row_base(A.tab, g.n_theta, z, rb, lane, 32);
+    compute_row_base<Real>(A.tab, g.n_theta, z, rb, lane, 32);
     __syncwarp();
     for (int y = 0; y < g.n_y; ++y) {
-      float* es = A.e + static_cast<size_t>(A.tab.t_first[y]) * sino_plane;
-      voxel_step<NB>(g, A.flt, A.x, es, g.n_rp, static_cast<int>(sino_plane), rb, sH, sbx, sgw,
-                     z, x, y, A.tab.t_count[y], A.tab.hval + y * kMaxTRows, kModeICD,
-                     A.iter_nonzero, A.zero_skipping, lane, wst);
+      Real* es = ge + static_cast<size_t>(A.tab.t_first[y]) * sino_plane;
+      voxel_step<Real, NB>(g, A.flt, gx, es, g.n_rp, static_cast<int>(sino_plane), rb, sH,
+                           kF32 ? sbx : nullptr, kF32 ? nullptr : sbxd, sgw, z, x, y,
+                           A.tab.t_count[y], ghv + y * kMaxTRows, kModeICD, A.iter_nonzero,
+                           A.zero_skipping, lane, wst);
       __syncwarp();
     }
   }
@@ -488,7 +557,8 @@ __global__ void __launch_bounds__(32, 1) ref_order_kernel(RefOrderArgs A) {
 }
 
 // ---- layout conversions ----------------------------------------------------------------
-__global__ void sino_to_dev_kernel(const float* __restrict__ h, float* __restrict__ d, int n_theta,
+template <typename Real>
+__global__ void sino_to_dev_kernel(const float* __restrict__ h, Real* __restrict__ d, int n_theta,
                                    int n_r, int n_rp, int n_t) {
   const size_t total = static_cast<size_t>(n_t) * n_theta * n_rp;
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < total;
@@ -497,10 +567,11 @@ __global__ void sino_to_dev_kernel(const float* __restrict__ h, float* __restric
     const size_t rest = i / n_rp;
     const int v = static_cast<int>(rest % n_theta);
     const int t = static_cast<int>(rest / n_theta);
-    d[i] = (r < n_r) ? h[(static_cast<size_t>(v) * n_r + r) * n_t + t] : 0.f;
+    d[i] = (r < n_r) ? static_cast<Real>(h[(static_cast<size_t>(v) * n_r + r) * n_t + t]) : Real(0);
   }
 }
-__global__ void sino_to_host_kernel(const float* __restrict__ d, float* __restrict__ h, int n_theta,
+template <typename Real>
+__global__ void sino_to_host_kernel(const Real* __restrict__ d, float* __restrict__ h, int n_theta,
                                     int n_r, int n_rp, int n_t) {
   const size_t total = static_cast<size_t>(n_theta) * n_r * n_t;
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < total;
@@ -509,10 +580,11 @@ __global__ void sino_to_host_kernel(const float* __restrict__ d, float* __restri
     const size_t rest = i / n_t;
     const int r = static_cast<int>(rest % n_r);
     const int v = static_cast<int>(rest / n_r);
-    h[i] = d[(static_cast<size_t>(t) * n_theta + v) * n_rp + r];
+    h[i] = static_cast<float>(d[(static_cast<size_t>(t) * n_theta + v) * n_rp + r]);
   }
 }
-__global__ void vol_to_dev_kernel(const float* __restrict__ zxy, float* __restrict__ yzx, int n_z,
+template <typename Real>
+__global__ void vol_to_dev_kernel(const float* __restrict__ zxy, Real* __restrict__ yzx, int n_z,
                                   int n_x, int n_y) {
   const size_t total = static_cast<size_t>(n_z) * n_x * n_y;
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < total;
@@ -521,10 +593,11 @@ __global__ void vol_to_dev_kernel(const float* __restrict__ zxy, float* __restri
     const size_t rest = i / n_x;
     const int z = static_cast<int>(rest % n_z);
     const int y = static_cast<int>(rest / n_z);
-    yzx[i] = zxy[(static_cast<size_t>(z) * n_x + x) * n_y + y];
+    yzx[i] = static_cast<Real>(zxy[(static_cast<size_t>(z) * n_x + x) * n_y + y]);
   }
 }
-__global__ void vol_to_host_kernel(const float* __restrict__ yzx, float* __restrict__ zxy, int n_z,
+template <typename Real>
+__global__ void vol_to_host_kernel(const Real* __restrict__ yzx, float* __restrict__ zxy, int n_z,
                                    int n_x, int n_y) {
   const size_t total = static_cast<size_t>(n_z) * n_x * n_y;
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < total;
@@ -533,13 +606,14 @@ __global__ void vol_to_host_kernel(const float* __restrict__ yzx, float* __restr
     const size_t rest = i / n_y;
     const int x = static_cast<int>(rest % n_x);
     const int z = static_cast<int>(rest / n_x);
-    zxy[i] = yzx[(static_cast<size_t>(y) * n_z + z) * n_x + x];
+    zxy[i] = static_cast<float>(yzx[(static_cast<size_t>(y) * n_z + z) * n_x + x]);
   }
 }
 
 // e = y - yest - mu_theta (calculateMeasurementWeight, HAADF_ReconstructionEngine_Extra.cpp:693-771)
-__global__ void error_from_projection_kernel(const float* __restrict__ y,
-                                             const float* __restrict__ yest, float* __restrict__ e,
+template <typename Real>
+__global__ void error_from_projection_kernel(const Real* __restrict__ y,
+                                             const Real* __restrict__ yest, Real* __restrict__ e,
                                              const double* __restrict__ mu, int n_theta, int n_rp,
                                              int n_r, int n_t) {
   const size_t total = static_cast<size_t>(n_t) * n_theta * n_rp;
@@ -547,17 +621,17 @@ __global__ void error_from_projection_kernel(const float* __restrict__ y,
        i += static_cast<size_t>(gridDim.x) * blockDim.x) {
     const int r = static_cast<int>(i % n_rp);
     const int v = static_cast<int>((i / n_rp) % n_theta);
-    e[i] = (r < n_r) ? static_cast<float>(static_cast<double>(y[i]) -
-                                          static_cast<double>(yest[i]) - mu[v])
-                     : 0.f;
+    e[i] = (r < n_r) ? static_cast<Real>(static_cast<double>(y[i]) -
+                                         static_cast<double>(yest[i]) - mu[v])
+                     : Real(0);
   }
 }
 
 // Per-view FP64 sums.  kind 0 (jointEstimation, HAADF_ReconstructionEngine_Extra.cpp:474-517):
 //   [0] sum y w, [1] sum w, [2] sum yh w, [3] sum yh w y, [4] sum y^2 w, [5] sum yh^2 w,
 //   yh = (y - e - mu)/I.  kind 1 (updateWeights :825-833): [0] sum e^2.
-template <int K>
-__global__ void view_sums_kernel(const float* __restrict__ y, const float* __restrict__ e,
+template <typename Real, int K>
+__global__ void view_sums_kernel(const Real* __restrict__ y, const Real* __restrict__ e,
                                  const double* __restrict__ mu, const double* __restrict__ gain,
                                  const double* __restrict__ wv, double* __restrict__ partial,
                                  int n_theta, int n_rp, int n_r, int n_t, int n_chunk) {
@@ -590,7 +664,7 @@ __global__ void view_sums_kernel(const float* __restrict__ y, const float* __res
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < K; ++k) {
-    const double s = warp_sum_d(acc[k]);
+    const double s = warp_sum(acc[k]);
     if (lane == 0) red[warp][k] = s;
   }
   __syncthreads();
@@ -613,7 +687,8 @@ __global__ void view_sums_final_kernel(const double* __restrict__ partial, doubl
 
 // e = y - mu_new - I_new * yh, yh = (y - e - mu_old)/I_old
 // (jointEstimation, HAADF_ReconstructionEngine_Extra.cpp:464-472 and :600-612)
-__global__ void rebuild_error_kernel(const float* __restrict__ y, float* __restrict__ e,
+template <typename Real>
+__global__ void rebuild_error_kernel(const Real* __restrict__ y, Real* __restrict__ e,
                                      const double* __restrict__ mu_old,
                                      const double* __restrict__ gain_old,
                                      const double* __restrict__ mu_new,
@@ -627,7 +702,7 @@ __global__ void rebuild_error_kernel(const float* __restrict__ y, float* __restr
     const int v = static_cast<int>((i / n_rp) % n_theta);
     const double yv = y[i];
     const double yh = (yv - static_cast<double>(e[i]) - mu_old[v]) / gain_old[v];
-    e[i] = static_cast<float>(yv - mu_new[v] - (gain_new[v] * yh));
+    e[i] = static_cast<Real>(yv - mu_new[v] - (gain_new[v] * yh));
   }
 }
 
@@ -638,11 +713,11 @@ __constant__ int c_fwd[13][3] = {{0, 0, 1},  {0, 1, -1}, {0, 1, 0},   {0, 1, 1},
                                  {1, 0, 0},  {1, 1, 0},  {1, -1, -1}, {1, -1, 1},  {1, 0, -1},
                                  {1, 1, -1}, {1, 1, 1},  {1, 0, 1}};
 
-__global__ void prior_cost_kernel(const float* __restrict__ x, DevFilter q, int n_z, int n_x,
+template <typename Real>
+__global__ void prior_cost_kernel(const Real* __restrict__ x, DevFilter q, int n_z, int n_x,
                                   int n_y, double* __restrict__ partial) {
   const size_t total = static_cast<size_t>(n_z) * n_x * n_y;
   double acc = 0.0;
-  const double sig_p = q.sig_p, sig_pq = q.sig_pq;
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < total;
        i += static_cast<size_t>(gridDim.x) * blockDim.x) {
     const int xi = static_cast<int>(i % n_x);
@@ -656,14 +731,23 @@ __global__ void prior_cost_kernel(const float* __restrict__ x, DevFilter q, int 
       const double d = c - static_cast<double>(
                                x[(static_cast<size_t>(yy) * n_z + zz) * n_x + xx]);
       const double ad = fabs(d);
-      const double num = (q.mrf_p == 2.f) ? ad * ad : static_cast<double>(powf(ad, q.mrf_p));
-      const double den =
-          q.mrf_c + static_cast<double>(powf(static_cast<float>(ad), q.mrf_p - q.mrf_q)) / sig_pq;
+      double num, pq;
+      if constexpr (std::is_same<Real, float>::value) {
+        // FP32 elementwise power (relative error ~1e-7), FP64 accumulation
+        num = (q.mrf_p == 2.0) ? ad * ad
+                               : static_cast<double>(powf(static_cast<float>(ad),
+                                                          static_cast<float>(q.mrf_p)));
+        pq = static_cast<double>(
+            powf(static_cast<float>(ad), static_cast<float>(q.mrf_p - q.mrf_q)));
+      } else {
+        num = pow(ad, q.mrf_p);
+        pq = pow(ad, q.mrf_p - q.mrf_q);
+      }
       const int fi = 9 * (c_fwd[k][2] + 1) + 3 * (c_fwd[k][0] + 1) + (c_fwd[k][1] + 1);
-      acc += static_cast<double>(q.f[fi]) * ((num / sig_p) / den);
+      acc += q.f[fi] * ((num / q.sig_p) / (q.mrf_c + pq / q.sig_pq));
     }
   }
-  acc = warp_sum_d(acc);
+  acc = warp_sum(acc);
   __shared__ double red[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) red[warp] = acc;
@@ -692,19 +776,37 @@ inline int grid_for(size_t n, int block) {
   return static_cast<int>(g);
 }
 
-template <int NB, bool STAGE>
-int launch_sweep_t(const SweepArgs& a, int nb, size_t smem, cudaStream_t s) {
-  auto k = sweep_kernel<NB, STAGE>;
+template <typename Real, int NB, bool STAGE>
+int launch_sweep_t(const SweepArgs& a, size_t smem, cudaStream_t s) {
+  auto k = sweep_kernel<Real, NB, STAGE>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem));
   if (e != cudaSuccess) return -3;
-  k<<<nb, kWarps * 32, smem, s>>>(a);
+  k<<<a.n_slices, kWarps * 32, smem, s>>>(a);
   return ok_or(cudaGetLastError());
 }
 
-template <int NB>
+template <typename Real>
+int launch_sweep_r(const SweepArgs& a, int nb, size_t smem, cudaStream_t s) {
+  const bool st = a.smem_rows != 0;
+  switch (nb) {
+    case 3:
+      return st ? launch_sweep_t<Real, 3, true>(a, smem, s)
+                : launch_sweep_t<Real, 3, false>(a, smem, s);
+    case 5:
+      return st ? launch_sweep_t<Real, 5, true>(a, smem, s)
+                : launch_sweep_t<Real, 5, false>(a, smem, s);
+    case 9:
+      return st ? launch_sweep_t<Real, 9, true>(a, smem, s)
+                : launch_sweep_t<Real, 9, false>(a, smem, s);
+    default:
+      return -7;
+  }
+}
+
+template <typename Real, int NB>
 int launch_ref_t(const RefOrderArgs& a, size_t smem, cudaStream_t s) {
-  auto k = ref_order_kernel<NB>;
+  auto k = ref_order_kernel<Real, NB>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem));
   if (e != cudaSuccess) return -3;
@@ -712,109 +814,156 @@ int launch_ref_t(const RefOrderArgs& a, size_t smem, cudaStream_t s) {
   return ok_or(cudaGetLastError());
 }
 
+template <typename Real>
+int launch_ref_r(const RefOrderArgs& a, int nb, cudaStream_t s) {
+  const size_t smem = smem_layout(a.g.n_theta, 0, 0, a.g.bins, false, sizeof(Real)).total;
+  switch (nb) {
+    case 3:
+      return launch_ref_t<Real, 3>(a, smem, s);
+    case 5:
+      return launch_ref_t<Real, 5>(a, smem, s);
+    case 9:
+      return launch_ref_t<Real, 9>(a, smem, s);
+    default:
+      return -7;
+  }
+}
+
 }  // namespace
 
-size_t sweep_smem_bytes(int n_theta, int n_rs, int t_rows, int bins) {
-  return smem_layout(n_theta, n_rs, t_rows, bins, n_rs > 0).total;
+size_t sweep_smem_bytes(int n_theta, int n_rs, int t_rows, int bins, int fp64) {
+  return smem_layout(n_theta, n_rs, t_rows, bins, n_rs > 0, fp64 ? 8 : 4).total;
 }
 
 int launch_sweep(const SweepArgs& a, int nb, size_t smem, void* stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const bool st = a.smem_rows != 0;
-  switch (nb) {
-    case 3:
-      return st ? launch_sweep_t<3, true>(a, a.n_slices, smem, s)
-                : launch_sweep_t<3, false>(a, a.n_slices, smem, s);
-    case 5:
-      return st ? launch_sweep_t<5, true>(a, a.n_slices, smem, s)
-                : launch_sweep_t<5, false>(a, a.n_slices, smem, s);
-    case 9:
-      return st ? launch_sweep_t<9, true>(a, a.n_slices, smem, s)
-                : launch_sweep_t<9, false>(a, a.n_slices, smem, s);
-    default:
-      return -7;
-  }
+  return a.fp64 ? launch_sweep_r<double>(a, nb, smem, s) : launch_sweep_r<float>(a, nb, smem, s);
 }
 
 int launch_ref_order(const RefOrderArgs& a, int nb, void* stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const size_t smem = smem_layout(a.g.n_theta, 0, 0, a.g.bins, false).total;
-  switch (nb) {
-    case 3:
-      return launch_ref_t<3>(a, smem, s);
-    case 5:
-      return launch_ref_t<5>(a, smem, s);
-    case 9:
-      return launch_ref_t<9>(a, smem, s);
-    default:
-      return -7;
-  }
+  return a.fp64 ? launch_ref_r<double>(a, nb, s) : launch_ref_r<float>(a, nb, s);
 }
 
-int launch_sino_to_dev(const float* h, float* d, int n_theta, int n_r, int n_rp, int n_t,
+#define MBIR_DISPATCH(fp64, KERNEL, GRID, BLOCK, STREAM, ...)                             \
+  do {                                                                                    \
+    if (fp64)                                                                             \
+      KERNEL<double><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);                            \
+    else                                                                                  \
+      KERNEL<float><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);                             \
+  } while (0)
+
+template <typename Real>
+static inline Real* RP(void* p) {
+  return static_cast<Real*>(p);
+}
+template <typename Real>
+static inline const Real* RP(const void* p) {
+  return static_cast<const Real*>(p);
+}
+
+int launch_sino_to_dev(const float* h, void* d, int n_theta, int n_r, int n_rp, int n_t, int fp64,
                        void* stream) {
   const size_t n = static_cast<size_t>(n_t) * n_theta * n_rp;
-  sino_to_dev_kernel<<<grid_for(n, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      h, d, n_theta, n_r, n_rp, n_t);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (fp64)
+    sino_to_dev_kernel<double><<<grid_for(n, 256), 256, 0, s>>>(h, RP<double>(d), n_theta, n_r,
+                                                                 n_rp, n_t);
+  else
+    sino_to_dev_kernel<float><<<grid_for(n, 256), 256, 0, s>>>(h, RP<float>(d), n_theta, n_r,
+                                                                n_rp, n_t);
   return ok_or(cudaGetLastError());
 }
-int launch_sino_to_host(const float* d, float* h, int n_theta, int n_r, int n_rp, int n_t,
-                        void* stream) {
+int launch_sino_to_host(const void* d, float* h, int n_theta, int n_r, int n_rp, int n_t,
+                        int fp64, void* stream) {
   const size_t n = static_cast<size_t>(n_theta) * n_r * n_t;
-  sino_to_host_kernel<<<grid_for(n, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      d, h, n_theta, n_r, n_rp, n_t);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (fp64)
+    sino_to_host_kernel<double><<<grid_for(n, 256), 256, 0, s>>>(RP<double>(d), h, n_theta, n_r,
+                                                                  n_rp, n_t);
+  else
+    sino_to_host_kernel<float><<<grid_for(n, 256), 256, 0, s>>>(RP<float>(d), h, n_theta, n_r,
+                                                                 n_rp, n_t);
   return ok_or(cudaGetLastError());
 }
-int launch_vol_to_dev(const float* zxy, float* yzx, int n_z, int n_x, int n_y, void* stream) {
+int launch_vol_to_dev(const float* zxy, void* yzx, int n_z, int n_x, int n_y, int fp64,
+                      void* stream) {
   const size_t n = static_cast<size_t>(n_z) * n_x * n_y;
-  vol_to_dev_kernel<<<grid_for(n, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(zxy, yzx,
-                                                                                      n_z, n_x, n_y);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (fp64)
+    vol_to_dev_kernel<double><<<grid_for(n, 256), 256, 0, s>>>(zxy, RP<double>(yzx), n_z, n_x, n_y);
+  else
+    vol_to_dev_kernel<float><<<grid_for(n, 256), 256, 0, s>>>(zxy, RP<float>(yzx), n_z, n_x, n_y);
   return ok_or(cudaGetLastError());
 }
-int launch_vol_to_host(const float* yzx, float* zxy, int n_z, int n_x, int n_y, void* stream) {
+int launch_vol_to_host(const void* yzx, float* zxy, int n_z, int n_x, int n_y, int fp64,
+                       void* stream) {
   const size_t n = static_cast<size_t>(n_z) * n_x * n_y;
-  vol_to_host_kernel<<<grid_for(n, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      yzx, zxy, n_z, n_x, n_y);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (fp64)
+    vol_to_host_kernel<double><<<grid_for(n, 256), 256, 0, s>>>(RP<double>(yzx), zxy, n_z, n_x, n_y);
+  else
+    vol_to_host_kernel<float><<<grid_for(n, 256), 256, 0, s>>>(RP<float>(yzx), zxy, n_z, n_x, n_y);
   return ok_or(cudaGetLastError());
 }
-int launch_error_from_projection(const float* y, const float* yest, float* e, const double* mu,
-                                 int n_theta, int n_rp, int n_r, int n_t, void* stream) {
+int launch_error_from_projection(const void* y, const void* yest, void* e, const double* mu,
+                                 int n_theta, int n_rp, int n_r, int n_t, int fp64, void* stream) {
   const size_t n = static_cast<size_t>(n_t) * n_theta * n_rp;
-  error_from_projection_kernel<<<grid_for(n, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      y, yest, e, mu, n_theta, n_rp, n_r, n_t);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (fp64)
+    error_from_projection_kernel<double><<<grid_for(n, 256), 256, 0, s>>>(
+        RP<double>(y), RP<double>(yest), RP<double>(e), mu, n_theta, n_rp, n_r, n_t);
+  else
+    error_from_projection_kernel<float><<<grid_for(n, 256), 256, 0, s>>>(
+        RP<float>(y), RP<float>(yest), RP<float>(e), mu, n_theta, n_rp, n_r, n_t);
   return ok_or(cudaGetLastError());
 }
-int launch_view_sums(int kind, const float* y, const float* e, const double* mu,
+int launch_view_sums(int kind, const void* y, const void* e, const double* mu,
                      const double* gain, const double* wv, double* partial, double* out,
-                     int n_theta, int n_rp, int n_r, int n_t, int n_chunk, void* stream) {
+                     int n_theta, int n_rp, int n_r, int n_t, int n_chunk, int fp64,
+                     void* stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   dim3 grid(n_theta, n_chunk);
-  int K;
-  if (kind == 0) {
-    K = 6;
-    view_sums_kernel<6><<<grid, 256, 0, s>>>(y, e, mu, gain, wv, partial, n_theta, n_rp, n_r, n_t,
-                                             n_chunk);
+  const int K = kind == 0 ? 6 : 1;
+  if (fp64) {
+    if (kind == 0)
+      view_sums_kernel<double, 6><<<grid, 256, 0, s>>>(RP<double>(y), RP<double>(e), mu, gain, wv,
+                                                        partial, n_theta, n_rp, n_r, n_t, n_chunk);
+    else
+      view_sums_kernel<double, 1><<<grid, 256, 0, s>>>(RP<double>(y), RP<double>(e), mu, gain, wv,
+                                                        partial, n_theta, n_rp, n_r, n_t, n_chunk);
   } else {
-    K = 1;
-    view_sums_kernel<1><<<grid, 256, 0, s>>>(y, e, mu, gain, wv, partial, n_theta, n_rp, n_r, n_t,
-                                             n_chunk);
+    if (kind == 0)
+      view_sums_kernel<float, 6><<<grid, 256, 0, s>>>(RP<float>(y), RP<float>(e), mu, gain, wv,
+                                                       partial, n_theta, n_rp, n_r, n_t, n_chunk);
+    else
+      view_sums_kernel<float, 1><<<grid, 256, 0, s>>>(RP<float>(y), RP<float>(e), mu, gain, wv,
+                                                       partial, n_theta, n_rp, n_r, n_t, n_chunk);
   }
   const int n = n_theta * K;
   view_sums_final_kernel<<<(n + 127) / 128, 128, 0, s>>>(partial, out, n_theta, n_chunk, K);
   return ok_or(cudaGetLastError());
 }
-int launch_rebuild_error(const float* y, float* e, const double* mu_old, const double* gain_old,
+int launch_rebuild_error(const void* y, void* e, const double* mu_old, const double* gain_old,
                          const double* mu_new, const double* gain_new, int n_theta, int n_rp,
-                         int n_r, int n_t, void* stream) {
+                         int n_r, int n_t, int fp64, void* stream) {
   const size_t n = static_cast<size_t>(n_t) * n_theta * n_rp;
-  rebuild_error_kernel<<<grid_for(n, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      y, e, mu_old, gain_old, mu_new, gain_new, n_theta, n_rp, n_r, n_t);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (fp64)
+    rebuild_error_kernel<double><<<grid_for(n, 256), 256, 0, s>>>(
+        RP<double>(y), RP<double>(e), mu_old, gain_old, mu_new, gain_new, n_theta, n_rp, n_r, n_t);
+  else
+    rebuild_error_kernel<float><<<grid_for(n, 256), 256, 0, s>>>(
+        RP<float>(y), RP<float>(e), mu_old, gain_old, mu_new, gain_new, n_theta, n_rp, n_r, n_t);
   return ok_or(cudaGetLastError());
 }
-int launch_prior_cost(const float* x, const DevFilter& f, int n_z, int n_x, int n_y,
-                      double* partial, int n_blocks, void* stream) {
-  prior_cost_kernel<<<n_blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(x, f, n_z, n_x, n_y,
-                                                                            partial);
+int launch_prior_cost(const void* x, const DevFilter& f, int n_z, int n_x, int n_y,
+                      double* partial, int n_blocks, int fp64, void* stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (fp64)
+    prior_cost_kernel<double><<<n_blocks, 256, 0, s>>>(RP<double>(x), f, n_z, n_x, n_y, partial);
+  else
+    prior_cost_kernel<float><<<n_blocks, 256, 0, s>>>(RP<float>(x), f, n_z, n_x, n_y, partial);
   return ok_or(cudaGetLastError());
 }
 int launch_reduce_stats(const double* in, int n_rows, int n_cols, double* out, void* stream) {

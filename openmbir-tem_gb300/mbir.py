@@ -24,6 +24,7 @@ ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "EDEVICE", -4: "EIO", -5: "ESTATE", -6
           -7: "ENOTSUP", -999: "ECANCELLED"}
 HAADF, BF = 0, 1
 ORDER_PARALLEL, ORDER_REFERENCE = 0, 1
+FP32, FP64 = 0, 1
 
 
 class MbirParams(C.Structure):
@@ -73,6 +74,7 @@ class MbirParams(C.Structure):
         ("bf_offset", C.c_double),
         ("default_dosage", C.c_double),
         ("order_mode", C.c_int32),
+        ("precision", C.c_int32),
         ("seed", C.c_uint32),
         ("compat_double_angle", C.c_int32),
         ("cost_every_sweep", C.c_int32),

@@ -6,12 +6,13 @@
  *
  * All paths below are relative to the reference project root (Code/MBIRLib/...).
  * Arithmetic is FP64 throughout, in the reference's loop order, so that the restatement
- * reproduces the reference to rounding; it is pinned against the reference's own sources
- * (oracle/ref_harness.cpp, tests/test_oracle_pin.py).
+ * reproduces the reference to rounding.  Parity unpinned: the reference has no golden vectors
+ * for this path and cannot be built from its own sources alone (mbir_oracle.h says why).
  */
 #include "mbir_oracle.h"
 
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -490,8 +491,8 @@ int orc_init_nuisance(orc_ctx* c) {
   if (c->p.use_default_offset) {
     for (int i = 0; i < nt; i++) c->init_offset[i] = c->p.default_offset;
   } else {
-    double* avg = (double*)calloc(nt, sizeof(double));
-    double* tg = (double*)calloc(nt, sizeof(double));
+    double* avg = (double*)calloc((size_t)(nt > 0 ? nt : 1), sizeof(double));
+    double* tg = (double*)calloc((size_t)(nt > 0 ? nt : 1), sizeof(double));
     for (int th = 0; th < nt; th++) {
       double sum = 0;
       for (int r = 0; r < c->n_r; r++)
@@ -579,7 +580,8 @@ void orc_measurement_weight(orc_ctx* c) {
 }
 
 /* One voxel of UpdateYSlice::execute (HAADF_ReconstructionEngine_UpdateVoxels.cpp:265-460). */
-static void update_voxel(orc_ctx* c, int jn, int kn, int i, int outer, int inner, double* stats) {
+static void update_voxel(orc_ctx* c, int jn, int kn, int i, int outer, int inner, double* stats,
+                         double* mag) {
   double nb[27];
   unsigned char bf[27];
   memset(nb, 0, sizeof(nb));
@@ -635,7 +637,7 @@ static void update_voxel(orc_ctx* c, int jn, int kn, int i, int outer, int inner
   double nv = q_substitution(c, low, high, V, bf, nb, th1, th2);
   if (nv < 0.0) nv = 0.0; /* POSITIVITY_CONSTRAINT :394-400 */
   X3(c, jn, kn, i) = nv;
-  c->mag_map[l] += fabs(nv - V);
+  mag[l] += fabs(nv - V);
   if (c->mask[l] == 1) {
     stats[0] += fabs(nv - V);
     stats[1] += fabs(V);
@@ -714,7 +716,7 @@ void orc_icd_sweep_lines(orc_ctx* c, const int32_t* lines, int n_lines, int oute
     int l = lines[n];
     if (c->col_count[l] <= 0) continue;
     int jn = l / c->n_x, kn = l % c->n_x;
-    for (int i = 0; i < c->n_y; i++) update_voxel(c, jn, kn, i, outer, inner, stats);
+    for (int i = 0; i < c->n_y; i++) update_voxel(c, jn, kn, i, outer, inner, stats, c->mag_map);
   }
 }
 
@@ -723,6 +725,73 @@ void orc_icd_sweep_reference(orc_ctx* c, uint32_t seed, int outer, int inner, do
   int32_t* order = (int32_t*)malloc(sizeof(int32_t) * nl);
   orc_visit_order(seed, c->n_z, c->n_x, order);
   orc_icd_sweep_lines(c, order, nl, outer, inner, stats);
+  free(order);
+}
+
+/* updateVoxels with OpenMBIR_USE_PARALLEL_ALGORITHMS (_UpdateVoxels.cpp:666-723): the y range is
+ * split round-robin by count into one contiguous range per worker; every worker walks the same
+ * random line order over its own y range.  Neighbour reads across range boundaries race exactly
+ * as in the reference; the per-line update magnitudes are kept per worker and summed. */
+typedef struct {
+  orc_ctx* c;
+  const int32_t* order;
+  int n_lines, y0, y1, outer, inner;
+  double st[4];
+  double* mag;
+} orc_task;
+
+static void* orc_task_run(void* arg) {
+  orc_task* t = (orc_task*)arg;
+  orc_ctx* c = t->c;
+  for (int n = 0; n < t->n_lines; n++) {
+    int l = t->order[n];
+    if (c->col_count[l] <= 0) continue;
+    int jn = l / c->n_x, kn = l % c->n_x;
+    for (int i = t->y0; i < t->y1; i++) update_voxel(c, jn, kn, i, t->outer, t->inner, t->st, t->mag);
+  }
+  return NULL;
+}
+
+void orc_icd_sweep_reference_mt(orc_ctx* c, uint32_t seed, int outer, int inner, int n_threads,
+                                double* stats) {
+  int nl = c->n_z * c->n_x;
+  if (n_threads < 1) n_threads = 1;
+  int32_t* order = (int32_t*)malloc(sizeof(int32_t) * nl);
+  orc_visit_order(seed, c->n_z, c->n_x, order);
+  int* ycount = (int*)calloc(n_threads, sizeof(int));
+  for (int y = 0, t = 0; y < c->n_y; ++y) {
+    ycount[t]++;
+    if (++t == n_threads) t = 0;
+  }
+  orc_task* tasks = (orc_task*)calloc(n_threads, sizeof(orc_task));
+  pthread_t* th = (pthread_t*)calloc(n_threads, sizeof(pthread_t));
+  int ystart = 0, used = 0;
+  for (int t = 0; t < n_threads; t++) {
+    if (ycount[t] == 0) continue;
+    orc_task* k = &tasks[used];
+    k->c = c;
+    k->order = order;
+    k->n_lines = nl;
+    k->y0 = ystart;
+    k->y1 = ystart + ycount[t];
+    k->outer = outer;
+    k->inner = inner;
+    k->mag = (double*)calloc(nl, sizeof(double));
+    ystart = k->y1;
+    used++;
+  }
+  for (int t = 0; t < used; t++) pthread_create(&th[t], NULL, orc_task_run, &tasks[t]);
+  for (int t = 0; t < used; t++) pthread_join(th[t], NULL);
+  stats[0] = stats[1] = stats[2] = stats[3] = 0;
+  for (int l = 0; l < nl; l++) c->mag_map[l] = 0;
+  for (int t = 0; t < used; t++) {
+    for (int s = 0; s < 4; s++) stats[s] += tasks[t].st[s];
+    for (int l = 0; l < nl; l++) c->mag_map[l] += tasks[t].mag[l];
+    free(tasks[t].mag);
+  }
+  free(tasks);
+  free(th);
+  free(ycount);
   free(order);
 }
 
@@ -736,7 +805,8 @@ void orc_icd_sweep_slices(orc_ctx* c, const int32_t* row_order, int stride, int 
         int z = row_order[rr];
         for (int k = 0; k < stride; k++)
           for (int x = k; x < c->n_x; x += stride)
-            if (c->col_count[z * c->n_x + x] > 0) update_voxel(c, z, x, i, outer, inner, stats);
+            if (c->col_count[z * c->n_x + x] > 0)
+              update_voxel(c, z, x, i, outer, inner, stats, c->mag_map);
       }
 }
 

@@ -7,9 +7,14 @@
  *
  * Every function restates one piece of the reference (Code/MBIRLib/...) in plain C with
  * the reference's own FP64 arithmetic and loop order; each cites the file:line it follows.
- * Parity pin: the restatement is checked against the reference's own sources compiled
- * from where they lie (oracle/ref_harness.cpp, built by oracle/Makefile into oracle/_ref/);
- * see tests/test_oracle_pin.py.
+ *
+ * PARITY UNPINNED: the reference ships no golden vectors, known-answer tests or expected
+ * outputs for this path (its Code/Test programs print values without assertions), and its
+ * engine cannot be compiled from its own sources alone (it needs cmake-generated
+ * configuration headers, Boost and TBB), so this restatement is not checked against outputs of
+ * the reference itself.  It is checked against published known answers (MT19937), algebraic
+ * properties of the reference algorithm (tests/test_oracle.py) and two independent FP64
+ * implementations of the setup tables (this file and the engine's host code).
  */
 #ifndef MBIR_ORACLE_H_
 #define MBIR_ORACLE_H_
@@ -81,6 +86,9 @@ void orc_measurement_weight(orc_ctx* c);  /* e = y - yest - mu, w = 1/alpha */
 /* stats[0] = sum|dx| over ROI, stats[1] = sum|x_old| over ROI, stats[2] = zero-skipped count,
  * stats[3] = updated voxel count */
 void orc_icd_sweep_reference(orc_ctx* c, uint32_t seed, int outer, int inner, double* stats);
+/* the reference's multi-threaded sweep: contiguous y ranges, one per worker thread */
+void orc_icd_sweep_reference_mt(orc_ctx* c, uint32_t seed, int outer, int inner, int n_threads,
+                                double* stats);
 /* the GPU parallel order: colour c in {0,1}: slices y = c, c+2, ...; rows in row_order; within
  * a row, classes k = 0..stride-1 of x = k, k+stride, ... */
 void orc_icd_sweep_slices(orc_ctx* c, const int32_t* row_order, int stride, int outer, int inner,

@@ -39,8 +39,8 @@ _lib = None
 
 def build(force=False):
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
-        subprocess.check_call(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-o", LIB, SRC,
-                               "-lm"])
+        subprocess.check_call(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-pthread", "-o", LIB,
+                               SRC, "-lm"])
     return LIB
 
 
@@ -68,6 +68,8 @@ def lib():
             "orc_forward_project": (None, [C.c_void_p]),
             "orc_measurement_weight": (None, [C.c_void_p]),
             "orc_icd_sweep_reference": (None, [C.c_void_p, C.c_uint32, C.c_int, C.c_int, _D]),
+            "orc_icd_sweep_reference_mt": (None, [C.c_void_p, C.c_uint32, C.c_int, C.c_int, C.c_int,
+                                                   _D]),
             "orc_icd_sweep_slices": (None, [C.c_void_p, _I, C.c_int, C.c_int, C.c_int, _D]),
             "orc_icd_sweep_lines": (None, [C.c_void_p, _I, C.c_int, C.c_int, C.c_int, _D]),
             "orc_joint_estimation": (C.c_int, [C.c_void_p]),
@@ -215,6 +217,12 @@ class Oracle:
     def sweep_reference(self, seed, outer=0, inner=0):
         st = np.zeros(4)
         lib().orc_icd_sweep_reference(self._h, seed, outer, inner, st.ctypes.data_as(_D))
+        return st
+
+    def sweep_reference_mt(self, seed, outer=0, inner=0, threads=None):
+        st = np.zeros(4)
+        n = threads or os.cpu_count() or 1
+        lib().orc_icd_sweep_reference_mt(self._h, seed, outer, inner, n, st.ctypes.data_as(_D))
         return st
 
     def sweep_slices(self, row_order, stride, outer=0, inner=0):
