@@ -107,6 +107,7 @@ void Engine::release() {
   dfree(d_tcount_);
   dfree(d_hval_);
   dfree(d_rows_);
+  dfree(d_lineok_);
   dfree(d_lines_);
   dfree(d_stats_);
   dfree(d_stat4_);
@@ -477,9 +478,9 @@ int Engine::alloc_device() {
   n_rs_ = (n_rp_ % 32 == 0) ? n_rp_ + 4 : n_rp_;
   int max_smem = 0;
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, p_.device);
-  smem_bytes_ = sweep_smem_bytes(g.n_theta, n_rs_, t_rows_, bins_, fp64_);
+  smem_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, n_rs_, t_rows_, bins_, fp64_);
   stage_ = smem_bytes_ <= static_cast<size_t>(max_smem);
-  if (!stage_) smem_bytes_ = sweep_smem_bytes(g.n_theta, 0, t_rows_, bins_, fp64_);
+  if (!stage_) smem_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, 0, t_rows_, bins_, fp64_);
   const size_t ns = static_cast<size_t>(g.n_t) * g.n_theta * n_rp_;
   const size_t nh = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;
   const size_t nv = static_cast<size_t>(g.n_z) * g.n_x * g.n_y;
@@ -499,6 +500,7 @@ int Engine::alloc_device() {
   rc |= dmalloc(&d_tcount_, g.n_y);
   rc |= dmalloc_bytes(&d_hval_, static_cast<size_t>(g.n_y) * kMaxTRows * rb_);
   rc |= dmalloc(&d_rows_, g.n_z);
+  rc |= dmalloc(&d_lineok_, static_cast<size_t>(g.n_z) * g.n_x);
   rc |= dmalloc(&d_lines_, static_cast<size_t>(g.n_z) * g.n_x);
   rc |= dmalloc(&d_stats_, static_cast<size_t>((g.n_y + 1) / 2 + 1) * kStatSlots * 2);
   rc |= dmalloc(&d_stat4_, kStatSlots);
@@ -622,6 +624,8 @@ int Engine::prepare() {
   cudaMemcpyAsync(d_bz_, bz.data(), sizeof(double) * bz.size(), cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(d_tfirst_, tab_.t_first.data(), sizeof(int) * g.n_y, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(d_tcount_, tab_.t_count.data(), sizeof(int) * g.n_y, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(d_lineok_, tab_.line_nonempty.data(), tab_.line_nonempty.size(),
+                  cudaMemcpyHostToDevice, s);
 
   // measured sinogram -> [t][theta][r_pad]
   const size_t nh = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;
@@ -704,7 +708,7 @@ int Engine::forward_project() {
   cudaMemcpyAsync(d_rows_, rows.data(), sizeof(int) * g.n_z, cudaMemcpyHostToDevice, s);
   SweepArgs a{};
   a.g = dg_;
-  a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_};
+  a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_, d_lineok_};
   a.flt = flt_;
   a.x = d_x_;
   a.e = d_yest_;
@@ -755,7 +759,7 @@ int Engine::sweep(int outer, int inner, double* stats4) {
     cudaMemcpyAsync(d_lines_, lines.data(), sizeof(int32_t) * lines.size(), cudaMemcpyHostToDevice, s);
     RefOrderArgs a{};
     a.g = dg_;
-    a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_};
+    a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_, d_lineok_};
     a.flt = flt_;
     a.x = d_x_;
     a.e = d_e_;
@@ -772,7 +776,7 @@ int Engine::sweep(int outer, int inner, double* stats4) {
     cudaMemcpyAsync(d_rows_, rows.data(), sizeof(int) * g.n_z, cudaMemcpyHostToDevice, s);
     SweepArgs a{};
     a.g = dg_;
-    a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_};
+    a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_, d_lineok_};
     a.flt = flt_;
     a.x = d_x_;
     a.e = d_e_;

@@ -144,6 +144,7 @@ class Engine {
   int* d_tcount_ = nullptr;
   void* d_hval_ = nullptr;    // Real [n_y][kMaxTRows]
   int* d_rows_ = nullptr;
+  uint8_t* d_lineok_ = nullptr;
   int* d_lines_ = nullptr;
   double* d_stats_ = nullptr;   // [max slices][4]
   double* d_stat4_ = nullptr;   // [4]

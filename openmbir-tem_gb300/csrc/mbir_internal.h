@@ -39,6 +39,7 @@ struct DevTables {
   const int* t_first;    // [n_y]
   const int* t_count;    // [n_y]
   const void* hval;      // Real [n_y][kMaxTRows]
+  const uint8_t* lineok; // [n_z][n_x] 1 when the voxel line's A-column is not empty
 };
 
 struct DevFilter {
@@ -86,7 +87,12 @@ struct RefOrderArgs {
 // launchers (mbir_kernels.cu); fp64 selects Real = double for the void* arrays
 int launch_sweep(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_ref_order(const RefOrderArgs& a, int nb, void* stream);
-size_t sweep_smem_bytes(int n_theta, int n_rs, int t_rows, int bins, int fp64);
+size_t sweep_smem_bytes(int n_theta, int n_x, int n_rs, int t_rows, int bins, int fp64);
+int launch_sweep_f32_smem(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
+int launch_sweep_f32_hbm(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
+int launch_sweep_f64(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
+int launch_ref_order_f32(const RefOrderArgs& a, int nb, void* stream);
+int launch_ref_order_f64(const RefOrderArgs& a, int nb, void* stream);
 int launch_sino_to_dev(const float* host_layout, void* dev_layout, int n_theta, int n_r, int n_rp,
                        int n_t, int fp64, void* stream);
 int launch_sino_to_host(const void* dev_layout, float* host_layout, int n_theta, int n_r,

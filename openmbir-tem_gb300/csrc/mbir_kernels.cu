@@ -1,17 +1,7 @@
 // mbir_kernels.cu -- sm_103a kernels of the MBIR hot path.
 //
-//   sweep_kernel      ICD sweep (and forward projection) over the voxel slices of one y-colour.
-//                     One CTA owns one voxel slice y: the detector rows t of that slice (all
-//                     views, all r) are staged into shared memory with TMA bulk copies and stay
-//                     there for the whole sweep, so every theta1/theta2 gather and every
-//                     error-sinogram scatter is an on-chip access.  Inside the slice, warps
-//                     update voxels of one z-row whose A-columns do not overlap (x stride S),
-//                     so the result is the sequential ICD of a fixed visit order.  Each warp
-//                     builds its voxel's A-column on the fly (lanes over views), reduces
-//                     theta1/theta2 with warp shuffles and solves the QGGMRF surrogate with one
-//                     neighbour per lane.
-//   ref_order_kernel  the reference's visit order (one voxel line after another, y in order)
-//                     with the error sinogram in HBM; one warp, used for order-exact parity.
+// The ICD sweep / projection kernels live in mbir_sweep.cuh (instantiated by
+// mbir_sweep_f32.cu, mbir_sweep_f32_hbm.cu and mbir_sweep_f64.cu).  This file holds the rest:
 //   view_sums_kernel  FP64 per-view reductions for gain/offset and variance estimation.
 //   prior_cost_kernel FP64 accumulation of the QGGMRF prior term of the MAP cost.
 // Every kernel is instantiated for Real = float (production) and Real = double (the
@@ -123,437 +113,6 @@ __device__ __forceinline__ T warp_max(T v) {
     v = w > v ? w : v;
   }
   return v;
-}
-
-// Detector coordinate of a voxel row at one view.  FP32: integer + fraction so that the
-// per-voxel position keeps ~1e-7 bin accuracy; FP64: the coordinate itself.
-struct RowBaseF {
-  int ib;
-  float fb;
-};
-struct RowBaseD {
-  double base;
-};
-template <typename Real>
-using RowBase = typename std::conditional<std::is_same<Real, float>::value, RowBaseF,
-                                          RowBaseD>::type;
-
-// u = j0 + f (f in [0,1)) for voxel column x: u = base(z) + x * bx with bx given as hi+lo.
-__device__ __forceinline__ void detector_pos(int x, RowBaseF rb, float2 bx, double, int& j0,
-                                             float& f) {
-  const float xf = static_cast<float>(x);
-  const float p = xf * bx.x;
-  const float pe = fmaf(xf, bx.x, -p);  // exact rounding error of x*bx.hi
-  const float jp = floorf(p);
-  float ff = (p - jp) + rb.fb + (pe + xf * bx.y);
-  const float jf = floorf(ff);
-  ff -= jf;
-  j0 = rb.ib + static_cast<int>(jp) + static_cast<int>(jf);
-  f = ff;
-}
-__device__ __forceinline__ void detector_pos(int x, RowBaseD rb, float2, double bxd, int& j0,
-                                             double& f) {
-  const double u = fma(static_cast<double>(x), bxd, rb.base);
-  const double fl = floor(u);
-  j0 = static_cast<int>(fl);
-  f = u - fl;
-}
-
-template <typename Real>
-__device__ __forceinline__ void compute_row_base(const DevTables& tab, int n_theta, int z,
-                                                 RowBase<Real>* rb, int tid, int nthreads) {
-  for (int v = tid; v < n_theta; v += nthreads) {
-    const double b = tab.u0[v] - static_cast<double>(z) * tab.bz[v];
-    if constexpr (std::is_same<Real, float>::value) {
-      const double fl = floor(b);
-      rb[v].ib = static_cast<int>(fl);
-      rb[v].fb = static_cast<float>(b - fl);
-    } else {
-      rb[v].base = b;
-    }
-  }
-}
-
-// A-matrix entries of one voxel at one view (AMatrixCol.cpp:148-232): bins j in
-// [floor(u-d), floor(u+d)] on the detector, value = linear interpolation of the detector
-// response at |u - (j+0.5)|, kept when > 0.
-template <typename Real, int NB>
-__device__ __forceinline__ void view_footprint(const DevGeom& g, const Real* __restrict__ hrow,
-                                               int j0, Real f, int& jlo, Real (&a)[NB]) {
-  const Real hw = static_cast<Real>(g.half_width);
-  const Real kr = static_cast<Real>(g.kr);
-  const int lo = j0 + static_cast<int>(floor(f - hw));
-  const int hi = j0 + static_cast<int>(floor(f + hw));
-  jlo = lo;
-#pragma unroll
-  for (int b = 0; b < NB; ++b) {
-    const int j = lo + b;
-    Real v = Real(0);
-    if (j <= hi && j >= 0 && j < g.n_r) {
-      const Real delta = fabs(static_cast<Real>(j0 - j) + f - Real(0.5));
-      const Real xr = delta * kr;
-      const int idx = static_cast<int>(xr);
-      if (idx < g.bins) {
-        const Real t = xr - static_cast<Real>(idx);
-        v = (Real(1) - t) * hrow[idx] + t * hrow[idx + 1];
-      }
-    }
-    a[b] = v > Real(0) ? v : Real(0);
-  }
-}
-
-// rho'(d)/d of the QGGMRF prior (QGGMRF_Functions.cpp:90-104 divided by d), or rho''(0)
-// (:109-112) when d == 0.
-template <typename Real>
-__device__ __forceinline__ Real qggmrf_coef(const DevFilter& q, Real d0) {
-  const Real P = static_cast<Real>(q.mrf_p), Q = static_cast<Real>(q.mrf_q);
-  const Real c = static_cast<Real>(q.mrf_c), sp = static_cast<Real>(q.sig_p);
-  if (d0 == Real(0)) return P / (sp * c);
-  const Real ad = fabs(d0);
-  const Real t1 = pow(ad, P - Q) / static_cast<Real>(q.sig_pq);
-  const Real t3 = c + t1;
-  Real r = (P - ((P - Q) * t1) / t3) / (t3 * sp);
-  if (P != Real(2)) r *= pow(ad, P - Real(2));
-  return r;
-}
-
-// One voxel (z, x, y) processed by one warp.  es points at the first detector row of slice y
-// (row stride rs values between views, plane stride ps between t rows).  Returns in wst
-// (lane 0): ROI sum|dx|, ROI sum|x|, zero-skipped, updated.
-template <typename Real, int NB>
-__device__ __forceinline__ void voxel_step(const DevGeom& g, const DevFilter& q,
-                                           Real* __restrict__ vol, Real* es, int rs, int ps,
-                                           const RowBase<Real>* rb, const Real* sH,
-                                           const float2* sbx, const double* sbxd,
-                                           const typename V2<Real>::type* sgw, int z, int x,
-                                           int y, int tcount, const Real* hv, int mode,
-                                           int iter_nonzero, int zero_skipping, int lane,
-                                           double* wst) {
-  using R2 = typename V2<Real>::type;
-  const size_t plane = static_cast<size_t>(g.n_z) * g.n_x;
-  const size_t vidx = static_cast<size_t>(y) * plane + static_cast<size_t>(z) * g.n_x + x;
-  const Real V = vol[vidx];
-  const Real hw = static_cast<Real>(g.half_width);
-
-  int jlo[kMaxViewsPerLane];
-  Real a[kMaxViewsPerLane][NB];
-  bool any = false;
-#pragma unroll
-  for (int i = 0; i < kMaxViewsPerLane; ++i) {
-    const int v = lane + 32 * i;
-    jlo[i] = 0;
-#pragma unroll
-    for (int b = 0; b < NB; ++b) a[i][b] = Real(0);
-    if (v < g.n_theta) {
-      int j0;
-      Real f;
-      detector_pos(x, rb[v], sbx ? sbx[v] : float2{0.f, 0.f}, sbxd ? sbxd[v] : 0.0, j0, f);
-      const Real u = static_cast<Real>(j0) + f;
-      if (!(u + hw < Real(0) || u - hw > static_cast<Real>(g.n_r))) {
-        view_footprint<Real, NB>(g, sH + v * (g.bins + 1), j0, f, jlo[i], a[i]);
-#pragma unroll
-        for (int b = 0; b < NB; ++b) any |= (a[i][b] > Real(0));
-      }
-    }
-  }
-  if (!__any_sync(kFull, any)) return;  // empty A-column: the line is never visited
-
-  if (mode == kModeProject) {
-    if (V != Real(0)) {
-#pragma unroll
-      for (int i = 0; i < kMaxViewsPerLane; ++i) {
-        const int v = lane + 32 * i;
-        if (v >= g.n_theta) continue;
-        const Real gain = sgw[v].x;
-        for (int tr = 0; tr < tcount; ++tr) {
-          const Real hh = hv[tr];
-          Real* row = es + tr * ps + v * rs + jlo[i];
-#pragma unroll
-          for (int b = 0; b < NB; ++b)
-            if (a[i][b] > Real(0)) row[b] += gain * (a[i][b] * hh * V);
-        }
-      }
-    }
-    return;
-  }
-
-  // 26-neighbourhood, one neighbour per lane (UpdateVoxels.cpp:283-306)
-  Real nb = Real(0);
-  bool nvalid = false;
-  if (lane < 27) {
-    const int dy = lane / 9 - 1, dz = (lane / 3) % 3 - 1, dx = lane % 3 - 1;
-    const int yy = y + dy, zz = z + dz, xx = x + dx;
-    if (lane != 13 && yy >= 0 && yy < g.n_y && zz >= 0 && zz < g.n_z && xx >= 0 && xx < g.n_x) {
-      nb = vol[static_cast<size_t>(yy) * plane + static_cast<size_t>(zz) * g.n_x + xx];
-      nvalid = true;
-    }
-  }
-  // zero skipping (UpdateVoxels.cpp:310-338)
-  if (zero_skipping && iter_nonzero && V == Real(0)) {
-    if (!__any_sync(kFull, nb > Real(0))) {
-      if (lane == 0) wst[2] += 1.0;
-      return;
-    }
-  }
-  // theta1 / theta2 (UpdateVoxels.cpp:343-369)
-  Real t1 = Real(0), t2 = Real(0);
-#pragma unroll
-  for (int i = 0; i < kMaxViewsPerLane; ++i) {
-    const int v = lane + 32 * i;
-    if (v >= g.n_theta) continue;
-    const R2 gw = sgw[v];
-    for (int tr = 0; tr < tcount; ++tr) {
-      const Real hh = hv[tr];
-      const Real* row = es + tr * ps + v * rs + jlo[i];
-#pragma unroll
-      for (int b = 0; b < NB; ++b) {
-        if (a[i][b] > Real(0)) {
-          const Real pe = gw.x * a[i][b] * hh;
-          t2 += pe * pe * gw.y;
-          t1 += row[b] * pe * gw.y;
-        }
-      }
-    }
-  }
-  const Real theta1 = -warp_sum(t1);
-  const Real theta2 = warp_sum(t2);
-  // bracket (find_min_max, UpdateVoxels.cpp:47-63): over all 27 entries, centre and
-  // out-of-range entries count as 0
-  Real lo = warp_min(nb), hi = warp_max(nb);
-  if (theta2 != Real(0)) {
-    const Real cand = V - theta1 / theta2;
-    lo = lo > cand ? cand : lo;
-    hi = hi < cand ? cand : hi;
-  }
-  // QGGMRF surrogate, one iteration (QGGMRF_Functions.cpp:153-206)
-  Real s1 = Real(0), s2 = Real(0);
-  if (nvalid) {
-    const Real tc = static_cast<Real>(q.f[lane]) * qggmrf_coef<Real>(q, V - nb);
-    s1 = tc * nb;
-    s2 = tc;
-  }
-  s1 = warp_sum(s1);
-  s2 = warp_sum(s2);
-  const Real u = (s1 + theta2 * V - theta1) / (s2 + theta2);
-  Real nv = V + static_cast<Real>(q.mrf_alpha) * (u - V);
-  nv = (nv < lo) ? lo : ((nv > hi) ? hi : nv);
-  if (nv < Real(0)) nv = Real(0);  // positivity (UpdateVoxels.cpp:394-400)
-  const Real dlt = nv - V;
-  // error-sinogram scatter (UpdateVoxels.cpp:423-449)
-  if (dlt != Real(0)) {
-#pragma unroll
-    for (int i = 0; i < kMaxViewsPerLane; ++i) {
-      const int v = lane + 32 * i;
-      if (v >= g.n_theta) continue;
-      const Real gain = sgw[v].x;
-      for (int tr = 0; tr < tcount; ++tr) {
-        const Real hh = hv[tr];
-        Real* row = es + tr * ps + v * rs + jlo[i];
-#pragma unroll
-        for (int b = 0; b < NB; ++b)
-          if (a[i][b] > Real(0)) row[b] -= gain * (a[i][b] * hh * dlt);
-      }
-    }
-  }
-  if (lane == 0) {
-    vol[vidx] = nv;
-    if (x >= g.roi_x0 && x <= g.roi_x1 && z >= g.roi_z0 && z <= g.roi_z1) {
-      wst[0] += fabs(static_cast<double>(dlt));
-      wst[1] += fabs(static_cast<double>(V));
-    }
-    wst[3] += 1.0;
-  }
-}
-
-struct SmemLayout {
-  size_t bar, stats, rb, bx, bxd, gw, H, hv, es, total;
-};
-
-__host__ __device__ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
-
-__host__ __device__ inline SmemLayout smem_layout(int n_theta, int n_rs, int t_rows, int bins,
-                                                  bool stage, size_t real_bytes) {
-  SmemLayout L;
-  size_t o = 0;
-  L.bar = o;
-  o += 16;
-  L.stats = o;
-  o += sizeof(double) * kWarps * kStatSlots;
-  L.rb = o;
-  o = align_up(o + 8 * static_cast<size_t>(n_theta), 16);
-  L.bx = o;
-  o = align_up(o + sizeof(float2) * n_theta, 16);
-  L.bxd = o;
-  o = align_up(o + sizeof(double) * n_theta, 16);
-  L.gw = o;
-  o = align_up(o + 2 * real_bytes * n_theta, 16);
-  L.H = o;
-  o = align_up(o + real_bytes * n_theta * (bins + 1), 16);
-  L.hv = o;
-  o = align_up(o + real_bytes * kMaxTRows, 128);
-  L.es = o;
-  if (stage) o += real_bytes * static_cast<size_t>(t_rows) * n_theta * n_rs;
-  L.total = align_up(o, 16);
-  return L;
-}
-
-template <typename Real, int NB, bool STAGE>
-__global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
-  using R2 = typename V2<Real>::type;
-  extern __shared__ __align__(128) unsigned char smem[];
-  const DevGeom& g = A.g;
-  const int y = A.colour + 2 * static_cast<int>(blockIdx.x);
-  if (y >= g.n_y) return;
-  const int tid = threadIdx.x, nthreads = blockDim.x;
-  const int warp = tid >> 5, lane = tid & 31;
-  const int tcount = A.tab.t_count[y], tfirst = A.tab.t_first[y];
-  const SmemLayout L = smem_layout(g.n_theta, A.n_rs, tcount, g.bins, STAGE, sizeof(Real));
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L.bar);
-  double* sstat = reinterpret_cast<double*>(smem + L.stats);
-  RowBase<Real>* rb = reinterpret_cast<RowBase<Real>*>(smem + L.rb);
-  float2* sbx = reinterpret_cast<float2*>(smem + L.bx);
-  double* sbxd = reinterpret_cast<double*>(smem + L.bxd);
-  R2* sgw = reinterpret_cast<R2*>(smem + L.gw);
-  Real* sH = reinterpret_cast<Real*>(smem + L.H);
-  Real* shv = reinterpret_cast<Real*>(smem + L.hv);
-  const Real* gH = static_cast<const Real*>(A.tab.H);
-  const R2* ggw = static_cast<const R2*>(A.tab.gw);
-  const Real* ghv = static_cast<const Real*>(A.tab.hval);
-  Real* const ge = static_cast<Real*>(A.e);
-  Real* const gx = static_cast<Real*>(A.x);
-  constexpr bool kF32 = std::is_same<Real, float>::value;
-
-  for (int i = tid; i < g.n_theta * (g.bins + 1); i += nthreads) sH[i] = gH[i];
-  for (int v = tid; v < g.n_theta; v += nthreads) {
-    if (kF32) sbx[v] = A.tab.bx[v];
-    else sbxd[v] = A.tab.bxd[v];
-    sgw[v] = ggw[v];
-  }
-  if (tid < kMaxTRows) shv[tid] = ghv[y * kMaxTRows + tid];
-
-  const size_t sino_plane = static_cast<size_t>(g.n_theta) * g.n_rp;
-  Real* es;
-  int rs, ps;
-  const int rows = tcount * g.n_theta;
-  const uint32_t row_bytes = static_cast<uint32_t>(g.n_rp * sizeof(Real));
-  if (STAGE) {
-    es = reinterpret_cast<Real*>(smem + L.es);
-    rs = A.n_rs;
-    ps = g.n_theta * A.n_rs;
-    if (A.mode == kModeProject) {
-      for (int i = tid; i < tcount * ps; i += nthreads) es[i] = Real(0);
-      __syncthreads();
-    } else {
-      if (tid == 0) {
-        mbar_init(bar, 1);
-        fence_mbar_init();
-      }
-      __syncthreads();
-      if (tid == 0) mbar_expect_tx(bar, static_cast<uint32_t>(rows) * row_bytes);
-      __syncthreads();
-      for (int r = tid; r < rows; r += nthreads) {
-        const int tr = r / g.n_theta, v = r % g.n_theta;
-        bulk_g2s(es + tr * ps + v * rs,
-                 ge + (static_cast<size_t>(tfirst + tr)) * sino_plane +
-                     static_cast<size_t>(v) * g.n_rp,
-                 row_bytes, bar);
-      }
-      const bool ok = mbar_wait(bar, 0);
-      if (!__syncthreads_and(ok)) {
-        if (tid == 0) atomicOr(A.err, 1);
-        mbar_wait(bar, 0);  // give copies still in flight a second bounded chance to land
-        return;
-      }
-    }
-  } else {
-    es = ge + static_cast<size_t>(tfirst) * sino_plane;
-    rs = g.n_rp;
-    ps = static_cast<int>(sino_plane);
-  }
-
-  double wst[kStatSlots] = {0.0, 0.0, 0.0, 0.0};
-  for (int rr = 0; rr < g.n_z; ++rr) {
-    const int z = A.row_order[rr];
-    __syncthreads();
-    compute_row_base<Real>(A.tab, g.n_theta, z, rb, tid, nthreads);
-    __syncthreads();
-    for (int k = 0; k < A.stride; ++k) {
-      for (int x = k + A.stride * warp; x < g.n_x; x += A.stride * kWarps)
-        voxel_step<Real, NB>(g, A.flt, gx, es, rs, ps, rb, sH, kF32 ? sbx : nullptr,
-                             kF32 ? nullptr : sbxd, sgw, z, x, y, tcount, shv, A.mode,
-                             A.iter_nonzero, A.zero_skipping, lane, wst);
-      __syncthreads();
-    }
-  }
-
-  if (STAGE) {
-    fence_proxy_async_smem();
-    __syncthreads();
-    for (int r = tid; r < rows; r += nthreads) {
-      const int tr = r / g.n_theta, v = r % g.n_theta;
-      bulk_s2g(ge + (static_cast<size_t>(tfirst + tr)) * sino_plane +
-                   static_cast<size_t>(v) * g.n_rp,
-               es + tr * ps + v * rs, row_bytes);
-    }
-    bulk_commit();
-    bulk_wait_all();
-  }
-  if (A.stats != nullptr) {
-    if (lane == 0)
-      for (int s = 0; s < kStatSlots; ++s) sstat[warp * kStatSlots + s] = wst[s];
-    __syncthreads();
-    if (tid < kStatSlots) {
-      double acc = 0.0;
-      for (int w = 0; w < nthreads / 32; ++w) acc += sstat[w * kStatSlots + tid];
-      A.stats[static_cast<size_t>(blockIdx.x) * kStatSlots + tid] = acc;
-    }
-  }
-}
-
-template <typename Real, int NB>
-__global__ void __launch_bounds__(32, 1) ref_order_kernel(RefOrderArgs A) {
-  using R2 = typename V2<Real>::type;
-  extern __shared__ __align__(128) unsigned char smem[];
-  const DevGeom& g = A.g;
-  const int lane = threadIdx.x;
-  const SmemLayout L = smem_layout(g.n_theta, 0, 0, g.bins, false, sizeof(Real));
-  RowBase<Real>* rb = reinterpret_cast<RowBase<Real>*>(smem + L.rb);
-  float2* sbx = reinterpret_cast<float2*>(smem + L.bx);
-  double* sbxd = reinterpret_cast<double*>(smem + L.bxd);
-  R2* sgw = reinterpret_cast<R2*>(smem + L.gw);
-  Real* sH = reinterpret_cast<Real*>(smem + L.H);
-  const Real* gH = static_cast<const Real*>(A.tab.H);
-  const R2* ggw = static_cast<const R2*>(A.tab.gw);
-  const Real* ghv = static_cast<const Real*>(A.tab.hval);
-  Real* const ge = static_cast<Real*>(A.e);
-  Real* const gx = static_cast<Real*>(A.x);
-  constexpr bool kF32 = std::is_same<Real, float>::value;
-  for (int i = lane; i < g.n_theta * (g.bins + 1); i += 32) sH[i] = gH[i];
-  for (int v = lane; v < g.n_theta; v += 32) {
-    if (kF32) sbx[v] = A.tab.bx[v];
-    else sbxd[v] = A.tab.bxd[v];
-    sgw[v] = ggw[v];
-  }
-  __syncwarp();
-  const size_t sino_plane = static_cast<size_t>(g.n_theta) * g.n_rp;
-  double wst[kStatSlots] = {0.0, 0.0, 0.0, 0.0};
-  for (int n = 0; n < A.n_lines; ++n) {
-    const int l = A.lines[n];
-    const int z = l / g.n_x, x = l % g.n_x;
-    __syncwarp();
-    compute_row_base<Real>(A.tab, g.n_theta, z, rb, lane, 32);
-    __syncwarp();
-    for (int y = 0; y < g.n_y; ++y) {
-      Real* es = ge + static_cast<size_t>(A.tab.t_first[y]) * sino_plane;
-      voxel_step<Real, NB>(g, A.flt, gx, es, g.n_rp, static_cast<int>(sino_plane), rb, sH,
-                           kF32 ? sbx : nullptr, kF32 ? nullptr : sbxd, sgw, z, x, y,
-                           A.tab.t_count[y], ghv + y * kMaxTRows, kModeICD, A.iter_nonzero,
-                           A.zero_skipping, lane, wst);
-      __syncwarp();
-    }
-  }
-  if (lane == 0)
-    for (int s = 0; s < kStatSlots; ++s) A.stats[s] = wst[s];
 }
 
 // ---- layout conversions ----------------------------------------------------------------
@@ -776,82 +335,17 @@ inline int grid_for(size_t n, int block) {
   return static_cast<int>(g);
 }
 
-template <typename Real, int NB, bool STAGE>
-int launch_sweep_t(const SweepArgs& a, size_t smem, cudaStream_t s) {
-  auto k = sweep_kernel<Real, NB, STAGE>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(smem));
-  if (e != cudaSuccess) return -3;
-  k<<<a.n_slices, kWarps * 32, smem, s>>>(a);
-  return ok_or(cudaGetLastError());
-}
-
-template <typename Real>
-int launch_sweep_r(const SweepArgs& a, int nb, size_t smem, cudaStream_t s) {
-  const bool st = a.smem_rows != 0;
-  switch (nb) {
-    case 3:
-      return st ? launch_sweep_t<Real, 3, true>(a, smem, s)
-                : launch_sweep_t<Real, 3, false>(a, smem, s);
-    case 5:
-      return st ? launch_sweep_t<Real, 5, true>(a, smem, s)
-                : launch_sweep_t<Real, 5, false>(a, smem, s);
-    case 9:
-      return st ? launch_sweep_t<Real, 9, true>(a, smem, s)
-                : launch_sweep_t<Real, 9, false>(a, smem, s);
-    default:
-      return -7;
-  }
-}
-
-template <typename Real, int NB>
-int launch_ref_t(const RefOrderArgs& a, size_t smem, cudaStream_t s) {
-  auto k = ref_order_kernel<Real, NB>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(smem));
-  if (e != cudaSuccess) return -3;
-  k<<<1, 32, smem, s>>>(a);
-  return ok_or(cudaGetLastError());
-}
-
-template <typename Real>
-int launch_ref_r(const RefOrderArgs& a, int nb, cudaStream_t s) {
-  const size_t smem = smem_layout(a.g.n_theta, 0, 0, a.g.bins, false, sizeof(Real)).total;
-  switch (nb) {
-    case 3:
-      return launch_ref_t<Real, 3>(a, smem, s);
-    case 5:
-      return launch_ref_t<Real, 5>(a, smem, s);
-    case 9:
-      return launch_ref_t<Real, 9>(a, smem, s);
-    default:
-      return -7;
-  }
-}
-
 }  // namespace
 
-size_t sweep_smem_bytes(int n_theta, int n_rs, int t_rows, int bins, int fp64) {
-  return smem_layout(n_theta, n_rs, t_rows, bins, n_rs > 0, fp64 ? 8 : 4).total;
-}
-
 int launch_sweep(const SweepArgs& a, int nb, size_t smem, void* stream) {
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  return a.fp64 ? launch_sweep_r<double>(a, nb, smem, s) : launch_sweep_r<float>(a, nb, smem, s);
+  if (a.fp64) return launch_sweep_f64(a, nb, smem, stream);
+  return a.smem_rows ? launch_sweep_f32_smem(a, nb, smem, stream)
+                     : launch_sweep_f32_hbm(a, nb, smem, stream);
 }
 
 int launch_ref_order(const RefOrderArgs& a, int nb, void* stream) {
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  return a.fp64 ? launch_ref_r<double>(a, nb, s) : launch_ref_r<float>(a, nb, s);
+  return a.fp64 ? launch_ref_order_f64(a, nb, stream) : launch_ref_order_f32(a, nb, stream);
 }
-
-#define MBIR_DISPATCH(fp64, KERNEL, GRID, BLOCK, STREAM, ...)                             \
-  do {                                                                                    \
-    if (fp64)                                                                             \
-      KERNEL<double><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);                            \
-    else                                                                                  \
-      KERNEL<float><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);                             \
-  } while (0)
 
 template <typename Real>
 static inline Real* RP(void* p) {

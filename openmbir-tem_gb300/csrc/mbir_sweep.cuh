@@ -1,0 +1,697 @@
+// mbir_sweep.cuh -- the ICD sweep / forward-projection kernels (device code, templated on the
+// real type).  Included by mbir_sweep_f32.cu and mbir_sweep_f64.cu, which instantiate them.
+//
+//   sweep_kernel      ICD sweep (and forward projection) over the voxel slices of one y-colour.
+//                     One CTA owns one voxel slice y: the detector rows t of that slice (all
+//                     views, all r) are staged into shared memory with TMA bulk copies and stay
+//                     there for the whole sweep, so every theta1/theta2 gather and every
+//                     error-sinogram scatter is an on-chip access.  Inside the slice the CTA
+//                     walks the z-rows; for each row it caches the 9 neighbouring voxel rows
+//                     (y-1..y+1, z-1..z+1) in shared memory and updates the voxels of one
+//                     conflict-free class (x = k, k+S, ...: no two share a detector bin at any
+//                     view, none are prior neighbours) in parallel, one voxel per group of G
+//                     lanes.  The result equals the sequential ICD of that visit order.
+//   ref_order_kernel  the reference's visit order (one voxel line after another, y in order)
+//                     with the error sinogram in HBM; one warp, used for order-exact parity.
+//
+// Reference semantics: UpdateYSlice::execute (Code/MBIRLib/HAADF/
+// HAADF_ReconstructionEngine_UpdateVoxels.cpp:149-484), the A-column of
+// Code/MBIRLib/Common/AMatrixCol.cpp:82-239 and the QGGMRF surrogate of
+// Code/MBIRLib/Reconstruction/QGGMRF_Functions.cpp:82-206.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <type_traits>
+
+#include "mbir_internal.h"
+
+namespace mbir {
+namespace sweep {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr uint32_t kWaitLimit = 1u << 24;  // bounded mbarrier polls before giving up
+
+template <typename Real>
+struct V2;
+template <>
+struct V2<float> {
+  using type = float2;
+};
+template <>
+struct V2<double> {
+  using type = double2;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// ---- TMA bulk-copy helpers (cp.async.bulk + mbarrier) ------------------------------------
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Waits for the mbarrier phase; gives up after kWaitNs of wall time (or kWaitLimit polls).
+constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
+  const uint32_t a = smem_u32(bar);
+  const uint64_t t0 = global_ns();
+  for (uint32_t i = 0; i < kWaitLimit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(phase)
+        : "memory");
+    if (done) return true;
+    if ((i & 255u) == 255u && global_ns() - t0 > kWaitNs) return false;
+  }
+  return false;
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_s2g(void* dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
+               "r"(smem_u32(src)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+// ---- reductions within aligned groups of G lanes (all 32 lanes take part) -----------------
+template <int G, typename T>
+__device__ __forceinline__ T group_sum(T v) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+template <int G, typename T>
+__device__ __forceinline__ T group_min(T v) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    const T w = __shfl_xor_sync(kFull, v, o);
+    v = w < v ? w : v;
+  }
+  return v;
+}
+template <int G, typename T>
+__device__ __forceinline__ T group_max(T v) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    const T w = __shfl_xor_sync(kFull, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+template <int G>
+__device__ __forceinline__ bool group_any(bool p, int lane) {
+  const unsigned b = __ballot_sync(kFull, p);
+  if (G == 32) return b != 0u;
+  const unsigned m = ((1u << G) - 1u) << (lane & ~(G - 1));
+  return (b & m) != 0u;
+}
+
+// Detector coordinate of a voxel row at one view.  FP32: integer + fraction so that the
+// per-voxel position keeps ~1e-7 bin accuracy; FP64: the coordinate itself.
+struct RowBaseF {
+  int ib;
+  float fb;
+};
+struct RowBaseD {
+  double base;
+};
+template <typename Real>
+using RowBase = typename std::conditional<std::is_same<Real, float>::value, RowBaseF,
+                                          RowBaseD>::type;
+
+// u = j0 + f (f in [0,1)) for voxel column x: u = base(z) + x * bx with bx given as hi+lo.
+__device__ __forceinline__ void detector_pos(int x, RowBaseF rb, float2 bx, double, int& j0,
+                                             float& f) {
+  const float xf = static_cast<float>(x);
+  const float p = xf * bx.x;
+  const float pe = fmaf(xf, bx.x, -p);  // exact rounding error of x*bx.hi
+  const float jp = floorf(p);
+  float ff = (p - jp) + rb.fb + (pe + xf * bx.y);
+  const float jf = floorf(ff);
+  ff -= jf;
+  j0 = rb.ib + static_cast<int>(jp) + static_cast<int>(jf);
+  f = ff;
+}
+__device__ __forceinline__ void detector_pos(int x, RowBaseD rb, float2, double bxd, int& j0,
+                                             double& f) {
+  const double u = fma(static_cast<double>(x), bxd, rb.base);
+  const double fl = floor(u);
+  j0 = static_cast<int>(fl);
+  f = u - fl;
+}
+
+template <typename Real>
+__device__ __forceinline__ void compute_row_base(const DevTables& tab, int n_theta, int z,
+                                                 RowBase<Real>* rb, int tid, int nthreads) {
+  for (int v = tid; v < n_theta; v += nthreads) {
+    const double b = tab.u0[v] - static_cast<double>(z) * tab.bz[v];
+    if constexpr (std::is_same<Real, float>::value) {
+      const double fl = floor(b);
+      rb[v].ib = static_cast<int>(fl);
+      rb[v].fb = static_cast<float>(b - fl);
+    } else {
+      rb[v].base = b;
+    }
+  }
+}
+
+// A-matrix entries of one voxel at one view (AMatrixCol.cpp:148-232): bins j in
+// [floor(u-d), floor(u+d)] on the detector, value = linear interpolation of the detector
+// response at |u - (j+0.5)|, kept when > 0.
+template <typename Real, int NB>
+__device__ __forceinline__ void view_footprint(const DevGeom& g, const Real* __restrict__ hrow,
+                                               int j0, Real f, int& jlo, Real (&a)[NB]) {
+  const Real hw = static_cast<Real>(g.half_width);
+  const Real kr = static_cast<Real>(g.kr);
+  const int lo = j0 + static_cast<int>(floor(f - hw));
+  const int hi = j0 + static_cast<int>(floor(f + hw));
+  jlo = lo;
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    const int j = lo + b;
+    Real v = Real(0);
+    if (j <= hi && j >= 0 && j < g.n_r) {
+      const Real delta = fabs(static_cast<Real>(j0 - j) + f - Real(0.5));
+      const Real xr = delta * kr;
+      const int idx = static_cast<int>(xr);
+      if (idx < g.bins) {
+        const Real t = xr - static_cast<Real>(idx);
+        v = (Real(1) - t) * hrow[idx] + t * hrow[idx + 1];
+      }
+    }
+    a[b] = v > Real(0) ? v : Real(0);
+  }
+}
+
+// rho'(d)/d of the QGGMRF prior (QGGMRF_Functions.cpp:90-104 divided by d), or rho''(0)
+// (:109-112) when d == 0.
+template <typename Real>
+__device__ __forceinline__ Real qggmrf_coef(const DevFilter& q, Real d0) {
+  const Real P = static_cast<Real>(q.mrf_p), Q = static_cast<Real>(q.mrf_q);
+  const Real c = static_cast<Real>(q.mrf_c), sp = static_cast<Real>(q.sig_p);
+  if (d0 == Real(0)) return P / (sp * c);
+  const Real ad = fabs(d0);
+  const Real t1 = pow(ad, P - Q) / static_cast<Real>(q.sig_pq);
+  const Real t3 = c + t1;
+  Real r = (P - ((P - Q) * t1) / t3) / (t3 * sp);
+  if (P != Real(2)) r *= pow(ad, P - Real(2));
+  return r;
+}
+
+// Everything one CTA (or the reference-order warp) shares while it works on voxel slice y.
+template <typename Real>
+struct SliceCtx {
+  using R2 = typename V2<Real>::type;
+  const DevGeom* g;
+  const DevFilter* q;
+  Real* vol;                 // global volume [n_y][n_z][n_x]
+  Real* es;                  // first detector row of the slice
+  int rs, ps;                // row stride (between views), plane stride (between t rows)
+  const RowBase<Real>* rb;   // current z-row's detector coordinates per view
+  const Real* sH;            // [n_theta][bins+1]
+  const float2* sbx;         // FP32 path
+  const double* sbxd;        // FP64 path
+  const R2* sgw;             // (gain, weight) per view
+  const Real* hv;            // t-response of the slice
+  const uint8_t* lineok;     // [n_z][n_x] A-column not empty
+  Real* cache;               // [9][n_x] neighbour rows (dy,dz) or nullptr (read global)
+  int tcount;
+  int mode, iter_nonzero, zero_skipping;
+};
+
+// One voxel (z, x, y) updated by one group of G lanes (G = 16: two voxels per warp).  All 32
+// lanes of the warp call this together; `active` is false for a group with no voxel.
+// wst (group lane 0): ROI sum|dx|, ROI sum|x|, zero-skipped, updated.
+template <typename Real, int NB, int G, int VPL>
+__device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x_req, int y,
+                                           bool active, int lane, double* wst) {
+  using R2 = typename V2<Real>::type;
+  const DevGeom& g = *c.g;
+  const int gl = lane & (G - 1);
+  const int x = active ? x_req : 0;
+  const size_t plane = static_cast<size_t>(g.n_z) * g.n_x;
+  const size_t vidx = static_cast<size_t>(y) * plane + static_cast<size_t>(z) * g.n_x + x;
+  const Real V = c.cache ? c.cache[4 * g.n_x + x] : c.vol[vidx];
+  const bool line_ok = active && c.lineok[static_cast<size_t>(z) * g.n_x + x] != 0;
+  bool live = line_ok;
+
+  // 26-neighbourhood, entries k = gl, gl+G, ... (UpdateVoxels.cpp:283-306); centre and
+  // out-of-range entries are 0 in the bracket, as in the reference
+  constexpr int NNB = (27 + G - 1) / G;
+  Real nb[NNB];
+  bool nvalid[NNB];
+  bool pos = false;
+  if (c.mode != kModeProject) {
+#pragma unroll
+    for (int i = 0; i < NNB; ++i) {
+      const int k = gl + G * i;
+      nb[i] = Real(0);
+      nvalid[i] = false;
+      if (k < 27 && k != 13) {
+        const int dy = k / 9 - 1, dz = (k / 3) % 3 - 1, dx = k % 3 - 1;
+        const int yy = y + dy, zz = z + dz, xx = x + dx;
+        if (yy >= 0 && yy < g.n_y && zz >= 0 && zz < g.n_z && xx >= 0 && xx < g.n_x) {
+          nb[i] = c.cache ? c.cache[((dy + 1) * 3 + (dz + 1)) * g.n_x + xx]
+                          : c.vol[static_cast<size_t>(yy) * plane +
+                                  static_cast<size_t>(zz) * g.n_x + xx];
+          nvalid[i] = true;
+          pos |= nb[i] > Real(0);
+        }
+      }
+    }
+    // zero skipping (UpdateVoxels.cpp:310-338).  The ballot runs on all 32 lanes: the two
+    // voxel groups of a warp may disagree on whether their voxel is zero.
+    const bool any_pos = group_any<G>(pos, lane);
+    if (c.zero_skipping && c.iter_nonzero && V == Real(0) && !any_pos) {
+      if (live && gl == 0) wst[2] += 1.0;
+      live = false;
+    }
+  } else {
+    live = live && V != Real(0);
+  }
+  if (!__any_sync(kFull, live)) return;
+
+  // A-column of the voxel, lanes over views (AMatrixCol.cpp:148-232)
+  const Real hw = static_cast<Real>(g.half_width);
+  int jlo[VPL];
+  Real a[VPL][NB];
+#pragma unroll
+  for (int i = 0; i < VPL; ++i) {
+    const int v = gl + G * i;
+    jlo[i] = 0;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) a[i][b] = Real(0);
+    if (v < g.n_theta && live) {
+      int j0;
+      Real f;
+      detector_pos(x, c.rb[v], c.sbx ? c.sbx[v] : float2{0.f, 0.f}, c.sbxd ? c.sbxd[v] : 0.0, j0,
+                   f);
+      const Real u = static_cast<Real>(j0) + f;
+      if (!(u + hw < Real(0) || u - hw > static_cast<Real>(g.n_r)))
+        view_footprint<Real, NB>(g, c.sH + v * (g.bins + 1), j0, f, jlo[i], a[i]);
+    }
+  }
+
+  if (c.mode == kModeProject) {
+#pragma unroll
+    for (int i = 0; i < VPL; ++i) {
+      const int v = gl + G * i;
+      if (v >= g.n_theta || !live) continue;
+      const Real gain = c.sgw[v].x;
+      for (int tr = 0; tr < c.tcount; ++tr) {
+        const Real hh = c.hv[tr];
+        Real* row = c.es + tr * c.ps + v * c.rs + jlo[i];
+#pragma unroll
+        for (int b = 0; b < NB; ++b)
+          if (a[i][b] > Real(0)) row[b] += gain * (a[i][b] * hh * V);
+      }
+    }
+    return;
+  }
+
+  // theta1 / theta2 (UpdateVoxels.cpp:343-369)
+  Real t1 = Real(0), t2 = Real(0);
+#pragma unroll
+  for (int i = 0; i < VPL; ++i) {
+    const int v = gl + G * i;
+    if (v >= g.n_theta || !live) continue;
+    const R2 gw = c.sgw[v];
+    for (int tr = 0; tr < c.tcount; ++tr) {
+      const Real hh = c.hv[tr];
+      const Real* row = c.es + tr * c.ps + v * c.rs + jlo[i];
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        if (a[i][b] > Real(0)) {
+          const Real pe = gw.x * a[i][b] * hh;
+          t2 += pe * pe * gw.y;
+          t1 += row[b] * pe * gw.y;
+        }
+      }
+    }
+  }
+  const Real theta1 = -group_sum<G>(t1);
+  const Real theta2 = group_sum<G>(t2);
+  // bracket (find_min_max, UpdateVoxels.cpp:47-63)
+  Real lo = Real(0), hi = Real(0);
+#pragma unroll
+  for (int i = 0; i < NNB; ++i) {
+    lo = nb[i] < lo ? nb[i] : lo;
+    hi = nb[i] > hi ? nb[i] : hi;
+  }
+  lo = group_min<G>(lo);
+  hi = group_max<G>(hi);
+  if (theta2 != Real(0)) {
+    const Real cand = V - theta1 / theta2;
+    lo = lo > cand ? cand : lo;
+    hi = hi < cand ? cand : hi;
+  }
+  // QGGMRF surrogate, one iteration (QGGMRF_Functions.cpp:153-206)
+  Real s1 = Real(0), s2 = Real(0);
+#pragma unroll
+  for (int i = 0; i < NNB; ++i) {
+    if (nvalid[i]) {
+      const Real tc = static_cast<Real>(c.q->f[gl + G * i]) * qggmrf_coef<Real>(*c.q, V - nb[i]);
+      s1 += tc * nb[i];
+      s2 += tc;
+    }
+  }
+  s1 = group_sum<G>(s1);
+  s2 = group_sum<G>(s2);
+  const Real u = (s1 + theta2 * V - theta1) / (s2 + theta2);
+  Real nv = V + static_cast<Real>(c.q->mrf_alpha) * (u - V);
+  nv = (nv < lo) ? lo : ((nv > hi) ? hi : nv);
+  if (nv < Real(0)) nv = Real(0);  // positivity (UpdateVoxels.cpp:394-400)
+  const Real dlt = nv - V;
+  if (!live) return;
+  // error-sinogram scatter (UpdateVoxels.cpp:423-449)
+  if (dlt != Real(0)) {
+#pragma unroll
+    for (int i = 0; i < VPL; ++i) {
+      const int v = gl + G * i;
+      if (v >= g.n_theta) continue;
+      const Real gain = c.sgw[v].x;
+      for (int tr = 0; tr < c.tcount; ++tr) {
+        const Real hh = c.hv[tr];
+        Real* row = c.es + tr * c.ps + v * c.rs + jlo[i];
+#pragma unroll
+        for (int b = 0; b < NB; ++b)
+          if (a[i][b] > Real(0)) row[b] -= gain * (a[i][b] * hh * dlt);
+      }
+    }
+  }
+  if (gl == 0) {
+    c.vol[vidx] = nv;
+    if (c.cache) c.cache[4 * g.n_x + x] = nv;
+    if (x >= g.roi_x0 && x <= g.roi_x1 && z >= g.roi_z0 && z <= g.roi_z1) {
+      wst[0] += fabs(static_cast<double>(dlt));
+      wst[1] += fabs(static_cast<double>(V));
+    }
+    wst[3] += 1.0;
+  }
+}
+
+struct SmemLayout {
+  size_t bar, stats, rb, bx, bxd, gw, H, hv, cache, es, total;
+};
+
+__host__ __device__ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+__host__ __device__ inline SmemLayout smem_layout(int n_theta, int n_x, int n_rs, int t_rows,
+                                                  int bins, bool stage, size_t real_bytes) {
+  SmemLayout L;
+  size_t o = 0;
+  L.bar = o;
+  o += 16;
+  L.stats = o;
+  o += sizeof(double) * kWarps * 2 * kStatSlots;
+  L.rb = o;
+  o = align_up(o + 8 * static_cast<size_t>(n_theta), 16);
+  L.bx = o;
+  o = align_up(o + sizeof(float2) * n_theta, 16);
+  L.bxd = o;
+  o = align_up(o + sizeof(double) * n_theta, 16);
+  L.gw = o;
+  o = align_up(o + 2 * real_bytes * n_theta, 16);
+  L.H = o;
+  o = align_up(o + real_bytes * n_theta * (bins + 1), 16);
+  L.hv = o;
+  o = align_up(o + real_bytes * kMaxTRows, 16);
+  L.cache = o;
+  o = align_up(o + real_bytes * 9 * static_cast<size_t>(n_x), 128);
+  L.es = o;
+  if (stage) o += real_bytes * static_cast<size_t>(t_rows) * n_theta * n_rs;
+  L.total = align_up(o, 16);
+  return L;
+}
+
+template <typename Real, int NB, int G, int VPL, bool STAGE>
+__global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
+  using R2 = typename V2<Real>::type;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const DevGeom& g = A.g;
+  const int y = A.colour + 2 * static_cast<int>(blockIdx.x);
+  if (y >= g.n_y) return;
+  const int tid = threadIdx.x, nthreads = blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  constexpr int GPW = 32 / G;  // voxel groups per warp
+  const int group = warp * GPW + (lane / G);
+  const int n_groups = (nthreads / 32) * GPW;
+  const int tcount = A.tab.t_count[y], tfirst = A.tab.t_first[y];
+  const SmemLayout L = smem_layout(g.n_theta, g.n_x, A.n_rs, tcount, g.bins, STAGE, sizeof(Real));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L.bar);
+  double* sstat = reinterpret_cast<double*>(smem + L.stats);
+  RowBase<Real>* rb = reinterpret_cast<RowBase<Real>*>(smem + L.rb);
+  float2* sbx = reinterpret_cast<float2*>(smem + L.bx);
+  double* sbxd = reinterpret_cast<double*>(smem + L.bxd);
+  R2* sgw = reinterpret_cast<R2*>(smem + L.gw);
+  Real* sH = reinterpret_cast<Real*>(smem + L.H);
+  Real* shv = reinterpret_cast<Real*>(smem + L.hv);
+  Real* cache = reinterpret_cast<Real*>(smem + L.cache);
+  const Real* gH = static_cast<const Real*>(A.tab.H);
+  const R2* ggw = static_cast<const R2*>(A.tab.gw);
+  const Real* ghv = static_cast<const Real*>(A.tab.hval);
+  Real* const ge = static_cast<Real*>(A.e);
+  Real* const gx = static_cast<Real*>(A.x);
+  constexpr bool kF32 = std::is_same<Real, float>::value;
+
+  for (int i = tid; i < g.n_theta * (g.bins + 1); i += nthreads) sH[i] = gH[i];
+  for (int v = tid; v < g.n_theta; v += nthreads) {
+    if (kF32)
+      sbx[v] = A.tab.bx[v];
+    else
+      sbxd[v] = A.tab.bxd[v];
+    sgw[v] = ggw[v];
+  }
+  if (tid < kMaxTRows) shv[tid] = ghv[y * kMaxTRows + tid];
+
+  const size_t sino_plane = static_cast<size_t>(g.n_theta) * g.n_rp;
+  Real* es;
+  int rs, ps;
+  const int rows = tcount * g.n_theta;
+  const uint32_t row_bytes = static_cast<uint32_t>(g.n_rp * sizeof(Real));
+  if (STAGE) {
+    es = reinterpret_cast<Real*>(smem + L.es);
+    rs = A.n_rs;
+    ps = g.n_theta * A.n_rs;
+    if (A.mode == kModeProject) {
+      for (int i = tid; i < tcount * ps; i += nthreads) es[i] = Real(0);
+      __syncthreads();
+    } else {
+      if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+      }
+      __syncthreads();
+      if (tid == 0) mbar_expect_tx(bar, static_cast<uint32_t>(rows) * row_bytes);
+      __syncthreads();
+      for (int r = tid; r < rows; r += nthreads) {
+        const int tr = r / g.n_theta, v = r % g.n_theta;
+        bulk_g2s(es + tr * ps + v * rs,
+                 ge + (static_cast<size_t>(tfirst + tr)) * sino_plane +
+                     static_cast<size_t>(v) * g.n_rp,
+                 row_bytes, bar);
+      }
+      const bool ok = mbar_wait(bar, 0);
+      if (!__syncthreads_and(ok)) {
+        if (tid == 0) atomicOr(A.err, 1);
+        mbar_wait(bar, 0);  // give copies still in flight a second bounded chance to land
+        return;
+      }
+    }
+  } else {
+    es = ge + static_cast<size_t>(tfirst) * sino_plane;
+    rs = g.n_rp;
+    ps = static_cast<int>(sino_plane);
+  }
+
+  SliceCtx<Real> c;
+  c.g = &A.g;
+  c.q = &A.flt;
+  c.vol = gx;
+  c.es = es;
+  c.rs = rs;
+  c.ps = ps;
+  c.rb = rb;
+  c.sH = sH;
+  c.sbx = kF32 ? sbx : nullptr;
+  c.sbxd = kF32 ? nullptr : sbxd;
+  c.sgw = sgw;
+  c.hv = shv;
+  c.lineok = A.tab.lineok;
+  c.cache = cache;
+  c.tcount = tcount;
+  c.mode = A.mode;
+  c.iter_nonzero = A.iter_nonzero;
+  c.zero_skipping = A.zero_skipping;
+
+  const size_t vplane = static_cast<size_t>(g.n_z) * g.n_x;
+  double wst[kStatSlots] = {0.0, 0.0, 0.0, 0.0};
+  for (int rr = 0; rr < g.n_z; ++rr) {
+    const int z = A.row_order[rr];
+    __syncthreads();
+    compute_row_base<Real>(A.tab, g.n_theta, z, rb, tid, nthreads);
+    // neighbour rows (y+dy, z+dz), dy, dz in {-1,0,1}; rows outside the volume read as 0
+    for (int i = tid; i < 9 * g.n_x; i += nthreads) {
+      const int r = i / g.n_x, xx = i - r * g.n_x;
+      const int yy = y + r / 3 - 1, zz = z + r % 3 - 1;
+      Real v = Real(0);
+      if (yy >= 0 && yy < g.n_y && zz >= 0 && zz < g.n_z)
+        v = gx[static_cast<size_t>(yy) * vplane + static_cast<size_t>(zz) * g.n_x + xx];
+      cache[i] = v;
+    }
+    __syncthreads();
+    for (int k = 0; k < A.stride; ++k) {
+      for (int m = group;; m += n_groups) {
+        const int x = k + A.stride * m;
+        const bool active = x < g.n_x;
+        if (!__any_sync(kFull, active)) break;
+        group_step<Real, NB, G, VPL>(c, z, x, y, active, lane, wst);
+      }
+      __syncthreads();
+    }
+  }
+
+  if (STAGE) {
+    fence_proxy_async_smem();
+    __syncthreads();
+    for (int r = tid; r < rows; r += nthreads) {
+      const int tr = r / g.n_theta, v = r % g.n_theta;
+      bulk_s2g(ge + (static_cast<size_t>(tfirst + tr)) * sino_plane +
+                   static_cast<size_t>(v) * g.n_rp,
+               es + tr * ps + v * rs, row_bytes);
+    }
+    bulk_commit();
+    bulk_wait_all();
+  }
+  if (A.stats != nullptr) {
+    const int gl = lane & (G - 1);
+    if (gl == 0)
+      for (int s = 0; s < kStatSlots; ++s) sstat[group * kStatSlots + s] = wst[s];
+    __syncthreads();
+    if (tid < kStatSlots) {
+      double acc = 0.0;
+      for (int w = 0; w < n_groups; ++w) acc += sstat[w * kStatSlots + tid];
+      A.stats[static_cast<size_t>(blockIdx.x) * kStatSlots + tid] = acc;
+    }
+  }
+}
+
+template <typename Real, int NB, int VPL>
+__global__ void __launch_bounds__(32, 1) ref_order_kernel(RefOrderArgs A) {
+  using R2 = typename V2<Real>::type;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const DevGeom& g = A.g;
+  const int lane = threadIdx.x;
+  const SmemLayout L = smem_layout(g.n_theta, 0, 0, 0, g.bins, false, sizeof(Real));
+  RowBase<Real>* rb = reinterpret_cast<RowBase<Real>*>(smem + L.rb);
+  float2* sbx = reinterpret_cast<float2*>(smem + L.bx);
+  double* sbxd = reinterpret_cast<double*>(smem + L.bxd);
+  R2* sgw = reinterpret_cast<R2*>(smem + L.gw);
+  Real* sH = reinterpret_cast<Real*>(smem + L.H);
+  const Real* gH = static_cast<const Real*>(A.tab.H);
+  const R2* ggw = static_cast<const R2*>(A.tab.gw);
+  const Real* ghv = static_cast<const Real*>(A.tab.hval);
+  constexpr bool kF32 = std::is_same<Real, float>::value;
+  for (int i = lane; i < g.n_theta * (g.bins + 1); i += 32) sH[i] = gH[i];
+  for (int v = lane; v < g.n_theta; v += 32) {
+    if (kF32)
+      sbx[v] = A.tab.bx[v];
+    else
+      sbxd[v] = A.tab.bxd[v];
+    sgw[v] = ggw[v];
+  }
+  __syncwarp();
+  SliceCtx<Real> c;
+  c.g = &A.g;
+  c.q = &A.flt;
+  c.vol = static_cast<Real*>(A.x);
+  c.rs = g.n_rp;
+  c.ps = g.n_theta * g.n_rp;
+  c.rb = rb;
+  c.sH = sH;
+  c.sbx = kF32 ? sbx : nullptr;
+  c.sbxd = kF32 ? nullptr : sbxd;
+  c.sgw = sgw;
+  c.lineok = A.tab.lineok;
+  c.cache = nullptr;
+  c.mode = kModeICD;
+  c.iter_nonzero = A.iter_nonzero;
+  c.zero_skipping = A.zero_skipping;
+  Real* const ge = static_cast<Real*>(A.e);
+  const size_t sino_plane = static_cast<size_t>(g.n_theta) * g.n_rp;
+  double wst[kStatSlots] = {0.0, 0.0, 0.0, 0.0};
+  for (int n = 0; n < A.n_lines; ++n) {
+    const int l = A.lines[n];
+    const int z = l / g.n_x, x = l % g.n_x;
+    __syncwarp();
+    compute_row_base<Real>(A.tab, g.n_theta, z, rb, lane, 32);
+    __syncwarp();
+    for (int y = 0; y < g.n_y; ++y) {
+      c.es = ge + static_cast<size_t>(A.tab.t_first[y]) * sino_plane;
+      c.tcount = A.tab.t_count[y];
+      c.hv = ghv + y * kMaxTRows;
+      group_step<Real, NB, 32, VPL>(c, z, x, y, true, lane, wst);
+      __syncwarp();
+    }
+  }
+  if (lane == 0)
+    for (int s = 0; s < kStatSlots; ++s) A.stats[s] = wst[s];
+}
+
+inline int ok_or(cudaError_t e) { return e == cudaSuccess ? 0 : -3; }
+
+template <typename Real, int NB, int G, int VPL, bool STAGE>
+int launch_sweep_t(const SweepArgs& a, size_t smem, cudaStream_t s) {
+  auto k = sweep_kernel<Real, NB, G, VPL, STAGE>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem));
+  if (e != cudaSuccess) return -3;
+  k<<<a.n_slices, kWarps * 32, smem, s>>>(a);
+  return ok_or(cudaGetLastError());
+}
+
+template <typename Real, int NB, int VPL>
+int launch_ref_t(const RefOrderArgs& a, cudaStream_t s) {
+  const size_t smem = smem_layout(a.g.n_theta, 0, 0, 0, a.g.bins, false, sizeof(Real)).total;
+  auto k = ref_order_kernel<Real, NB, VPL>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem));
+  if (e != cudaSuccess) return -3;
+  k<<<1, 32, smem, s>>>(a);
+  return ok_or(cudaGetLastError());
+}
+
+}  // namespace sweep
+}  // namespace mbir

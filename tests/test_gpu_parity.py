@@ -64,24 +64,42 @@ def test_forward_projection_two_spheres_full_size(lib_built, oracle_mod):
     assert err <= 1e-5, err
 
 
-def test_parallel_sweeps_match_oracle_same_order(lib_built, oracle_mod):
+def test_parallel_sweep_fp32_matches_oracle_same_order(lib_built, oracle_mod):
+    """One FP32 sweep in the engine's parallel order against the FP64 oracle in the same order.
+    (Later FP32 sweeps drift from FP64 by the chaotic sensitivity of ICD iterates to rounding;
+    the FP64 engine is compared over several sweeps below.)"""
     e, o, p, y = pair(lib_built, oracle_mod)
     e.prepare()
     o.prepare()
-    for k in range(3):
+    rows, stride = e.schedule(0)
+    sg = e.sweep(0, 0)
+    so = o.sweep_slices(rows, stride, 0, 0)
+    assert sg[3] == so[3] and sg[2] == so[2], (sg, so)  # updated / zero-skipped counts
+    assert rel(e.volume(), o.volume()) <= 1e-5
+    assert rel(e.error_sinogram(), o.error()) <= 1e-5
+
+
+def test_parallel_sweeps_fp64_match_oracle_same_order(lib_built, oracle_mod):
+    e, o, p, y = pair(lib_built, oracle_mod, precision=lib_built.FP64)
+    e.prepare()
+    o.prepare()
+    for k in range(4):
         rows, stride = e.schedule(k)
         sg = e.sweep(0, k)
         so = o.sweep_slices(rows, stride, 0, k)
-        assert sg[3] == so[3] and sg[2] == so[2], (sg, so)  # updated / zero-skipped counts
-        r = rel(e.volume(), o.volume())
-        assert r <= 1e-5 * (k + 1), (k, r)
-        assert rel(e.error_sinogram(), o.error()) <= 1e-5 * (k + 1)
+        assert sg[3] == so[3] and sg[2] == so[2], (k, sg, so)
+        assert rel(e.volume(), o.volume()) <= 1e-6, k   # float read-out of FP64 state
+    e.joint_estimation()
+    o.joint_estimation()
+    np.testing.assert_allclose(e.nuisance()[0], o.gain(), rtol=1e-9)
 
 
 def test_reference_order_iterates_after_five_outer(lib_built, oracle_mod):
-    """Reference-order mode reproduces the reference iterates (same MT19937 visit order, one
-    task over all y) after 5 outer iterations with gain/offset and variance updates."""
-    e, o, p, y = pair(lib_built, oracle_mod, order_mode=1, seed=20121, outer_iterations=5)
+    """Reference-order mode (same MT19937 visit order, one task over all y, FP64 as the
+    reference's Real_t) reproduces the reference iterates after 5 outer iterations with
+    gain/offset and variance updates."""
+    e, o, p, y = pair(lib_built, oracle_mod, order_mode=1, seed=20121, outer_iterations=5,
+                      precision=lib_built.FP64)
     e.run()
     o.prepare()
     n, _ = o.run(20121)
@@ -92,6 +110,30 @@ def test_reference_order_iterates_after_five_outer(lib_built, oracle_mod):
     assert rel(g, o.gain()) <= 1e-4
     assert rel(off, o.offset()) <= 1e-4
     assert rel(var, o.variance()) <= 1e-4
+
+
+def test_reference_order_fp32_first_sweep(lib_built, oracle_mod):
+    e, o, p, y = pair(lib_built, oracle_mod, order_mode=1, seed=77)
+    e.prepare()
+    o.prepare()
+    e.sweep(0, 0)
+    o.sweep_reference(77, 0, 0)
+    assert rel(e.volume(), o.volume()) <= 1e-5
+
+
+def test_fp32_vs_fp64_engine_precision(lib_built, oracle_mod):
+    """Precision study: the FP32 engine against the all-FP64 engine from the same start, one
+    sweep in the same order (error stated against the FP64 run)."""
+    mbir = lib_built
+    y, ang, th = small_case()
+    vols = []
+    for prec in (mbir.FP32, mbir.FP64):
+        with mbir.Engine(haadf_params(mbir, th, precision=prec)) as e:
+            e.set_sinogram(y, ang)
+            e.prepare()
+            e.sweep(0, 0)
+            vols.append(e.volume())
+    assert rel(vols[0], vols[1]) <= 1e-5
 
 
 def _sync_oracle(e, o):
@@ -162,8 +204,12 @@ def test_global_slice_path_matches_oracle(lib_built, oracle_mod):
     proj = synthetic.ellipsoid_projection(ang, 384, 4, [(0, 0, 0, 60, 60, 20, 1.0)])
     y, _ = synthetic.haadf_measurements(proj, seed=5)
     e, o, p, y = pair(lib_built, oracle_mod, case=(y, ang.astype(np.float32), 24.0))
+    nz, nx, ny = e.dims()[:3]
+    vol = np.random.default_rng(2).random((nz, nx, ny)).astype(np.float32)
+    e.set_initial_volume(vol)
     e.prepare()
-    o.prepare()
+    assert e.status().staged == 0  # 150 x 388 floats per detector row exceed shared memory
+    o.prepare(vol.astype(np.float64))
     assert np.abs(e.projection() - o.yest()).max() / np.abs(o.yest()).max() <= 1e-5
     rows, stride = e.schedule(0)
     e.sweep(0, 0)
