@@ -189,6 +189,60 @@ int32_t mbir_run_multires(const mbir_params* p, const float* counts, const float
                           int32_t n_theta, int32_t n_r, int32_t n_t, double delta_r,
                           double delta_t, float* out, int64_t n, int32_t* dims_out);
 
+/* Batched execution (config "many uneven reconstructions"): prepared FP32 parallel-order
+ * engines on one device advance together, one persistent cooperative launch per ICD sweep
+ * covering every voxel slice of every engine; gain/offset, variance and cost stay per engine.
+ * The reference has no counterpart: it runs one reconstruction per process
+ * (HAADF_MultiResolutionReconstruction.cpp:175-485). */
+typedef struct mbir_batch mbir_batch;
+mbir_batch* mbir_batch_create(int32_t device);
+void mbir_batch_destroy(mbir_batch* b);
+int32_t mbir_batch_add(mbir_batch* b, mbir_engine* e);
+int32_t mbir_batch_remove(mbir_batch* b, mbir_engine* e);
+int32_t mbir_batch_size(const mbir_batch* b);
+/* one sweep of every engine (outer index drives zero skipping); stats: 4 doubles per engine */
+int32_t mbir_batch_sweep(mbir_batch* b, int32_t outer, double* stats);
+/* outer iterations (batched sweep + per-engine gain/offset, variance, cost) until each engine's
+ * relative cost change <= cost_rel_tol or max_outer; per-engine iteration counts and costs */
+int32_t mbir_batch_run(mbir_batch* b, int32_t max_outer, double cost_rel_tol,
+                       int32_t* outer_done, double* final_cost);
+/* device time (ms) of the last batched sweep and of all batched sweeps */
+double mbir_batch_last_ms(const mbir_batch* b);
+double mbir_batch_total_ms(const mbir_batch* b);
+const char* mbir_batch_last_error(const mbir_batch* b);
+
+/* Serving (config "served stream"): a request loop on one device that admits tilt series of
+ * any size by device memory, keeps each admitted request resident, advances all active
+ * requests together (one batched sweep per outer iteration, continuous batching: arrivals join
+ * between sweeps) and retires each one when its relative cost change <= cost_rel_tol or after
+ * max_outer iterations.  Thread-safe.  No reference counterpart. */
+typedef struct mbir_server mbir_server;
+typedef struct mbir_server_stats {
+  int64_t submitted, completed, failed;
+  int32_t active, queued;
+  double p50_ms, p99_ms, mean_ms;  /* request latency: completion - submission */
+  double voxel_updates;            /* voxel visits of retired requests */
+  double busy_s;                   /* worker time with requests on the device */
+  double batched_sweep_ms;         /* device time of all batched sweeps */
+  int64_t batched_sweeps;
+} mbir_server_stats;
+/* mem_budget_bytes <= 0: 80% of the free device memory; max_active <= 0: 64 */
+mbir_server* mbir_server_create(int32_t device, int64_t mem_budget_bytes, int32_t max_active);
+void mbir_server_destroy(mbir_server* s);
+/* returns a request id > 0, or a negative MBIR_E* code; inputs are copied */
+int64_t mbir_server_submit(mbir_server* s, const mbir_params* p, const float* counts,
+                           const float* tilts_deg, int32_t n_theta, int32_t n_r, int32_t n_t,
+                           double delta_r, double delta_t, int32_t max_outer,
+                           double cost_rel_tol);
+/* state: 0 queued, 1 active, 2 done, < 0 failed with that code */
+int32_t mbir_server_poll(mbir_server* s, int64_t id, int32_t* state, double* latency_ms,
+                         int32_t* outer_done, double* cost);
+int32_t mbir_server_wait(mbir_server* s, int64_t id, double timeout_s);
+int32_t mbir_server_result(mbir_server* s, int64_t id, float* out, int64_t n, int32_t* dims);
+int32_t mbir_server_release(mbir_server* s, int64_t id);
+int32_t mbir_server_get_stats(mbir_server* s, mbir_server_stats* st);
+const char* mbir_server_last_error(const mbir_server* s);
+
 /* Library version string */
 const char* mbir_version(void);
 

@@ -18,8 +18,10 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmbir_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["mbir_sweep_f32.cu", "mbir_sweep_f32_hbm.cu", "mbir_sweep_f64.cu", "mbir_kernels.cu",
-           "mbir_engine.cu", "mrc_io.cpp", "mbir_capi.cpp"]
-HEADERS = ["mbir_internal.h", "mbir_engine.h", "mbir_sweep.cuh"]
+           "mbir_engine.cu", "mbir_batch.cu", "mbir_server.cpp", "mrc_io.cpp",
+           "mbir_capi.cpp"]
+HEADERS = ["mbir_internal.h", "mbir_engine.h", "mbir_sweep.cuh", "mbir_batch.h",
+           "mbir_server.h"]
 
 
 def nvcc():

@@ -1,0 +1,234 @@
+// mbir_batch.cu -- many reconstructions of uneven size advanced together: one persistent,
+// cooperative launch per ICD sweep covers every voxel slice of every engine in the batch
+// (batch_sweep_kernel in mbir_sweep.cuh); gain/offset, variance and cost updates stay per
+// engine.  Each engine keeps its volume, error sinogram and nuisance state resident in HBM.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "mbir_batch.h"
+
+namespace mbir {
+
+Batch::Batch(int device) : device_(device) {}
+
+Batch::~Batch() {
+  if (d_series_) cudaFree(d_series_);
+  if (d_items_) cudaFree(d_items_);
+  if (d_ctr_) cudaFree(d_ctr_);
+  if (d_st4_) cudaFree(d_st4_);
+  if (ev0_) cudaEventDestroy(static_cast<cudaEvent_t>(ev0_));
+  if (ev1_) cudaEventDestroy(static_cast<cudaEvent_t>(ev1_));
+  if (stream_) cudaStreamDestroy(static_cast<cudaStream_t>(stream_));
+}
+
+int Batch::fail(int code, const std::string& m) {
+  err_ = m;
+  return code;
+}
+
+int Batch::add(Engine* e) {
+  if (!e) return fail(MBIR_EINVAL, "batch_add: null engine");
+  if (e->state() < 2) return fail(MBIR_ESTATE, "batch_add: prepare the engine first");
+  if (e->fp64() || e->params().order_mode != MBIR_ORDER_PARALLEL)
+    return fail(MBIR_ENOTSUP, "batch_add: FP32 parallel-order engines only");
+  if (e->params().device != device_) return fail(MBIR_EINVAL, "batch_add: engine on another device");
+  if (std::find(eng_.begin(), eng_.end(), e) != eng_.end()) return MBIR_OK;
+  eng_.push_back(e);
+  dirty_ = true;
+  return MBIR_OK;
+}
+
+int Batch::remove(Engine* e) {
+  auto it = std::find(eng_.begin(), eng_.end(), e);
+  if (it == eng_.end()) return fail(MBIR_EINVAL, "batch_remove: engine not in batch");
+  eng_.erase(it);
+  dirty_ = true;
+  return MBIR_OK;
+}
+
+int Batch::ensure_resources() {
+  if (!stream_) {
+    if (cudaSetDevice(device_) != cudaSuccess) return fail(MBIR_EDEVICE, "batch: cudaSetDevice");
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+      return fail(MBIR_EDEVICE, "batch: stream");
+    stream_ = s;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    ev0_ = a;
+    ev1_ = b;
+  }
+  const size_t n = eng_.size();
+  if (n > cap_series_) {
+    if (d_series_) cudaFree(d_series_);
+    if (d_ctr_) cudaFree(d_ctr_);
+    if (d_st4_) cudaFree(d_st4_);
+    cap_series_ = std::max<size_t>(n, 64);
+    if (cudaMalloc(&d_series_, sizeof(SweepArgs) * cap_series_) != cudaSuccess ||
+        cudaMalloc(&d_ctr_, sizeof(int) * (1 + 2 * cap_series_)) != cudaSuccess ||
+        cudaMalloc(&d_st4_, sizeof(double) * kStatSlots * cap_series_) != cudaSuccess)
+      return fail(MBIR_ENOMEM, "batch: device allocation");
+  }
+  return MBIR_OK;
+}
+
+// Queue order: colour-0 slices of every engine, then colour-1 slices; engines with the most
+// voxels per slice first so the long items start early.
+int Batch::build_items(const std::vector<SweepArgs>& args) {
+  const int n = static_cast<int>(args.size());
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return static_cast<long long>(args[a].g.n_z) * args[a].g.n_x >
+           static_cast<long long>(args[b].g.n_z) * args[b].g.n_x;
+  });
+  items_.clear();
+  need_.assign(n, 0);
+  for (int colour = 0; colour < 2; colour++)
+    for (int s : order)
+      for (int y = colour; y < args[s].g.n_y; y += 2) {
+        items_.push_back(make_int2(s, y));
+        if (colour == 0) need_[s]++;
+      }
+  if (items_.size() > cap_items_) {
+    if (d_items_) cudaFree(d_items_);
+    cap_items_ = items_.size() * 2;
+    if (cudaMalloc(&d_items_, sizeof(int2) * cap_items_) != cudaSuccess)
+      return fail(MBIR_ENOMEM, "batch: item allocation");
+  }
+  cudaMemcpy(d_items_, items_.data(), sizeof(int2) * items_.size(), cudaMemcpyHostToDevice);
+  return MBIR_OK;
+}
+
+int Batch::sweep(const std::vector<std::pair<int, int>>& iters, double* stats) {
+  if (eng_.empty()) return MBIR_OK;
+  int rc = ensure_resources();
+  if (rc) return rc;
+  const int n = static_cast<int>(eng_.size());
+  std::vector<SweepArgs> args(n);
+  size_t smem = 0;
+  int nb = -1, max_theta = 0;
+  int max_optin = 0;
+  cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_);
+  for (int i = 0; i < n; i++) {
+    size_t need = 0;
+    const int outer = iters.empty() ? 0 : iters[i].first;
+    const int inner = iters.empty() ? 0 : iters[i].second;
+    if ((rc = eng_[i]->batch_args(outer, inner, &args[i], &need)))
+      return fail(rc, eng_[i]->last_error());
+    if (nb < 0) nb = eng_[i]->nb();
+    if (eng_[i]->nb() != nb) return fail(MBIR_ENOTSUP, "batch: engines at different voxel sizes");
+    max_theta = std::max(max_theta, args[i].g.n_theta);
+    if (args[i].smem_rows) {
+      // room for the kernel's own static shared memory
+      if (need + 2048 > static_cast<size_t>(max_optin)) {
+        args[i].smem_rows = 0;
+        args[i].n_rs = 0;
+      } else {
+        smem = std::max(smem, need);
+      }
+    }
+  }
+  for (int i = 0; i < n; i++)
+    if (!args[i].smem_rows)
+      smem = std::max(smem, sweep_smem_bytes(args[i].g.n_theta, args[i].g.n_x, 0, 1,
+                                             args[i].g.bins, 0));
+  const int vpl = max_theta <= 64 ? 4 : (max_theta <= 128 ? 8 : 10);
+  if (dirty_ || items_.empty()) {
+    if ((rc = build_items(args))) return rc;
+    dirty_ = false;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  cudaMemcpyAsync(d_series_, args.data(), sizeof(SweepArgs) * n, cudaMemcpyHostToDevice, s);
+  std::vector<int> ctr(1 + 2 * n, 0);
+  for (int i = 0; i < n; i++) ctr[1 + n + i] = need_[i];
+  cudaMemcpyAsync(d_ctr_, ctr.data(), sizeof(int) * ctr.size(), cudaMemcpyHostToDevice, s);
+  BatchArgs b{};
+  b.series = d_series_;
+  b.items = d_items_;
+  b.n_items = static_cast<int>(items_.size());
+  b.queue = d_ctr_;
+  b.done = d_ctr_ + 1;
+  b.need = d_ctr_ + 1 + n;
+  cudaEventRecord(static_cast<cudaEvent_t>(ev0_), s);
+  rc = launch_batch_sweep(b, nb, vpl, smem, grid_, s);
+  if (rc) return fail(MBIR_EDEVICE, std::string("batch sweep launch: ") +
+                                        cudaGetErrorString(cudaGetLastError()));
+  for (int i = 0; i < n; i++) {
+    const int ny = args[i].g.n_y;
+    if ((rc = launch_reduce_stats(eng_[i]->slice_stats(), ny, kStatSlots, d_st4_ + kStatSlots * i, s)))
+      return fail(MBIR_EDEVICE, "batch stats reduce");
+  }
+  cudaEventRecord(static_cast<cudaEvent_t>(ev1_), s);
+  std::vector<double> st(static_cast<size_t>(kStatSlots) * n);
+  cudaMemcpyAsync(st.data(), d_st4_, sizeof(double) * st.size(), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess)
+    return fail(MBIR_EDEVICE, std::string("batch sweep: ") + cudaGetErrorString(cudaGetLastError()));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, static_cast<cudaEvent_t>(ev0_), static_cast<cudaEvent_t>(ev1_));
+  last_ms_ = ms;
+  total_ms_ += ms;
+  sweeps_++;
+  for (int i = 0; i < n; i++) {
+    if ((rc = eng_[i]->check_errors())) return fail(rc, eng_[i]->last_error());
+    const int outer = iters.empty() ? 0 : iters[i].first;
+    const int inner = iters.empty() ? 0 : iters[i].second;
+    eng_[i]->batch_finish(outer, inner, st.data() + kStatSlots * i, ms / n);
+    if (stats)
+      for (int k = 0; k < kStatSlots; k++) stats[kStatSlots * i + k] = st[kStatSlots * i + k];
+  }
+  return MBIR_OK;
+}
+
+// Outer iterations for every engine: batched sweep, then per engine gain/offset and variance
+// estimation and the FP64 MAP cost; an engine leaves the batch once its relative cost change
+// falls below tol (after its first outer iteration) or after max_outer iterations.
+int Batch::run(int max_outer, double tol, int* outer_done, double* final_cost) {
+  std::vector<Engine*> all = eng_;
+  const int n = static_cast<int>(all.size());
+  std::vector<double> prev(n, 0.0), cost(n, 0.0);
+  std::vector<int> done_at(n, 0);
+  std::vector<char> active(n, 1);
+  for (int it = 0; it < max_outer; ++it) {
+    std::vector<Engine*> cur;
+    std::vector<int> idx;
+    for (int i = 0; i < n; i++)
+      if (active[i]) {
+        cur.push_back(all[i]);
+        idx.push_back(i);
+      }
+    if (cur.empty()) break;
+    if (cur.size() != eng_.size() || !std::equal(cur.begin(), cur.end(), eng_.begin())) {
+      eng_ = cur;
+      dirty_ = true;
+    }
+    std::vector<std::pair<int, int>> iters(cur.size(), std::make_pair(it, 0));
+    int rc = sweep(iters, nullptr);
+    if (rc) return rc;
+    for (size_t k = 0; k < cur.size(); k++) {
+      Engine* e = cur[k];
+      const int i = idx[k];
+      if (e->params().joint_estimation && (rc = e->joint_estimation())) return fail(rc, e->last_error());
+      if (e->params().noise_model && (rc = e->update_weights())) return fail(rc, e->last_error());
+      if ((rc = e->compute_cost(nullptr, &cost[i]))) return fail(rc, e->last_error());
+      done_at[i] = it + 1;
+      if (it > 0 && std::fabs(cost[i] - prev[i]) <= tol * std::fabs(cost[i])) active[i] = 0;
+      prev[i] = cost[i];
+    }
+  }
+  eng_ = all;
+  dirty_ = true;
+  for (int i = 0; i < n; i++) {
+    if (outer_done) outer_done[i] = done_at[i];
+    if (final_cost) final_cost[i] = cost[i];
+  }
+  return MBIR_OK;
+}
+
+}  // namespace mbir

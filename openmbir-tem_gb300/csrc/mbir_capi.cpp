@@ -5,10 +5,18 @@
 #include <string>
 #include <vector>
 
+#include "mbir_batch.h"
+#include "mbir_server.h"
 #include "mbir_engine.h"
 
 struct mbir_engine {
   mbir::Engine* impl;
+};
+struct mbir_batch {
+  mbir::Batch* impl;
+};
+struct mbir_server {
+  mbir::Server* impl;
 };
 
 namespace {
@@ -252,6 +260,129 @@ int32_t mbir_run_multires(const mbir_params* p, const float* counts, const float
     std::memcpy(out, prev.data(), nv * sizeof(float));
   }
   return MBIR_OK;
+}
+
+mbir_batch* mbir_batch_create(int32_t device) {
+  try {
+    auto* b = new mbir_batch;
+    b->impl = new mbir::Batch(device);
+    return b;
+  } catch (...) {
+    return nullptr;
+  }
+}
+void mbir_batch_destroy(mbir_batch* b) {
+  if (!b) return;
+  delete b->impl;
+  delete b;
+}
+int32_t mbir_batch_add(mbir_batch* b, mbir_engine* e) {
+  if (!b || !e || !e->impl) return MBIR_EINVAL;
+  try {
+    return b->impl->add(e->impl);
+  } catch (...) {
+    return MBIR_ENOMEM;
+  }
+}
+int32_t mbir_batch_remove(mbir_batch* b, mbir_engine* e) {
+  if (!b || !e || !e->impl) return MBIR_EINVAL;
+  return b->impl->remove(e->impl);
+}
+int32_t mbir_batch_size(const mbir_batch* b) {
+  return b ? static_cast<int32_t>(b->impl->size()) : 0;
+}
+int32_t mbir_batch_sweep(mbir_batch* b, int32_t outer, double* stats) {
+  if (!b) return MBIR_EINVAL;
+  try {
+    std::vector<std::pair<int, int>> it(b->impl->size(), std::make_pair(outer, 0));
+    return b->impl->sweep(it, stats);
+  } catch (...) {
+    return b->impl->fail(MBIR_ENOMEM, "host allocation failed");
+  }
+}
+int32_t mbir_batch_run(mbir_batch* b, int32_t max_outer, double tol, int32_t* outer_done,
+                       double* final_cost) {
+  if (!b || max_outer < 0) return MBIR_EINVAL;
+  try {
+    std::vector<int> od(b->impl->size());
+    int rc = b->impl->run(max_outer, tol, od.data(), final_cost);
+    if (outer_done)
+      for (size_t i = 0; i < od.size(); i++) outer_done[i] = od[i];
+    return rc;
+  } catch (...) {
+    return b->impl->fail(MBIR_ENOMEM, "host allocation failed");
+  }
+}
+double mbir_batch_last_ms(const mbir_batch* b) { return b ? b->impl->last_ms() : 0.0; }
+double mbir_batch_total_ms(const mbir_batch* b) { return b ? b->impl->total_ms() : 0.0; }
+const char* mbir_batch_last_error(const mbir_batch* b) {
+  return b ? b->impl->last_error() : "null batch";
+}
+
+mbir_server* mbir_server_create(int32_t device, int64_t budget, int32_t max_active) {
+  try {
+    auto* s = new mbir_server;
+    s->impl = new mbir::Server(device, budget, max_active);
+    return s;
+  } catch (...) {
+    return nullptr;
+  }
+}
+void mbir_server_destroy(mbir_server* s) {
+  if (!s) return;
+  delete s->impl;
+  delete s;
+}
+int64_t mbir_server_submit(mbir_server* s, const mbir_params* p, const float* counts,
+                           const float* tilts, int32_t n_theta, int32_t n_r, int32_t n_t,
+                           double dr, double dt, int32_t max_outer, double tol) {
+  if (!s || !p || !counts || !tilts) return MBIR_EINVAL;
+  if (p->struct_size != static_cast<int32_t>(sizeof(mbir_params))) return MBIR_EINVAL;
+  if (p->modality != MBIR_MODALITY_HAADF) return MBIR_ENOTSUP;
+  try {
+    return s->impl->submit(*p, counts, tilts, n_theta, n_r, n_t, dr, dt, max_outer, tol);
+  } catch (...) {
+    return MBIR_ENOMEM;
+  }
+}
+int32_t mbir_server_poll(mbir_server* s, int64_t id, int32_t* state, double* latency_ms,
+                         int32_t* outer_done, double* cost) {
+  if (!s) return MBIR_EINVAL;
+  int st = 0, od = 0;
+  int rc = s->impl->poll(id, &st, latency_ms, &od, cost);
+  if (state) *state = st;
+  if (outer_done) *outer_done = od;
+  return rc;
+}
+int32_t mbir_server_wait(mbir_server* s, int64_t id, double timeout_s) {
+  return s ? s->impl->wait(id, timeout_s) : MBIR_EINVAL;
+}
+int32_t mbir_server_result(mbir_server* s, int64_t id, float* out, int64_t n, int32_t* dims) {
+  return s ? s->impl->result(id, out, n, dims) : MBIR_EINVAL;
+}
+int32_t mbir_server_release(mbir_server* s, int64_t id) {
+  return s ? s->impl->release(id) : MBIR_EINVAL;
+}
+int32_t mbir_server_get_stats(mbir_server* s, mbir_server_stats* st) {
+  if (!s || !st) return MBIR_EINVAL;
+  mbir::ServerStats x;
+  int rc = s->impl->stats(&x);
+  st->submitted = x.submitted;
+  st->completed = x.completed;
+  st->failed = x.failed;
+  st->active = x.active;
+  st->queued = x.queued;
+  st->p50_ms = x.p50_ms;
+  st->p99_ms = x.p99_ms;
+  st->mean_ms = x.mean_ms;
+  st->voxel_updates = x.voxel_updates;
+  st->busy_s = x.busy_s;
+  st->batched_sweep_ms = x.batched_sweep_ms;
+  st->batched_sweeps = x.batched_sweeps;
+  return rc;
+}
+const char* mbir_server_last_error(const mbir_server* s) {
+  return s ? s->impl->last_error() : "null server";
 }
 
 }  // extern "C"

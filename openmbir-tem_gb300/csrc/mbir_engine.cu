@@ -819,6 +819,49 @@ int Engine::sweep(int outer, int inner, double* stats4) {
   return MBIR_OK;
 }
 
+int Engine::batch_args(int outer, int inner, SweepArgs* out, size_t* smem_needed) {
+  if (state_ < 2) return fail(MBIR_ESTATE, "batch: engine not prepared");
+  if (fp64_ || p_.order_mode != MBIR_ORDER_PARALLEL)
+    return fail(MBIR_ENOTSUP, "batch: FP32 parallel-order engines only");
+  const Geometry& g = g_;
+  std::vector<int32_t> rows;
+  row_order_for_sweep(sweeps_done_, rows);
+  if (cudaMemcpy(d_rows_, rows.data(), sizeof(int) * g.n_z, cudaMemcpyHostToDevice) != cudaSuccess)
+    return cuda_check(MBIR_EDEVICE, "batch row order");
+  SweepArgs a{};
+  a.g = dg_;
+  a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_, d_lineok_};
+  a.flt = flt_;
+  a.x = d_x_;
+  a.e = d_e_;
+  a.row_order = d_rows_;
+  a.stride = stride_;
+  a.mode = kModeICD;
+  a.fp64 = 0;
+  a.iter_nonzero = (inner > 0 || outer > 0) ? 1 : 0;
+  a.zero_skipping = p_.zero_skipping;
+  a.smem_rows = stage_ ? 1 : 0;
+  a.n_rs = stage_ ? n_rs_ : 0;
+  a.err = d_err_;
+  a.stats = d_stats_;
+  a.colour = 0;
+  a.n_slices = (g.n_y + 1) / 2;
+  *out = a;
+  if (smem_needed) *smem_needed = smem_bytes_;
+  return MBIR_OK;
+}
+
+int Engine::batch_finish(int outer, int inner, const double* st, double ms) {
+  icd_ms_ += ms;
+  sweeps_done_++;
+  visited_ += static_cast<int64_t>(st[2] + st[3]);
+  updated_ += static_cast<int64_t>(st[3]);
+  last_rel_ = st[1] > 0 ? st[0] / st[1] : 0.0;
+  outer_ = outer;
+  inner_ = inner;
+  return MBIR_OK;
+}
+
 // jointEstimation, gain + offset branch (HAADF_ReconstructionEngine_Extra.cpp:419-636)
 int Engine::joint_estimation() {
   if (state_ < 2) return fail(MBIR_ESTATE, "joint_estimation: call prepare first");

@@ -84,6 +84,21 @@ class Engine {
 
   const Geometry& geometry() const { return g_; }
 
+  // Hooks for the batched sweep (mbir_batch.cu).  batch_args fills the sweep arguments of this
+  // engine's next parallel-order sweep (uploading its row order) and reports the shared memory
+  // a staged slice needs; batch_finish records a sweep that ran inside a batch.
+  int batch_args(int outer, int inner, SweepArgs* out, size_t* smem_needed);
+  int batch_finish(int outer, int inner, const double* st4, double ms);
+  double* slice_stats() const { return d_stats_; }
+  double* sweep_stats() const { return d_stat4_; }
+  int* error_word() const { return d_err_; }
+  int nb() const { return nb_; }
+  bool fp64() const { return fp64_ != 0; }
+  const mbir_params& params() const { return p_; }
+  int state() const { return state_; }
+  int sweeps_done() const { return sweeps_done_; }
+  int check_errors() { return check_device_error(); }
+
  private:
   int build_host();  // geometry, tables, stride, initial nuisance: no GPU needed
   int build_geometry();

@@ -70,6 +70,16 @@ struct SweepArgs {
   int* err;              // device error word
 };
 
+// Batched sweep: per-series sweep arguments and a queue of (series, slice y) items.
+struct BatchArgs {
+  const SweepArgs* series;   // [n_series] in device memory (colour field unused)
+  const int2* items;         // [n_items] (series, y): colour-0 items first, then colour-1
+  int n_items;
+  int* queue;                // item counter (zeroed before the launch)
+  int* done;                 // [n_series] finished colour-0 slices (zeroed before the launch)
+  const int* need;           // [n_series] number of colour-0 slices
+};
+
 struct RefOrderArgs {
   DevGeom g;
   DevTables tab;
@@ -92,6 +102,9 @@ int launch_sweep_f32_smem(const SweepArgs& a, int nb, size_t smem_bytes, void* s
 int launch_sweep_f32_hbm(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_sweep_f64(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_ref_order_f32(const RefOrderArgs& a, int nb, void* stream);
+// persistent batched sweep (FP32, slices staged or in HBM per series); vpl from max n_theta
+int launch_batch_sweep(const BatchArgs& b, int nb, int vpl, size_t smem_bytes, int grid,
+                       void* stream);
 int launch_ref_order_f64(const RefOrderArgs& a, int nb, void* stream);
 int launch_sino_to_dev(const float* host_layout, void* dev_layout, int n_theta, int n_r, int n_rp,
                        int n_t, int fp64, void* stream);

@@ -1,0 +1,290 @@
+// mbir_server.cpp -- continuous-batching reconstruction server.
+//
+// Requests (a tilt series + parameters) are queued by submit(); one worker thread owns the GPU.
+// Between batched sweeps it admits queued requests in arrival order while their estimated
+// device footprint fits the memory budget and a slot is free (each admitted request is
+// prepared: upload, tables, forward projection, and stays resident), runs one outer iteration
+// for every active request (one persistent batched ICD sweep, then per-request gain/offset,
+// variance and FP64 cost), and retires requests whose relative cost change fell below their
+// tolerance (or that reached max_outer), copying their volume to host memory and freeing the
+// device memory for the next arrivals.  Latency = completion - submission.
+#include "mbir_server.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+
+namespace mbir {
+
+namespace {
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
+Server::Server(int device, int64_t mem_budget, int max_active)
+    : device_(device), budget_(mem_budget), max_active_(max_active > 0 ? max_active : 64) {
+  if (budget_ <= 0) {
+    size_t free_b = 0, total_b = 0;
+    cudaSetDevice(device_);
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+      budget_ = static_cast<int64_t>(free_b * 0.8);
+    else
+      budget_ = int64_t(8) << 30;
+  }
+  worker_ = std::thread([this] { loop(); });
+}
+
+Server::~Server() {
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    stop_ = true;
+  }
+  cv_.notify_all();
+  if (worker_.joinable()) worker_.join();
+  batch_.reset();
+  for (auto& kv : all_) kv.second->engine.reset();
+}
+
+size_t Server::estimate_bytes(const Request& r) const {
+  const size_t rb = r.params.precision == MBIR_PRECISION_FP64 ? 8 : 4;
+  const size_t n_rp = (static_cast<size_t>(r.n_r) + 3) / 4 * 4;
+  const size_t sino = static_cast<size_t>(r.n_t) * r.n_theta * n_rp;
+  const size_t vox = static_cast<size_t>(r.dims[0]) * r.dims[1] * r.dims[2];
+  const size_t host_layout = std::max(static_cast<size_t>(r.n_theta) * r.n_r * r.n_t, vox) * 4;
+  return rb * (3 * sino + vox) + host_layout + (1u << 20);
+}
+
+int64_t Server::submit(const mbir_params& p, const float* counts, const float* tilts, int n_theta,
+                       int n_r, int n_t, double delta_r, double delta_t, int max_outer,
+                       double tol) {
+  auto r = std::make_unique<Request>();
+  r->params = p;
+  r->params.device = device_;
+  r->params.order_mode = MBIR_ORDER_PARALLEL;
+  r->params.precision = MBIR_PRECISION_FP32;
+  r->n_theta = n_theta;
+  r->n_r = n_r;
+  r->n_t = n_t;
+  r->delta_r = delta_r;
+  r->delta_t = delta_t;
+  r->max_outer = max_outer > 0 ? max_outer : 1;
+  r->tol = tol;
+  r->engine = std::make_unique<Engine>(r->params);
+  int rc = r->engine->set_sinogram(counts, tilts, n_theta, n_r, n_t, delta_r, delta_t);
+  int32_t d[6];
+  if (rc == 0) rc = r->engine->dims(d);
+  if (rc) {
+    err_ = r->engine->last_error();
+    return rc;
+  }
+  r->dims[0] = d[0];
+  r->dims[1] = d[1];
+  r->dims[2] = d[2];
+  r->bytes = estimate_bytes(*r);
+  r->t_submit = now_s();
+  std::lock_guard<std::mutex> lk(mu_);
+  if (static_cast<int64_t>(r->bytes) > budget_) {
+    err_ = "request larger than the server's device-memory budget";
+    return MBIR_ENOMEM;
+  }
+  r->id = next_id_++;
+  const int64_t id = r->id;
+  queue_.push_back(r.get());
+  all_[id] = std::move(r);
+  stats_.submitted++;
+  cv_.notify_all();
+  return id;
+}
+
+int Server::admit_locked(std::vector<Request*>& admitted) {
+  while (!queue_.empty() &&
+         static_cast<int>(active_.size() + admitted.size()) < max_active_) {
+    Request* r = queue_.front();
+    if (used_ + static_cast<int64_t>(r->bytes) > budget_) break;  // arrival order: no overtaking
+    queue_.pop_front();
+    used_ += static_cast<int64_t>(r->bytes);
+    admitted.push_back(r);
+  }
+  return 0;
+}
+
+void Server::retire(Request* r, int code, const std::string& msg) {
+  // called with mu_ held
+  r->t_done = now_s();
+  r->state = code == 0 ? 2 : code;
+  r->error = msg;
+  used_ -= static_cast<int64_t>(r->bytes);
+  if (code == 0) {
+    stats_.completed++;
+    latencies_ms_.push_back((r->t_done - r->t_submit) * 1e3);
+  } else {
+    stats_.failed++;
+  }
+  done_cv_.notify_all();
+}
+
+void Server::loop() {
+  cudaSetDevice(device_);
+  batch_ = std::make_unique<Batch>(device_);
+  std::unique_lock<std::mutex> lk(mu_);
+  for (;;) {
+    cv_.wait(lk, [&] { return stop_ || !queue_.empty() || !active_.empty(); });
+    if (stop_) break;
+    std::vector<Request*> admitted;
+    admit_locked(admitted);
+    lk.unlock();
+    const double t_busy0 = now_s();
+    std::vector<std::pair<Request*, std::string>> failed;
+    std::vector<Request*> ok;
+    for (Request* r : admitted) {
+      r->t_admit = now_s();
+      int rc = r->engine->prepare();
+      if (rc == 0) rc = batch_->add(r->engine.get());
+      if (rc)
+        failed.emplace_back(r, r->engine->last_error());
+      else
+        ok.push_back(r);
+    }
+    lk.lock();
+    for (auto& f : failed) retire(f.first, MBIR_EDEVICE, f.second);
+    for (Request* r : ok) {
+      r->state = 1;
+      active_.push_back(r);
+    }
+    std::vector<Request*> cur = active_;
+    lk.unlock();
+
+    std::vector<Request*> finished;
+    std::vector<std::pair<Request*, std::string>> broken;
+    if (!cur.empty()) {
+      // the batch keeps engines in insertion order; map each to its own outer index
+      std::vector<std::pair<int, int>> iters;
+      iters.reserve(cur.size());
+      for (Request* r : cur) iters.emplace_back(r->outer_done, 0);
+      int rc = batch_->sweep(iters, nullptr);
+      if (rc) {
+        for (Request* r : cur) broken.emplace_back(r, batch_->last_error());
+      } else {
+        for (Request* r : cur) {
+          Engine* e = r->engine.get();
+          int erc = 0;
+          if (r->params.joint_estimation) erc = e->joint_estimation();
+          if (!erc && r->params.noise_model) erc = e->update_weights();
+          double c = 0;
+          if (!erc) erc = e->compute_cost(nullptr, &c);
+          if (erc) {
+            broken.emplace_back(r, e->last_error());
+            continue;
+          }
+          r->outer_done++;
+          const bool conv = r->outer_done > 1 && std::fabs(c - r->cost) <= r->tol * std::fabs(c);
+          r->prev_cost = r->cost;
+          r->cost = c;
+          if (conv || r->outer_done >= r->max_outer) finished.push_back(r);
+        }
+      }
+      for (Request* r : finished) {
+        r->result.resize(static_cast<size_t>(r->dims[0]) * r->dims[1] * r->dims[2]);
+        r->engine->get_volume(r->result.data(), static_cast<int64_t>(r->result.size()));
+      }
+    }
+    lk.lock();
+    stats_.busy_s += now_s() - t_busy0;
+    stats_.batched_sweeps = batch_->sweeps();
+    stats_.batched_sweep_ms = batch_->total_ms();
+    auto drop = [&](Request* r) {
+      batch_->remove(r->engine.get());
+      mbir_status st{};
+      r->engine->status(&st);
+      stats_.voxel_updates += static_cast<double>(st.voxels_visited);
+      r->engine.reset();
+      active_.erase(std::remove(active_.begin(), active_.end(), r), active_.end());
+    };
+    for (Request* r : finished) {
+      drop(r);
+      retire(r, 0, "");
+    }
+    for (auto& b : broken) {
+      drop(b.first);
+      retire(b.first, MBIR_EDEVICE, b.second);
+    }
+  }
+}
+
+int Server::poll(int64_t id, int* state, double* latency_ms, int* outer_done, double* cost) {
+  std::lock_guard<std::mutex> lk(mu_);
+  auto it = all_.find(id);
+  if (it == all_.end()) return MBIR_EINVAL;
+  Request* r = it->second.get();
+  if (state) *state = r->state;
+  if (latency_ms) *latency_ms = r->state == 2 ? (r->t_done - r->t_submit) * 1e3 : -1.0;
+  if (outer_done) *outer_done = r->outer_done;
+  if (cost) *cost = r->cost;
+  return MBIR_OK;
+}
+
+int Server::wait(int64_t id, double timeout_s) {
+  std::unique_lock<std::mutex> lk(mu_);
+  auto it = all_.find(id);
+  if (it == all_.end()) return MBIR_EINVAL;
+  Request* r = it->second.get();
+  const auto deadline = std::chrono::steady_clock::now() +
+                        std::chrono::duration_cast<std::chrono::steady_clock::duration>(
+                            std::chrono::duration<double>(timeout_s));
+  if (!done_cv_.wait_until(lk, deadline, [&] { return r->state == 2 || r->state < 0; }))
+    return MBIR_ETIMEOUT;
+  return r->state == 2 ? MBIR_OK : r->state;
+}
+
+int Server::result(int64_t id, float* out, int64_t n, int32_t* dims) {
+  std::lock_guard<std::mutex> lk(mu_);
+  auto it = all_.find(id);
+  if (it == all_.end()) return MBIR_EINVAL;
+  Request* r = it->second.get();
+  if (r->state != 2) return r->state < 0 ? r->state : MBIR_ESTATE;
+  if (dims)
+    for (int i = 0; i < 3; i++) dims[i] = r->dims[i];
+  if (out) {
+    if (n < static_cast<int64_t>(r->result.size())) return MBIR_EINVAL;
+    std::copy(r->result.begin(), r->result.end(), out);
+  }
+  return MBIR_OK;
+}
+
+int Server::release(int64_t id) {
+  std::lock_guard<std::mutex> lk(mu_);
+  auto it = all_.find(id);
+  if (it == all_.end()) return MBIR_EINVAL;
+  if (it->second->state == 0 || it->second->state == 1) return MBIR_ESTATE;
+  all_.erase(it);
+  return MBIR_OK;
+}
+
+int Server::stats(ServerStats* st) {
+  std::lock_guard<std::mutex> lk(mu_);
+  ServerStats s = stats_;
+  s.active = static_cast<int32_t>(active_.size());
+  s.queued = static_cast<int32_t>(queue_.size());
+  if (!latencies_ms_.empty()) {
+    std::vector<double> v = latencies_ms_;
+    std::sort(v.begin(), v.end());
+    auto pct = [&](double q) {
+      const double pos = q * (v.size() - 1);
+      const size_t i = static_cast<size_t>(pos);
+      const double f = pos - i;
+      return i + 1 < v.size() ? v[i] * (1 - f) + v[i + 1] * f : v[i];
+    };
+    s.p50_ms = pct(0.5);
+    s.p99_ms = pct(0.99);
+    double m = 0;
+    for (double x : v) m += x;
+    s.mean_ms = m / v.size();
+  }
+  *st = s;
+  return MBIR_OK;
+}
+
+}  // namespace mbir

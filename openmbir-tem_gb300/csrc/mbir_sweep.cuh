@@ -456,13 +456,17 @@ __host__ __device__ inline SmemLayout smem_layout(int n_theta, int n_x, int n_rs
   return L;
 }
 
+// One voxel slice y of one reconstruction, processed by the whole CTA: stage the slice's
+// detector rows, walk the z-rows, update every conflict-free class, store the rows back.
+// `phase` is the parity of the CTA's mbarrier (it alternates when a CTA processes several
+// slices); `coherent` makes neighbour-row loads bypass L1 (needed when other CTAs of the same
+// launch write neighbouring slices).  Writes the slice's four statistics to stat_out when it
+// is not null.  Returns false when a bounded wait gave up (A.err is set).
 template <typename Real, int NB, int G, int VPL, bool STAGE>
-__global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
+__device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned char* smem,
+                                          uint32_t& phase, bool coherent, double* stat_out) {
   using R2 = typename V2<Real>::type;
-  extern __shared__ __align__(128) unsigned char smem[];
   const DevGeom& g = A.g;
-  const int y = A.colour + 2 * static_cast<int>(blockIdx.x);
-  if (y >= g.n_y) return;
   const int tid = threadIdx.x, nthreads = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31;
   constexpr int GPW = 32 / G;  // voxel groups per warp
@@ -509,11 +513,6 @@ __global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
       for (int i = tid; i < tcount * ps; i += nthreads) es[i] = Real(0);
       __syncthreads();
     } else {
-      if (tid == 0) {
-        mbar_init(bar, 1);
-        fence_mbar_init();
-      }
-      __syncthreads();
       if (tid == 0) mbar_expect_tx(bar, static_cast<uint32_t>(rows) * row_bytes);
       __syncthreads();
       for (int r = tid; r < rows; r += nthreads) {
@@ -523,11 +522,12 @@ __global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
                      static_cast<size_t>(v) * g.n_rp,
                  row_bytes, bar);
       }
-      const bool ok = mbar_wait(bar, 0);
+      const bool ok = mbar_wait(bar, phase);
+      phase ^= 1u;
       if (!__syncthreads_and(ok)) {
         if (tid == 0) atomicOr(A.err, 1);
-        mbar_wait(bar, 0);  // give copies still in flight a second bounded chance to land
-        return;
+        mbar_wait(bar, phase ^ 1u);  // give copies still in flight a second bounded chance
+        return false;
       }
     }
   } else {
@@ -567,8 +567,10 @@ __global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
       const int r = i / g.n_x, xx = i - r * g.n_x;
       const int yy = y + r / 3 - 1, zz = z + r % 3 - 1;
       Real v = Real(0);
-      if (yy >= 0 && yy < g.n_y && zz >= 0 && zz < g.n_z)
-        v = gx[static_cast<size_t>(yy) * vplane + static_cast<size_t>(zz) * g.n_x + xx];
+      if (yy >= 0 && yy < g.n_y && zz >= 0 && zz < g.n_z) {
+        const Real* src = gx + static_cast<size_t>(yy) * vplane + static_cast<size_t>(zz) * g.n_x + xx;
+        v = coherent ? __ldcg(src) : *src;
+      }
       cache[i] = v;
     }
     __syncthreads();
@@ -595,7 +597,7 @@ __global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
     bulk_commit();
     bulk_wait_all();
   }
-  if (A.stats != nullptr) {
+  if (stat_out != nullptr) {
     const int gl = lane & (G - 1);
     if (gl == 0)
       for (int s = 0; s < kStatSlots; ++s) sstat[group * kStatSlots + s] = wst[s];
@@ -603,7 +605,88 @@ __global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
     if (tid < kStatSlots) {
       double acc = 0.0;
       for (int w = 0; w < n_groups; ++w) acc += sstat[w * kStatSlots + tid];
-      A.stats[static_cast<size_t>(blockIdx.x) * kStatSlots + tid] = acc;
+      stat_out[tid] = acc;
+    }
+  }
+  __syncthreads();
+  return true;
+}
+
+__device__ __forceinline__ void init_slice_barrier(unsigned char* smem) {
+  if (threadIdx.x == 0) {
+    mbar_init(reinterpret_cast<uint64_t*>(smem), 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+}
+
+// One launch = the slices of one y-colour of one reconstruction, one CTA per slice.
+template <typename Real, int NB, int G, int VPL, bool STAGE>
+__global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int y = A.colour + 2 * static_cast<int>(blockIdx.x);
+  if (y >= A.g.n_y) return;
+  init_slice_barrier(smem);
+  uint32_t phase = 0;
+  run_slice<Real, NB, G, VPL, STAGE>(
+      A, y, smem, phase, false,
+      A.stats != nullptr ? A.stats + static_cast<size_t>(blockIdx.x) * kStatSlots : nullptr);
+}
+
+// Many reconstructions of uneven size in one persistent launch per sweep (FP32).  CTAs pull
+// (series, slice) items from a queue: first every colour-0 slice, then every colour-1 slice.
+// A colour-1 slice needs the colour-0 neighbours y+-1 of its own series, so it waits (with a
+// time bound) until all colour-0 slices of that series are done; those were taken from the
+// queue earlier by running CTAs, so the wait always ends.  Launched cooperatively so every CTA
+// is resident.
+template <int NB, int G, int VPL>
+__global__ void __launch_bounds__(kWarps * 32, 1) batch_sweep_kernel(BatchArgs B) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ SweepArgs sA;
+  __shared__ int s_item;
+  __shared__ int s_wait_ok;
+  init_slice_barrier(smem);
+  uint32_t phase = 0;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(B.queue, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= B.n_items) break;
+    const int2 it = B.items[item];
+    const int s = it.x, y = it.y;
+    if (threadIdx.x == 0) {
+      sA = B.series[s];
+      int ok = 1;
+      if (y & 1) {
+        const uint64_t t0 = global_ns();
+        unsigned ns = 64;
+        for (;;) {
+          int done;
+          asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(done) : "l"(B.done + s) : "memory");
+          if (done >= B.need[s]) break;
+          if (global_ns() - t0 > kWaitNs * 5) {
+            ok = 0;
+            atomicOr(B.series[s].err, 2);
+            break;
+          }
+          __nanosleep(ns);
+          if (ns < 4096) ns <<= 1;
+        }
+      }
+      s_wait_ok = ok;
+    }
+    __syncthreads();
+    if (!s_wait_ok) continue;
+    const int n0 = (sA.g.n_y + 1) / 2;
+    const int slot = (y & 1) ? n0 + (y >> 1) : (y >> 1);
+    double* stat_out = sA.stats + static_cast<size_t>(slot) * kStatSlots;
+    if (sA.smem_rows)
+      run_slice<float, NB, G, VPL, true>(sA, y, smem, phase, true, stat_out);
+    else
+      run_slice<float, NB, G, VPL, false>(sA, y, smem, phase, true, stat_out);
+    if (threadIdx.x == 0 && !(y & 1)) {
+      __threadfence();
+      atomicAdd(B.done + s, 1);
     }
   }
 }
@@ -680,6 +763,27 @@ int launch_sweep_t(const SweepArgs& a, size_t smem, cudaStream_t s) {
   if (e != cudaSuccess) return -3;
   k<<<a.n_slices, kWarps * 32, smem, s>>>(a);
   return ok_or(cudaGetLastError());
+}
+
+template <int NB, int G, int VPL>
+int launch_batch_t(const BatchArgs& b, size_t smem, int grid, cudaStream_t s) {
+  auto k = batch_sweep_kernel<NB, G, VPL>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem));
+  if (e != cudaSuccess) return -3;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kWarps * 32, smem) != cudaSuccess ||
+      per_sm < 1)
+    return -3;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (grid <= 0 || grid > per_sm * sms) grid = per_sm * sms;
+  BatchArgs arg = b;
+  void* params[] = {&arg};
+  e = cudaLaunchCooperativeKernel(reinterpret_cast<void*>(k), dim3(grid), dim3(kWarps * 32), params,
+                                  smem, s);
+  return ok_or(e);
 }
 
 template <typename Real, int NB, int VPL>

@@ -18,6 +18,19 @@ int launch_sweep_f32_smem(const SweepArgs& a, int nb, size_t smem, void* stream)
   return -7;
 }
 
+int launch_batch_sweep(const BatchArgs& b, int nb, int vpl, size_t smem, int grid,
+                       void* stream) {
+  using namespace sweep;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (nb == 3 && vpl == 4) return launch_batch_t<3, 16, 4>(b, smem, grid, s);
+  if (nb == 3 && vpl == 8) return launch_batch_t<3, 16, 8>(b, smem, grid, s);
+  if (nb == 3 && vpl == 10) return launch_batch_t<3, 16, 10>(b, smem, grid, s);
+  if (nb == 5 && vpl == 4) return launch_batch_t<5, 16, 4>(b, smem, grid, s);
+  if (nb == 5 && vpl == 8) return launch_batch_t<5, 16, 8>(b, smem, grid, s);
+  if (nb == 5 && vpl == 10) return launch_batch_t<5, 16, 10>(b, smem, grid, s);
+  return -7;
+}
+
 int launch_ref_order_f32(const RefOrderArgs& a, int nb, void* stream) {
   using namespace sweep;
   cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -93,6 +93,15 @@ class MbirStatus(C.Structure):
     ]
 
 
+class MbirServerStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
+        ("active", C.c_int32), ("queued", C.c_int32), ("p50_ms", C.c_double),
+        ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("voxel_updates", C.c_double),
+        ("busy_s", C.c_double), ("batched_sweep_ms", C.c_double), ("batched_sweeps", C.c_int64),
+    ]
+
+
 _lib = None
 
 _F = C.POINTER(C.c_float)
@@ -127,6 +136,27 @@ SIGNATURES = {
     "mbir_status_get": (C.c_int32, [C.c_void_p, C.POINTER(MbirStatus)]),
     "mbir_cancel": (None, [C.c_void_p]),
     "mbir_write_outputs": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_char_p]),
+    "mbir_batch_create": (C.c_void_p, [C.c_int32]),
+    "mbir_batch_destroy": (None, [C.c_void_p]),
+    "mbir_batch_add": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "mbir_batch_remove": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "mbir_batch_size": (C.c_int32, [C.c_void_p]),
+    "mbir_batch_sweep": (C.c_int32, [C.c_void_p, C.c_int32, _D]),
+    "mbir_batch_run": (C.c_int32, [C.c_void_p, C.c_int32, C.c_double, _I, _D]),
+    "mbir_batch_last_ms": (C.c_double, [C.c_void_p]),
+    "mbir_batch_total_ms": (C.c_double, [C.c_void_p]),
+    "mbir_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "mbir_server_create": (C.c_void_p, [C.c_int32, C.c_int64, C.c_int32]),
+    "mbir_server_destroy": (None, [C.c_void_p]),
+    "mbir_server_submit": (C.c_int64, [C.c_void_p, C.POINTER(MbirParams), _F, _F, C.c_int32,
+                                       C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32,
+                                       C.c_double]),
+    "mbir_server_poll": (C.c_int32, [C.c_void_p, C.c_int64, _I, _D, _I, _D]),
+    "mbir_server_wait": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double]),
+    "mbir_server_result": (C.c_int32, [C.c_void_p, C.c_int64, _F, C.c_int64, _I]),
+    "mbir_server_release": (C.c_int32, [C.c_void_p, C.c_int64]),
+    "mbir_server_get_stats": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "mbir_server_last_error": (C.c_char_p, [C.c_void_p]),
     "mbir_run_multires": (C.c_int32, [C.POINTER(MbirParams), _F, _F, C.c_int32, C.c_int32,
                                       C.c_int32, C.c_double, C.c_double, _F, C.c_int64, _I]),
 }
@@ -300,6 +330,128 @@ class Engine:
     def write_outputs(self, directory, mrc_path=""):
         return self._check(lib().mbir_write_outputs(self._h, str(directory).encode(),
                                                     str(mrc_path).encode()))
+
+
+class Batch:
+    """Many prepared FP32 engines advanced together (mbir_batch*)."""
+
+    def __init__(self, device=0):
+        self._h = lib().mbir_batch_create(device)
+        if not self._h:
+            raise MbirError(-2, "mbir_batch_create failed")
+        self.engines = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mbir_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != MBIR_OK:
+            raise MbirError(rc, lib().mbir_batch_last_error(self._h).decode())
+        return rc
+
+    def add(self, engine):
+        self._check(lib().mbir_batch_add(self._h, engine._h))
+        self.engines.append(engine)
+
+    def remove(self, engine):
+        self._check(lib().mbir_batch_remove(self._h, engine._h))
+        self.engines.remove(engine)
+
+    def sweep(self, outer=0):
+        st = np.zeros((len(self.engines), 4))
+        self._check(lib().mbir_batch_sweep(self._h, outer, _dp(st)))
+        return st
+
+    def run(self, max_outer, tol):
+        n = len(self.engines)
+        od = np.zeros(n, np.int32)
+        fc = np.zeros(n)
+        self._check(lib().mbir_batch_run(self._h, max_outer, tol, od.ctypes.data_as(_I), _dp(fc)))
+        return od, fc
+
+    def last_ms(self):
+        return lib().mbir_batch_last_ms(self._h)
+
+    def total_ms(self):
+        return lib().mbir_batch_total_ms(self._h)
+
+
+class Server:
+    """Continuous-batching reconstruction server on one device (mbir_server*)."""
+
+    def __init__(self, device=0, mem_budget=0, max_active=0):
+        self._h = lib().mbir_server_create(device, mem_budget, max_active)
+        if not self._h:
+            raise MbirError(-2, "mbir_server_create failed")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mbir_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, params, counts, tilts_deg, delta_r=1.0, delta_t=1.0, max_outer=20,
+               tol=1e-4):
+        counts = np.ascontiguousarray(counts, np.float32)
+        tilts = np.ascontiguousarray(tilts_deg, np.float32)
+        nt, nr, ntt = counts.shape
+        rid = lib().mbir_server_submit(self._h, C.byref(params), _fp(counts), _fp(tilts), nt, nr,
+                                       ntt, delta_r, delta_t, max_outer, tol)
+        if rid <= 0:
+            raise MbirError(int(rid), lib().mbir_server_last_error(self._h).decode())
+        return rid
+
+    def poll(self, rid):
+        st, od = C.c_int32(), C.c_int32()
+        lat, cost = C.c_double(), C.c_double()
+        rc = lib().mbir_server_poll(self._h, rid, C.byref(st), C.byref(lat), C.byref(od),
+                                    C.byref(cost))
+        if rc != MBIR_OK:
+            raise MbirError(rc, "poll")
+        return st.value, lat.value, od.value, cost.value
+
+    def wait(self, rid, timeout=600.0):
+        rc = lib().mbir_server_wait(self._h, rid, timeout)
+        if rc != MBIR_OK:
+            raise MbirError(rc, lib().mbir_server_last_error(self._h).decode())
+
+    def result(self, rid):
+        dims = np.zeros(3, np.int32)
+        rc = lib().mbir_server_result(self._h, rid, None, 0, dims.ctypes.data_as(_I))
+        if rc != MBIR_OK:
+            raise MbirError(rc, "result")
+        out = np.empty(tuple(int(d) for d in dims), np.float32)
+        rc = lib().mbir_server_result(self._h, rid, _fp(out), out.size, dims.ctypes.data_as(_I))
+        if rc != MBIR_OK:
+            raise MbirError(rc, "result")
+        return out
+
+    def release(self, rid):
+        return lib().mbir_server_release(self._h, rid)
+
+    def stats(self):
+        st = MbirServerStats()
+        lib().mbir_server_get_stats(self._h, C.byref(st))
+        return st
 
 
 def run_multires(params, counts, tilts_deg, delta_r=1.0, delta_t=1.0):

@@ -174,3 +174,30 @@ def test_mrc_errors(lib_built, tmp_path):
         bad.write_bytes(b"\0" * 100)
         with pytest.raises(mbir.MbirError):
             e.load_mrc(bad)
+
+
+def test_server_reports_device_failure_without_gpu(lib_built):
+    """Failure path of the serving loop, exercised on the host: with no usable device the
+    request is admitted, its preparation fails, and it is retired with an error code instead of
+    hanging the queue."""
+    import conftest
+    if conftest.has_gpu():
+        pytest.skip("a GPU is present: the failure path needs a host without one")
+    mbir = lib_built
+    y, ang, th = small_case(n_r=32, n_t=4)
+    with mbir.Server(0, 1 << 30, 0) as s:
+        rid = s.submit(haadf_params(mbir, th), y, ang, max_outer=2, tol=0.0)
+        with pytest.raises(mbir.MbirError):
+            s.wait(rid, timeout=30.0)
+        state = s.poll(rid)[0]
+        assert state < 0
+        assert s.stats().failed == 1
+
+
+def test_server_rejects_oversized_request(lib_built):
+    mbir = lib_built
+    y, ang, th = small_case(n_r=32, n_t=4)
+    with mbir.Server(0, 1024, 0) as s:
+        with pytest.raises(mbir.MbirError) as ei:
+            s.submit(haadf_params(mbir, th), y, ang)
+        assert ei.value.code == -2

@@ -1,0 +1,61 @@
+"""Served stream: requests admitted by device memory with continuous batching.  Each result must
+be the same when the request is served alone and when it shares the device with others."""
+import time
+
+import numpy as np
+import pytest
+
+from conftest import haadf_params
+from test_gpu_batch import CASES, series
+
+pytestmark = pytest.mark.gpu
+
+
+def requests(mbir):
+    out = []
+    for (seed, n_r, n_t, views, mx, th) in CASES:
+        y, ang, th = series(mbir, seed, n_r, n_t, views, mx, th)
+        out.append((haadf_params(mbir, th), y, ang))
+    return out
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a.astype(np.float64) - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_results_same_alone_and_in_the_mix(lib_built):
+    mbir = lib_built
+    reqs = requests(mbir)
+    alone = []
+    with mbir.Server(0, 0, 1) as s:  # one request on the device at a time
+        for p, y, ang in reqs:
+            rid = s.submit(p, y, ang, max_outer=12, tol=1e-4)
+            s.wait(rid)
+            alone.append((s.result(rid), s.poll(rid)[2]))
+    with mbir.Server(0, 0, 0) as s:
+        ids = []
+        for p, y, ang in reqs:  # staggered arrivals: later requests join a running batch
+            ids.append(s.submit(p, y, ang, max_outer=12, tol=1e-4))
+            time.sleep(0.01)
+        for rid in ids:
+            s.wait(rid)
+        mixed = [(s.result(rid), s.poll(rid)[2]) for rid in ids]
+        st = s.stats()
+        assert st.completed == len(reqs) and st.failed == 0
+        assert 0 < st.p50_ms <= st.p99_ms
+    for (va, na), (vm, nm) in zip(alone, mixed):
+        assert na == nm
+        assert rel(vm, va) <= 1e-5
+
+
+def test_admission_respects_memory_budget(lib_built):
+    mbir = lib_built
+    reqs = requests(mbir)
+    # a budget that fits about one request forces one-at-a-time admission, in arrival order
+    with mbir.Server(0, 24 << 20, 0) as s:
+        ids = [s.submit(p, y, ang, max_outer=3, tol=0.0) for p, y, ang in reqs]
+        for rid in ids:
+            s.wait(rid)
+        lat = [s.poll(rid)[1] for rid in ids]
+        assert all(l > 0 for l in lat)
+        assert lat == sorted(lat)
