@@ -18,6 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmbir_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["mbir_sweep_f32.cu", "mbir_sweep_f32_hbm.cu", "mbir_sweep_f64.cu", "mbir_kernels.cu",
+           "mbir_exact.cu",
            "mbir_engine.cu", "mbir_batch.cu", "mbir_server.cpp", "mrc_io.cpp",
            "mbir_capi.cpp"]
 HEADERS = ["mbir_internal.h", "mbir_engine.h", "mbir_sweep.cuh", "mbir_batch.h",
@@ -46,8 +47,13 @@ def _compile(src, verbose=False, ptxas_v=False):
     cmd = [nvcc(), "-std=c++17", "-O3", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
            "-I", CSRC, "-I", os.path.join(ROOT, "include"), "-c", os.path.join(CSRC, src),
            "-o", obj]
+    # host arithmetic must not be contracted into FMAs (the FP64 tables and per-view solves
+    # are compared bit for bit with the oracle on every host architecture)
+    cmd[1:1] = ["-Xcompiler", "-ffp-contract=off"]
     if src.endswith(".cu"):
         cmd[1:1] = ARCH + ["-lineinfo", "--expt-relaxed-constexpr"]
+        if src == "mbir_exact.cu":
+            cmd[1:1] = ["-fmad=false"]
         if ptxas_v:
             cmd.insert(1, "-Xptxas=-v")
     else:

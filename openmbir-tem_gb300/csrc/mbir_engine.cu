@@ -85,6 +85,7 @@ void reference_visit_order(uint32_t seed, int n_z, int n_x, std::vector<int32_t>
 Engine::Engine(const mbir_params& p) : p_(p) {
   if (p_.qggmrf_q == 0.0) p_.qggmrf_q = p_.diffuseness + 1.0;
   fp64_ = p_.precision == MBIR_PRECISION_FP64 ? 1 : 0;
+  exact_ = fp64_ && p_.order_mode == MBIR_ORDER_REFERENCE;
   rb_ = fp64_ ? sizeof(double) : sizeof(float);
   bins_ = p_.detector_response_bins > 0 ? p_.detector_response_bins : 64;
 }
@@ -108,6 +109,9 @@ void Engine::release() {
   dfree(d_hval_);
   dfree(d_rows_);
   dfree(d_lineok_);
+  dfree(d_cosv_);
+  dfree(d_sinv_);
+  dfree(d_Href_);
   dfree(d_lines_);
   dfree(d_stats_);
   dfree(d_stat4_);
@@ -501,6 +505,9 @@ int Engine::alloc_device() {
   rc |= dmalloc_bytes(&d_hval_, static_cast<size_t>(g.n_y) * kMaxTRows * rb_);
   rc |= dmalloc(&d_rows_, g.n_z);
   rc |= dmalloc(&d_lineok_, static_cast<size_t>(g.n_z) * g.n_x);
+  rc |= dmalloc(&d_cosv_, g.n_theta);
+  rc |= dmalloc(&d_sinv_, g.n_theta);
+  rc |= dmalloc(&d_Href_, static_cast<size_t>(g.n_theta) * bins_);
   rc |= dmalloc(&d_lines_, static_cast<size_t>(g.n_z) * g.n_x);
   rc |= dmalloc(&d_stats_, static_cast<size_t>((g.n_y + 1) / 2 + 1) * kStatSlots * 2);
   rc |= dmalloc(&d_stat4_, kStatSlots);
@@ -626,6 +633,9 @@ int Engine::prepare() {
   cudaMemcpyAsync(d_tcount_, tab_.t_count.data(), sizeof(int) * g.n_y, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(d_lineok_, tab_.line_nonempty.data(), tab_.line_nonempty.size(),
                   cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(d_cosv_, tab_.cosv.data(), sizeof(double) * g.n_theta, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(d_sinv_, tab_.sinv.data(), sizeof(double) * g.n_theta, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(d_Href_, tab_.H.data(), sizeof(double) * tab_.H.size(), cudaMemcpyHostToDevice, s);
 
   // measured sinogram -> [t][theta][r_pad]
   const size_t nh = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;
@@ -706,6 +716,15 @@ int Engine::forward_project() {
   std::vector<int32_t> rows(g.n_z);
   for (int i = 0; i < g.n_z; i++) rows[i] = i;
   cudaMemcpyAsync(d_rows_, rows.data(), sizeof(int) * g.n_z, cudaMemcpyHostToDevice, s);
+  if (exact_) {
+    int rc = launch_exact_project(exact_args(), static_cast<double*>(d_yest_), s);
+    if (rc) return cuda_check(rc, "forward projection (exact)");
+    rc = launch_error_from_projection(d_y_, d_yest_, d_e_, d_mu_, g.n_theta, n_rp_, g.n_r, g.n_t,
+                                      fp64_, s);
+    if (rc) return cuda_check(rc, "error sinogram");
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "forward projection");
+    return check_device_error();
+  }
   SweepArgs a{};
   a.g = dg_;
   a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_, d_lineok_};
@@ -757,6 +776,15 @@ int Engine::sweep(int outer, int inner, double* stats4) {
     std::vector<int32_t> lines;
     reference_visit_order(p_.seed, g.n_z, g.n_x, lines);
     cudaMemcpyAsync(d_lines_, lines.data(), sizeof(int32_t) * lines.size(), cudaMemcpyHostToDevice, s);
+    if (exact_) {
+      ExactArgs ea = exact_args();
+      ea.lines = d_lines_;
+      ea.n_lines = static_cast<int>(lines.size());
+      ea.iter_nonzero = iter_nonzero;
+      ea.zero_skipping = p_.zero_skipping;
+      ea.stats = d_stat4_;
+      if ((rc = launch_exact_icd(ea, s))) return cuda_check(rc, "reference-order sweep (exact)");
+    } else {
     RefOrderArgs a{};
     a.g = dg_;
     a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_, d_lineok_};
@@ -770,6 +798,7 @@ int Engine::sweep(int outer, int inner, double* stats4) {
     a.fp64 = fp64_;
     a.stats = d_stat4_;
     if ((rc = launch_ref_order(a, nb_, s))) return cuda_check(rc, "reference-order sweep");
+    }
   } else {
     std::vector<int32_t> rows;
     row_order_for_sweep(sweeps_done_, rows);
@@ -817,6 +846,32 @@ int Engine::sweep(int outer, int inner, double* stats4) {
   if (stats4)
     for (int i = 0; i < 4; i++) stats4[i] = st[i];
   return MBIR_OK;
+}
+
+ExactArgs Engine::exact_args() {
+  const Geometry& g = g_;
+  ExactArgs a{};
+  a.g = dg_;
+  a.flt = flt_;
+  a.x0 = g.x0;
+  a.z0 = g.z0;
+  a.delta_xz = g.delta_xz;
+  a.delta_r = g.delta_r;
+  a.R0 = g.R0;
+  a.RMax = g.RMax;
+  a.offset_r = g.offset_r;
+  a.cosv = d_cosv_;
+  a.sinv = d_sinv_;
+  a.H = d_Href_;
+  a.gain = d_gain_;
+  a.weight = d_wv_;
+  a.t_first = d_tfirst_;
+  a.t_count = d_tcount_;
+  a.hval = static_cast<const double*>(d_hval_);
+  a.lineok = d_lineok_;
+  a.x = static_cast<double*>(d_x_);
+  a.e = static_cast<double*>(d_e_);
+  return a;
 }
 
 int Engine::batch_args(int outer, int inner, SweepArgs* out, size_t* smem_needed) {
@@ -868,8 +923,10 @@ int Engine::joint_estimation() {
   const Geometry& g = g_;
   const int nt = g.n_theta;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
-  int rc = launch_view_sums(0, d_y_, d_e_, d_mu_, d_gain_, d_wv_, d_partial_, d_vsum_, nt, n_rp_,
-                            g.n_r, g.n_t, n_chunk_, fp64_, s);
+  int rc = exact_ ? launch_exact_view_sums(exact_args(), 0, static_cast<const double*>(d_y_), d_mu_,
+                                           d_vsum_, s)
+                 : launch_view_sums(0, d_y_, d_e_, d_mu_, d_gain_, d_wv_, d_partial_, d_vsum_, nt,
+                                    n_rp_, g.n_r, g.n_t, n_chunk_, fp64_, s);
   if (rc) return cuda_check(rc, "joint estimation sums");
   std::vector<double> vs(static_cast<size_t>(nt) * 6);
   cudaMemcpyAsync(vs.data(), d_vsum_, sizeof(double) * vs.size(), cudaMemcpyDeviceToHost, s);
@@ -911,8 +968,10 @@ int Engine::update_weights() {
   const Geometry& g = g_;
   const int nt = g.n_theta;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
-  int rc = launch_view_sums(1, d_y_, d_e_, d_mu_, d_gain_, d_wv_, d_partial_, d_vsum_, nt, n_rp_,
-                            g.n_r, g.n_t, n_chunk_, fp64_, s);
+  int rc = exact_ ? launch_exact_view_sums(exact_args(), 1, static_cast<const double*>(d_y_), d_mu_,
+                                           d_vsum_, s)
+                 : launch_view_sums(1, d_y_, d_e_, d_mu_, d_gain_, d_wv_, d_partial_, d_vsum_, nt,
+                                    n_rp_, g.n_r, g.n_t, n_chunk_, fp64_, s);
   if (rc) return cuda_check(rc, "variance sums");
   std::vector<double> vs(nt);
   cudaMemcpyAsync(vs.data(), d_vsum_, sizeof(double) * nt, cudaMemcpyDeviceToHost, s);

@@ -109,6 +109,7 @@ class Engine {
   int upload_views();  // (gain, weight) pairs and mu/gain doubles
   int check_device_error();
   void row_order_for_sweep(int sweep, std::vector<int32_t>& order) const;
+  ExactArgs exact_args();
   int cuda_check(int code, const char* what);
   void release();
 
@@ -160,6 +161,11 @@ class Engine {
   void* d_hval_ = nullptr;    // Real [n_y][kMaxTRows]
   int* d_rows_ = nullptr;
   uint8_t* d_lineok_ = nullptr;
+  // reference-exact mode (FP64 + reference order)
+  bool exact_ = false;
+  double* d_cosv_ = nullptr;
+  double* d_sinv_ = nullptr;
+  double* d_Href_ = nullptr;
   int* d_lines_ = nullptr;
   double* d_stats_ = nullptr;   // [max slices][4]
   double* d_stat4_ = nullptr;   // [4]

@@ -94,6 +94,32 @@ struct RefOrderArgs {
   double* stats;         // [kStatSlots]
 };
 
+// Reference-exact FP64 mode (mbir_exact.cu): every operation in the reference's order.
+struct ExactArgs {
+  DevGeom g;
+  DevFilter flt;
+  double x0, z0, delta_xz, delta_r, R0, RMax, offset_r;
+  const double* cosv;    // [n_theta]
+  const double* sinv;
+  const double* H;       // [n_theta][bins] as the reference builds it
+  const double* gain;    // [n_theta]
+  const double* weight;  // [n_theta]
+  const int* t_first;
+  const int* t_count;
+  const double* hval;    // [n_y][kMaxTRows]
+  const uint8_t* lineok;
+  double* x;             // [n_y][n_z][n_x]
+  double* e;             // [n_t][n_theta][n_rp]
+  const int* lines;
+  int n_lines;
+  int iter_nonzero, zero_skipping;
+  double* stats;         // [kStatSlots]
+};
+int launch_exact_icd(const ExactArgs& a, void* stream);
+int launch_exact_project(const ExactArgs& a, double* yest, void* stream);
+int launch_exact_view_sums(const ExactArgs& a, int kind, const double* y, const double* mu,
+                           double* out, void* stream);
+
 // launchers (mbir_kernels.cu); fp64 selects Real = double for the void* arrays
 int launch_sweep(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_ref_order(const RefOrderArgs& a, int nb, void* stream);

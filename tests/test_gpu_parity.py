@@ -80,15 +80,18 @@ def test_parallel_sweep_fp32_matches_oracle_same_order(lib_built, oracle_mod):
 
 
 def test_parallel_sweeps_fp64_match_oracle_same_order(lib_built, oracle_mod):
+    """FP64 engine, parallel order, two sweeps against the oracle in the same order.  This path
+    sums theta with warp shuffles (not in the reference's order), so later sweeps may flip a
+    zero-skip decision on last-bit differences; the reference-exact mode is checked below."""
     e, o, p, y = pair(lib_built, oracle_mod, precision=lib_built.FP64)
     e.prepare()
     o.prepare()
-    for k in range(4):
+    for k in range(2):
         rows, stride = e.schedule(k)
         sg = e.sweep(0, k)
         so = o.sweep_slices(rows, stride, 0, k)
         assert sg[3] == so[3] and sg[2] == so[2], (k, sg, so)
-        assert rel(e.volume(), o.volume()) <= 1e-6, k   # float read-out of FP64 state
+        assert rel(e.volume(), o.volume()) <= 1e-7, k   # float read-out of FP64 state
     e.joint_estimation()
     o.joint_estimation()
     np.testing.assert_allclose(e.nuisance()[0], o.gain(), rtol=1e-9)
@@ -96,8 +99,8 @@ def test_parallel_sweeps_fp64_match_oracle_same_order(lib_built, oracle_mod):
 
 def test_reference_order_iterates_after_five_outer(lib_built, oracle_mod):
     """Reference-order mode (same MT19937 visit order, one task over all y, FP64 as the
-    reference's Real_t) reproduces the reference iterates after 5 outer iterations with
-    gain/offset and variance updates."""
+    reference's Real_t, every operation in the reference's order) reproduces the reference
+    iterates after 5 outer iterations with gain/offset and variance updates."""
     e, o, p, y = pair(lib_built, oracle_mod, order_mode=1, seed=20121, outer_iterations=5,
                       precision=lib_built.FP64)
     e.run()
@@ -264,3 +267,15 @@ def test_cancel_before_sweep(lib_built, oracle_mod):
     with pytest.raises(lib_built.MbirError) as ei:
         e.sweep(0, 0)
     assert ei.value.code == -999
+
+
+def test_reference_order_exact_five_sweeps_fixed_nuisance(lib_built, oracle_mod):
+    e, o, p, y = pair(lib_built, oracle_mod, order_mode=1, seed=4242, precision=lib_built.FP64)
+    e.prepare()
+    o.prepare()
+    assert rel(e.error_sinogram(), o.error()) <= 1e-7
+    for k in range(5):
+        sg = e.sweep(0, k)
+        so = o.sweep_reference(4242, 0, k)
+        assert sg[2] == so[2] and sg[3] == so[3], (k, sg, so)
+    assert rel(e.volume(), o.volume()) <= 1e-6
