@@ -109,6 +109,10 @@ typedef struct mbir_params {
   int32_t cost_every_sweep;   /* 1: evaluate the FP64 MAP cost after every sweep */
   int32_t device;             /* CUDA device ordinal */
   int32_t verbose;
+  int32_t slice_staging;      /* 0: a slice's detector rows sit in shared memory when they fit,
+                                 1: always work on them in HBM (same results, for tuning) */
+  int32_t nhicd;              /* BF: 1 = non-homogeneous ICD line lists (the reference's NHICD
+                                 build, BFConstants.h), 0 = every voxel line in each call */
 } mbir_params;
 
 typedef struct mbir_status {

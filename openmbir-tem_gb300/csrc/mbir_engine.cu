@@ -483,7 +483,7 @@ int Engine::alloc_device() {
   int max_smem = 0;
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, p_.device);
   smem_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, n_rs_, t_rows_, bins_, fp64_);
-  stage_ = smem_bytes_ <= static_cast<size_t>(max_smem);
+  stage_ = smem_bytes_ <= static_cast<size_t>(max_smem) && p_.slice_staging == 0;
   if (!stage_) smem_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, 0, t_rows_, bins_, fp64_);
   const size_t ns = static_cast<size_t>(g.n_t) * g.n_theta * n_rp_;
   const size_t nh = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;

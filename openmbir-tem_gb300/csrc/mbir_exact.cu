@@ -11,7 +11,9 @@
 //   * theta1/theta2 and the surrogate sums accumulated sequentially in the reference's entry and
 //     neighbour order (_UpdateVoxels.cpp:343-369, QGGMRF_Functions.cpp:170-190);
 //   * per-view sums of jointEstimation / updateWeights sequentially over r then t
-//     (_Extra.cpp:474-517, :825-833).
+//     (_Extra.cpp:474-517, :825-833);
+//   * powers by a pinned double-double method instead of a math library's pow (the oracle
+//     evaluates them the same way in this mode).
 // Only the elementwise parts run in parallel.  It is a parity mode, not a fast path.
 #include <cuda_runtime.h>
 
@@ -91,12 +93,105 @@ __device__ void build_column(const ExactArgs& A, int row, int col, ExactCol* c) 
   __syncwarp();
 }
 
+// ---- pinned power function ------------------------------------------------------------
+// The reference calls the C library's pow; its last bit differs between libraries (and
+// from CUDA's pow), and the iterates amplify that.  This mode evaluates x^y by double-double
+// arithmetic built from IEEE add/mul/div only (Knuth two-sum; Dekker exact product with
+// Veltkamp splitting; this file is compiled without fused multiply-adds):
+//   ln x = k ln2 + 2 atanh(s), s = (m-1)/(m+1), m in [sqrt(1/2), sqrt(2)), by the power series
+//   of atanh to s^45;  e^t = 2^k (1 + expm1(r)), expm1 by its Taylor series at r/256 to the
+//   14th power followed by eight doublings expm1(2u) = expm1(u) (2 + expm1(u)).
+// The result is the double nearest to x^y except within ~1e-30 of a rounding boundary.
+struct DD {
+  double hi, lo;
+};
+__device__ __forceinline__ DD dd(double hi, double lo = 0.0) { return DD{hi, lo}; }
+__device__ __forceinline__ DD two_sum(double a, double b) {
+  const double s = a + b;
+  const double bb = s - a;
+  return DD{s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ DD fast_sum(double a, double b) {
+  const double s = a + b;
+  return DD{s, b - (s - a)};
+}
+__device__ __forceinline__ void vsplit(double a, double& hi, double& lo) {
+  const double t = 134217729.0 * a;  // 2^27 + 1
+  hi = t - (t - a);
+  lo = a - hi;
+}
+__device__ __forceinline__ DD two_prod(double a, double b) {
+  const double p = a * b;
+  double ah, al, bh, bl;
+  vsplit(a, ah, al);
+  vsplit(b, bh, bl);
+  return DD{p, (((ah * bh) - p) + (ah * bl) + (al * bh)) + (al * bl)};
+}
+__device__ __forceinline__ DD dd_add(DD a, DD b) {
+  DD s = two_sum(a.hi, b.hi);
+  const DD t = two_sum(a.lo, b.lo);
+  s.lo = s.lo + t.hi;
+  s = fast_sum(s.hi, s.lo);
+  s.lo = s.lo + t.lo;
+  return fast_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ DD dd_mul(DD a, DD b) {
+  DD p = two_prod(a.hi, b.hi);
+  p.lo = p.lo + ((a.hi * b.lo) + (a.lo * b.hi));
+  return fast_sum(p.hi, p.lo);
+}
+__device__ DD dd_div(DD a, DD b) {
+  const double q1 = a.hi / b.hi;
+  DD r = dd_add(a, dd_mul(b, dd(-q1)));
+  const double q2 = r.hi / b.hi;
+  r = dd_add(r, dd_mul(b, dd(-q2)));
+  const double q3 = r.hi / b.hi;
+  return dd_add(fast_sum(q1, q2), dd(q3));
+}
+constexpr double kLn2Hi = 6.93147180559945286227e-01;  // ln 2 = kLn2Hi + kLn2Lo
+constexpr double kLn2Lo = 2.31904681384629955842e-17;
+
+__device__ DD dd_log(double x) {
+  int k;
+  double m = frexp(x, &k);
+  if (m < 0.70710678118654752440) {
+    m = m * 2.0;
+    k = k - 1;
+  }
+  const DD s = dd_div(dd(m - 1.0), two_sum(m, 1.0));
+  const DD s2 = dd_mul(s, s);
+  DD acc = dd_div(dd(1.0), dd(45.0));
+  for (int n = 21; n >= 0; n--) acc = dd_add(dd_mul(acc, s2), dd_div(dd(1.0), dd(2.0 * n + 1.0)));
+  const DD lm = dd_mul(dd_mul(s, acc), dd(2.0));
+  return dd_add(dd_mul(DD{kLn2Hi, kLn2Lo}, dd(static_cast<double>(k))), lm);
+}
+__device__ double dd_exp(DD t) {
+  const double kf = floor(t.hi / kLn2Hi + 0.5);
+  DD r = dd_add(t, dd_mul(DD{kLn2Hi, kLn2Lo}, dd(-kf)));
+  r.hi = ldexp(r.hi, -8);
+  r.lo = ldexp(r.lo, -8);
+  DD term = r, sum = r;
+  for (int n = 2; n <= 14; n++) {
+    term = dd_div(dd_mul(term, r), dd(static_cast<double>(n)));
+    sum = dd_add(sum, term);
+  }
+  for (int i = 0; i < 8; i++) sum = dd_mul(sum, dd_add(sum, dd(2.0)));
+  sum = dd_add(sum, dd(1.0));
+  return ldexp(sum.hi, static_cast<int>(kf));
+}
+__device__ double pinned_pow(double x, double y) {
+  if (y == 0.0) return 1.0;
+  if (x == 0.0) return 0.0;
+  if (y == 1.0) return x;
+  return dd_exp(dd_mul(dd_log(x), dd(y)));
+}
+
 // rho'(d)/d exactly as QGGMRF::Derivative (QGGMRF_Functions.cpp:90-104) divided by d
 __device__ double exact_coef(const DevFilter& q, double d0) {
   if (d0 == 0) return q.mrf_p / (q.sig_p * q.mrf_c);
   const double P = q.mrf_p, Q = q.mrf_q;
-  const double t1 = pow(fabs(d0), P - Q) / q.sig_pq;
-  const double t2 = pow(fabs(d0), P - 1);
+  const double t1 = pinned_pow(fabs(d0), P - Q) / q.sig_pq;
+  const double t2 = pinned_pow(fabs(d0), P - 1);
   const double t3 = q.mrf_c + t1;
   double der;
   if (d0 < 0)

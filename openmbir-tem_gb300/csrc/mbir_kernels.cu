@@ -261,7 +261,8 @@ __global__ void rebuild_error_kernel(const Real* __restrict__ y, Real* __restric
     const int v = static_cast<int>((i / n_rp) % n_theta);
     const double yv = y[i];
     const double yh = (yv - static_cast<double>(e[i]) - mu_old[v]) / gain_old[v];
-    e[i] = static_cast<Real>(yv - mu_new[v] - (gain_new[v] * yh));
+    // the product is rounded on its own (no fused multiply-subtract), as in the reference
+    e[i] = static_cast<Real>(yv - mu_new[v] - __dmul_rn(gain_new[v], yh));
   }
 }
 

@@ -80,6 +80,8 @@ class MbirParams(C.Structure):
         ("cost_every_sweep", C.c_int32),
         ("device", C.c_int32),
         ("verbose", C.c_int32),
+        ("slice_staging", C.c_int32),
+        ("nhicd", C.c_int32),
     ]
 
 

@@ -70,19 +70,124 @@ struct orc_ctx {
 };
 
 /* ---------------------------------------------------------------------------------------
+ * Pinned power function.  The reference calls the C library's pow, whose last bit differs
+ * between libraries (and from CUDA's); ICD iterates amplify such differences.  With
+ * pinned_pow set, x^y is evaluated here by double-double arithmetic from plain IEEE
+ * additions, multiplications and divisions only (Knuth's two-sum, Dekker's exact product with
+ * Veltkamp splitting): ln x = k ln2 + 2 atanh((m-1)/(m+1)) by its power series, and
+ * e^t = 2^k (1 + expm1(r)) with expm1 by its Taylor series at r/256 followed by eight
+ * doublings expm1(2u) = expm1(u) (2 + expm1(u)).  The result is the double nearest to
+ * x^y except in cases closer than ~1e-30 to a rounding boundary, and is the same on every
+ * machine that does not fuse multiply-adds.
+ * ------------------------------------------------------------------------------------- */
+typedef struct {
+  double hi, lo;
+} dd_t;
+
+static dd_t dd_make(double hi, double lo) {
+  dd_t r;
+  r.hi = hi;
+  r.lo = lo;
+  return r;
+}
+static dd_t dd_two_sum(double a, double b) {
+  double s = a + b;
+  double bb = s - a;
+  return dd_make(s, (a - (s - bb)) + (b - bb));
+}
+static dd_t dd_fast_sum(double a, double b) {
+  double s = a + b;
+  return dd_make(s, b - (s - a));
+}
+static void dd_split(double a, double* hi, double* lo) {
+  double t = 134217729.0 * a; /* 2^27 + 1 */
+  *hi = t - (t - a);
+  *lo = a - *hi;
+}
+static dd_t dd_two_prod(double a, double b) {
+  double p = a * b, ah, al, bh, bl;
+  dd_split(a, &ah, &al);
+  dd_split(b, &bh, &bl);
+  return dd_make(p, (((ah * bh) - p) + (ah * bl) + (al * bh)) + (al * bl));
+}
+static dd_t dd_add(dd_t a, dd_t b) {
+  dd_t s = dd_two_sum(a.hi, b.hi);
+  dd_t t = dd_two_sum(a.lo, b.lo);
+  s.lo = s.lo + t.hi;
+  s = dd_fast_sum(s.hi, s.lo);
+  s.lo = s.lo + t.lo;
+  return dd_fast_sum(s.hi, s.lo);
+}
+static dd_t dd_mul(dd_t a, dd_t b) {
+  dd_t p = dd_two_prod(a.hi, b.hi);
+  p.lo = p.lo + ((a.hi * b.lo) + (a.lo * b.hi));
+  return dd_fast_sum(p.hi, p.lo);
+}
+static dd_t dd_div(dd_t a, dd_t b) {
+  double q1 = a.hi / b.hi;
+  dd_t r = dd_add(a, dd_mul(b, dd_make(-q1, 0.0)));
+  double q2 = r.hi / b.hi;
+  r = dd_add(r, dd_mul(b, dd_make(-q2, 0.0)));
+  double q3 = r.hi / b.hi;
+  return dd_add(dd_fast_sum(q1, q2), dd_make(q3, 0.0));
+}
+static const double kLn2Hi = 6.93147180559945286227e-01; /* ln 2 = kLn2Hi + kLn2Lo */
+static const double kLn2Lo = 2.31904681384629955842e-17;
+
+static dd_t dd_log(double x) { /* x > 0 and finite */
+  int k;
+  double m = frexp(x, &k);
+  if (m < 0.70710678118654752440) {
+    m = m * 2.0;
+    k = k - 1;
+  }
+  dd_t s = dd_div(dd_make(m - 1.0, 0.0), dd_two_sum(m, 1.0));
+  dd_t s2 = dd_mul(s, s);
+  dd_t acc = dd_div(dd_make(1.0, 0.0), dd_make(45.0, 0.0));
+  for (int n = 21; n >= 0; n--)
+    acc = dd_add(dd_mul(acc, s2), dd_div(dd_make(1.0, 0.0), dd_make(2.0 * n + 1.0, 0.0)));
+  dd_t lm = dd_mul(dd_mul(s, acc), dd_make(2.0, 0.0));
+  return dd_add(dd_mul(dd_make(kLn2Hi, kLn2Lo), dd_make((double)k, 0.0)), lm);
+}
+static double dd_exp(dd_t t) {
+  double kf = floor(t.hi / kLn2Hi + 0.5);
+  dd_t r = dd_add(t, dd_mul(dd_make(kLn2Hi, kLn2Lo), dd_make(-kf, 0.0)));
+  r.hi = ldexp(r.hi, -8);
+  r.lo = ldexp(r.lo, -8);
+  dd_t term = r, sum = r;
+  for (int n = 2; n <= 14; n++) {
+    term = dd_div(dd_mul(term, r), dd_make((double)n, 0.0));
+    sum = dd_add(sum, term);
+  }
+  for (int i = 0; i < 8; i++) sum = dd_mul(sum, dd_add(sum, dd_make(2.0, 0.0)));
+  sum = dd_add(sum, dd_make(1.0, 0.0));
+  return ldexp(sum.hi, (int)kf);
+}
+double orc_pinned_pow(double x, double y) {
+  if (y == 0.0) return 1.0;
+  if (x == 0.0) return 0.0;
+  if (y == 1.0) return x;
+  return dd_exp(dd_mul(dd_log(x), dd_make(y, 0.0)));
+}
+
+static double q_pow(const orc_ctx* c, double x, double y) {
+  return c->p.pinned_pow ? orc_pinned_pow(x, y) : pow(x, y);
+}
+
+/* ---------------------------------------------------------------------------------------
  * QGGMRF prior (Reconstruction/QGGMRF_Functions.cpp:82-206)
  * ------------------------------------------------------------------------------------- */
 static double q_value(const orc_ctx* c, double delta) {
   /* QGGMRF_Functions.cpp:82-85 */
-  return (pow(fabs(delta), c->p.mrf_p) / c->sig_p) /
-         (c->p.mrf_c + pow(fabs(delta), c->p.mrf_p - c->p.mrf_q) / c->sig_pq);
+  return (q_pow(c, fabs(delta), c->p.mrf_p) / c->sig_p) /
+         (c->p.mrf_c + q_pow(c, fabs(delta), c->p.mrf_p - c->p.mrf_q) / c->sig_pq);
 }
 
 static double q_derivative(const orc_ctx* c, double delta) {
   /* QGGMRF_Functions.cpp:90-104 */
   double P = c->p.mrf_p, Q = c->p.mrf_q;
-  double t1 = pow(fabs(delta), P - Q) / c->sig_pq;
-  double t2 = pow(fabs(delta), P - 1);
+  double t1 = q_pow(c, fabs(delta), P - Q) / c->sig_pq;
+  double t2 = q_pow(c, fabs(delta), P - 1);
   double t3 = c->p.mrf_c + t1;
   if (delta < 0) return ((-1 * t2 / (t3 * c->sig_p)) * (P - ((P - Q) * t1) / (t3)));
   return ((t2 / (t3 * c->sig_p)) * (P - ((P - Q) * t1) / (t3)));

@@ -46,9 +46,13 @@ typedef struct orc_params {
   double stop_threshold;
   int32_t outer_iterations, inner_iterations;
   double threshold_reduction_factor;
+  int32_t pinned_pow;         /* 1: QGGMRF powers by orc_pinned_pow instead of the C library */
 } orc_params;
 
 typedef struct orc_ctx orc_ctx;
+
+/* x^y (x >= 0) by double-double arithmetic from IEEE add/mul/div only; see mbir_oracle.c */
+double orc_pinned_pow(double x, double y);
 
 /* geometry + tables; counts is [n_theta][n_r][n_t] (t fastest), tilts in degrees */
 orc_ctx* orc_create(const orc_params* p, const double* counts, const double* tilts_deg,

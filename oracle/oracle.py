@@ -29,6 +29,7 @@ class OrcParams(C.Structure):
         ("noise_model", C.c_int32), ("zero_skipping", C.c_int32), ("stop_threshold", C.c_double),
         ("outer_iterations", C.c_int32), ("inner_iterations", C.c_int32),
         ("threshold_reduction_factor", C.c_double),
+        ("pinned_pow", C.c_int32),
     ]
 
 
@@ -53,6 +54,7 @@ def lib():
             "orc_create": (C.c_void_p, [C.POINTER(OrcParams), _D, _D, C.c_int, C.c_int, C.c_int,
                                         C.c_double, C.c_double]),
             "orc_destroy": (None, [C.c_void_p]),
+            "orc_pinned_pow": (C.c_double, [C.c_double, C.c_double]),
             "orc_dims": (None, [C.c_void_p, _I, _D]),
             "orc_offsets": (None, [C.c_void_p, _D]),
             "orc_volume": (_D, [C.c_void_p]), "orc_error": (_D, [C.c_void_p]),
@@ -119,6 +121,9 @@ def params_from_mbir(p):
     o.outer_iterations = p.outer_iterations
     o.inner_iterations = p.inner_iterations
     o.threshold_reduction_factor = p.threshold_reduction_factor
+    # the engine's reference-exact mode (FP64, reference order) evaluates powers by the
+    # pinned method; the oracle does the same for that mode
+    o.pinned_pow = 1 if (p.precision == 1 and p.order_mode == 1) else 0
     return o
 
 
@@ -260,3 +265,8 @@ def visit_order(seed, nz, nx):
     out = np.zeros(nz * nx, np.int32)
     lib().orc_visit_order(seed, nz, nx, out.ctypes.data_as(_I))
     return out
+
+
+def pinned_pow(x, y):
+    """x**y by the oracle's pinned double-double method (see mbir_oracle.c)."""
+    return lib().orc_pinned_pow(float(x), float(y))

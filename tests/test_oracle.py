@@ -134,3 +134,21 @@ def test_cost_parts_finite(lib_built, oracle_mod, c):
     total, parts = o.cost()
     assert np.isfinite(total) and parts[1] > 0
     assert abs(total - parts.sum()) < 1e-9 * abs(total)
+
+
+def test_pinned_pow_is_correctly_rounded(oracle_mod):
+    """The oracle's pinned pow (used in the reference-exact mode) against the C library
+    (within one ulp) and against 200-bit arithmetic (nearest double)."""
+    import math
+    rng = np.random.default_rng(0)
+    xs = 10.0 ** rng.uniform(-12, 3, 3000)
+    ys = rng.choice([0.9, 0.5, 1.1, 2.0, 1.9], 3000)
+    got = np.array([oracle_mod.pinned_pow(x, y) for x, y in zip(xs, ys)])
+    ref = xs ** ys
+    assert np.all(np.abs(got - ref) <= np.spacing(np.abs(ref)))
+    assert oracle_mod.pinned_pow(2.0, 0.5) == math.sqrt(2.0)
+    assert oracle_mod.pinned_pow(3.0, 2.0) == 9.0 and oracle_mod.pinned_pow(0.0, 0.9) == 0.0
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.prec = 200
+    for x, y, g in zip(xs[:400], ys[:400], got[:400]):
+        assert g == float(mpmath.power(mpmath.mpf(float(x)), mpmath.mpf(float(y))))
