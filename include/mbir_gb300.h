@@ -229,6 +229,12 @@ typedef struct mbir_server_stats {
   double busy_s;                   /* worker time with requests on the device */
   double batched_sweep_ms;         /* device time of all batched sweeps */
   int64_t batched_sweeps;
+  int64_t budget_bytes;            /* device-memory budget for admitted requests */
+  int64_t peak_bytes;              /* largest estimated footprint resident at one time */
+  int32_t peak_active;             /* most requests on the device at one time */
+  int32_t reserved;
+  int64_t admitted;                /* requests admitted so far */
+  int64_t admitted_out_of_order;   /* admissions that overtook an earlier request (0: FIFO) */
 } mbir_server_stats;
 /* mem_budget_bytes <= 0: 80% of the free device memory; max_active <= 0: 64 */
 mbir_server* mbir_server_create(int32_t device, int64_t mem_budget_bytes, int32_t max_active);

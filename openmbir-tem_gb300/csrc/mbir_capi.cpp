@@ -379,6 +379,12 @@ int32_t mbir_server_get_stats(mbir_server* s, mbir_server_stats* st) {
   st->busy_s = x.busy_s;
   st->batched_sweep_ms = x.batched_sweep_ms;
   st->batched_sweeps = x.batched_sweeps;
+  st->budget_bytes = x.budget_bytes;
+  st->peak_bytes = x.peak_bytes;
+  st->peak_active = x.peak_active;
+  st->reserved = 0;
+  st->admitted = x.admitted;
+  st->admitted_out_of_order = x.admitted_out_of_order;
   return rc;
 }
 const char* mbir_server_last_error(const mbir_server* s) {

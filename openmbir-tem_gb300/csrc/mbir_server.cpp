@@ -107,6 +107,12 @@ int Server::admit_locked(std::vector<Request*>& admitted) {
     queue_.pop_front();
     used_ += static_cast<int64_t>(r->bytes);
     admitted.push_back(r);
+    stats_.admitted++;
+    if (r->id < last_admitted_id_) stats_.admitted_out_of_order++;
+    last_admitted_id_ = r->id;
+    stats_.peak_bytes = std::max(stats_.peak_bytes, used_);
+    stats_.peak_active = std::max(stats_.peak_active,
+                                  static_cast<int32_t>(active_.size() + admitted.size()));
   }
   return 0;
 }
@@ -266,6 +272,7 @@ int Server::release(int64_t id) {
 int Server::stats(ServerStats* st) {
   std::lock_guard<std::mutex> lk(mu_);
   ServerStats s = stats_;
+  s.budget_bytes = budget_;
   s.active = static_cast<int32_t>(active_.size());
   s.queued = static_cast<int32_t>(queue_.size());
   if (!latencies_ms_.empty()) {

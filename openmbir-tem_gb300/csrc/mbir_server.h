@@ -42,6 +42,9 @@ struct ServerStats {
   double busy_s = 0;          // time the worker spent with at least one active request
   double batched_sweep_ms = 0;
   int64_t batched_sweeps = 0;
+  int64_t budget_bytes = 0, peak_bytes = 0;
+  int32_t peak_active = 0;
+  int64_t admitted = 0, admitted_out_of_order = 0;
 };
 
 class Server {
@@ -68,6 +71,7 @@ class Server {
   int64_t budget_;
   int max_active_;
   int64_t used_ = 0;
+  int64_t last_admitted_id_ = 0;
   int64_t next_id_ = 1;
   std::mutex mu_;
   std::condition_variable cv_, done_cv_;

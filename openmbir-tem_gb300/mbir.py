@@ -101,6 +101,8 @@ class MbirServerStats(C.Structure):
         ("active", C.c_int32), ("queued", C.c_int32), ("p50_ms", C.c_double),
         ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("voxel_updates", C.c_double),
         ("busy_s", C.c_double), ("batched_sweep_ms", C.c_double), ("batched_sweeps", C.c_int64),
+        ("budget_bytes", C.c_int64), ("peak_bytes", C.c_int64), ("peak_active", C.c_int32),
+        ("reserved", C.c_int32), ("admitted", C.c_int64), ("admitted_out_of_order", C.c_int64),
     ]
 
 

@@ -96,6 +96,42 @@ def particles_on_slab(n_r=512, n_t=256, thickness=64.0, max_deg=60.0, step_deg=2
     return y, ang.astype(np.float32), g
 
 
+def bf_counts(proj, dose=1.0e4, drift=0.03, atten=0.02, seed=0):
+    """Bright-field raw counts: Poisson(dose * d_k * exp(-atten * proj)) with a per-view dose
+    drift d_k = 1 +- U(drift).  `proj` holds line integrals of the phantom's values; `atten`
+    turns them into attenuation (the phantom values U(0.5, 2.0) per voxel times 0.02 keep the
+    thickest particle stacks at a few percent transmission).  Returns (counts float32, d)."""
+    rng = np.random.default_rng(seed)
+    d = 1.0 + rng.uniform(-drift, drift, proj.shape[0])
+    lam = dose * d[:, None, None] * np.exp(-atten * proj)
+    counts = rng.poisson(lam).astype(np.float32)
+    return np.maximum(counts, 1.0), d
+
+
+def bf_particles_on_slab(n_r=512, n_t=256, thickness=64.0, max_deg=60.0, step_deg=2.0,
+                         n_particles=200, slab=(-0.75, -0.5), slab_value=0.1, seed=0,
+                         dose=1.0e4):
+    """The bright-field workload: the particles-on-slab phantom of particles_on_slab seen as
+    Poisson counts at `dose` electrons with +-3% per-view drift.  Returns (counts, angles)."""
+    ang = tilt_angles(max_deg, step_deg)
+    lz = 2 * thickness
+    z0, z1 = slab[0] * lz / 2, slab[1] * lz / 2
+    shapes = random_ellipsoids(n_particles, n_r, n_t, lz, seed=seed, z_range=(z1, lz / 2))
+    proj = np.zeros((len(ang), n_r, n_t), np.float64)
+    t = -n_t / 2 + np.arange(n_t) + 0.5
+    for s in shapes:
+        rows = np.nonzero(np.abs(t - s[1]) < s[4])[0]
+        if len(rows) == 0:
+            continue
+        lo, hi = rows[0], rows[-1] + 1
+        offset = -n_t / 2 + lo + (hi - lo) / 2
+        sub = (s[0], s[1] - offset, s[2], s[3], s[4], s[5], s[6])
+        proj[:, :, lo:hi] += ellipsoid_projection(ang, n_r, hi - lo, [sub])
+    proj += slab_value * (z1 - z0) / np.cos(np.deg2rad(ang))[:, None, None]
+    counts, _ = bf_counts(proj, dose=dose, seed=seed + 1)
+    return counts, ang.astype(np.float32)
+
+
 def random_ellipsoids(n, extent_x, extent_y, extent_z, seed=0, axes=(3.0, 15.0),
                       values=(0.5, 2.0), z_range=None):
     rng = np.random.default_rng(seed)

@@ -67,6 +67,11 @@ struct orc_ctx {
   unsigned char* mask;
   double* mag_map;
   double sig_p, sig_pq, sig_q;
+  /* bright field */
+  unsigned char* sel;  /* Bragg selector [n_theta][n_r][n_t] */
+  double* filt_map;    /* VSC-filtered mag map [n_z][n_x] */
+  double bragg_t;      /* current Bragg threshold T */
+  int counts_logged;   /* processRawCounts applied */
 };
 
 /* ---------------------------------------------------------------------------------------
@@ -511,6 +516,10 @@ orc_ctx* orc_create(const orc_params* p, const double* counts, const double* til
   c->init_var = (double*)calloc(n_theta, sizeof(double));
   c->mag_map = (double*)calloc((size_t)c->n_z * c->n_x, sizeof(double));
   c->mask = (unsigned char*)calloc((size_t)c->n_z * c->n_x, 1);
+  c->filt_map = (double*)calloc((size_t)c->n_z * c->n_x, sizeof(double));
+  c->sel = (unsigned char*)malloc(ns);
+  memset(c->sel, 1, ns);
+  c->bragg_t = p->bragg_threshold;
   /* HAADF_QGGMRFPriorModel.cpp:10-21 (c, P and alpha come from params) */
   c->sig_p = pow(p->sigma_x, p->mrf_p);
   c->sig_pq = pow(p->sigma_x, (p->mrf_p - p->mrf_q));
@@ -536,7 +545,7 @@ void orc_destroy(orc_ctx* c) {
                   c->col_start,  c->col_count, c->col_index, c->col_val,     c->counts,
                   c->x,          c->e,        c->w,          c->yest,        c->I,
                   c->mu,         c->alpha,    c->init_gain,  c->init_offset, c->init_var,
-                  c->mask,       c->mag_map};
+                  c->mask,       c->mag_map,  c->filt_map,   c->sel};
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) free(ptrs[i]);
   free(c);
 }
@@ -643,6 +652,21 @@ int orc_init_nuisance(orc_ctx* c) {
     double t = c->p.target_gain / sum;
     for (int k = 0; k < nt; k++) c->I[k] = c->init_gain[k] * t;
   }
+  /* BF: BFReconstructionEngine::execute creates the nuisance parameters from the raw counts
+   * (:374) and only then takes the log (processRawCounts :385,
+   * BFForwardModel.cpp:939-972): counts += bf_offset; y = -log(counts / BF_MAX), BF_MAX = 1.
+   * A negative count ends that (theta, r) row early, as the reference's break does. */
+  if (c->p.modality == 1 && !c->counts_logged) {
+    for (int th = 0; th < nt; th++)
+      for (int r = 0; r < c->n_r; r++)
+        for (int t = 0; t < c->n_t; t++) {
+          double* v = &S3(c, counts, th, r, t);
+          *v += c->p.bf_offset;
+          if (*v < 0) break;
+          *v = -log(*v / 1.0);
+        }
+    c->counts_logged = 1;
+  }
   return 0;
 }
 
@@ -672,6 +696,22 @@ void orc_forward_project(orc_ctx* c) {
 /* calculateMeasurementWeight (HAADF_ReconstructionEngine_Extra.cpp:693-771) with
  * IDENTITY_NOISE_MODEL (HAADFConstants.h:56) and no bright-field data. */
 void orc_measurement_weight(orc_ctx* c) {
+  if (c->p.modality == 1) {
+    /* BFForwardModel::calculateMeasurementWeight (BFForwardModel.cpp:328-385): no
+     * IDENTITY_NOISE_MODEL in the BF build, so w = BF_MAX / exp(y), divided by alpha */
+    for (int th = 0; th < c->n_theta; th++) {
+      if (c->p.noise_estimation) c->alpha[th] = c->init_var[th];
+      for (int r = 0; r < c->n_r; r++)
+        for (int t = 0; t < c->n_t; t++) {
+          S3(c, e, th, r, t) = S3(c, counts, th, r, t) - S3(c, yest, th, r, t) - c->mu[th];
+          double w = 1.0 / exp(S3(c, counts, th, r, t));
+          S3(c, sel, th, r, t) = 1;
+          if (c->p.noise_estimation) w /= c->alpha[th];
+          S3(c, w, th, r, t) = w;
+        }
+    }
+    return;
+  }
   for (int th = 0; th < c->n_theta; th++) {
     if (c->p.noise_model) c->alpha[th] = c->init_var[th];
     for (int r = 0; r < c->n_r; r++)
@@ -992,6 +1032,8 @@ void orc_update_weights(orc_ctx* c) {
 }
 
 /* computeCost, QGGMRF branch (HAADF_ReconstructionEngine.cpp:1147-1364). */
+static double prior_cost(const orc_ctx* c);
+
 double orc_cost(const orc_ctx* c, double* parts) {
   double cost = 0, temp = 0;
   for (int i = 0; i < c->n_theta; i++)
@@ -1002,6 +1044,33 @@ double orc_cost(const orc_ctx* c, double* parts) {
       }
   cost /= 2;
   double data = cost;
+  temp = prior_cost(c);
+  cost += temp;
+  double noise = 0;
+  if (c->p.noise_model) {
+    double tn = 0;
+    for (int i = 0; i < c->n_theta; i++)
+      for (int j = 0; j < c->n_r; j++)
+        for (int k = 0; k < c->n_t; k++) {
+          double w = S3(c, w, i, j, k);
+          if (w != 0) tn += log(2 * M_PI * (1.0 / w));
+        }
+    tn /= 2;
+    noise = tn;
+    cost += tn;
+  }
+  if (parts) {
+    parts[0] = data;
+    parts[1] = temp;
+    parts[2] = noise;
+  }
+  return cost;
+}
+
+/* QGGMRF prior term of computeCost (HAADF_ReconstructionEngine.cpp:1285-1359; the same
+ * 13-neighbour loop is QGGMRF::PriorModelCost, BF_QGGMRFPriorModel.cpp:162-262). */
+static double prior_cost(const orc_ctx* c) {
+  double temp = 0;
 #define XV(zz, xx, yy) X3(c, zz, xx, yy)
 #define ACC(fi, z2, x2, y2) temp += k_filter[fi] * q_value(c, XV(i, j, k) - XV(z2, x2, y2))
   for (int i = 0; i < c->n_z; i++)
@@ -1031,26 +1100,7 @@ double orc_cost(const orc_ctx* c, double* parts) {
       }
 #undef ACC
 #undef XV
-  cost += temp;
-  double noise = 0;
-  if (c->p.noise_model) {
-    double tn = 0;
-    for (int i = 0; i < c->n_theta; i++)
-      for (int j = 0; j < c->n_r; j++)
-        for (int k = 0; k < c->n_t; k++) {
-          double w = S3(c, w, i, j, k);
-          if (w != 0) tn += log(2 * M_PI * (1.0 / w));
-        }
-    tn /= 2;
-    noise = tn;
-    cost += tn;
-  }
-  if (parts) {
-    parts[0] = data;
-    parts[1] = temp;
-    parts[2] = noise;
-  }
-  return cost;
+  return temp;
 }
 
 /* HAADF_ReconstructionEngine::execute outer/inner loops (HAADF_ReconstructionEngine.cpp:706-815)
@@ -1083,4 +1133,420 @@ int orc_run(orc_ctx* c, uint32_t seed, double* cost_log, int n_cost) {
     }
   }
   return sweeps;
+}
+
+/* =========================================================================================
+ * Bright field (Code/MBIRLib/BrightField/...)
+ * ========================================================================================= */
+unsigned char* orc_selector(orc_ctx* c) { return c->sel; }
+double* orc_filt_map(orc_ctx* c) { return c->filt_map; }
+void orc_set_bragg(orc_ctx* c, double t) { c->bragg_t = t; }
+double orc_get_bragg(const orc_ctx* c) { return c->bragg_t; }
+
+/* boost::uniform_int<uint32_t>(0, range) drawn from mt19937 (boost's integer bucket method:
+ * the raw 32-bit draw divided by bucket_size, redrawn when the quotient exceeds range). */
+static uint32_t boost_uniform(mt_state* s, uint32_t range) {
+  const uint32_t brange = 0xffffffffu;
+  if (range == 0) return 0;
+  if (range == brange) return mt_next(s);
+  uint32_t bucket = brange / (range + 1u);
+  if (brange % (range + 1u) == range) ++bucket;
+  for (;;) {
+    uint32_t r = mt_next(s) / bucket;
+    if (r <= range) return r;
+  }
+}
+
+/* VoxelUpdateList::GenRandList (Common/VoxelUpdateList.cpp:157-215): newIndexes starts as
+ * the identity; for i = 1..n-1 it is swapped with a uniform position in [0, n-1]; element i
+ * of the input goes to position newIndexes[i].  The reference seeds with the clock; here the
+ * seed is explicit. */
+void orc_rand_list_perm(uint32_t seed, int n, int32_t* idx) {
+  for (int i = 0; i < n; i++) idx[i] = i;
+  if (n < 2) return;
+  mt_state s;
+  mt_seed(&s, seed);
+  for (int i = 1; i < n; i++) {
+    uint32_t r = boost_uniform(&s, (uint32_t)(n - 1));
+    if (r >= (uint32_t)n) continue;
+    int32_t t = idx[i];
+    idx[i] = idx[r];
+    idx[r] = t;
+  }
+}
+
+/* One voxel of BFUpdateYSlice::execute (BrightField/BFUpdateYSlice.cpp:185-322) with
+ * BFForwardModel::computeTheta (BFForwardModel.cpp:851-892) and updateErrorSinogram
+ * (:898-932): entries rejected by the Bragg selector enter theta1/theta2 with the weight
+ * delta*T / (|e| sqrt(w)); the scatter re-evaluates the selector as |e sqrt(w)| < T. */
+static void bf_update_voxel(orc_ctx* c, int jn, int kn, int i, int outer, int inner,
+                            double* stats, double* mag) {
+  double nb[27];
+  unsigned char bf[27];
+  memset(nb, 0, sizeof(nb));
+  memset(bf, 0, sizeof(bf));
+  for (int p = -1; p <= 1; p++)
+    for (int q = -1; q <= 1; q++)
+      for (int r = -1; r <= 1; r++)
+        if (i + p >= 0 && i + p < c->n_y && jn + q >= 0 && jn + q < c->n_z && kn + r >= 0 &&
+            kn + r < c->n_x) {
+          nb[IDX3(p + 1, q + 1, r + 1)] = X3(c, q + jn, r + kn, p + i);
+          bf[IDX3(p + 1, q + 1, r + 1)] = 1;
+        }
+  nb[IDX3(1, 1, 1)] = 0.0;
+  double V = X3(c, jn, kn, i);
+  int zs = 0;
+  if (c->p.zero_skipping == 1 && V == 0.0 && (inner > 0 || outer > 0)) {
+    zs = 1;
+    for (int a = 0; a < 27; a++)
+      if (nb[a] > 0.0) zs = 0;
+  }
+  if (zs) {
+    stats[2] += 1;
+    return;
+  }
+  const double T = c->bragg_t, dlt = c->p.bragg_delta;
+  int l = jn * c->n_x + kn;
+  int base = c->col_start[l], cnt = c->col_count[l];
+  int t0 = c->vlr_first[i], tc = c->vlr_count[i];
+  const double* hv = c->vlr_val + (size_t)i * c->vlr_cap;
+  double th1 = 0.0, th2 = 0.0;
+  for (int q = 0; q < cnt; q++) {
+    int id = c->col_index[base + q];
+    int th = id / c->n_r, r = id % c->n_r;
+    double k0 = c->I[th] * (c->col_val[base + q]);
+    for (int a = 0; a < tc; a++) {
+      size_t ei = ((size_t)th * c->n_r + r) * c->n_t + (t0 + a);
+      double ev = c->e[ei], w = c->w[ei];
+      if (c->sel[ei] == 1) {
+        double pe = k0 * hv[a];
+        th2 += (pe * pe * w);
+        th1 += (ev * pe * w);
+      } else {
+        double qc = (dlt * T) / (fabs(ev) * sqrt(w));
+        double pe = k0 * hv[a];
+        th2 += qc * (pe * pe * w);
+        th1 += qc * (ev * pe * w);
+      }
+    }
+  }
+  th1 *= -1;
+  double low = nb[0], high = nb[0];
+  for (int a = 0; a < 27; a++) {
+    if (nb[a] < low) low = nb[a];
+    if (nb[a] > high) high = nb[a];
+  }
+  if (th2 != 0) {
+    low = (low > (V - (th1 / th2)) ? (V - (th1 / th2)) : low);
+    high = (high < (V - (th1 / th2)) ? (V - (th1 / th2)) : high);
+  }
+  double nv = q_substitution(c, low, high, V, bf, nb, th1, th2);
+  if (nv < 0.0) nv = 0.0; /* POSITIVITY_CONSTRAINT (BFConstants.h) */
+  X3(c, jn, kn, i) = nv;
+  mag[l] = mag[l] + fabs(nv - V);
+  if (c->mask[l] == 1) {
+    stats[0] += fabs(nv - V);
+    stats[1] += fabs(V);
+  }
+  stats[3] += 1;
+  double d = nv - V;
+  for (int q = 0; q < cnt; q++) {
+    int id = c->col_index[base + q];
+    int th = id / c->n_r, r = id % c->n_r;
+    for (int a = 0; a < tc; a++) {
+      size_t ei = ((size_t)th * c->n_r + r) * c->n_t + (t0 + a);
+      double k2 = (c->I[th] * (c->col_val[base + q] * hv[a] * (d)));
+      c->e[ei] -= k2;
+      c->sel[ei] = (fabs(c->e[ei] * sqrt(c->w[ei])) < T) ? 1 : 0;
+    }
+  }
+}
+
+/* One updateVoxels call (BFReconstructionEngine_Extra.cpp:476-859) with one worker: the
+ * lines' magnitudes restart at 0, then every line sweeps y = 0..n_y-1 in list order. */
+void orc_bf_sweep_lines(orc_ctx* c, const int32_t* lines, int n_lines, int outer, int inner,
+                        double* stats) {
+  stats[0] = stats[1] = stats[2] = stats[3] = 0;
+  for (int n = 0; n < n_lines; n++) c->mag_map[lines[n]] = 0;
+  for (int n = 0; n < n_lines; n++) {
+    int l = lines[n];
+    c->mag_map[l] = 0;
+    if (c->col_count[l] <= 0) continue;
+    for (int y = 0; y < c->n_y; y++)
+      bf_update_voxel(c, l / c->n_x, l % c->n_x, y, outer, inner, stats, c->mag_map);
+  }
+}
+
+void orc_bf_sweep_slices(orc_ctx* c, const unsigned char* active, const int32_t* row_order,
+                         int stride, int outer, int inner, double* stats) {
+  stats[0] = stats[1] = stats[2] = stats[3] = 0;
+  size_t nl = (size_t)c->n_z * c->n_x;
+  for (size_t l = 0; l < nl; l++)
+    if (active[l]) c->mag_map[l] = 0;
+  for (int colour = 0; colour < 2; colour++)
+    for (int i = colour; i < c->n_y; i += 2)
+      for (int rr = 0; rr < c->n_z; rr++) {
+        int z = row_order[rr];
+        for (int k = 0; k < stride; k++)
+          for (int x = k; x < c->n_x; x += stride) {
+            int l = z * c->n_x + x;
+            if (active[l] && c->col_count[l] > 0)
+              bf_update_voxel(c, z, x, i, outer, inner, stats, c->mag_map);
+          }
+      }
+}
+
+/* ComputeVSC (BFReconstructionEngine_Extra.cpp:888-947): 5x5 Hamming window
+ * (BFReconstructionEngine.cpp:157-185) over the update-magnitude map, zero outside. */
+static const double k_hamming[5][5] = {{0.0013, 0.0086, 0.0159, 0.0086, 0.0013},
+                                       {0.0086, 0.0581, 0.1076, 0.0581, 0.0086},
+                                       {0.0159, 0.1076, 0.1993, 0.1076, 0.0159},
+                                       {0.0086, 0.0581, 0.1076, 0.0581, 0.0086},
+                                       {0.0013, 0.0086, 0.0159, 0.0086, 0.0013}};
+void orc_bf_vsc(orc_ctx* c) {
+  for (int i = 0; i < c->n_z; i++)
+    for (int j = 0; j < c->n_x; j++) {
+      double f = 0;
+      for (int p = -2; p <= 2; p++)
+        for (int q = -2; q <= 2; q++)
+          if (i + p >= 0 && i + p < c->n_z && j + q >= 0 && j + q < c->n_x)
+            f += k_hamming[p + 2][q + 2] * c->mag_map[(size_t)(i + p) * c->n_x + (j + q)];
+      c->filt_map[(size_t)i * c->n_x + j] = f;
+    }
+}
+
+static int cmp_double(const void* a, const void* b) {
+  double x = *(const double*)a, y = *(const double*)b;
+  return (x > y) - (x < y);
+}
+
+/* SetNonHomThreshold (BFReconstructionEngine_Extra.cpp:954-1011): the order statistic at
+ * position N - N/20 (ascending, 0-based) of the filtered map.  RandomizedSelect's random
+ * pivots do not change the value it returns; this takes it from a sorted copy.  (For N < 20
+ * the reference's position is out of range; here it is clamped to N-1.) */
+double orc_bf_nh_threshold(const orc_ctx* c) {
+  size_t n = (size_t)c->n_z * c->n_x;
+  double* a = (double*)malloc(sizeof(double) * n);
+  memcpy(a, c->filt_map, sizeof(double) * n);
+  qsort(a, n, sizeof(double), cmp_double);
+  size_t k = n - n / 20;
+  if (k >= n) k = n - 1;
+  double t = a[k];
+  free(a);
+  return t;
+}
+
+/* GenNonHomList (BFReconstructionEngine_Extra.cpp:1016-1047) before its randomisation: lines
+ * whose filtered magnitude exceeds the threshold, z-major. */
+int orc_bf_nh_lines(const orc_ctx* c, double threshold, int32_t* lines) {
+  int n = 0;
+  for (int j = 0; j < c->n_z; j++)
+    for (int k = 0; k < c->n_x; k++)
+      if (c->filt_map[(size_t)j * c->n_x + k] > threshold) lines[n++] = j * c->n_x + k;
+  return n;
+}
+
+/* roiVolumeSum (BFReconstructionEngine_Extra.cpp:1200-1215) */
+double orc_roi_volume_sum(const orc_ctx* c) {
+  double sum = 0;
+  for (int j = 0; j < c->n_z; j++)
+    for (int k = 0; k < c->n_x; k++)
+      if (c->mask[(size_t)j * c->n_x + k] == 1)
+        for (int i = 0; i < c->n_y; i++) sum += X3(c, j, k, i);
+  return sum;
+}
+
+/* the ROI sum of stopCriteria (BFReconstructionEngine_Extra.cpp:1239-1248) */
+double orc_roi_mag_sum(const orc_ctx* c) {
+  double sum = 0;
+  for (int j = 0; j < c->n_z; j++)
+    for (int k = 0; k < c->n_x; k++)
+      if (c->mask[(size_t)j * c->n_x + k] == 1) sum += c->mag_map[(size_t)j * c->n_x + k];
+  return sum;
+}
+
+/* BFForwardModel::jointEstimation (BFForwardModel.cpp:390-441): per view, the offset
+ * (log dosage) step alpha = num/den over selected entries (e w, w) and rejected ones
+ * (T delta sign(e) sqrt(w), T delta sqrt(w) / |e|); e -= alpha, mu += alpha. */
+void orc_bf_joint_estimation(orc_ctx* c) {
+  const double T = c->bragg_t, dl = c->p.bragg_delta;
+  for (int th = 0; th < c->n_theta; th++) {
+    double num = 0, den = 0;
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = 0; t < c->n_t; t++) {
+        double ev = S3(c, e, th, r, t), w = S3(c, w, th, r, t);
+        if (S3(c, sel, th, r, t) == 1) {
+          num += (ev * w);
+          den += w;
+        } else {
+          num += (T * dl * ev / fabs(ev)) * sqrt(w);
+          den += ((T * dl * sqrt(w)) / fabs(ev));
+        }
+      }
+    double a = num / den;
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = 0; t < c->n_t; t++) S3(c, e, th, r, t) -= a;
+    c->mu[th] += a;
+  }
+}
+
+/* BFForwardModel::updateWeights (BFForwardModel.cpp:447-511): one variance for all views. */
+void orc_bf_update_weights(orc_ctx* c) {
+  const double T = c->bragg_t, dl = c->p.bragg_delta;
+  for (int th = 0; th < c->n_theta; th++)
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = 0; t < c->n_t; t++) S3(c, w, th, r, t) *= c->alpha[th];
+  double sum1 = 0, sum2 = 0;
+  for (int th = 0; th < c->n_theta; th++)
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = 0; t < c->n_t; t++) {
+        double ev = S3(c, e, th, r, t), w = S3(c, w, th, r, t);
+        if (S3(c, sel, th, r, t) == 1)
+          sum1 += (ev * ev * w);
+        else
+          sum2 += fabs(ev) * sqrt(c->alpha[th] * w);
+      }
+  double upd = (sum1 + (dl * T) * sum2) / (c->n_theta * c->n_r * c->n_t);
+  for (int th = 0; th < c->n_theta; th++) c->alpha[th] = upd;
+  for (int th = 0; th < c->n_theta; th++)
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = 0; t < c->n_t; t++) S3(c, w, th, r, t) /= c->alpha[th];
+}
+
+/* BFForwardModel::updateSelector (BFForwardModel.cpp:517-531) */
+void orc_bf_update_selector(orc_ctx* c) {
+  const double T = c->bragg_t;
+  size_t ns = (size_t)c->n_theta * c->n_r * c->n_t;
+  for (size_t i = 0; i < ns; i++) c->sel[i] = (c->e[i] * c->e[i] * c->w[i] < T * T) ? 1 : 0;
+}
+
+/* BFReconstructionEngine::computeCost (BFReconstructionEngine.cpp:1084-1097) =
+ * BFForwardModel::forwardCost (BFForwardModel.cpp:812-846) + QGGMRF::PriorModelCost.
+ * parts: [0] data, [1] prior, [2] noise. */
+double orc_bf_cost(const orc_ctx* c, double* parts) {
+  const double T = c->bragg_t, dl = c->p.bragg_delta;
+  double cost = 0;
+  for (int i = 0; i < c->n_theta; i++)
+    for (int j = 0; j < c->n_r; j++)
+      for (int k = 0; k < c->n_t; k++) {
+        double ev = S3(c, e, i, j, k), w = S3(c, w, i, j, k);
+        if (S3(c, sel, i, j, k) == 1)
+          cost += (ev * ev * w);
+        else
+          cost += (2 * T * dl * fabs(ev) * sqrt(w) + T * T * (1 - 2 * dl));
+      }
+  cost /= 2;
+  double data = cost, noise = 0;
+  if (c->p.noise_estimation) {
+    /* (N_theta N_r N_t / 2) in integer arithmetic, as the reference writes it */
+    noise = (double)((c->n_theta * c->n_r * c->n_t) / 2) * log(c->alpha[0]);
+    cost += noise;
+  }
+  double prior = prior_cost(c);
+  if (parts) {
+    parts[0] = data;
+    parts[1] = prior;
+    parts[2] = noise;
+  }
+  return cost + prior;
+}
+
+#define K_NHOM 20      /* MBIR::Constants::k_NumHomogeniousIter (ReconstructionConstants.h:76) */
+#define K_NNHOM 20     /* k_NumNonHomogeniousIter (:77) */
+#define K_DEF_BRAGG 5e10 /* DefBraggThreshold (BFConstants.h) */
+
+/* BFReconstructionEngine::execute outer/inner loops (BFReconstructionEngine.cpp:555-858) with
+ * NHICD (even calls: the next 1/20 of a random permutation of all lines; odd calls: lines
+ * whose filtered update magnitude is in the top 1/20), the Bragg threshold schedule, the
+ * stop rule of stopCriteria and the nuisance updates.  Each call visits its list in the order
+ * of orc_rand_list_perm(seed + 1 + call) (the reference: GenRandList per worker, clock seed). */
+int orc_bf_run(orc_ctx* c, uint32_t seed, int max_calls) {
+  const int nl = c->n_z * c->n_x;
+  int32_t* perm = (int32_t*)malloc(sizeof(int32_t) * (nl > 0 ? nl : 1));
+  int32_t* master = (int32_t*)malloc(sizeof(int32_t) * (nl > 0 ? nl : 1));
+  int32_t* list = (int32_t*)malloc(sizeof(int32_t) * (nl > 0 ? nl : 1));
+  int32_t* order = (int32_t*)malloc(sizeof(int32_t) * (nl > 0 ? nl : 1));
+  orc_rand_list_perm(seed, nl, perm);
+  for (int i = 0; i < nl; i++) master[perm[i]] = i;
+  int num_iter = c->p.inner_iterations;
+  double des_t = 0, temp_t;
+  if (num_iter > 1) {
+    des_t = c->p.bragg_threshold;
+    temp_t = K_DEF_BRAGG;
+  } else {
+    temp_t = c->p.bragg_threshold;
+  }
+  c->bragg_t = temp_t;
+  for (int i = 0; i < nl; i++) c->mag_map[i] = 0;
+  uint32_t listsel = 0, eff = 0;
+  double prev_mag = 0, stop = c->p.stop_threshold;
+  int calls = 0, done = 0;
+  for (int outer = 0; outer < c->p.outer_iterations && !done; outer++) {
+    if (outer > 0) {
+      num_iter = 1;
+      c->bragg_t = temp_t;
+    }
+    int status = 1;
+    for (int inner = 0; inner < num_iter; inner++) {
+      if (num_iter > 1 && inner == 0) c->bragg_t = K_DEF_BRAGG;
+      int n = 0;
+      if (!c->p.nhicd) {
+        memcpy(list, master, sizeof(int32_t) * nl);
+        n = nl;
+      } else if (eff % 2 == 0) {
+        listsel %= K_NHOM;
+        int n_el = (int)floor((double)nl / K_NHOM);
+        if (listsel == K_NHOM - 1) n_el += nl - n_el * K_NHOM;
+        int start = (int)(floor((double)nl / K_NHOM) * listsel);
+        memcpy(list, master + start, sizeof(int32_t) * n_el);
+        n = n_el;
+        listsel++;
+      } else {
+        orc_bf_vsc(c);
+        n = orc_bf_nh_lines(c, orc_bf_nh_threshold(c), list);
+      }
+      orc_rand_list_perm(seed + 1u + (uint32_t)calls, n, perm);
+      for (int i = 0; i < n; i++) order[perm[i]] = list[i];
+      double st[4];
+      orc_bf_sweep_lines(c, order, n, outer, inner, st);
+      status = 1;
+      int check = c->p.nhicd ? (eff % K_NNHOM == 0) : 1;
+      if (check && eff > 0 && prev_mag > 0) {
+        double ratio = fabs(orc_roi_mag_sum(c)) / fabs(prev_mag);
+        if (ratio < stop) {
+          stop *= c->p.threshold_reduction_factor;
+          status = 0;
+        }
+      }
+      if (!c->p.nhicd || eff % K_NNHOM == 0) prev_mag = orc_roi_volume_sum(c);
+      eff++;
+      calls++;
+      if (max_calls > 0 && calls >= max_calls) {
+        done = 1;
+        break;
+      }
+      if (status == 0) break;
+      if (inner == num_iter - 1 && inner != 0) {
+        temp_t = des_t;
+        c->bragg_t = temp_t;
+      }
+    }
+    if (done) break;
+    if (status == 0 && outer >= 1) break;
+    if (c->p.outer_iterations > 1) {
+      if (c->p.joint_estimation) {
+        orc_bf_joint_estimation(c);
+        orc_bf_update_selector(c);
+      }
+      if (c->p.noise_estimation) {
+        orc_bf_update_weights(c);
+        orc_bf_update_selector(c);
+      }
+    }
+  }
+  free(perm);
+  free(master);
+  free(list);
+  free(order);
+  return calls;
 }

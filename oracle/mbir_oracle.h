@@ -47,6 +47,13 @@ typedef struct orc_params {
   int32_t outer_iterations, inner_iterations;
   double threshold_reduction_factor;
   int32_t pinned_pow;         /* 1: QGGMRF powers by orc_pinned_pow instead of the C library */
+  /* bright field (BrightField/BFConstants.h, BFForwardModel) */
+  int32_t modality;           /* 0 HAADF, 1 BF */
+  int32_t noise_estimation;   /* BF NOISE_ESTIMATION (1): one global variance */
+  double bragg_threshold;     /* desired T of the Bragg selector */
+  double bragg_delta;         /* delta of the Bragg rejector */
+  double bf_offset;           /* added to the raw counts before -log */
+  int32_t nhicd;              /* BF NHICD line lists (BFConstants.h); 0: every line per call */
 } orc_params;
 
 typedef struct orc_ctx orc_ctx;
@@ -113,6 +120,34 @@ void orc_visit_order(uint32_t seed, int n_z, int n_x, int32_t* out);
  * loops with a fixed reference-order seed per sweep.  cost_log (optional, capacity n_cost)
  * receives the cost after every sweep; returns the number of sweeps run. */
 int orc_run(orc_ctx* c, uint32_t seed, double* cost_log, int n_cost);
+
+/* ---- bright field -------------------------------------------------------------------- */
+/* selector [n_theta][n_r][n_t] (1: entry selected, quadratic data term) */
+unsigned char* orc_selector(orc_ctx* c);
+double* orc_filt_map(orc_ctx* c);    /* [n_z][n_x] 5x5 Hamming-filtered mag map */
+void orc_set_bragg(orc_ctx* c, double t);
+double orc_get_bragg(const orc_ctx* c);
+/* GenRandList permutation (boost uniform_int on mt19937): out_index[i] = new position of
+ * element i */
+void orc_rand_list_perm(uint32_t seed, int n, int32_t* out_index);
+/* one BFUpdateYSlice call over voxel lines (z*n_x+x) in the given order, y ascending */
+void orc_bf_sweep_lines(orc_ctx* c, const int32_t* lines, int n_lines, int outer, int inner,
+                        double* stats);
+/* the same call in the GPU's slice order over the lines with active[z*n_x+x] != 0 */
+void orc_bf_sweep_slices(orc_ctx* c, const unsigned char* active, const int32_t* row_order,
+                         int stride, int outer, int inner, double* stats);
+void orc_bf_vsc(orc_ctx* c);
+double orc_bf_nh_threshold(const orc_ctx* c);
+int orc_bf_nh_lines(const orc_ctx* c, double threshold, int32_t* lines);
+double orc_roi_volume_sum(const orc_ctx* c);
+double orc_roi_mag_sum(const orc_ctx* c);
+void orc_bf_joint_estimation(orc_ctx* c);
+void orc_bf_update_weights(orc_ctx* c);
+void orc_bf_update_selector(orc_ctx* c);
+double orc_bf_cost(const orc_ctx* c, double* parts);
+/* BFReconstructionEngine::execute loops in reference (list) order with lists drawn from
+ * `seed`; runs at most max_calls updateVoxels calls (<= 0: no limit); returns the calls run */
+int orc_bf_run(orc_ctx* c, uint32_t seed, int max_calls);
 
 #ifdef __cplusplus
 }

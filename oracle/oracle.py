@@ -30,11 +30,15 @@ class OrcParams(C.Structure):
         ("outer_iterations", C.c_int32), ("inner_iterations", C.c_int32),
         ("threshold_reduction_factor", C.c_double),
         ("pinned_pow", C.c_int32),
+        ("modality", C.c_int32), ("noise_estimation", C.c_int32),
+        ("bragg_threshold", C.c_double), ("bragg_delta", C.c_double), ("bf_offset", C.c_double),
+        ("nhicd", C.c_int32),
     ]
 
 
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int32)
+_U8 = C.POINTER(C.c_uint8)
 _lib = None
 
 
@@ -79,6 +83,22 @@ def lib():
             "orc_cost": (C.c_double, [C.c_void_p, _D]),
             "orc_visit_order": (None, [C.c_uint32, C.c_int, C.c_int, _I]),
             "orc_run": (C.c_int, [C.c_void_p, C.c_uint32, _D, C.c_int]),
+            "orc_selector": (_U8, [C.c_void_p]), "orc_filt_map": (_D, [C.c_void_p]),
+            "orc_set_bragg": (None, [C.c_void_p, C.c_double]),
+            "orc_get_bragg": (C.c_double, [C.c_void_p]),
+            "orc_rand_list_perm": (None, [C.c_uint32, C.c_int, _I]),
+            "orc_bf_sweep_lines": (None, [C.c_void_p, _I, C.c_int, C.c_int, C.c_int, _D]),
+            "orc_bf_sweep_slices": (None, [C.c_void_p, _U8, _I, C.c_int, C.c_int, C.c_int, _D]),
+            "orc_bf_vsc": (None, [C.c_void_p]),
+            "orc_bf_nh_threshold": (C.c_double, [C.c_void_p]),
+            "orc_bf_nh_lines": (C.c_int, [C.c_void_p, C.c_double, _I]),
+            "orc_roi_volume_sum": (C.c_double, [C.c_void_p]),
+            "orc_roi_mag_sum": (C.c_double, [C.c_void_p]),
+            "orc_bf_joint_estimation": (None, [C.c_void_p]),
+            "orc_bf_update_weights": (None, [C.c_void_p]),
+            "orc_bf_update_selector": (None, [C.c_void_p]),
+            "orc_bf_cost": (C.c_double, [C.c_void_p, _D]),
+            "orc_bf_run": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int]),
         }
         for n, (r, a) in sig.items():
             f = getattr(L, n)
@@ -124,6 +144,16 @@ def params_from_mbir(p):
     # the engine's reference-exact mode (FP64, reference order) evaluates powers by the
     # pinned method; the oracle does the same for that mode
     o.pinned_pow = 1 if (p.precision == 1 and p.order_mode == 1) else 0
+    o.modality = p.modality
+    o.noise_estimation = p.noise_estimation
+    o.bragg_threshold = p.bragg_threshold
+    o.bragg_delta = p.bragg_delta
+    o.bf_offset = p.bf_offset
+    o.nhicd = p.nhicd
+    if p.modality == 1:
+        # the BF command line turns the void dosage into the offset d = -log(dosage + bf_offset)
+        # (BFReconstructionArgsParser.cpp:272-274)
+        o.default_offset = -np.log(p.default_dosage + p.bf_offset) if p.use_default_offset else 0.0
     return o
 
 
@@ -255,6 +285,71 @@ class Oracle:
         c = lib().orc_cost(self._h, parts.ctypes.data_as(_D))
         return c, parts
 
+    # ---- bright field ---------------------------------------------------------------------
+    def selector(self):
+        return self._view(lib().orc_selector, self.shape)
+
+    def mag_map(self):
+        return self._view(lib().orc_mag_map, (self.nz, self.nx))
+
+    def filt_map(self):
+        return self._view(lib().orc_filt_map, (self.nz, self.nx))
+
+    def set_bragg(self, t):
+        lib().orc_set_bragg(self._h, t)
+
+    def bragg(self):
+        return lib().orc_get_bragg(self._h)
+
+    def bf_sweep_lines(self, lines, outer=0, inner=0):
+        lines = np.ascontiguousarray(lines, np.int32)
+        st = np.zeros(4)
+        lib().orc_bf_sweep_lines(self._h, lines.ctypes.data_as(_I), len(lines), outer, inner,
+                                 st.ctypes.data_as(_D))
+        return st
+
+    def bf_sweep_slices(self, active, row_order, stride, outer=0, inner=0):
+        active = np.ascontiguousarray(active, np.uint8)
+        rows = np.ascontiguousarray(row_order, np.int32)
+        st = np.zeros(4)
+        lib().orc_bf_sweep_slices(self._h, active.ctypes.data_as(_U8), rows.ctypes.data_as(_I),
+                                  stride, outer, inner, st.ctypes.data_as(_D))
+        return st
+
+    def bf_vsc(self):
+        lib().orc_bf_vsc(self._h)
+
+    def bf_nh_threshold(self):
+        return lib().orc_bf_nh_threshold(self._h)
+
+    def bf_nh_lines(self, threshold):
+        out = np.zeros(self.nz * self.nx, np.int32)
+        n = lib().orc_bf_nh_lines(self._h, threshold, out.ctypes.data_as(_I))
+        return out[:n]
+
+    def roi_volume_sum(self):
+        return lib().orc_roi_volume_sum(self._h)
+
+    def roi_mag_sum(self):
+        return lib().orc_roi_mag_sum(self._h)
+
+    def bf_joint_estimation(self):
+        lib().orc_bf_joint_estimation(self._h)
+
+    def bf_update_weights(self):
+        lib().orc_bf_update_weights(self._h)
+
+    def bf_update_selector(self):
+        lib().orc_bf_update_selector(self._h)
+
+    def bf_cost(self):
+        parts = np.zeros(3)
+        c = lib().orc_bf_cost(self._h, parts.ctypes.data_as(_D))
+        return c, parts
+
+    def bf_run(self, seed, max_calls=0):
+        return lib().orc_bf_run(self._h, seed, max_calls)
+
     def run(self, seed, n_cost=0):
         log = np.zeros(max(n_cost, 1))
         n = lib().orc_run(self._h, seed, log.ctypes.data_as(_D) if n_cost else None, n_cost)
@@ -265,6 +360,13 @@ def visit_order(seed, nz, nx):
     out = np.zeros(nz * nx, np.int32)
     lib().orc_visit_order(seed, nz, nx, out.ctypes.data_as(_I))
     return out
+
+
+def rand_list_perm(seed, n):
+    """GenRandList's permutation: element i of a list goes to position out[i]."""
+    out = np.zeros(max(n, 1), np.int32)
+    lib().orc_rand_list_perm(seed, n, out.ctypes.data_as(_I))
+    return out[:n]
 
 
 def pinned_pow(x, y):

@@ -296,10 +296,9 @@ def test_sweep_staging_modes_match_oracle(lib_built, oracle_mod, staging):
     e.prepare()
     assert e.status().staged == (1 if staging == 0 else 0)
     o.prepare()
-    for k in range(2):
-        rows, stride = e.schedule(k)
-        e.sweep(0, k)
-        o.sweep_slices(rows, stride, 0, k)
+    rows, stride = e.schedule(0)
+    e.sweep(0, 0)
+    o.sweep_slices(rows, stride, 0, 0)
     assert rel(e.volume(), o.volume()) <= 1e-5
 
 
