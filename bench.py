@@ -2,17 +2,23 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload ...]
 
-A step is one full ICD sweep (every voxel of the volume visited once) of a HAADF
-reconstruction resident in HBM.  The default workload is the 512 x 256 x 128 volume with 61
-views over +-60 deg at 2 deg on a 512 x 256 detector (nanoparticles on a substrate, seeded
-synthetic data).  Metric: voxel updates per second (voxel visits per sweep / sweep time).
+Default workload: bright-field (BF) reconstruction of a 512 x 256 x 128 (x, y, z) volume from 61
+views over +-60 deg at 2 deg on a 512 x 256 detector: 200 ellipsoid nanoparticles on a slab,
+seeded synthetic Poisson counts at 1e4 electrons with +-3% per-view dose drift (the engine
+takes -log itself).  A step is one NHICD equivalent iteration: 20 updateVoxels calls (10 on
+homogeneous 1/20 line lists, 10 on the non-homogeneous top-1/20 lists), i.e. about one sweep's
+worth of voxel updates.  HAADF workloads (one step = one full ICD sweep) remain selectable.
 
-Timing: W untimed warm-up sweeps, then K sweeps each bracketed by CUDA events on the engine's
-launching stream; between timed sweeps a 512 MiB buffer is written to flush the 129 MB L2.
-`e2e` runs the same workload through the public C ABI from host buffers: upload of the tilt
-series, forward projection, sweeps with gain/offset and variance updates, and read-back of the
-volume, all inside the timed region.  `--impl reference` times the reference algorithm on the
-host cores instead (CPU, bounded sample of the same workload).
+Metric: voxel updates per second = voxels updated in the timed steps / ICD device time
+(zero-skipped visits are reported beside it, not counted).
+
+Timing: W untimed warm-up steps, then K steps whose ICD kernels are bracketed by CUDA events on
+the engine's launching stream (the engine accumulates them); before every timed step a 512 MiB
+buffer is written to flush the 129 MB L2.  `e2e` runs the same workload through the public C
+ABI from host buffers: upload of the tilt series, set-up and forward projection, calls with
+offset and variance updates, and read-back of the volume, all inside the timed region.
+`--impl reference` times the reference algorithm (the FP64 oracle restatement of the
+reference's multi-threaded CPU path) on all host cores on a bounded sample of the workload.
 """
 import argparse
 import json
@@ -30,12 +36,14 @@ sys.path.insert(0, PKG)
 import numpy as np  # noqa: E402
 
 WORKLOADS = {
-    # name: (n_r, n_t, thickness_nm, max_deg, step_deg, particles)
-    "haadf-512x256x128-61v": (512, 256, 64.0, 60.0, 2.0, 200),
-    "haadf-128x32x64-71v": (128, 32, 32.0, 70.0, 2.0, 0),
+    # name: (modality, n_r, n_t, thickness_nm, max_deg, step_deg, particles)
+    "bf-512x256x128-61v": ("BF", 512, 256, 64.0, 60.0, 2.0, 200),
+    "haadf-512x256x128-61v": ("HAADF", 512, 256, 64.0, 60.0, 2.0, 200),
+    "haadf-128x32x64-71v": ("HAADF", 128, 32, 32.0, 70.0, 2.0, 0),
 }
-DEFAULT_WORKLOAD = "haadf-512x256x128-61v"
+DEFAULT_WORKLOAD = "bf-512x256x128-61v"
 METRIC = "ICD voxel-updates/s"
+CALLS_PER_EQUIT = 20  # k_NumNonHomogeniousIter: updateVoxels calls per equivalent iteration
 
 
 def load_peaks():
@@ -49,23 +57,33 @@ def load_peaks():
 
 def make_data(name, seed=0, n_t_override=None):
     import synthetic
-    n_r, n_t, th, mx, st, npart = WORKLOADS[name]
+    mod, n_r, n_t, th, mx, st, npart = WORKLOADS[name]
     if n_t_override:
         n_t = n_t_override
-    if npart == 0:
+    if mod == "BF":
+        y, ang = synthetic.bf_particles_on_slab(n_r=n_r, n_t=n_t, thickness=th, max_deg=mx,
+                                                step_deg=st, n_particles=npart, seed=seed)
+    elif npart == 0:
         y, ang, _ = synthetic.haadf_two_spheres(n_r=n_r, n_t=n_t, max_deg=mx, step_deg=st,
                                                 seed=seed)
     else:
         y, ang, _ = synthetic.particles_on_slab(n_r=n_r, n_t=n_t, thickness=th, max_deg=mx,
                                                 step_deg=st, n_particles=npart, seed=seed)
-    return y, ang, th
+    return y, ang, th, mod
 
 
-def params_for(mbir, th, outer=20, inner=1):
-    p = mbir.default_params()
+def params_for(mbir, th, mod, outer=20, inner=1):
+    if mod == "BF":
+        p = mbir.default_params(mbir.BF)
+        p.sigma_x = 0.02
+        p.use_default_offset = 1
+        p.default_dosage = 1.0e4
+        p.bragg_threshold = 5.0e10  # Bragg rejection off, as the workload runs it
+    else:
+        p = mbir.default_params()
+        p.sigma_x = 0.2
     p.sample_thickness = th
     p.diffuseness = 0.1
-    p.sigma_x = 0.2
     p.num_resolutions = 1
     p.outer_iterations = outer
     p.inner_iterations = inner
@@ -122,26 +140,54 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
-def cpu_reference_sample(name, sweeps=3, n_t=8, threads=None):
-    """The reference algorithm on the host cores: the oracle's CPU restatement of the
-    reference ICD (same visit order and arithmetic), on the workload's x-z geometry with
-    n_t detector rows (n_t voxel slices).  Returns voxel updates/s and the description."""
+def cpu_reference_sample(name, budget_s=12.0, n_t=32, threads=None, max_calls=None):
+    """The reference algorithm on the host cores: the oracle's restatement of the reference's
+    CPU path (same arithmetic; y split into one contiguous range per worker as the reference's
+    task split) on the workload's x-z geometry with n_t detector rows (n_t voxel slices), for
+    about `budget_s` seconds of calls.  BF: NHICD calls (homogeneous and non-homogeneous lists
+    alternating); HAADF: full sweeps.  Returns the cpu_baseline dict (voxel updates/s)."""
     sys.path.insert(0, ORACLE)
     import mbir
     import oracle
-    y, ang, th = make_data(name, n_t_override=n_t)
-    p = params_for(mbir, th)
+    threads = threads or os.cpu_count() or 1
+    y, ang, th, mod = make_data(name, n_t_override=n_t)
+    p = params_for(mbir, th, mod)
     o = oracle.Oracle(oracle.params_from_mbir(p), y, ang)
     o.prepare()
-    o.sweep_reference(1, 0, 0)  # first sweep touches every voxel; later sweeps skip zeros
+    upd = 0.0
+    calls = 0
     t0 = time.perf_counter()
-    for k in range(sweeps):
-        o.sweep_reference(1, 0, k + 1)
+    if mod == "BF":
+        nl = o.nz * o.nx
+        perm = oracle.rand_list_perm(p.seed, nl)
+        master = np.empty(nl, np.int32)
+        master[perm] = np.arange(nl, dtype=np.int32)
+        n_el = nl // CALLS_PER_EQUIT
+        while True:
+            k = calls
+            if k % 2 == 0:
+                s = (k // 2) % CALLS_PER_EQUIT
+                lines = master[s * n_el:(s + 1) * n_el]
+            else:
+                o.bf_vsc()
+                lines = o.bf_nh_lines(o.bf_nh_threshold())
+            upd += o.bf_sweep_lines_mt(lines, 0 if k == 0 else 1, 0, threads)[3]
+            calls += 1
+            if (max_calls and calls >= max_calls) or time.perf_counter() - t0 > budget_s:
+                break
+        what = f"{calls} NHICD calls"
+    else:
+        while True:
+            upd += o.sweep_reference_mt(1, 0 if calls == 0 else 1, 0, threads)[3]
+            calls += 1
+            if (max_calls and calls >= max_calls) or time.perf_counter() - t0 > budget_s:
+                break
+        what = f"{calls} reference-order sweeps"
     dt = time.perf_counter() - t0
-    vox = o.nz * o.nx * o.ny
-    return {"value": vox * sweeps / dt, "unit": "voxel-updates/s", "cores": 1, "kind": "port",
+    return {"value": upd / dt, "unit": "voxel-updates/s", "cores": threads, "kind": "port",
             "sample": f"{o.nz}x{o.nx}x{o.ny} volume ({n_t} detector rows of the workload), "
-                      f"{sweeps} reference-order ICD sweeps, FP64 oracle, 1 thread"}
+                      f"{what}, FP64 oracle restatement of the reference's CPU path, "
+                      f"{threads} threads, {dt:.1f} s"}
 
 
 def run_reference(args):
@@ -149,13 +195,14 @@ def run_reference(args):
     if rank != 0:
         return
     t0 = time.perf_counter()
-    res = cpu_reference_sample(args.workload, sweeps=max(args.steps, 1))
+    budget = min(60.0, max(5.0, 4.0 * max(args.steps, 1)))
+    res = cpu_reference_sample(args.workload, budget_s=budget)
     wall = time.perf_counter() - t0
     line = {"metric": METRIC, "value": res["value"], "unit": res["unit"], "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": args.workload, "note": "CPU sample of the workload"},
+            "config": {"workload": args.workload, "note": "bounded CPU sample of the workload"},
             "cpu_baseline": res,
             "e2e": {"value": res["value"], "unit": res["unit"], "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
@@ -166,7 +213,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
@@ -191,23 +238,28 @@ def main():
     pkg_build.build()
     import mbir
 
-    y, ang, th = make_data(args.workload, seed=rank)
-    p = params_for(mbir, th)
+    y, ang, th, mod = make_data(args.workload, seed=rank)
+    bf = mod == "BF"
+    p = params_for(mbir, th, mod)
     p.device = local
     eng = mbir.Engine(p)
     eng.set_sinogram(y, ang)
     eng.prepare()
     nz, nx, ny = eng.dims()[:3]
-    nvox = nz * nx * ny
     flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")
+    calls_per_step = CALLS_PER_EQUIT if bf else 1
+    ncall = [0]
 
-    def step(k):
-        st = eng.sweep(0, k)
-        return st
+    def step():
+        tot = np.zeros(4)
+        for _ in range(calls_per_step):
+            k = ncall[0]
+            tot += eng.sweep(0 if k == 0 else 1, 0)  # zero skipping after the first call
+            ncall[0] += 1
+        return tot
 
-    for k in range(args.warmup):
-        step(k)
-    st0 = eng.status()
+    for _ in range(args.warmup):
+        step()
 
     def barrier():
         if dist is not None:
@@ -223,7 +275,7 @@ def main():
             flush.fill_(float(k))
             torch.cuda.synchronize()
             before = eng.status().icd_ms_total
-            s = step(args.warmup + k)
+            s = step()
             per_ms.append(eng.status().icd_ms_total - before)
             upd += s[3]
             visited += s[2] + s[3]
@@ -234,20 +286,24 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     ms_step = total_ms / args.steps
-    value = world * visited / (total_ms / 1e3) / max(1, 1)
+    value = world * upd / (total_ms / 1e3)
     st = eng.status()
 
-    # roofline of the ICD sweep kernel: algorithmic bytes per updated voxel = 8 F L + 8
+    # roofline of the ICD kernels: algorithmic bytes per updated voxel = 8 F L + 8
+    # (+ 5 F L for bright field: FP32 weight + u8 selector per footprint entry)
     f_mean = st.footprint_entries / float(nz * nx)
-    bytes_step = (upd / args.steps) * (8.0 * f_mean * st.t_rows + 8.0)
+    per_vox = (13.0 if bf else 8.0) * f_mean * st.t_rows + 8.0
+    bytes_step = (upd / args.steps) * per_vox
     peak, peak_kind = load_peaks()
     achieved = bytes_step / (ms_step / 1e3) / 1e9
+    launches = calls_per_step * 3  # two colour launches + one stats reduction per call
     traffic = None
     tp = os.path.join(ROOT, "profiles", "icd_sweep_traffic.json")
     if os.path.exists(tp):
         try:
             with open(tp) as f:
-                traffic = json.load(f).get(args.workload)
+                ent = json.load(f).get(args.workload)
+            traffic = ent.get("bytes_per_launch") if isinstance(ent, dict) else ent
         except Exception:
             traffic = None
 
@@ -255,25 +311,31 @@ def main():
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic",
-           "config": {"workload": args.workload, "volume_zxy": [nz, nx, ny],
-                      "views": int(y.shape[0]), "detector": [int(y.shape[1]), int(y.shape[2])],
-                      "modality": "HAADF", "order": "parallel (red/black y, conflict-free x)",
-                      "l2": "flushed between timed steps (512 MiB write)",
+           "config": {"workload": args.workload, "modality": mod,
+                      "volume_zxy": [nz, nx, ny], "views": int(y.shape[0]),
+                      "detector": [int(y.shape[1]), int(y.shape[2])],
+                      "step": ("one NHICD equivalent iteration (20 updateVoxels calls)" if bf
+                               else "one full ICD sweep"),
+                      "order": "parallel (red/black y, conflict-free x)",
+                      "l2": "flushed before every timed step (512 MiB write)",
                       "parallelism": f"replicas x{world}",
                       "voxels_updated_per_step": upd / args.steps,
                       "voxels_visited_per_step": visited / args.steps,
                       "slices_in_smem": bool(st.staged), "x_stride": st.stride},
-           "gpu_launches": 3 * args.steps,
+           "gpu_launches": launches * args.steps,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "traffic": traffic,
                         "peak_source": peak_kind,
-                        "bytes_model": "8*F*L+8 per updated voxel, F=A-column nnz, L=t rows",
-                        "kernel": "sweep_kernel (2 colour launches + 1 stats reduce per step)"},
+                        "algorithmic_bytes_per_step": bytes_step,
+                        "bytes_model": ("13*F*L+8" if bf else "8*F*L+8") +
+                                       " per updated voxel, F=A-column nnz, L=t rows",
+                        "kernel": "sweep_kernel (two colour launches per call)"},
            "clocks": clk.summary()}
 
     if not args.no_e2e:
         # end to end through the C ABI from host buffers
-        pe = params_for(mbir, th, outer=3, inner=1)
+        n_outer = CALLS_PER_EQUIT if bf else 3
+        pe = params_for(mbir, th, mod, outer=n_outer, inner=1)
         pe.device = local
         host_vol = np.empty((nz, nx, ny), np.float32)
         barrier()
@@ -284,10 +346,11 @@ def main():
             host_vol[...] = e2.volume()
             s2 = e2.status()
         dt = time.perf_counter() - t0
-        out["e2e"] = {"value": s2.voxels_visited / dt * world, "unit": "voxel-updates/s",
-                      "h2d_bytes_per_step": int(y.nbytes), "d2h_bytes_per_step": int(host_vol.nbytes),
-                      "step": "mbir_set_sinogram + mbir_run (3 outer iterations: sweep, gain/offset,"
-                              " variance) + mbir_get_volume, host buffers",
+        out["e2e"] = {"value": s2.voxels_updated / dt * world, "unit": "voxel-updates/s",
+                      "h2d_bytes_per_step": int(y.nbytes),
+                      "d2h_bytes_per_step": int(host_vol.nbytes),
+                      "step": f"mbir_set_sinogram + mbir_run ({n_outer} outer iterations: call, "
+                              "offset and variance updates) + mbir_get_volume, host buffers",
                       "wall_s": dt}
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_reference_sample(args.workload)

@@ -179,6 +179,18 @@ int32_t mbir_get_nuisance(mbir_engine* e, double* gains, double* offsets, double
 int32_t mbir_get_tables(mbir_engine* e, double* H, double* Ht);
 /* parallel-mode schedule: row order of sweep `sweep` (N_z entries) and the x stride */
 int32_t mbir_get_schedule(mbir_engine* e, int32_t sweep, int32_t* row_order, int32_t* stride);
+/* voxel lines (z*N_x + x) of the last sweep or bright-field call: the visit order in reference
+ * order, ascending in parallel order (a bright-field NHICD call updates a subset of lines).
+ * *n receives the count; lines may be null to query it. */
+int32_t mbir_get_call_lines(mbir_engine* e, int32_t* lines, int32_t cap, int32_t* n);
+/* bright field: Bragg selector [theta][r][t] (1 = selected), weights [theta][r][t], per-line
+ * update magnitudes and their VSC-filtered map [z][x], current Bragg threshold T.  Outputs may
+ * be null.  Replaces BFForwardModel's selector/weight state and the magUpdateMap of
+ * BFReconstructionEngine::execute (BFReconstructionEngine.cpp:670-690). */
+int32_t mbir_get_bf_state(mbir_engine* e, uint8_t* selector, float* weights, double* mag,
+                          double* filtered_mag, double* bragg_t);
+/* BFForwardModel::setBraggThreshold (BFForwardModel.h): T used by the next calls */
+int32_t mbir_set_bragg_threshold(mbir_engine* e, double t);
 int32_t mbir_status_get(mbir_engine* e, mbir_status* st);
 void mbir_cancel(mbir_engine* e);
 

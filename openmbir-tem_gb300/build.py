@@ -17,9 +17,11 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmbir_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["mbir_sweep_f32.cu", "mbir_sweep_f32_hbm.cu", "mbir_sweep_f64.cu", "mbir_kernels.cu",
-           "mbir_exact.cu",
-           "mbir_engine.cu", "mbir_batch.cu", "mbir_server.cpp", "mrc_io.cpp",
+SOURCES = ["mbir_sweep_f32.cu", "mbir_sweep_f32_bf.cu", "mbir_sweep_f32_hbm.cu",
+           "mbir_sweep_f32_batch3.cu", "mbir_sweep_f32_batch5.cu", "mbir_sweep_f64.cu",
+           "mbir_kernels.cu",
+           "mbir_exact.cu", "mbir_bf.cu",
+           "mbir_engine.cu", "mbir_engine_bf.cu", "mbir_batch.cu", "mbir_server.cpp", "mrc_io.cpp",
            "mbir_capi.cpp"]
 HEADERS = ["mbir_internal.h", "mbir_engine.h", "mbir_sweep.cuh", "mbir_batch.h",
            "mbir_server.h"]
@@ -52,7 +54,7 @@ def _compile(src, verbose=False, ptxas_v=False):
     cmd[1:1] = ["-Xcompiler", "-ffp-contract=off"]
     if src.endswith(".cu"):
         cmd[1:1] = ARCH + ["-lineinfo", "--expt-relaxed-constexpr"]
-        if src == "mbir_exact.cu":
+        if src in ("mbir_exact.cu", "mbir_bf.cu"):
             cmd[1:1] = ["-fmad=false"]
         if ptxas_v:
             cmd.insert(1, "-Xptxas=-v")

@@ -138,8 +138,8 @@ int Batch::sweep(const std::vector<std::pair<int, int>>& iters, double* stats) {
   for (int i = 0; i < n; i++)
     if (!args[i].smem_rows)
       smem = std::max(smem, sweep_smem_bytes(args[i].g.n_theta, args[i].g.n_x, 0, 1,
-                                             args[i].g.bins, 0));
-  const int vpl = max_theta <= 64 ? 4 : (max_theta <= 128 ? 8 : 10);
+                                             args[i].g.bins, 0, 0));
+  const int shape = lane_shape(max_theta);
   if (dirty_ || items_.empty()) {
     if ((rc = build_items(args))) return rc;
     dirty_ = false;
@@ -157,7 +157,7 @@ int Batch::sweep(const std::vector<std::pair<int, int>>& iters, double* stats) {
   b.done = d_ctr_ + 1;
   b.need = d_ctr_ + 1 + n;
   cudaEventRecord(static_cast<cudaEvent_t>(ev0_), s);
-  rc = launch_batch_sweep(b, nb, vpl, smem, grid_, s);
+  rc = launch_batch_sweep(b, nb, shape, smem, grid_, s);
   if (rc) return fail(MBIR_EDEVICE, std::string("batch sweep launch: ") +
                                         cudaGetErrorString(cudaGetLastError()));
   for (int i = 0; i < n; i++) {

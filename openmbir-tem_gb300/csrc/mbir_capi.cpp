@@ -87,6 +87,19 @@ void mbir_params_default(mbir_params* p, int32_t modality) {
   p->compat_double_angle = modality == MBIR_MODALITY_BF ? 0 : 1;
   p->cost_every_sweep = 0;
   p->device = 0;
+  p->slice_staging = 0;
+  p->nhicd = 0;
+  if (modality == MBIR_MODALITY_BF) {
+    // BFReconstructionArgsParser.cpp:143-226 and BFReconstructionEngine.cpp:246-260
+    p->stop_threshold = 0.001;
+    p->outer_iterations = 600;
+    p->inner_iterations = 100;
+    p->bragg_threshold = 3.0;
+    p->bragg_delta = 0.5;
+    p->noise_estimation = 1;
+    p->noise_model = 0;
+    p->nhicd = 1;  // NHICD is defined in BFConstants.h
+  }
 }
 
 mbir_engine* mbir_create(const mbir_params* p) {
@@ -94,8 +107,14 @@ mbir_engine* mbir_create(const mbir_params* p) {
     g_create_error = "mbir_create: params missing or struct_size mismatch";
     return nullptr;
   }
-  if (p->modality != MBIR_MODALITY_HAADF) {
-    g_create_error = "mbir_create: only the HAADF modality is built";
+  if (p->modality != MBIR_MODALITY_HAADF && p->modality != MBIR_MODALITY_BF) {
+    g_create_error = "mbir_create: unknown modality";
+    return nullptr;
+  }
+  if (p->modality == MBIR_MODALITY_BF &&
+      (!(p->bragg_threshold > 0) || !(p->bragg_delta >= 0) ||
+       (p->use_default_offset && !(p->default_dosage + p->bf_offset > 0)))) {
+    g_create_error = "mbir_create: invalid bright-field parameter";
     return nullptr;
   }
   if (!(p->sigma_x > 0) || p->num_resolutions < 1 || p->final_resolution < 1 ||
@@ -183,6 +202,18 @@ int32_t mbir_get_tables(mbir_engine* e, double* H, double* Ht) {
 }
 int32_t mbir_get_schedule(mbir_engine* e, int32_t sweep, int32_t* rows, int32_t* stride) {
   return guarded(e, [&](mbir::Engine& m) { return m.get_schedule(sweep, rows, stride); });
+}
+int32_t mbir_get_call_lines(mbir_engine* e, int32_t* lines, int32_t cap, int32_t* n) {
+  return guarded(e, [&](mbir::Engine& m) { return m.get_call_lines(lines, cap, n); });
+}
+int32_t mbir_get_bf_state(mbir_engine* e, uint8_t* selector, float* weights, double* mag,
+                          double* filtered_mag, double* bragg_t) {
+  return guarded(e, [&](mbir::Engine& m) {
+    return m.get_bf_state(selector, weights, mag, filtered_mag, bragg_t);
+  });
+}
+int32_t mbir_set_bragg_threshold(mbir_engine* e, double t) {
+  return guarded(e, [&](mbir::Engine& m) { return m.set_bragg_threshold(t); });
 }
 int32_t mbir_status_get(mbir_engine* e, mbir_status* st) {
   return guarded(e, [&](mbir::Engine& m) { return m.status(st); });

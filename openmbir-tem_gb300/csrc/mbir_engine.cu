@@ -86,6 +86,7 @@ Engine::Engine(const mbir_params& p) : p_(p) {
   if (p_.qggmrf_q == 0.0) p_.qggmrf_q = p_.diffuseness + 1.0;
   fp64_ = p_.precision == MBIR_PRECISION_FP64 ? 1 : 0;
   exact_ = fp64_ && p_.order_mode == MBIR_ORDER_REFERENCE;
+  bf_ = p_.modality == MBIR_MODALITY_BF;
   rb_ = fp64_ ? sizeof(double) : sizeof(float);
   bins_ = p_.detector_response_bins > 0 ? p_.detector_response_bins : 64;
 }
@@ -123,6 +124,16 @@ void Engine::release() {
   dfree(d_partial_);
   dfree(d_vsum_);
   dfree(d_err_);
+  dfree(d_w_);
+  dfree(d_sel_);
+  dfree(d_magfx_);
+  dfree(d_mag_);
+  dfree(d_filt_);
+  dfree(d_active_);
+  dfree(d_bfpart_);
+  dfree(d_bfout_);
+  dfree(d_alpha_);
+  dfree(d_stage64_);
   if (ev0_) cudaEventDestroy(static_cast<cudaEvent_t>(ev0_));
   if (ev1_) cudaEventDestroy(static_cast<cudaEvent_t>(ev1_));
   if (stream_) cudaStreamDestroy(static_cast<cudaStream_t>(stream_));
@@ -419,7 +430,7 @@ int Engine::init_nuisance_host() {
   // createInitialGainsData / OffsetsData / VariancesData (HAADF_ForwardModel.cpp:248-402)
   init_gain_.assign(nt, p_.target_gain);
   if (!user_gain_.empty()) init_gain_ = user_gain_;
-  init_offset_.assign(nt, p_.default_offset);
+  init_offset_.assign(nt, bf_ ? bf_default_offset() : p_.default_offset);
   if (!user_offset_.empty()) {
     init_offset_ = user_offset_;
   } else if (!p_.use_default_offset) {
@@ -462,13 +473,16 @@ int Engine::init_nuisance_host() {
     const double t = p_.target_gain / s;
     for (int k = 0; k < nt; k++) I_[k] = init_gain_[k] * t;
   }
-  // calculateMeasurementWeight (_Extra.cpp:693-771), IDENTITY_NOISE_MODEL: w = 1 / alpha
+  // calculateMeasurementWeight (_Extra.cpp:693-771), IDENTITY_NOISE_MODEL: w = 1 / alpha.
+  // Bright field: per-entry weights (bf_upload); alpha starts at the initial variance when
+  // NOISE_ESTIMATION is on (BFForwardModel.cpp:337-341).
   alpha_.assign(nt, 1.0);
   w_.assign(nt, 1.0);
+  const bool per_view_var = bf_ ? p_.noise_estimation != 0 : p_.noise_model != 0;
   for (int k = 0; k < nt; k++) {
-    if (p_.noise_model) {
+    if (per_view_var) {
       alpha_[k] = init_var_[k];
-      w_[k] = 1.0 / alpha_[k];
+      if (!bf_) w_[k] = 1.0 / alpha_[k];
     }
   }
   return MBIR_OK;
@@ -482,9 +496,10 @@ int Engine::alloc_device() {
   n_rs_ = (n_rp_ % 32 == 0) ? n_rp_ + 4 : n_rp_;
   int max_smem = 0;
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, p_.device);
-  smem_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, n_rs_, t_rows_, bins_, fp64_);
+  n_sp_ = bf_ ? (g.n_r + 15) / 16 * 16 : 0;
+  smem_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, n_rs_, t_rows_, bins_, fp64_, n_sp_);
   stage_ = smem_bytes_ <= static_cast<size_t>(max_smem) && p_.slice_staging == 0;
-  if (!stage_) smem_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, 0, t_rows_, bins_, fp64_);
+  if (!stage_) smem_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, 0, t_rows_, bins_, fp64_, 0);
   const size_t ns = static_cast<size_t>(g.n_t) * g.n_theta * n_rp_;
   const size_t nh = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;
   const size_t nv = static_cast<size_t>(g.n_z) * g.n_x * g.n_y;
@@ -521,6 +536,19 @@ int Engine::alloc_device() {
                                  static_cast<size_t>(prior_blocks_));
   rc |= dmalloc(&d_vsum_, static_cast<size_t>(g.n_theta) * 6);
   rc |= dmalloc(&d_err_, 1);
+  if (bf_) {
+    const size_t nl = static_cast<size_t>(g.n_z) * g.n_x;
+    rc |= dmalloc_bytes(&d_w_, ns * rb_);
+    rc |= dmalloc(&d_sel_, static_cast<size_t>(g.n_t) * g.n_theta * n_sp_);
+    rc |= dmalloc(&d_magfx_, nl);
+    rc |= dmalloc(&d_mag_, nl);
+    rc |= dmalloc(&d_filt_, nl);
+    rc |= dmalloc(&d_active_, nl);
+    rc |= dmalloc(&d_bfpart_, 4096);
+    rc |= dmalloc(&d_bfout_, 16);
+    rc |= dmalloc(&d_alpha_, g.n_theta);
+    rc |= dmalloc(&d_stage64_, nh);
+  }
   if (rc) return fail(MBIR_ENOMEM, "device allocation failed");
   cudaStream_t s;
   if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
@@ -576,6 +604,7 @@ int Engine::build_host() {
     return fail(MBIR_ENOTSUP, "voxel/detector size ratio must be 1, 2 or 4");
   if ((rc = compute_stride())) return rc;
   if ((rc = init_nuisance_host())) return rc;
+  if (bf_ && (rc = bf_prepare_host())) return rc;
   host_ready_ = true;
   return MBIR_OK;
 }
@@ -639,9 +668,15 @@ int Engine::prepare() {
 
   // measured sinogram -> [t][theta][r_pad]
   const size_t nh = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;
-  cudaMemcpyAsync(d_stage_, counts_.data(), sizeof(float) * nh, cudaMemcpyHostToDevice, s);
-  if ((rc = launch_sino_to_dev(d_stage_, d_y_, g.n_theta, g.n_r, n_rp_, g.n_t, fp64_, s)))
-    return cuda_check(rc, "sinogram upload");
+  if (bf_) {
+    cudaMemcpyAsync(d_stage64_, ylog_.data(), sizeof(double) * nh, cudaMemcpyHostToDevice, s);
+    if ((rc = launch_layout_from_double(d_stage64_, d_y_, g.n_theta, g.n_r, n_rp_, g.n_t, fp64_, s)))
+      return cuda_check(rc, "sinogram upload");
+  } else {
+    cudaMemcpyAsync(d_stage_, counts_.data(), sizeof(float) * nh, cudaMemcpyHostToDevice, s);
+    if ((rc = launch_sino_to_dev(d_stage_, d_y_, g.n_theta, g.n_r, n_rp_, g.n_t, fp64_, s)))
+      return cuda_check(rc, "sinogram upload");
+  }
 
   // initial volume (InitialReconstructionInitializer::initializeData, :74-90)
   const size_t nv = static_cast<size_t>(g.n_z) * g.n_x * g.n_y;
@@ -704,6 +739,7 @@ int Engine::prepare() {
   sweeps_done_ = 0;
   // forward projection + error sinogram (HAADF_ReconstructionEngine.cpp:636-691)
   if ((rc = forward_project())) return rc;
+  if (bf_ && (rc = bf_upload())) return rc;
   return MBIR_OK;
 }
 
@@ -767,6 +803,7 @@ void Engine::row_order_for_sweep(int sweep, std::vector<int32_t>& order) const {
 int Engine::sweep(int outer, int inner, double* stats4) {
   if (state_ < 2) return fail(MBIR_ESTATE, "sweep: call prepare first");
   if (cancel_.load()) return fail(MBIR_ECANCELLED, "cancelled");
+  if (bf_) return bf_call(outer, inner, stats4);
   const Geometry& g = g_;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
   const int iter_nonzero = (inner > 0 || outer > 0) ? 1 : 0;
@@ -775,6 +812,7 @@ int Engine::sweep(int outer, int inner, double* stats4) {
   if (p_.order_mode == MBIR_ORDER_REFERENCE) {
     std::vector<int32_t> lines;
     reference_visit_order(p_.seed, g.n_z, g.n_x, lines);
+    call_lines_ = lines;
     cudaMemcpyAsync(d_lines_, lines.data(), sizeof(int32_t) * lines.size(), cudaMemcpyHostToDevice, s);
     if (exact_) {
       ExactArgs ea = exact_args();
@@ -920,6 +958,7 @@ int Engine::batch_finish(int outer, int inner, const double* st, double ms) {
 // jointEstimation, gain + offset branch (HAADF_ReconstructionEngine_Extra.cpp:419-636)
 int Engine::joint_estimation() {
   if (state_ < 2) return fail(MBIR_ESTATE, "joint_estimation: call prepare first");
+  if (bf_) return bf_joint_estimation();
   const Geometry& g = g_;
   const int nt = g.n_theta;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
@@ -965,6 +1004,7 @@ int Engine::joint_estimation() {
 // updateWeights (HAADF_ReconstructionEngine_Extra.cpp:795-881), IDENTITY_NOISE_MODEL
 int Engine::update_weights() {
   if (state_ < 2) return fail(MBIR_ESTATE, "update_weights: call prepare first");
+  if (bf_) return bf_update_weights();
   const Geometry& g = g_;
   const int nt = g.n_theta;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
@@ -986,6 +1026,7 @@ int Engine::update_weights() {
 // computeCost (HAADF_ReconstructionEngine.cpp:1147-1364): data + prior + noise terms
 int Engine::compute_cost(double* parts3, double* total) {
   if (state_ < 2) return fail(MBIR_ESTATE, "compute_cost: call prepare first");
+  if (bf_) return bf_compute_cost(parts3, total);
   const Geometry& g = g_;
   const int nt = g.n_theta;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
@@ -1026,6 +1067,12 @@ int Engine::run() {
   int rc = prepare();
   if (rc) return rc;
   state_ = 3;
+  if (bf_) {
+    if ((rc = bf_run())) return rc;
+    state_ = 4;
+    total_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return MBIR_OK;
+  }
   double stop = p_.stop_threshold;
   int num_iter = p_.inner_iterations;
   for (int outer = 0; outer < p_.outer_iterations; outer++) {

@@ -75,6 +75,12 @@ class Engine {
   int get_nuisance(double* g, double* o, double* v);
   int get_tables(double* H, double* Ht);
   int get_schedule(int sweep, int32_t* row_order, int32_t* stride);
+  // lines (z*n_x+x) of the last sweep/call in visit order (reference order) or ascending
+  int get_call_lines(int32_t* lines, int32_t cap, int32_t* n) const;
+  // bright field: selector [theta][r][t], weights [theta][r][t], magnitude map [z][x],
+  // filtered map [z][x], current Bragg threshold (each output optional)
+  int get_bf_state(uint8_t* sel, float* w, double* mag, double* filt, double* bragg_t);
+  int set_bragg_threshold(double t);
   int status(mbir_status* st) const;
   void cancel() { cancel_.store(1); }
   int write_outputs(const char* dir, const char* mrc_path);
@@ -100,6 +106,20 @@ class Engine {
   int check_errors() { return check_device_error(); }
 
  private:
+  // bright field (mbir_engine_bf.cu)
+  int bf_prepare_host();                          // -log counts, master line list
+  int bf_upload();                                // y, weights, selector, maps
+  int bf_call_begin(int outer, int inner, DevBF* out);  // list, active mask, magnitude reset
+  int bf_call_end();                              // magnitude map, counters
+  int bf_call(int outer, int inner, double* stats4);
+  int bf_joint_estimation();
+  int bf_update_weights();
+  int bf_compute_cost(double* parts3, double* total);
+  int bf_run();
+  int bf_roi_sum(int kind, double* out);
+  BfSino bf_sino() const;
+  double bf_default_offset() const;
+
   int build_host();  // geometry, tables, stride, initial nuisance: no GPU needed
   int build_geometry();
   int build_tables();
@@ -131,6 +151,8 @@ class Engine {
   int nb_ = 3;        // candidate bins per view (2*half_width + 1)
   int n_rp_ = 0;      // HBM row stride
   int n_rs_ = 0;      // shared-memory row stride
+  int n_sp_ = 0;      // bright-field selector row stride (bytes, multiple of 16)
+  bool bf_ = false;   // bright-field modality
   int t_rows_ = 1;    // max t rows per voxel slice
   int stride_ = 2;    // conflict-free x stride
   bool stage_ = true; // slice fits in shared memory
@@ -192,7 +214,30 @@ class Engine {
   double total_ms_ = 0.0;
   int64_t visited_ = 0, updated_ = 0;
   int64_t footprint_entries_ = 0;
+
+  // bright-field state
+  void* d_w_ = nullptr;                     // Real [n_t][n_theta][n_rp] weights
+  uint8_t* d_sel_ = nullptr;                // [n_t][n_theta][n_sp] Bragg selector
+  unsigned long long* d_magfx_ = nullptr;   // [n_z][n_x] fixed-point magnitudes of a call
+  double* d_mag_ = nullptr;                 // [n_z][n_x] update-magnitude map
+  double* d_filt_ = nullptr;                // [n_z][n_x] VSC-filtered map
+  uint8_t* d_active_ = nullptr;             // [n_z][n_x] lines of the current call
+  double* d_bfpart_ = nullptr;              // reduction partials
+  double* d_bfout_ = nullptr;               // reduction results
+  double* d_alpha_ = nullptr;               // [n_theta] variance per view
+  double* d_stage64_ = nullptr;             // FP64 host-layout staging
+  std::vector<double> ylog_;                // -log(counts + bf_offset), [theta][r][t]
+  std::vector<int32_t> bf_master_;          // random permutation of all lines
+  std::vector<int32_t> call_lines_;         // lines of the last sweep/call
+  std::vector<uint8_t> active_host_;
+  uint32_t bf_listsel_ = 0, bf_eff_ = 0;
+  int bf_calls_ = 0;
+  double bragg_t_ = 0;
 };
+
+// GenRandList's permutation (Common/VoxelUpdateList.cpp:157-215) drawn from mt19937 through
+// boost's uniform_int(0, n-1): element i of a list goes to position out[i].
+void rand_list_perm(uint32_t seed, int n, std::vector<int32_t>& out);
 
 // MRC I/O (mrc_io.cpp)
 struct MrcVolume {

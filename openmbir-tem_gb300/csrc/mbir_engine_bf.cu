@@ -1,0 +1,503 @@
+// mbir_engine_bf.cu -- bright-field (BF) side of the engine: -log counts, per-entry weights and
+// the Bragg selector, the non-homogeneous ICD (NHICD) line lists, offset-only joint estimation,
+// the single global noise variance, the BF cost and the BFReconstructionEngine::execute loops.
+//
+// Reference: Code/MBIRLib/BrightField/BFReconstructionEngine.cpp:555-858 (execute loops),
+// BFReconstructionEngine_Extra.cpp:476-1273 (updateVoxels, NHICD, stop rule),
+// BFForwardModel.cpp:328-531, 812-972 (weights, estimates, selector, cost, raw counts).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "mbir_engine.h"
+
+namespace mbir {
+
+namespace {
+constexpr int kNumHomogeneous = 20;     // MBIR::Constants::k_NumHomogeniousIter
+constexpr int kNumNonHomogeneous = 20;  // k_NumNonHomogeniousIter
+constexpr double kDefBragg = 5e10;      // DefBraggThreshold (BFConstants.h)
+
+// boost::uniform_int<uint32_t>(0, range) on mt19937: the raw draw divided by the bucket size,
+// redrawn when the quotient exceeds range
+uint32_t uniform_draw(MT19937& gen, uint32_t range) {
+  const uint32_t brange = 0xffffffffu;
+  if (range == 0) return 0;
+  if (range == brange) return gen.next();
+  uint32_t bucket = brange / (range + 1u);
+  if (brange % (range + 1u) == range) ++bucket;
+  for (;;) {
+    const uint32_t r = gen.next() / bucket;
+    if (r <= range) return r;
+  }
+}
+}  // namespace
+
+void rand_list_perm(uint32_t seed, int n, std::vector<int32_t>& out) {
+  out.resize(std::max(n, 0));
+  for (int i = 0; i < n; i++) out[i] = i;
+  if (n < 2) return;
+  MT19937 gen(seed);
+  for (int i = 1; i < n; i++) {
+    const uint32_t r = uniform_draw(gen, static_cast<uint32_t>(n - 1));
+    if (r >= static_cast<uint32_t>(n)) continue;
+    std::swap(out[i], out[r]);
+  }
+}
+
+// the BF command line passes the offset d = -log(default_dosage + bf_offset)
+// (BFReconstructionArgsParser.cpp:272-274)
+double Engine::bf_default_offset() const {
+  return -std::log(p_.default_dosage + p_.bf_offset);
+}
+
+// processRawCounts (BFForwardModel.cpp:939-972): counts + bf_offset, then -log(c / BF_MAX) with
+// BF_MAX = 1; the nuisance parameters were created from the raw counts before this (execute
+// :374-385).  A negative count ends its (theta, r) row early, as the reference's break does.
+int Engine::bf_prepare_host() {
+  const Geometry& g = g_;
+  const size_t nh = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;
+  ylog_.resize(nh);
+  for (int th = 0; th < g.n_theta; th++)
+    for (int r = 0; r < g.n_r; r++) {
+      const size_t b = (static_cast<size_t>(th) * g.n_r + r) * g.n_t;
+      bool stopped = false;
+      for (int t = 0; t < g.n_t; t++) {
+        double v = static_cast<double>(counts_[b + t]);
+        if (!stopped) {
+          v += p_.bf_offset;
+          if (v < 0) {
+            stopped = true;
+          } else {
+            v = -std::log(v / 1.0);
+          }
+        }
+        ylog_[b + t] = v;
+      }
+    }
+  // GenRegularList + GenRandList (execute :555-559): position perm[i] holds line i
+  const int nl = g.n_z * g.n_x;
+  std::vector<int32_t> perm;
+  rand_list_perm(p_.seed, nl, perm);
+  bf_master_.assign(nl, 0);
+  for (int i = 0; i < nl; i++) bf_master_[perm[i]] = i;
+  bf_listsel_ = 0;
+  bf_eff_ = 0;
+  bf_calls_ = 0;
+  bragg_t_ = p_.bragg_threshold;
+  return MBIR_OK;
+}
+
+BfSino Engine::bf_sino() const {
+  BfSino b{};
+  b.e = d_e_;
+  b.w = d_w_;
+  b.sel = d_sel_;
+  b.n_theta = g_.n_theta;
+  b.n_r = g_.n_r;
+  b.n_rp = n_rp_;
+  b.n_sp = n_sp_;
+  b.n_t = g_.n_t;
+  b.fp64 = fp64_;
+  return b;
+}
+
+// calculateMeasurementWeight (BFForwardModel.cpp:328-385) without IDENTITY_NOISE_MODEL:
+// w = BF_MAX / exp(y), divided by the view's variance when NOISE_ESTIMATION is on; every entry
+// selected.
+int Engine::bf_upload() {
+  const Geometry& g = g_;
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const size_t nh = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;
+  std::vector<double> w(nh);
+  for (int th = 0; th < g.n_theta; th++)
+    for (int r = 0; r < g.n_r; r++)
+      for (int t = 0; t < g.n_t; t++) {
+        const size_t i = (static_cast<size_t>(th) * g.n_r + r) * g.n_t + t;
+        double v = 1.0 / std::exp(ylog_[i]);
+        if (p_.noise_estimation) v /= alpha_[th];
+        w[i] = v;
+      }
+  cudaMemcpyAsync(d_stage64_, w.data(), sizeof(double) * nh, cudaMemcpyHostToDevice, s);
+  int rc = launch_layout_from_double(d_stage64_, d_w_, g.n_theta, g.n_r, n_rp_, g.n_t, fp64_, s);
+  if (rc) return cuda_check(rc, "weights upload");
+  cudaMemsetAsync(d_sel_, 1, static_cast<size_t>(g.n_t) * g.n_theta * n_sp_, s);
+  const size_t nl = static_cast<size_t>(g.n_z) * g.n_x;
+  cudaMemsetAsync(d_magfx_, 0, sizeof(unsigned long long) * nl, s);
+  cudaMemsetAsync(d_mag_, 0, sizeof(double) * nl, s);
+  cudaMemsetAsync(d_filt_, 0, sizeof(double) * nl, s);
+  cudaMemsetAsync(d_active_, 1, nl, s);
+  cudaMemcpyAsync(d_alpha_, alpha_.data(), sizeof(double) * g.n_theta, cudaMemcpyHostToDevice, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "BF upload");
+  return MBIR_OK;
+}
+
+// The lines of one updateVoxels call (BFReconstructionEngine.cpp:610-646 and
+// BFReconstructionEngine_Extra.cpp:576-628): without NHICD every line; with NHICD the even
+// calls take the next 1/20 of the master permutation (the last sublist takes the remainder),
+// the odd calls the lines whose VSC-filtered update magnitude exceeds the order statistic at
+// N - N/20.  Uploads the active mask and clears the calls' line magnitudes.
+int Engine::bf_call_begin(int outer, int inner, DevBF* out) {
+  (void)outer;
+  (void)inner;
+  const Geometry& g = g_;
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const int nl = g.n_z * g.n_x;
+  std::vector<int32_t> list;
+  if (!p_.nhicd) {
+    list = bf_master_;
+  } else if (bf_eff_ % 2 == 0) {
+    bf_listsel_ %= kNumHomogeneous;
+    int n_el = static_cast<int>(std::floor(static_cast<double>(nl) / kNumHomogeneous));
+    if (bf_listsel_ == kNumHomogeneous - 1) n_el += nl - n_el * kNumHomogeneous;
+    const int start = static_cast<int>(std::floor(static_cast<double>(nl) / kNumHomogeneous) *
+                                       bf_listsel_);
+    list.assign(bf_master_.begin() + start, bf_master_.begin() + start + n_el);
+    bf_listsel_++;
+  } else {
+    // ComputeVSC + SetNonHomThreshold + GenNonHomList (_Extra.cpp:888-1047)
+    int rc = launch_bf_vsc(d_mag_, d_filt_, g.n_z, g.n_x, s);
+    if (rc) return cuda_check(rc, "VSC filter");
+    std::vector<double> filt(nl);
+    cudaMemcpyAsync(filt.data(), d_filt_, sizeof(double) * nl, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "VSC read");
+    std::vector<double> tmp = filt;
+    size_t k = static_cast<size_t>(nl) - static_cast<size_t>(nl) / kNumNonHomogeneous;
+    if (k >= static_cast<size_t>(nl)) k = nl - 1;
+    std::nth_element(tmp.begin(), tmp.begin() + k, tmp.end());
+    const double thr = tmp[k];
+    for (int l = 0; l < nl; l++)
+      if (filt[l] > thr) list.push_back(l);
+  }
+  if (p_.order_mode == MBIR_ORDER_REFERENCE) {
+    // the call's visit order: GenRandList of its list (one worker), seeded per call
+    std::vector<int32_t> perm;
+    rand_list_perm(p_.seed + 1u + static_cast<uint32_t>(bf_calls_), static_cast<int>(list.size()),
+                   perm);
+    call_lines_.assign(list.size(), 0);
+    for (size_t i = 0; i < list.size(); i++) call_lines_[perm[i]] = list[i];
+  } else {
+    call_lines_ = list;
+    std::sort(call_lines_.begin(), call_lines_.end());
+  }
+  active_host_.assign(nl, 0);
+  for (int32_t l : list) active_host_[l] = 1;
+  cudaMemcpyAsync(d_active_, active_host_.data(), nl, cudaMemcpyHostToDevice, s);
+  int rc = launch_bf_mag_reset(d_magfx_, d_active_, nl, s);
+  if (rc) return cuda_check(rc, "magnitude reset");
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "call setup");
+  if (out) {
+    out->w = d_w_;
+    out->sel = d_sel_;
+    out->n_sp = n_sp_;
+    out->active = d_active_;
+    out->mag_fx = d_magfx_;
+    out->bragg_t = bragg_t_;
+    out->bragg_dt = p_.bragg_delta * bragg_t_;
+  }
+  return MBIR_OK;
+}
+
+int Engine::bf_call_end() {
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const int nl = g_.n_z * g_.n_x;
+  if (!exact_) {
+    int rc = launch_bf_mag_update(d_magfx_, d_active_, d_mag_, nl, s);
+    if (rc) return cuda_check(rc, "magnitude map");
+  }
+  bf_calls_++;
+  bf_eff_++;
+  return MBIR_OK;
+}
+
+// One updateVoxels call: lines of the call in the GPU slice order (parallel) or in the call's
+// visit order with y ascending (reference order).
+int Engine::bf_call(int outer, int inner, double* st4) {
+  const Geometry& g = g_;
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const int iter_nonzero = (inner > 0 || outer > 0) ? 1 : 0;
+  DevBF bfa{};
+  int rc = bf_call_begin(outer, inner, &bfa);
+  if (rc) return rc;
+  cudaEventRecord(static_cast<cudaEvent_t>(ev0_), s);
+  if (p_.order_mode == MBIR_ORDER_REFERENCE) {
+    cudaMemcpyAsync(d_lines_, call_lines_.data(), sizeof(int32_t) * call_lines_.size(),
+                    cudaMemcpyHostToDevice, s);
+    if (exact_) {
+      ExactArgs ea = exact_args();
+      ea.lines = d_lines_;
+      ea.n_lines = static_cast<int>(call_lines_.size());
+      ea.iter_nonzero = iter_nonzero;
+      ea.zero_skipping = p_.zero_skipping;
+      ea.stats = d_stat4_;
+      ea.bf = 1;
+      ea.bw = static_cast<const double*>(d_w_);
+      ea.bsel = d_sel_;
+      ea.n_sp = n_sp_;
+      ea.bragg_t = bragg_t_;
+      ea.bragg_delta = p_.bragg_delta;
+      ea.mag = d_mag_;
+      if ((rc = launch_exact_icd(ea, s))) return cuda_check(rc, "BF call (exact)");
+    } else {
+      RefOrderArgs a{};
+      a.g = dg_;
+      a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_,
+                        d_lineok_};
+      a.flt = flt_;
+      a.x = d_x_;
+      a.e = d_e_;
+      a.lines = d_lines_;
+      a.n_lines = static_cast<int>(call_lines_.size());
+      a.iter_nonzero = iter_nonzero;
+      a.zero_skipping = p_.zero_skipping;
+      a.fp64 = fp64_;
+      a.bf = 1;
+      a.bfa = bfa;
+      a.stats = d_stat4_;
+      if ((rc = launch_ref_order(a, nb_, s))) return cuda_check(rc, "BF call (reference order)");
+    }
+  } else {
+    std::vector<int32_t> rows;
+    row_order_for_sweep(sweeps_done_, rows);
+    cudaMemcpyAsync(d_rows_, rows.data(), sizeof(int) * g.n_z, cudaMemcpyHostToDevice, s);
+    SweepArgs a{};
+    a.g = dg_;
+    a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_,
+                      d_lineok_};
+    a.flt = flt_;
+    a.x = d_x_;
+    a.e = d_e_;
+    a.row_order = d_rows_;
+    a.stride = stride_;
+    a.mode = kModeICD;
+    a.fp64 = fp64_;
+    a.bf = 1;
+    a.bfa = bfa;
+    a.iter_nonzero = iter_nonzero;
+    a.zero_skipping = p_.zero_skipping;
+    a.smem_rows = stage_ ? 1 : 0;
+    a.n_rs = stage_ ? n_rs_ : 0;
+    a.err = d_err_;
+    const int n0 = (g.n_y + 1) / 2;
+    for (int colour = 0; colour < 2; colour++) {
+      a.colour = colour;
+      a.n_slices = (g.n_y - colour + 1) / 2;
+      a.stats = d_stats_ + (colour ? static_cast<size_t>(n0) * kStatSlots : 0);
+      if (a.n_slices <= 0) continue;
+      if ((rc = launch_sweep(a, nb_, smem_bytes_, s))) return cuda_check(rc, "BF call launch");
+    }
+    if ((rc = launch_reduce_stats(d_stats_, g.n_y, kStatSlots, d_stat4_, s)))
+      return cuda_check(rc, "stats reduce");
+  }
+  cudaEventRecord(static_cast<cudaEvent_t>(ev1_), s);
+  if ((rc = bf_call_end())) return rc;
+  double st[kStatSlots];
+  cudaMemcpyAsync(st, d_stat4_, sizeof(st), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "BF call");
+  if ((rc = check_device_error())) return rc;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, static_cast<cudaEvent_t>(ev0_), static_cast<cudaEvent_t>(ev1_));
+  icd_ms_ += ms;
+  sweeps_done_++;
+  visited_ += static_cast<int64_t>(st[2] + st[3]);
+  updated_ += static_cast<int64_t>(st[3]);
+  last_rel_ = st[1] > 0 ? st[0] / st[1] : 0.0;
+  outer_ = outer;
+  inner_ = inner;
+  if (st4)
+    for (int i = 0; i < 4; i++) st4[i] = st[i];
+  return MBIR_OK;
+}
+
+// BFForwardModel::jointEstimation (BFForwardModel.cpp:390-441) followed by updateSelector, as
+// execute() pairs them (BFReconstructionEngine.cpp:836-838)
+int Engine::bf_joint_estimation() {
+  const int nt = g_.n_theta;
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const BfSino b = bf_sino();
+  int rc = launch_bf_offset_sums(b, exact_ ? 1 : 0, bragg_t_, p_.bragg_delta, d_partial_,
+                                 n_chunk_, d_vsum_, s);
+  if (rc) return cuda_check(rc, "offset sums");
+  std::vector<double> vs(static_cast<size_t>(nt) * 2), step(nt);
+  cudaMemcpyAsync(vs.data(), d_vsum_, sizeof(double) * vs.size(), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "offset sums");
+  for (int v = 0; v < nt; v++) {
+    step[v] = vs[v * 2 + 0] / vs[v * 2 + 1];
+    mu_[v] += step[v];
+  }
+  cudaMemcpyAsync(d_mu2_, step.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, s);
+  if ((rc = launch_bf_offset_apply(b, d_mu2_, s))) return cuda_check(rc, "offset apply");
+  if ((rc = launch_bf_selector(b, bragg_t_, s))) return cuda_check(rc, "selector");
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "offset step");
+  return upload_views();
+}
+
+// BFForwardModel::updateWeights (BFForwardModel.cpp:447-511) followed by updateSelector
+// (BFReconstructionEngine.cpp:850-851)
+int Engine::bf_update_weights() {
+  const Geometry& g = g_;
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const BfSino b = bf_sino();
+  cudaMemcpyAsync(d_alpha_, alpha_.data(), sizeof(double) * g.n_theta, cudaMemcpyHostToDevice, s);
+  int rc = launch_bf_variance_sums(b, exact_ ? 1 : 0, d_alpha_, d_bfpart_, d_bfout_, s);
+  if (rc) return cuda_check(rc, "variance sums");
+  double sums[2];
+  cudaMemcpyAsync(sums, d_bfout_, sizeof(sums), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "variance sums");
+  const double upd = (sums[0] + (p_.bragg_delta * bragg_t_) * sums[1]) /
+                     (g.n_theta * g.n_r * g.n_t);
+  for (int v = 0; v < g.n_theta; v++) alpha_[v] = upd;
+  if ((rc = launch_bf_scale_weights(b, upd, s))) return cuda_check(rc, "weight scale");
+  if ((rc = launch_bf_selector(b, bragg_t_, s))) return cuda_check(rc, "selector");
+  cudaMemcpyAsync(d_alpha_, alpha_.data(), sizeof(double) * g.n_theta, cudaMemcpyHostToDevice, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "variance");
+  return MBIR_OK;
+}
+
+// BFReconstructionEngine::computeCost (BFReconstructionEngine.cpp:1084-1097): forwardCost
+// (data term over selected / rejected entries, halved, plus (N/2) log(alpha_0) with the
+// reference's integer N/2) + QGGMRF::PriorModelCost
+int Engine::bf_compute_cost(double* parts3, double* total) {
+  const Geometry& g = g_;
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  int rc = launch_bf_cost_sums(bf_sino(), exact_ ? 1 : 0, bragg_t_, p_.bragg_delta, d_bfpart_,
+                               d_bfout_, s);
+  if (rc) return cuda_check(rc, "BF data term");
+  double* prior_partial = d_partial_ + static_cast<size_t>(g.n_theta) * n_chunk_ * 6;
+  rc = launch_prior_cost(d_x_, flt_, g.n_z, g.n_x, g.n_y, prior_partial, prior_blocks_, fp64_, s);
+  if (rc) return cuda_check(rc, "cost prior term");
+  double data = 0;
+  std::vector<double> pp(prior_blocks_);
+  cudaMemcpyAsync(&data, d_bfout_, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(pp.data(), prior_partial, sizeof(double) * prior_blocks_, cudaMemcpyDeviceToHost,
+                  s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "BF cost");
+  data /= 2;
+  double prior = 0;
+  for (double v : pp) prior += v;
+  double noise = 0;
+  if (p_.noise_estimation)
+    noise = static_cast<double>((g.n_theta * g.n_r * g.n_t) / 2) * std::log(alpha_[0]);
+  if (parts3) {
+    parts3[0] = data;
+    parts3[1] = prior;
+    parts3[2] = noise;
+  }
+  last_cost_ = data + noise + prior;
+  if (total) *total = last_cost_;
+  return MBIR_OK;
+}
+
+int Engine::bf_roi_sum(int kind, double* out) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  int rc = launch_roi_sum(dg_, exact_ ? 1 : 0, kind, d_mag_, d_x_, fp64_, d_bfpart_, d_bfout_, s);
+  if (rc) return cuda_check(rc, "ROI sum");
+  cudaMemcpyAsync(out, d_bfout_, sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "ROI sum");
+  return MBIR_OK;
+}
+
+// BFReconstructionEngine::execute outer/inner loops (BFReconstructionEngine.cpp:595-858):
+// the Bragg threshold starts at DefBraggThreshold while the first outer iteration's inner
+// calls run (when there is more than one) and is set to the requested T after them; the stop
+// rule compares the ROI sum of the update-magnitude map with the ROI volume sum of the previous
+// equivalent iteration (stopCriteria, _Extra.cpp:1217-1273); JE and variance updates follow
+// each outer iteration when there is more than one.
+int Engine::bf_run() {
+  const int nl = g_.n_z * g_.n_x;
+  (void)nl;
+  int num_iter = p_.inner_iterations;
+  double des_t = 0, temp_t;
+  if (num_iter > 1) {
+    des_t = p_.bragg_threshold;
+    temp_t = kDefBragg;
+  } else {
+    temp_t = p_.bragg_threshold;
+  }
+  bragg_t_ = temp_t;
+  double prev_mag = 0, stop = p_.stop_threshold;
+  int rc;
+  for (int outer = 0; outer < p_.outer_iterations; outer++) {
+    if (outer > 0) {
+      num_iter = 1;
+      bragg_t_ = temp_t;
+    }
+    int status = 1;
+    for (int inner = 0; inner < num_iter; inner++) {
+      if (num_iter > 1 && inner == 0) bragg_t_ = kDefBragg;
+      const uint32_t eff = bf_eff_;
+      double st[4];
+      if ((rc = bf_call(outer, inner, st))) return rc;
+      if (p_.cost_every_sweep && (rc = bf_compute_cost(nullptr, nullptr))) return rc;
+      status = 1;
+      const bool check = p_.nhicd ? (eff % kNumNonHomogeneous == 0) : true;
+      if (check && eff > 0 && prev_mag > 0) {
+        double mag_sum = 0;
+        if ((rc = bf_roi_sum(0, &mag_sum))) return rc;
+        if (std::fabs(mag_sum) / std::fabs(prev_mag) < stop) {
+          stop *= p_.threshold_reduction_factor;
+          status = 0;
+        }
+      }
+      if (!p_.nhicd || eff % kNumNonHomogeneous == 0)
+        if ((rc = bf_roi_sum(1, &prev_mag))) return rc;
+      if (cancel_.load()) return fail(MBIR_ECANCELLED, "cancelled");
+      if (status == 0) break;
+      if (inner == num_iter - 1 && inner != 0) {
+        temp_t = des_t;
+        bragg_t_ = temp_t;
+      }
+    }
+    if (status == 0 && outer >= 1) break;
+    if (p_.outer_iterations > 1) {
+      if (p_.joint_estimation && (rc = bf_joint_estimation())) return rc;
+      if (p_.noise_estimation && (rc = bf_update_weights())) return rc;
+    }
+  }
+  return MBIR_OK;
+}
+
+int Engine::get_call_lines(int32_t* lines, int32_t cap, int32_t* n) const {
+  if (n) *n = static_cast<int32_t>(call_lines_.size());
+  if (lines) {
+    if (cap < static_cast<int32_t>(call_lines_.size())) return MBIR_EINVAL;
+    std::copy(call_lines_.begin(), call_lines_.end(), lines);
+  }
+  return MBIR_OK;
+}
+
+int Engine::get_bf_state(uint8_t* sel, float* w, double* mag, double* filt, double* bragg) {
+  if (state_ < 2) return fail(MBIR_ESTATE, "get_bf_state: call prepare first");
+  if (!bf_) return fail(MBIR_EINVAL, "get_bf_state: not a bright-field engine");
+  const Geometry& g = g_;
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const size_t nl = static_cast<size_t>(g.n_z) * g.n_x;
+  if (bragg) *bragg = bragg_t_;
+  if (mag) cudaMemcpyAsync(mag, d_mag_, sizeof(double) * nl, cudaMemcpyDeviceToHost, s);
+  if (filt) cudaMemcpyAsync(filt, d_filt_, sizeof(double) * nl, cudaMemcpyDeviceToHost, s);
+  if (w) {
+    int rc = launch_sino_to_host(d_w_, d_stage_, g.n_theta, g.n_r, n_rp_, g.n_t, fp64_, s);
+    if (rc) return cuda_check(rc, "weights read-out");
+    cudaMemcpyAsync(w, d_stage_, sizeof(float) * g.n_theta * g.n_r * g.n_t, cudaMemcpyDeviceToHost,
+                    s);
+  }
+  if (sel) {
+    std::vector<uint8_t> dev(static_cast<size_t>(g.n_t) * g.n_theta * n_sp_);
+    cudaMemcpyAsync(dev.data(), d_sel_, dev.size(), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "selector");
+    for (int th = 0; th < g.n_theta; th++)
+      for (int r = 0; r < g.n_r; r++)
+        for (int t = 0; t < g.n_t; t++)
+          sel[(static_cast<size_t>(th) * g.n_r + r) * g.n_t + t] =
+              dev[(static_cast<size_t>(t) * g.n_theta + th) * n_sp_ + r];
+  }
+  return cudaStreamSynchronize(s) == cudaSuccess ? MBIR_OK : cuda_check(MBIR_EDEVICE, "BF state");
+}
+
+int Engine::set_bragg_threshold(double t) {
+  if (!(t > 0)) return fail(MBIR_EINVAL, "Bragg threshold must be > 0");
+  bragg_t_ = t;
+  return MBIR_OK;
+}
+
+}  // namespace mbir

@@ -216,9 +216,11 @@ __global__ void __launch_bounds__(32, 1) exact_icd_kernel(ExactArgs A) {
   const size_t plane = static_cast<size_t>(g.n_z) * g.n_x;
   const size_t sino_plane = static_cast<size_t>(g.n_theta) * g.n_rp;
   double st[kStatSlots] = {0, 0, 0, 0};
+  const size_t sel_plane = A.bf ? static_cast<size_t>(g.n_theta) * A.n_sp : 0;
   for (int n = 0; n < A.n_lines; ++n) {
     const int l = A.lines[n];
     const int jn = l / g.n_x, kn = l % g.n_x;
+    if (A.bf && lane == 0) A.mag[l] = 0;  // BFUpdateYSlice.cpp:171
     build_column(A, jn, kn, &col);
     if (col.n == 0) continue;
     for (int i = 0; i < g.n_y; ++i) {
@@ -282,10 +284,27 @@ __global__ void __launch_bounds__(32, 1) exact_icd_kernel(ExactArgs A) {
           for (int a = 0; a < tc; a++) {
             const size_t ei = static_cast<size_t>(t0 + a) * sino_plane +
                               static_cast<size_t>(th) * g.n_rp + r;
-            const double pe = k0 * hv[a];
             const double evv = pre ? ev[q * 2 + a] : e[ei];
-            th2 += (pe * pe * A.weight[th]);
-            th1 += (evv * pe * A.weight[th]);
+            if (A.bf) {
+              // BFForwardModel::computeTheta (BFForwardModel.cpp:866-887)
+              const double w = A.bw[ei];
+              const size_t si = static_cast<size_t>(t0 + a) * sel_plane +
+                                static_cast<size_t>(th) * A.n_sp + r;
+              if (A.bsel[si] == 1) {
+                const double pe = k0 * hv[a];
+                th2 += (pe * pe * w);
+                th1 += (evv * pe * w);
+              } else {
+                const double qc = (A.bragg_delta * A.bragg_t) / (fabs(evv) * sqrt(w));
+                const double pe = k0 * hv[a];
+                th2 += qc * (pe * pe * w);
+                th1 += qc * (evv * pe * w);
+              }
+            } else {
+              const double pe = k0 * hv[a];
+              th2 += (pe * pe * A.weight[th]);
+              th1 += (evv * pe * A.weight[th]);
+            }
           }
         }
         th1 *= -1;
@@ -312,6 +331,7 @@ __global__ void __launch_bounds__(32, 1) exact_icd_kernel(ExactArgs A) {
         if (nv < 0.0) nv = 0.0;
         s_new = nv;
         vol[vidx] = nv;
+        if (A.bf) A.mag[l] = A.mag[l] + fabs(nv - V);
         if (kn >= g.roi_x0 && kn <= g.roi_x1 && jn >= g.roi_z0 && jn <= g.roi_z1) {
           st[0] += fabs(nv - V);
           st[1] += fabs(V);
@@ -329,6 +349,11 @@ __global__ void __launch_bounds__(32, 1) exact_icd_kernel(ExactArgs A) {
                             static_cast<size_t>(th) * g.n_rp + r;
           const double k2 = (A.gain[th] * (col.val[q] * hv[a] * (nv - V)));
           e[ei] -= k2;
+          if (A.bf) {  // BFForwardModel::updateErrorSinogram (BFForwardModel.cpp:921-929)
+            const size_t si = static_cast<size_t>(t0 + a) * sel_plane +
+                              static_cast<size_t>(th) * A.n_sp + r;
+            A.bsel[si] = (fabs(e[ei] * sqrt(A.bw[ei])) < A.bragg_t) ? 1 : 0;
+          }
         }
       }
       __syncwarp();

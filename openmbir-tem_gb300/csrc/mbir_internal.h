@@ -15,6 +15,10 @@
 namespace mbir {
 
 constexpr int kMaxViewsPerLane = 5;   // n_theta <= 160
+
+// Voxel-group shape of the FP32 sweep kernels for n_theta views: 0 = 16 lanes x 4 views per
+// lane (two voxels per warp), 1 = 32 lanes x 3 views, 2 = 32 lanes x 5 views.
+inline int lane_shape(int n_theta) { return n_theta <= 64 ? 0 : (n_theta <= 96 ? 1 : 2); }
 constexpr int kWarps = 16;            // warps per ICD block
 constexpr int kMaxTRows = 4;          // t rows a voxel slice may touch
 constexpr int kStatSlots = 4;         // sum|dx| (ROI), sum|x| (ROI), zero-skipped, updated
@@ -50,6 +54,24 @@ struct DevFilter {
 
 enum SweepMode : int { kModeICD = 0, kModeProject = 1 };
 
+// Fixed-point scale of the per-line update magnitudes and the ROI sums accumulated with
+// integer atomics (integer addition is associative, so the sums do not depend on the order in
+// which voxels finish): value = count * 2^-32.
+constexpr double kFixScale = 4294967296.0;
+
+// Bright-field extras of a sweep (BFForwardModel / BFUpdateYSlice).  Per-entry arrays share the
+// sinogram layout [t][theta][row]; the selector rows are padded to n_sp bytes (a multiple of 16)
+// so a slice's selector rows are bulk-copied like its error rows.
+struct DevBF {
+  const void* w;                // Real [n_t][n_theta][n_rp] measurement weights
+  uint8_t* sel;                 // [n_t][n_theta][n_sp] Bragg selector (1 = selected)
+  int n_sp;                     // selector row stride (bytes)
+  const uint8_t* active;        // [n_z][n_x] lines of this call (nullptr: all lines)
+  unsigned long long* mag_fx;   // [n_z][n_x] fixed-point sum |dx| per line (nullptr: off)
+  double bragg_t;               // current Bragg threshold T
+  double bragg_dt;              // delta * T
+};
+
 struct SweepArgs {
   DevGeom g;
   DevTables tab;
@@ -66,6 +88,8 @@ struct SweepArgs {
   int smem_rows;         // 1: stage the slice in shared memory
   int n_rs;              // shared-memory row stride (values)
   int fp64;              // 1: Real = double
+  int bf;                // 1: bright-field data term (DevBF below)
+  DevBF bfa;
   double* stats;         // [gridDim.x][kStatSlots]
   int* err;              // device error word
 };
@@ -91,6 +115,8 @@ struct RefOrderArgs {
   int iter_nonzero;
   int zero_skipping;
   int fp64;
+  int bf;
+  DevBF bfa;
   double* stats;         // [kStatSlots]
 };
 
@@ -114,7 +140,42 @@ struct ExactArgs {
   int n_lines;
   int iter_nonzero, zero_skipping;
   double* stats;         // [kStatSlots]
+  // bright field (BFUpdateYSlice / BFForwardModel::computeTheta, updateErrorSinogram)
+  int bf;
+  const double* bw;      // [n_t][n_theta][n_rp] weights
+  uint8_t* bsel;         // [n_t][n_theta][n_sp] selector
+  int n_sp;
+  double bragg_t, bragg_delta;
+  double* mag;           // [n_z][n_x] per-line sum |dx| (reset for each line of the call)
 };
+
+// Bright-field sinogram-wide passes (mbir_bf.cu).  Arrays share the [t][theta][row] layout.
+struct BfSino {
+  void* e;               // Real error sinogram
+  void* w;               // Real weights
+  uint8_t* sel;          // selector, rows of n_sp bytes
+  int n_theta, n_r, n_rp, n_sp, n_t;
+  int fp64;
+};
+int launch_layout_from_double(const double* host_layout, void* dev_layout, int n_theta, int n_r,
+                              int n_rp, int n_t, int fp64, void* stream);
+int launch_bf_offset_sums(const BfSino& b, int exact, double T, double dl, double* partial,
+                          int n_chunk, double* out, void* stream);
+int launch_bf_offset_apply(const BfSino& b, const double* step, void* stream);
+int launch_bf_selector(const BfSino& b, double T, void* stream);
+int launch_bf_variance_sums(const BfSino& b, int exact, const double* alpha, double* partial,
+                            double* out, void* stream);
+int launch_bf_scale_weights(const BfSino& b, double alpha, void* stream);
+int launch_bf_cost_sums(const BfSino& b, int exact, double T, double dl, double* partial,
+                        double* out, void* stream);
+int launch_bf_mag_reset(unsigned long long* fx, const uint8_t* active, int n, void* stream);
+int launch_bf_mag_update(const unsigned long long* fx, const uint8_t* active, double* mag, int n,
+                         void* stream);
+int launch_bf_vsc(const double* mag, double* filt, int n_z, int n_x, void* stream);
+int launch_bf_nh_mask(const double* filt, double thr, uint8_t* active, int n, void* stream);
+int launch_roi_sum(const DevGeom& g, int exact, int kind, const double* mag, const void* x,
+                   int fp64, double* partial, double* out, void* stream);
+
 int launch_exact_icd(const ExactArgs& a, void* stream);
 int launch_exact_project(const ExactArgs& a, double* yest, void* stream);
 int launch_exact_view_sums(const ExactArgs& a, int kind, const double* y, const double* mu,
@@ -123,14 +184,22 @@ int launch_exact_view_sums(const ExactArgs& a, int kind, const double* y, const 
 // launchers (mbir_kernels.cu); fp64 selects Real = double for the void* arrays
 int launch_sweep(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_ref_order(const RefOrderArgs& a, int nb, void* stream);
-size_t sweep_smem_bytes(int n_theta, int n_x, int n_rs, int t_rows, int bins, int fp64);
+size_t sweep_smem_bytes(int n_theta, int n_x, int n_rs, int t_rows, int bins, int fp64,
+                        int n_sp);
 int launch_sweep_f32_smem(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
+int launch_sweep_f32_smem_haadf(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
+int launch_sweep_f32_smem_bf(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_sweep_f32_hbm(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_sweep_f64(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_ref_order_f32(const RefOrderArgs& a, int nb, void* stream);
-// persistent batched sweep (FP32, slices staged or in HBM per series); vpl from max n_theta
-int launch_batch_sweep(const BatchArgs& b, int nb, int vpl, size_t smem_bytes, int grid,
+// persistent batched sweep (FP32, slices staged or in HBM per series); shape = lane_shape of
+// the largest n_theta in the batch
+int launch_batch_sweep(const BatchArgs& b, int nb, int shape, size_t smem_bytes, int grid,
                        void* stream);
+int launch_batch_sweep_nb3(const BatchArgs& b, int shape, size_t smem_bytes, int grid,
+                           void* stream);
+int launch_batch_sweep_nb5(const BatchArgs& b, int shape, size_t smem_bytes, int grid,
+                           void* stream);
 int launch_ref_order_f64(const RefOrderArgs& a, int nb, void* stream);
 int launch_sino_to_dev(const float* host_layout, void* dev_layout, int n_theta, int n_r, int n_rp,
                        int n_t, int fp64, void* stream);

@@ -338,6 +338,18 @@ inline int grid_for(size_t n, int block) {
 
 }  // namespace
 
+int launch_sweep_f32_smem(const SweepArgs& a, int nb, size_t smem, void* stream) {
+  return a.bf ? launch_sweep_f32_smem_bf(a, nb, smem, stream)
+              : launch_sweep_f32_smem_haadf(a, nb, smem, stream);
+}
+
+int launch_batch_sweep(const BatchArgs& b, int nb, int shape, size_t smem, int grid,
+                       void* stream) {
+  if (nb == 3) return launch_batch_sweep_nb3(b, shape, smem, grid, stream);
+  if (nb == 5) return launch_batch_sweep_nb5(b, shape, smem, grid, stream);
+  return -7;
+}
+
 int launch_sweep(const SweepArgs& a, int nb, size_t smem, void* stream) {
   if (a.fp64) return launch_sweep_f64(a, nb, smem, stream);
   return a.smem_rows ? launch_sweep_f32_smem(a, nb, smem, stream)

@@ -133,9 +133,12 @@ __device__ __forceinline__ T group_max(T v) {
 template <int G>
 __device__ __forceinline__ bool group_any(bool p, int lane) {
   const unsigned b = __ballot_sync(kFull, p);
-  if (G == 32) return b != 0u;
-  const unsigned m = ((1u << G) - 1u) << (lane & ~(G - 1));
-  return (b & m) != 0u;
+  if constexpr (G == 32) {
+    return b != 0u;
+  } else {
+    const unsigned m = ((1u << G) - 1u) << (lane & ~(G - 1));
+    return (b & m) != 0u;
+  }
 }
 
 // Detector coordinate of a voxel row at one view.  FP32: integer + fraction so that the
@@ -249,14 +252,45 @@ struct SliceCtx {
   Real* cache;               // [9][n_x] neighbour rows (dy,dz) or nullptr (read global)
   int tcount;
   int mode, iter_nonzero, zero_skipping;
+  // bright field: per-entry weights (HBM), Bragg selector (shared memory or HBM)
+  const Real* bw;
+  int bw_rs, bw_ps;
+  uint8_t* bs;
+  int bs_rs, bs_ps;
+  Real bt, bdt;              // T, delta*T
+  unsigned long long* mag_fx;
+};
+
+// Zero skipping (UpdateVoxels.cpp:310-338, BFUpdateYSlice.cpp:238-262): after the first sweep a
+// voxel that is 0 with no neighbour > 0 is not updated.  One thread, from the neighbour cache
+// (rows outside the volume are cached as 0).
+template <typename Real>
+__device__ __forceinline__ bool zero_skipped(const SliceCtx<Real>& c, int x, Real V) {
+  if (!(c.zero_skipping && c.iter_nonzero && V == Real(0))) return false;
+  const int n_x = c.g->n_x;
+#pragma unroll
+  for (int r = 0; r < 9; ++r) {
+    const Real* row = c.cache + r * n_x;
+    if (row[x] > Real(0)) return false;
+    if (x > 0 && row[x - 1] > Real(0)) return false;
+    if (x + 1 < n_x && row[x + 1] > Real(0)) return false;
+  }
+  return true;
+}
+
+// Per-group accumulators: [0] ROI sum |dx|, [1] ROI sum |x| (fixed point, kFixScale),
+// [2] zero-skipped, [3] updated.
+struct GroupAcc {
+  unsigned long long v[kStatSlots];
 };
 
 // One voxel (z, x, y) updated by one group of G lanes (G = 16: two voxels per warp).  All 32
-// lanes of the warp call this together; `active` is false for a group with no voxel.
-// wst (group lane 0): ROI sum|dx|, ROI sum|x|, zero-skipped, updated.
-template <typename Real, int NB, int G, int VPL>
+// lanes of the warp call this together; `active` is false for a group with no voxel.  With
+// INLINE_ZS the zero-skipping test runs here (reference order); otherwise the caller has
+// already removed skipped voxels.
+template <typename Real, int NB, int G, int VPL, bool BF, bool INLINE_ZS>
 __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x_req, int y,
-                                           bool active, int lane, double* wst) {
+                                           bool active, int lane, GroupAcc& acc) {
   using R2 = typename V2<Real>::type;
   const DevGeom& g = *c.g;
   const int gl = lane & (G - 1);
@@ -264,16 +298,15 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
   const size_t plane = static_cast<size_t>(g.n_z) * g.n_x;
   const size_t vidx = static_cast<size_t>(y) * plane + static_cast<size_t>(z) * g.n_x + x;
   const Real V = c.cache ? c.cache[4 * g.n_x + x] : c.vol[vidx];
-  const bool line_ok = active && c.lineok[static_cast<size_t>(z) * g.n_x + x] != 0;
-  bool live = line_ok;
+  bool live = active && c.lineok[static_cast<size_t>(z) * g.n_x + x] != 0;
 
   // 26-neighbourhood, entries k = gl, gl+G, ... (UpdateVoxels.cpp:283-306); centre and
   // out-of-range entries are 0 in the bracket, as in the reference
   constexpr int NNB = (27 + G - 1) / G;
   Real nb[NNB];
   bool nvalid[NNB];
-  bool pos = false;
   if (c.mode != kModeProject) {
+    bool pos = false;
 #pragma unroll
     for (int i = 0; i < NNB; ++i) {
       const int k = gl + G * i;
@@ -291,12 +324,13 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
         }
       }
     }
-    // zero skipping (UpdateVoxels.cpp:310-338).  The ballot runs on all 32 lanes: the two
-    // voxel groups of a warp may disagree on whether their voxel is zero.
-    const bool any_pos = group_any<G>(pos, lane);
-    if (c.zero_skipping && c.iter_nonzero && V == Real(0) && !any_pos) {
-      if (live && gl == 0) wst[2] += 1.0;
-      live = false;
+    if constexpr (INLINE_ZS) {
+      // the ballot runs on all 32 lanes: the two voxel groups of a warp may disagree
+      const bool any_pos = group_any<G>(pos, lane);
+      if (c.zero_skipping && c.iter_nonzero && V == Real(0) && !any_pos) {
+        if (live && gl == 0) acc.v[2] += 1;
+        live = false;
+      }
     }
   } else {
     live = live && V != Real(0);
@@ -341,7 +375,9 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
     return;
   }
 
-  // theta1 / theta2 (UpdateVoxels.cpp:343-369)
+  // theta1 / theta2 (UpdateVoxels.cpp:343-369; BF: BFForwardModel::computeTheta,
+  // BFForwardModel.cpp:851-892, entries the Bragg selector rejects weighted by
+  // delta T / (|e| sqrt(w)))
   Real t1 = Real(0), t2 = Real(0);
 #pragma unroll
   for (int i = 0; i < VPL; ++i) {
@@ -351,12 +387,33 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
     for (int tr = 0; tr < c.tcount; ++tr) {
       const Real hh = c.hv[tr];
       const Real* row = c.es + tr * c.ps + v * c.rs + jlo[i];
+      if constexpr (BF) {
+        const Real* wr = c.bw + tr * c.bw_ps + v * c.bw_rs + jlo[i];
+        const uint8_t* sr = c.bs + tr * c.bs_ps + v * c.bs_rs + jlo[i];
 #pragma unroll
-      for (int b = 0; b < NB; ++b) {
-        if (a[i][b] > Real(0)) {
-          const Real pe = gw.x * a[i][b] * hh;
-          t2 += pe * pe * gw.y;
-          t1 += row[b] * pe * gw.y;
+        for (int b = 0; b < NB; ++b) {
+          if (a[i][b] > Real(0)) {
+            const Real ev = row[b];
+            const Real w = __ldg(wr + b);
+            const Real pe = gw.x * a[i][b] * hh;
+            if (sr[b]) {
+              t2 += pe * pe * w;
+              t1 += ev * pe * w;
+            } else {
+              const Real qc = c.bdt / (fabs(ev) * sqrt(w));
+              t2 += qc * (pe * pe * w);
+              t1 += qc * (ev * pe * w);
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+          if (a[i][b] > Real(0)) {
+            const Real pe = gw.x * a[i][b] * hh;
+            t2 += pe * pe * gw.y;
+            t1 += row[b] * pe * gw.y;
+          }
         }
       }
     }
@@ -392,10 +449,11 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
   const Real u = (s1 + theta2 * V - theta1) / (s2 + theta2);
   Real nv = V + static_cast<Real>(c.q->mrf_alpha) * (u - V);
   nv = (nv < lo) ? lo : ((nv > hi) ? hi : nv);
-  if (nv < Real(0)) nv = Real(0);  // positivity (UpdateVoxels.cpp:394-400)
+  if (nv < Real(0)) nv = Real(0);  // positivity (UpdateVoxels.cpp:394-400, BFConstants.h)
   const Real dlt = nv - V;
   if (!live) return;
-  // error-sinogram scatter (UpdateVoxels.cpp:423-449)
+  // error-sinogram scatter (UpdateVoxels.cpp:423-449; BF also re-evaluates the selector,
+  // BFForwardModel.cpp:898-932)
   if (dlt != Real(0)) {
 #pragma unroll
     for (int i = 0; i < VPL; ++i) {
@@ -405,9 +463,21 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
       for (int tr = 0; tr < c.tcount; ++tr) {
         const Real hh = c.hv[tr];
         Real* row = c.es + tr * c.ps + v * c.rs + jlo[i];
+        if constexpr (BF) {
+          const Real* wr = c.bw + tr * c.bw_ps + v * c.bw_rs + jlo[i];
+          uint8_t* sr = c.bs + tr * c.bs_ps + v * c.bs_rs + jlo[i];
 #pragma unroll
-        for (int b = 0; b < NB; ++b)
-          if (a[i][b] > Real(0)) row[b] -= gain * (a[i][b] * hh * dlt);
+          for (int b = 0; b < NB; ++b)
+            if (a[i][b] > Real(0)) {
+              const Real ne = row[b] - gain * (a[i][b] * hh * dlt);
+              row[b] = ne;
+              sr[b] = fabs(ne * sqrt(__ldg(wr + b))) < c.bt ? 1 : 0;
+            }
+        } else {
+#pragma unroll
+          for (int b = 0; b < NB; ++b)
+            if (a[i][b] > Real(0)) row[b] -= gain * (a[i][b] * hh * dlt);
+        }
       }
     }
   }
@@ -415,27 +485,38 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
     c.vol[vidx] = nv;
     if (c.cache) c.cache[4 * g.n_x + x] = nv;
     if (x >= g.roi_x0 && x <= g.roi_x1 && z >= g.roi_z0 && z <= g.roi_z1) {
-      wst[0] += fabs(static_cast<double>(dlt));
-      wst[1] += fabs(static_cast<double>(V));
+      acc.v[0] += __double2ull_rn(fabs(static_cast<double>(dlt)) * kFixScale);
+      acc.v[1] += __double2ull_rn(fabs(static_cast<double>(V)) * kFixScale);
     }
-    wst[3] += 1.0;
+    acc.v[3] += 1;
+    if constexpr (BF) {
+      if (c.mag_fx != nullptr && dlt != Real(0))
+        atomicAdd(c.mag_fx + static_cast<size_t>(z) * g.n_x + x,
+                  __double2ull_rn(fabs(static_cast<double>(dlt)) * kFixScale));
+    }
   }
 }
 
 struct SmemLayout {
-  size_t bar, stats, rb, bx, bxd, gw, H, hv, cache, es, total;
+  size_t bar, ctl, stats, rb, bx, bxd, gw, H, hv, list, cache, es, sel, total;
 };
 
 __host__ __device__ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+constexpr int kMaxGroups = kWarps * 32 / 16;  // voxel groups per CTA at G = 16
+
+// n_sp > 0: the slice's selector rows are staged too (bright field)
 __host__ __device__ inline SmemLayout smem_layout(int n_theta, int n_x, int n_rs, int t_rows,
-                                                  int bins, bool stage, size_t real_bytes) {
+                                                  int bins, bool stage, size_t real_bytes,
+                                                  int n_sp) {
   SmemLayout L;
   size_t o = 0;
   L.bar = o;
   o += 16;
+  L.ctl = o;  // class counters [2], zero-skip counter
+  o += 16;
   L.stats = o;
-  o += sizeof(double) * kWarps * 2 * kStatSlots;
+  o += sizeof(unsigned long long) * kMaxGroups * kStatSlots;
   L.rb = o;
   o = align_up(o + 8 * static_cast<size_t>(n_theta), 16);
   L.bx = o;
@@ -448,21 +529,32 @@ __host__ __device__ inline SmemLayout smem_layout(int n_theta, int n_x, int n_rs
   o = align_up(o + real_bytes * n_theta * (bins + 1), 16);
   L.hv = o;
   o = align_up(o + real_bytes * kMaxTRows, 16);
+  L.list = o;
+  o = align_up(o + sizeof(int) * static_cast<size_t>(n_x), 16);
   L.cache = o;
   o = align_up(o + real_bytes * 9 * static_cast<size_t>(n_x), 128);
   L.es = o;
   if (stage) o += real_bytes * static_cast<size_t>(t_rows) * n_theta * n_rs;
+  o = align_up(o, 16);
+  L.sel = o;
+  if (stage && n_sp > 0) o += static_cast<size_t>(t_rows) * n_theta * n_sp;
   L.total = align_up(o, 16);
   return L;
 }
 
 // One voxel slice y of one reconstruction, processed by the whole CTA: stage the slice's
-// detector rows, walk the z-rows, update every conflict-free class, store the rows back.
+// detector rows (and, for bright field, its selector rows), walk the z-rows, update every
+// conflict-free class, store the rows back.  Each class is first compacted: its candidate
+// voxels that are updated (non-empty A-column, in the call's line list, not zero-skipped) are
+// appended to a shared list, and the CTA's voxel groups then take the list in turns, so
+// skipped voxels cost one thread's neighbour test instead of a group iteration.  Voxels of a
+// class are independent (no shared detector bin, no prior neighbours), so the order in which
+// the list is filled does not change any result.
 // `phase` is the parity of the CTA's mbarrier (it alternates when a CTA processes several
 // slices); `coherent` makes neighbour-row loads bypass L1 (needed when other CTAs of the same
 // launch write neighbouring slices).  Writes the slice's four statistics to stat_out when it
 // is not null.  Returns false when a bounded wait gave up (A.err is set).
-template <typename Real, int NB, int G, int VPL, bool STAGE>
+template <typename Real, int NB, int G, int VPL, bool STAGE, bool BF>
 __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned char* smem,
                                           uint32_t& phase, bool coherent, double* stat_out) {
   using R2 = typename V2<Real>::type;
@@ -473,15 +565,19 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
   const int group = warp * GPW + (lane / G);
   const int n_groups = (nthreads / 32) * GPW;
   const int tcount = A.tab.t_count[y], tfirst = A.tab.t_first[y];
-  const SmemLayout L = smem_layout(g.n_theta, g.n_x, A.n_rs, tcount, g.bins, STAGE, sizeof(Real));
+  const int n_sp = BF ? A.bfa.n_sp : 0;
+  const SmemLayout L =
+      smem_layout(g.n_theta, g.n_x, A.n_rs, tcount, g.bins, STAGE, sizeof(Real), n_sp);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L.bar);
-  double* sstat = reinterpret_cast<double*>(smem + L.stats);
+  unsigned* ctl = reinterpret_cast<unsigned*>(smem + L.ctl);
+  unsigned long long* sstat = reinterpret_cast<unsigned long long*>(smem + L.stats);
   RowBase<Real>* rb = reinterpret_cast<RowBase<Real>*>(smem + L.rb);
   float2* sbx = reinterpret_cast<float2*>(smem + L.bx);
   double* sbxd = reinterpret_cast<double*>(smem + L.bxd);
   R2* sgw = reinterpret_cast<R2*>(smem + L.gw);
   Real* sH = reinterpret_cast<Real*>(smem + L.H);
   Real* shv = reinterpret_cast<Real*>(smem + L.hv);
+  int* list = reinterpret_cast<int*>(smem + L.list);
   Real* cache = reinterpret_cast<Real*>(smem + L.cache);
   const Real* gH = static_cast<const Real*>(A.tab.H);
   const R2* ggw = static_cast<const R2*>(A.tab.gw);
@@ -499,21 +595,30 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
     sgw[v] = ggw[v];
   }
   if (tid < kMaxTRows) shv[tid] = ghv[y * kMaxTRows + tid];
+  if (tid < 4) ctl[tid] = 0u;
 
   const size_t sino_plane = static_cast<size_t>(g.n_theta) * g.n_rp;
+  const size_t sel_plane = static_cast<size_t>(g.n_theta) * n_sp;
   Real* es;
-  int rs, ps;
+  uint8_t* ssel = nullptr;
+  int rs, ps, srs = 0, sps = 0;
   const int rows = tcount * g.n_theta;
   const uint32_t row_bytes = static_cast<uint32_t>(g.n_rp * sizeof(Real));
   if (STAGE) {
     es = reinterpret_cast<Real*>(smem + L.es);
     rs = A.n_rs;
     ps = g.n_theta * A.n_rs;
+    if (BF) {
+      ssel = smem + L.sel;
+      srs = n_sp;
+      sps = g.n_theta * n_sp;
+    }
     if (A.mode == kModeProject) {
       for (int i = tid; i < tcount * ps; i += nthreads) es[i] = Real(0);
       __syncthreads();
     } else {
-      if (tid == 0) mbar_expect_tx(bar, static_cast<uint32_t>(rows) * row_bytes);
+      const uint32_t total = static_cast<uint32_t>(rows) * (row_bytes + (BF ? n_sp : 0));
+      if (tid == 0) mbar_expect_tx(bar, total);
       __syncthreads();
       for (int r = tid; r < rows; r += nthreads) {
         const int tr = r / g.n_theta, v = r % g.n_theta;
@@ -521,6 +626,11 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
                  ge + (static_cast<size_t>(tfirst + tr)) * sino_plane +
                      static_cast<size_t>(v) * g.n_rp,
                  row_bytes, bar);
+        if (BF)
+          bulk_g2s(ssel + tr * sps + v * srs,
+                   A.bfa.sel + (static_cast<size_t>(tfirst + tr)) * sel_plane +
+                       static_cast<size_t>(v) * n_sp,
+                   static_cast<uint32_t>(n_sp), bar);
       }
       const bool ok = mbar_wait(bar, phase);
       phase ^= 1u;
@@ -534,6 +644,11 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
     es = ge + static_cast<size_t>(tfirst) * sino_plane;
     rs = g.n_rp;
     ps = static_cast<int>(sino_plane);
+    if (BF) {
+      ssel = A.bfa.sel + static_cast<size_t>(tfirst) * sel_plane;
+      srs = n_sp;
+      sps = static_cast<int>(sel_plane);
+    }
   }
 
   SliceCtx<Real> c;
@@ -555,9 +670,30 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
   c.mode = A.mode;
   c.iter_nonzero = A.iter_nonzero;
   c.zero_skipping = A.zero_skipping;
+  c.bw = nullptr;
+  c.bs = nullptr;
+  c.mag_fx = nullptr;
+  c.bw_rs = c.bw_ps = c.bs_rs = c.bs_ps = 0;
+  c.bt = c.bdt = Real(0);
+  if (BF) {
+    c.bw = static_cast<const Real*>(A.bfa.w) + static_cast<size_t>(tfirst) * sino_plane;
+    c.bw_rs = g.n_rp;
+    c.bw_ps = static_cast<int>(sino_plane);
+    c.bs = ssel;
+    c.bs_rs = srs;
+    c.bs_ps = sps;
+    c.bt = static_cast<Real>(A.bfa.bragg_t);
+    c.bdt = static_cast<Real>(A.bfa.bragg_dt);
+    c.mag_fx = A.bfa.mag_fx;
+  }
+  const uint8_t* active_lines = BF ? A.bfa.active : nullptr;
 
   const size_t vplane = static_cast<size_t>(g.n_z) * g.n_x;
-  double wst[kStatSlots] = {0.0, 0.0, 0.0, 0.0};
+  GroupAcc acc;
+#pragma unroll
+  for (int s = 0; s < kStatSlots; ++s) acc.v[s] = 0ull;
+  unsigned skipped = 0;
+  unsigned step = 0;  // class steps so far: selects the double-buffered list counter
   for (int rr = 0; rr < g.n_z; ++rr) {
     const int z = A.row_order[rr];
     __syncthreads();
@@ -574,12 +710,31 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
       cache[i] = v;
     }
     __syncthreads();
-    for (int k = 0; k < A.stride; ++k) {
-      for (int m = group;; m += n_groups) {
-        const int x = k + A.stride * m;
-        const bool active = x < g.n_x;
-        if (!__any_sync(kFull, active)) break;
-        group_step<Real, NB, G, VPL>(c, z, x, y, active, lane, wst);
+    const uint8_t* okrow = A.tab.lineok + static_cast<size_t>(z) * g.n_x;
+    const uint8_t* actrow = active_lines ? active_lines + static_cast<size_t>(z) * g.n_x : nullptr;
+    for (int k = 0; k < A.stride; ++k, ++step) {
+      // compact the class: x = k, k+S, ... that will be updated.  The counter of this step
+      // was cleared during the previous step; the other one (read as the previous step's list
+      // length before the previous barrier) is cleared now for the next step.
+      unsigned* cnt = ctl + (step & 1u);
+      if (tid == 0) ctl[(step + 1u) & 1u] = 0u;
+      for (int x = k + A.stride * tid; x < g.n_x; x += A.stride * nthreads) {
+        if (!okrow[x] || (actrow && !actrow[x])) continue;
+        const Real V = cache[4 * g.n_x + x];
+        if (A.mode == kModeProject) {
+          if (V == Real(0)) continue;
+        } else if (zero_skipped(c, x, V)) {
+          ++skipped;
+          continue;
+        }
+        list[atomicAdd(cnt, 1u)] = x;
+      }
+      __syncthreads();
+      const int n = static_cast<int>(*cnt);
+      for (int base = 0; base < n; base += n_groups) {
+        const int i = base + group;
+        const bool act = i < n;
+        group_step<Real, NB, G, VPL, BF, false>(c, z, act ? list[i] : 0, y, act, lane, acc);
       }
       __syncthreads();
     }
@@ -593,6 +748,10 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
       bulk_s2g(ge + (static_cast<size_t>(tfirst + tr)) * sino_plane +
                    static_cast<size_t>(v) * g.n_rp,
                es + tr * ps + v * rs, row_bytes);
+      if (BF && A.mode != kModeProject)
+        bulk_s2g(A.bfa.sel + (static_cast<size_t>(tfirst + tr)) * sel_plane +
+                     static_cast<size_t>(v) * n_sp,
+                 ssel + tr * sps + v * srs, static_cast<uint32_t>(n_sp));
     }
     bulk_commit();
     bulk_wait_all();
@@ -600,12 +759,14 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
   if (stat_out != nullptr) {
     const int gl = lane & (G - 1);
     if (gl == 0)
-      for (int s = 0; s < kStatSlots; ++s) sstat[group * kStatSlots + s] = wst[s];
+      for (int s = 0; s < kStatSlots; ++s) sstat[group * kStatSlots + s] = acc.v[s];
+    if (skipped) atomicAdd(ctl + 2, skipped);
     __syncthreads();
     if (tid < kStatSlots) {
-      double acc = 0.0;
-      for (int w = 0; w < n_groups; ++w) acc += sstat[w * kStatSlots + tid];
-      stat_out[tid] = acc;
+      unsigned long long t = 0;
+      for (int w = 0; w < n_groups; ++w) t += sstat[w * kStatSlots + tid];
+      if (tid == 2) t += ctl[2];
+      stat_out[tid] = tid < 2 ? static_cast<double>(t) / kFixScale : static_cast<double>(t);
     }
   }
   __syncthreads();
@@ -621,14 +782,14 @@ __device__ __forceinline__ void init_slice_barrier(unsigned char* smem) {
 }
 
 // One launch = the slices of one y-colour of one reconstruction, one CTA per slice.
-template <typename Real, int NB, int G, int VPL, bool STAGE>
+template <typename Real, int NB, int G, int VPL, bool STAGE, bool BF>
 __global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int y = A.colour + 2 * static_cast<int>(blockIdx.x);
   if (y >= A.g.n_y) return;
   init_slice_barrier(smem);
   uint32_t phase = 0;
-  run_slice<Real, NB, G, VPL, STAGE>(
+  run_slice<Real, NB, G, VPL, STAGE, BF>(
       A, y, smem, phase, false,
       A.stats != nullptr ? A.stats + static_cast<size_t>(blockIdx.x) * kStatSlots : nullptr);
 }
@@ -680,10 +841,17 @@ __global__ void __launch_bounds__(kWarps * 32, 1) batch_sweep_kernel(BatchArgs B
     const int n0 = (sA.g.n_y + 1) / 2;
     const int slot = (y & 1) ? n0 + (y >> 1) : (y >> 1);
     double* stat_out = sA.stats + static_cast<size_t>(slot) * kStatSlots;
-    if (sA.smem_rows)
-      run_slice<float, NB, G, VPL, true>(sA, y, smem, phase, true, stat_out);
-    else
-      run_slice<float, NB, G, VPL, false>(sA, y, smem, phase, true, stat_out);
+    if (sA.bf) {
+      if (sA.smem_rows)
+        run_slice<float, NB, G, VPL, true, true>(sA, y, smem, phase, true, stat_out);
+      else
+        run_slice<float, NB, G, VPL, false, true>(sA, y, smem, phase, true, stat_out);
+    } else {
+      if (sA.smem_rows)
+        run_slice<float, NB, G, VPL, true, false>(sA, y, smem, phase, true, stat_out);
+      else
+        run_slice<float, NB, G, VPL, false, false>(sA, y, smem, phase, true, stat_out);
+    }
     if (threadIdx.x == 0 && !(y & 1)) {
       __threadfence();
       atomicAdd(B.done + s, 1);
@@ -691,13 +859,16 @@ __global__ void __launch_bounds__(kWarps * 32, 1) batch_sweep_kernel(BatchArgs B
   }
 }
 
-template <typename Real, int NB, int VPL>
+// The reference's visit order: voxel lines one after another in list order, y ascending
+// (UpdateYSlice::execute / BFUpdateYSlice::execute with one task), one warp, error sinogram in
+// HBM.  BF: the lines' update magnitudes restart at 0 (BFUpdateYSlice.cpp:171).
+template <typename Real, int NB, int VPL, bool BF>
 __global__ void __launch_bounds__(32, 1) ref_order_kernel(RefOrderArgs A) {
   using R2 = typename V2<Real>::type;
   extern __shared__ __align__(128) unsigned char smem[];
   const DevGeom& g = A.g;
   const int lane = threadIdx.x;
-  const SmemLayout L = smem_layout(g.n_theta, 0, 0, 0, g.bins, false, sizeof(Real));
+  const SmemLayout L = smem_layout(g.n_theta, 0, 0, 0, g.bins, false, sizeof(Real), 0);
   RowBase<Real>* rb = reinterpret_cast<RowBase<Real>*>(smem + L.rb);
   float2* sbx = reinterpret_cast<float2*>(smem + L.bx);
   double* sbxd = reinterpret_cast<double*>(smem + L.bxd);
@@ -732,12 +903,30 @@ __global__ void __launch_bounds__(32, 1) ref_order_kernel(RefOrderArgs A) {
   c.mode = kModeICD;
   c.iter_nonzero = A.iter_nonzero;
   c.zero_skipping = A.zero_skipping;
+  c.bw = nullptr;
+  c.bs = nullptr;
+  c.mag_fx = nullptr;
+  c.bw_rs = c.bw_ps = c.bs_rs = c.bs_ps = 0;
+  c.bt = c.bdt = Real(0);
   Real* const ge = static_cast<Real*>(A.e);
   const size_t sino_plane = static_cast<size_t>(g.n_theta) * g.n_rp;
-  double wst[kStatSlots] = {0.0, 0.0, 0.0, 0.0};
+  const size_t sel_plane = BF ? static_cast<size_t>(g.n_theta) * A.bfa.n_sp : 0;
+  if (BF) {
+    c.bw_rs = g.n_rp;
+    c.bw_ps = static_cast<int>(sino_plane);
+    c.bs_rs = A.bfa.n_sp;
+    c.bs_ps = static_cast<int>(sel_plane);
+    c.bt = static_cast<Real>(A.bfa.bragg_t);
+    c.bdt = static_cast<Real>(A.bfa.bragg_dt);
+    c.mag_fx = A.bfa.mag_fx;
+  }
+  GroupAcc acc;
+#pragma unroll
+  for (int s = 0; s < kStatSlots; ++s) acc.v[s] = 0ull;
   for (int n = 0; n < A.n_lines; ++n) {
     const int l = A.lines[n];
     const int z = l / g.n_x, x = l % g.n_x;
+    if (BF && c.mag_fx != nullptr && lane == 0) c.mag_fx[l] = 0ull;
     __syncwarp();
     compute_row_base<Real>(A.tab, g.n_theta, z, rb, lane, 32);
     __syncwarp();
@@ -745,24 +934,34 @@ __global__ void __launch_bounds__(32, 1) ref_order_kernel(RefOrderArgs A) {
       c.es = ge + static_cast<size_t>(A.tab.t_first[y]) * sino_plane;
       c.tcount = A.tab.t_count[y];
       c.hv = ghv + y * kMaxTRows;
-      group_step<Real, NB, 32, VPL>(c, z, x, y, true, lane, wst);
+      if (BF) {
+        c.bw = static_cast<const Real*>(A.bfa.w) + static_cast<size_t>(A.tab.t_first[y]) * sino_plane;
+        c.bs = A.bfa.sel + static_cast<size_t>(A.tab.t_first[y]) * sel_plane;
+      }
+      group_step<Real, NB, 32, VPL, BF, true>(c, z, x, y, true, lane, acc);
       __syncwarp();
     }
   }
   if (lane == 0)
-    for (int s = 0; s < kStatSlots; ++s) A.stats[s] = wst[s];
+    for (int s = 0; s < kStatSlots; ++s)
+      A.stats[s] = s < 2 ? static_cast<double>(acc.v[s]) / kFixScale : static_cast<double>(acc.v[s]);
 }
 
 inline int ok_or(cudaError_t e) { return e == cudaSuccess ? 0 : -3; }
 
-template <typename Real, int NB, int G, int VPL, bool STAGE>
+template <typename Real, int NB, int G, int VPL, bool STAGE, bool BF>
 int launch_sweep_t(const SweepArgs& a, size_t smem, cudaStream_t s) {
-  auto k = sweep_kernel<Real, NB, G, VPL, STAGE>;
+  auto k = sweep_kernel<Real, NB, G, VPL, STAGE, BF>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem));
   if (e != cudaSuccess) return -3;
   k<<<a.n_slices, kWarps * 32, smem, s>>>(a);
   return ok_or(cudaGetLastError());
+}
+template <typename Real, int NB, int G, int VPL, bool STAGE>
+int launch_sweep_m(const SweepArgs& a, size_t smem, cudaStream_t s) {
+  return a.bf ? launch_sweep_t<Real, NB, G, VPL, STAGE, true>(a, smem, s)
+              : launch_sweep_t<Real, NB, G, VPL, STAGE, false>(a, smem, s);
 }
 
 template <int NB, int G, int VPL>
@@ -788,13 +987,42 @@ int launch_batch_t(const BatchArgs& b, size_t smem, int grid, cudaStream_t s) {
 
 template <typename Real, int NB, int VPL>
 int launch_ref_t(const RefOrderArgs& a, cudaStream_t s) {
-  const size_t smem = smem_layout(a.g.n_theta, 0, 0, 0, a.g.bins, false, sizeof(Real)).total;
-  auto k = ref_order_kernel<Real, NB, VPL>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(smem));
-  if (e != cudaSuccess) return -3;
-  k<<<1, 32, smem, s>>>(a);
-  return ok_or(cudaGetLastError());
+  const size_t smem = smem_layout(a.g.n_theta, 0, 0, 0, a.g.bins, false, sizeof(Real), 0).total;
+  auto launch = [&](auto kern) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return -3;
+    kern<<<1, 32, smem, s>>>(a);
+    return ok_or(cudaGetLastError());
+  };
+  return a.bf ? launch(ref_order_kernel<Real, NB, VPL, true>)
+              : launch(ref_order_kernel<Real, NB, VPL, false>);
+}
+
+// FP32 sweep launch for one (STAGE, BF) pair: NB (footprint bins) and the lane shape select
+// the instantiation.
+template <bool STAGE, bool BF>
+int launch_sweep_f32_pick(const SweepArgs& a, int nb, size_t smem, cudaStream_t s) {
+  const int shape = lane_shape(a.g.n_theta);
+  if (nb == 9) return launch_sweep_t<float, 9, 32, 5, STAGE, BF>(a, smem, s);
+  if (nb == 3) {
+    if (shape == 0) return launch_sweep_t<float, 3, 16, 4, STAGE, BF>(a, smem, s);
+    if (shape == 1) return launch_sweep_t<float, 3, 32, 3, STAGE, BF>(a, smem, s);
+    return launch_sweep_t<float, 3, 32, 5, STAGE, BF>(a, smem, s);
+  }
+  if (nb == 5) {
+    if (shape == 0) return launch_sweep_t<float, 5, 16, 4, STAGE, BF>(a, smem, s);
+    if (shape == 1) return launch_sweep_t<float, 5, 32, 3, STAGE, BF>(a, smem, s);
+    return launch_sweep_t<float, 5, 32, 5, STAGE, BF>(a, smem, s);
+  }
+  return -7;
+}
+
+template <int NB>
+int launch_batch_pick(const BatchArgs& b, int shape, size_t smem, int grid, cudaStream_t s) {
+  if (shape == 0) return launch_batch_t<NB, 16, 4>(b, smem, grid, s);
+  if (shape == 1) return launch_batch_t<NB, 32, 3>(b, smem, grid, s);
+  return launch_batch_t<NB, 32, 5>(b, smem, grid, s);
 }
 
 }  // namespace sweep

@@ -1,0 +1,10 @@
+// mbir_sweep_f32_batch3.cu -- persistent batched sweep kernels, three-bin footprints.
+#include "mbir_sweep.cuh"
+
+namespace mbir {
+
+int launch_batch_sweep_nb3(const BatchArgs& b, int shape, size_t smem, int grid, void* stream) {
+  return sweep::launch_batch_pick<3>(b, shape, smem, grid, static_cast<cudaStream_t>(stream));
+}
+
+}  // namespace mbir

@@ -1,20 +1,22 @@
 // mbir_sweep_f32_hbm.cu -- FP32 ICD sweep kernels for voxel slices too large for shared
-// memory: the slice's detector rows are used in place in HBM.
+// memory (the slice's detector rows are used in place in HBM), and the FP32 reference-order
+// kernel.
 #include "mbir_sweep.cuh"
 
 namespace mbir {
 
 int launch_sweep_f32_hbm(const SweepArgs& a, int nb, size_t smem, void* stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return a.bf ? sweep::launch_sweep_f32_pick<false, true>(a, nb, smem, s)
+              : sweep::launch_sweep_f32_pick<false, false>(a, nb, smem, s);
+}
+
+int launch_ref_order_f32(const RefOrderArgs& a, int nb, void* stream) {
   using namespace sweep;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int vpl = a.g.n_theta <= 64 ? 4 : (a.g.n_theta <= 128 ? 8 : 10);
-  if (nb == 3 && vpl == 4) return launch_sweep_t<float, 3, 16, 4, false>(a, smem, s);
-  if (nb == 3 && vpl == 8) return launch_sweep_t<float, 3, 16, 8, false>(a, smem, s);
-  if (nb == 3 && vpl == 10) return launch_sweep_t<float, 3, 16, 10, false>(a, smem, s);
-  if (nb == 5 && vpl == 4) return launch_sweep_t<float, 5, 16, 4, false>(a, smem, s);
-  if (nb == 5 && vpl == 8) return launch_sweep_t<float, 5, 16, 8, false>(a, smem, s);
-  if (nb == 5 && vpl == 10) return launch_sweep_t<float, 5, 16, 10, false>(a, smem, s);
-  if (nb == 9) return launch_sweep_t<float, 9, 32, 5, false>(a, smem, s);
+  if (nb == 3) return launch_ref_t<float, 3, 5>(a, s);
+  if (nb == 5) return launch_ref_t<float, 5, 5>(a, s);
+  if (nb == 9) return launch_ref_t<float, 9, 5>(a, s);
   return -7;
 }
 

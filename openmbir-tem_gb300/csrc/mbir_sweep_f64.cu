@@ -9,14 +9,14 @@ int launch_sweep_f64(const SweepArgs& a, int nb, size_t smem, void* stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const bool st = a.smem_rows != 0;
   if (nb == 3)
-    return st ? launch_sweep_t<double, 3, 32, 5, true>(a, smem, s)
-              : launch_sweep_t<double, 3, 32, 5, false>(a, smem, s);
+    return st ? launch_sweep_m<double, 3, 32, 5, true>(a, smem, s)
+              : launch_sweep_m<double, 3, 32, 5, false>(a, smem, s);
   if (nb == 5)
-    return st ? launch_sweep_t<double, 5, 32, 5, true>(a, smem, s)
-              : launch_sweep_t<double, 5, 32, 5, false>(a, smem, s);
+    return st ? launch_sweep_m<double, 5, 32, 5, true>(a, smem, s)
+              : launch_sweep_m<double, 5, 32, 5, false>(a, smem, s);
   if (nb == 9)
-    return st ? launch_sweep_t<double, 9, 32, 5, true>(a, smem, s)
-              : launch_sweep_t<double, 9, 32, 5, false>(a, smem, s);
+    return st ? launch_sweep_m<double, 9, 32, 5, true>(a, smem, s)
+              : launch_sweep_m<double, 9, 32, 5, false>(a, smem, s);
   return -7;
 }
 
@@ -29,8 +29,9 @@ int launch_ref_order_f64(const RefOrderArgs& a, int nb, void* stream) {
   return -7;
 }
 
-size_t sweep_smem_bytes(int n_theta, int n_x, int n_rs, int t_rows, int bins, int fp64) {
-  return sweep::smem_layout(n_theta, n_x, n_rs, t_rows, bins, n_rs > 0, fp64 ? 8 : 4).total;
+size_t sweep_smem_bytes(int n_theta, int n_x, int n_rs, int t_rows, int bins, int fp64,
+                        int n_sp) {
+  return sweep::smem_layout(n_theta, n_x, n_rs, t_rows, bins, n_rs > 0, fp64 ? 8 : 4, n_sp).total;
 }
 
 }  // namespace mbir

@@ -137,6 +137,9 @@ SIGNATURES = {
     "mbir_get_nuisance": (C.c_int32, [C.c_void_p, _D, _D, _D]),
     "mbir_get_tables": (C.c_int32, [C.c_void_p, _D, _D]),
     "mbir_get_schedule": (C.c_int32, [C.c_void_p, C.c_int32, _I, _I]),
+    "mbir_get_call_lines": (C.c_int32, [C.c_void_p, _I, C.c_int32, _I]),
+    "mbir_get_bf_state": (C.c_int32, [C.c_void_p, C.POINTER(C.c_uint8), _F, _D, _D, _D]),
+    "mbir_set_bragg_threshold": (C.c_int32, [C.c_void_p, C.c_double]),
     "mbir_status_get": (C.c_int32, [C.c_void_p, C.POINTER(MbirStatus)]),
     "mbir_cancel": (None, [C.c_void_p]),
     "mbir_write_outputs": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_char_p]),
@@ -322,6 +325,29 @@ class Engine:
         self._check(lib().mbir_get_schedule(self._h, sweep, rows.ctypes.data_as(_I),
                                             C.byref(stride)))
         return rows, stride.value
+
+    def call_lines(self):
+        n = C.c_int32()
+        self._check(lib().mbir_get_call_lines(self._h, None, 0, C.byref(n)))
+        out = np.zeros(max(n.value, 1), np.int32)
+        self._check(lib().mbir_get_call_lines(self._h, out.ctypes.data_as(_I), n.value, C.byref(n)))
+        return out[:n.value]
+
+    def bf_state(self):
+        """(selector [theta][r][t] uint8, weights float32, mag [z][x], filtered mag, T)"""
+        nz, nx, ny, nt, nr, ntt = self.dims()
+        sel = np.zeros((nt, nr, ntt), np.uint8)
+        w = np.zeros((nt, nr, ntt), np.float32)
+        mag = np.zeros((nz, nx))
+        filt = np.zeros((nz, nx))
+        t = C.c_double()
+        self._check(lib().mbir_get_bf_state(self._h, sel.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                            w.ctypes.data_as(_F), mag.ctypes.data_as(_D),
+                                            filt.ctypes.data_as(_D), C.byref(t)))
+        return sel, w, mag, filt, t.value
+
+    def set_bragg(self, t):
+        self._check(lib().mbir_set_bragg_threshold(self._h, float(t)))
 
     def status(self):
         st = MbirStatus()

@@ -881,9 +881,13 @@ typedef struct {
   orc_ctx* c;
   const int32_t* order;
   int n_lines, y0, y1, outer, inner;
+  int bf;
   double st[4];
   double* mag;
 } orc_task;
+
+static void bf_update_voxel(orc_ctx* c, int jn, int kn, int i, int outer, int inner,
+                            double* stats, double* mag);
 
 static void* orc_task_run(void* arg) {
   orc_task* t = (orc_task*)arg;
@@ -892,7 +896,12 @@ static void* orc_task_run(void* arg) {
     int l = t->order[n];
     if (c->col_count[l] <= 0) continue;
     int jn = l / c->n_x, kn = l % c->n_x;
-    for (int i = t->y0; i < t->y1; i++) update_voxel(c, jn, kn, i, t->outer, t->inner, t->st, t->mag);
+    for (int i = t->y0; i < t->y1; i++) {
+      if (t->bf)
+        bf_update_voxel(c, jn, kn, i, t->outer, t->inner, t->st, t->mag);
+      else
+        update_voxel(c, jn, kn, i, t->outer, t->inner, t->st, t->mag);
+    }
   }
   return NULL;
 }
@@ -1549,4 +1558,50 @@ int orc_bf_run(orc_ctx* c, uint32_t seed, int max_calls) {
   free(list);
   free(order);
   return calls;
+}
+
+/* updateVoxels of the BF engine with OpenMBIR_USE_PARALLEL_ALGORITHMS
+ * (BFReconstructionEngine_Extra.cpp:654-753): contiguous y ranges, one per worker, every worker
+ * walking the call's lines over its range (the reference gives each worker its own random order
+ * of the list; here they share the given order).  Per-worker magnitudes are summed into the
+ * lines of the call.  Used to time the reference's CPU path. */
+void orc_bf_sweep_lines_mt(orc_ctx* c, const int32_t* lines, int n_lines, int outer, int inner,
+                           int n_threads, double* stats) {
+  int nl = c->n_z * c->n_x;
+  if (n_threads < 1) n_threads = 1;
+  int* ycount = (int*)calloc(n_threads, sizeof(int));
+  for (int y = 0, t = 0; y < c->n_y; ++y) {
+    ycount[t]++;
+    if (++t == n_threads) t = 0;
+  }
+  orc_task* tasks = (orc_task*)calloc(n_threads, sizeof(orc_task));
+  pthread_t* th = (pthread_t*)calloc(n_threads, sizeof(pthread_t));
+  int ystart = 0, used = 0;
+  for (int t = 0; t < n_threads; t++) {
+    if (ycount[t] == 0) continue;
+    orc_task* k = &tasks[used];
+    k->c = c;
+    k->order = lines;
+    k->n_lines = n_lines;
+    k->y0 = ystart;
+    k->y1 = ystart + ycount[t];
+    k->outer = outer;
+    k->inner = inner;
+    k->bf = 1;
+    k->mag = (double*)calloc(nl, sizeof(double));
+    ystart = k->y1;
+    used++;
+  }
+  for (int t = 0; t < used; t++) pthread_create(&th[t], NULL, orc_task_run, &tasks[t]);
+  for (int t = 0; t < used; t++) pthread_join(th[t], NULL);
+  stats[0] = stats[1] = stats[2] = stats[3] = 0;
+  for (int n = 0; n < n_lines; n++) c->mag_map[lines[n]] = 0;
+  for (int t = 0; t < used; t++) {
+    for (int s = 0; s < 4; s++) stats[s] += tasks[t].st[s];
+    for (int n = 0; n < n_lines; n++) c->mag_map[lines[n]] += tasks[t].mag[lines[n]];
+    free(tasks[t].mag);
+  }
+  free(tasks);
+  free(th);
+  free(ycount);
 }

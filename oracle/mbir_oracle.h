@@ -148,6 +148,9 @@ double orc_bf_cost(const orc_ctx* c, double* parts);
 /* BFReconstructionEngine::execute loops in reference (list) order with lists drawn from
  * `seed`; runs at most max_calls updateVoxels calls (<= 0: no limit); returns the calls run */
 int orc_bf_run(orc_ctx* c, uint32_t seed, int max_calls);
+/* one call with the reference's worker split over y (timing of the reference CPU path) */
+void orc_bf_sweep_lines_mt(orc_ctx* c, const int32_t* lines, int n_lines, int outer, int inner,
+                           int n_threads, double* stats);
 
 #ifdef __cplusplus
 }

@@ -99,6 +99,8 @@ def lib():
             "orc_bf_update_selector": (None, [C.c_void_p]),
             "orc_bf_cost": (C.c_double, [C.c_void_p, _D]),
             "orc_bf_run": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int]),
+            "orc_bf_sweep_lines_mt": (None, [C.c_void_p, _I, C.c_int, C.c_int, C.c_int, C.c_int,
+                                             _D]),
         }
         for n, (r, a) in sig.items():
             f = getattr(L, n)
@@ -314,6 +316,13 @@ class Oracle:
         st = np.zeros(4)
         lib().orc_bf_sweep_slices(self._h, active.ctypes.data_as(_U8), rows.ctypes.data_as(_I),
                                   stride, outer, inner, st.ctypes.data_as(_D))
+        return st
+
+    def bf_sweep_lines_mt(self, lines, outer=0, inner=0, threads=None):
+        lines = np.ascontiguousarray(lines, np.int32)
+        st = np.zeros(4)
+        lib().orc_bf_sweep_lines_mt(self._h, lines.ctypes.data_as(_I), len(lines), outer, inner,
+                                    threads or os.cpu_count() or 1, st.ctypes.data_as(_D))
         return st
 
     def bf_vsc(self):

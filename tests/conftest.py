@@ -70,3 +70,32 @@ def haadf_params(mbir, thickness, **kw):
     for k, v in kw.items():
         setattr(p, k, v)
     return p
+
+
+def bf_case(n_r=64, n_t=8, max_deg=60.0, step=4.0, seed=2, thickness=16.0, n_particles=6):
+    """A reduced bright-field case: a few ellipsoids seen as Poisson counts (1e4 electrons,
+    +-3% per-view dose drift).  Returns (counts, angles, thickness)."""
+    import synthetic
+    ang = synthetic.tilt_angles(max_deg, step)
+    shapes = synthetic.random_ellipsoids(n_particles, n_r, n_t, 2 * thickness, seed=seed,
+                                         axes=(3.0, 8.0), z_range=(-thickness / 4, thickness))
+    proj = synthetic.ellipsoid_projection(ang, n_r, n_t, shapes)
+    counts, _ = synthetic.bf_counts(proj, seed=seed + 1)
+    return counts, ang.astype(np.float32), thickness
+
+
+def bf_params(mbir, thickness, **kw):
+    p = mbir.default_params(mbir.BF)
+    p.sample_thickness = thickness
+    p.diffuseness = 0.1
+    p.sigma_x = 0.02
+    p.num_resolutions = 1
+    p.outer_iterations = 5
+    p.inner_iterations = 1
+    p.stop_threshold = 0.0
+    p.use_default_offset = 1
+    p.default_dosage = 1.0e4
+    p.bragg_threshold = 3.0
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p

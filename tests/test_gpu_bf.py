@@ -1,0 +1,141 @@
+"""Bright-field parity: the sm_103a engine (C ABI) against the FP64 oracle's restatement of
+BFForwardModel / BFUpdateYSlice / BFReconstructionEngine.
+
+Tolerances (FP32 engine vs FP64 oracle, same state and order):
+  error sinogram / weights after set-up          relative          <= 1e-5
+  one NHICD call (volume, error, magnitudes)     ||d|| / ||ref||   <= 1e-5
+  Bragg selector after a call or an update       entries differing <= 1e-4 of all
+  offset / variance estimates from equal state   relative          <= 1e-6
+  cost terms from equal state                    relative          <= 1e-6 (data), 1e-5 (prior)
+  reference-exact FP64 run (calls + JE + UW)     bitwise (float32 read-out)
+"""
+import numpy as np
+import pytest
+
+from conftest import bf_case, bf_params
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def pair(mbir, oracle_mod, **kw):
+    y, ang, th = bf_case()
+    p = bf_params(mbir, th, **kw)
+    e = mbir.Engine(p)
+    e.set_sinogram(y, ang)
+    o = oracle_mod.Oracle(oracle_mod.params_from_mbir(p), y, ang)
+    return e, o, p, y
+
+
+def sync_oracle(e, o):
+    """Copy the engine's state into the oracle (float32 values, as doubles)."""
+    sel, w, mag, _, t = e.bf_state()
+    o.volume()[...] = e.volume()
+    o.error()[...] = e.error_sinogram()
+    o.selector()[...] = sel
+    o.weight()[...] = w
+    o.mag_map()[...] = mag
+    o.set_bragg(t)
+
+
+def test_bf_setup_matches_oracle(lib_built, oracle_mod):
+    e, o, p, y = pair(lib_built, oracle_mod)
+    e.prepare()
+    o.prepare()
+    g, off, var = e.nuisance()
+    np.testing.assert_allclose(off, o.offset(), rtol=1e-12)  # -log(dosage), host FP64
+    np.testing.assert_allclose(var, o.variance(), rtol=1e-12)
+    sel, w, mag, _, t = e.bf_state()
+    assert t == 3.0 and sel.all() and not mag.any()
+    assert rel(w, o.weight()) <= 1e-6
+    assert rel(e.error_sinogram(), o.error()) <= 1e-5
+
+
+@pytest.mark.parametrize("precision,bragg,tol", [(0, 5.0e10, 1e-5), (1, 3.0, 1e-9)])
+def test_bf_call_matches_oracle_same_order(lib_built, oracle_mod, precision, bragg, tol):
+    """First two NHICD calls (homogeneous, then non-homogeneous) against the oracle's slice-order
+    call over the same lines.  The Bragg selector is a threshold on |e sqrt(w)|: in the first
+    calls almost every touched entry crosses T, so FP32 rounding flips decisions at the
+    threshold and the FP32 engine is compared with the selector off (T = 5e10); the FP64 engine
+    is compared at T = 3 with the selector switching."""
+    e, o, p, y = pair(lib_built, oracle_mod, precision=precision, bragg_threshold=bragg)
+    e.prepare()
+    o.prepare()
+    nz, nx = e.dims()[:2]
+    for k in range(2):
+        rows, stride = e.schedule(k)
+        sg = e.sweep(0, k)
+        lines = e.call_lines()
+        if k == 1:  # the NH list: lines whose filtered magnitude exceeds the 1/20 percentile
+            o.bf_vsc()
+            np.testing.assert_array_equal(lines, o.bf_nh_lines(o.bf_nh_threshold()))
+        active = np.zeros(nz * nx, np.uint8)
+        active[lines] = 1
+        so = o.bf_sweep_slices(active, rows, stride, 0, k)
+        assert sg[3] == so[3] and sg[2] == so[2], (k, sg, so)
+        assert rel(e.volume(), o.volume()) <= max(tol, 1e-7), (k, rel(e.volume(), o.volume()))
+        assert rel(e.error_sinogram(), o.error()) <= max(tol, 1e-7), k
+        sel, w, mag, _, _ = e.bf_state()
+        assert np.mean(sel != o.selector()) <= 1e-4
+        assert rel(mag, o.mag_map()) <= max(tol, 1e-7), k
+
+
+def test_bf_estimates_and_cost_match(lib_built, oracle_mod):
+    e, o, p, y = pair(lib_built, oracle_mod)
+    e.prepare()
+    o.prepare()
+    for k in range(3):
+        e.sweep(0, k)
+    sync_oracle(e, o)
+    o.offset()[...] = e.nuisance()[1]
+    o.variance()[...] = e.nuisance()[2]
+    cg, pg = e.cost()
+    co, po = o.bf_cost()
+    np.testing.assert_allclose(pg[0], po[0], rtol=1e-6)
+    np.testing.assert_allclose(pg[1], po[1], rtol=1e-5)
+    np.testing.assert_allclose(pg[2], po[2], rtol=1e-12)
+    e.joint_estimation()
+    o.bf_joint_estimation()
+    o.bf_update_selector()
+    np.testing.assert_allclose(e.nuisance()[1], o.offset(), rtol=1e-6)
+    assert rel(e.error_sinogram(), o.error()) <= 1e-5
+    sync_oracle(e, o)
+    e.update_weights()
+    o.bf_update_weights()
+    o.bf_update_selector()
+    np.testing.assert_allclose(e.nuisance()[2], o.variance(), rtol=1e-6)
+    sel, w, _, _, _ = e.bf_state()
+    assert rel(w, o.weight()) <= 1e-6
+    assert np.mean(sel != o.selector()) <= 1e-4
+
+
+def test_bf_reference_exact_run_bitwise(lib_built, oracle_mod):
+    """FP64 reference order: calls with the Bragg schedule (3 inner calls at T = 5e10, then T),
+    offset and variance updates between outer iterations, NHICD lists; the volume rounds to the
+    same float32 values as the oracle's."""
+    mbir = lib_built
+    e, o, p, y = pair(mbir, oracle_mod, order_mode=1, precision=mbir.FP64, outer_iterations=4,
+                      inner_iterations=3, seed=31)
+    e.run()
+    o.prepare()
+    n = o.bf_run(31, 0)
+    assert n == e.status().sweeps_done == 6
+    v = o.volume()
+    assert np.array_equal(e.volume(), v.astype(np.float32)), rel(e.volume(), v)
+    _, off, var = e.nuisance()
+    np.testing.assert_array_equal(off, o.offset())
+    np.testing.assert_array_equal(var, o.variance())
+
+
+def test_bf_calls_decrease_cost(lib_built, oracle_mod):
+    """With the nuisance parameters and T fixed, every ICD call lowers the BF MAP cost."""
+    e, o, p, y = pair(lib_built, oracle_mod)
+    e.prepare()
+    costs = [e.cost()[0]]
+    for k in range(8):
+        e.sweep(0, k)
+        costs.append(e.cost()[0])
+    assert all(b <= a for a, b in zip(costs, costs[1:])), costs

@@ -49,17 +49,25 @@ def test_results_same_alone_and_in_the_mix(lib_built):
 
 
 def test_admission_respects_memory_budget(lib_built):
+    """Each request's estimated footprint is measured alone; with a budget below their sum the
+    server keeps some requests waiting, never exceeds the budget and admits in arrival order."""
     mbir = lib_built
     reqs = requests(mbir)
-    # a budget that fits about one request forces one-at-a-time admission, in arrival order
-    with mbir.Server(0, 24 << 20, 0) as s:
+    sizes = []
+    for p, y, ang in reqs:
+        with mbir.Server(0, 0, 1) as s:
+            s.wait(s.submit(p, y, ang, max_outer=1, tol=0.0))
+            sizes.append(s.stats().peak_bytes)
+    budget = max(sizes) + min(sizes) // 2
+    assert budget < sum(sizes)
+    with mbir.Server(0, budget, 0) as s:
         ids = [s.submit(p, y, ang, max_outer=3, tol=0.0) for p, y, ang in reqs]
         for rid in ids:
             s.wait(rid)
         lat = [s.poll(rid)[1] for rid in ids]
         assert all(l > 0 for l in lat)
         st = s.stats()
-        assert st.budget_bytes == 24 << 20
+        assert st.budget_bytes == budget
         assert 0 < st.peak_bytes <= st.budget_bytes
         assert st.admitted == len(reqs) and st.admitted_out_of_order == 0
         assert st.peak_active < len(reqs)  # the budget kept some requests waiting

@@ -152,3 +152,29 @@ def test_pinned_pow_is_correctly_rounded(oracle_mod):
     mpmath.mp.prec = 200
     for x, y, g in zip(xs[:400], ys[:400], got[:400]):
         assert g == float(mpmath.power(mpmath.mpf(float(x)), mpmath.mpf(float(y))))
+
+
+def test_bf_oracle_monotone_and_nh_lists(oracle_mod):
+    """Oracle self-checks for bright field: NHICD calls with fixed nuisance lower the cost, the
+    NH list has about N/20 lines, and GenRandList's permutation is a permutation."""
+    from conftest import bf_case, bf_params
+    import mbir
+    y, ang, th = bf_case()
+    p = bf_params(mbir, th)
+    o = oracle_mod.Oracle(oracle_mod.params_from_mbir(p), y, ang)
+    o.prepare()
+    nl = o.nz * o.nx
+    c0 = o.bf_cost()[0]
+    perm = oracle_mod.rand_list_perm(7, nl)
+    assert sorted(perm.tolist()) == list(range(nl))
+    master = np.empty(nl, np.int32)
+    master[perm] = np.arange(nl)
+    lines = master[: nl // 20]
+    o.bf_sweep_lines(lines, 0, 0)
+    c1 = o.bf_cost()[0]
+    o.bf_vsc()
+    nh = o.bf_nh_lines(o.bf_nh_threshold())
+    assert 0 < len(nh) <= nl // 20 + 1
+    o.bf_sweep_lines(nh, 0, 1)
+    c2 = o.bf_cost()[0]
+    assert c1 < c0 and c2 <= c1
