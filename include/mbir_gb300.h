@@ -268,6 +268,19 @@ const char* mbir_server_last_error(const mbir_server* s);
 /* Library version string */
 const char* mbir_version(void);
 
+/* Per-view sums of squared errors, sums_dev[v] = sum over r, t of error_dev[v][r][t]^2 (the sums
+ * updateWeights divides by N_r N_t, HAADF_ReconstructionEngine_Extra.cpp:825-833), computed on
+ * caller-owned device buffers (FP32 error sinogram in the reference's [theta][r][t] layout, FP64
+ * output of n_theta values) with no allocation: for callers whose device memory is owned by their
+ * own pool, or whose path must not allocate.  No counterpart in the reference (it is this
+ * library's addition).  Limits: n_theta <= 1024 (MBIR_EINVAL beyond); the scratch (128 KiB of
+ * per-view partial sums, fully rewritten by every call) lives in one static device array per
+ * device, so calls that overlap in time race and must be serialised by the caller.  The first call
+ * on a device looks the scratch up (with that device current): make it before any stream capture.
+ * Launches on `stream` (a cudaStream_t, 0 = legacy default stream) and does not synchronise. */
+int32_t mbir_error_view_sums_noalloc(const float* error_dev, int32_t n_theta, int32_t n_r,
+                                     int32_t n_t, double* sums_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,7 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["mbir_sweep_f32.cu", "mbir_sweep_f32_bf.cu", "mbir_sweep_f32_hbm.cu",
            "mbir_sweep_f32_batch3.cu", "mbir_sweep_f32_batch5.cu", "mbir_sweep_f64.cu",
            "mbir_kernels.cu",
-           "mbir_exact.cu", "mbir_bf.cu",
+           "mbir_exact.cu", "mbir_bf.cu", "mbir_noalloc.cu",
            "mbir_engine.cu", "mbir_engine_bf.cu", "mbir_batch.cu", "mbir_server.cpp", "mrc_io.cpp",
            "mbir_capi.cpp"]
 HEADERS = ["mbir_internal.h", "mbir_engine.h", "mbir_sweep.cuh", "mbir_batch.h",

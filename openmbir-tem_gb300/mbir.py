@@ -138,6 +138,8 @@ SIGNATURES = {
     "mbir_get_tables": (C.c_int32, [C.c_void_p, _D, _D]),
     "mbir_get_schedule": (C.c_int32, [C.c_void_p, C.c_int32, _I, _I]),
     "mbir_get_call_lines": (C.c_int32, [C.c_void_p, _I, C.c_int32, _I]),
+    "mbir_error_view_sums_noalloc": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                                 C.c_void_p, C.c_void_p]),
     "mbir_get_bf_state": (C.c_int32, [C.c_void_p, C.POINTER(C.c_uint8), _F, _D, _D, _D]),
     "mbir_set_bragg_threshold": (C.c_int32, [C.c_void_p, C.c_double]),
     "mbir_status_get": (C.c_int32, [C.c_void_p, C.POINTER(MbirStatus)]),
