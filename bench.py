@@ -327,6 +327,8 @@ def main():
                         "frac": achieved / peak, "traffic": traffic,
                         "peak_source": peak_kind,
                         "algorithmic_bytes_per_step": bytes_step,
+                        "algorithmic_bytes_per_launch": bytes_step / (2 * calls_per_step),
+                        "traffic_unit": "bytes per colour launch (ncu capture)",
                         "bytes_model": ("13*F*L+8" if bf else "8*F*L+8") +
                                        " per updated voxel, F=A-column nnz, L=t rows",
                         "kernel": "sweep_kernel (two colour launches per call)"},

@@ -252,6 +252,7 @@ struct SliceCtx {
   Real* cache;               // [9][n_x] neighbour rows (dy,dz) or nullptr (read global)
   int tcount;
   int mode, iter_nonzero, zero_skipping;
+  int inline_zs;             // run the zero-skipping test in group_step (candidates may be skipped)
   // bright field: per-entry weights (HBM), Bragg selector (shared memory or HBM)
   const Real* bw;
   int bw_rs, bw_ps;
@@ -324,7 +325,7 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
         }
       }
     }
-    if constexpr (INLINE_ZS) {
+    if (INLINE_ZS || c.inline_zs) {
       // the ballot runs on all 32 lanes: the two voxel groups of a warp may disagree
       const bool any_pos = group_any<G>(pos, lane);
       if (c.zero_skipping && c.iter_nonzero && V == Real(0) && !any_pos) {
@@ -452,9 +453,10 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
   if (nv < Real(0)) nv = Real(0);  // positivity (UpdateVoxels.cpp:394-400, BFConstants.h)
   const Real dlt = nv - V;
   if (!live) return;
-  // error-sinogram scatter (UpdateVoxels.cpp:423-449; BF also re-evaluates the selector,
-  // BFForwardModel.cpp:898-932)
-  if (dlt != Real(0)) {
+  // error-sinogram scatter (UpdateVoxels.cpp:423-449).  BF re-evaluates the selector of every
+  // footprint entry even when the voxel did not change (BFForwardModel.cpp:898-932), so the
+  // scatter runs then too.
+  if (BF || dlt != Real(0)) {
 #pragma unroll
     for (int i = 0; i < VPL; ++i) {
       const int v = gl + G * i;
@@ -498,7 +500,7 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
 }
 
 struct SmemLayout {
-  size_t bar, ctl, stats, rb, bx, bxd, gw, H, hv, list, cache, es, sel, total;
+  size_t bar, ctl, stats, rb, bx, bxd, gw, H, hv, list, cls, okr, lv, cache, es, sel, total;
 };
 
 __host__ __device__ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -529,8 +531,14 @@ __host__ __device__ inline SmemLayout smem_layout(int n_theta, int n_x, int n_rs
   o = align_up(o + real_bytes * n_theta * (bins + 1), 16);
   L.hv = o;
   o = align_up(o + real_bytes * kMaxTRows, 16);
-  L.list = o;
-  o = align_up(o + sizeof(int) * static_cast<size_t>(n_x), 16);
+  L.list = o;  // class segments of the current row: S * ceil(n_x / S) <= 2 n_x + 2 slots
+  o = align_up(o + sizeof(int) * (2 * static_cast<size_t>(n_x) + 2), 16);
+  L.cls = o;   // candidates per class (S <= max(n_x, 2))
+  o = align_up(o + sizeof(int) * (static_cast<size_t>(n_x) + 2), 16);
+  L.okr = o;   // row flags: non-empty A-column and in the call's line list
+  o = align_up(o + static_cast<size_t>(n_x), 16);
+  L.lv = o;    // row flags: bit 0 live at row start, bit 1 live-or-reachable (period prefix)
+  o = align_up(o + static_cast<size_t>(n_x), 16);
   L.cache = o;
   o = align_up(o + real_bytes * 9 * static_cast<size_t>(n_x), 128);
   L.es = o;
@@ -687,13 +695,20 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
     c.mag_fx = A.bfa.mag_fx;
   }
   const uint8_t* active_lines = BF ? A.bfa.active : nullptr;
+  int* cls = reinterpret_cast<int*>(smem + L.cls);
+  uint8_t* okr = smem + L.okr;
+  uint8_t* lv = smem + L.lv;
+  const int S = A.stride;
+  const int cap = (g.n_x + S - 1) / S;
+  const bool project = A.mode == kModeProject;
+  const bool zs_on = !project && A.zero_skipping && A.iter_nonzero;
+  c.inline_zs = zs_on ? 1 : 0;
 
   const size_t vplane = static_cast<size_t>(g.n_z) * g.n_x;
   GroupAcc acc;
 #pragma unroll
-  for (int s = 0; s < kStatSlots; ++s) acc.v[s] = 0ull;
+  for (int s2 = 0; s2 < kStatSlots; ++s2) acc.v[s2] = 0ull;
   unsigned skipped = 0;
-  unsigned step = 0;  // class steps so far: selects the double-buffered list counter
   for (int rr = 0; rr < g.n_z; ++rr) {
     const int z = A.row_order[rr];
     __syncthreads();
@@ -709,32 +724,64 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
       }
       cache[i] = v;
     }
+    for (int x = tid; x < g.n_x; x += nthreads) {
+      const size_t l = static_cast<size_t>(z) * g.n_x + x;
+      okr[x] = (A.tab.lineok[l] && (active_lines == nullptr || active_lines[l])) ? 1 : 0;
+    }
     __syncthreads();
-    const uint8_t* okrow = A.tab.lineok + static_cast<size_t>(z) * g.n_x;
-    const uint8_t* actrow = active_lines ? active_lines + static_cast<size_t>(z) * g.n_x : nullptr;
-    for (int k = 0; k < A.stride; ++k, ++step) {
-      // compact the class: x = k, k+S, ... that will be updated.  The counter of this step
-      // was cleared during the previous step; the other one (read as the previous step's list
-      // length before the previous barrier) is cleared now for the next step.
-      unsigned* cnt = ctl + (step & 1u);
-      if (tid == 0) ctl[(step + 1u) & 1u] = 0u;
-      for (int x = k + A.stride * tid; x < g.n_x; x += A.stride * nthreads) {
-        if (!okrow[x] || (actrow && !actrow[x])) continue;
+    // liveness at the start of the row: projection needs V != 0; ICD voxels that would be
+    // zero-skipped now are not live
+    for (int x = tid; x < g.n_x; x += nthreads) {
+      uint8_t f = 0;
+      if (okr[x]) {
         const Real V = cache[4 * g.n_x + x];
-        if (A.mode == kModeProject) {
-          if (V == Real(0)) continue;
-        } else if (zero_skipped(c, x, V)) {
-          ++skipped;
-          continue;
+        f = project ? (V != Real(0)) : !zero_skipped(c, x, V);
+      }
+      lv[x] = f;
+    }
+    __syncthreads();
+    // A voxel skipped at the start of its row can still be updated if a same-row neighbour that
+    // is processed before it became positive: within a stride period [mS, mS+S) classes run
+    // left to right, so reachability is the period's prefix-OR; the period's last voxel also
+    // follows the next period's first one.  Bit 1 marks the candidates.
+    if (zs_on) {
+      for (int m = tid; m * S < g.n_x; m += nthreads) {
+        uint8_t a = 0;
+        const int x0 = m * S;
+        for (int j = 0; j < S && x0 + j < g.n_x; ++j) {
+          a |= lv[x0 + j] & 1;
+          uint8_t b = a;
+          if (j == S - 1 && x0 + S < g.n_x) b |= lv[x0 + S] & 1;
+          lv[x0 + j] = static_cast<uint8_t>((lv[x0 + j] & 1) | (b << 1));
         }
-        list[atomicAdd(cnt, 1u)] = x;
       }
       __syncthreads();
-      const int n = static_cast<int>(*cnt);
-      for (int base = 0; base < n; base += n_groups) {
-        const int i = base + group;
+    }
+    // compaction: warp w lists the candidates of classes w, w + warps, ... in ascending x
+    for (int k = warp; k < S; k += nthreads / 32) {
+      int base = 0;
+      for (int m0 = 0; k + S * m0 < g.n_x; m0 += 32) {
+        const int x = k + S * (m0 + lane);
+        bool cand = false;
+        if (x < g.n_x && okr[x]) {
+          cand = zs_on ? ((lv[x] >> 1) & 1) != 0 : (lv[x] & 1) != 0;
+          if (!cand && !project) ++skipped;
+        }
+        const unsigned b = __ballot_sync(kFull, cand);
+        if (cand) list[k * cap + base + __popc(b & ((1u << lane) - 1u))] = x;
+        base += __popc(b);
+      }
+      if (lane == 0) cls[k] = base;
+    }
+    __syncthreads();
+    for (int k = 0; k < S; ++k) {
+      const int n = cls[k];
+      if (n == 0) continue;
+      for (int b0 = 0; b0 < n; b0 += n_groups) {
+        const int i = b0 + group;
         const bool act = i < n;
-        group_step<Real, NB, G, VPL, BF, false>(c, z, act ? list[i] : 0, y, act, lane, acc);
+        group_step<Real, NB, G, VPL, BF, false>(c, z, act ? list[k * cap + i] : 0, y, act, lane,
+                                                acc);
       }
       __syncthreads();
     }
@@ -903,6 +950,7 @@ __global__ void __launch_bounds__(32, 1) ref_order_kernel(RefOrderArgs A) {
   c.mode = kModeICD;
   c.iter_nonzero = A.iter_nonzero;
   c.zero_skipping = A.zero_skipping;
+  c.inline_zs = 1;
   c.bw = nullptr;
   c.bs = nullptr;
   c.mag_fx = nullptr;
