@@ -113,6 +113,10 @@ typedef struct mbir_params {
                                  1: always work on them in HBM (same results, for tuning) */
   int32_t nhicd;              /* BF: 1 = non-homogeneous ICD line lists (the reference's NHICD
                                  build, BFConstants.h), 0 = every voxel line in each call */
+  int32_t lane_shape;         /* FP32 voxel-group shape: 0 = autotuned at prepare; 1 = 16 lanes x
+                                 4 views (<= 64 views), 2 = 32 x 2 (<= 64), 3 = 32 x 3 (<= 96),
+                                 4 = 32 x 5 (<= 160).  Results depend on the shape in the last bits
+                                 (summation order); fix it for bit-reproducible runs. */
 } mbir_params;
 
 typedef struct mbir_status {
@@ -129,7 +133,7 @@ typedef struct mbir_status {
   int32_t t_rows;         /* detector rows touched by one voxel slice (voxel-line response) */
   int32_t stride;         /* x stride of the conflict-free voxel sets */
   int32_t staged;         /* 1: voxel slices staged in shared memory, 0: slices read from HBM */
-  int32_t reserved;
+  int32_t lane_shape;     /* voxel-group shape in use (see mbir_params.lane_shape) */
 } mbir_status;
 
 typedef struct mbir_engine mbir_engine;
@@ -191,6 +195,28 @@ int32_t mbir_get_bf_state(mbir_engine* e, uint8_t* selector, float* weights, dou
                           double* filtered_mag, double* bragg_t);
 /* BFForwardModel::setBraggThreshold (BFForwardModel.h): T used by the next calls */
 int32_t mbir_set_bragg_threshold(mbir_engine* e, double t);
+
+/* y-slab sharding of one reconstruction over several engines (one per GPU), driven by a host
+ * that exchanges boundary planes and sums per-view statistics between them.  Replaces the
+ * y-range task split of updateVoxels (HAADF_ReconstructionEngine_UpdateVoxels.cpp:666-723)
+ * across devices instead of threads.  HAADF, parallel order.
+ *   mbir_set_slab: later colour sweeps and view sums cover slices [y0, y1) only (0, 0 = all)
+ *   mbir_sweep_colour: one colour (0 even, 1 odd slices) of the parallel sweep; the row order of
+ *     sweep k serves both colours and the sweep counts after colour 1
+ *   mbir_get_planes / mbir_set_planes: voxel planes y .. y+n-1 as [n][z][x] floats (FP32 engines)
+ *   mbir_view_sums: kind 0 = the six jointEstimation sums per view [theta][6] (y w, w, yh w,
+ *     yh w y, y^2 w, yh^2 w; _Extra.cpp:474-517), kind 1 = sum e^2 per view (:825-833), over the
+ *     detector rows of the slab
+ *   mbir_apply_nuisance: new gain/offset (null to keep) with the jointEstimation error rebuild
+ *     (:600-612) and/or new variance (null to keep) */
+int32_t mbir_set_slab(mbir_engine* e, int32_t y0, int32_t y1);
+int32_t mbir_sweep_colour(mbir_engine* e, int32_t colour, int32_t outer, int32_t inner,
+                          double* stats4);
+int32_t mbir_get_planes(mbir_engine* e, int32_t y, int32_t n, float* out);
+int32_t mbir_set_planes(mbir_engine* e, int32_t y, int32_t n, const float* in);
+int32_t mbir_view_sums(mbir_engine* e, int32_t kind, double* out);
+int32_t mbir_apply_nuisance(mbir_engine* e, const double* gain, const double* offset,
+                            const double* variance);
 int32_t mbir_status_get(mbir_engine* e, mbir_status* st);
 void mbir_cancel(mbir_engine* e);
 

@@ -21,7 +21,7 @@ SOURCES = ["mbir_sweep_f32.cu", "mbir_sweep_f32_bf.cu", "mbir_sweep_f32_hbm.cu",
            "mbir_sweep_f32_batch3.cu", "mbir_sweep_f32_batch5.cu", "mbir_sweep_f64.cu",
            "mbir_kernels.cu",
            "mbir_exact.cu", "mbir_bf.cu", "mbir_noalloc.cu",
-           "mbir_engine.cu", "mbir_engine_bf.cu", "mbir_batch.cu", "mbir_server.cpp", "mrc_io.cpp",
+           "mbir_engine.cu", "mbir_engine_bf.cu", "mbir_shard.cu", "mbir_batch.cu", "mbir_server.cpp", "mrc_io.cpp",
            "mbir_capi.cpp"]
 HEADERS = ["mbir_internal.h", "mbir_engine.h", "mbir_sweep.cuh", "mbir_batch.h",
            "mbir_server.h"]
@@ -54,7 +54,10 @@ def _compile(src, verbose=False, ptxas_v=False):
     cmd[1:1] = ["-Xcompiler", "-ffp-contract=off"]
     if src.endswith(".cu"):
         cmd[1:1] = ARCH + ["-lineinfo", "--expt-relaxed-constexpr"]
-        if src in ("mbir_exact.cu", "mbir_bf.cu"):
+        # no fused multiply-adds: the reference-exact and BF passes must reproduce FP64 operation
+        # by operation, and every FP32 sweep kernel (single slice, batched, any caller) must round
+        # identically so a reconstruction gives the same bits alone and inside a batch
+        if src in ("mbir_exact.cu", "mbir_bf.cu") or src.startswith("mbir_sweep_f32"):
             cmd[1:1] = ["-fmad=false"]
         if ptxas_v:
             cmd.insert(1, "-Xptxas=-v")

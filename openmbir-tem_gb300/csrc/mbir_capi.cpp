@@ -215,6 +215,26 @@ int32_t mbir_get_bf_state(mbir_engine* e, uint8_t* selector, float* weights, dou
 int32_t mbir_set_bragg_threshold(mbir_engine* e, double t) {
   return guarded(e, [&](mbir::Engine& m) { return m.set_bragg_threshold(t); });
 }
+int32_t mbir_set_slab(mbir_engine* e, int32_t y0, int32_t y1) {
+  return guarded(e, [&](mbir::Engine& m) { return m.set_slab(y0, y1); });
+}
+int32_t mbir_sweep_colour(mbir_engine* e, int32_t colour, int32_t outer, int32_t inner,
+                          double* stats4) {
+  return guarded(e, [&](mbir::Engine& m) { return m.sweep_colour(colour, outer, inner, stats4); });
+}
+int32_t mbir_get_planes(mbir_engine* e, int32_t y, int32_t n, float* out) {
+  return guarded(e, [&](mbir::Engine& m) { return m.get_planes(y, n, out); });
+}
+int32_t mbir_set_planes(mbir_engine* e, int32_t y, int32_t n, const float* in) {
+  return guarded(e, [&](mbir::Engine& m) { return m.set_planes(y, n, in); });
+}
+int32_t mbir_view_sums(mbir_engine* e, int32_t kind, double* out) {
+  return guarded(e, [&](mbir::Engine& m) { return m.view_sums(kind, out); });
+}
+int32_t mbir_apply_nuisance(mbir_engine* e, const double* gain, const double* offset,
+                            const double* variance) {
+  return guarded(e, [&](mbir::Engine& m) { return m.apply_nuisance(gain, offset, variance); });
+}
 int32_t mbir_status_get(mbir_engine* e, mbir_status* st) {
   return guarded(e, [&](mbir::Engine& m) { return m.status(st); });
 }

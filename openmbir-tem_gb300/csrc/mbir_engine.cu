@@ -12,6 +12,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <sstream>
 
 #include "mbir_engine.h"
@@ -737,9 +739,18 @@ int Engine::prepare() {
   if ((rc = upload_views())) return rc;
   state_ = 2;
   sweeps_done_ = 0;
+  // voxel-group shape: the requested one when it covers the views, else the default
+  shape_ = 0;
+  if (p_.lane_shape >= 1 && p_.lane_shape <= 4 && g.n_theta <= shape_max_views(p_.lane_shape))
+    shape_ = p_.lane_shape;
+  if (shape_ == 0) {
+    const int d = lane_shape(g.n_theta);
+    shape_ = d == 0 ? 1 : d + 2;
+  }
   // forward projection + error sinogram (HAADF_ReconstructionEngine.cpp:636-691)
   if ((rc = forward_project())) return rc;
   if (bf_ && (rc = bf_upload())) return rc;
+  if (p_.lane_shape == 0 && (rc = autotune_shape())) return rc;
   return MBIR_OK;
 }
 
@@ -773,6 +784,7 @@ int Engine::forward_project() {
   a.fp64 = fp64_;
   a.smem_rows = stage_ ? 1 : 0;
   a.n_rs = stage_ ? n_rs_ : 0;
+  a.shape = shape_;
   a.stats = nullptr;
   a.err = d_err_;
   for (int colour = 0; colour < 2; colour++) {
@@ -855,6 +867,7 @@ int Engine::sweep(int outer, int inner, double* stats4) {
     a.zero_skipping = p_.zero_skipping;
     a.smem_rows = stage_ ? 1 : 0;
     a.n_rs = stage_ ? n_rs_ : 0;
+    a.shape = shape_;
     a.err = d_err_;
     const int n0 = (g.n_y + 1) / 2;
     for (int colour = 0; colour < 2; colour++) {
@@ -935,6 +948,7 @@ int Engine::batch_args(int outer, int inner, SweepArgs* out, size_t* smem_needed
   a.zero_skipping = p_.zero_skipping;
   a.smem_rows = stage_ ? 1 : 0;
   a.n_rs = stage_ ? n_rs_ : 0;
+  a.shape = shape_;
   a.err = d_err_;
   a.stats = d_stats_;
   a.colour = 0;
@@ -1201,7 +1215,7 @@ int Engine::status(mbir_status* st) const {
   st->t_rows = t_rows_;
   st->stride = stride_;
   st->staged = stage_ ? 1 : 0;
-  st->reserved = 0;
+  st->lane_shape = shape_;
   return MBIR_OK;
 }
 
@@ -1261,4 +1275,124 @@ int Engine::write_outputs(const char* dir, const char* mrc_path) {
   return MBIR_OK;
 }
 
+// Autotuner of the FP32 voxel-group shape (lanes per voxel x views per lane).  When more than one
+// shape covers the view count, each candidate runs one trial ICD pass (both colours, every
+// line, the current state) on a snapshot of the volume, error sinogram and selector; the state
+// is restored after every trial and the fastest candidate is kept.  Choices are cached per
+// (views, x, z, y, footprint bins, modality, staging) for the life of the process, so engines of
+// the same geometry tune once.
+namespace {
+std::mutex g_tune_mu;
+std::map<std::vector<int>, int> g_tune_cache;
+}  // namespace
+
+int Engine::autotune_shape() {
+  if (fp64_ || p_.order_mode != MBIR_ORDER_PARALLEL) return MBIR_OK;
+  const Geometry& g = g_;
+  std::vector<int> cands;
+  for (int sh = 1; sh <= 4; sh++)
+    if (g.n_theta <= shape_max_views(sh) && (sh == 1 || sh == 2 || g.n_theta > shape_max_views(sh - 1)))
+      cands.push_back(sh);
+  if (nb_ == 9 || cands.size() < 2) return MBIR_OK;
+  const std::vector<int> key = {g.n_theta, g.n_x, g.n_z, g.n_y, nb_, bf_ ? 1 : 0, stage_ ? 1 : 0};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      shape_ = it->second;
+      return MBIR_OK;
+    }
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const size_t nvb = static_cast<size_t>(g.n_z) * g.n_x * g.n_y * rb_;
+  const size_t neb = static_cast<size_t>(g.n_t) * g.n_theta * n_rp_ * rb_;
+  const size_t nsb = bf_ ? static_cast<size_t>(g.n_t) * g.n_theta * n_sp_ : 0;
+  const size_t nl = static_cast<size_t>(g.n_z) * g.n_x;
+  void *sx = nullptr, *se = nullptr, *ss = nullptr, *sm = nullptr;
+  if (cudaMalloc(&sx, nvb) != cudaSuccess || cudaMalloc(&se, neb) != cudaSuccess ||
+      (nsb && cudaMalloc(&ss, nsb) != cudaSuccess) ||
+      (bf_ && cudaMalloc(&sm, nl * sizeof(unsigned long long)) != cudaSuccess)) {
+    cudaFree(sx);
+    cudaFree(se);
+    cudaFree(ss);
+    cudaFree(sm);
+    cudaGetLastError();
+    return MBIR_OK;  // no room for a snapshot: keep the default shape
+  }
+  cudaMemcpyAsync(sx, d_x_, nvb, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(se, d_e_, neb, cudaMemcpyDeviceToDevice, s);
+  if (nsb) cudaMemcpyAsync(ss, d_sel_, nsb, cudaMemcpyDeviceToDevice, s);
+  if (bf_) {
+    cudaMemcpyAsync(sm, d_magfx_, nl * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, s);
+    cudaMemsetAsync(d_active_, 1, nl, s);
+  }
+  std::vector<int32_t> rows(g.n_z);
+  for (int i = 0; i < g.n_z; i++) rows[i] = i;
+  cudaMemcpyAsync(d_rows_, rows.data(), sizeof(int) * g.n_z, cudaMemcpyHostToDevice, s);
+  SweepArgs a{};
+  a.g = dg_;
+  a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_, d_lineok_};
+  a.flt = flt_;
+  a.x = d_x_;
+  a.e = d_e_;
+  a.row_order = d_rows_;
+  a.stride = stride_;
+  a.mode = kModeICD;
+  a.fp64 = 0;
+  a.iter_nonzero = 0;
+  a.zero_skipping = p_.zero_skipping;
+  a.smem_rows = stage_ ? 1 : 0;
+  a.n_rs = stage_ ? n_rs_ : 0;
+  a.err = d_err_;
+  if (bf_) {
+    a.bf = 1;
+    a.bfa.w = d_w_;
+    a.bfa.sel = d_sel_;
+    a.bfa.n_sp = n_sp_;
+    a.bfa.active = d_active_;
+    a.bfa.mag_fx = d_magfx_;
+    a.bfa.bragg_t = bragg_t_;
+    a.bfa.bragg_dt = p_.bragg_delta * bragg_t_;
+  }
+  const int n0 = (g.n_y + 1) / 2;
+  int best = shape_;
+  float best_ms = 0;
+  int rc = MBIR_OK;
+  for (int sh : cands) {
+    a.shape = sh;
+    cudaEventRecord(static_cast<cudaEvent_t>(ev0_), s);
+    for (int colour = 0; colour < 2 && rc == MBIR_OK; colour++) {
+      a.colour = colour;
+      a.n_slices = (g.n_y - colour + 1) / 2;
+      a.stats = d_stats_ + (colour ? static_cast<size_t>(n0) * kStatSlots : 0);
+      if (a.n_slices > 0) rc = launch_sweep(a, nb_, smem_bytes_, s);
+    }
+    cudaEventRecord(static_cast<cudaEvent_t>(ev1_), s);
+    // restore the state for the next candidate (and for the reconstruction itself)
+    cudaMemcpyAsync(d_x_, sx, nvb, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(d_e_, se, neb, cudaMemcpyDeviceToDevice, s);
+    if (nsb) cudaMemcpyAsync(d_sel_, ss, nsb, cudaMemcpyDeviceToDevice, s);
+    if (bf_) cudaMemcpyAsync(d_magfx_, sm, nl * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, s);
+    if (rc != MBIR_OK || cudaStreamSynchronize(s) != cudaSuccess) break;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, static_cast<cudaEvent_t>(ev0_), static_cast<cudaEvent_t>(ev1_));
+    if (best_ms == 0 || ms < best_ms) {
+      best_ms = ms;
+      best = sh;
+    }
+  }
+  cudaFree(sx);
+  cudaFree(se);
+  cudaFree(ss);
+  cudaFree(sm);
+  if (rc != MBIR_OK) return cuda_check(rc, "shape autotune");
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "shape autotune");
+  if ((rc = check_device_error())) return rc;
+  shape_ = best;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_cache[key] = best;
+  return MBIR_OK;
+}
+
 }  // namespace mbir
+

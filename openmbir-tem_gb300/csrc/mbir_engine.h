@@ -81,6 +81,13 @@ class Engine {
   // filtered map [z][x], current Bragg threshold (each output optional)
   int get_bf_state(uint8_t* sel, float* w, double* mag, double* filt, double* bragg_t);
   int set_bragg_threshold(double t);
+  // y-slab sharding (mbir_shard.cu): sweeps and per-view sums restricted to slices [y0, y1)
+  int set_slab(int y0, int y1);
+  int sweep_colour(int colour, int outer, int inner, double* stats4);
+  int get_planes(int y, int n, float* out);
+  int set_planes(int y, int n, const float* in);
+  int view_sums(int kind, double* out);
+  int apply_nuisance(const double* gain, const double* offset, const double* variance);
   int status(mbir_status* st) const;
   void cancel() { cancel_.store(1); }
   int write_outputs(const char* dir, const char* mrc_path);
@@ -120,6 +127,7 @@ class Engine {
   BfSino bf_sino() const;
   double bf_default_offset() const;
 
+  int autotune_shape();  // pick the fastest voxel-group shape on a snapshot of the state
   int build_host();  // geometry, tables, stride, initial nuisance: no GPU needed
   int build_geometry();
   int build_tables();
@@ -152,6 +160,7 @@ class Engine {
   int n_rp_ = 0;      // HBM row stride
   int n_rs_ = 0;      // shared-memory row stride
   int n_sp_ = 0;      // bright-field selector row stride (bytes, multiple of 16)
+  int shape_ = 0;     // FP32 voxel-group shape in use (mbir_params.lane_shape)
   bool bf_ = false;   // bright-field modality
   int t_rows_ = 1;    // max t rows per voxel slice
   int stride_ = 2;    // conflict-free x stride
@@ -231,6 +240,7 @@ class Engine {
   std::vector<int32_t> call_lines_;         // lines of the last sweep/call
   std::vector<uint8_t> active_host_;
   uint32_t bf_listsel_ = 0, bf_eff_ = 0;
+  int slab_y0_ = 0, slab_y1_ = 0;           // 0, 0: the whole volume
   int bf_calls_ = 0;
   double bragg_t_ = 0;
 };

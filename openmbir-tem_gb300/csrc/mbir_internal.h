@@ -19,6 +19,11 @@ constexpr int kMaxViewsPerLane = 5;   // n_theta <= 160
 // Voxel-group shape of the FP32 sweep kernels for n_theta views: 0 = 16 lanes x 4 views per
 // lane (two voxels per warp), 1 = 32 lanes x 3 views, 2 = 32 lanes x 5 views.
 inline int lane_shape(int n_theta) { return n_theta <= 64 ? 0 : (n_theta <= 96 ? 1 : 2); }
+// Explicit shapes of the public parameter: 1 = 16x4, 2 = 32x2, 3 = 32x3, 4 = 32x5; the largest
+// view count each covers
+inline int shape_max_views(int shape) {
+  return shape == 1 ? 64 : shape == 2 ? 64 : shape == 3 ? 96 : shape == 4 ? 160 : 0;
+}
 constexpr int kWarps = 16;            // warps per ICD block
 constexpr int kMaxTRows = 4;          // t rows a voxel slice may touch
 constexpr int kStatSlots = 4;         // sum|dx| (ROI), sum|x| (ROI), zero-skipped, updated
@@ -90,6 +95,9 @@ struct SweepArgs {
   int fp64;              // 1: Real = double
   int bf;                // 1: bright-field data term (DevBF below)
   DevBF bfa;
+  int shape;             // FP32 voxel-group shape (1..4), 0: lane_shape(n_theta)
+  int y_first;           // slab launch: first slice (its parity is the colour)
+  int y_end;             // slab launch: slices y < y_end; 0 = whole-volume launch from `colour`
   double* stats;         // [gridDim.x][kStatSlots]
   int* err;              // device error word
 };
@@ -212,6 +220,11 @@ int launch_vol_to_host(const void* yzx, float* zxy, int n_z, int n_x, int n_y, i
 int launch_error_from_projection(const void* y, const void* yest, void* e, const double* mu,
                                  int n_theta, int n_rp, int n_r, int n_t, int fp64, void* stream);
 // per-view FP64 sums; kind 0: joint-estimation sums (6), kind 1: sum e^2 (1)
+// per-view sums over detector rows [t_begin, t_end)
+int launch_view_sums_rows(int kind, const void* y, const void* e, const double* mu,
+                          const double* gain, const double* wv, double* partial, double* out,
+                          int n_theta, int n_rp, int n_r, int t_begin, int t_end, int n_chunk,
+                          int fp64, void* stream);
 int launch_view_sums(int kind, const void* y, const void* e, const double* mu,
                      const double* gain, const double* wv, double* partial, double* out,
                      int n_theta, int n_rp, int n_r, int n_t, int n_chunk, int fp64,

@@ -193,10 +193,12 @@ template <typename Real, int K>
 __global__ void view_sums_kernel(const Real* __restrict__ y, const Real* __restrict__ e,
                                  const double* __restrict__ mu, const double* __restrict__ gain,
                                  const double* __restrict__ wv, double* __restrict__ partial,
-                                 int n_theta, int n_rp, int n_r, int n_t, int n_chunk) {
+                                 int n_theta, int n_rp, int n_r, int t_begin, int t_end,
+                                 int n_chunk) {
   const int v = blockIdx.x, ch = blockIdx.y;
-  const int t0 = static_cast<int>(static_cast<long long>(ch) * n_t / n_chunk);
-  const int t1 = static_cast<int>(static_cast<long long>(ch + 1) * n_t / n_chunk);
+  const int n_t = t_end - t_begin;
+  const int t0 = t_begin + static_cast<int>(static_cast<long long>(ch) * n_t / n_chunk);
+  const int t1 = t_begin + static_cast<int>(static_cast<long long>(ch + 1) * n_t / n_chunk);
   double acc[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) acc[k] = 0.0;
@@ -429,23 +431,31 @@ int launch_view_sums(int kind, const void* y, const void* e, const double* mu,
                      const double* gain, const double* wv, double* partial, double* out,
                      int n_theta, int n_rp, int n_r, int n_t, int n_chunk, int fp64,
                      void* stream) {
+  return launch_view_sums_rows(kind, y, e, mu, gain, wv, partial, out, n_theta, n_rp, n_r, 0, n_t,
+                               n_chunk, fp64, stream);
+}
+
+int launch_view_sums_rows(int kind, const void* y, const void* e, const double* mu,
+                          const double* gain, const double* wv, double* partial, double* out,
+                          int n_theta, int n_rp, int n_r, int t_begin, int t_end, int n_chunk,
+                          int fp64, void* stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   dim3 grid(n_theta, n_chunk);
   const int K = kind == 0 ? 6 : 1;
   if (fp64) {
     if (kind == 0)
       view_sums_kernel<double, 6><<<grid, 256, 0, s>>>(RP<double>(y), RP<double>(e), mu, gain, wv,
-                                                        partial, n_theta, n_rp, n_r, n_t, n_chunk);
+                                                        partial, n_theta, n_rp, n_r, t_begin, t_end, n_chunk);
     else
       view_sums_kernel<double, 1><<<grid, 256, 0, s>>>(RP<double>(y), RP<double>(e), mu, gain, wv,
-                                                        partial, n_theta, n_rp, n_r, n_t, n_chunk);
+                                                        partial, n_theta, n_rp, n_r, t_begin, t_end, n_chunk);
   } else {
     if (kind == 0)
       view_sums_kernel<float, 6><<<grid, 256, 0, s>>>(RP<float>(y), RP<float>(e), mu, gain, wv,
-                                                       partial, n_theta, n_rp, n_r, n_t, n_chunk);
+                                                       partial, n_theta, n_rp, n_r, t_begin, t_end, n_chunk);
     else
       view_sums_kernel<float, 1><<<grid, 256, 0, s>>>(RP<float>(y), RP<float>(e), mu, gain, wv,
-                                                       partial, n_theta, n_rp, n_r, n_t, n_chunk);
+                                                       partial, n_theta, n_rp, n_r, t_begin, t_end, n_chunk);
   }
   const int n = n_theta * K;
   view_sums_final_kernel<<<(n + 127) / 128, 128, 0, s>>>(partial, out, n_theta, n_chunk, K);

@@ -338,6 +338,22 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
   }
   if (!__any_sync(kFull, live)) return;
 
+  // QGGMRF surrogate sums of this lane's neighbours (QGGMRF_Functions.cpp:153-206): they need
+  // only V and the neighbours, so their transcendental arithmetic is issued before the
+  // footprint's memory traffic and overlaps it
+  Real s1 = Real(0), s2 = Real(0);
+  if (c.mode != kModeProject) {
+#pragma unroll
+    for (int i = 0; i < NNB; ++i) {
+      if (nvalid[i]) {
+        const Real tc =
+            static_cast<Real>(c.q->f[gl + G * i]) * qggmrf_coef<Real>(*c.q, V - nb[i]);
+        s1 += tc * nb[i];
+        s2 += tc;
+      }
+    }
+  }
+
   // A-column of the voxel, lanes over views (AMatrixCol.cpp:148-232)
   const Real hw = static_cast<Real>(g.half_width);
   int jlo[VPL];
@@ -380,40 +396,97 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
   // BFForwardModel.cpp:851-892, entries the Bragg selector rejects weighted by
   // delta T / (|e| sqrt(w)))
   Real t1 = Real(0), t2 = Real(0);
+  // One detector row per slice (delta_xy = delta_t, every fine level): the footprint's error
+  // values (and, for bright field, weights and selector bytes) are gathered into registers in
+  // one batch -- unconditional loads from a safe index, so they are all in flight together --
+  // and reused by the scatter.
+  const bool one_row = c.tcount == 1;
+  constexpr int BV = BF ? VPL : 1, BN = BF ? NB : 1;
+  Real ev[VPL][NB];
+  Real wv[BV][BN];
+  uint8_t sv[BV][BN];
+  int eidx[VPL];
+  if (one_row) {
+    const Real hh = c.hv[0];
 #pragma unroll
-  for (int i = 0; i < VPL; ++i) {
-    const int v = gl + G * i;
-    if (v >= g.n_theta || !live) continue;
-    const R2 gw = c.sgw[v];
-    for (int tr = 0; tr < c.tcount; ++tr) {
-      const Real hh = c.hv[tr];
-      const Real* row = c.es + tr * c.ps + v * c.rs + jlo[i];
-      if constexpr (BF) {
-        const Real* wr = c.bw + tr * c.bw_ps + v * c.bw_rs + jlo[i];
-        const uint8_t* sr = c.bs + tr * c.bs_ps + v * c.bs_rs + jlo[i];
+    for (int i = 0; i < VPL; ++i) {
+      const int v = gl + G * i;
+      const bool vok = v < g.n_theta && live;
+      eidx[i] = vok ? v * c.rs + jlo[i] : 0;
+      const int widx = vok ? v * c.bw_rs + jlo[i] : 0;
+      const int sidx = vok ? v * c.bs_rs + jlo[i] : 0;
 #pragma unroll
-        for (int b = 0; b < NB; ++b) {
-          if (a[i][b] > Real(0)) {
-            const Real ev = row[b];
-            const Real w = __ldg(wr + b);
-            const Real pe = gw.x * a[i][b] * hh;
-            if (sr[b]) {
+      for (int b = 0; b < NB; ++b) {
+        const bool ok = vok && a[i][b] > Real(0);
+        ev[i][b] = c.es[ok ? eidx[i] + b : 0];
+        if constexpr (BF) {
+          wv[i][b] = __ldg(c.bw + (ok ? widx + b : 0));
+          sv[i][b] = c.bs[ok ? sidx + b : 0];
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < VPL; ++i) {
+      const int v = gl + G * i;
+      if (v >= g.n_theta || !live) continue;
+      const R2 gw = c.sgw[v];
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        if (a[i][b] > Real(0)) {
+          const Real pe = gw.x * a[i][b] * hh;
+          if constexpr (BF) {
+            const Real w = wv[i][b];
+            if (sv[i][b]) {
               t2 += pe * pe * w;
-              t1 += ev * pe * w;
+              t1 += ev[i][b] * pe * w;
             } else {
-              const Real qc = c.bdt / (fabs(ev) * sqrt(w));
+              const Real qc = c.bdt / (fabs(ev[i][b]) * sqrt(w));
               t2 += qc * (pe * pe * w);
-              t1 += qc * (ev * pe * w);
+              t1 += qc * (ev[i][b] * pe * w);
             }
+          } else {
+            t2 += pe * pe * gw.y;
+            t1 += ev[i][b] * pe * gw.y;
           }
         }
-      } else {
+      }
+    }
+  } else {
 #pragma unroll
-        for (int b = 0; b < NB; ++b) {
-          if (a[i][b] > Real(0)) {
-            const Real pe = gw.x * a[i][b] * hh;
-            t2 += pe * pe * gw.y;
-            t1 += row[b] * pe * gw.y;
+    for (int i = 0; i < VPL; ++i) {
+      const int v = gl + G * i;
+      if (v >= g.n_theta || !live) continue;
+      const R2 gw = c.sgw[v];
+      for (int tr = 0; tr < c.tcount; ++tr) {
+        const Real hh = c.hv[tr];
+        const Real* row = c.es + tr * c.ps + v * c.rs + jlo[i];
+        if constexpr (BF) {
+          const Real* wr = c.bw + tr * c.bw_ps + v * c.bw_rs + jlo[i];
+          const uint8_t* sr = c.bs + tr * c.bs_ps + v * c.bs_rs + jlo[i];
+#pragma unroll
+          for (int b = 0; b < NB; ++b) {
+            if (a[i][b] > Real(0)) {
+              const Real e0 = row[b];
+              const Real w = __ldg(wr + b);
+              const Real pe = gw.x * a[i][b] * hh;
+              if (sr[b]) {
+                t2 += pe * pe * w;
+                t1 += e0 * pe * w;
+              } else {
+                const Real qc = c.bdt / (fabs(e0) * sqrt(w));
+                t2 += qc * (pe * pe * w);
+                t1 += qc * (e0 * pe * w);
+              }
+            }
+          }
+        } else {
+#pragma unroll
+          for (int b = 0; b < NB; ++b) {
+            if (a[i][b] > Real(0)) {
+              const Real pe = gw.x * a[i][b] * hh;
+              t2 += pe * pe * gw.y;
+              t1 += row[b] * pe * gw.y;
+            }
           }
         }
       }
@@ -436,15 +509,6 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
     hi = hi < cand ? cand : hi;
   }
   // QGGMRF surrogate, one iteration (QGGMRF_Functions.cpp:153-206)
-  Real s1 = Real(0), s2 = Real(0);
-#pragma unroll
-  for (int i = 0; i < NNB; ++i) {
-    if (nvalid[i]) {
-      const Real tc = static_cast<Real>(c.q->f[gl + G * i]) * qggmrf_coef<Real>(*c.q, V - nb[i]);
-      s1 += tc * nb[i];
-      s2 += tc;
-    }
-  }
   s1 = group_sum<G>(s1);
   s2 = group_sum<G>(s2);
   const Real u = (s1 + theta2 * V - theta1) / (s2 + theta2);
@@ -457,28 +521,46 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
   // footprint entry even when the voxel did not change (BFForwardModel.cpp:898-932), so the
   // scatter runs then too.
   if (BF || dlt != Real(0)) {
+    if (one_row) {
+      const Real hh = c.hv[0];
 #pragma unroll
-    for (int i = 0; i < VPL; ++i) {
-      const int v = gl + G * i;
-      if (v >= g.n_theta) continue;
-      const Real gain = c.sgw[v].x;
-      for (int tr = 0; tr < c.tcount; ++tr) {
-        const Real hh = c.hv[tr];
-        Real* row = c.es + tr * c.ps + v * c.rs + jlo[i];
-        if constexpr (BF) {
-          const Real* wr = c.bw + tr * c.bw_ps + v * c.bw_rs + jlo[i];
-          uint8_t* sr = c.bs + tr * c.bs_ps + v * c.bs_rs + jlo[i];
+      for (int i = 0; i < VPL; ++i) {
+        const int v = gl + G * i;
+        if (v >= g.n_theta) continue;
+        const Real gain = c.sgw[v].x;
 #pragma unroll
-          for (int b = 0; b < NB; ++b)
-            if (a[i][b] > Real(0)) {
-              const Real ne = row[b] - gain * (a[i][b] * hh * dlt);
-              row[b] = ne;
-              sr[b] = fabs(ne * sqrt(__ldg(wr + b))) < c.bt ? 1 : 0;
-            }
-        } else {
+        for (int b = 0; b < NB; ++b)
+          if (a[i][b] > Real(0)) {
+            const Real ne = ev[i][b] - gain * (a[i][b] * hh * dlt);
+            c.es[eidx[i] + b] = ne;
+            if constexpr (BF)
+              c.bs[v * c.bs_rs + jlo[i] + b] = fabs(ne * sqrt(wv[i][b])) < c.bt ? 1 : 0;
+          }
+      }
+    } else {
 #pragma unroll
-          for (int b = 0; b < NB; ++b)
-            if (a[i][b] > Real(0)) row[b] -= gain * (a[i][b] * hh * dlt);
+      for (int i = 0; i < VPL; ++i) {
+        const int v = gl + G * i;
+        if (v >= g.n_theta) continue;
+        const Real gain = c.sgw[v].x;
+        for (int tr = 0; tr < c.tcount; ++tr) {
+          const Real hh = c.hv[tr];
+          Real* row = c.es + tr * c.ps + v * c.rs + jlo[i];
+          if constexpr (BF) {
+            const Real* wr = c.bw + tr * c.bw_ps + v * c.bw_rs + jlo[i];
+            uint8_t* sr = c.bs + tr * c.bs_ps + v * c.bs_rs + jlo[i];
+#pragma unroll
+            for (int b = 0; b < NB; ++b)
+              if (a[i][b] > Real(0)) {
+                const Real ne = row[b] - gain * (a[i][b] * hh * dlt);
+                row[b] = ne;
+                sr[b] = fabs(ne * sqrt(__ldg(wr + b))) < c.bt ? 1 : 0;
+              }
+          } else {
+#pragma unroll
+            for (int b = 0; b < NB; ++b)
+              if (a[i][b] > Real(0)) row[b] -= gain * (a[i][b] * hh * dlt);
+          }
         }
       }
     }
@@ -713,49 +795,62 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
     const int z = A.row_order[rr];
     __syncthreads();
     compute_row_base<Real>(A.tab, g.n_theta, z, rb, tid, nthreads);
-    // neighbour rows (y+dy, z+dz), dy, dz in {-1,0,1}; rows outside the volume read as 0
-    for (int i = tid; i < 9 * g.n_x; i += nthreads) {
-      const int r = i / g.n_x, xx = i - r * g.n_x;
-      const int yy = y + r / 3 - 1, zz = z + r % 3 - 1;
-      Real v = Real(0);
-      if (yy >= 0 && yy < g.n_y && zz >= 0 && zz < g.n_z) {
-        const Real* src = gx + static_cast<size_t>(yy) * vplane + static_cast<size_t>(zz) * g.n_x + xx;
-        v = coherent ? __ldcg(src) : *src;
-      }
-      cache[i] = v;
-    }
+    // neighbour rows (y+dy, z+dz), dy, dz in {-1,0,1} (rows outside the volume read as 0),
+    // loaded column by column: each thread also records whether its column holds a value > 0
+    // (bit 2 of lv), from which the zero-skipping test of every voxel follows
     for (int x = tid; x < g.n_x; x += nthreads) {
+      bool pos = false;
+#pragma unroll
+      for (int r = 0; r < 9; ++r) {
+        const int yy = y + r / 3 - 1, zz = z + r % 3 - 1;
+        Real v = Real(0);
+        if (yy >= 0 && yy < g.n_y && zz >= 0 && zz < g.n_z) {
+          const Real* src = gx + static_cast<size_t>(yy) * vplane + static_cast<size_t>(zz) * g.n_x + x;
+          v = coherent ? __ldcg(src) : *src;
+        }
+        cache[r * g.n_x + x] = v;
+        pos |= v > Real(0);
+      }
       const size_t l = static_cast<size_t>(z) * g.n_x + x;
       okr[x] = (A.tab.lineok[l] && (active_lines == nullptr || active_lines[l])) ? 1 : 0;
+      lv[x] = pos ? 4 : 0;
     }
     __syncthreads();
-    // liveness at the start of the row: projection needs V != 0; ICD voxels that would be
-    // zero-skipped now are not live
-    for (int x = tid; x < g.n_x; x += nthreads) {
-      uint8_t f = 0;
-      if (okr[x]) {
+    // liveness at the start of the row (bit 0): projection needs V != 0; an ICD voxel that would
+    // be zero-skipped now (V == 0, no neighbour > 0) is not live.  A voxel skipped at the start
+    // of its row can still be updated if a same-row neighbour processed before it became
+    // positive: within a stride period [mS, mS+S) classes run left to right, so reachability
+    // is the period's prefix-OR, and the period's last voxel also follows the next period's
+    // first one.  Bit 1 marks the candidates.  One thread per period.
+    int any_cand = 0;
+    for (int m = tid; m * S < g.n_x; m += nthreads) {
+      const int x0 = m * S;
+      const int x1 = min(x0 + S, g.n_x);
+      auto live_at = [&](int x) -> int {
+        if (!okr[x]) return 0;
         const Real V = cache[4 * g.n_x + x];
-        f = project ? (V != Real(0)) : !zero_skipped(c, x, V);
+        if (project) return V != Real(0);
+        if (!zs_on || V != Real(0)) return 1;
+        const bool nbpos = (lv[x] & 4) || (x > 0 && (lv[x - 1] & 4)) ||
+                           (x + 1 < g.n_x && (lv[x + 1] & 4));
+        return nbpos ? 1 : 0;
+      };
+      int a = 0;
+      for (int x = x0; x < x1; ++x) {
+        const int l0 = live_at(x);
+        a |= l0;
+        int cand = zs_on ? a : l0;
+        if (zs_on && x == x0 + S - 1 && x + 1 < g.n_x) cand |= live_at(x + 1);
+        cand &= okr[x];
+        any_cand |= cand;
+        lv[x] = static_cast<uint8_t>((lv[x] & 4) | l0 | (cand << 1));
       }
-      lv[x] = f;
     }
-    __syncthreads();
-    // A voxel skipped at the start of its row can still be updated if a same-row neighbour that
-    // is processed before it became positive: within a stride period [mS, mS+S) classes run
-    // left to right, so reachability is the period's prefix-OR; the period's last voxel also
-    // follows the next period's first one.  Bit 1 marks the candidates.
-    if (zs_on) {
-      for (int m = tid; m * S < g.n_x; m += nthreads) {
-        uint8_t a = 0;
-        const int x0 = m * S;
-        for (int j = 0; j < S && x0 + j < g.n_x; ++j) {
-          a |= lv[x0 + j] & 1;
-          uint8_t b = a;
-          if (j == S - 1 && x0 + S < g.n_x) b |= lv[x0 + S] & 1;
-          lv[x0 + j] = static_cast<uint8_t>((lv[x0 + j] & 1) | (b << 1));
-        }
-      }
-      __syncthreads();
+    if (!__syncthreads_or(any_cand)) {
+      // nothing in this row can be updated: count its listed voxels as skipped
+      if (!project)
+        for (int x = tid; x < g.n_x; x += nthreads) skipped += okr[x];
+      continue;
     }
     // compaction: warp w lists the candidates of classes w, w + warps, ... in ascending x
     for (int k = warp; k < S; k += nthreads / 32) {
@@ -764,7 +859,7 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
         const int x = k + S * (m0 + lane);
         bool cand = false;
         if (x < g.n_x && okr[x]) {
-          cand = zs_on ? ((lv[x] >> 1) & 1) != 0 : (lv[x] & 1) != 0;
+          cand = ((lv[x] >> 1) & 1) != 0;
           if (!cand && !project) ++skipped;
         }
         const unsigned b = __ballot_sync(kFull, cand);
@@ -832,8 +927,9 @@ __device__ __forceinline__ void init_slice_barrier(unsigned char* smem) {
 template <typename Real, int NB, int G, int VPL, bool STAGE, bool BF>
 __global__ void __launch_bounds__(kWarps * 32, 1) sweep_kernel(SweepArgs A) {
   extern __shared__ __align__(128) unsigned char smem[];
-  const int y = A.colour + 2 * static_cast<int>(blockIdx.x);
-  if (y >= A.g.n_y) return;
+  // slab launches (y_end > 0) start at y_first; whole-volume launches at the colour
+  const int y = (A.y_end > 0 ? A.y_first : A.colour) + 2 * static_cast<int>(blockIdx.x);
+  if (y >= (A.y_end > 0 ? A.y_end : A.g.n_y)) return;
   init_slice_barrier(smem);
   uint32_t phase = 0;
   run_slice<Real, NB, G, VPL, STAGE, BF>(
@@ -1051,16 +1147,21 @@ int launch_ref_t(const RefOrderArgs& a, cudaStream_t s) {
 // the instantiation.
 template <bool STAGE, bool BF>
 int launch_sweep_f32_pick(const SweepArgs& a, int nb, size_t smem, cudaStream_t s) {
-  const int shape = lane_shape(a.g.n_theta);
+  // explicit shape (1..4) when it covers the views, else the default for the view count
+  int shape = a.shape;
+  if (shape < 1 || shape > 4 || a.g.n_theta > shape_max_views(shape))
+    shape = 1 + (lane_shape(a.g.n_theta) == 0 ? 0 : lane_shape(a.g.n_theta) + 1);
   if (nb == 9) return launch_sweep_t<float, 9, 32, 5, STAGE, BF>(a, smem, s);
   if (nb == 3) {
-    if (shape == 0) return launch_sweep_t<float, 3, 16, 4, STAGE, BF>(a, smem, s);
-    if (shape == 1) return launch_sweep_t<float, 3, 32, 3, STAGE, BF>(a, smem, s);
+    if (shape == 1) return launch_sweep_t<float, 3, 16, 4, STAGE, BF>(a, smem, s);
+    if (shape == 2) return launch_sweep_t<float, 3, 32, 2, STAGE, BF>(a, smem, s);
+    if (shape == 3) return launch_sweep_t<float, 3, 32, 3, STAGE, BF>(a, smem, s);
     return launch_sweep_t<float, 3, 32, 5, STAGE, BF>(a, smem, s);
   }
   if (nb == 5) {
-    if (shape == 0) return launch_sweep_t<float, 5, 16, 4, STAGE, BF>(a, smem, s);
-    if (shape == 1) return launch_sweep_t<float, 5, 32, 3, STAGE, BF>(a, smem, s);
+    if (shape == 1) return launch_sweep_t<float, 5, 16, 4, STAGE, BF>(a, smem, s);
+    if (shape == 2) return launch_sweep_t<float, 5, 32, 2, STAGE, BF>(a, smem, s);
+    if (shape == 3) return launch_sweep_t<float, 5, 32, 3, STAGE, BF>(a, smem, s);
     return launch_sweep_t<float, 5, 32, 5, STAGE, BF>(a, smem, s);
   }
   return -7;

@@ -82,6 +82,7 @@ class MbirParams(C.Structure):
         ("verbose", C.c_int32),
         ("slice_staging", C.c_int32),
         ("nhicd", C.c_int32),
+        ("lane_shape", C.c_int32),
     ]
 
 
@@ -91,7 +92,7 @@ class MbirStatus(C.Structure):
         ("sweeps_done", C.c_int32), ("last_cost", C.c_double), ("last_rel_update", C.c_double),
         ("icd_ms_total", C.c_double), ("total_ms", C.c_double), ("voxels_visited", C.c_int64),
         ("voxels_updated", C.c_int64), ("footprint_entries", C.c_int64), ("t_rows", C.c_int32),
-        ("stride", C.c_int32), ("staged", C.c_int32), ("reserved", C.c_int32),
+        ("stride", C.c_int32), ("staged", C.c_int32), ("lane_shape", C.c_int32),
     ]
 
 
@@ -142,6 +143,12 @@ SIGNATURES = {
                                                  C.c_void_p, C.c_void_p]),
     "mbir_get_bf_state": (C.c_int32, [C.c_void_p, C.POINTER(C.c_uint8), _F, _D, _D, _D]),
     "mbir_set_bragg_threshold": (C.c_int32, [C.c_void_p, C.c_double]),
+    "mbir_set_slab": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32]),
+    "mbir_sweep_colour": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _D]),
+    "mbir_get_planes": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, _F]),
+    "mbir_set_planes": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, _F]),
+    "mbir_view_sums": (C.c_int32, [C.c_void_p, C.c_int32, _D]),
+    "mbir_apply_nuisance": (C.c_int32, [C.c_void_p, _D, _D, _D]),
     "mbir_status_get": (C.c_int32, [C.c_void_p, C.POINTER(MbirStatus)]),
     "mbir_cancel": (None, [C.c_void_p]),
     "mbir_write_outputs": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_char_p]),
@@ -347,6 +354,42 @@ class Engine:
                                             w.ctypes.data_as(_F), mag.ctypes.data_as(_D),
                                             filt.ctypes.data_as(_D), C.byref(t)))
         return sel, w, mag, filt, t.value
+
+    # ---- y-slab sharding -----------------------------------------------------------------
+    def set_slab(self, y0, y1):
+        self._check(lib().mbir_set_slab(self._h, y0, y1))
+
+    def sweep_colour(self, colour, outer=0, inner=0):
+        st = np.zeros(4)
+        self._check(lib().mbir_sweep_colour(self._h, colour, outer, inner, st.ctypes.data_as(_D)))
+        return st
+
+    def get_planes(self, y, n):
+        nz, nx = self.dims()[:2]
+        out = np.zeros((n, nz, nx), np.float32)
+        self._check(lib().mbir_get_planes(self._h, y, n, out.ctypes.data_as(_F)))
+        return out
+
+    def set_planes(self, y, planes):
+        planes = np.ascontiguousarray(planes, np.float32)
+        self._check(lib().mbir_set_planes(self._h, y, planes.shape[0], planes.ctypes.data_as(_F)))
+
+    def view_sums(self, kind):
+        nt = self.dims()[3]
+        out = np.zeros(nt * (6 if kind == 0 else 1))
+        self._check(lib().mbir_view_sums(self._h, kind, out.ctypes.data_as(_D)))
+        return out
+
+    def apply_nuisance(self, gain=None, offset=None, variance=None):
+        def ptr(a):
+            return None if a is None else np.ascontiguousarray(a, np.float64).ctypes.data_as(_D)
+        g = None if gain is None else np.ascontiguousarray(gain, np.float64)
+        o = None if offset is None else np.ascontiguousarray(offset, np.float64)
+        v = None if variance is None else np.ascontiguousarray(variance, np.float64)
+        self._check(lib().mbir_apply_nuisance(
+            self._h, g.ctypes.data_as(_D) if g is not None else None,
+            o.ctypes.data_as(_D) if o is not None else None,
+            v.ctypes.data_as(_D) if v is not None else None))
 
     def set_bragg(self, t):
         self._check(lib().mbir_set_bragg_threshold(self._h, float(t)))

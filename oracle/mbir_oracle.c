@@ -1605,3 +1605,70 @@ void orc_bf_sweep_lines_mt(orc_ctx* c, const int32_t* lines, int n_lines, int ou
   free(th);
   free(ycount);
 }
+
+/* =========================================================================================
+ * y-slab sharding support (test infrastructure for the multi-rank driver): one colour phase of
+ * the slice-order sweep restricted to slices y in [y0, y1), per-view sums over a detector-row
+ * range, and the nuisance update with the error rebuild of jointEstimation.
+ * ========================================================================================= */
+void orc_icd_sweep_colour(orc_ctx* c, const int32_t* row_order, int stride, int colour, int y0,
+                          int y1, int outer, int inner, double* stats) {
+  stats[0] = stats[1] = stats[2] = stats[3] = 0;
+  for (int i = y0; i < y1; i++) {
+    if ((i & 1) != colour) continue;
+    for (int rr = 0; rr < c->n_z; rr++) {
+      int z = row_order[rr];
+      for (int k = 0; k < stride; k++)
+        for (int x = k; x < c->n_x; x += stride)
+          if (c->col_count[z * c->n_x + x] > 0)
+            update_voxel(c, z, x, i, outer, inner, stats, c->mag_map);
+    }
+  }
+}
+
+/* kind 0: the six sums of jointEstimation per view ([theta][6]: y w, w, yh w, yh w y, y^2 w,
+ * yh^2 w with yh = (y - e - mu)/I); kind 1: sum e^2 per view.  Rows t in [t0, t1). */
+void orc_view_sums(const orc_ctx* c, int kind, int t0, int t1, double* out) {
+  for (int th = 0; th < c->n_theta; th++) {
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = t0; t < t1; t++) {
+        double ev = S3(c, e, th, r, t);
+        if (kind == 1) {
+          s[0] += ev * ev;
+        } else {
+          double y = S3(c, counts, th, r, t), w = S3(c, w, th, r, t);
+          double yh = (y - ev - c->mu[th]) / c->I[th];
+          s[0] += (y * w);
+          s[1] += (w);
+          s[2] += (yh * w);
+          s[3] += (yh * w * y);
+          s[4] += (y * y * w);
+          s[5] += (yh * yh * w);
+        }
+      }
+    if (kind == 1)
+      out[th] = s[0];
+    else
+      for (int k = 0; k < 6; k++) out[th * 6 + k] = s[k];
+  }
+}
+
+/* new gain/offset (and variance) per view; e = y - mu' - I' yh, yh = (y - e - mu)/I
+ * (HAADF_ReconstructionEngine_Extra.cpp:600-612); weights 1/alpha (identity noise model) */
+void orc_apply_nuisance(orc_ctx* c, const double* gain, const double* offset,
+                        const double* variance) {
+  for (int th = 0; th < c->n_theta; th++)
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = 0; t < c->n_t; t++) {
+        double yv = S3(c, counts, th, r, t);
+        double yh = (yv - S3(c, e, th, r, t) - c->mu[th]) / c->I[th];
+        S3(c, e, th, r, t) = yv - offset[th] - (gain[th] * yh);
+        if (variance) S3(c, w, th, r, t) = 1.0 / variance[th];
+      }
+  for (int th = 0; th < c->n_theta; th++) {
+    c->I[th] = gain[th];
+    c->mu[th] = offset[th];
+    if (variance) c->alpha[th] = variance[th];
+  }
+}

@@ -148,6 +148,14 @@ double orc_bf_cost(const orc_ctx* c, double* parts);
 /* BFReconstructionEngine::execute loops in reference (list) order with lists drawn from
  * `seed`; runs at most max_calls updateVoxels calls (<= 0: no limit); returns the calls run */
 int orc_bf_run(orc_ctx* c, uint32_t seed, int max_calls);
+/* y-slab sharding: one colour of the slice-order sweep over slices [y0, y1); per-view sums over
+ * detector rows [t0, t1) (kind 0: [theta][6] jointEstimation sums, kind 1: [theta] sum e^2);
+ * nuisance update with the jointEstimation error rebuild (variance may be null) */
+void orc_icd_sweep_colour(orc_ctx* c, const int32_t* row_order, int stride, int colour, int y0,
+                          int y1, int outer, int inner, double* stats);
+void orc_view_sums(const orc_ctx* c, int kind, int t0, int t1, double* out);
+void orc_apply_nuisance(orc_ctx* c, const double* gain, const double* offset,
+                        const double* variance);
 /* one call with the reference's worker split over y (timing of the reference CPU path) */
 void orc_bf_sweep_lines_mt(orc_ctx* c, const int32_t* lines, int n_lines, int outer, int inner,
                            int n_threads, double* stats);

@@ -99,6 +99,10 @@ def lib():
             "orc_bf_update_selector": (None, [C.c_void_p]),
             "orc_bf_cost": (C.c_double, [C.c_void_p, _D]),
             "orc_bf_run": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int]),
+            "orc_icd_sweep_colour": (None, [C.c_void_p, _I, C.c_int, C.c_int, C.c_int, C.c_int,
+                                            C.c_int, C.c_int, _D]),
+            "orc_view_sums": (None, [C.c_void_p, C.c_int, C.c_int, C.c_int, _D]),
+            "orc_apply_nuisance": (None, [C.c_void_p, _D, _D, _D]),
             "orc_bf_sweep_lines_mt": (None, [C.c_void_p, _I, C.c_int, C.c_int, C.c_int, C.c_int,
                                              _D]),
         }
@@ -286,6 +290,26 @@ class Oracle:
         parts = np.zeros(3)
         c = lib().orc_cost(self._h, parts.ctypes.data_as(_D))
         return c, parts
+
+    # ---- y-slab sharding ---------------------------------------------------------------------
+    def sweep_colour(self, row_order, stride, colour, y0, y1, outer=0, inner=0):
+        rows = np.ascontiguousarray(row_order, np.int32)
+        st = np.zeros(4)
+        lib().orc_icd_sweep_colour(self._h, rows.ctypes.data_as(_I), stride, colour, y0, y1,
+                                   outer, inner, st.ctypes.data_as(_D))
+        return st
+
+    def view_sums(self, kind, t0, t1):
+        out = np.zeros(self.shape[0] * (6 if kind == 0 else 1))
+        lib().orc_view_sums(self._h, kind, t0, t1, out.ctypes.data_as(_D))
+        return out
+
+    def apply_nuisance(self, gain, offset, variance=None):
+        g = np.ascontiguousarray(gain, np.float64)
+        o = np.ascontiguousarray(offset, np.float64)
+        v = np.ascontiguousarray(variance, np.float64) if variance is not None else None
+        lib().orc_apply_nuisance(self._h, g.ctypes.data_as(_D), o.ctypes.data_as(_D),
+                                 v.ctypes.data_as(_D) if v is not None else None)
 
     # ---- bright field ---------------------------------------------------------------------
     def selector(self):

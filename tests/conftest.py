@@ -67,6 +67,7 @@ def haadf_params(mbir, thickness, **kw):
     p.outer_iterations = 5
     p.inner_iterations = 1
     p.stop_threshold = 0.0
+    p.lane_shape = 1  # fixed voxel-group shape: engines compared bit for bit must agree
     for k, v in kw.items():
         setattr(p, k, v)
     return p
@@ -96,6 +97,7 @@ def bf_params(mbir, thickness, **kw):
     p.use_default_offset = 1
     p.default_dosage = 1.0e4
     p.bragg_threshold = 3.0
+    p.lane_shape = 1
     for k, v in kw.items():
         setattr(p, k, v)
     return p

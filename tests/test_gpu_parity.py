@@ -352,3 +352,31 @@ def test_reference_exact_mode_bitwise(lib_built, oracle_mod):
     np.testing.assert_array_equal(g, o.gain())
     np.testing.assert_array_equal(off, o.offset())
     np.testing.assert_array_equal(var, o.variance())
+
+
+@pytest.mark.parametrize("shape", [1, 2])
+def test_lane_shapes_match_oracle(lib_built, oracle_mod, shape):
+    """Both voxel-group shapes for <= 64 views (16 lanes x 4 views, 32 lanes x 2 views)."""
+    e, o, p, y = pair(lib_built, oracle_mod, lane_shape=shape)
+    e.prepare()
+    assert e.status().lane_shape == shape
+    o.prepare()
+    rows, stride = e.schedule(0)
+    sg = e.sweep(0, 0)
+    so = o.sweep_slices(rows, stride, 0, 0)
+    assert sg[3] == so[3]
+    assert rel(e.volume(), o.volume()) <= 1e-5
+
+
+def test_autotuned_shape_is_valid_and_restores_state(lib_built, oracle_mod):
+    """lane_shape = 0: trial passes on a snapshot choose the shape; the state after prepare is
+    the untouched initial state (the first sweep still matches the oracle)."""
+    e, o, p, y = pair(lib_built, oracle_mod, lane_shape=0)
+    e.prepare()
+    assert e.status().lane_shape in (1, 2)
+    o.prepare()
+    assert rel(e.error_sinogram(), o.error()) <= 1e-5
+    rows, stride = e.schedule(0)
+    e.sweep(0, 0)
+    o.sweep_slices(rows, stride, 0, 0)
+    assert rel(e.volume(), o.volume()) <= 1e-5
