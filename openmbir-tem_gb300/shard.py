@@ -1,0 +1,152 @@
+"""y-slab sharding of one HAADF reconstruction over ranks (one GPU per rank).
+
+Voxel slice y touches only its own detector rows, so contiguous slabs of slices own disjoint
+blocks of the error sinogram and the ICD sweep needs no sinogram exchange.  The prior couples
+neighbouring slices: after each colour phase (red/black in y) every rank publishes its two
+boundary planes and takes its neighbours' planes as read-only halos.  The per-view sums of the
+gain/offset estimate (jointEstimation, HAADF_ReconstructionEngine_Extra.cpp:419-636) and of the
+variance estimate (updateWeights, :795-881) are summed over ranks, solved on the host and
+applied by every rank.  This is the reference's y-range task split of updateVoxels
+(HAADF_ReconstructionEngine_UpdateVoxels.cpp:666-723) across devices instead of threads, with
+the same result as one engine running the whole volume (the colour order makes the slabs
+independent within a phase).
+
+Communication goes through torch.distributed on host tensors (gloo): planes and sums are small
+(one N_z x N_x plane per neighbour, 6 N_theta doubles) and are exchanged between kernel launches,
+so no kernel ever waits on another rank.
+
+Backends: `EngineBackend` (the engine's C ABI, one GPU per rank) and, for tests on CPU ranks,
+any object with the same methods (tests use the FP64 oracle).
+"""
+import numpy as np
+
+
+def slabs(n_y, world):
+    """Contiguous slabs [y0, y1) per rank; sizes differ by at most one slice."""
+    counts = [n_y // world + (1 if r < n_y % world else 0) for r in range(world)]
+    out, y = [], 0
+    for c in counts:
+        out.append((y, y + c))
+        y += c
+    return out
+
+
+def solve_gain_offset(sums, target_gain):
+    """The Lagrange solve of jointEstimation (HAADF_ReconstructionEngine_Extra.cpp:521-598) from
+    the six per-view sums [theta][6] = (y w, w, yh w, yh w y, y^2 w, yh^2 w); mean gain fixed to
+    target_gain.  Same operations in the same order as the engine's host solve."""
+    s = np.asarray(sums, np.float64).reshape(-1, 6)
+    nt = s.shape[0]
+    q0, q1, b0 = s[:, 5], s[:, 2], s[:, 3]
+    d1 = [s[v, 0] / s[v, 1] for v in range(nt)]
+    d2 = [s[v, 2] / s[v, 1] for v in range(nt)]
+    sum1 = 0.0
+    sum2 = 0.0
+    for v in range(nt):
+        sum1 += (1.0 / (q0[v] - q1[v] * d2[v]))
+        sum2 += ((b0[v] - q1[v] * d1[v]) / (q0[v] - q1[v] * d2[v]))
+    lm = (-nt * target_gain + sum2) / sum1
+    gain = np.empty(nt)
+    offset = np.empty(nt)
+    for v in range(nt):
+        gain[v] = (-1 * lm - q1[v] * d1[v] + b0[v]) / (q0[v] - q1[v] * d2[v])
+        offset[v] = d1[v] - d2[v] * gain[v]
+    return gain, offset
+
+
+class EngineBackend:
+    """One rank's engine (C ABI).  The engine holds the whole problem; only its slab is swept
+    and summed."""
+
+    def __init__(self, engine):
+        self.e = engine
+
+    def dims(self):
+        return self.e.dims()
+
+    def set_slab(self, y0, y1):
+        self.e.set_slab(y0, y1)
+
+    def sweep_colour(self, colour, outer, inner):
+        return self.e.sweep_colour(colour, outer, inner)
+
+    def get_planes(self, y, n):
+        return self.e.get_planes(y, n)
+
+    def set_planes(self, y, planes):
+        self.e.set_planes(y, planes)
+
+    def view_sums(self, kind):
+        return self.e.view_sums(kind)
+
+    def apply_nuisance(self, gain=None, offset=None, variance=None):
+        self.e.apply_nuisance(gain, offset, variance)
+
+
+def _exchange(dist, backend, y0, y1, n_y, nz, nx):
+    """Every rank publishes its first and last plane; ranks take their neighbours' planes."""
+    import torch
+    world = dist.get_world_size()
+    rank = dist.get_rank()
+    dtype = getattr(backend, "plane_dtype", np.float32)
+    mine = np.zeros((2, nz, nx), dtype)
+    if y1 > y0:
+        mine[0] = backend.get_planes(y0, 1)[0]
+        mine[1] = backend.get_planes(y1 - 1, 1)[0]
+    out = [torch.zeros((2, nz, nx), dtype=torch.from_numpy(mine).dtype) for _ in range(world)]
+    dist.all_gather(out, torch.from_numpy(mine))
+    bounds = slabs(n_y, world)
+    if rank > 0 and y0 > 0:
+        left = out[rank - 1].numpy()
+        if bounds[rank - 1][1] == y0:
+            backend.set_planes(y0 - 1, left[1:2])
+    if rank + 1 < world and y1 < n_y:
+        right = out[rank + 1].numpy()
+        if bounds[rank + 1][0] == y1:
+            backend.set_planes(y1, right[0:1])
+
+
+def _allreduce(dist, arr):
+    import torch
+    t = torch.from_numpy(np.ascontiguousarray(arr, np.float64))
+    dist.all_reduce(t)
+    return t.numpy().copy()
+
+
+def run_sharded(dist, backend, n_outer, target_gain=1.0, joint_estimation=True,
+                noise_model=True):
+    """Outer iterations of the parallel-order reconstruction on this rank's slab: per outer
+    iteration one sweep (colour 0, halo exchange, colour 1, halo exchange), then the gain/offset
+    and variance updates from sums over all ranks.  Returns the rank's (y0, y1) and the summed
+    sweep statistics (sum |dx|, sum |x| over the ROI, zero-skipped, updated) per sweep."""
+    nz, nx, n_y, n_theta, n_r, n_t = backend.dims()
+    world = dist.get_world_size()
+    rank = dist.get_rank()
+    y0, y1 = slabs(n_y, world)[rank]
+    backend.set_slab(y0, y1)
+    history = []
+    for outer in range(n_outer):
+        st = np.zeros(4)
+        for colour in (0, 1):
+            st += backend.sweep_colour(colour, outer, 0)
+            _exchange(dist, backend, y0, y1, n_y, nz, nx)
+        history.append(_allreduce(dist, st))
+        if joint_estimation:
+            gain, offset = solve_gain_offset(_allreduce(dist, backend.view_sums(0)), target_gain)
+            backend.apply_nuisance(gain, offset, None)
+        if noise_model:
+            var = _allreduce(dist, backend.view_sums(1)) / (n_r * n_t)
+            backend.apply_nuisance(None, None, var)
+    return (y0, y1), history
+
+
+def gather_volume(dist, backend, y0, y1):
+    """The full volume [z][x][y] on every rank, assembled from the ranks' slabs."""
+    import torch
+    nz, nx, n_y = backend.dims()[:3]
+    mine = np.zeros((n_y, nz, nx), np.float32)
+    if y1 > y0:
+        mine[y0:y1] = backend.get_planes(y0, y1 - y0)
+    t = torch.from_numpy(mine)
+    dist.all_reduce(t)
+    return t.numpy().transpose(1, 2, 0).copy()
