@@ -210,18 +210,182 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+# ---- batched and served forms ------------------------------------------------------------
+def uneven_series(n, seed=0, large_frac=0.0, bf_frac=0.0):
+    """n tilt series with the uneven sizes of the batched workload: N_x in U{128..512},
+    N_y (detector rows) in U{16..256}, N_z in U{32..128}, views in U{41..141} over +-60..70 deg;
+    a fraction `large_frac` takes the 512x256x128 / 61-view shape, `bf_frac` are bright field.
+    Random ellipsoid phantoms, seeded noise.  Returns [(modality, counts, angles, thickness)]."""
+    import synthetic
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        if rng.uniform() < large_frac:
+            n_r, n_t, n_z, views, mx = 512, 256, 128, 61, 60.0
+        else:
+            n_r = int(rng.integers(128, 513))
+            n_t = int(rng.integers(16, 257))
+            n_z = int(rng.integers(32, 129))
+            views = int(rng.integers(41, 142))
+            mx = float(rng.uniform(60.0, 70.0))
+        th = n_z / 2.0
+        ang = np.linspace(-mx, mx, views)
+        shapes = synthetic.random_ellipsoids(6, n_r, n_t, n_z, seed=int(rng.integers(1 << 30)),
+                                             axes=(3.0, min(15.0, n_z / 4)))
+        proj = np.zeros((views, n_r, n_t))
+        t = -n_t / 2 + np.arange(n_t) + 0.5
+        for sh in shapes:  # each ellipsoid projected onto the detector rows it covers
+            rows = np.nonzero(np.abs(t - sh[1]) < sh[4])[0]
+            if len(rows) == 0:
+                continue
+            lo, hi = rows[0], rows[-1] + 1
+            off = -n_t / 2 + lo + (hi - lo) / 2
+            sub = (sh[0], sh[1] - off, sh[2], sh[3], sh[4], sh[5], sh[6])
+            proj[:, :, lo:hi] += synthetic.ellipsoid_projection(ang, n_r, hi - lo, [sub])
+        if rng.uniform() < bf_frac:
+            y, _ = synthetic.bf_counts(proj, seed=k)
+            out.append(("BF", y, ang.astype(np.float32), th))
+        else:
+            y, _ = synthetic.haadf_measurements(proj, seed=k)
+            out.append(("HAADF", y, ang.astype(np.float32), th))
+    return out
+
+
+def run_batch(args):
+    """Time to a 1e-4 relative cost tolerance for 64 uneven HAADF reconstructions: one at a time
+    through the step-wise C ABI (sweep, gain/offset, variance, cost per outer iteration) against
+    all of them advancing together in one persistent launch per sweep (mbir_batch_run)."""
+    import torch
+    import build as pkg_build
+    pkg_build.build()
+    import mbir
+    torch.cuda.set_device(0)
+    n = args.series
+    data = uneven_series(n, seed=1)
+    tol, max_outer = 1e-4, 60
+
+    def engine(item):
+        mod, y, ang, th = item
+        p = params_for(mbir, th, mod, outer=max_outer)
+        p.lane_shape = 4 if y.shape[0] > 96 else (3 if y.shape[0] > 64 else 1)
+        e = mbir.Engine(p)
+        e.set_sinogram(y, ang)
+        e.prepare()
+        return e
+
+    # one at a time
+    seq_s, seq_upd, seq_iters = 0.0, 0.0, []
+    for item in data:
+        with engine(item) as e:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            prev = None
+            for it in range(max_outer):
+                e.sweep(it, 0)
+                e.joint_estimation()
+                e.update_weights()
+                c = e.cost()[0]
+                if prev is not None and abs(c - prev) <= tol * abs(c):
+                    break
+                prev = c
+            seq_s += time.perf_counter() - t0
+            seq_iters.append(it + 1)
+            seq_upd += e.status().voxels_updated
+    # all together
+    engines = [engine(item) for item in data]
+    with mbir.Batch(0) as b:
+        for e in engines:
+            b.add(e)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        iters, _ = b.run(max_outer, tol)
+        bat_s = time.perf_counter() - t0
+        bat_upd = sum(e.status().voxels_updated for e in engines)
+    for e in engines:
+        e.close()
+    vox = sum(int(np.prod([d[1].shape[1], d[1].shape[2], 2 * d[3]])) for d in data)
+    line = {"metric": "batched time-to-tolerance speed-up vs one-at-a-time GPU path",
+            "value": seq_s / bat_s, "unit": "x", "higher_is_better": True, "n_gpus": 1,
+            "data": "synthetic",
+            "config": {"workload": "batch-64-uneven-haadf", "series": n, "voxels_total": vox,
+                       "tolerance": tol, "max_outer": max_outer},
+            "sequential": {"wall_s": seq_s, "voxel_updates": seq_upd,
+                           "voxel_updates_per_s": seq_upd / seq_s,
+                           "outer_iterations": int(np.sum(seq_iters))},
+            "batched": {"wall_s": bat_s, "voxel_updates": bat_upd,
+                        "voxel_updates_per_s": bat_upd / bat_s,
+                        "outer_iterations": int(np.sum(iters))}}
+    print(json.dumps(line))
+
+
+def run_serve(args):
+    """Served stream: Poisson arrivals (mean 20 requests/s) of mixed HAADF/BF requests from the
+    uneven size distribution plus 5% of the 512x256x128 / 61-view shape, each to a 1e-4 relative
+    cost tolerance; p50/p99 latency and throughput, against the same requests served one at a
+    time."""
+    import torch
+    import build as pkg_build
+    pkg_build.build()
+    import mbir
+    torch.cuda.set_device(0)
+    n = args.series
+    data = uneven_series(n, seed=2, large_frac=0.05, bf_frac=0.3)
+    rng = np.random.default_rng(3)
+    gaps = rng.exponential(1.0 / 20.0, n)
+
+    def submit_all(server):
+        ids = []
+        t0 = time.perf_counter()
+        for item, gap in zip(data, gaps):
+            mod, y, ang, th = item
+            p = params_for(mbir, th, mod, outer=200)
+            ids.append(server.submit(p, y, ang, max_outer=200 if mod == "BF" else 60, tol=1e-4))
+            time.sleep(gap)
+        for rid in ids:
+            server.wait(rid, timeout=3600)
+        return time.perf_counter() - t0
+
+    with mbir.Server(0, 0, 0) as s:
+        wall = submit_all(s)
+        st = s.stats()
+        served = {"wall_s": wall, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms,
+                  "mean_ms": st.mean_ms, "completed": st.completed, "failed": st.failed,
+                  "peak_active": st.peak_active, "requests_per_s": st.completed / wall,
+                  "voxel_updates_per_s": st.voxel_updates / wall}
+    with mbir.Server(0, 0, 1) as s:
+        wall1 = submit_all(s)
+        st = s.stats()
+        single = {"wall_s": wall1, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms,
+                  "requests_per_s": st.completed / wall1}
+    line = {"metric": "served p50/p99 request latency and throughput", "value": served["p99_ms"],
+            "unit": "ms (p99)", "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": "serve-poisson-20rps", "requests": n, "bf_fraction": 0.3,
+                       "large_fraction": 0.05, "tolerance": 1e-4},
+            "continuous_batching": served, "one_at_a_time": single,
+            "throughput_ratio": served["requests_per_s"] / max(single["requests_per_s"], 1e-12)}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
+                    choices=sorted(WORKLOADS) + ["batch-64", "serve-poisson"])
+    ap.add_argument("--series", type=int, default=64, help="batch/serve: number of requests")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "batch-64":
+        run_batch(args)
+        return
+    if args.workload == "serve-poisson":
+        run_serve(args)
         return
 
     import torch

@@ -214,11 +214,18 @@ int Batch::run(int max_outer, double tol, int* outer_done, double* final_cost) {
     for (size_t k = 0; k < cur.size(); k++) {
       Engine* e = cur[k];
       const int i = idx[k];
-      if (e->params().joint_estimation && (rc = e->joint_estimation())) return fail(rc, e->last_error());
-      if (e->params().noise_model && (rc = e->update_weights())) return fail(rc, e->last_error());
-      if ((rc = e->compute_cost(nullptr, &cost[i]))) return fail(rc, e->last_error());
+      const mbir_params& p = e->params();
+      const bool bf = p.modality == MBIR_MODALITY_BF;
+      if (p.joint_estimation && (rc = e->joint_estimation())) return fail(rc, e->last_error());
+      if ((bf ? p.noise_estimation : p.noise_model) && (rc = e->update_weights()))
+        return fail(rc, e->last_error());
       done_at[i] = it + 1;
-      if (it > 0 && std::fabs(cost[i] - prev[i]) <= tol * std::fabs(cost[i])) active[i] = 0;
+      // bright field: one NHICD call per outer iteration, the cost compared once per
+      // equivalent iteration (20 calls)
+      const int period = bf ? 20 : 1;
+      if ((it + 1) % period != 0 && it + 1 < max_outer) continue;
+      if ((rc = e->compute_cost(nullptr, &cost[i]))) return fail(rc, e->last_error());
+      if (it + 1 > period && std::fabs(cost[i] - prev[i]) <= tol * std::fabs(cost[i])) active[i] = 0;
       prev[i] = cost[i];
     }
   }

@@ -952,6 +952,11 @@ int Engine::batch_args(int outer, int inner, SweepArgs* out, size_t* smem_needed
   a.err = d_err_;
   a.stats = d_stats_;
   a.colour = 0;
+  if (bf_) {  // this call's NHICD list, active mask and magnitude reset
+    int rc = bf_call_begin(outer, inner, &a.bfa);
+    if (rc) return rc;
+    a.bf = 1;
+  }
   a.n_slices = (g.n_y + 1) / 2;
   *out = a;
   if (smem_needed) *smem_needed = smem_bytes_;
@@ -959,6 +964,12 @@ int Engine::batch_args(int outer, int inner, SweepArgs* out, size_t* smem_needed
 }
 
 int Engine::batch_finish(int outer, int inner, const double* st, double ms) {
+  if (bf_) {
+    int rc = bf_call_end();
+    if (rc) return rc;
+    if (cudaStreamSynchronize(static_cast<cudaStream_t>(stream_)) != cudaSuccess)
+      return cuda_check(MBIR_EDEVICE, "batch call end");
+  }
   icd_ms_ += ms;
   sweeps_done_++;
   visited_ += static_cast<int64_t>(st[2] + st[3]);

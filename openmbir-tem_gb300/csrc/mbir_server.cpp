@@ -54,7 +54,14 @@ size_t Server::estimate_bytes(const Request& r) const {
   const size_t sino = static_cast<size_t>(r.n_t) * r.n_theta * n_rp;
   const size_t vox = static_cast<size_t>(r.dims[0]) * r.dims[1] * r.dims[2];
   const size_t host_layout = std::max(static_cast<size_t>(r.n_theta) * r.n_r * r.n_t, vox) * 4;
-  return rb * (3 * sino + vox) + host_layout + (1u << 20);
+  size_t bf = 0;
+  if (r.params.modality == MBIR_MODALITY_BF) {
+    const size_t n_sp = (static_cast<size_t>(r.n_r) + 15) / 16 * 16;
+    const size_t lines = static_cast<size_t>(r.dims[0]) * r.dims[1];
+    bf = rb * sino + static_cast<size_t>(r.n_t) * r.n_theta * n_sp +
+         8 * static_cast<size_t>(r.n_theta) * r.n_r * r.n_t + lines * (8 * 3 + 1);
+  }
+  return rb * (3 * sino + vox) + host_layout + bf + (1u << 20);
 }
 
 int64_t Server::submit(const mbir_params& p, const float* counts, const float* tilts, int n_theta,
@@ -176,19 +183,30 @@ void Server::loop() {
       } else {
         for (Request* r : cur) {
           Engine* e = r->engine.get();
+          const bool bf = r->params.modality == MBIR_MODALITY_BF;
           int erc = 0;
           if (r->params.joint_estimation) erc = e->joint_estimation();
-          if (!erc && r->params.noise_model) erc = e->update_weights();
-          double c = 0;
-          if (!erc) erc = e->compute_cost(nullptr, &c);
+          if (!erc && (bf ? r->params.noise_estimation : r->params.noise_model))
+            erc = e->update_weights();
           if (erc) {
             broken.emplace_back(r, e->last_error());
             continue;
           }
           r->outer_done++;
-          const bool conv = r->outer_done > 1 && std::fabs(c - r->cost) <= r->tol * std::fabs(c);
-          r->prev_cost = r->cost;
-          r->cost = c;
+          // a bright-field call updates 1/20 of the voxel lines (NHICD): the cost is compared
+          // once per equivalent iteration of 20 calls
+          const int period = bf ? 20 : 1;
+          bool conv = false;
+          if (r->outer_done % period == 0 || r->outer_done >= r->max_outer) {
+            double c = 0;
+            if ((erc = e->compute_cost(nullptr, &c))) {
+              broken.emplace_back(r, e->last_error());
+              continue;
+            }
+            conv = r->outer_done > period && std::fabs(c - r->cost) <= r->tol * std::fabs(c);
+            r->prev_cost = r->cost;
+            r->cost = c;
+          }
           if (conv || r->outer_done >= r->max_outer) finished.push_back(r);
         }
       }

@@ -582,7 +582,8 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
 }
 
 struct SmemLayout {
-  size_t bar, ctl, stats, rb, bx, bxd, gw, H, hv, list, cls, okr, lv, cache, es, sel, total;
+  size_t bar, ctl, stats, rb, bx, bxd, gw, H, hv, list, cls, okr, lv, flat, gofs, bits, cache, es,
+      sel, total;
 };
 
 __host__ __device__ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -621,6 +622,12 @@ __host__ __device__ inline SmemLayout smem_layout(int n_theta, int n_x, int n_rs
   o = align_up(o + static_cast<size_t>(n_x), 16);
   L.lv = o;    // row flags: bit 0 live at row start, bit 1 live-or-reachable (period prefix)
   o = align_up(o + static_cast<size_t>(n_x), 16);
+  L.flat = o;  // the row's candidates in step order
+  o = align_up(o + sizeof(int) * (static_cast<size_t>(n_x) + 2), 16);
+  L.gofs = o;  // step offsets into flat
+  o = align_up(o + sizeof(int) * (static_cast<size_t>(n_x) + 4), 16);
+  L.bits = o;  // candidates of the step being formed, one bit per x
+  o = align_up(o + sizeof(unsigned) * ((static_cast<size_t>(n_x) + 31) / 32 + 2), 16);
   L.cache = o;
   o = align_up(o + real_bytes * 9 * static_cast<size_t>(n_x), 128);
   L.es = o;
@@ -778,6 +785,9 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
   }
   const uint8_t* active_lines = BF ? A.bfa.active : nullptr;
   int* cls = reinterpret_cast<int*>(smem + L.cls);
+  int* flat = reinterpret_cast<int*>(smem + L.flat);
+  int* gofs = reinterpret_cast<int*>(smem + L.gofs);
+  unsigned* bits = reinterpret_cast<unsigned*>(smem + L.bits);
   uint8_t* okr = smem + L.okr;
   uint8_t* lv = smem + L.lv;
   const int S = A.stride;
@@ -869,14 +879,60 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
       if (lane == 0) cls[k] = base;
     }
     __syncthreads();
-    for (int k = 0; k < S; ++k) {
-      const int n = cls[k];
-      if (n == 0) continue;
+    // Steps: consecutive classes are merged while none of the next class's candidates lies
+    // within S of a candidate already in the step.  Voxels of one step are then pairwise
+    // independent (no shared detector bin, no prior neighbours, no zero-skipping influence),
+    // and independent updates commute, so a step gives exactly the result of running its
+    // classes in order.  One warp forms the steps in class order.
+    if (warp == 0) {
+      const int words = (g.n_x + 31) >> 5;
+      for (int w = lane; w < words; w += 32) bits[w] = 0u;
+      __syncwarp();
+      int ns = 0, nf = 0, step0 = 0;
+      if (lane == 0) gofs[0] = 0;
+      for (int k = 0; k < S; ++k) {
+        const int n = cls[k];
+        if (n == 0) continue;
+        bool conf = false;
+        for (int j = lane; j < n && !conf; j += 32) {
+          const int x = list[k * cap + j];
+          const int lo = max(x - S + 1, 0), hi = min(x + S - 1, g.n_x - 1);
+          for (int w = lo >> 5; w <= (hi >> 5); ++w) {
+            const int a = max(lo - (w << 5), 0), b = min(hi - (w << 5), 31);
+            const unsigned mask =
+                (b - a == 31) ? 0xffffffffu : (((1u << (b - a + 1)) - 1u) << a);
+            if (bits[w] & mask) conf = true;
+          }
+        }
+        if (__any_sync(kFull, conf) && nf > step0) {
+          // close the step: clear the words holding its candidates, open the next one
+          for (int j = step0 + lane; j < nf; j += 32) bits[flat[j] >> 5] = 0u;
+          ++ns;
+          step0 = nf;
+          if (lane == 0) gofs[ns] = nf;
+          __syncwarp();
+        }
+        for (int j = lane; j < n; j += 32) {
+          const int x = list[k * cap + j];
+          flat[nf + j] = x;
+          atomicOr(&bits[x >> 5], 1u << (x & 31));
+        }
+        nf += n;
+        __syncwarp();
+      }
+      if (lane == 0) {
+        gofs[ns + 1] = nf;
+        ctl[0] = static_cast<unsigned>(ns + 1);
+      }
+    }
+    __syncthreads();
+    const int n_steps = static_cast<int>(ctl[0]);
+    for (int st = 0; st < n_steps; ++st) {
+      const int b = gofs[st], n = gofs[st + 1] - b;
       for (int b0 = 0; b0 < n; b0 += n_groups) {
         const int i = b0 + group;
         const bool act = i < n;
-        group_step<Real, NB, G, VPL, BF, false>(c, z, act ? list[k * cap + i] : 0, y, act, lane,
-                                                acc);
+        group_step<Real, NB, G, VPL, BF, false>(c, z, act ? flat[b + i] : 0, y, act, lane, acc);
       }
       __syncthreads();
     }

@@ -80,3 +80,37 @@ def test_batch_rejects_fp64_and_reference_order(lib_built):
             with pytest.raises(mbir.MbirError):
                 b.add(e)
         e.close()
+
+
+def make_mixed(mbir):
+    """Two HAADF and two bright-field reconstructions of different sizes."""
+    from conftest import bf_case, bf_params
+    out = make_engines(mbir)[:2]
+    for (n_r, n_t, seed) in ((64, 8, 5), (48, 12, 6)):
+        y, ang, th = bf_case(n_r=n_r, n_t=n_t, seed=seed)
+        e = mbir.Engine(bf_params(mbir, th))
+        e.set_sinogram(y, ang)
+        e.prepare()
+        out.append(e)
+    return out
+
+
+def test_batched_mixed_haadf_bf_match_single(lib_built):
+    """HAADF sweeps and bright-field NHICD calls in one persistent launch give the same bits as
+    each engine alone (same lists, same order, same arithmetic)."""
+    mbir = lib_built
+    alone = make_mixed(mbir)
+    batched = make_mixed(mbir)
+    with mbir.Batch(0) as b:
+        for e in batched:
+            b.add(e)
+        for k in range(4):
+            st_b = b.sweep(outer=k)
+            st_s = np.stack([e.sweep(k, 0) for e in alone])
+            np.testing.assert_array_equal(st_b[:, 2:], st_s[:, 2:])
+    for ea, eb in zip(alone, batched):
+        assert np.array_equal(eb.volume(), ea.volume())
+        assert np.array_equal(eb.error_sinogram(), ea.error_sinogram())
+    for ea, eb in zip(alone[2:], batched[2:]):
+        np.testing.assert_array_equal(eb.call_lines(), ea.call_lines())
+        np.testing.assert_array_equal(eb.bf_state()[0], ea.bf_state()[0])  # selectors

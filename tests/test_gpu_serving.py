@@ -71,3 +71,33 @@ def test_admission_respects_memory_budget(lib_built):
         assert 0 < st.peak_bytes <= st.budget_bytes
         assert st.admitted == len(reqs) and st.admitted_out_of_order == 0
         assert st.peak_active < len(reqs)  # the budget kept some requests waiting
+
+
+def test_mixed_haadf_bf_same_alone_and_in_the_mix(lib_built):
+    """Bright-field and HAADF requests served together: each result equals the same request
+    served alone (bright field converges per equivalent iteration of 20 calls)."""
+    from conftest import bf_case, bf_params
+    mbir = lib_built
+    reqs = requests(mbir)[:2]
+    for (n_r, n_t, seed) in ((64, 8, 5), (48, 12, 6)):
+        y, ang, th = bf_case(n_r=n_r, n_t=n_t, seed=seed)
+        reqs.append((bf_params(mbir, th), y, ang))
+    outers = [6, 6, 40, 40]
+    alone = []
+    with mbir.Server(0, 0, 1) as s:
+        for (p, y, ang), mo in zip(reqs, outers):
+            rid = s.submit(p, y, ang, max_outer=mo, tol=1e-4)
+            s.wait(rid)
+            alone.append((s.result(rid), s.poll(rid)[2]))
+    with mbir.Server(0, 0, 0) as s:
+        ids = []
+        for (p, y, ang), mo in zip(reqs, outers):
+            ids.append(s.submit(p, y, ang, max_outer=mo, tol=1e-4))
+            time.sleep(0.005)
+        for rid in ids:
+            s.wait(rid)
+        mixed = [(s.result(rid), s.poll(rid)[2]) for rid in ids]
+        assert s.stats().failed == 0
+    for (va, na), (vm, nm) in zip(alone, mixed):
+        assert na == nm
+        assert np.array_equal(va, vm)
