@@ -389,7 +389,7 @@ int64_t mbir_server_submit(mbir_server* s, const mbir_params* p, const float* co
                            double dr, double dt, int32_t max_outer, double tol) {
   if (!s || !p || !counts || !tilts) return MBIR_EINVAL;
   if (p->struct_size != static_cast<int32_t>(sizeof(mbir_params))) return MBIR_EINVAL;
-  if (p->modality != MBIR_MODALITY_HAADF) return MBIR_ENOTSUP;
+  if (p->modality != MBIR_MODALITY_HAADF && p->modality != MBIR_MODALITY_BF) return MBIR_EINVAL;
   try {
     return s->impl->submit(*p, counts, tilts, n_theta, n_r, n_t, dr, dt, max_outer, tol);
   } catch (...) {
