@@ -434,6 +434,7 @@ def main():
     upd = 0.0
     visited = 0.0
     barrier()
+    st0 = eng.status()
     with ClockSampler(local) as clk:
         for k in range(args.steps):
             flush.fill_(float(k))
@@ -444,6 +445,11 @@ def main():
             upd += s[3]
             visited += s[2] + s[3]
     barrier()
+    st1 = eng.status()
+    # the sweep kernels' own device time (events around the colour launches) and the host time
+    # spent building level schedules, both inside the ICD interval above
+    kernel_ms_step = (st1.kernel_ms_total - st0.kernel_ms_total) / args.steps
+    sched_ms_step = (st1.sched_ms_total - st0.sched_ms_total) / args.steps
     total_ms = float(np.sum(per_ms))
     if dist is not None:
         t = torch.tensor([total_ms], device=f"cuda:{local}")
@@ -459,7 +465,7 @@ def main():
     per_vox = (13.0 if bf else 8.0) * f_mean * st.t_rows + 8.0
     bytes_step = (upd / args.steps) * per_vox
     peak, peak_kind = load_peaks()
-    achieved = bytes_step / (ms_step / 1e3) / 1e9
+    achieved = bytes_step / (kernel_ms_step / 1e3) / 1e9
     launches = calls_per_step * 3  # two colour launches + one stats reduction per call
     traffic = None
     tp = os.path.join(ROOT, "profiles", "icd_sweep_traffic.json")
@@ -485,7 +491,10 @@ def main():
                       "parallelism": f"replicas x{world}",
                       "voxels_updated_per_step": upd / args.steps,
                       "voxels_visited_per_step": visited / args.steps,
-                      "slices_in_smem": bool(st.staged), "x_stride": st.stride},
+                      "slices_in_smem": bool(st.staged), "x_stride": st.stride,
+                      "sweep_kernel_ms_per_step": kernel_ms_step,
+                      "host_schedule_ms_per_step": sched_ms_step,
+                      "levels_last_call": st.sched_levels},
            "gpu_launches": launches * args.steps,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "traffic": traffic,
@@ -495,7 +504,8 @@ def main():
                         "traffic_unit": "bytes per colour launch (ncu capture)",
                         "bytes_model": ("13*F*L+8" if bf else "8*F*L+8") +
                                        " per updated voxel, F=A-column nnz, L=t rows",
-                        "kernel": "sweep_kernel (two colour launches per call)"},
+                        "kernel": "sweep_kernel (two colour launches per call)",
+                        "kernel_ms_per_launch": kernel_ms_step / (2 * calls_per_step)},
            "clocks": clk.summary()}
 
     if not args.no_e2e:

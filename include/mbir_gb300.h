@@ -117,6 +117,9 @@ typedef struct mbir_params {
                                  4 views (<= 64 views), 2 = 32 x 2 (<= 64), 3 = 32 x 3 (<= 96),
                                  4 = 32 x 5 (<= 160).  Results depend on the shape in the last bits
                                  (summation order); fix it for bit-reproducible runs. */
+  int32_t row_walk;           /* BF NHICD calls (FP32, parallel order): 0 = run the call's voxel
+                                 lines in dependency levels (one barrier per level), 1 = walk the
+                                 rows class by class.  Same visit order, same results. */
 } mbir_params;
 
 typedef struct mbir_status {
@@ -134,6 +137,10 @@ typedef struct mbir_status {
   int32_t stride;         /* x stride of the conflict-free voxel sets */
   int32_t staged;         /* 1: voxel slices staged in shared memory, 0: slices read from HBM */
   int32_t lane_shape;     /* voxel-group shape in use (see mbir_params.lane_shape) */
+  int32_t sched_levels;   /* dependency levels of the last level-scheduled BF call (0: none) */
+  double sched_ms_total;  /* host time spent building level schedules */
+  double kernel_ms_total; /* device time of the parallel-order sweep kernels alone (colour
+                             launches; icd_ms_total also holds list, schedule and statistics) */
 } mbir_status;
 
 typedef struct mbir_engine mbir_engine;
@@ -306,6 +313,23 @@ const char* mbir_version(void);
  * Launches on `stream` (a cudaStream_t, 0 = legacy default stream) and does not synchronise. */
 int32_t mbir_error_view_sums_noalloc(const float* error_dev, int32_t n_theta, int32_t n_r,
                                      int32_t n_t, double* sums_dev, void* stream);
+
+/* Dependency levels of one sparse ICD call (host only; the schedule a level-scheduled BF NHICD
+ * call runs, see mbir_params.row_walk).  The visit order is the row walk's: rows in rows[n_z],
+ * within a row the classes x = k (mod stride), k = 0..stride-1, x ascending.  A line (z*n_x + x)
+ * is in the call when lineok[l] and (active == NULL or active[l]).  lo[l*n_theta + v] is the
+ * first detector bin of line l at view v and bit b of mask[l*n_theta + v] marks bin lo+b as
+ * touched (b < nb <= 16, lo+b in [0, n_r)).  level(l) = 1 + the largest level of an earlier line
+ * that shares a touched bin at some view or lies in l's 3x3 (z, x) neighbourhood.  Writes the
+ * lines level by level (visit order within a level) to lines[lines_cap] and the level offsets to
+ * lofs[lofs_cap] (n_levels + 1 values); *n_lines, *n_levels receive the counts.  Replaces no
+ * reference interface (the reference updates a call's lines one after another,
+ * BFReconstructionEngine_Extra.cpp:476-628).  MBIR_EINVAL on bad input or short buffers. */
+int32_t mbir_level_schedule(int32_t n_z, int32_t n_x, int32_t n_theta, int32_t n_r, int32_t nb,
+                            int32_t stride, const int32_t* rows, const uint8_t* lineok,
+                            const uint8_t* active, const int16_t* lo, const uint16_t* mask,
+                            int32_t* lines, int32_t lines_cap, int32_t* lofs, int32_t lofs_cap,
+                            int32_t* n_lines, int32_t* n_levels);
 
 #ifdef __cplusplus
 }

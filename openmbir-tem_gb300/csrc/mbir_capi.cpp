@@ -1,4 +1,5 @@
 // mbir_capi.cpp -- extern "C" boundary over mbir::Engine.  No C++ exception crosses it.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -440,6 +441,41 @@ int32_t mbir_server_get_stats(mbir_server* s, mbir_server_stats* st) {
 }
 const char* mbir_server_last_error(const mbir_server* s) {
   return s ? s->impl->last_error() : "null server";
+}
+
+int32_t mbir_level_schedule(int32_t n_z, int32_t n_x, int32_t n_theta, int32_t n_r, int32_t nb,
+                            int32_t stride, const int32_t* rows, const uint8_t* lineok,
+                            const uint8_t* active, const int16_t* lo, const uint16_t* mask,
+                            int32_t* lines, int32_t lines_cap, int32_t* lofs, int32_t lofs_cap,
+                            int32_t* n_lines, int32_t* n_levels) {
+  if (!rows || !lineok || !lo || !mask || !lines || !lofs || !n_lines || !n_levels)
+    return MBIR_EINVAL;
+  if (n_z <= 0 || n_x <= 0 || n_theta <= 0 || n_r <= 0 || nb <= 0 || nb > 16 || stride <= 0)
+    return MBIR_EINVAL;
+  const size_t nl = static_cast<size_t>(n_z) * n_x;
+  for (size_t i = 0; i < nl * n_theta; ++i) {
+    if (!mask[i]) continue;
+    if (mask[i] >> nb) return MBIR_EINVAL;
+    for (int b = 0; b < nb; ++b)
+      if (((mask[i] >> b) & 1u) && (lo[i] + b < 0 || lo[i] + b >= n_r)) return MBIR_EINVAL;
+  }
+  try {
+    mbir::LevelScheduleIn in{n_z, n_x, n_theta, n_r, nb, stride, rows, lineok, active, lo, mask};
+    mbir::LevelScheduleWork w;
+    std::vector<int32_t> out, ofs;
+    const int levels = mbir::level_schedule(in, w, out, ofs);
+    if (levels < 0) return MBIR_EINVAL;
+    if (static_cast<int64_t>(out.size()) > lines_cap ||
+        static_cast<int64_t>(ofs.size()) > lofs_cap)
+      return MBIR_EINVAL;
+    std::copy(out.begin(), out.end(), lines);
+    std::copy(ofs.begin(), ofs.end(), lofs);
+    *n_lines = static_cast<int32_t>(out.size());
+    *n_levels = levels;
+    return MBIR_OK;
+  } catch (...) {
+    return MBIR_ENOMEM;
+  }
 }
 
 }  // extern "C"

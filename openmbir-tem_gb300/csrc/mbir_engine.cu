@@ -136,10 +136,27 @@ void Engine::release() {
   dfree(d_bfout_);
   dfree(d_alpha_);
   dfree(d_stage64_);
+  dfree(d_acol_);
+  dfree(d_sched_);
+  dfree(d_lofs_);
+  acol_lo_.clear();
+  acol_mask_.clear();
   if (ev0_) cudaEventDestroy(static_cast<cudaEvent_t>(ev0_));
   if (ev1_) cudaEventDestroy(static_cast<cudaEvent_t>(ev1_));
+  if (ev2_) cudaEventDestroy(static_cast<cudaEvent_t>(ev2_));
+  if (ev3_) cudaEventDestroy(static_cast<cudaEvent_t>(ev3_));
   if (stream_) cudaStreamDestroy(static_cast<cudaStream_t>(stream_));
-  ev0_ = ev1_ = stream_ = nullptr;
+  ev0_ = ev1_ = ev2_ = ev3_ = stream_ = nullptr;
+}
+
+// device time of the colour launches of the last sweep/call (events ev2_ -> ev3_)
+void Engine::add_kernel_time() {
+  if (!kernel_timed_) return;
+  kernel_timed_ = false;
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, static_cast<cudaEvent_t>(ev2_), static_cast<cudaEvent_t>(ev3_)) ==
+      cudaSuccess)
+    kernel_ms_ += ms;
 }
 
 int Engine::fail(int code, const std::string& msg) {
@@ -556,11 +573,15 @@ int Engine::alloc_device() {
   if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
     return fail(MBIR_EDEVICE, "stream creation failed");
   stream_ = s;
-  cudaEvent_t e0, e1;
+  cudaEvent_t e0, e1, e2, e3;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  cudaEventCreate(&e3);
   ev0_ = e0;
   ev1_ = e1;
+  ev2_ = e2;
+  ev3_ = e3;
   cudaMemsetAsync(d_err_, 0, sizeof(int), s);
   return MBIR_OK;
 }
@@ -750,6 +771,7 @@ int Engine::prepare() {
   // forward projection + error sinogram (HAADF_ReconstructionEngine.cpp:636-691)
   if ((rc = forward_project())) return rc;
   if (bf_ && (rc = bf_upload())) return rc;
+  if (bf_ && (rc = bf_prepare_schedule())) return rc;
   if (p_.lane_shape == 0 && (rc = autotune_shape())) return rc;
   return MBIR_OK;
 }
@@ -870,6 +892,7 @@ int Engine::sweep(int outer, int inner, double* stats4) {
     a.shape = shape_;
     a.err = d_err_;
     const int n0 = (g.n_y + 1) / 2;
+    cudaEventRecord(static_cast<cudaEvent_t>(ev2_), s);
     for (int colour = 0; colour < 2; colour++) {
       a.colour = colour;
       a.n_slices = (g.n_y - colour + 1) / 2;
@@ -877,6 +900,8 @@ int Engine::sweep(int outer, int inner, double* stats4) {
       if (a.n_slices <= 0) continue;
       if ((rc = launch_sweep(a, nb_, smem_bytes_, s))) return cuda_check(rc, "ICD sweep launch");
     }
+    cudaEventRecord(static_cast<cudaEvent_t>(ev3_), s);
+    kernel_timed_ = true;
     if ((rc = launch_reduce_stats(d_stats_, g.n_y, kStatSlots, d_stat4_, s)))
       return cuda_check(rc, "stats reduce");
   }
@@ -888,6 +913,7 @@ int Engine::sweep(int outer, int inner, double* stats4) {
   float ms = 0;
   cudaEventElapsedTime(&ms, static_cast<cudaEvent_t>(ev0_), static_cast<cudaEvent_t>(ev1_));
   icd_ms_ += ms;
+  add_kernel_time();
   sweeps_done_++;
   visited_ += static_cast<int64_t>(st[2] + st[3]);
   updated_ += static_cast<int64_t>(st[3]);
@@ -952,10 +978,13 @@ int Engine::batch_args(int outer, int inner, SweepArgs* out, size_t* smem_needed
   a.err = d_err_;
   a.stats = d_stats_;
   a.colour = 0;
-  if (bf_) {  // this call's NHICD list, active mask and magnitude reset
+  if (bf_) {  // this call's NHICD list, active mask and magnitude reset, its level schedule
     int rc = bf_call_begin(outer, inner, &a.bfa);
     if (rc) return rc;
     a.bf = 1;
+    if ((rc = bf_schedule(rows, a))) return rc;
+    if (cudaStreamSynchronize(static_cast<cudaStream_t>(stream_)) != cudaSuccess)
+      return cuda_check(MBIR_EDEVICE, "batch schedule upload");
   }
   a.n_slices = (g.n_y + 1) / 2;
   *out = a;
@@ -1227,6 +1256,9 @@ int Engine::status(mbir_status* st) const {
   st->stride = stride_;
   st->staged = stage_ ? 1 : 0;
   st->lane_shape = shape_;
+  st->sched_levels = n_levels_;
+  st->sched_ms_total = sched_ms_;
+  st->kernel_ms_total = kernel_ms_;
   return MBIR_OK;
 }
 

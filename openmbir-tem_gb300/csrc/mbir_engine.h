@@ -10,6 +10,7 @@
 
 #include "../../include/mbir_gb300.h"
 #include "mbir_internal.h"
+#include "mbir_schedule.h"
 
 namespace mbir {
 
@@ -124,6 +125,8 @@ class Engine {
   int bf_compute_cost(double* parts3, double* total);
   int bf_run();
   int bf_roi_sum(int kind, double* out);
+  int bf_prepare_schedule();                      // A-column table for level-scheduled calls
+  int bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a);  // the call's levels
   BfSino bf_sino() const;
   double bf_default_offset() const;
 
@@ -140,6 +143,7 @@ class Engine {
   ExactArgs exact_args();
   int cuda_check(int code, const char* what);
   void release();
+  void add_kernel_time();
 
   mbir_params p_;
   std::string err_;
@@ -211,6 +215,10 @@ class Engine {
   void* stream_ = nullptr;
   void* ev0_ = nullptr;
   void* ev1_ = nullptr;
+  void* ev2_ = nullptr;   // around the colour launches of a sweep/call
+  void* ev3_ = nullptr;
+  bool kernel_timed_ = false;
+  double kernel_ms_ = 0.0;  // device time of the sweep kernels alone
   int n_chunk_ = 8;
   int prior_blocks_ = 152 * 4;
 
@@ -243,6 +251,18 @@ class Engine {
   int slab_y0_ = 0, slab_y1_ = 0;           // 0, 0: the whole volume
   int bf_calls_ = 0;
   double bragg_t_ = 0;
+
+  // level-scheduled calls (FP32, parallel order, NHICD): A-column table on the device, its
+  // bins on the host, the call's schedule
+  float4* d_acol_ = nullptr;                // [n_z*n_x][n_theta][acol_width(nb)]
+  std::vector<int16_t> acol_lo_;            // [n_z*n_x][n_theta]
+  std::vector<uint16_t> acol_mask_;         // [n_z*n_x][n_theta]
+  int* d_sched_ = nullptr;                  // [n_z*n_x] lines level by level
+  int* d_lofs_ = nullptr;                   // [n_z*n_x + 1] level offsets
+  int n_levels_ = 0;                        // levels of the last scheduled call
+  double sched_ms_ = 0;                     // host time spent building schedules
+  LevelScheduleWork sched_work_;
+  std::vector<int32_t> sched_lines_, sched_lofs_;
 };
 
 // GenRandList's permutation (Common/VoxelUpdateList.cpp:157-215) drawn from mt19937 through

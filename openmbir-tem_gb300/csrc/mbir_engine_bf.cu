@@ -5,7 +5,10 @@
 // Reference: Code/MBIRLib/BrightField/BFReconstructionEngine.cpp:555-858 (execute loops),
 // BFReconstructionEngine_Extra.cpp:476-1273 (updateVoxels, NHICD, stop rule),
 // BFForwardModel.cpp:328-531, 812-972 (weights, estimates, selector, cost, raw counts).
+#include <cuda_runtime.h>
+
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 
@@ -17,6 +20,12 @@ namespace {
 constexpr int kNumHomogeneous = 20;     // MBIR::Constants::k_NumHomogeniousIter
 constexpr int kNumNonHomogeneous = 20;  // k_NumNonHomogeniousIter
 constexpr double kDefBragg = 5e10;      // DefBraggThreshold (BFConstants.h)
+
+template <typename T>
+void dfree_any(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
 
 // boost::uniform_int<uint32_t>(0, range) on mt19937: the raw draw divided by the bucket size,
 // redrawn when the quotient exceeds range
@@ -129,6 +138,65 @@ int Engine::bf_upload() {
   cudaMemsetAsync(d_active_, 1, nl, s);
   cudaMemcpyAsync(d_alpha_, alpha_.data(), sizeof(double) * g.n_theta, cudaMemcpyHostToDevice, s);
   if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "BF upload");
+  return MBIR_OK;
+}
+
+// Level-scheduled calls (FP32, parallel order, NHICD): the A-column table of every voxel line
+// (built once on the device by the sweep's own arithmetic) and, on the host, each entry's first
+// bin and nonzero mask, from which every call's dependency levels are computed.  Without room
+// for the table the calls walk the rows.
+int Engine::bf_prepare_schedule() {
+  if (fp64_ || !p_.nhicd || p_.order_mode != MBIR_ORDER_PARALLEL || p_.row_walk) return MBIR_OK;
+  const Geometry& g = g_;
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const size_t nl = static_cast<size_t>(g.n_z) * g.n_x;
+  const size_t n4 = nl * g.n_theta * acol_width(nb_);
+  if (cudaMalloc(&d_acol_, n4 * sizeof(float4)) != cudaSuccess ||
+      cudaMalloc(&d_sched_, nl * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&d_lofs_, (nl + 1) * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    dfree_any(d_acol_);
+    dfree_any(d_sched_);
+    dfree_any(d_lofs_);
+    return MBIR_OK;
+  }
+  const DevTables tab{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_,
+                      d_lineok_};
+  int rc = launch_acol_f32(dg_, tab, nb_, d_acol_, s);
+  if (rc) return cuda_check(rc, "A-column table");
+  std::vector<float> host(n4 * 4);
+  cudaMemcpyAsync(host.data(), d_acol_, n4 * sizeof(float4), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "A-column table");
+  acol_lo_.assign(nl * g.n_theta, 0);
+  acol_mask_.assign(nl * g.n_theta, 0);
+  acol_bins(host.data(), static_cast<int>(nl), g.n_theta, nb_, acol_lo_.data(), acol_mask_.data());
+  return MBIR_OK;
+}
+
+// The call's dependency levels over the row walk's visit order (rows, then classes), uploaded
+// for the sweep; leaves `a` walking the rows when the engine has no A-column table.
+int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
+  if (d_acol_ == nullptr) return MBIR_OK;
+  const Geometry& g = g_;
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const auto t0 = std::chrono::steady_clock::now();
+  LevelScheduleIn in{g.n_z, g.n_x, g.n_theta, g.n_r, nb_, stride_, rows.data(),
+                     tab_.line_nonempty.data(), active_host_.data(), acol_lo_.data(),
+                     acol_mask_.data()};
+  const int levels = level_schedule(in, sched_work_, sched_lines_, sched_lofs_);
+  if (levels < 0) return fail(MBIR_EINVAL, "level schedule: invalid row order");
+  sched_ms_ += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
+                   .count();
+  n_levels_ = levels;
+  if (!sched_lines_.empty())
+    cudaMemcpyAsync(d_sched_, sched_lines_.data(), sizeof(int) * sched_lines_.size(),
+                    cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(d_lofs_, sched_lofs_.data(), sizeof(int) * sched_lofs_.size(),
+                  cudaMemcpyHostToDevice, s);
+  a.sched_lines = d_sched_;
+  a.sched_lofs = d_lofs_;
+  a.n_levels = levels;
+  a.acol = d_acol_;
   return MBIR_OK;
 }
 
@@ -278,7 +346,9 @@ int Engine::bf_call(int outer, int inner, double* st4) {
     a.smem_rows = stage_ ? 1 : 0;
     a.n_rs = stage_ ? n_rs_ : 0;
     a.err = d_err_;
+    if ((rc = bf_schedule(rows, a))) return rc;
     const int n0 = (g.n_y + 1) / 2;
+    cudaEventRecord(static_cast<cudaEvent_t>(ev2_), s);
     for (int colour = 0; colour < 2; colour++) {
       a.colour = colour;
       a.n_slices = (g.n_y - colour + 1) / 2;
@@ -286,6 +356,8 @@ int Engine::bf_call(int outer, int inner, double* st4) {
       if (a.n_slices <= 0) continue;
       if ((rc = launch_sweep(a, nb_, smem_bytes_, s))) return cuda_check(rc, "BF call launch");
     }
+    cudaEventRecord(static_cast<cudaEvent_t>(ev3_), s);
+    kernel_timed_ = true;
     if ((rc = launch_reduce_stats(d_stats_, g.n_y, kStatSlots, d_stat4_, s)))
       return cuda_check(rc, "stats reduce");
   }
@@ -298,6 +370,7 @@ int Engine::bf_call(int outer, int inner, double* st4) {
   float ms = 0;
   cudaEventElapsedTime(&ms, static_cast<cudaEvent_t>(ev0_), static_cast<cudaEvent_t>(ev1_));
   icd_ms_ += ms;
+  add_kernel_time();
   sweeps_done_++;
   visited_ += static_cast<int64_t>(st[2] + st[3]);
   updated_ += static_cast<int64_t>(st[3]);

@@ -100,7 +100,20 @@ struct SweepArgs {
   int y_end;             // slab launch: slices y < y_end; 0 = whole-volume launch from `colour`
   double* stats;         // [gridDim.x][kStatSlots]
   int* err;              // device error word
+  // Level schedule (FP32; nullptr: walk the rows).  The voxel lines of the call in levels:
+  // lines of one level are pairwise independent (no shared detector bin at any view, not prior
+  // neighbours) and every line's level is above that of each earlier line of the visit order it
+  // conflicts with, so running the levels in turn gives the visit order's result.  Footprints
+  // do not depend on y, so one schedule serves every slice.
+  const int* sched_lines;  // [lofs[n_levels]] z*n_x + x, level by level
+  const int* sched_lofs;   // [n_levels + 1]
+  int n_levels;
+  const float4* acol;      // [n_z*n_x][n_theta][acol_width(NB)] A-column table (FP32)
 };
+
+// A-column table entry of one voxel line at one view: the first bin (int bits) and the NB
+// footprint values, padded to whole float4s.
+constexpr int acol_width(int nb) { return (nb + 1 + 3) / 4; }
 
 // Batched sweep: per-series sweep arguments and a queue of (series, slice y) items.
 struct BatchArgs {
@@ -198,6 +211,8 @@ int launch_sweep_f32_smem(const SweepArgs& a, int nb, size_t smem_bytes, void* s
 int launch_sweep_f32_smem_haadf(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_sweep_f32_smem_bf(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_sweep_f32_hbm(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
+// A-column table [n_z*n_x][n_theta][acol_width(nb)] of the FP32 sweep (level-scheduled calls)
+int launch_acol_f32(const DevGeom& g, const DevTables& tab, int nb, float4* out, void* stream);
 int launch_sweep_f64(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_ref_order_f32(const RefOrderArgs& a, int nb, void* stream);
 // persistent batched sweep (FP32, slices staged or in HBM per series); shape = lane_shape of

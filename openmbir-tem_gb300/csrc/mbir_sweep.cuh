@@ -21,6 +21,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "mbir_internal.h"
@@ -176,18 +177,23 @@ __device__ __forceinline__ void detector_pos(int x, RowBaseD rb, float2, double 
 }
 
 template <typename Real>
+__device__ __forceinline__ RowBase<Real> row_base(const DevTables& tab, int z, int v) {
+  const double b = tab.u0[v] - static_cast<double>(z) * tab.bz[v];
+  RowBase<Real> r;
+  if constexpr (std::is_same<Real, float>::value) {
+    const double fl = floor(b);
+    r.ib = static_cast<int>(fl);
+    r.fb = static_cast<float>(b - fl);
+  } else {
+    r.base = b;
+  }
+  return r;
+}
+
+template <typename Real>
 __device__ __forceinline__ void compute_row_base(const DevTables& tab, int n_theta, int z,
                                                  RowBase<Real>* rb, int tid, int nthreads) {
-  for (int v = tid; v < n_theta; v += nthreads) {
-    const double b = tab.u0[v] - static_cast<double>(z) * tab.bz[v];
-    if constexpr (std::is_same<Real, float>::value) {
-      const double fl = floor(b);
-      rb[v].ib = static_cast<int>(fl);
-      rb[v].fb = static_cast<float>(b - fl);
-    } else {
-      rb[v].base = b;
-    }
-  }
+  for (int v = tid; v < n_theta; v += nthreads) rb[v] = row_base<Real>(tab, z, v);
 }
 
 // A-matrix entries of one voxel at one view (AMatrixCol.cpp:148-232): bins j in
@@ -260,6 +266,9 @@ struct SliceCtx {
   int bs_rs, bs_ps;
   Real bt, bdt;              // T, delta*T
   unsigned long long* mag_fx;
+  const float4* acol;        // A-column table (level-scheduled sweeps) or nullptr
+  bool coherent;             // neighbour planes read from the volume bypass L1 (other CTAs of
+                             // the launch write them)
 };
 
 // Zero skipping (UpdateVoxels.cpp:310-338, BFUpdateYSlice.cpp:238-262): after the first sweep a
@@ -289,15 +298,36 @@ struct GroupAcc {
 // lanes of the warp call this together; `active` is false for a group with no voxel.  With
 // INLINE_ZS the zero-skipping test runs here (reference order); otherwise the caller has
 // already removed skipped voxels.
-template <typename Real, int NB, int G, int VPL, bool BF, bool INLINE_ZS>
+__device__ __forceinline__ float f4_at(const float4& q, int k) {
+  return k == 0 ? q.x : (k == 1 ? q.y : (k == 2 ? q.z : q.w));
+}
+
+// With ACOL the voxel's A-column comes from the table (level-scheduled sweeps, FP32): the
+// same values the in-kernel computation gives, loaded first so that their latency overlaps
+// the neighbour loads.
+template <typename Real, int NB, int G, int VPL, bool BF, bool INLINE_ZS, bool ACOL = false>
 __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x_req, int y,
                                            bool active, int lane, GroupAcc& acc) {
   using R2 = typename V2<Real>::type;
+  static_assert(!ACOL || std::is_same<Real, float>::value, "A-column table is FP32");
   const DevGeom& g = *c.g;
   const int gl = lane & (G - 1);
   const int x = active ? x_req : 0;
   const size_t plane = static_cast<size_t>(g.n_z) * g.n_x;
   const size_t vidx = static_cast<size_t>(y) * plane + static_cast<size_t>(z) * g.n_x + x;
+  constexpr int AW = acol_width(NB);
+  float4 aq[ACOL ? VPL : 1][ACOL ? AW : 1];
+  if constexpr (ACOL) {
+    const float4* ac = c.acol + (static_cast<size_t>(z) * g.n_x + x) * g.n_theta * AW;
+#pragma unroll
+    for (int i = 0; i < VPL; ++i) {
+      const int v = gl + G * i;
+#pragma unroll
+      for (int w = 0; w < AW; ++w)
+        aq[i][w] = (active && v < g.n_theta) ? __ldg(ac + v * AW + w)
+                                             : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
   const Real V = c.cache ? c.cache[4 * g.n_x + x] : c.vol[vidx];
   bool live = active && c.lineok[static_cast<size_t>(z) * g.n_x + x] != 0;
 
@@ -317,9 +347,13 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
         const int dy = k / 9 - 1, dz = (k / 3) % 3 - 1, dx = k % 3 - 1;
         const int yy = y + dy, zz = z + dz, xx = x + dx;
         if (yy >= 0 && yy < g.n_y && zz >= 0 && zz < g.n_z && xx >= 0 && xx < g.n_x) {
-          nb[i] = c.cache ? c.cache[((dy + 1) * 3 + (dz + 1)) * g.n_x + xx]
-                          : c.vol[static_cast<size_t>(yy) * plane +
-                                  static_cast<size_t>(zz) * g.n_x + xx];
+          if (c.cache) {
+            nb[i] = c.cache[((dy + 1) * 3 + (dz + 1)) * g.n_x + xx];
+          } else {
+            const Real* src =
+                c.vol + static_cast<size_t>(yy) * plane + static_cast<size_t>(zz) * g.n_x + xx;
+            nb[i] = (c.coherent && dy != 0) ? __ldcg(src) : *src;
+          }
           nvalid[i] = true;
           pos |= nb[i] > Real(0);
         }
@@ -364,6 +398,14 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
     jlo[i] = 0;
 #pragma unroll
     for (int b = 0; b < NB; ++b) a[i][b] = Real(0);
+    if constexpr (ACOL) {
+      if (v < g.n_theta && live) {
+        jlo[i] = __float_as_int(aq[i][0].x);
+#pragma unroll
+        for (int b = 0; b < NB; ++b) a[i][b] = f4_at(aq[i][(b + 1) >> 2], (b + 1) & 3);
+      }
+      continue;
+    }
     if (v < g.n_theta && live) {
       int j0;
       Real f;
@@ -772,6 +814,8 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
   c.mag_fx = nullptr;
   c.bw_rs = c.bw_ps = c.bs_rs = c.bs_ps = 0;
   c.bt = c.bdt = Real(0);
+  c.acol = nullptr;
+  c.coherent = coherent;
   if (BF) {
     c.bw = static_cast<const Real*>(A.bfa.w) + static_cast<size_t>(tfirst) * sino_plane;
     c.bw_rs = g.n_rp;
@@ -801,7 +845,30 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
 #pragma unroll
   for (int s2 = 0; s2 < kStatSlots; ++s2) acc.v[s2] = 0ull;
   unsigned skipped = 0;
-  for (int rr = 0; rr < g.n_z; ++rr) {
+  // Level schedule: the call's lines level by level, one CTA barrier per level; neighbours are
+  // read from the volume (the slice's own plane is written only by this CTA, the planes y+-1
+  // belong to the other colour and do not change during the launch), the zero-skipping test
+  // runs at the visit, and the A-column comes from the table.
+  bool scheduled = false;
+  if constexpr (kF32) {
+    if (A.sched_lines != nullptr && A.acol != nullptr && !project) {
+      scheduled = true;
+      c.cache = nullptr;
+      c.acol = A.acol;
+      for (int lv = 0; lv < A.n_levels; ++lv) {
+        const int b = __ldg(A.sched_lofs + lv), n = __ldg(A.sched_lofs + lv + 1) - b;
+        for (int b0 = 0; b0 < n; b0 += n_groups) {
+          const int i = b0 + group;
+          const bool act = i < n;
+          const int l = act ? __ldg(A.sched_lines + b + i) : 0;
+          group_step<Real, NB, G, VPL, BF, false, true>(c, l / g.n_x, l % g.n_x, y, act, lane,
+                                                        acc);
+        }
+        __syncthreads();
+      }
+    }
+  }
+  for (int rr = 0; !scheduled && rr < g.n_z; ++rr) {
     const int z = A.row_order[rr];
     __syncthreads();
     compute_row_base<Real>(A.tab, g.n_theta, z, rb, tid, nthreads);
@@ -1108,6 +1175,8 @@ __global__ void __launch_bounds__(32, 1) ref_order_kernel(RefOrderArgs A) {
   c.mag_fx = nullptr;
   c.bw_rs = c.bw_ps = c.bs_rs = c.bs_ps = 0;
   c.bt = c.bdt = Real(0);
+  c.acol = nullptr;
+  c.coherent = false;
   Real* const ge = static_cast<Real*>(A.e);
   const size_t sino_plane = static_cast<size_t>(g.n_theta) * g.n_rp;
   const size_t sel_plane = BF ? static_cast<size_t>(g.n_theta) * A.bfa.n_sp : 0;
@@ -1147,7 +1216,58 @@ __global__ void __launch_bounds__(32, 1) ref_order_kernel(RefOrderArgs A) {
       A.stats[s] = s < 2 ? static_cast<double>(acc.v[s]) / kFixScale : static_cast<double>(acc.v[s]);
 }
 
+// A-column table of every voxel line (z, x): per view the first bin and the NB footprint
+// values, by the same arithmetic (and compile flags) as the in-kernel A-column of group_step,
+// so a sweep that reads the table gives the same bits as one that computes it.
+template <int NB>
+__global__ void acol_kernel(DevGeom g, DevTables tab, float4* __restrict__ out) {
+  constexpr int AW = acol_width(NB);
+  const size_t n = static_cast<size_t>(g.n_z) * g.n_x * g.n_theta;
+  const float hw = static_cast<float>(g.half_width);
+  const float* H = static_cast<const float*>(tab.H);
+  for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const int v = static_cast<int>(i % g.n_theta);
+    const size_t l = i / g.n_theta;
+    const int z = static_cast<int>(l / g.n_x), x = static_cast<int>(l % g.n_x);
+    int j0;
+    float f;
+    detector_pos(x, row_base<float>(tab, z, v), tab.bx[v], 0.0, j0, f);
+    const float u = static_cast<float>(j0) + f;
+    int jlo = 0;
+    float a[NB];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) a[b] = 0.f;
+    if (!(u + hw < 0.f || u - hw > static_cast<float>(g.n_r)))
+      view_footprint<float, NB>(g, H + v * (g.bins + 1), j0, f, jlo, a);
+    float t[AW * 4];
+#pragma unroll
+    for (int k = 0; k < AW * 4; ++k) t[k] = 0.f;
+    t[0] = __int_as_float(jlo);
+#pragma unroll
+    for (int b = 0; b < NB; ++b) t[1 + b] = a[b];
+#pragma unroll
+    for (int w = 0; w < AW; ++w)
+      out[i * AW + w] = make_float4(t[4 * w], t[4 * w + 1], t[4 * w + 2], t[4 * w + 3]);
+  }
+}
+
 inline int ok_or(cudaError_t e) { return e == cudaSuccess ? 0 : -3; }
+
+inline int launch_acol_t(const DevGeom& g, const DevTables& tab, int nb, float4* out,
+                         cudaStream_t s) {
+  const size_t n = static_cast<size_t>(g.n_z) * g.n_x * g.n_theta;
+  const int grid = static_cast<int>(std::min<size_t>((n + 255) / 256, 152 * 16));
+  if (nb == 3)
+    acol_kernel<3><<<grid, 256, 0, s>>>(g, tab, out);
+  else if (nb == 5)
+    acol_kernel<5><<<grid, 256, 0, s>>>(g, tab, out);
+  else if (nb == 9)
+    acol_kernel<9><<<grid, 256, 0, s>>>(g, tab, out);
+  else
+    return -7;
+  return ok_or(cudaGetLastError());
+}
 
 template <typename Real, int NB, int G, int VPL, bool STAGE, bool BF>
 int launch_sweep_t(const SweepArgs& a, size_t smem, cudaStream_t s) {

@@ -83,6 +83,7 @@ class MbirParams(C.Structure):
         ("slice_staging", C.c_int32),
         ("nhicd", C.c_int32),
         ("lane_shape", C.c_int32),
+        ("row_walk", C.c_int32),
     ]
 
 
@@ -93,6 +94,8 @@ class MbirStatus(C.Structure):
         ("icd_ms_total", C.c_double), ("total_ms", C.c_double), ("voxels_visited", C.c_int64),
         ("voxels_updated", C.c_int64), ("footprint_entries", C.c_int64), ("t_rows", C.c_int32),
         ("stride", C.c_int32), ("staged", C.c_int32), ("lane_shape", C.c_int32),
+        ("sched_levels", C.c_int32), ("sched_ms_total", C.c_double),
+        ("kernel_ms_total", C.c_double),
     ]
 
 
@@ -175,7 +178,39 @@ SIGNATURES = {
     "mbir_server_last_error": (C.c_char_p, [C.c_void_p]),
     "mbir_run_multires": (C.c_int32, [C.POINTER(MbirParams), _F, _F, C.c_int32, C.c_int32,
                                       C.c_int32, C.c_double, C.c_double, _F, C.c_int64, _I]),
+    "mbir_level_schedule": (C.c_int32, [C.c_int32] * 6 + [_I, C.POINTER(C.c_uint8),
+                                                          C.POINTER(C.c_uint8),
+                                                          C.POINTER(C.c_int16),
+                                                          C.POINTER(C.c_uint16), _I, C.c_int32,
+                                                          _I, C.c_int32, _I, _I]),
 }
+
+
+def level_schedule(rows, lineok, lo, mask, nb, stride, n_r, active=None):
+    """Dependency levels of a sparse ICD call (mbir_level_schedule): returns (lines, lofs).
+    lineok/active are [n_z, n_x] bytes, lo/mask [n_z, n_x, n_theta]."""
+    lineok = np.ascontiguousarray(lineok, np.uint8)
+    n_z, n_x = lineok.shape
+    lo = np.ascontiguousarray(lo, np.int16)
+    mask = np.ascontiguousarray(mask, np.uint16)
+    n_theta = lo.shape[2]
+    rows = np.ascontiguousarray(rows, np.int32)
+    act = None if active is None else np.ascontiguousarray(active, np.uint8)
+    cap = n_z * n_x
+    lines = np.zeros(cap, np.int32)
+    lofs = np.zeros(cap + 1, np.int32)
+    nl = C.c_int32()
+    nlev = C.c_int32()
+    u8 = C.POINTER(C.c_uint8)
+    rc = lib().mbir_level_schedule(
+        n_z, n_x, n_theta, int(n_r), int(nb), int(stride), rows.ctypes.data_as(_I),
+        lineok.ctypes.data_as(u8), None if act is None else act.ctypes.data_as(u8),
+        lo.ctypes.data_as(C.POINTER(C.c_int16)), mask.ctypes.data_as(C.POINTER(C.c_uint16)),
+        lines.ctypes.data_as(_I), cap, lofs.ctypes.data_as(_I), cap + 1, C.byref(nl),
+        C.byref(nlev))
+    if rc != 0:
+        raise MbirError(rc, "mbir_level_schedule failed")
+    return lines[:nl.value].copy(), lofs[:nlev.value + 1].copy()
 
 
 def lib():

@@ -139,3 +139,32 @@ def test_bf_calls_decrease_cost(lib_built, oracle_mod):
         e.sweep(0, k)
         costs.append(e.cost()[0])
     assert all(b <= a for a, b in zip(costs, costs[1:])), costs
+
+
+@pytest.mark.parametrize("staging", [0, 1])
+def test_bf_level_schedule_bitwise_row_walk(lib_built, oracle_mod, staging):
+    """Level-scheduled NHICD calls give the row walk's bits: a run with the Bragg schedule,
+    offset and variance updates and homogeneous and non-homogeneous lists, slices staged in
+    shared memory or used in place in HBM."""
+    mbir = lib_built
+    y, ang, th = bf_case()
+    out = []
+    for row_walk in (0, 1):
+        p = bf_params(mbir, th, outer_iterations=3, inner_iterations=4, row_walk=row_walk,
+                      slice_staging=staging, seed=7)
+        e = mbir.Engine(p)
+        e.set_sinogram(y, ang)
+        e.run()
+        st = e.status()
+        sel, w, mag, _, _ = e.bf_state()
+        out.append((e.volume(), e.error_sinogram(), sel, mag, e.nuisance(), st))
+    (v0, e0, s0, m0, n0, st0), (v1, e1, s1, m1, n1, st1) = out
+    assert st0.sched_levels > 0 and st1.sched_levels == 0
+    assert st0.sweeps_done == st1.sweeps_done
+    assert st0.voxels_updated == st1.voxels_updated
+    assert st0.voxels_visited == st1.voxels_visited
+    assert np.array_equal(v0, v1), rel(v0, v1)
+    assert np.array_equal(e0, e1), rel(e0, e1)
+    assert np.array_equal(s0, s1) and np.array_equal(m0, m1)
+    for a, b in zip(n0, n1):
+        np.testing.assert_array_equal(a, b)
