@@ -275,16 +275,24 @@ def run_batch(args):
 
     # one at a time
     seq_s, seq_upd, seq_iters = 0.0, 0.0, []
+    phase = {"sweep_s": 0.0, "joint_estimation_s": 0.0, "variance_s": 0.0, "cost_s": 0.0}
+
+    def timed(key, fn):
+        t = time.perf_counter()
+        r = fn()
+        phase[key] += time.perf_counter() - t
+        return r
+
     for item in data:
         with engine(item) as e:
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             prev = None
             for it in range(max_outer):
-                e.sweep(it, 0)
-                e.joint_estimation()
-                e.update_weights()
-                c = e.cost()[0]
+                timed("sweep_s", lambda: e.sweep(it, 0))
+                timed("joint_estimation_s", e.joint_estimation)
+                timed("variance_s", e.update_weights)
+                c = timed("cost_s", e.cost)[0]
                 if prev is not None and abs(c - prev) <= tol * abs(c):
                     break
                 prev = c
@@ -300,6 +308,7 @@ def run_batch(args):
         t0 = time.perf_counter()
         iters, _ = b.run(max_outer, tol)
         bat_s = time.perf_counter() - t0
+        bat_sweep_s = b.total_ms() / 1e3
         bat_upd = sum(e.status().voxels_updated for e in engines)
     for e in engines:
         e.close()
@@ -311,8 +320,9 @@ def run_batch(args):
                        "tolerance": tol, "max_outer": max_outer},
             "sequential": {"wall_s": seq_s, "voxel_updates": seq_upd,
                            "voxel_updates_per_s": seq_upd / seq_s,
-                           "outer_iterations": int(np.sum(seq_iters))},
+                           "outer_iterations": int(np.sum(seq_iters)), "phases": phase},
             "batched": {"wall_s": bat_s, "voxel_updates": bat_upd,
+                        "sweep_device_s": bat_sweep_s,
                         "voxel_updates_per_s": bat_upd / bat_s,
                         "outer_iterations": int(np.sum(iters))}}
     print(json.dumps(line))

@@ -117,9 +117,13 @@ typedef struct mbir_params {
                                  4 views (<= 64 views), 2 = 32 x 2 (<= 64), 3 = 32 x 3 (<= 96),
                                  4 = 32 x 5 (<= 160).  Results depend on the shape in the last bits
                                  (summation order); fix it for bit-reproducible runs. */
-  int32_t row_walk;           /* BF NHICD calls (FP32, parallel order): 0 = run the call's voxel
-                                 lines in dependency levels (one barrier per level), 1 = walk the
-                                 rows class by class.  Same visit order, same results. */
+  int32_t call_schedule;      /* BF NHICD calls (FP32, parallel order): 0 = colour the call's
+                                 conflict graph and run the colour classes in turn (one barrier
+                                 per class; the visit order is colour by colour), 1 = walk the
+                                 rows class by class, 2 = the row walk's visit order run in
+                                 dependency levels (one barrier per level, the row walk's
+                                 bits).  mbir_get_call_lines returns the visit order of 0 and 2.
+                                 Default 2. */
 } mbir_params;
 
 typedef struct mbir_status {
@@ -315,7 +319,7 @@ int32_t mbir_error_view_sums_noalloc(const float* error_dev, int32_t n_theta, in
                                      int32_t n_t, double* sums_dev, void* stream);
 
 /* Dependency levels of one sparse ICD call (host only; the schedule a level-scheduled BF NHICD
- * call runs, see mbir_params.row_walk).  The visit order is the row walk's: rows in rows[n_z],
+ * call runs with mbir_params.call_schedule = 2).  The visit order is the row walk's: rows in rows[n_z],
  * within a row the classes x = k (mod stride), k = 0..stride-1, x ascending.  A line (z*n_x + x)
  * is in the call when lineok[l] and (active == NULL or active[l]).  lo[l*n_theta + v] is the
  * first detector bin of line l at view v and bit b of mask[l*n_theta + v] marks bin lo+b as
@@ -330,6 +334,23 @@ int32_t mbir_level_schedule(int32_t n_z, int32_t n_x, int32_t n_theta, int32_t n
                             const uint8_t* active, const int16_t* lo, const uint16_t* mask,
                             int32_t* lines, int32_t lines_cap, int32_t* lofs, int32_t lofs_cap,
                             int32_t* n_lines, int32_t* n_levels);
+
+/* Colour schedule of one sparse ICD call (host only; what a BF NHICD call runs with
+ * call_schedule = 0).  Same inputs as mbir_level_schedule without the row walk: the call's
+ * lines are visited z-major (z, then x ascending) and each takes the smallest colour that no
+ * earlier line sharing a touched bin at some view, or lying in its 3x3 (z, x) neighbourhood,
+ * holds and that has fewer than class_cap lines (0: no cap; the engine caps classes at the
+ * sweep kernel's voxel groups).  Writes the lines colour by colour (z-major within a colour)
+ * and the colour offsets;
+ * MBIR_EINVAL on bad input, short buffers or more than max_colours (<= 4096) colours.  Replaces
+ * no reference interface (the reference draws a random visit order per call,
+ * BFReconstructionEngine_Extra.cpp:576-628). */
+int32_t mbir_colour_schedule(int32_t n_z, int32_t n_x, int32_t n_theta, int32_t n_r, int32_t nb,
+                             int32_t max_colours, int32_t class_cap, const uint8_t* lineok,
+                             const uint8_t* active,
+                             const int16_t* lo, const uint16_t* mask, int32_t* lines,
+                             int32_t lines_cap, int32_t* lofs, int32_t lofs_cap, int32_t* n_lines,
+                             int32_t* n_colours);
 
 #ifdef __cplusplus
 }

@@ -116,12 +116,17 @@ int Batch::sweep(const std::vector<std::pair<int, int>>& iters, double* stats) {
   int nb = -1, max_theta = 0;
   int max_optin = 0;
   cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_);
-  for (int i = 0; i < n; i++) {
-    size_t need = 0;
+  // per-engine set-up (row order, bright-field list, active mask, level schedule) side by side
+  std::vector<size_t> needs(n, 0);
+  const std::vector<int> rcs = parallel_for(n, device_, [&](int i) {
     const int outer = iters.empty() ? 0 : iters[i].first;
     const int inner = iters.empty() ? 0 : iters[i].second;
-    if ((rc = eng_[i]->batch_args(outer, inner, &args[i], &need)))
-      return fail(rc, eng_[i]->last_error());
+    return eng_[i]->batch_args(outer, inner, &args[i], &needs[i]);
+  });
+  for (int i = 0; i < n; i++)
+    if (rcs[i]) return fail(rcs[i], eng_[i]->last_error());
+  for (int i = 0; i < n; i++) {
+    const size_t need = needs[i];
     if (nb < 0) nb = eng_[i]->nb();
     if (eng_[i]->nb() != nb) return fail(MBIR_ENOTSUP, "batch: engines at different voxel sizes");
     max_theta = std::max(max_theta, args[i].g.n_theta);
@@ -175,11 +180,15 @@ int Batch::sweep(const std::vector<std::pair<int, int>>& iters, double* stats) {
   last_ms_ = ms;
   total_ms_ += ms;
   sweeps_++;
-  for (int i = 0; i < n; i++) {
+  for (int i = 0; i < n; i++)
     if ((rc = eng_[i]->check_errors())) return fail(rc, eng_[i]->last_error());
+  const std::vector<int> fin = parallel_for(n, device_, [&](int i) {
     const int outer = iters.empty() ? 0 : iters[i].first;
     const int inner = iters.empty() ? 0 : iters[i].second;
-    eng_[i]->batch_finish(outer, inner, st.data() + kStatSlots * i, ms / n);
+    return eng_[i]->batch_finish(outer, inner, st.data() + kStatSlots * i, ms / n);
+  });
+  for (int i = 0; i < n; i++) {
+    if (fin[i]) return fail(fin[i], eng_[i]->last_error());
     if (stats)
       for (int k = 0; k < kStatSlots; k++) stats[kStatSlots * i + k] = st[kStatSlots * i + k];
   }
@@ -211,23 +220,27 @@ int Batch::run(int max_outer, double tol, int* outer_done, double* final_cost) {
     std::vector<std::pair<int, int>> iters(cur.size(), std::make_pair(it, 0));
     int rc = sweep(iters, nullptr);
     if (rc) return rc;
-    for (size_t k = 0; k < cur.size(); k++) {
+    // per engine (side by side): gain/offset, variance, cost and the stop test
+    const std::vector<int> rcs = parallel_for(static_cast<int>(cur.size()), device_, [&](int k) {
       Engine* e = cur[k];
       const int i = idx[k];
       const mbir_params& p = e->params();
       const bool bf = p.modality == MBIR_MODALITY_BF;
-      if (p.joint_estimation && (rc = e->joint_estimation())) return fail(rc, e->last_error());
-      if ((bf ? p.noise_estimation : p.noise_model) && (rc = e->update_weights()))
-        return fail(rc, e->last_error());
+      int erc;
+      if (p.joint_estimation && (erc = e->joint_estimation())) return erc;
+      if ((bf ? p.noise_estimation : p.noise_model) && (erc = e->update_weights())) return erc;
       done_at[i] = it + 1;
       // bright field: one NHICD call per outer iteration, the cost compared once per
       // equivalent iteration (20 calls)
       const int period = bf ? 20 : 1;
-      if ((it + 1) % period != 0 && it + 1 < max_outer) continue;
-      if ((rc = e->compute_cost(nullptr, &cost[i]))) return fail(rc, e->last_error());
+      if ((it + 1) % period != 0 && it + 1 < max_outer) return 0;
+      if ((erc = e->compute_cost(nullptr, &cost[i]))) return erc;
       if (it + 1 > period && std::fabs(cost[i] - prev[i]) <= tol * std::fabs(cost[i])) active[i] = 0;
       prev[i] = cost[i];
-    }
+      return 0;
+    });
+    for (size_t k = 0; k < cur.size(); k++)
+      if (rcs[k]) return fail(rcs[k], cur[k]->last_error());
   }
   eng_ = all;
   dirty_ = true;

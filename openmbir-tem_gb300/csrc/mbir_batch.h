@@ -1,12 +1,45 @@
 // mbir_batch.h -- batched execution of many resident reconstructions (see mbir_batch.cu).
 #pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
 #include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 
 #include "mbir_engine.h"
 
 namespace mbir {
+
+// Runs fn(i) for i in [0, n) on up to 16 host threads (the caller's included), each with
+// `device` current; fn(i) touches only item i's state.  Returns the results per item.  The
+// engines' host steps (list and schedule set-up, gain/offset and variance solves, cost) wait on
+// their own streams, so running them side by side overlaps those waits and the engines' small
+// kernels.
+template <typename F>
+std::vector<int> parallel_for(int n, int device, F fn) {
+  std::vector<int> rc(static_cast<size_t>(std::max(n, 0)), 0);
+  if (n <= 0) return rc;
+  const int hw = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+  const int nt = std::min(n, std::min(hw, 16));
+  std::atomic<int> next{0};
+  auto work = [&](bool set_device) {
+    if (set_device) cudaSetDevice(device);
+    for (;;) {
+      const int i = next.fetch_add(1);
+      if (i >= n) break;
+      rc[i] = fn(i);
+    }
+  };
+  std::vector<std::thread> pool;
+  pool.reserve(nt > 0 ? nt - 1 : 0);
+  for (int t = 1; t < nt; ++t) pool.emplace_back(work, true);
+  work(false);
+  for (auto& t : pool) t.join();
+  return rc;
+}
 
 class Batch {
  public:

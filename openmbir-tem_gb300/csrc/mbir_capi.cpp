@@ -100,6 +100,7 @@ void mbir_params_default(mbir_params* p, int32_t modality) {
     p->noise_estimation = 1;
     p->noise_model = 0;
     p->nhicd = 1;  // NHICD is defined in BFConstants.h
+    p->call_schedule = 2;
   }
 }
 
@@ -472,6 +473,42 @@ int32_t mbir_level_schedule(int32_t n_z, int32_t n_x, int32_t n_theta, int32_t n
     std::copy(ofs.begin(), ofs.end(), lofs);
     *n_lines = static_cast<int32_t>(out.size());
     *n_levels = levels;
+    return MBIR_OK;
+  } catch (...) {
+    return MBIR_ENOMEM;
+  }
+}
+
+int32_t mbir_colour_schedule(int32_t n_z, int32_t n_x, int32_t n_theta, int32_t n_r, int32_t nb,
+                             int32_t max_colours, int32_t class_cap, const uint8_t* lineok,
+                             const uint8_t* active,
+                             const int16_t* lo, const uint16_t* mask, int32_t* lines,
+                             int32_t lines_cap, int32_t* lofs, int32_t lofs_cap, int32_t* n_lines,
+                             int32_t* n_colours) {
+  if (!lineok || !lo || !mask || !lines || !lofs || !n_lines || !n_colours) return MBIR_EINVAL;
+  if (n_z <= 0 || n_x <= 0 || n_theta <= 0 || n_r <= 0 || nb <= 0 || nb > 16 ||
+      max_colours <= 0 || max_colours > 4096 || class_cap < 0)
+    return MBIR_EINVAL;
+  const size_t nl = static_cast<size_t>(n_z) * n_x;
+  for (size_t i = 0; i < nl * n_theta; ++i) {
+    if (!mask[i]) continue;
+    if (mask[i] >> nb) return MBIR_EINVAL;
+    for (int b = 0; b < nb; ++b)
+      if (((mask[i] >> b) & 1u) && (lo[i] + b < 0 || lo[i] + b >= n_r)) return MBIR_EINVAL;
+  }
+  try {
+    mbir::LevelScheduleIn in{n_z, n_x, n_theta, n_r, nb, 1, nullptr, lineok, active, lo, mask};
+    mbir::LevelScheduleWork w;
+    std::vector<int32_t> out, ofs;
+    const int colours = mbir::colour_schedule(in, max_colours, class_cap, w, out, ofs);
+    if (colours < 0) return MBIR_EINVAL;
+    if (static_cast<int64_t>(out.size()) > lines_cap ||
+        static_cast<int64_t>(ofs.size()) > lofs_cap)
+      return MBIR_EINVAL;
+    std::copy(out.begin(), out.end(), lines);
+    std::copy(ofs.begin(), ofs.end(), lofs);
+    *n_lines = static_cast<int32_t>(out.size());
+    *n_colours = colours;
     return MBIR_OK;
   } catch (...) {
     return MBIR_ENOMEM;

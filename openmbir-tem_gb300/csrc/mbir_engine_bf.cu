@@ -146,7 +146,8 @@ int Engine::bf_upload() {
 // bin and nonzero mask, from which every call's dependency levels are computed.  Without room
 // for the table the calls walk the rows.
 int Engine::bf_prepare_schedule() {
-  if (fp64_ || !p_.nhicd || p_.order_mode != MBIR_ORDER_PARALLEL || p_.row_walk) return MBIR_OK;
+  if (fp64_ || !p_.nhicd || p_.order_mode != MBIR_ORDER_PARALLEL || p_.call_schedule == 1)
+    return MBIR_OK;
   const Geometry& g = g_;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
   const size_t nl = static_cast<size_t>(g.n_z) * g.n_x;
@@ -173,9 +174,13 @@ int Engine::bf_prepare_schedule() {
   return MBIR_OK;
 }
 
-// The call's dependency levels over the row walk's visit order (rows, then classes), uploaded
-// for the sweep; leaves `a` walking the rows when the engine has no A-column table.
+// The call's schedule, uploaded for the sweep: colour classes of its conflict graph
+// (call_schedule 0; the levels of the row walk when more colours than kMaxColours would be
+// needed) or the dependency levels of the row walk (call_schedule 2).  The call's visit order
+// (call_lines_) becomes the schedule's line order.  Leaves `a` walking the rows when the engine
+// has no A-column table.
 int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
+  constexpr int kMaxColours = 512;
   if (d_acol_ == nullptr) return MBIR_OK;
   const Geometry& g = g_;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
@@ -183,8 +188,14 @@ int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
   LevelScheduleIn in{g.n_z, g.n_x, g.n_theta, g.n_r, nb_, stride_, rows.data(),
                      tab_.line_nonempty.data(), active_host_.data(), acol_lo_.data(),
                      acol_mask_.data()};
-  const int levels = level_schedule(in, sched_work_, sched_lines_, sched_lofs_);
-  if (levels < 0) return fail(MBIR_EINVAL, "level schedule: invalid row order");
+  int levels = -2;
+  // a colour class holds at most as many lines as the kernel has voxel groups
+  const int groups = kWarps * (shape_ == 1 ? 2 : 1);
+  if (p_.call_schedule == 0)
+    levels = colour_schedule(in, kMaxColours, groups, sched_work_, sched_lines_, sched_lofs_);
+  if (levels == -2) levels = level_schedule(in, sched_work_, sched_lines_, sched_lofs_);
+  if (levels < 0) return fail(MBIR_EINVAL, "call schedule: invalid row order");
+  call_lines_ = sched_lines_;
   sched_ms_ += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
                    .count();
   n_levels_ = levels;

@@ -90,6 +90,126 @@ int level_schedule(const LevelScheduleIn& in, LevelScheduleWork& w, std::vector<
   return max_level;
 }
 
+// Colouring: the same independence argument as the levels above, with the visit order chosen
+// for few barrier steps instead of given.  Colour classes are independent sets of the conflict
+// graph; running them in colour order is the sequential ICD of the order "all lines of colour
+// 0, then colour 1, ...", whose result does not depend on the order inside a class.  A 1/20 NHICD
+// call of a 128 x 512 plane with 61 views needs about 0.45 times as many colours as the row
+// walk needs levels.
+// Colour sets are bit planes: word k of bin (v, j) at bin_used[k][v][j] and of line l at
+// line_used[k][l], so the few words in use (colours < 64 * used words) stay cache-resident.
+// zero the colour-set words (planes 0..words-1, the planes in use) of every line coloured so
+// far (w.order) and of its bins
+static void colour_clear(const LevelScheduleIn& in, int words, LevelScheduleWork& w) {
+  const int nt = in.n_theta, nr = in.n_r, nb = in.nb;
+  const size_t bplane = static_cast<size_t>(nt) * nr;
+  const size_t lplane = static_cast<size_t>(in.n_z) * in.n_x;
+  for (int32_t l : w.order) {
+    const int16_t* lo = in.lo + static_cast<size_t>(l) * nt;
+    const uint16_t* mk = in.mask + static_cast<size_t>(l) * nt;
+    for (int v = 0; v < nt; ++v) {
+      const unsigned bits = mk[v];
+      if (!bits) continue;
+      const size_t j0 = static_cast<size_t>(v) * nr + lo[v];
+      for (int k = 0; k < words; ++k)
+        for (int b = 0; b < nb; ++b)
+          if ((bits >> b) & 1u) w.bin_used[k * bplane + j0 + b] = 0;
+    }
+    for (int k = 0; k < words; ++k) w.line_used[k * lplane + l] = 0;
+  }
+}
+
+// Colouring: the same independence argument as the levels above, with the visit order chosen
+// for few barrier steps instead of given.  Colour classes are independent sets of the conflict
+// graph; running them in colour order is the sequential ICD of the order "all lines of colour
+// 0, then colour 1, ...", whose result does not depend on the order inside a class.  A 1/20 NHICD
+// call of a 128 x 512 plane with 61 views needs about 0.45 times as many colours as the row
+// walk needs levels.
+int colour_schedule(const LevelScheduleIn& in, int max_colours, int class_cap,
+                    LevelScheduleWork& w, std::vector<int32_t>& lines,
+                    std::vector<int32_t>& lofs) {
+  const int nz = in.n_z, nx = in.n_x, nt = in.n_theta, nr = in.n_r, nb = in.nb;
+  if (nz <= 0 || nx <= 0 || nt <= 0 || nr <= 0 || nb <= 0 || nb > 16 || max_colours <= 0)
+    return -1;
+  const int words = (max_colours + 63) / 64;
+  const size_t bplane = static_cast<size_t>(nt) * nr, lplane = static_cast<size_t>(nz) * nx;
+  // the colour-set planes stay allocated between calls; a call clears what it set
+  if (w.bin_used.size() != bplane * words) w.bin_used.assign(bplane * words, 0);
+  if (w.line_used.size() != lplane * words) w.line_used.assign(lplane * words, 0);
+  w.order.clear();
+  w.level.clear();
+  int n_colours = 0;
+  std::vector<uint64_t> forbid(words), full(words, 0);
+  w.class_size.assign(static_cast<size_t>(words) * 64, 0);
+  for (int z = 0; z < nz; ++z) {
+    for (int x = 0; x < nx; ++x) {
+      const size_t l = static_cast<size_t>(z) * nx + x;
+      if (!in.lineok[l] || (in.active != nullptr && !in.active[l])) continue;
+      const int16_t* lo = in.lo + l * nt;
+      const uint16_t* mk = in.mask + l * nt;
+      const int used_words = std::min(n_colours / 64 + 1, words);
+      std::copy(full.begin(), full.end(), forbid.begin());
+      for (int k = 0; k < used_words; ++k) {
+        const uint64_t* plane = w.bin_used.data() + k * bplane;
+        uint64_t f = forbid[k];
+        for (int v = 0; v < nt; ++v) {
+          const unsigned bits = mk[v];
+          if (!bits) continue;
+          const uint64_t* row = plane + static_cast<size_t>(v) * nr + lo[v];
+          for (int b = 0; b < nb; ++b)
+            if ((bits >> b) & 1u) f |= row[b];
+        }
+        const uint64_t* lp = w.line_used.data() + k * lplane;
+        for (int dz = -1; dz <= 1; ++dz) {
+          const int zz = z + dz;
+          if (zz < 0 || zz >= nz) continue;
+          for (int dx = -1; dx <= 1; ++dx) {
+            const int xx = x + dx;
+            if (xx >= 0 && xx < nx) f |= lp[static_cast<size_t>(zz) * nx + xx];
+          }
+        }
+        forbid[k] = f;
+      }
+      int col = -1;
+      for (int k = 0; k < words && col < 0; ++k)
+        if (~forbid[k]) {
+          const uint64_t free_bits = ~forbid[k];
+          int b = 0;
+          while (!((free_bits >> b) & 1ull)) ++b;
+          col = 64 * k + b;
+        }
+      if (col < 0 || col >= max_colours) {
+        colour_clear(in, std::min(n_colours / 64 + 1, words), w);
+        return -2;
+      }
+      const uint64_t bit = 1ull << (col & 63);
+      const int wk = col >> 6;
+      uint64_t* plane = w.bin_used.data() + wk * bplane;
+      for (int v = 0; v < nt; ++v) {
+        const unsigned bits = mk[v];
+        if (!bits) continue;
+        uint64_t* row = plane + static_cast<size_t>(v) * nr + lo[v];
+        for (int b = 0; b < nb; ++b)
+          if ((bits >> b) & 1u) row[b] |= bit;
+      }
+      w.line_used[wk * lplane + l] |= bit;
+      if (class_cap > 0 && ++w.class_size[col] >= class_cap) full[wk] |= bit;
+      w.order.push_back(static_cast<int32_t>(l));
+      w.level.push_back(col + 1);
+      if (col + 1 > n_colours) n_colours = col + 1;
+    }
+  }
+  colour_clear(in, std::min((n_colours + 63) / 64, words), w);
+  lofs.assign(static_cast<size_t>(n_colours) + 1, 0);
+  for (int L : w.level) lofs[L]++;
+  for (int L = 1; L <= n_colours; ++L) lofs[L] += lofs[L - 1];
+  lines.assign(w.order.size(), 0);
+  std::vector<int32_t>& pos = w.pos;
+  pos.assign(lofs.begin(), lofs.end() - 1);
+  for (size_t i = 0; i < w.order.size(); ++i) lines[pos[w.level[i] - 1]++] = w.order[i];
+  return n_colours;
+}
+
 // Per-view first bin and nonzero-bin mask of every voxel line from the A-column table
 // ([line][view][acol_width(nb) float4]: first bin as int bits, then nb values).
 void acol_bins(const float* table, int n_lines, int n_theta, int nb, int16_t* lo,

@@ -83,7 +83,7 @@ class MbirParams(C.Structure):
         ("slice_staging", C.c_int32),
         ("nhicd", C.c_int32),
         ("lane_shape", C.c_int32),
-        ("row_walk", C.c_int32),
+        ("call_schedule", C.c_int32),
     ]
 
 
@@ -178,12 +178,41 @@ SIGNATURES = {
     "mbir_server_last_error": (C.c_char_p, [C.c_void_p]),
     "mbir_run_multires": (C.c_int32, [C.POINTER(MbirParams), _F, _F, C.c_int32, C.c_int32,
                                       C.c_int32, C.c_double, C.c_double, _F, C.c_int64, _I]),
+    "mbir_colour_schedule": (C.c_int32, [C.c_int32] * 7 + [C.POINTER(C.c_uint8),
+                                                           C.POINTER(C.c_uint8),
+                                                           C.POINTER(C.c_int16),
+                                                           C.POINTER(C.c_uint16), _I, C.c_int32,
+                                                           _I, C.c_int32, _I, _I]),
     "mbir_level_schedule": (C.c_int32, [C.c_int32] * 6 + [_I, C.POINTER(C.c_uint8),
                                                           C.POINTER(C.c_uint8),
                                                           C.POINTER(C.c_int16),
                                                           C.POINTER(C.c_uint16), _I, C.c_int32,
                                                           _I, C.c_int32, _I, _I]),
 }
+
+
+def colour_schedule(lineok, lo, mask, nb, n_r, active=None, max_colours=512, class_cap=0):
+    """Colour schedule of a sparse ICD call (mbir_colour_schedule): returns (lines, lofs)."""
+    lineok = np.ascontiguousarray(lineok, np.uint8)
+    n_z, n_x = lineok.shape
+    lo = np.ascontiguousarray(lo, np.int16)
+    mask = np.ascontiguousarray(mask, np.uint16)
+    act = None if active is None else np.ascontiguousarray(active, np.uint8)
+    cap = n_z * n_x
+    lines = np.zeros(cap, np.int32)
+    lofs = np.zeros(cap + 1, np.int32)
+    nl = C.c_int32()
+    nc = C.c_int32()
+    u8 = C.POINTER(C.c_uint8)
+    rc = lib().mbir_colour_schedule(
+        n_z, n_x, lo.shape[2], int(n_r), int(nb), int(max_colours), int(class_cap),
+        lineok.ctypes.data_as(u8),
+        None if act is None else act.ctypes.data_as(u8), lo.ctypes.data_as(C.POINTER(C.c_int16)),
+        mask.ctypes.data_as(C.POINTER(C.c_uint16)), lines.ctypes.data_as(_I), cap,
+        lofs.ctypes.data_as(_I), cap + 1, C.byref(nl), C.byref(nc))
+    if rc != 0:
+        raise MbirError(rc, "mbir_colour_schedule failed")
+    return lines[:nl.value].copy(), lofs[:nc.value + 1].copy()
 
 
 def level_schedule(rows, lineok, lo, mask, nb, stride, n_r, active=None):

@@ -1305,6 +1305,21 @@ void orc_bf_sweep_slices(orc_ctx* c, const unsigned char* active, const int32_t*
       }
 }
 
+/* The same call with every voxel slice visiting the call's lines in the given order (the
+ * GPU's scheduled calls: colour classes one after another); slices in colour order as above. */
+void orc_bf_sweep_slices_order(orc_ctx* c, const int32_t* lines, int n_lines, int outer,
+                               int inner, double* stats) {
+  stats[0] = stats[1] = stats[2] = stats[3] = 0;
+  for (int n = 0; n < n_lines; n++) c->mag_map[lines[n]] = 0;
+  for (int colour = 0; colour < 2; colour++)
+    for (int i = colour; i < c->n_y; i += 2)
+      for (int n = 0; n < n_lines; n++) {
+        int l = lines[n];
+        if (c->col_count[l] > 0)
+          bf_update_voxel(c, l / c->n_x, l % c->n_x, i, outer, inner, stats, c->mag_map);
+      }
+}
+
 /* ComputeVSC (BFReconstructionEngine_Extra.cpp:888-947): 5x5 Hamming window
  * (BFReconstructionEngine.cpp:157-185) over the update-magnitude map, zero outside. */
 static const double k_hamming[5][5] = {{0.0013, 0.0086, 0.0159, 0.0086, 0.0013},

@@ -136,6 +136,9 @@ void orc_bf_sweep_lines(orc_ctx* c, const int32_t* lines, int n_lines, int outer
 /* the same call in the GPU's slice order over the lines with active[z*n_x+x] != 0 */
 void orc_bf_sweep_slices(orc_ctx* c, const unsigned char* active, const int32_t* row_order,
                          int stride, int outer, int inner, double* stats);
+/* the same call with each slice visiting the given lines (z*n_x+x) in the given order */
+void orc_bf_sweep_slices_order(orc_ctx* c, const int32_t* lines, int n_lines, int outer,
+                               int inner, double* stats);
 void orc_bf_vsc(orc_ctx* c);
 double orc_bf_nh_threshold(const orc_ctx* c);
 int orc_bf_nh_lines(const orc_ctx* c, double threshold, int32_t* lines);

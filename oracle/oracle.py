@@ -89,6 +89,7 @@ def lib():
             "orc_rand_list_perm": (None, [C.c_uint32, C.c_int, _I]),
             "orc_bf_sweep_lines": (None, [C.c_void_p, _I, C.c_int, C.c_int, C.c_int, _D]),
             "orc_bf_sweep_slices": (None, [C.c_void_p, _U8, _I, C.c_int, C.c_int, C.c_int, _D]),
+            "orc_bf_sweep_slices_order": (None, [C.c_void_p, _I, C.c_int, C.c_int, C.c_int, _D]),
             "orc_bf_vsc": (None, [C.c_void_p]),
             "orc_bf_nh_threshold": (C.c_double, [C.c_void_p]),
             "orc_bf_nh_lines": (C.c_int, [C.c_void_p, C.c_double, _I]),
@@ -340,6 +341,14 @@ class Oracle:
         st = np.zeros(4)
         lib().orc_bf_sweep_slices(self._h, active.ctypes.data_as(_U8), rows.ctypes.data_as(_I),
                                   stride, outer, inner, st.ctypes.data_as(_D))
+        return st
+
+    def bf_sweep_slices_order(self, lines, outer=0, inner=0):
+        """The slice-parallel call with every slice visiting `lines` in the given order."""
+        lines = np.ascontiguousarray(lines, np.int32)
+        st = np.zeros(4)
+        lib().orc_bf_sweep_slices_order(self._h, lines.ctypes.data_as(_I), len(lines), outer,
+                                        inner, st.ctypes.data_as(_D))
         return st
 
     def bf_sweep_lines_mt(self, lines, outer=0, inner=0, threads=None):

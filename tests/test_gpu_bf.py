@@ -61,20 +61,25 @@ def test_bf_call_matches_oracle_same_order(lib_built, oracle_mod, precision, bra
     calls almost every touched entry crosses T, so FP32 rounding flips decisions at the
     threshold and the FP32 engine is compared with the selector off (T = 5e10); the FP64 engine
     is compared at T = 3 with the selector switching."""
-    e, o, p, y = pair(lib_built, oracle_mod, precision=precision, bragg_threshold=bragg)
+    e, o, p, y = pair(lib_built, oracle_mod, precision=precision, bragg_threshold=bragg,
+                      call_schedule=0)
     e.prepare()
     o.prepare()
     nz, nx = e.dims()[:2]
     for k in range(2):
         rows, stride = e.schedule(k)
         sg = e.sweep(0, k)
-        lines = e.call_lines()
+        lines = e.call_lines()  # FP32: the coloured visit order; FP64: ascending (row walk)
         if k == 1:  # the NH list: lines whose filtered magnitude exceeds the 1/20 percentile
             o.bf_vsc()
-            np.testing.assert_array_equal(lines, o.bf_nh_lines(o.bf_nh_threshold()))
+            np.testing.assert_array_equal(np.sort(lines), o.bf_nh_lines(o.bf_nh_threshold()))
         active = np.zeros(nz * nx, np.uint8)
         active[lines] = 1
-        so = o.bf_sweep_slices(active, rows, stride, 0, k)
+        if precision == 0:
+            assert e.status().sched_levels > 0
+            so = o.bf_sweep_slices_order(lines, 0, k)
+        else:
+            so = o.bf_sweep_slices(active, rows, stride, 0, k)
         assert sg[3] == so[3] and sg[2] == so[2], (k, sg, so)
         assert rel(e.volume(), o.volume()) <= max(tol, 1e-7), (k, rel(e.volume(), o.volume()))
         assert rel(e.error_sinogram(), o.error()) <= max(tol, 1e-7), k
@@ -149,8 +154,8 @@ def test_bf_level_schedule_bitwise_row_walk(lib_built, oracle_mod, staging):
     mbir = lib_built
     y, ang, th = bf_case()
     out = []
-    for row_walk in (0, 1):
-        p = bf_params(mbir, th, outer_iterations=3, inner_iterations=4, row_walk=row_walk,
+    for sched in (2, 1):
+        p = bf_params(mbir, th, outer_iterations=3, inner_iterations=4, call_schedule=sched,
                       slice_staging=staging, seed=7)
         e = mbir.Engine(p)
         e.set_sinogram(y, ang)

@@ -160,3 +160,97 @@ def test_schedule_rejects_bad_input(lib_built):
     badlo[1, 1, 1] = n_r                  # touched bin past the detector
     with pytest.raises(mbir.MbirError):
         mbir.level_schedule(np.arange(n_z, dtype=np.int32), lineok, badlo, mask, nb, 2, n_r)
+
+
+def py_colour(lineok, active, lo, mask, nb, cap=0):
+    """Greedy colouring by definition: lines z-major, smallest colour no conflicting earlier
+    line holds and with fewer than cap lines (cap 0: no limit)."""
+    n_z, n_x, n_t = lo.shape
+    col = {}
+    bins = {}
+    for z in range(n_z):
+        for x in range(n_x):
+            if not lineok[z, x] or (active is not None and not active[z, x]):
+                continue
+            used = set()
+            mine = [(v, int(lo[z, x, v]) + b) for v in range(n_t) for b in range(nb)
+                    if (int(mask[z, x, v]) >> b) & 1]
+            for key in mine:
+                used |= bins.get(key, set())
+            for zz in range(max(z - 1, 0), min(z + 2, n_z)):
+                for xx in range(max(x - 1, 0), min(x + 2, n_x)):
+                    if (zz, xx) in col:
+                        used.add(col[(zz, xx)])
+            c = 0
+            while c in used or (cap and sum(1 for q in col.values() if q == c) >= cap):
+                c += 1
+            col[(z, x)] = c
+            for key in mine:
+                bins.setdefault(key, set()).add(c)
+    n = max(col.values()) + 1 if col else 0
+    lines = [z * n_x + x for c in range(n) for (z, x), q in sorted(col.items()) if q == c]
+    lofs = [0]
+    for c in range(n):
+        lofs.append(lofs[-1] + sum(1 for q in col.values() if q == c))
+    return np.array(lines, np.int32), np.array(lofs, np.int32)
+
+
+def check_independent(lines, lofs, lo, mask, nb):
+    """No two lines of one colour class share a touched bin or are 3x3 (z, x) neighbours."""
+    n_z, n_x, n_t = lo.shape
+    for c in range(len(lofs) - 1):
+        seen = {}
+        pos = set()
+        for l in lines[lofs[c]:lofs[c + 1]]:
+            z, x = divmod(int(l), n_x)
+            for zz in range(z - 1, z + 2):
+                for xx in range(x - 1, x + 2):
+                    assert (zz, xx) not in pos, f"colour {c}: neighbours {(z, x)}, {(zz, xx)}"
+            pos.add((z, x))
+            for v in range(n_t):
+                for b in range(nb):
+                    if (int(mask[z, x, v]) >> b) & 1:
+                        key = (v, int(lo[z, x, v]) + b)
+                        assert key not in seen, f"colour {c}: bin {key} shared"
+                        seen[key] = l
+
+
+def test_colour_schedule_matches_definition(lib_built):
+    mbir = lib_built
+    rng = np.random.default_rng(12)
+    n_z, n_x, n_r = 7, 24, 28
+    lo, mask, nb = footprints(n_z, n_x, n_r, np.arange(-60, 61, 24))
+    lineok = (rng.random((n_z, n_x)) < 0.9).astype(np.uint8)
+    for frac, cap in ((1.0, 0), (0.3, 0), (0.05, 0), (1.0, 3), (0.3, 2)):
+        active = (rng.random((n_z, n_x)) < frac).astype(np.uint8)
+        lines, lofs = mbir.colour_schedule(lineok, lo, mask, nb, n_r, active, class_cap=cap)
+        pl, po = py_colour(lineok, active, lo, mask, nb, cap)
+        np.testing.assert_array_equal(lines, pl)
+        np.testing.assert_array_equal(lofs, po)
+        check_independent(lines, lofs, lo, mask, nb)
+        if cap:
+            assert np.diff(lofs).max() <= cap
+
+
+def test_colour_schedule_bright_field_call_shape(lib_built):
+    """A 1/20 NHICD call on a 64 x 256 plane, 61 views over +-60 deg: every class independent,
+    every line once, and fewer classes than the row walk's dependency levels."""
+    mbir = lib_built
+    rng = np.random.default_rng(5)
+    n_z, n_x, n_r = 64, 256, 256
+    lo, mask, nb = footprints(n_z, n_x, n_r, np.arange(-60, 61, 2))
+    lineok = (mask != 0).any(axis=2).astype(np.uint8)
+    active = np.zeros(n_z * n_x, np.uint8)
+    active[rng.permutation(n_z * n_x)[: n_z * n_x // 20]] = 1
+    active = active.reshape(n_z, n_x)
+    lines, lofs = mbir.colour_schedule(lineok, lo, mask, nb, n_r, active)
+    check_independent(lines, lofs, lo, mask, nb)
+    assert sorted(lines.tolist()) == sorted(np.flatnonzero(active & lineok).tolist())
+    rows = rng.permutation(n_z).astype(np.int32)
+    _, lvl = mbir.level_schedule(rows, lineok, lo, mask, nb, 6, n_r, active)
+    assert len(lofs) < len(lvl)
+    capped, cofs = mbir.colour_schedule(lineok, lo, mask, nb, n_r, active, class_cap=16)
+    check_independent(capped, cofs, lo, mask, nb)
+    assert np.diff(cofs).max() <= 16 and sorted(capped.tolist()) == sorted(lines.tolist())
+    with pytest.raises(mbir.MbirError):  # more colours needed than allowed
+        mbir.colour_schedule(lineok, lo, mask, nb, n_r, active, max_colours=4)
