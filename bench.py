@@ -387,6 +387,8 @@ def main():
     ap.add_argument("--series", type=int, default=64, help="batch/serve: number of requests")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--call-schedule", type=int, default=None,
+                    help="BF NHICD call schedule (0 colour classes, 1 row walk, 2 levels)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -416,6 +418,8 @@ def main():
     bf = mod == "BF"
     p = params_for(mbir, th, mod)
     p.device = local
+    if args.call_schedule is not None:
+        p.call_schedule = args.call_schedule
     eng = mbir.Engine(p)
     eng.set_sinogram(y, ang)
     eng.prepare()
@@ -523,6 +527,8 @@ def main():
         n_outer = CALLS_PER_EQUIT if bf else 3
         pe = params_for(mbir, th, mod, outer=n_outer, inner=1)
         pe.device = local
+        if args.call_schedule is not None:
+            pe.call_schedule = args.call_schedule
         host_vol = np.empty((nz, nx, ny), np.float32)
         barrier()
         t0 = time.perf_counter()

@@ -123,7 +123,8 @@ typedef struct mbir_params {
                                  rows class by class, 2 = the row walk's visit order run in
                                  dependency levels (one barrier per level, the row walk's
                                  bits).  mbir_get_call_lines returns the visit order of 0 and 2.
-                                 Default 2. */
+                                 The colouring runs on the device; the schedules of the 20
+                                 homogeneous sub-lists are built once and reused. */
 } mbir_params;
 
 typedef struct mbir_status {
@@ -345,6 +346,20 @@ int32_t mbir_level_schedule(int32_t n_z, int32_t n_x, int32_t n_theta, int32_t n
  * MBIR_EINVAL on bad input, short buffers or more than max_colours (<= 4096) colours.  Replaces
  * no reference interface (the reference draws a random visit order per call,
  * BFReconstructionEngine_Extra.cpp:576-628). */
+/* The last scheduled BF call's schedule (call_schedule 0 or 2): its lines level by level
+ * (lines[cap]) and the level offsets (lofs[lofs_cap], n_levels + 1 values); *n_lines and
+ * *n_levels receive the counts (0 after a row-walk call).  Any pointer may be NULL.  No
+ * counterpart in the reference (its calls run one line after another). */
+int32_t mbir_get_call_schedule(mbir_engine* e, int32_t* lines, int32_t cap, int32_t* lofs,
+                               int32_t lofs_cap, int32_t* n_lines, int32_t* n_levels);
+/* The footprint support the schedules use, for a prepared FP32 BF engine with NHICD: per line
+ * l = z*n_x + x and view v, lo[l*n_theta + v] = first detector bin and bit b of
+ * mask[l*n_theta + v] = bin lo+b has a nonzero FP32 A-matrix entry; lineok[l] = the line's
+ * A-column is not empty.  MBIR_ENOTSUP when the engine builds no schedules.  Mirrors the A-column
+ * support of AMatrixCol (Code/MBIRLib/Common/AMatrixCol.cpp:148-232). */
+int32_t mbir_get_footprint_bins(mbir_engine* e, int16_t* lo, uint16_t* mask,
+                                uint8_t* lineok);
+
 int32_t mbir_colour_schedule(int32_t n_z, int32_t n_x, int32_t n_theta, int32_t n_r, int32_t nb,
                              int32_t max_colours, int32_t class_cap, const uint8_t* lineok,
                              const uint8_t* active,

@@ -22,7 +22,7 @@ SOURCES = ["mbir_sweep_f32.cu", "mbir_sweep_f32_bf.cu", "mbir_sweep_f32_hbm.cu",
            "mbir_kernels.cu",
            "mbir_exact.cu", "mbir_bf.cu", "mbir_noalloc.cu",
            "mbir_engine.cu", "mbir_engine_bf.cu", "mbir_shard.cu", "mbir_batch.cu", "mbir_server.cpp", "mrc_io.cpp",
-           "mbir_schedule.cpp", "mbir_capi.cpp"]
+           "mbir_schedule.cpp", "mbir_colour.cu", "mbir_capi.cpp"]
 HEADERS = ["mbir_internal.h", "mbir_engine.h", "mbir_sweep.cuh", "mbir_batch.h",
            "mbir_server.h", "mbir_schedule.h"]
 

@@ -100,7 +100,6 @@ void mbir_params_default(mbir_params* p, int32_t modality) {
     p->noise_estimation = 1;
     p->noise_model = 0;
     p->nhicd = 1;  // NHICD is defined in BFConstants.h
-    p->call_schedule = 2;
   }
 }
 
@@ -207,6 +206,15 @@ int32_t mbir_get_schedule(mbir_engine* e, int32_t sweep, int32_t* rows, int32_t*
 }
 int32_t mbir_get_call_lines(mbir_engine* e, int32_t* lines, int32_t cap, int32_t* n) {
   return guarded(e, [&](mbir::Engine& m) { return m.get_call_lines(lines, cap, n); });
+}
+int32_t mbir_get_call_schedule(mbir_engine* e, int32_t* lines, int32_t cap, int32_t* lofs,
+                               int32_t lofs_cap, int32_t* n_lines, int32_t* n_levels) {
+  return guarded(e, [&](mbir::Engine& m) {
+    return m.get_call_schedule(lines, cap, lofs, lofs_cap, n_lines, n_levels);
+  });
+}
+int32_t mbir_get_footprint_bins(mbir_engine* e, int16_t* lo, uint16_t* mask, uint8_t* lineok) {
+  return guarded(e, [&](mbir::Engine& m) { return m.get_footprint_bins(lo, mask, lineok); });
 }
 int32_t mbir_get_bf_state(mbir_engine* e, uint8_t* selector, float* weights, double* mag,
                           double* filtered_mag, double* bragg_t) {

@@ -1,0 +1,288 @@
+// mbir_colour.cu -- the colour schedule of a sparse ICD call, built on the device.
+//
+// Same result as colour_schedule (mbir_schedule.cpp), the host definition: the call's voxel
+// lines (non-empty A-column, in the call's active mask) are visited in ascending line order
+// (z-major); each takes the smallest colour that no earlier conflicting line holds and whose
+// class has fewer than class_cap lines.  Two lines conflict when they touch a common detector
+// bin at some view or are 3x3 (z, x) neighbours.  Output: the lines colour by colour (ascending
+// within a colour), the colour offsets and the counts, all in device memory, so the sweep that
+// follows reads them without a host round trip.
+//
+// One CTA of 1024 threads.  Lines are coloured 32 at a time: every warp ORs the colour sets of
+// its line's bins (bit planes in global memory, L2-resident) into the set of colours taken by
+// earlier blocks; the 32 x 32 conflict matrix of the block comes from the lines' footprints
+// staged in shared memory; warp 0 then assigns the 32 colours in order, which is the
+// sequential greedy choice because each line sees the colours of the earlier lines of its
+// block that it conflicts with; finally the block's colours are ORed into the bit planes.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "mbir_internal.h"
+
+namespace mbir {
+namespace {
+
+constexpr int kThreads = 1024;
+constexpr int kBlock = 32;  // lines coloured per step
+
+__device__ __forceinline__ bool bins_overlap(int32_t pi, int32_t pj) {
+  const unsigned mi = static_cast<unsigned>(pi) & 0xffffu, mj = static_cast<unsigned>(pj) & 0xffffu;
+  if (!mi || !mj) return false;
+  const int d = (pj >> 16) - (pi >> 16);  // first bins: lo_j - lo_i
+  if (d >= 16 || d <= -16) return false;
+  return d >= 0 ? ((mj << d) & mi) != 0u : ((mi << -d) & mj) != 0u;
+}
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int* warp_sums, int* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int n = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += n;
+  }
+  if (lane == 31) warp_sums[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const int s = warp_sums[lane];
+    int si = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int n = __shfl_up_sync(0xffffffffu, si, o);
+      if (lane >= o) si += n;
+    }
+    warp_sums[lane] = si - s;
+    if (lane == 31) *total = si;
+  }
+  __syncthreads();
+  return warp_sums[warp] + incl - v;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int W = A.words;
+  const int nt = A.n_theta, nx = A.n_x, nl = A.n_z * A.n_x;
+  int32_t* pk = reinterpret_cast<int32_t*>(smem);                     // [kBlock][nt]
+  unsigned long long* F = reinterpret_cast<unsigned long long*>(pk + kBlock * nt);  // [kBlock][W]
+  int* csize = reinterpret_cast<int*>(F + kBlock * W);                // [64 W] class sizes
+  __shared__ unsigned conf[kBlock];
+  __shared__ int col[kBlock];
+  __shared__ int vline[kBlock], vz[kBlock], vx[kBlock];
+  __shared__ int warp_sums[32];
+  __shared__ unsigned long long full_s[8];
+  __shared__ int s_total, s_ncol, s_fail;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  for (int c = tid; c < 64 * W; c += kThreads) csize[c] = 0;
+  if (tid < 8) full_s[tid] = 0ull;
+  if (tid == 0) {
+    s_ncol = 0;
+    s_fail = 0;
+  }
+  // phase 0: the call's lines in ascending order (coalesced chunks of kThreads lines)
+  int n = 0;
+  for (int c0 = 0; c0 < nl; c0 += kThreads) {
+    const int l = c0 + tid;
+    const bool f = l < nl && A.lineok[l] && (A.active == nullptr || A.active[l]);
+    const int p = block_exclusive_scan(f ? 1 : 0, warp_sums, &s_total);
+    if (f) A.vis[n + p] = l;
+    n += s_total;
+    __syncthreads();
+  }
+
+  // phase 1: colour kBlock lines per step
+  for (int s = 0; s < n; s += kBlock) {
+    const int m = min(kBlock, n - s);
+    const int uw = min(s_ncol / 64 + 1, W);  // words holding colours so far
+    if (warp < m) {
+      const int l = A.vis[s + warp];
+      const int z = l / nx, x = l - z * nx;
+      unsigned long long f[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) f[k] = 0ull;
+      for (int v = lane; v < nt; v += 32) {
+        const int32_t p = A.packed[static_cast<size_t>(l) * nt + v];
+        pk[warp * nt + v] = p;
+        const unsigned mk = static_cast<unsigned>(p) & 0xffffu;
+        const int lo = p >> 16;
+        for (int b = 0; b < A.nb; ++b)
+          if ((mk >> b) & 1u) {
+            const unsigned long long* row =
+                A.bin_used + (static_cast<size_t>(v) * A.n_r + lo + b) * W;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+              if (k < uw) f[k] |= __ldcg(row + k);
+          }
+      }
+      if (lane < 9) {
+        const int zz = z + lane / 3 - 1, xx = x + lane % 3 - 1;
+        if (zz >= 0 && zz < A.n_z && xx >= 0 && xx < nx) {
+          const unsigned long long* nb = A.line_used + (static_cast<size_t>(zz) * nx + xx) * W;
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            if (k < uw) f[k] |= __ldcg(nb + k);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) f[k] |= __shfl_xor_sync(0xffffffffu, f[k], o);
+      }
+      if (lane == 0) {
+        for (int k = 0; k < W; ++k) F[warp * W + k] = k < 8 ? f[k] : 0ull;
+        vline[warp] = l;
+        vz[warp] = z;
+        vx[warp] = x;
+      }
+    }
+    __syncthreads();
+    // conflicts with earlier lines of the block: warp i tests its line against line j < i on
+    // lane j, over every view
+    if (warp < m) {
+      const int i = warp, j = lane;
+      bool c = false;
+      if (j < i) {
+        c = abs(vz[i] - vz[j]) <= 1 && abs(vx[i] - vx[j]) <= 1;
+        for (int v = 0; v < nt && !c; ++v) c = bins_overlap(pk[i * nt + v], pk[j * nt + v]);
+      }
+      const unsigned b = __ballot_sync(0xffffffffu, c);
+      if (lane == 0) conf[i] = b;
+    }
+    __syncthreads();
+    // warp 0: the greedy choice, line by line
+    if (warp == 0) {
+      unsigned long long acc[8], full[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        acc[k] = (lane < m && k < W) ? F[lane * W + k] : 0ull;
+        full[k] = full_s[k];  // classes already full
+      }
+      const unsigned my_conf = lane < m ? conf[lane] : 0u;
+      int ncol = s_ncol;
+      for (int i = 0; i < m; ++i) {
+        int c = -1;
+        if (lane == i) {
+          for (int k = 0; k < W && k < 8 && c < 0; ++k) {
+            const unsigned long long freeb = ~(acc[k] | full[k]);
+            if (freeb) c = 64 * k + __ffsll(static_cast<long long>(freeb)) - 1;
+          }
+        }
+        c = __shfl_sync(0xffffffffu, c, i);
+        if (c < 0 || c >= A.max_colours) {
+          if (lane == 0) s_fail = 1;
+          break;
+        }
+        if ((my_conf >> i) & 1u) acc[c >> 6] |= 1ull << (c & 63);
+        int sz = 0;
+        if (lane == 0) {
+          sz = ++csize[c];
+          col[i] = c;
+        }
+        sz = __shfl_sync(0xffffffffu, sz, 0);
+        if (A.class_cap > 0 && sz >= A.class_cap) full[c >> 6] |= 1ull << (c & 63);
+        ncol = max(ncol, c + 1);
+      }
+      if (lane == 0) {
+        s_ncol = ncol;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) full_s[k] = full[k];
+      }
+    }
+    __syncthreads();
+    if (s_fail) break;
+    // record the colours and set them in the bins and lines
+    if (warp < m) {
+      const int c = col[warp], l = vline[warp];
+      const unsigned long long bit = 1ull << (c & 63);
+      const int wk = c >> 6;
+      for (int v = lane; v < nt; v += 32) {
+        const int32_t p = pk[warp * nt + v];
+        const unsigned mk = static_cast<unsigned>(p) & 0xffffu;
+        const int lo = p >> 16;
+        for (int b = 0; b < A.nb; ++b)
+          if ((mk >> b) & 1u)
+            atomicOr(A.bin_used + (static_cast<size_t>(v) * A.n_r + lo + b) * W + wk, bit);
+      }
+      if (lane == 0) {
+        atomicOr(A.line_used + static_cast<size_t>(l) * W + wk, bit);
+        A.colour[s + warp] = static_cast<int16_t>(c);
+      }
+    }
+    __threadfence_block();
+    __syncthreads();
+  }
+  if (s_fail) {
+    if (tid == 0) {
+      A.count[0] = 0;
+      A.count[1] = 0;
+      atomicOr(A.err, 4);
+    }
+    return;
+  }
+  // phase 2: colour offsets, lines colour by colour, ascending within a colour
+  const int ncol = s_ncol;
+  int cs = 0;
+  const int cper = (ncol + kThreads - 1) / kThreads;
+  const int c0 = min(tid * cper, ncol), c1 = min(c0 + cper, ncol);
+  for (int c = c0; c < c1; ++c) cs += csize[c];
+  int off = block_exclusive_scan(cs, warp_sums, &s_total);
+  for (int c = c0; c < c1; ++c) {
+    A.lofs[c] = off;
+    const int sz = csize[c];
+    csize[c] = off;  // cursor
+    off += sz;
+  }
+  if (tid == 0) {
+    A.lofs[ncol] = n;
+    A.count[0] = n;
+    A.count[1] = ncol;
+  }
+  __syncthreads();
+  for (int i = tid; i < n; i += kThreads) {
+    const int p = atomicAdd(&csize[A.colour[i]], 1);
+    A.lines[p] = A.vis[i];
+  }
+  __syncthreads();
+  __threadfence_block();
+  // sort each class ascending (classes hold at most 32 lines): one warp per class
+  for (int c = warp; c < ncol; c += kThreads / 32) {
+    const int b = A.lofs[c], e = (c + 1 < ncol) ? A.lofs[c + 1] : n;
+    int v = (lane < e - b) ? A.lines[b + lane] : 0x7fffffff;
+    // bitonic sort across the warp
+    for (int k = 2; k <= 32; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        const int o = __shfl_xor_sync(0xffffffffu, v, j);
+        const bool up = ((lane & k) == 0);
+        const bool lower = (lane & j) == 0;
+        v = (lower == up) ? min(v, o) : max(v, o);
+      }
+    if (lane < e - b) A.lines[b + lane] = v;
+  }
+}
+
+}  // namespace
+
+size_t colour_smem_bytes(int n_theta, int words) {
+  return sizeof(int32_t) * kBlock * n_theta + sizeof(unsigned long long) * kBlock * words +
+         sizeof(int) * 64 * words;
+}
+
+int launch_colour_schedule(const ColourArgs& a, void* stream) {
+  if (a.words < 1 || a.words > 8 || a.max_colours > 64 * a.words || a.class_cap < 1 ||
+      a.class_cap > 32 || a.nb > 16)
+    return -7;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t bins = static_cast<size_t>(a.n_theta) * a.n_r * a.words;
+  const size_t lines = static_cast<size_t>(a.n_z) * a.n_x * a.words;
+  cudaMemsetAsync(a.bin_used, 0, bins * sizeof(unsigned long long), s);
+  cudaMemsetAsync(a.line_used, 0, lines * sizeof(unsigned long long), s);
+  const size_t smem = colour_smem_bytes(a.n_theta, a.words);
+  if (cudaFuncSetAttribute(colour_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(smem)) != cudaSuccess)
+    return -3;
+  colour_kernel<<<1, kThreads, smem, s>>>(a);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+}  // namespace mbir

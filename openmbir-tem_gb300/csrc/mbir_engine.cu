@@ -139,6 +139,16 @@ void Engine::release() {
   dfree(d_acol_);
   dfree(d_sched_);
   dfree(d_lofs_);
+  dfree(d_packed_);
+  dfree(d_vis_);
+  dfree(d_colour_);
+  dfree(d_bin_used_);
+  dfree(d_line_used_);
+  dfree(d_sched_count_);
+  dfree(d_hc_lines_);
+  dfree(d_hc_lofs_);
+  dfree(d_hc_count_);
+  hc_valid_.clear();
   acol_lo_.clear();
   acol_mask_.clear();
   if (ev0_) cudaEventDestroy(static_cast<cudaEvent_t>(ev0_));
@@ -612,6 +622,9 @@ int Engine::check_device_error() {
   if (cudaMemcpyAsync(&h, d_err_, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return cuda_check(MBIR_EDEVICE, "device error check");
+  if (h & 4)
+    return fail(MBIR_ENOTSUP,
+                "call schedule: the call needs more than 512 colours (use call_schedule 2)");
   if (h) return fail(MBIR_ETIMEOUT, "a bounded device wait timed out");
   return 0;
 }
@@ -998,6 +1011,7 @@ int Engine::batch_finish(int outer, int inner, const double* st, double ms) {
     if (rc) return rc;
     if (cudaStreamSynchronize(static_cast<cudaStream_t>(stream_)) != cudaSuccess)
       return cuda_check(MBIR_EDEVICE, "batch call end");
+    bf_schedule_settle();
   }
   icd_ms_ += ms;
   sweeps_done_++;

@@ -78,6 +78,11 @@ class Engine {
   int get_schedule(int sweep, int32_t* row_order, int32_t* stride);
   // lines (z*n_x+x) of the last sweep/call in visit order (reference order) or ascending
   int get_call_lines(int32_t* lines, int32_t cap, int32_t* n) const;
+  // the last scheduled call's lines level by level (colour classes or levels) and offsets
+  int get_call_schedule(int32_t* lines, int32_t cap, int32_t* lofs, int32_t lofs_cap,
+                        int32_t* n_lines, int32_t* n_levels) const;
+  // first footprint bin and nonzero mask per (line, view) of the FP32 A-column, line flags
+  int get_footprint_bins(int16_t* lo, uint16_t* mask, uint8_t* lineok) const;
   // bright field: selector [theta][r][t], weights [theta][r][t], magnitude map [z][x],
   // filtered map [z][x], current Bragg threshold (each output optional)
   int get_bf_state(uint8_t* sel, float* w, double* mag, double* filt, double* bragg_t);
@@ -127,6 +132,8 @@ class Engine {
   int bf_roi_sum(int kind, double* out);
   int bf_prepare_schedule();                      // A-column table for level-scheduled calls
   int bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a);  // the call's levels
+  void bf_schedule_readback();                    // queue the device schedule's copy to host
+  void bf_schedule_settle();                      // after the stream synchronised
   BfSino bf_sino() const;
   double bf_default_offset() const;
 
@@ -263,6 +270,28 @@ class Engine {
   double sched_ms_ = 0;                     // host time spent building schedules
   LevelScheduleWork sched_work_;
   std::vector<int32_t> sched_lines_, sched_lofs_;
+  // device colour schedule (call_schedule 0)
+  int32_t* d_packed_ = nullptr;             // [n_z*n_x][n_theta] (first bin << 16) | mask
+  int32_t* d_vis_ = nullptr;                // [n_z*n_x] scratch
+  int16_t* d_colour_ = nullptr;             // [n_z*n_x] scratch
+  unsigned long long* d_bin_used_ = nullptr;   // [n_theta][n_r][kColourWords]
+  unsigned long long* d_line_used_ = nullptr;  // [n_z*n_x][kColourWords]
+  int32_t* d_sched_count_ = nullptr;        // [2] lines, colours
+  bool sched_on_device_ = false;            // the last call's schedule was built on the device
+  bool readback_pending_ = false;
+  int32_t sched_count_host_[2] = {0, 0};
+  static constexpr int kColourWords = 8;    // up to 512 colours
+  // colour schedules of the homogeneous sub-lists, which repeat every 20 calls: built once
+  int cur_hslot_ = -1;                      // sub-list of the current call, -1: not homogeneous
+  int32_t* d_hc_lines_ = nullptr;           // [n_z*n_x] slot k at its sub-list's offset
+  int32_t* d_hc_lofs_ = nullptr;            // [20][lofs_cap()]
+  int32_t* d_hc_count_ = nullptr;           // [20][2]
+  std::vector<char> hc_valid_;
+  std::vector<int> hc_start_;
+  const int32_t* rb_lines_ = nullptr;       // the current call's schedule (for the read-back)
+  const int32_t* rb_lofs_ = nullptr;
+  const int32_t* rb_count_ = nullptr;
+  size_t lofs_cap() const;
 };
 
 // GenRandList's permutation (Common/VoxelUpdateList.cpp:157-215) drawn from mt19937 through

@@ -171,6 +171,39 @@ int Engine::bf_prepare_schedule() {
   acol_lo_.assign(nl * g.n_theta, 0);
   acol_mask_.assign(nl * g.n_theta, 0);
   acol_bins(host.data(), static_cast<int>(nl), g.n_theta, nb_, acol_lo_.data(), acol_mask_.data());
+  if (p_.call_schedule != 0) return MBIR_OK;
+  // device colour schedule: packed bins and scratch
+  std::vector<int32_t> packed(nl * g.n_theta);
+  for (size_t i = 0; i < packed.size(); ++i)
+    packed[i] = static_cast<int32_t>(
+        (static_cast<uint32_t>(static_cast<uint16_t>(acol_lo_[i])) << 16) | acol_mask_[i]);
+  if (cudaMalloc(&d_packed_, packed.size() * sizeof(int32_t)) != cudaSuccess ||
+      cudaMalloc(&d_vis_, nl * sizeof(int32_t)) != cudaSuccess ||
+      cudaMalloc(&d_colour_, nl * sizeof(int16_t)) != cudaSuccess ||
+      cudaMalloc(&d_bin_used_, static_cast<size_t>(g.n_theta) * g.n_r * kColourWords * 8) !=
+          cudaSuccess ||
+      cudaMalloc(&d_line_used_, nl * kColourWords * 8) != cudaSuccess ||
+      cudaMalloc(&d_sched_count_, 2 * sizeof(int32_t)) != cudaSuccess ||
+      cudaMalloc(&d_hc_lines_, nl * sizeof(int32_t)) != cudaSuccess ||
+      cudaMalloc(&d_hc_lofs_, kNumHomogeneous * lofs_cap() * sizeof(int32_t)) != cudaSuccess ||
+      cudaMalloc(&d_hc_count_, kNumHomogeneous * 2 * sizeof(int32_t)) != cudaSuccess) {
+    cudaGetLastError();
+    dfree_any(d_packed_);
+    dfree_any(d_vis_);
+    dfree_any(d_colour_);
+    dfree_any(d_bin_used_);
+    dfree_any(d_line_used_);
+    dfree_any(d_sched_count_);
+    dfree_any(d_hc_lines_);
+    dfree_any(d_hc_lofs_);
+    dfree_any(d_hc_count_);
+    return MBIR_OK;  // host colouring instead
+  }
+  hc_valid_.assign(kNumHomogeneous, 0);
+  hc_start_.assign(kNumHomogeneous, 0);
+  cudaMemcpyAsync(d_packed_, packed.data(), packed.size() * sizeof(int32_t),
+                  cudaMemcpyHostToDevice, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "packed bins");
   return MBIR_OK;
 }
 
@@ -180,17 +213,63 @@ int Engine::bf_prepare_schedule() {
 // (call_lines_) becomes the schedule's line order.  Leaves `a` walking the rows when the engine
 // has no A-column table.
 int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
-  constexpr int kMaxColours = 512;
+  constexpr int kMaxColours = 64 * kColourWords;
   if (d_acol_ == nullptr) return MBIR_OK;
   const Geometry& g = g_;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  // a colour class holds at most as many lines as the kernel has voxel groups
+  const int groups = kWarps * (shape_ == 1 ? 2 : 1);
+  sched_on_device_ = false;
+  if (p_.call_schedule == 0 && d_packed_ != nullptr) {
+    int32_t* out_lines = d_sched_;
+    int32_t* out_lofs = d_lofs_;
+    int32_t* out_count = d_sched_count_;
+    bool build = true;
+    if (cur_hslot_ >= 0) {  // a homogeneous sub-list: its cached schedule, built the first time
+      out_lines = d_hc_lines_ + hc_start_[cur_hslot_];
+      out_lofs = d_hc_lofs_ + static_cast<size_t>(cur_hslot_) * lofs_cap();
+      out_count = d_hc_count_ + 2 * cur_hslot_;
+      build = !hc_valid_[cur_hslot_];
+    }
+    rb_lines_ = out_lines;
+    rb_lofs_ = out_lofs;
+    rb_count_ = out_count;
+    sched_on_device_ = true;
+    a.sched_lines = out_lines;
+    a.sched_lofs = out_lofs;
+    a.sched_count = out_count;
+    a.n_levels = 0;
+    a.acol = d_acol_;
+    if (!build) return MBIR_OK;
+    ColourArgs ca{};
+    ca.n_z = g.n_z;
+    ca.n_x = g.n_x;
+    ca.n_theta = g.n_theta;
+    ca.n_r = g.n_r;
+    ca.nb = nb_;
+    ca.words = kColourWords;
+    ca.max_colours = 64 * kColourWords;
+    ca.class_cap = groups;
+    ca.packed = d_packed_;
+    ca.lineok = d_lineok_;
+    ca.active = d_active_;
+    ca.vis = d_vis_;
+    ca.colour = d_colour_;
+    ca.bin_used = d_bin_used_;
+    ca.line_used = d_line_used_;
+    ca.lines = out_lines;
+    ca.lofs = out_lofs;
+    ca.count = out_count;
+    ca.err = d_err_;
+    if (launch_colour_schedule(ca, s)) return cuda_check(MBIR_EDEVICE, "colour schedule");
+    if (cur_hslot_ >= 0) hc_valid_[cur_hslot_] = 1;
+    return MBIR_OK;
+  }
   const auto t0 = std::chrono::steady_clock::now();
   LevelScheduleIn in{g.n_z, g.n_x, g.n_theta, g.n_r, nb_, stride_, rows.data(),
                      tab_.line_nonempty.data(), active_host_.data(), acol_lo_.data(),
                      acol_mask_.data()};
   int levels = -2;
-  // a colour class holds at most as many lines as the kernel has voxel groups
-  const int groups = kWarps * (shape_ == 1 ? 2 : 1);
   if (p_.call_schedule == 0)
     levels = colour_schedule(in, kMaxColours, groups, sched_work_, sched_lines_, sched_lofs_);
   if (levels == -2) levels = level_schedule(in, sched_work_, sched_lines_, sched_lofs_);
@@ -223,6 +302,7 @@ int Engine::bf_call_begin(int outer, int inner, DevBF* out) {
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
   const int nl = g.n_z * g.n_x;
   std::vector<int32_t> list;
+  cur_hslot_ = -1;
   if (!p_.nhicd) {
     list = bf_master_;
   } else if (bf_eff_ % 2 == 0) {
@@ -232,6 +312,10 @@ int Engine::bf_call_begin(int outer, int inner, DevBF* out) {
     const int start = static_cast<int>(std::floor(static_cast<double>(nl) / kNumHomogeneous) *
                                        bf_listsel_);
     list.assign(bf_master_.begin() + start, bf_master_.begin() + start + n_el);
+    if (!hc_valid_.empty()) {
+      cur_hslot_ = static_cast<int>(bf_listsel_);
+      hc_start_[cur_hslot_] = start;
+    }
     bf_listsel_++;
   } else {
     // ComputeVSC + SetNonHomThreshold + GenNonHomList (_Extra.cpp:888-1047)
@@ -277,7 +361,43 @@ int Engine::bf_call_begin(int outer, int inner, DevBF* out) {
   return MBIR_OK;
 }
 
+// The device schedule's lines, offsets and counts, copied to the host behind the call (the
+// caller synchronises the stream before bf_schedule_settle).
+void Engine::bf_schedule_readback() {
+  readback_pending_ = false;
+  if (!sched_on_device_) return;
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  size_t n_call = 0;
+  for (size_t l = 0; l < active_host_.size(); ++l)
+    n_call += (active_host_[l] && tab_.line_nonempty[l]) ? 1 : 0;
+  call_lines_.assign(n_call, 0);
+  sched_lofs_.assign(lofs_cap(), 0);
+  if (n_call)
+    cudaMemcpyAsync(call_lines_.data(), rb_lines_, n_call * sizeof(int32_t),
+                    cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(sched_lofs_.data(), rb_lofs_, sched_lofs_.size() * sizeof(int32_t),
+                  cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(sched_count_host_, rb_count_, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+  readback_pending_ = true;
+}
+
+// colours <= lines, so a call's colour offsets fit in min(max colours, lines) + 1 values
+size_t Engine::lofs_cap() const {
+  return std::min<size_t>(64 * kColourWords, static_cast<size_t>(g_.n_z) * g_.n_x) + 1;
+}
+
+void Engine::bf_schedule_settle() {
+  if (!readback_pending_) return;
+  readback_pending_ = false;
+  n_levels_ = sched_count_host_[1];
+  if (sched_count_host_[0] >= 0 && static_cast<size_t>(sched_count_host_[0]) <= call_lines_.size())
+    call_lines_.resize(static_cast<size_t>(sched_count_host_[0]));
+  sched_lofs_.resize(static_cast<size_t>(std::max(n_levels_, 0)) + 1);
+  sched_lines_ = call_lines_;
+}
+
 int Engine::bf_call_end() {
+  bf_schedule_readback();
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
   const int nl = g_.n_z * g_.n_x;
   if (!exact_) {
@@ -377,6 +497,7 @@ int Engine::bf_call(int outer, int inner, double* st4) {
   double st[kStatSlots];
   cudaMemcpyAsync(st, d_stat4_, sizeof(st), cudaMemcpyDeviceToHost, s);
   if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "BF call");
+  bf_schedule_settle();
   if ((rc = check_device_error())) return rc;
   float ms = 0;
   cudaEventElapsedTime(&ms, static_cast<cudaEvent_t>(ev0_), static_cast<cudaEvent_t>(ev1_));
@@ -538,6 +659,33 @@ int Engine::bf_run() {
       if (p_.noise_estimation && (rc = bf_update_weights())) return rc;
     }
   }
+  return MBIR_OK;
+}
+
+int Engine::get_call_schedule(int32_t* lines, int32_t cap, int32_t* lofs, int32_t lofs_cap,
+                              int32_t* n_lines, int32_t* n_levels) const {
+  const bool sched = !sched_lofs_.empty() && n_levels_ > 0;
+  const size_t nlev = sched ? sched_lofs_.size() - 1 : 0;
+  if (n_lines) *n_lines = sched ? static_cast<int32_t>(sched_lines_.size()) : 0;
+  if (n_levels) *n_levels = static_cast<int32_t>(nlev);
+  if (!sched) return MBIR_OK;
+  if (lines) {
+    if (cap < static_cast<int32_t>(sched_lines_.size())) return MBIR_EINVAL;
+    std::copy(sched_lines_.begin(), sched_lines_.end(), lines);
+  }
+  if (lofs) {
+    if (lofs_cap < static_cast<int32_t>(sched_lofs_.size())) return MBIR_EINVAL;
+    std::copy(sched_lofs_.begin(), sched_lofs_.end(), lofs);
+  }
+  return MBIR_OK;
+}
+
+int Engine::get_footprint_bins(int16_t* lo, uint16_t* mask, uint8_t* lineok) const {
+  if (state_ < 2) return MBIR_ESTATE;
+  if (acol_lo_.empty()) return MBIR_ENOTSUP;
+  if (lo) std::copy(acol_lo_.begin(), acol_lo_.end(), lo);
+  if (mask) std::copy(acol_mask_.begin(), acol_mask_.end(), mask);
+  if (lineok) std::copy(tab_.line_nonempty.begin(), tab_.line_nonempty.end(), lineok);
   return MBIR_OK;
 }
 

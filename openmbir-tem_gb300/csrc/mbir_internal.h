@@ -108,12 +108,36 @@ struct SweepArgs {
   const int* sched_lines;  // [lofs[n_levels]] z*n_x + x, level by level
   const int* sched_lofs;   // [n_levels + 1]
   int n_levels;
+  const int* sched_count;  // device [2] (lines, levels) written by the colour kernel, or nullptr
+                           // (then n_levels holds the level count)
   const float4* acol;      // [n_z*n_x][n_theta][acol_width(NB)] A-column table (FP32)
 };
 
 // A-column table entry of one voxel line at one view: the first bin (int bits) and the NB
 // footprint values, padded to whole float4s.
 constexpr int acol_width(int nb) { return (nb + 1 + 3) / 4; }
+
+// Colour schedule of a sparse ICD call on the device (mbir_colour.cu); the same result as the
+// host colour_schedule.
+struct ColourArgs {
+  int n_z, n_x, n_theta, n_r, nb;
+  int words;                      // colour-set words per bin and line (1..8)
+  int max_colours;                // <= 64 * words
+  int class_cap;                  // 1..32 lines per colour
+  const int32_t* packed;          // [n_z*n_x][n_theta] (first bin << 16) | nonzero-bin mask
+  const uint8_t* lineok;          // [n_z*n_x]
+  const uint8_t* active;          // [n_z*n_x] lines of the call (nullptr: all)
+  int32_t* vis;                   // [n_z*n_x] scratch: the call's lines, ascending
+  int16_t* colour;                // [n_z*n_x] scratch: colour of each of them
+  unsigned long long* bin_used;   // [n_theta][n_r][words] scratch, cleared by the launcher
+  unsigned long long* line_used;  // [n_z*n_x][words] scratch, cleared by the launcher
+  int32_t* lines;                 // [n_z*n_x] out: lines colour by colour
+  int32_t* lofs;                  // [max_colours + 1] out: colour offsets
+  int32_t* count;                 // [2] out: lines, colours
+  int* err;                       // value 4 is ORed in when max_colours do not suffice
+};
+int launch_colour_schedule(const ColourArgs& a, void* stream);
+size_t colour_smem_bytes(int n_theta, int words);
 
 // Batched sweep: per-series sweep arguments and a queue of (series, slice y) items.
 struct BatchArgs {

@@ -855,7 +855,8 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
       scheduled = true;
       c.cache = nullptr;
       c.acol = A.acol;
-      for (int lv = 0; lv < A.n_levels; ++lv) {
+      const int n_levels = A.sched_count != nullptr ? __ldg(A.sched_count + 1) : A.n_levels;
+      for (int lv = 0; lv < n_levels; ++lv) {
         const int b = __ldg(A.sched_lofs + lv), n = __ldg(A.sched_lofs + lv + 1) - b;
         for (int b0 = 0; b0 < n; b0 += n_groups) {
           const int i = b0 + group;

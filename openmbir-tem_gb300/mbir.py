@@ -142,6 +142,9 @@ SIGNATURES = {
     "mbir_get_tables": (C.c_int32, [C.c_void_p, _D, _D]),
     "mbir_get_schedule": (C.c_int32, [C.c_void_p, C.c_int32, _I, _I]),
     "mbir_get_call_lines": (C.c_int32, [C.c_void_p, _I, C.c_int32, _I]),
+    "mbir_get_call_schedule": (C.c_int32, [C.c_void_p, _I, C.c_int32, _I, C.c_int32, _I, _I]),
+    "mbir_get_footprint_bins": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int16),
+                                            C.POINTER(C.c_uint16), C.POINTER(C.c_uint8)]),
     "mbir_error_view_sums_noalloc": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
                                                  C.c_void_p, C.c_void_p]),
     "mbir_get_bf_state": (C.c_int32, [C.c_void_p, C.POINTER(C.c_uint8), _F, _D, _D, _D]),
@@ -405,6 +408,30 @@ class Engine:
         out = np.zeros(max(n.value, 1), np.int32)
         self._check(lib().mbir_get_call_lines(self._h, out.ctypes.data_as(_I), n.value, C.byref(n)))
         return out[:n.value]
+
+    def call_schedule(self):
+        """(lines level by level, level offsets) of the last scheduled call."""
+        n = C.c_int32()
+        nl = C.c_int32()
+        self._check(lib().mbir_get_call_schedule(self._h, None, 0, None, 0, C.byref(n),
+                                                 C.byref(nl)))
+        lines = np.zeros(max(n.value, 1), np.int32)
+        lofs = np.zeros(nl.value + 1, np.int32)
+        self._check(lib().mbir_get_call_schedule(self._h, lines.ctypes.data_as(_I), n.value,
+                                                 lofs.ctypes.data_as(_I), nl.value + 1,
+                                                 C.byref(n), C.byref(nl)))
+        return lines[:n.value], lofs[:nl.value + 1]
+
+    def footprint_bins(self):
+        """(lo [z][x][theta] int16, mask uint16, lineok [z][x] uint8) of the schedules."""
+        nz, nx, ny, nt, nr, ntt = self.dims()
+        lo = np.zeros((nz, nx, nt), np.int16)
+        mask = np.zeros((nz, nx, nt), np.uint16)
+        ok = np.zeros((nz, nx), np.uint8)
+        self._check(lib().mbir_get_footprint_bins(
+            self._h, lo.ctypes.data_as(C.POINTER(C.c_int16)),
+            mask.ctypes.data_as(C.POINTER(C.c_uint16)), ok.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return lo, mask, ok
 
     def bf_state(self):
         """(selector [theta][r][t] uint8, weights float32, mag [z][x], filtered mag, T)"""

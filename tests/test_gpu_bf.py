@@ -173,3 +173,34 @@ def test_bf_level_schedule_bitwise_row_walk(lib_built, oracle_mod, staging):
     assert np.array_equal(s0, s1) and np.array_equal(m0, m1)
     for a, b in zip(n0, n1):
         np.testing.assert_array_equal(a, b)
+
+
+def test_bf_device_colour_schedule_matches_host(lib_built, oracle_mod):
+    """Each NHICD call's colour schedule, built on the device, equals the host definition
+    (mbir_colour_schedule on the engine's footprint bins, the call's lines and the kernel's class
+    cap of 32 voxel groups), its classes are independent, and the calls match the oracle run in
+    that visit order (FP32, 1e-5; Bragg rejection off)."""
+    mbir = lib_built
+    e, o, p, y = pair(mbir, oracle_mod, call_schedule=0, bragg_threshold=5.0e10)
+    e.prepare()
+    o.prepare()
+    lo, mask, ok = e.footprint_bins()
+    nz, nx = ok.shape
+    n_r = y.shape[1]
+    for k in range(22):  # calls 20 and 22 reuse the cached schedules of sub-lists 0 and 1
+        sg = e.sweep(0, k)
+        lines, lofs = e.call_schedule()
+        assert len(lines) > 0 and len(lofs) >= 2 and e.status().sched_levels == len(lofs) - 1
+        act = np.zeros(nz * nx, np.uint8)
+        act[lines] = 1
+        hl, ho = mbir.colour_schedule(ok, lo, mask, 3, n_r, act.reshape(nz, nx), class_cap=32)
+        np.testing.assert_array_equal(lines, hl)
+        np.testing.assert_array_equal(lofs, ho)
+        assert np.diff(lofs).max() <= 32
+        np.testing.assert_array_equal(e.call_lines(), lines)
+        if k >= 4:
+            continue
+        so = o.bf_sweep_slices_order(lines, 0, k)
+        assert sg[3] == so[3] and sg[2] == so[2], (k, sg, so)
+        assert rel(e.volume(), o.volume()) <= 1e-5, (k, rel(e.volume(), o.volume()))
+        assert rel(e.error_sinogram(), o.error()) <= 1e-5, k
