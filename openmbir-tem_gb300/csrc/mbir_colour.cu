@@ -8,12 +8,14 @@
 // within a colour), the colour offsets and the counts, all in device memory, so the sweep that
 // follows reads them without a host round trip.
 //
-// One CTA of 1024 threads.  Lines are coloured 32 at a time: every warp ORs the colour sets of
-// its line's bins (bit planes in global memory, L2-resident) into the set of colours taken by
-// earlier blocks; the 32 x 32 conflict matrix of the block comes from the lines' footprints
-// staged in shared memory; warp 0 then assigns the 32 colours in order, which is the
-// sequential greedy choice because each line sees the colours of the earlier lines of its
-// block that it conflicts with; finally the block's colours are ORed into the bit planes.
+// Lines are coloured 32 at a time (a block).  First, one CTA per block computes the block's
+// conflict words (bit j of word i: line j < i of the block conflicts with line i) from the
+// lines' footprints; this needs no colours, so every block runs in parallel.  Then one CTA of
+// 1024 threads walks the blocks in order: every warp ORs the colour sets of its line's bins
+// (bit planes in global memory, L2-resident) into the set of colours taken by earlier blocks;
+// warp 0 assigns the 32 colours in order, which is the sequential greedy choice because each
+// line also sees the colours of the earlier lines of its block that it conflicts with; finally
+// the block's colours are ORed into the bit planes.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -59,6 +61,37 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* warp_sums, int* 
   return warp_sums[warp] + incl - v;
 }
 
+// conflict words of block blockIdx.x of the call's lines
+__global__ void __launch_bounds__(kThreads) colour_conflicts_kernel(ColourArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int nt = A.n_theta, nx = A.n_x;
+  int32_t* pk = reinterpret_cast<int32_t*>(smem);  // [kBlock][nt]
+  __shared__ int vz[kBlock], vx[kBlock];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int s = blockIdx.x * kBlock;
+  const int m = min(kBlock, A.n - s);
+  if (m <= 0) return;
+  if (warp < m) {
+    const int l = A.vis[s + warp];
+    for (int v = lane; v < nt; v += 32) pk[warp * nt + v] = A.packed[static_cast<size_t>(l) * nt + v];
+    if (lane == 0) {
+      vz[warp] = l / nx;
+      vx[warp] = l - (l / nx) * nx;
+    }
+  }
+  __syncthreads();
+  if (warp < m) {
+    const int i = warp, j = lane;
+    bool c = false;
+    if (j < i) {
+      c = abs(vz[i] - vz[j]) <= 1 && abs(vx[i] - vx[j]) <= 1;
+      for (int v = 0; v < nt && !c; ++v) c = bins_overlap(pk[i * nt + v], pk[j * nt + v]);
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, c);
+    if (lane == 0) A.conf[s + i] = b;
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int W = A.words;
@@ -68,7 +101,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
   int* csize = reinterpret_cast<int*>(F + kBlock * W);                // [64 W] class sizes
   __shared__ unsigned conf[kBlock];
   __shared__ int col[kBlock];
-  __shared__ int vline[kBlock], vz[kBlock], vx[kBlock];
+  __shared__ int vline[kBlock];
   __shared__ int warp_sums[32];
   __shared__ unsigned long long full_s[8];
   __shared__ int s_total, s_ncol, s_fail;
@@ -80,16 +113,9 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
     s_ncol = 0;
     s_fail = 0;
   }
-  // phase 0: the call's lines in ascending order (coalesced chunks of kThreads lines)
-  int n = 0;
-  for (int c0 = 0; c0 < nl; c0 += kThreads) {
-    const int l = c0 + tid;
-    const bool f = l < nl && A.lineok[l] && (A.active == nullptr || A.active[l]);
-    const int p = block_exclusive_scan(f ? 1 : 0, warp_sums, &s_total);
-    if (f) A.vis[n + p] = l;
-    n += s_total;
-    __syncthreads();
-  }
+  (void)nl;
+  const int n = A.n;  // the call's lines, ascending, in A.vis
+  __syncthreads();
 
   // phase 1: colour kBlock lines per step
   for (int s = 0; s < n; s += kBlock) {
@@ -98,56 +124,32 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
     if (warp < m) {
       const int l = A.vis[s + warp];
       const int z = l / nx, x = l - z * nx;
-      unsigned long long f[8];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) f[k] = 0ull;
-      for (int v = lane; v < nt; v += 32) {
-        const int32_t p = A.packed[static_cast<size_t>(l) * nt + v];
-        pk[warp * nt + v] = p;
-        const unsigned mk = static_cast<unsigned>(p) & 0xffffu;
-        const int lo = p >> 16;
-        for (int b = 0; b < A.nb; ++b)
-          if ((mk >> b) & 1u) {
-            const unsigned long long* row =
-                A.bin_used + (static_cast<size_t>(v) * A.n_r + lo + b) * W;
-#pragma unroll
-            for (int k = 0; k < 8; ++k)
-              if (k < uw) f[k] |= __ldcg(row + k);
-          }
-      }
-      if (lane < 9) {
-        const int zz = z + lane / 3 - 1, xx = x + lane % 3 - 1;
-        if (zz >= 0 && zz < A.n_z && xx >= 0 && xx < nx) {
-          const unsigned long long* nb = A.line_used + (static_cast<size_t>(zz) * nx + xx) * W;
-#pragma unroll
-          for (int k = 0; k < 8; ++k)
-            if (k < uw) f[k] |= __ldcg(nb + k);
+      for (int k = 0; k < uw; ++k) {
+        unsigned long long f = 0ull;
+        for (int v = lane; v < nt; v += 32) {
+          const int32_t p = A.packed[static_cast<size_t>(l) * nt + v];
+          if (k == 0) pk[warp * nt + v] = p;
+          const unsigned mk = static_cast<unsigned>(p) & 0xffffu;
+          const int lo = p >> 16;
+          const unsigned long long* row = A.bin_used + (static_cast<size_t>(v) * A.n_r + lo) * W + k;
+          for (int b = 0; b < A.nb; ++b)
+            if ((mk >> b) & 1u) f |= __ldcg(row + static_cast<size_t>(b) * W);
         }
-      }
+        if (lane < 9) {
+          const int zz = z + lane / 3 - 1, xx = x + lane % 3 - 1;
+          if (zz >= 0 && zz < A.n_z && xx >= 0 && xx < nx)
+            f |= __ldcg(A.line_used + (static_cast<size_t>(zz) * nx + xx) * W + k);
+        }
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) f[k] |= __shfl_xor_sync(0xffffffffu, f[k], o);
+        for (int o = 16; o > 0; o >>= 1) f |= __shfl_xor_sync(0xffffffffu, f, o);
+        if (lane == 0) F[warp * W + k] = f;
       }
+      // words from uw on hold no colours yet; pk now holds the footprints for the updates below
       if (lane == 0) {
-        for (int k = 0; k < W; ++k) F[warp * W + k] = k < 8 ? f[k] : 0ull;
+        for (int k = uw; k < W; ++k) F[warp * W + k] = 0ull;
         vline[warp] = l;
-        vz[warp] = z;
-        vx[warp] = x;
+        conf[warp] = A.conf[s + warp];
       }
-    }
-    __syncthreads();
-    // conflicts with earlier lines of the block: warp i tests its line against line j < i on
-    // lane j, over every view
-    if (warp < m) {
-      const int i = warp, j = lane;
-      bool c = false;
-      if (j < i) {
-        c = abs(vz[i] - vz[j]) <= 1 && abs(vx[i] - vx[j]) <= 1;
-        for (int v = 0; v < nt && !c; ++v) c = bins_overlap(pk[i * nt + v], pk[j * nt + v]);
-      }
-      const unsigned b = __ballot_sync(0xffffffffu, c);
-      if (lane == 0) conf[i] = b;
     }
     __syncthreads();
     // warp 0: the greedy choice, line by line
@@ -277,6 +279,13 @@ int launch_colour_schedule(const ColourArgs& a, void* stream) {
   const size_t lines = static_cast<size_t>(a.n_z) * a.n_x * a.words;
   cudaMemsetAsync(a.bin_used, 0, bins * sizeof(unsigned long long), s);
   cudaMemsetAsync(a.line_used, 0, lines * sizeof(unsigned long long), s);
+  if (a.n > 0) {
+    const size_t csm = sizeof(int32_t) * kBlock * a.n_theta;
+    if (cudaFuncSetAttribute(colour_conflicts_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(csm)) != cudaSuccess)
+      return -3;
+    colour_conflicts_kernel<<<(a.n + kBlock - 1) / kBlock, kThreads, csm, s>>>(a);
+  }
   const size_t smem = colour_smem_bytes(a.n_theta, a.words);
   if (cudaFuncSetAttribute(colour_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            static_cast<int>(smem)) != cudaSuccess)

@@ -141,6 +141,7 @@ void Engine::release() {
   dfree(d_lofs_);
   dfree(d_packed_);
   dfree(d_vis_);
+  dfree(d_conf_);
   dfree(d_colour_);
   dfree(d_bin_used_);
   dfree(d_line_used_);

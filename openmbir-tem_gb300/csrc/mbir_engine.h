@@ -272,7 +272,9 @@ class Engine {
   std::vector<int32_t> sched_lines_, sched_lofs_;
   // device colour schedule (call_schedule 0)
   int32_t* d_packed_ = nullptr;             // [n_z*n_x][n_theta] (first bin << 16) | mask
-  int32_t* d_vis_ = nullptr;                // [n_z*n_x] scratch
+  int32_t* d_vis_ = nullptr;                // [n_z*n_x] the call's lines, ascending
+  unsigned* d_conf_ = nullptr;              // [n_z*n_x] conflict words
+  std::vector<int32_t> vis_host_;
   int16_t* d_colour_ = nullptr;             // [n_z*n_x] scratch
   unsigned long long* d_bin_used_ = nullptr;   // [n_theta][n_r][kColourWords]
   unsigned long long* d_line_used_ = nullptr;  // [n_z*n_x][kColourWords]

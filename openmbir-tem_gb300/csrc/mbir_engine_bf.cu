@@ -179,6 +179,7 @@ int Engine::bf_prepare_schedule() {
         (static_cast<uint32_t>(static_cast<uint16_t>(acol_lo_[i])) << 16) | acol_mask_[i]);
   if (cudaMalloc(&d_packed_, packed.size() * sizeof(int32_t)) != cudaSuccess ||
       cudaMalloc(&d_vis_, nl * sizeof(int32_t)) != cudaSuccess ||
+      cudaMalloc(&d_conf_, nl * sizeof(unsigned)) != cudaSuccess ||
       cudaMalloc(&d_colour_, nl * sizeof(int16_t)) != cudaSuccess ||
       cudaMalloc(&d_bin_used_, static_cast<size_t>(g.n_theta) * g.n_r * kColourWords * 8) !=
           cudaSuccess ||
@@ -190,6 +191,7 @@ int Engine::bf_prepare_schedule() {
     cudaGetLastError();
     dfree_any(d_packed_);
     dfree_any(d_vis_);
+    dfree_any(d_conf_);
     dfree_any(d_colour_);
     dfree_any(d_bin_used_);
     dfree_any(d_line_used_);
@@ -253,7 +255,16 @@ int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
     ca.packed = d_packed_;
     ca.lineok = d_lineok_;
     ca.active = d_active_;
+    // the call's lines (lineok and active), ascending
+    vis_host_.clear();
+    for (size_t l = 0; l < active_host_.size(); ++l)
+      if (active_host_[l] && tab_.line_nonempty[l]) vis_host_.push_back(static_cast<int32_t>(l));
+    if (!vis_host_.empty())
+      cudaMemcpyAsync(d_vis_, vis_host_.data(), vis_host_.size() * sizeof(int32_t),
+                      cudaMemcpyHostToDevice, s);
     ca.vis = d_vis_;
+    ca.n = static_cast<int>(vis_host_.size());
+    ca.conf = d_conf_;
     ca.colour = d_colour_;
     ca.bin_used = d_bin_used_;
     ca.line_used = d_line_used_;

@@ -127,8 +127,10 @@ struct ColourArgs {
   const int32_t* packed;          // [n_z*n_x][n_theta] (first bin << 16) | nonzero-bin mask
   const uint8_t* lineok;          // [n_z*n_x]
   const uint8_t* active;          // [n_z*n_x] lines of the call (nullptr: all)
-  int32_t* vis;                   // [n_z*n_x] scratch: the call's lines, ascending
-  int16_t* colour;                // [n_z*n_x] scratch: colour of each of them
+  const int32_t* vis;             // [n] the call's lines (lineok and active), ascending
+  int n;
+  unsigned* conf;                 // [n] scratch: conflict words of each block of 32 lines
+  int16_t* colour;                // [n_z*n_x] scratch: colour of each of the call's lines
   unsigned long long* bin_used;   // [n_theta][n_r][words] scratch, cleared by the launcher
   unsigned long long* line_used;  // [n_z*n_x][words] scratch, cleared by the launcher
   int32_t* lines;                 // [n_z*n_x] out: lines colour by colour

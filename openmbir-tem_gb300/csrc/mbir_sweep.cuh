@@ -224,6 +224,28 @@ __device__ __forceinline__ void view_footprint(const DevGeom& g, const Real* __r
   }
 }
 
+// |d|^e for the prior coefficient: FP32 uses the fast power intrinsic (a few ulp, far below the
+// FP32 sweep's tolerance); FP64 keeps pow.
+template <typename Real>
+__device__ __forceinline__ Real prior_pow(Real a, Real e) {
+  return pow(a, e);
+}
+template <>
+__device__ __forceinline__ float prior_pow<float>(float a, float e) {
+  return __powf(a, e);
+}
+
+// Bragg selector of one entry after the scatter (BFForwardModel.cpp:898-932): |e sqrt(w)| < T.
+// FP32 compares e^2 w < T^2 (the same test for T >= 0, without a square root per entry).
+template <typename Real>
+__device__ __forceinline__ uint8_t bragg_selected(Real e, Real w, Real t) {
+  return fabs(e * sqrt(w)) < t ? 1 : 0;
+}
+template <>
+__device__ __forceinline__ uint8_t bragg_selected<float>(float e, float w, float t) {
+  return e * e * w < t * t ? 1 : 0;
+}
+
 // rho'(d)/d of the QGGMRF prior (QGGMRF_Functions.cpp:90-104 divided by d), or rho''(0)
 // (:109-112) when d == 0.
 template <typename Real>
@@ -232,10 +254,10 @@ __device__ __forceinline__ Real qggmrf_coef(const DevFilter& q, Real d0) {
   const Real c = static_cast<Real>(q.mrf_c), sp = static_cast<Real>(q.sig_p);
   if (d0 == Real(0)) return P / (sp * c);
   const Real ad = fabs(d0);
-  const Real t1 = pow(ad, P - Q) / static_cast<Real>(q.sig_pq);
+  const Real t1 = prior_pow<Real>(ad, P - Q) / static_cast<Real>(q.sig_pq);
   const Real t3 = c + t1;
   Real r = (P - ((P - Q) * t1) / t3) / (t3 * sp);
-  if (P != Real(2)) r *= pow(ad, P - Real(2));
+  if (P != Real(2)) r *= prior_pow<Real>(ad, P - Real(2));
   return r;
 }
 
@@ -576,7 +598,7 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
             const Real ne = ev[i][b] - gain * (a[i][b] * hh * dlt);
             c.es[eidx[i] + b] = ne;
             if constexpr (BF)
-              c.bs[v * c.bs_rs + jlo[i] + b] = fabs(ne * sqrt(wv[i][b])) < c.bt ? 1 : 0;
+              c.bs[v * c.bs_rs + jlo[i] + b] = bragg_selected<Real>(ne, wv[i][b], c.bt);
           }
       }
     } else {
@@ -596,7 +618,7 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
               if (a[i][b] > Real(0)) {
                 const Real ne = row[b] - gain * (a[i][b] * hh * dlt);
                 row[b] = ne;
-                sr[b] = fabs(ne * sqrt(__ldg(wr + b))) < c.bt ? 1 : 0;
+                sr[b] = bragg_selected<Real>(ne, __ldg(wr + b), c.bt);
               }
           } else {
 #pragma unroll
