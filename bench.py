@@ -387,6 +387,8 @@ def main():
     ap.add_argument("--series", type=int, default=64, help="batch/serve: number of requests")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--lane-shape", type=int, default=None,
+                    help="voxel-group shape (1 16x4, 2 32x2, 3 32x3, 4 32x5; default autotuned)")
     ap.add_argument("--call-schedule", type=int, default=None,
                     help="BF NHICD call schedule (0 colour classes, 1 row walk, 2 levels)")
     args = ap.parse_args()
@@ -420,6 +422,8 @@ def main():
     p.device = local
     if args.call_schedule is not None:
         p.call_schedule = args.call_schedule
+    if args.lane_shape is not None:
+        p.lane_shape = args.lane_shape
     eng = mbir.Engine(p)
     eng.set_sinogram(y, ang)
     eng.prepare()
@@ -529,6 +533,8 @@ def main():
         pe.device = local
         if args.call_schedule is not None:
             pe.call_schedule = args.call_schedule
+        if args.lane_shape is not None:
+            pe.lane_shape = args.lane_shape
         host_vol = np.empty((nz, nx, ny), np.float32)
         barrier()
         t0 = time.perf_counter()
