@@ -302,6 +302,8 @@ def run_batch(args):
     # all together
     engines = [engine(item) for item in data]
     with mbir.Batch(0) as b:
+        if args.batch_threads:
+            b.set_threads(args.batch_threads)
         for e in engines:
             b.add(e)
         torch.cuda.synchronize()
@@ -387,6 +389,8 @@ def main():
     ap.add_argument("--series", type=int, default=64, help="batch/serve: number of requests")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--batch-threads", type=int, default=None,
+                    help="CTA size of the persistent batched sweep (512 or 256)")
     ap.add_argument("--lane-shape", type=int, default=None,
                     help="voxel-group shape (1 16x4, 2 32x2, 3 32x3, 4 32x5; default autotuned)")
     ap.add_argument("--call-schedule", type=int, default=None,

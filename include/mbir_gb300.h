@@ -254,6 +254,10 @@ void mbir_batch_destroy(mbir_batch* b);
 int32_t mbir_batch_add(mbir_batch* b, mbir_engine* e);
 int32_t mbir_batch_remove(mbir_batch* b, mbir_engine* e);
 int32_t mbir_batch_size(const mbir_batch* b);
+/* threads per CTA of the persistent batched sweep: 512 (default; one slice per SM) or 256 (two
+ * slices per SM; a slice's detector rows are staged in shared memory only when two CTAs' worth
+ * fits, otherwise they are used in place in HBM).  Same results either way. */
+int32_t mbir_batch_set_threads(mbir_batch* b, int32_t threads);
 /* one sweep of every engine (outer index drives zero skipping); stats: 4 doubles per engine */
 int32_t mbir_batch_sweep(mbir_batch* b, int32_t outer, double* stats);
 /* outer iterations (batched sweep + per-engine gain/offset, variance, cost) until each engine's

@@ -71,15 +71,16 @@ int Batch::ensure_resources() {
     if (d_st4_) cudaFree(d_st4_);
     cap_series_ = std::max<size_t>(n, 64);
     if (cudaMalloc(&d_series_, sizeof(SweepArgs) * cap_series_) != cudaSuccess ||
-        cudaMalloc(&d_ctr_, sizeof(int) * (1 + 2 * cap_series_)) != cudaSuccess ||
+        cudaMalloc(&d_ctr_, sizeof(int) * (kShapes + 2 * cap_series_)) != cudaSuccess ||
         cudaMalloc(&d_st4_, sizeof(double) * kStatSlots * cap_series_) != cudaSuccess)
       return fail(MBIR_ENOMEM, "batch: device allocation");
   }
   return MBIR_OK;
 }
 
-// Queue order: colour-0 slices of every engine, then colour-1 slices; engines with the most
-// voxels per slice first so the long items start early.
+// Items grouped by voxel-group shape and modality (one launch each); within a group, colour-0 slices of
+// every engine, then colour-1 slices, engines with the most voxels per slice first so the long
+// items start early.
 int Batch::build_items(const std::vector<SweepArgs>& args) {
   const int n = static_cast<int>(args.size());
   std::vector<int> order(n);
@@ -90,12 +91,19 @@ int Batch::build_items(const std::vector<SweepArgs>& args) {
   });
   items_.clear();
   need_.assign(n, 0);
-  for (int colour = 0; colour < 2; colour++)
-    for (int s : order)
-      for (int y = colour; y < args[s].g.n_y; y += 2) {
-        items_.push_back(make_int2(s, y));
-        if (colour == 0) need_[s]++;
+  for (int g = 0; g < kShapes; g++) {
+    group_off_[g] = static_cast<int>(items_.size());
+    for (int colour = 0; colour < 2; colour++)
+      for (int s : order) {
+        const int sh = (args[s].shape >= 1 && args[s].shape <= 4) ? args[s].shape : 4;
+        if (2 * (sh - 1) + (args[s].bf ? 1 : 0) != g) continue;
+        for (int y = colour; y < args[s].g.n_y; y += 2) {
+          items_.push_back(make_int2(s, y));
+          if (colour == 0) need_[s]++;
+        }
       }
+    group_cnt_[g] = static_cast<int>(items_.size()) - group_off_[g];
+  }
   if (items_.size() > cap_items_) {
     if (d_items_) cudaFree(d_items_);
     cap_items_ = items_.size() * 2;
@@ -114,8 +122,14 @@ int Batch::sweep(const std::vector<std::pair<int, int>>& iters, double* stats) {
   std::vector<SweepArgs> args(n);
   size_t smem = 0;
   int nb = -1, max_theta = 0;
-  int max_optin = 0;
+  int max_optin = 0, per_sm = 0;
   cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_);
+  cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device_);
+  // staged slices must leave room for the kernel's static shared memory (and, with 256-thread
+  // CTAs, for a second CTA on the SM)
+  const size_t stage_cap =
+      threads_ == 256 ? static_cast<size_t>(std::min(max_optin, per_sm / 2 - 1024)) - 2048
+                      : static_cast<size_t>(max_optin) - 2048;
   // per-engine set-up (row order, bright-field list, active mask, level schedule) side by side
   std::vector<size_t> needs(n, 0);
   const std::vector<int> rcs = parallel_for(n, device_, [&](int i) {
@@ -131,8 +145,7 @@ int Batch::sweep(const std::vector<std::pair<int, int>>& iters, double* stats) {
     if (eng_[i]->nb() != nb) return fail(MBIR_ENOTSUP, "batch: engines at different voxel sizes");
     max_theta = std::max(max_theta, args[i].g.n_theta);
     if (args[i].smem_rows) {
-      // room for the kernel's own static shared memory
-      if (need + 2048 > static_cast<size_t>(max_optin)) {
+      if (need > stage_cap) {
         args[i].smem_rows = 0;
         args[i].n_rs = 0;
       } else {
@@ -144,27 +157,31 @@ int Batch::sweep(const std::vector<std::pair<int, int>>& iters, double* stats) {
     if (!args[i].smem_rows)
       smem = std::max(smem, sweep_smem_bytes(args[i].g.n_theta, args[i].g.n_x, 0, 1,
                                              args[i].g.bins, 0, 0));
-  const int shape = lane_shape(max_theta);
+  (void)max_theta;
   if (dirty_ || items_.empty()) {
     if ((rc = build_items(args))) return rc;
     dirty_ = false;
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
   cudaMemcpyAsync(d_series_, args.data(), sizeof(SweepArgs) * n, cudaMemcpyHostToDevice, s);
-  std::vector<int> ctr(1 + 2 * n, 0);
-  for (int i = 0; i < n; i++) ctr[1 + n + i] = need_[i];
+  // counters: one queue per shape group, then done[n], need[n]
+  std::vector<int> ctr(kShapes + 2 * n, 0);
+  for (int i = 0; i < n; i++) ctr[kShapes + n + i] = need_[i];
   cudaMemcpyAsync(d_ctr_, ctr.data(), sizeof(int) * ctr.size(), cudaMemcpyHostToDevice, s);
-  BatchArgs b{};
-  b.series = d_series_;
-  b.items = d_items_;
-  b.n_items = static_cast<int>(items_.size());
-  b.queue = d_ctr_;
-  b.done = d_ctr_ + 1;
-  b.need = d_ctr_ + 1 + n;
   cudaEventRecord(static_cast<cudaEvent_t>(ev0_), s);
-  rc = launch_batch_sweep(b, nb, shape, smem, grid_, s);
-  if (rc) return fail(MBIR_EDEVICE, std::string("batch sweep launch: ") +
-                                        cudaGetErrorString(cudaGetLastError()));
+  for (int g = 0; g < kShapes; g++) {
+    if (group_cnt_[g] == 0) continue;
+    BatchArgs b{};
+    b.series = d_series_;
+    b.items = d_items_ + group_off_[g];
+    b.n_items = group_cnt_[g];
+    b.queue = d_ctr_ + g;
+    b.done = d_ctr_ + kShapes;
+    b.need = d_ctr_ + kShapes + n;
+    rc = launch_batch_sweep(b, nb, g, threads_, smem, grid_, s);
+    if (rc) return fail(MBIR_EDEVICE, std::string("batch sweep launch: ") +
+                                          cudaGetErrorString(cudaGetLastError()));
+  }
   for (int i = 0; i < n; i++) {
     const int ny = args[i].g.n_y;
     if ((rc = launch_reduce_stats(eng_[i]->slice_stats(), ny, kStatSlots, d_st4_ + kStatSlots * i, s)))

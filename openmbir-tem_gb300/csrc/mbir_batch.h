@@ -56,6 +56,13 @@ class Batch {
   double total_ms() const { return total_ms_; }
   int sweeps() const { return sweeps_; }
   void set_grid(int g) { grid_ = g; }
+  // threads per CTA of the persistent sweep: 512 (one CTA per SM) or 256 (two per SM; a slice is
+  // staged in shared memory only when two CTAs' worth fits)
+  int set_threads(int t) {
+    if (t != 256 && t != 512) return MBIR_EINVAL;
+    threads_ = t;
+    return MBIR_OK;
+  }
   const char* last_error() const { return err_.c_str(); }
   int fail(int code, const std::string& m);
 
@@ -78,6 +85,11 @@ class Batch {
   void* ev0_ = nullptr;
   void* ev1_ = nullptr;
   int grid_ = 0;
+  int threads_ = 512;
+  // launch groups: voxel-group shape (4) x modality (HAADF, bright field), one launch each
+  static constexpr int kShapes = 8;
+  int group_off_[kShapes] = {0};
+  int group_cnt_[kShapes] = {0};
   double last_ms_ = 0, total_ms_ = 0;
   int sweeps_ = 0;
 };

@@ -352,6 +352,9 @@ int32_t mbir_batch_remove(mbir_batch* b, mbir_engine* e) {
 int32_t mbir_batch_size(const mbir_batch* b) {
   return b ? static_cast<int32_t>(b->impl->size()) : 0;
 }
+int32_t mbir_batch_set_threads(mbir_batch* b, int32_t threads) {
+  return b ? b->impl->set_threads(threads) : MBIR_EINVAL;
+}
 int32_t mbir_batch_sweep(mbir_batch* b, int32_t outer, double* stats) {
   if (!b) return MBIR_EINVAL;
   try {

@@ -770,6 +770,7 @@ int Engine::prepare() {
   flt_.mrf_alpha = p_.qggmrf_alpha;
   flt_.sig_p = std::pow(p_.sigma_x, p_.qggmrf_p);
   flt_.sig_pq = std::pow(p_.sigma_x, p_.qggmrf_p - p_.qggmrf_q);
+  flt_.inv_sig_pq = 1.0 / flt_.sig_pq;
 
   if ((rc = upload_views())) return rc;
   state_ = 2;

@@ -55,6 +55,7 @@ struct DevFilter {
   double f[27];          // prior weights [dy+1][dz+1][dx+1]
   double mrf_p, mrf_q, mrf_c, mrf_alpha;
   double sig_p, sig_pq;  // sigma^P, sigma^(P-Q)
+  double inv_sig_pq;     // 1 / sigma^(P-Q)
 };
 
 enum SweepMode : int { kModeICD = 0, kModeProject = 1 };
@@ -243,11 +244,14 @@ int launch_sweep_f64(const SweepArgs& a, int nb, size_t smem_bytes, void* stream
 int launch_ref_order_f32(const RefOrderArgs& a, int nb, void* stream);
 // persistent batched sweep (FP32, slices staged or in HBM per series); shape = lane_shape of
 // the largest n_theta in the batch
-int launch_batch_sweep(const BatchArgs& b, int nb, int shape, size_t smem_bytes, int grid,
+// one launch per group = 2 * (voxel-group shape - 1) + bright field; threads: 512 (one CTA per
+// SM) or 256 (two CTAs per SM when the shared memory allows)
+int launch_batch_sweep(const BatchArgs& b, int nb, int group, int threads, size_t smem_bytes,
+                       int grid,
                        void* stream);
-int launch_batch_sweep_nb3(const BatchArgs& b, int shape, size_t smem_bytes, int grid,
+int launch_batch_sweep_nb3(const BatchArgs& b, int group, int threads, size_t smem_bytes, int grid,
                            void* stream);
-int launch_batch_sweep_nb5(const BatchArgs& b, int shape, size_t smem_bytes, int grid,
+int launch_batch_sweep_nb5(const BatchArgs& b, int group, int threads, size_t smem_bytes, int grid,
                            void* stream);
 int launch_ref_order_f64(const RefOrderArgs& a, int nb, void* stream);
 int launch_sino_to_dev(const float* host_layout, void* dev_layout, int n_theta, int n_r, int n_rp,

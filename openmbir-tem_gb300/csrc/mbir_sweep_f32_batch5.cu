@@ -3,8 +3,10 @@
 
 namespace mbir {
 
-int launch_batch_sweep_nb5(const BatchArgs& b, int shape, size_t smem, int grid, void* stream) {
-  return sweep::launch_batch_pick<5>(b, shape, smem, grid, static_cast<cudaStream_t>(stream));
+int launch_batch_sweep_nb5(const BatchArgs& b, int shape, int threads, size_t smem, int grid,
+                            void* stream) {
+  return sweep::launch_batch_pick<5>(b, shape, threads, smem, grid,
+                                     static_cast<cudaStream_t>(stream));
 }
 
 }  // namespace mbir

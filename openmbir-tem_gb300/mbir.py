@@ -163,6 +163,7 @@ SIGNATURES = {
     "mbir_batch_add": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "mbir_batch_remove": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "mbir_batch_size": (C.c_int32, [C.c_void_p]),
+    "mbir_batch_set_threads": (C.c_int32, [C.c_void_p, C.c_int32]),
     "mbir_batch_sweep": (C.c_int32, [C.c_void_p, C.c_int32, _D]),
     "mbir_batch_run": (C.c_int32, [C.c_void_p, C.c_int32, C.c_double, _I, _D]),
     "mbir_batch_last_ms": (C.c_double, [C.c_void_p]),
@@ -551,6 +552,10 @@ class Batch:
 
     def total_ms(self):
         return lib().mbir_batch_total_ms(self._h)
+
+    def set_threads(self, threads):
+        """CTA size of the persistent batched sweep: 512 or 256 (two slices per SM)."""
+        self._check(lib().mbir_batch_set_threads(self._h, int(threads)))
 
 
 class Server:
