@@ -127,9 +127,9 @@ int Batch::sweep(const std::vector<std::pair<int, int>>& iters, double* stats) {
   cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device_);
   // staged slices must leave room for the kernel's static shared memory (and, with 256-thread
   // CTAs, for a second CTA on the SM)
-  const size_t stage_cap =
-      threads_ == 256 ? static_cast<size_t>(std::min(max_optin, per_sm / 2 - 1024)) - 2048
-                      : static_cast<size_t>(max_optin) - 2048;
+  const bool two = threads_ == 256;
+  const size_t stage_cap = two ? static_cast<size_t>(std::min(max_optin, per_sm / 2 - 1024)) - 2048
+                               : static_cast<size_t>(max_optin) - 2048;
   // per-engine set-up (row order, bright-field list, active mask, level schedule) side by side
   std::vector<size_t> needs(n, 0);
   const std::vector<int> rcs = parallel_for(n, device_, [&](int i) {

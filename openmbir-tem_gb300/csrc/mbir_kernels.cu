@@ -350,10 +350,10 @@ int launch_sweep_f32_smem(const SweepArgs& a, int nb, size_t smem, void* stream)
               : launch_sweep_f32_smem_haadf(a, nb, smem, stream);
 }
 
-int launch_batch_sweep(const BatchArgs& b, int nb, int shape, int threads, size_t smem, int grid,
+int launch_batch_sweep(const BatchArgs& b, int nb, int group, int threads, size_t smem, int grid,
                        void* stream) {
-  if (nb == 3) return launch_batch_sweep_nb3(b, shape, threads, smem, grid, stream);
-  if (nb == 5) return launch_batch_sweep_nb5(b, shape, threads, smem, grid, stream);
+  if (nb == 3) return launch_batch_sweep_nb3(b, group, threads, smem, grid, stream);
+  if (nb == 5) return launch_batch_sweep_nb5(b, group, threads, smem, grid, stream);
   return -7;
 }
 

@@ -3,9 +3,9 @@
 
 namespace mbir {
 
-int launch_batch_sweep_nb5(const BatchArgs& b, int shape, int threads, size_t smem, int grid,
+int launch_batch_sweep_nb5(const BatchArgs& b, int group, int threads, size_t smem, int grid,
                             void* stream) {
-  return sweep::launch_batch_pick<5>(b, shape, threads, smem, grid,
+  return sweep::launch_batch_pick<5>(b, group, threads, smem, grid,
                                      static_cast<cudaStream_t>(stream));
 }
 
