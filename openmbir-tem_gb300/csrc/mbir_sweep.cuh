@@ -200,10 +200,9 @@ __device__ __forceinline__ void compute_row_base(const DevTables& tab, int n_the
 // [floor(u-d), floor(u+d)] on the detector, value = linear interpolation of the detector
 // response at |u - (j+0.5)|, kept when > 0.
 template <typename Real, int NB>
-__device__ __forceinline__ void view_footprint(const DevGeom& g, const Real* __restrict__ hrow,
-                                               int j0, Real f, int& jlo, Real (&a)[NB]) {
-  const Real hw = static_cast<Real>(g.half_width);
-  const Real kr = static_cast<Real>(g.kr);
+__device__ __forceinline__ void view_footprint(const DevGeom& g, Real hw, Real kr,
+                                               const Real* __restrict__ hrow, int j0, Real f,
+                                               int& jlo, Real (&a)[NB]) {
   const int lo = j0 + static_cast<int>(floor(f - hw));
   const int hi = j0 + static_cast<int>(floor(f + hw));
   jlo = lo;
@@ -246,15 +245,36 @@ __device__ __forceinline__ uint8_t bragg_selected<float>(float e, float w, float
   return e * e * w < t * t ? 1 : 0;
 }
 
+// Prior and footprint constants in the sweep's precision, converted from FP64 once per slice
+// (on GB300 every FP64-to-FP32 conversion runs on the narrow FP64 pipe, so converting them per
+// voxel cost ~2k cycles per voxel step).
+template <typename Real>
+struct PriorConst {
+  Real P, Q, c, sp, sig_pq, inv_sig_pq, alpha, hw, kr;
+};
+template <typename Real>
+__device__ __forceinline__ PriorConst<Real> prior_const(const DevFilter& q, const DevGeom& g) {
+  PriorConst<Real> k;
+  k.P = static_cast<Real>(q.mrf_p);
+  k.Q = static_cast<Real>(q.mrf_q);
+  k.c = static_cast<Real>(q.mrf_c);
+  k.sp = static_cast<Real>(q.sig_p);
+  k.sig_pq = static_cast<Real>(q.sig_pq);
+  k.inv_sig_pq = static_cast<Real>(q.inv_sig_pq);
+  k.alpha = static_cast<Real>(q.mrf_alpha);
+  k.hw = static_cast<Real>(g.half_width);
+  k.kr = static_cast<Real>(g.kr);
+  return k;
+}
+
 // rho'(d)/d of the QGGMRF prior (QGGMRF_Functions.cpp:90-104 divided by d), or rho''(0)
 // (:109-112) when d == 0.
 template <typename Real>
-__device__ __forceinline__ Real qggmrf_coef(const DevFilter& q, Real d0) {
-  const Real P = static_cast<Real>(q.mrf_p), Q = static_cast<Real>(q.mrf_q);
-  const Real c = static_cast<Real>(q.mrf_c), sp = static_cast<Real>(q.sig_p);
+__device__ __forceinline__ Real qggmrf_coef(const PriorConst<Real>& q, Real d0) {
+  const Real P = q.P, Q = q.Q, c = q.c, sp = q.sp;
   if (d0 == Real(0)) return P / (sp * c);
   const Real ad = fabs(d0);
-  const Real t1 = prior_pow<Real>(ad, P - Q) / static_cast<Real>(q.sig_pq);
+  const Real t1 = prior_pow<Real>(ad, P - Q) / q.sig_pq;
   const Real t3 = c + t1;
   Real r = (P - ((P - Q) * t1) / t3) / (t3 * sp);
   if (P != Real(2)) r *= prior_pow<Real>(ad, P - Real(2));
@@ -263,12 +283,11 @@ __device__ __forceinline__ Real qggmrf_coef(const DevFilter& q, Real d0) {
 // FP32: the same function as (P c + Q t1) / (t3^2 sigma^P) (P - (P-Q) t1/t3 = (P c + Q t1)/t3),
 // one fast division instead of three IEEE divisions (relative error a few ulp).
 template <>
-__device__ __forceinline__ float qggmrf_coef<float>(const DevFilter& q, float d0) {
-  const float P = static_cast<float>(q.mrf_p), Q = static_cast<float>(q.mrf_q);
-  const float c = static_cast<float>(q.mrf_c), sp = static_cast<float>(q.sig_p);
+__device__ __forceinline__ float qggmrf_coef<float>(const PriorConst<float>& q, float d0) {
+  const float P = q.P, Q = q.Q, c = q.c, sp = q.sp;
   if (d0 == 0.f) return P / (sp * c);
   const float ad = fabsf(d0);
-  const float t1 = __powf(ad, P - Q) * static_cast<float>(q.inv_sig_pq);
+  const float t1 = __powf(ad, P - Q) * q.inv_sig_pq;
   const float t3 = c + t1;
   float r = __fdividef(P * c + Q * t1, t3 * t3 * sp);
   if (P != 2.f) r *= __powf(ad, P - 2.f);
@@ -314,6 +333,8 @@ struct SliceCtx {
   Real bt, bdt;              // T, delta*T
   unsigned long long* mag_fx;
   const float4* acol;        // A-column table (level-scheduled sweeps) or nullptr
+  const PriorConst<Real>* pc;  // prior and footprint constants (shared memory)
+  const Real* qf;            // prior weights [27] (shared memory)
   bool coherent;             // neighbour planes read from the volume bypass L1 (other CTAs of
                              // the launch write them)
 };
@@ -429,7 +450,7 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
     for (int i = 0; i < NNB; ++i) {
       if (nvalid[i]) {
         const Real tc =
-            static_cast<Real>(c.q->f[gl + G * i]) * qggmrf_coef<Real>(*c.q, V - nb[i]);
+            c.qf[gl + G * i] * qggmrf_coef<Real>(*c.pc, V - nb[i]);
         s1 += tc * nb[i];
         s2 += tc;
       }
@@ -437,7 +458,7 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
   }
 
   // A-column of the voxel, lanes over views (AMatrixCol.cpp:148-232)
-  const Real hw = static_cast<Real>(g.half_width);
+  const Real hw = c.pc->hw;
   int jlo[VPL];
   Real a[VPL][NB];
 #pragma unroll
@@ -461,7 +482,7 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
                    f);
       const Real u = static_cast<Real>(j0) + f;
       if (!(u + hw < Real(0) || u - hw > static_cast<Real>(g.n_r)))
-        view_footprint<Real, NB>(g, c.sH + v * (g.bins + 1), j0, f, jlo[i], a[i]);
+        view_footprint<Real, NB>(g, hw, c.pc->kr, c.sH + v * (g.bins + 1), j0, f, jlo[i], a[i]);
     }
   }
 
@@ -602,7 +623,7 @@ __device__ __forceinline__ void group_step(const SliceCtx<Real>& c, int z, int x
   s1 = group_sum<G>(s1);
   s2 = group_sum<G>(s2);
   const Real u = (s1 + theta2 * V - theta1) / (s2 + theta2);
-  Real nv = V + static_cast<Real>(c.q->mrf_alpha) * (u - V);
+  Real nv = V + c.pc->alpha * (u - V);
   nv = (nv < lo) ? lo : ((nv > hi) ? hi : nv);
   if (nv < Real(0)) nv = Real(0);  // positivity (UpdateVoxels.cpp:394-400, BFConstants.h)
   const Real dlt = nv - V;
@@ -773,6 +794,10 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
   Real* const gx = static_cast<Real*>(A.x);
   constexpr bool kF32 = std::is_same<Real, float>::value;
 
+  __shared__ PriorConst<Real> s_pc;
+  __shared__ Real s_qf[27];
+  if (tid == 0) s_pc = prior_const<Real>(A.flt, A.g);
+  if (tid < 27) s_qf[tid] = static_cast<Real>(A.flt.f[tid]);
   for (int i = tid; i < g.n_theta * (g.bins + 1); i += nthreads) sH[i] = gH[i];
   for (int v = tid; v < g.n_theta; v += nthreads) {
     if (kF32)
@@ -783,6 +808,7 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
   }
   if (tid < kMaxTRows) shv[tid] = ghv[y * kMaxTRows + tid];
   if (tid < 4) ctl[tid] = 0u;
+  __syncthreads();  // constants and tables visible before any path uses them
 
   const size_t sino_plane = static_cast<size_t>(g.n_theta) * g.n_rp;
   const size_t sel_plane = static_cast<size_t>(g.n_theta) * n_sp;
@@ -864,6 +890,8 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
   c.bt = c.bdt = Real(0);
   c.acol = nullptr;
   c.coherent = coherent;
+  c.pc = &s_pc;
+  c.qf = s_qf;
   if (BF) {
     c.bw = static_cast<const Real*>(A.bfa.w) + static_cast<size_t>(tfirst) * sino_plane;
     c.bw_rs = g.n_rp;
@@ -1022,12 +1050,34 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
       if (lane == 0) cls[k] = base;
     }
     __syncthreads();
+    // Dense rows: once a class holds more than 8 candidates, consecutive classes practically
+    // always have candidates within S of each other and would not merge; each non-empty class
+    // becomes a step as it is (class order, the same result as merged steps), the class lists
+    // copied into the step list by all threads instead of the one-warp merge pass.
+    int cmax = 0;
+    for (int k = 0; k < S; ++k) cmax = max(cmax, static_cast<int>(cls[k]));
+    const bool dense = cmax > 8;
+    if (dense) {
+      int off = 0, ns = 0;
+      for (int k = 0; k < S; ++k) {
+        const int n = cls[k];
+        if (n == 0) continue;
+        if (tid == 0) gofs[ns] = off;
+        for (int j = tid; j < n; j += nthreads) flat[off + j] = list[k * cap + j];
+        off += n;
+        ++ns;
+      }
+      if (tid == 0) {
+        gofs[ns] = off;
+        ctl[0] = static_cast<unsigned>(ns);
+      }
+    }
     // Steps: consecutive classes are merged while none of the next class's candidates lies
     // within S of a candidate already in the step.  Voxels of one step are then pairwise
     // independent (no shared detector bin, no prior neighbours, no zero-skipping influence),
     // and independent updates commute, so a step gives exactly the result of running its
     // classes in order.  One warp forms the steps in class order.
-    if (warp == 0) {
+    if (!dense && warp == 0) {
       const int words = (g.n_x + 31) >> 5;
       for (int w = lane; w < words; w += 32) bits[w] = 0u;
       __syncwarp();
@@ -1222,6 +1272,10 @@ __global__ void __launch_bounds__(32, 1) ref_order_kernel(RefOrderArgs A) {
   const R2* ggw = static_cast<const R2*>(A.tab.gw);
   const Real* ghv = static_cast<const Real*>(A.tab.hval);
   constexpr bool kF32 = std::is_same<Real, float>::value;
+  __shared__ PriorConst<Real> s_pc;
+  __shared__ Real s_qf[27];
+  if (lane == 0) s_pc = prior_const<Real>(A.flt, A.g);
+  if (lane < 27) s_qf[lane] = static_cast<Real>(A.flt.f[lane]);
   for (int i = lane; i < g.n_theta * (g.bins + 1); i += 32) sH[i] = gH[i];
   for (int v = lane; v < g.n_theta; v += 32) {
     if (kF32)
@@ -1255,6 +1309,8 @@ __global__ void __launch_bounds__(32, 1) ref_order_kernel(RefOrderArgs A) {
   c.bt = c.bdt = Real(0);
   c.acol = nullptr;
   c.coherent = false;
+  c.pc = &s_pc;
+  c.qf = s_qf;
   Real* const ge = static_cast<Real*>(A.e);
   const size_t sino_plane = static_cast<size_t>(g.n_theta) * g.n_rp;
   const size_t sel_plane = BF ? static_cast<size_t>(g.n_theta) * A.bfa.n_sp : 0;
@@ -1317,7 +1373,8 @@ __global__ void acol_kernel(DevGeom g, DevTables tab, float4* __restrict__ out) 
 #pragma unroll
     for (int b = 0; b < NB; ++b) a[b] = 0.f;
     if (!(u + hw < 0.f || u - hw > static_cast<float>(g.n_r)))
-      view_footprint<float, NB>(g, H + v * (g.bins + 1), j0, f, jlo, a);
+      view_footprint<float, NB>(g, hw, static_cast<float>(g.kr), H + v * (g.bins + 1), j0, f,
+                                jlo, a);
     float t[AW * 4];
 #pragma unroll
     for (int k = 0; k < AW * 4; ++k) t[k] = 0.f;
