@@ -274,6 +274,9 @@ int launch_colour_schedule(const ColourArgs& a, void* stream) {
   if (a.words < 1 || a.words > 8 || a.max_colours > 64 * a.words || a.class_cap < 1 ||
       a.class_cap > 32 || a.nb > 16)
     return -7;
+  // an error left pending by an earlier call on this thread is reported as such
+  const cudaError_t pending = cudaGetLastError();
+  if (pending != cudaSuccess) return -1000 - static_cast<int>(pending);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t bins = static_cast<size_t>(a.n_theta) * a.n_r * a.words;
   const size_t lines = static_cast<size_t>(a.n_z) * a.n_x * a.words;
@@ -281,17 +284,21 @@ int launch_colour_schedule(const ColourArgs& a, void* stream) {
   cudaMemsetAsync(a.line_used, 0, lines * sizeof(unsigned long long), s);
   if (a.n > 0) {
     const size_t csm = sizeof(int32_t) * kBlock * a.n_theta;
-    if (cudaFuncSetAttribute(colour_conflicts_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(csm)) != cudaSuccess)
-      return -3;
+    cudaError_t e = cudaFuncSetAttribute(colour_conflicts_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(csm));
+    if (e != cudaSuccess) return -2000 - static_cast<int>(e);
     colour_conflicts_kernel<<<(a.n + kBlock - 1) / kBlock, kThreads, csm, s>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return -3000 - static_cast<int>(e);
   }
   const size_t smem = colour_smem_bytes(a.n_theta, a.words);
-  if (cudaFuncSetAttribute(colour_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           static_cast<int>(smem)) != cudaSuccess)
-    return -3;
+  cudaError_t e = cudaFuncSetAttribute(colour_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem));
+  if (e != cudaSuccess) return -4000 - static_cast<int>(e);
   colour_kernel<<<1, kThreads, smem, s>>>(a);
-  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+  e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : -5000 - static_cast<int>(e);
 }
 
 }  // namespace mbir

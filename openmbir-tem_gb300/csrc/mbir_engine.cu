@@ -528,8 +528,12 @@ int Engine::alloc_device() {
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, p_.device);
   n_sp_ = bf_ ? (g.n_r + 15) / 16 * 16 : 0;
   smem_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, n_rs_, t_rows_, bins_, fp64_, n_sp_);
+  smem_sched_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, n_rs_, t_rows_, bins_, fp64_, n_sp_, true);
   stage_ = smem_bytes_ <= static_cast<size_t>(max_smem) && p_.slice_staging == 0;
-  if (!stage_) smem_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, 0, t_rows_, bins_, fp64_, 0);
+  if (!stage_) {
+    smem_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, 0, t_rows_, bins_, fp64_, 0);
+    smem_sched_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, 0, t_rows_, bins_, fp64_, 0, true);
+  }
   const size_t ns = static_cast<size_t>(g.n_t) * g.n_theta * n_rp_;
   const size_t nh = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;
   const size_t nv = static_cast<size_t>(g.n_z) * g.n_x * g.n_y;

@@ -177,6 +177,7 @@ class Engine {
   int stride_ = 2;    // conflict-free x stride
   bool stage_ = true; // slice fits in shared memory
   size_t smem_bytes_ = 0;
+  size_t smem_sched_bytes_ = 0;  // scheduled bright-field calls
   DevFilter flt_{};
   DevGeom dg_{};
 

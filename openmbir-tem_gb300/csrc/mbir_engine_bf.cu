@@ -272,7 +272,14 @@ int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
     ca.lofs = out_lofs;
     ca.count = out_count;
     ca.err = d_err_;
-    if (launch_colour_schedule(ca, s)) return cuda_check(MBIR_EDEVICE, "colour schedule");
+    const int crc = launch_colour_schedule(ca, s);
+    if (crc) {
+      // -1000 - e: CUDA error e pending from an earlier call; -k000 - e: error e at step k
+      const int e = crc <= -1000 ? (-crc) % 1000 : 0;
+      return fail(MBIR_EDEVICE, "colour schedule: step " + std::to_string(-crc / 1000) + ": " +
+                                    (e ? cudaGetErrorString(static_cast<cudaError_t>(e))
+                                       : "invalid arguments"));
+    }
     if (cur_hslot_ >= 0) hc_valid_[cur_hslot_] = 1;
     return MBIR_OK;
   }
@@ -496,7 +503,8 @@ int Engine::bf_call(int outer, int inner, double* st4) {
       a.n_slices = (g.n_y - colour + 1) / 2;
       a.stats = d_stats_ + (colour ? static_cast<size_t>(n0) * kStatSlots : 0);
       if (a.n_slices <= 0) continue;
-      if ((rc = launch_sweep(a, nb_, smem_bytes_, s))) return cuda_check(rc, "BF call launch");
+      const size_t smem = a.sched_lines != nullptr ? smem_sched_bytes_ : smem_bytes_;
+      if ((rc = launch_sweep(a, nb_, smem, s))) return cuda_check(rc, "BF call launch");
     }
     cudaEventRecord(static_cast<cudaEvent_t>(ev3_), s);
     kernel_timed_ = true;

@@ -232,8 +232,9 @@ int launch_exact_view_sums(const ExactArgs& a, int kind, const double* y, const 
 // launchers (mbir_kernels.cu); fp64 selects Real = double for the void* arrays
 int launch_sweep(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_ref_order(const RefOrderArgs& a, int nb, void* stream);
+// sched: the layout of a scheduled bright-field call (smaller: no response table or row lists)
 size_t sweep_smem_bytes(int n_theta, int n_x, int n_rs, int t_rows, int bins, int fp64,
-                        int n_sp);
+                        int n_sp, bool sched = false);
 int launch_sweep_f32_smem(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_sweep_f32_smem_haadf(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_sweep_f32_smem_bf(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);

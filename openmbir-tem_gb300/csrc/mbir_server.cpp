@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <string>
 #include <cmath>
 
 namespace mbir {
@@ -265,6 +266,7 @@ int Server::wait(int64_t id, double timeout_s) {
                             std::chrono::duration<double>(timeout_s));
   if (!done_cv_.wait_until(lk, deadline, [&] { return r->state == 2 || r->state < 0; }))
     return MBIR_ETIMEOUT;
+  if (r->state < 0) err_ = "request " + std::to_string(id) + ": " + r->error;
   return r->state == 2 ? MBIR_OK : r->state;
 }
 

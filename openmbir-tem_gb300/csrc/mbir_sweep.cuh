@@ -701,10 +701,16 @@ __host__ __device__ inline size_t align_up(size_t v, size_t a) { return (v + a -
 
 constexpr int kMaxGroups = kWarps * 32 / 16;  // voxel groups per CTA at G = 16
 
-// n_sp > 0: the slice's selector rows are staged too (bright field)
+// n_sp > 0: the slice's selector rows are staged too (bright field).  sched: a scheduled call
+// (no detector-response table, no row-walk lists or neighbour cache), which leaves more of the
+// SM's L1 to the per-entry weights it gathers.
 __host__ __device__ inline SmemLayout smem_layout(int n_theta, int n_x, int n_rs, int t_rows,
                                                   int bins, bool stage, size_t real_bytes,
-                                                  int n_sp) {
+                                                  int n_sp, bool sched = false) {
+  if (sched) {
+    n_x = 0;
+    bins = -1;
+  }
   SmemLayout L;
   size_t o = 0;
   L.bar = o;
@@ -774,8 +780,10 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
   const int n_groups = (nthreads / 32) * GPW;
   const int tcount = A.tab.t_count[y], tfirst = A.tab.t_first[y];
   const int n_sp = BF ? A.bfa.n_sp : 0;
-  const SmemLayout L =
-      smem_layout(g.n_theta, g.n_x, A.n_rs, tcount, g.bins, STAGE, sizeof(Real), n_sp);
+  const bool sched_layout = BF && std::is_same<Real, float>::value && A.sched_lines != nullptr &&
+                            A.acol != nullptr && A.mode != kModeProject;
+  const SmemLayout L = smem_layout(g.n_theta, g.n_x, A.n_rs, tcount, g.bins, STAGE, sizeof(Real),
+                                   n_sp, sched_layout);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L.bar);
   unsigned* ctl = reinterpret_cast<unsigned*>(smem + L.ctl);
   unsigned long long* sstat = reinterpret_cast<unsigned long long*>(smem + L.stats);
@@ -798,7 +806,8 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
   __shared__ Real s_qf[27];
   if (tid == 0) s_pc = prior_const<Real>(A.flt, A.g);
   if (tid < 27) s_qf[tid] = static_cast<Real>(A.flt.f[tid]);
-  for (int i = tid; i < g.n_theta * (g.bins + 1); i += nthreads) sH[i] = gH[i];
+  if (!sched_layout)  // scheduled calls read the A-column from its table
+    for (int i = tid; i < g.n_theta * (g.bins + 1); i += nthreads) sH[i] = gH[i];
   for (int v = tid; v < g.n_theta; v += nthreads) {
     if (kF32)
       sbx[v] = A.tab.bx[v];
@@ -1410,6 +1419,18 @@ int launch_sweep_t(const SweepArgs& a, size_t smem, cudaStream_t s) {
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem));
   if (e != cudaSuccess) return -3;
+  // shared-memory carveout just large enough for this launch: the rest of the SM's unified
+  // L1/shared storage caches the gathered weights and neighbour rows
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  }
+  if (per_sm > 0) {
+    const int pct = static_cast<int>(std::min<size_t>(100, (100 * (smem + 4096) + per_sm - 1) / per_sm));
+    cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+  }
   k<<<a.n_slices, kWarps * 32, smem, s>>>(a);
   return ok_or(cudaGetLastError());
 }

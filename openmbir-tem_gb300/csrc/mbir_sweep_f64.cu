@@ -30,8 +30,9 @@ int launch_ref_order_f64(const RefOrderArgs& a, int nb, void* stream) {
 }
 
 size_t sweep_smem_bytes(int n_theta, int n_x, int n_rs, int t_rows, int bins, int fp64,
-                        int n_sp) {
-  return sweep::smem_layout(n_theta, n_x, n_rs, t_rows, bins, n_rs > 0, fp64 ? 8 : 4, n_sp).total;
+                        int n_sp, bool sched) {
+  return sweep::smem_layout(n_theta, n_x, n_rs, t_rows, bins, n_rs > 0, fp64 ? 8 : 4, n_sp, sched)
+      .total;
 }
 
 }  // namespace mbir
