@@ -284,17 +284,20 @@ int launch_colour_schedule(const ColourArgs& a, void* stream) {
   cudaMemsetAsync(a.line_used, 0, lines * sizeof(unsigned long long), s);
   if (a.n > 0) {
     const size_t csm = sizeof(int32_t) * kBlock * a.n_theta;
+    static const int lim = dyn_smem_limit(colour_conflicts_kernel);
+    if (csm > static_cast<size_t>(lim)) return -7;
     cudaError_t e = cudaFuncSetAttribute(colour_conflicts_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(csm));
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     if (e != cudaSuccess) return -2000 - static_cast<int>(e);
     colour_conflicts_kernel<<<(a.n + kBlock - 1) / kBlock, kThreads, csm, s>>>(a);
     e = cudaGetLastError();
     if (e != cudaSuccess) return -3000 - static_cast<int>(e);
   }
   const size_t smem = colour_smem_bytes(a.n_theta, a.words);
+  static const int lim = dyn_smem_limit(colour_kernel);
+  if (smem > static_cast<size_t>(lim)) return -7;
   cudaError_t e = cudaFuncSetAttribute(colour_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(smem));
+                                       lim);
   if (e != cudaSuccess) return -4000 - static_cast<int>(e);
   colour_kernel<<<1, kThreads, smem, s>>>(a);
   e = cudaGetLastError();

@@ -8,6 +8,7 @@
 //   per-view tables: detector response H [theta][bins+1], (gain, weight) pairs, projection
 //     coefficients; per-slice t-response (first row, count, values).
 #pragma once
+#include <cuda_runtime.h>
 #include <vector_types.h>
 
 #include <cstdint>
@@ -117,6 +118,30 @@ struct SweepArgs {
 // A-column table entry of one voxel line at one view: the first bin (int bits) and the NB
 // footprint values, padded to whole float4s.
 constexpr int acol_width(int nb) { return (nb + 1 + 3) / 4; }
+
+// The per-block shared-memory limit (opt-in) of the current device.  Launchers set a kernel's
+// dynamic limit attribute to this minus the kernel's static shared memory (dyn_smem_limit)
+// rather than to their own size: the attribute belongs to the function, not the launch, and
+// host threads launching the same kernel with different sizes would otherwise race (a launch
+// above the value another thread just set fails).
+inline int smem_optin_limit() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 48 * 1024;
+  if (cached[dev] == 0) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cached[dev] = v > 0 ? v : 48 * 1024;
+  }
+  return cached[dev];
+}
+
+template <typename F>
+inline int dyn_smem_limit(F* func) {
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(func)) != cudaSuccess) return 0;
+  return smem_optin_limit() - static_cast<int>(fa.sharedSizeBytes);
+}
 
 // Colour schedule of a sparse ICD call on the device (mbir_colour.cu); the same result as the
 // host colour_schedule.

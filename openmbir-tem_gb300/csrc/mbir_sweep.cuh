@@ -1416,8 +1416,9 @@ inline int launch_acol_t(const DevGeom& g, const DevTables& tab, int nb, float4*
 template <typename Real, int NB, int G, int VPL, bool STAGE, bool BF>
 int launch_sweep_t(const SweepArgs& a, size_t smem, cudaStream_t s) {
   auto k = sweep_kernel<Real, NB, G, VPL, STAGE, BF>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(smem));
+  static const int lim = dyn_smem_limit(k);
+  if (smem > static_cast<size_t>(lim)) return -3;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   if (e != cudaSuccess) return -3;
   // shared-memory carveout just large enough for this launch: the rest of the SM's unified
   // L1/shared storage caches the gathered weights and neighbour rows
@@ -1443,8 +1444,9 @@ int launch_sweep_m(const SweepArgs& a, size_t smem, cudaStream_t s) {
 template <int NB, int G, int VPL, bool BF>
 int launch_batch_t(const BatchArgs& b, size_t smem, int grid, int threads, cudaStream_t s) {
   auto k = batch_sweep_kernel<NB, G, VPL, BF>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(smem));
+  static const int lim = dyn_smem_limit(k);
+  if (smem > static_cast<size_t>(lim)) return -3;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   if (e != cudaSuccess) return -3;
   if (threads != 256 && threads != kWarps * 32) threads = kWarps * 32;
   int per_sm = 0;
@@ -1466,8 +1468,9 @@ template <typename Real, int NB, int VPL>
 int launch_ref_t(const RefOrderArgs& a, cudaStream_t s) {
   const size_t smem = smem_layout(a.g.n_theta, 0, 0, 0, a.g.bins, false, sizeof(Real), 0).total;
   auto launch = [&](auto kern) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
+    const int lim = dyn_smem_limit(kern);
+    if (smem > static_cast<size_t>(lim)) return -3;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     if (e != cudaSuccess) return -3;
     kern<<<1, 32, smem, s>>>(a);
     return ok_or(cudaGetLastError());

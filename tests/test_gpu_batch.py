@@ -114,3 +114,36 @@ def test_batched_mixed_haadf_bf_match_single(lib_built):
     for ea, eb in zip(alone[2:], batched[2:]):
         np.testing.assert_array_equal(eb.call_lines(), ea.call_lines())
         np.testing.assert_array_equal(eb.bf_state()[0], ea.bf_state()[0])  # selectors
+
+
+def test_batched_bf_uneven_views_match_single(lib_built):
+    """Bright-field engines with different view counts in one batch: their per-call colour
+    schedules are built side by side on host threads with different shared-memory sizes (the
+    kernels' size limit is set once, to the device maximum, so concurrent set-ups cannot race),
+    and every engine gives the same bits as alone."""
+    mbir = lib_built
+    from conftest import bf_case, bf_params
+
+    def make():
+        out = []
+        for (n_r, n_t, seed, step) in ((64, 8, 5, 4.0), (48, 10, 6, 3.0), (56, 6, 7, 2.0),
+                                       (40, 12, 8, 6.0)):
+            y, ang, th = bf_case(n_r=n_r, n_t=n_t, seed=seed, step=step)
+            e = mbir.Engine(bf_params(mbir, th))
+            e.set_sinogram(y, ang)
+            e.prepare()
+            out.append(e)
+        return out
+
+    alone, batched = make(), make()
+    assert len({e.dims()[3] for e in alone}) == 4  # four view counts
+    with mbir.Batch(0) as b:
+        for e in batched:
+            b.add(e)
+        for k in range(6):
+            st_b = b.sweep(outer=k)
+            st_s = np.stack([e.sweep(k, 0) for e in alone])
+            np.testing.assert_array_equal(st_b[:, 2:], st_s[:, 2:])
+    for ea, eb in zip(alone, batched):
+        assert np.array_equal(eb.volume(), ea.volume())
+        np.testing.assert_array_equal(eb.call_lines(), ea.call_lines())
