@@ -527,6 +527,9 @@ int Engine::alloc_device() {
   int max_smem = 0;
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, p_.device);
   n_sp_ = bf_ ? (g.n_r + 15) / 16 * 16 : 0;
+  // a selector row stride of a multiple of 128 bytes would put every view's byte of a detector
+  // bin into one shared-memory bank; 16 more bytes spread the views over eight banks
+  if (n_sp_ > 0 && n_sp_ % 128 == 0) n_sp_ += 16;
   smem_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, n_rs_, t_rows_, bins_, fp64_, n_sp_);
   smem_sched_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, n_rs_, t_rows_, bins_, fp64_, n_sp_, true);
   stage_ = smem_bytes_ <= static_cast<size_t>(max_smem) && p_.slice_staging == 0;
