@@ -124,25 +124,41 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
     if (warp < m) {
       const int l = A.vis[s + warp];
       const int z = l / nx, x = l - z * nx;
-      for (int k = 0; k < uw; ++k) {
-        unsigned long long f = 0ull;
-        for (int v = lane; v < nt; v += 32) {
-          const int32_t p = A.packed[static_cast<size_t>(l) * nt + v];
-          if (k == 0) pk[warp * nt + v] = p;
-          const unsigned mk = static_cast<unsigned>(p) & 0xffffu;
-          const int lo = p >> 16;
-          const unsigned long long* row = A.bin_used + (static_cast<size_t>(v) * A.n_r + lo) * W + k;
-          for (int b = 0; b < A.nb; ++b)
-            if ((mk >> b) & 1u) f |= __ldcg(row + static_cast<size_t>(b) * W);
-        }
-        if (lane < 9) {
-          const int zz = z + lane / 3 - 1, xx = x + lane % 3 - 1;
-          if (zz >= 0 && zz < A.n_z && xx >= 0 && xx < nx)
-            f |= __ldcg(A.line_used + (static_cast<size_t>(zz) * nx + xx) * W + k);
-        }
+      // footprints once, then every word in use of each touched bin and neighbour line: two
+      // dependent L2 round trips per block
+      unsigned long long f[8];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) f |= __shfl_xor_sync(0xffffffffu, f, o);
-        if (lane == 0) F[warp * W + k] = f;
+      for (int k = 0; k < 8; ++k) f[k] = 0ull;
+      for (int v = lane; v < nt; v += 32) {
+        const int32_t p = A.packed[static_cast<size_t>(l) * nt + v];
+        pk[warp * nt + v] = p;
+        const unsigned mk = static_cast<unsigned>(p) & 0xffffu;
+        const int lo = p >> 16;
+        for (int b = 0; b < A.nb; ++b)
+          if ((mk >> b) & 1u) {
+            const unsigned long long* row =
+                A.bin_used + (static_cast<size_t>(v) * A.n_r + lo + b) * W;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+              if (k < uw) f[k] |= __ldcg(row + k);
+          }
+      }
+      if (lane < 9) {
+        const int zz = z + lane / 3 - 1, xx = x + lane % 3 - 1;
+        if (zz >= 0 && zz < A.n_z && xx >= 0 && xx < nx) {
+          const unsigned long long* nbl = A.line_used + (static_cast<size_t>(zz) * nx + xx) * W;
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            if (k < uw) f[k] |= __ldcg(nbl + k);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        if (k < uw) {
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) f[k] |= __shfl_xor_sync(0xffffffffu, f[k], o);
+          if (lane == 0) F[warp * W + k] = f[k];
+        }
       }
       // words from uw on hold no colours yet; pk now holds the footprints for the updates below
       if (lane == 0) {
