@@ -472,6 +472,7 @@ def main():
     # spent building level schedules, both inside the ICD interval above
     kernel_ms_step = (st1.kernel_ms_total - st0.kernel_ms_total) / args.steps
     sched_ms_step = (st1.sched_ms_total - st0.sched_ms_total) / args.steps
+    colour_ms_step = (st1.colour_ms_total - st0.colour_ms_total) / args.steps
     total_ms = float(np.sum(per_ms))
     if dist is not None:
         t = torch.tensor([total_ms], device=f"cuda:{local}")
@@ -516,6 +517,7 @@ def main():
                       "slices_in_smem": bool(st.staged), "x_stride": st.stride,
                       "sweep_kernel_ms_per_step": kernel_ms_step,
                       "host_schedule_ms_per_step": sched_ms_step,
+                      "colour_schedule_ms_per_step": colour_ms_step,
                       "levels_last_call": st.sched_levels},
            "gpu_launches": launches * args.steps,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -146,6 +146,7 @@ typedef struct mbir_status {
   double sched_ms_total;  /* host time spent building level schedules */
   double kernel_ms_total; /* device time of the parallel-order sweep kernels alone (colour
                              launches; icd_ms_total also holds list, schedule and statistics) */
+  double colour_ms_total; /* device time of the colour-schedule launches (call_schedule 0) */
 } mbir_status;
 
 typedef struct mbir_engine mbir_engine;

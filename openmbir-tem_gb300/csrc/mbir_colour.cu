@@ -73,7 +73,8 @@ __global__ void __launch_bounds__(kThreads) colour_conflicts_kernel(ColourArgs A
   if (m <= 0) return;
   if (warp < m) {
     const int l = A.vis[s + warp];
-    for (int v = lane; v < nt; v += 32) pk[warp * nt + v] = A.packed[static_cast<size_t>(l) * nt + v];
+    const int32_t* pl = A.packed + static_cast<size_t>(l) * nt;
+    for (int v = lane; v < nt; v += 32) pk[warp * nt + v] = pl[v];
     if (lane == 0) {
       vz[warp] = l / nx;
       vx[warp] = l - (l / nx) * nx;
@@ -124,87 +125,143 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
     if (warp < m) {
       const int l = A.vis[s + warp];
       const int z = l / nx, x = l - z * nx;
-      // footprints once, then every word in use of each touched bin and neighbour line: two
-      // dependent L2 round trips per block
-      unsigned long long f[8];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) f[k] = 0ull;
-      for (int v = lane; v < nt; v += 32) {
-        const int32_t p = A.packed[static_cast<size_t>(l) * nt + v];
-        pk[warp * nt + v] = p;
-        const unsigned mk = static_cast<unsigned>(p) & 0xffffu;
-        const int lo = p >> 16;
-        for (int b = 0; b < A.nb; ++b)
-          if ((mk >> b) & 1u) {
-            const unsigned long long* row =
-                A.bin_used + (static_cast<size_t>(v) * A.n_r + lo + b) * W;
-#pragma unroll
-            for (int k = 0; k < 8; ++k)
-              if (k < uw) f[k] |= __ldcg(row + k);
-          }
+      // footprints once, then every word pair in use of each touched bin and neighbour line:
+      // each lane group reads one word pair, its lanes over (view, bin), so that consecutive
+      // lanes read neighbouring bins and a load touches few cache lines
+      const int32_t* pl = A.packed + static_cast<size_t>(l) * nt;
+      for (int v = lane; v < nt; v += 32) pk[warp * nt + v] = pl[v];
+      __syncwarp();
+      const int np = uw <= 2 ? 1 : uw <= 4 ? 2 : 4;  // word pairs read (W is 2, 4 or 8)
+      const int gs = 32 / np;                        // lanes per word pair
+      const int kk = lane / gs, sub = lane - kk * gs;
+      const int nb = A.nb, dv = gs / nb, db = gs - dv * nb;
+      unsigned long long fx = 0ull, fy = 0ull;
+      for (int v = sub / nb, b = sub - (sub / nb) * nb; v < nt;) {
+        const int32_t p = pk[warp * nt + v];
+        if ((static_cast<unsigned>(p) >> b) & 1u) {
+          const size_t row = (static_cast<size_t>(v) * A.n_r + (p >> 16) + b) * W;
+          const ulonglong2 q = __ldcg(reinterpret_cast<const ulonglong2*>(A.bin_used + row) + kk);
+          fx |= q.x;
+          fy |= q.y;
+        }
+        v += dv;
+        b += db;
+        if (b >= nb) {
+          b -= nb;
+          ++v;
+        }
       }
-      if (lane < 9) {
-        const int zz = z + lane / 3 - 1, xx = x + lane % 3 - 1;
+      for (int q = sub; q < 9; q += gs) {
+        const int zz = z + q / 3 - 1, xx = x + q % 3 - 1;
         if (zz >= 0 && zz < A.n_z && xx >= 0 && xx < nx) {
-          const unsigned long long* nbl = A.line_used + (static_cast<size_t>(zz) * nx + xx) * W;
-#pragma unroll
-          for (int k = 0; k < 8; ++k)
-            if (k < uw) f[k] |= __ldcg(nbl + k);
+          const size_t row = (static_cast<size_t>(zz) * nx + xx) * W;
+          const ulonglong2 u = __ldcg(reinterpret_cast<const ulonglong2*>(A.line_used + row) + kk);
+          fx |= u.x;
+          fy |= u.y;
         }
       }
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        if (k < uw) {
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) f[k] |= __shfl_xor_sync(0xffffffffu, f[k], o);
-          if (lane == 0) F[warp * W + k] = f[k];
-        }
+      for (int o = gs >> 1; o > 0; o >>= 1) {
+        fx |= __shfl_xor_sync(0xffffffffu, fx, o);
+        fy |= __shfl_xor_sync(0xffffffffu, fy, o);
       }
-      // words from uw on hold no colours yet; pk now holds the footprints for the updates below
+      if (sub == 0) {
+        F[warp * W + 2 * kk] = fx;
+        F[warp * W + 2 * kk + 1] = fy;
+      }
+      // words from 2 np on hold no colours yet; pk holds the footprints for the updates below
       if (lane == 0) {
-        for (int k = uw; k < W; ++k) F[warp * W + k] = 0ull;
+        for (int k = 2 * np; k < W; ++k) F[warp * W + k] = 0ull;
         vline[warp] = l;
         conf[warp] = A.conf[s + warp];
       }
     }
     __syncthreads();
-    // warp 0: the greedy choice, line by line
+    // warp 0: the greedy choice, line by line, on a window of 64 colours from base, the lowest
+    // colour free for some line of the block (colours below it are full or taken for every
+    // line, and stay so).  Every lane keeps in
+    // registers its line's taken colours of the window, the window's full classes and the sizes
+    // of two of its classes, and finds its first free colour; line i takes lane i's.  A line
+    // with no free colour in the window takes the first free colour found from the shared
+    // copies (written back for it); classes beyond the window are counted in shared memory.
     if (warp == 0) {
-      unsigned long long acc[8], full[8];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        acc[k] = (lane < m && k < W) ? F[lane * W + k] : 0ull;
-        full[k] = full_s[k];  // classes already full
-      }
-      const unsigned my_conf = lane < m ? conf[lane] : 0u;
-      int ncol = s_ncol;
-      for (int i = 0; i < m; ++i) {
-        int c = -1;
-        if (lane == i) {
-          for (int k = 0; k < W && k < 8 && c < 0; ++k) {
-            const unsigned long long freeb = ~(acc[k] | full[k]);
-            if (freeb) c = 64 * k + __ffsll(static_cast<long long>(freeb)) - 1;
+      int base = 64 * W;
+      if (lane < m)
+        for (int k = 0; k < W; ++k) {
+          const unsigned long long t = F[lane * W + k] | full_s[k];
+          if (~t) {
+            base = 64 * k + __ffsll(static_cast<long long>(~t)) - 1;
+            break;
           }
         }
-        c = __shfl_sync(0xffffffffu, c, i);
-        if (c < 0 || c >= A.max_colours) {
-          if (lane == 0) s_fail = 1;
-          break;
-        }
-        if ((my_conf >> i) & 1u) acc[c >> 6] |= 1ull << (c & 63);
-        int sz = 0;
-        if (lane == 0) {
-          sz = ++csize[c];
-          col[i] = c;
-        }
-        sz = __shfl_sync(0xffffffffu, sz, 0);
-        if (A.class_cap > 0 && sz >= A.class_cap) full[c >> 6] |= 1ull << (c & 63);
-        ncol = max(ncol, c + 1);
-      }
-      if (lane == 0) {
-        s_ncol = ncol;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) full_s[k] = full[k];
+      for (int o = 16; o > 0; o >>= 1) base = min(base, __shfl_xor_sync(0xffffffffu, base, o));
+      const int k0 = base >> 6, sh = base & 63;
+      auto window = [&](const unsigned long long* v) {
+        const unsigned long long lo = k0 < W ? v[k0] : 0ull, hi = k0 + 1 < W ? v[k0 + 1] : 0ull;
+        return sh ? (lo >> sh) | (hi << (64 - sh)) : lo;
+      };
+      unsigned long long acc = lane < m ? window(F + lane * W) : 0ull;
+      // colours from max_colours on count as full, so a free window colour is a valid one
+      const int lim = A.max_colours - base;
+      unsigned long long fullw =
+          window(full_s) | (lim >= 64 ? 0ull : lim <= 0 ? ~0ull : ~0ull << lim);
+      const int cap = A.class_cap > 0 ? A.class_cap : 0x7fffffff;
+      const int cl = base + lane, ch = base + 32 + lane;  // this lane's two window classes
+      int n_lo = cl < 64 * W ? csize[cl] : 0, n_hi = ch < 64 * W ? csize[ch] : 0;
+      const unsigned my_conf = lane < m ? conf[lane] : 0u;
+      int mine = -1;
+      bool fail = false;
+      auto write_back = [&]() {
+        col[lane] = mine;
+        if (cl < 64 * W) {
+          csize[cl] = n_lo;
+          if (n_lo >= cap) atomicOr(&full_s[cl >> 6], 1ull << (cl & 63));
+        }
+        if (ch < 64 * W) {
+          csize[ch] = n_hi;
+          if (n_hi >= cap) atomicOr(&full_s[ch >> 6], 1ull << (ch & 63));
+        }
+        __syncwarp();
+      };
+      for (int i = 0; i < m; ++i) {
+        const int first = __ffsll(static_cast<long long>(~(acc | fullw))) - 1;  // -1: none
+        const int rel = __shfl_sync(0xffffffffu, first, i);
+        if (rel < 0) {  // window exhausted for line i: the exact choice from the shared copies
+          write_back();
+          int cc = -1;
+          if (lane == i)
+            for (int k = 0; k < W && cc < 0; ++k) {
+              unsigned long long t = F[i * W + k] | full_s[k];
+              for (unsigned b = my_conf; b; b &= b - 1u) {
+                const int q = col[__ffs(b) - 1];
+                if ((q >> 6) == k) t |= 1ull << (q & 63);
+              }
+              if (~t) cc = 64 * k + __ffsll(static_cast<long long>(~t)) - 1;
+            }
+          const int c = __shfl_sync(0xffffffffu, cc, i);
+          if (c < 0 || c >= A.max_colours) {
+            fail = true;
+            break;
+          }
+          mine = lane == i ? c : mine;  // beyond the window: counted in shared memory
+          if (lane == 0 && ++csize[c] >= cap) full_s[c >> 6] |= 1ull << (c & 63);
+          __syncwarp();
+          continue;
+        }
+        mine = lane == i ? base + rel : mine;
+        acc |= ((my_conf >> i) & 1u) ? 1ull << rel : 0ull;
+        n_lo += rel == lane;
+        n_hi += rel == lane + 32;
+        fullw |= (static_cast<unsigned long long>(__ballot_sync(0xffffffffu, n_hi >= cap)) << 32) |
+                 __ballot_sync(0xffffffffu, n_lo >= cap);
+      }
+      write_back();
+      int top = mine;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) top = max(top, __shfl_xor_sync(0xffffffffu, top, o));
+      if (lane == 0) {
+        if (fail) s_fail = 1;
+        s_ncol = max(s_ncol, top + 1);
       }
     }
     __syncthreads();
@@ -214,13 +271,17 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
       const int c = col[warp], l = vline[warp];
       const unsigned long long bit = 1ull << (c & 63);
       const int wk = c >> 6;
-      for (int v = lane; v < nt; v += 32) {
+      const int nb = A.nb, dv = 32 / nb, db = 32 - dv * nb;
+      for (int v = lane / nb, b = lane - (lane / nb) * nb; v < nt;) {  // lanes over (view, bin)
         const int32_t p = pk[warp * nt + v];
-        const unsigned mk = static_cast<unsigned>(p) & 0xffffu;
-        const int lo = p >> 16;
-        for (int b = 0; b < A.nb; ++b)
-          if ((mk >> b) & 1u)
-            atomicOr(A.bin_used + (static_cast<size_t>(v) * A.n_r + lo + b) * W + wk, bit);
+        if ((static_cast<unsigned>(p) >> b) & 1u)
+          atomicOr(A.bin_used + (static_cast<size_t>(v) * A.n_r + (p >> 16) + b) * W + wk, bit);
+        v += dv;
+        b += db;
+        if (b >= nb) {
+          b -= nb;
+          ++v;
+        }
       }
       if (lane == 0) {
         atomicOr(A.line_used + static_cast<size_t>(l) * W + wk, bit);
@@ -287,8 +348,8 @@ size_t colour_smem_bytes(int n_theta, int words) {
 }
 
 int launch_colour_schedule(const ColourArgs& a, void* stream) {
-  if (a.words < 1 || a.words > 8 || a.max_colours > 64 * a.words || a.class_cap < 1 ||
-      a.class_cap > 32 || a.nb > 16)
+  if ((a.words != 2 && a.words != 4 && a.words != 8) || a.max_colours > 64 * a.words ||
+      a.class_cap < 1 || a.class_cap > 32 || a.nb > 16)
     return -7;
   // an error left pending by an earlier call on this thread is reported as such
   const cudaError_t pending = cudaGetLastError();

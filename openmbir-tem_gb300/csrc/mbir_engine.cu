@@ -156,8 +156,10 @@ void Engine::release() {
   if (ev1_) cudaEventDestroy(static_cast<cudaEvent_t>(ev1_));
   if (ev2_) cudaEventDestroy(static_cast<cudaEvent_t>(ev2_));
   if (ev3_) cudaEventDestroy(static_cast<cudaEvent_t>(ev3_));
+  if (ev4_) cudaEventDestroy(static_cast<cudaEvent_t>(ev4_));
+  if (ev5_) cudaEventDestroy(static_cast<cudaEvent_t>(ev5_));
   if (stream_) cudaStreamDestroy(static_cast<cudaStream_t>(stream_));
-  ev0_ = ev1_ = ev2_ = ev3_ = stream_ = nullptr;
+  ev0_ = ev1_ = ev2_ = ev3_ = ev4_ = ev5_ = stream_ = nullptr;
 }
 
 // device time of the colour launches of the last sweep/call (events ev2_ -> ev3_)
@@ -591,15 +593,19 @@ int Engine::alloc_device() {
   if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
     return fail(MBIR_EDEVICE, "stream creation failed");
   stream_ = s;
-  cudaEvent_t e0, e1, e2, e3;
+  cudaEvent_t e0, e1, e2, e3, e4, e5;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventCreate(&e2);
   cudaEventCreate(&e3);
+  cudaEventCreate(&e4);
+  cudaEventCreate(&e5);
   ev0_ = e0;
   ev1_ = e1;
   ev2_ = e2;
   ev3_ = e3;
+  ev4_ = e4;
+  ev5_ = e5;
   cudaMemsetAsync(d_err_, 0, sizeof(int), s);
   return MBIR_OK;
 }
@@ -1282,6 +1288,7 @@ int Engine::status(mbir_status* st) const {
   st->sched_levels = n_levels_;
   st->sched_ms_total = sched_ms_;
   st->kernel_ms_total = kernel_ms_;
+  st->colour_ms_total = colour_ms_;
   return MBIR_OK;
 }
 

@@ -226,6 +226,10 @@ class Engine {
   void* ev2_ = nullptr;   // around the colour launches of a sweep/call
   void* ev3_ = nullptr;
   bool kernel_timed_ = false;
+  void* ev4_ = nullptr;   // around the colour-schedule launches of a BF call
+  void* ev5_ = nullptr;
+  bool colour_timed_ = false;
+  double colour_ms_ = 0;
   double kernel_ms_ = 0.0;  // device time of the sweep kernels alone
   int n_chunk_ = 8;
   int prior_blocks_ = 152 * 4;

@@ -272,7 +272,10 @@ int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
     ca.lofs = out_lofs;
     ca.count = out_count;
     ca.err = d_err_;
+    cudaEventRecord(static_cast<cudaEvent_t>(ev4_), s);
     const int crc = launch_colour_schedule(ca, s);
+    cudaEventRecord(static_cast<cudaEvent_t>(ev5_), s);
+    colour_timed_ = crc == 0;
     if (crc) {
       // -1000 - e: CUDA error e pending from an earlier call; -k000 - e: error e at step k
       const int e = crc <= -1000 ? (-crc) % 1000 : 0;
@@ -405,6 +408,13 @@ size_t Engine::lofs_cap() const {
 }
 
 void Engine::bf_schedule_settle() {
+  if (colour_timed_) {
+    colour_timed_ = false;
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, static_cast<cudaEvent_t>(ev4_),
+                             static_cast<cudaEvent_t>(ev5_)) == cudaSuccess)
+      colour_ms_ += ms;
+  }
   if (!readback_pending_) return;
   readback_pending_ = false;
   n_levels_ = sched_count_host_[1];

@@ -147,7 +147,7 @@ inline int dyn_smem_limit(F* func) {
 // host colour_schedule.
 struct ColourArgs {
   int n_z, n_x, n_theta, n_r, nb;
-  int words;                      // colour-set words per bin and line (1..8)
+  int words;                      // colour-set words per bin and line (2, 4 or 8)
   int max_colours;                // <= 64 * words
   int class_cap;                  // 1..32 lines per colour
   const int32_t* packed;          // [n_z*n_x][n_theta] (first bin << 16) | nonzero-bin mask

@@ -95,7 +95,7 @@ class MbirStatus(C.Structure):
         ("voxels_updated", C.c_int64), ("footprint_entries", C.c_int64), ("t_rows", C.c_int32),
         ("stride", C.c_int32), ("staged", C.c_int32), ("lane_shape", C.c_int32),
         ("sched_levels", C.c_int32), ("sched_ms_total", C.c_double),
-        ("kernel_ms_total", C.c_double),
+        ("kernel_ms_total", C.c_double), ("colour_ms_total", C.c_double),
     ]
 
 
