@@ -9,13 +9,16 @@
 // follows reads them without a host round trip.
 //
 // Lines are coloured 32 at a time (a block).  First, one CTA per block computes the block's
-// conflict words (bit j of word i: line j < i of the block conflicts with line i) from the
-// lines' footprints; this needs no colours, so every block runs in parallel.  Then one CTA of
-// 1024 threads walks the blocks in order: every warp ORs the colour sets of its line's bins
-// (bit planes in global memory, L2-resident) into the set of colours taken by earlier blocks;
-// warp 0 assigns the 32 colours in order, which is the sequential greedy choice because each
-// line also sees the colours of the earlier lines of its block that it conflicts with; finally
-// the block's colours are ORed into the bit planes.
+// conflict words from the lines' footprints (bit j of conf[i]: line j < i of the block
+// conflicts with line i; bit j of conf_prev[i]: line j of the previous block does); this needs
+// no colours, so every block runs in parallel.  Then one CTA of 1024 threads walks the blocks in
+// order.  Each step ORs the colours of the previous block into the bit planes of its bins and
+// lines (global memory, L2-resident) while every warp reads the planes of its line's bins and
+// neighbours: they hold every block before the previous one, and the previous block's colours
+// that a line must see (those of lines it conflicts with) come from conf_prev, so the planes
+// being updated meanwhile change nothing.  Warp 0 then assigns the 32 colours in order, which
+// is the sequential greedy choice because each line also sees the colours of the earlier lines
+// of its block that it conflicts with.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -61,23 +64,26 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* warp_sums, int* 
   return warp_sums[warp] + incl - v;
 }
 
-// conflict words of block blockIdx.x of the call's lines
+// conflict words of block blockIdx.x of the call's lines: within the block and against the
+// previous block
 __global__ void __launch_bounds__(kThreads) colour_conflicts_kernel(ColourArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nt = A.n_theta, nx = A.n_x;
-  int32_t* pk = reinterpret_cast<int32_t*>(smem);  // [kBlock][nt]
-  __shared__ int vz[kBlock], vx[kBlock];
+  int32_t* pk = reinterpret_cast<int32_t*>(smem);  // [2 kBlock][nt]: this block, previous block
+  __shared__ int vz[2 * kBlock], vx[2 * kBlock];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int s = blockIdx.x * kBlock;
   const int m = min(kBlock, A.n - s);
+  const int mp = blockIdx.x > 0 ? kBlock : 0;
   if (m <= 0) return;
-  if (warp < m) {
-    const int l = A.vis[s + warp];
+  for (int r = warp; r < 2 * kBlock; r += kThreads / 32) {
+    if (r < kBlock ? r >= m : r - kBlock >= mp) continue;
+    const int l = A.vis[r < kBlock ? s + r : s - kBlock + (r - kBlock)];
     const int32_t* pl = A.packed + static_cast<size_t>(l) * nt;
-    for (int v = lane; v < nt; v += 32) pk[warp * nt + v] = pl[v];
+    for (int v = lane; v < nt; v += 32) pk[r * nt + v] = pl[v];
     if (lane == 0) {
-      vz[warp] = l / nx;
-      vx[warp] = l - (l / nx) * nx;
+      vz[r] = l / nx;
+      vx[r] = l - (l / nx) * nx;
     }
   }
   __syncthreads();
@@ -88,8 +94,17 @@ __global__ void __launch_bounds__(kThreads) colour_conflicts_kernel(ColourArgs A
       c = abs(vz[i] - vz[j]) <= 1 && abs(vx[i] - vx[j]) <= 1;
       for (int v = 0; v < nt && !c; ++v) c = bins_overlap(pk[i * nt + v], pk[j * nt + v]);
     }
-    const unsigned b = __ballot_sync(0xffffffffu, c);
-    if (lane == 0) A.conf[s + i] = b;
+    bool cp = false;
+    if (j < mp) {
+      const int q = kBlock + j;
+      cp = abs(vz[i] - vz[q]) <= 1 && abs(vx[i] - vx[q]) <= 1;
+      for (int v = 0; v < nt && !cp; ++v) cp = bins_overlap(pk[i * nt + v], pk[q * nt + v]);
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, c), bp = __ballot_sync(0xffffffffu, cp);
+    if (lane == 0) {
+      A.conf[s + i] = b;
+      A.conf_prev[s + i] = bp;
+    }
   }
 }
 
@@ -97,12 +112,13 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int W = A.words;
   const int nt = A.n_theta, nx = A.n_x, nl = A.n_z * A.n_x;
-  int32_t* pk = reinterpret_cast<int32_t*>(smem);                     // [kBlock][nt]
-  unsigned long long* F = reinterpret_cast<unsigned long long*>(pk + kBlock * nt);  // [kBlock][W]
-  int* csize = reinterpret_cast<int*>(F + kBlock * W);                // [64 W] class sizes
+  int32_t* pk = reinterpret_cast<int32_t*>(smem);  // [2][kBlock][nt] footprints, by block parity
+  // [kBlock][W] colours taken for each line of the block
+  unsigned long long* F = reinterpret_cast<unsigned long long*>(pk + 2 * kBlock * nt);
+  int* csize = reinterpret_cast<int*>(F + kBlock * W);  // [64 W] class sizes
   __shared__ unsigned conf[kBlock];
-  __shared__ int col[kBlock];
-  __shared__ int vline[kBlock];
+  __shared__ int col[2][kBlock];  // colours, by block parity
+  __shared__ int vline[2][kBlock];
   __shared__ int warp_sums[32];
   __shared__ unsigned long long full_s[8];
   __shared__ int s_total, s_ncol, s_fail;
@@ -119,36 +135,73 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
   __syncthreads();
 
   // phase 1: colour kBlock lines per step
+  int mp = 0;  // lines of the previous block
   for (int s = 0; s < n; s += kBlock) {
     const int m = min(kBlock, n - s);
+    const int cur = (s / kBlock) & 1, prv = cur ^ 1;
     const int uw = min(s_ncol / 64 + 1, W);  // words holding colours so far
-    if (warp < m) {
-      const int l = A.vis[s + warp];
-      const int z = l / nx, x = l - z * nx;
-      // footprints once, then every word pair in use of each touched bin and neighbour line:
-      // each lane group reads one word pair, its lanes over (view, bin), so that consecutive
-      // lanes read neighbouring bins and a load touches few cache lines
-      const int32_t* pl = A.packed + static_cast<size_t>(l) * nt;
-      for (int v = lane; v < nt; v += 32) pk[warp * nt + v] = pl[v];
-      __syncwarp();
-      const int np = uw <= 2 ? 1 : uw <= 4 ? 2 : 4;  // word pairs read (W is 2, 4 or 8)
-      const int gs = 32 / np;                        // lanes per word pair
-      const int kk = lane / gs, sub = lane - kk * gs;
-      const int nb = A.nb, dv = gs / nb, db = gs - dv * nb;
-      unsigned long long fx = 0ull, fy = 0ull;
-      for (int v = sub / nb, b = sub - (sub / nb) * nb; v < nt;) {
-        const int32_t p = pk[warp * nt + v];
-        if ((static_cast<unsigned>(p) >> b) & 1u) {
-          const size_t row = (static_cast<size_t>(v) * A.n_r + (p >> 16) + b) * W;
-          const ulonglong2 q = __ldcg(reinterpret_cast<const ulonglong2*>(A.bin_used + row) + kk);
-          fx |= q.x;
-          fy |= q.y;
-        }
+    const int nb = A.nb;
+    // the previous block's colours into the planes of its bins and lines, not waited for here;
+    // lanes over (view, bin)
+    if (warp < mp) {
+      const int c = col[prv][warp];
+      const unsigned long long bit = 1ull << (c & 63);
+      const int wk = c >> 6;
+      const int32_t* pw = pk + (prv * kBlock + warp) * nt;
+      const int dv = 32 / nb, db = 32 - dv * nb;
+      for (int v = lane / nb, b = lane - (lane / nb) * nb; v < nt;) {
+        const int32_t p = pw[v];
+        if ((static_cast<unsigned>(p) >> b) & 1u)
+          atomicOr(A.bin_used + (static_cast<size_t>(v) * A.n_r + (p >> 16) + b) * W + wk, bit);
         v += dv;
         b += db;
         if (b >= nb) {
           b -= nb;
           ++v;
+        }
+      }
+      if (lane == 0) atomicOr(A.line_used + static_cast<size_t>(vline[prv][warp]) * W + wk, bit);
+    }
+    if (warp < m) {
+      const int l = A.vis[s + warp];
+      const unsigned cprev = A.conf_prev[s + warp];
+      const int z = l / nx, x = l - z * nx;
+      // footprints once, then every word pair in use of each touched bin and neighbour line:
+      // each lane group reads one word pair, its lanes over (view, bin), so that consecutive
+      // lanes read neighbouring bins and a load touches few cache lines; eight loads in flight
+      int32_t* pw = pk + (cur * kBlock + warp) * nt;
+      const int32_t* pl = A.packed + static_cast<size_t>(l) * nt;
+      for (int v = lane; v < nt; v += 32) pw[v] = pl[v];
+      __syncwarp();
+      const int np = uw <= 2 ? 1 : uw <= 4 ? 2 : 4;  // word pairs read (W is 2, 4 or 8)
+      const int gs = 32 / np;                        // lanes per word pair
+      const int kk = lane / gs, sub = lane - kk * gs;
+      const int dv = gs / nb, db = gs - dv * nb;
+      unsigned long long fx = 0ull, fy = 0ull;
+      int v = sub / nb, b = sub - (sub / nb) * nb;
+      while (v < nt) {
+        ulonglong2 q[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          q[u] = make_ulonglong2(0ull, 0ull);
+          if (v < nt) {
+            const int32_t p = pw[v];
+            if ((static_cast<unsigned>(p) >> b) & 1u) {
+              const size_t row = (static_cast<size_t>(v) * A.n_r + (p >> 16) + b) * W;
+              q[u] = __ldcg(reinterpret_cast<const ulonglong2*>(A.bin_used + row) + kk);
+            }
+          }
+          v += dv;
+          b += db;
+          if (b >= nb) {
+            b -= nb;
+            ++v;
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          fx |= q[u].x;
+          fy |= q[u].y;
         }
       }
       for (int q = sub; q < 9; q += gs) {
@@ -168,13 +221,22 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
         F[warp * W + 2 * kk] = fx;
         F[warp * W + 2 * kk + 1] = fy;
       }
-      // words from 2 np on hold no colours yet; pk holds the footprints for the updates below
-      if (lane == 0) {
+      // words from 2 np on hold no colours yet
+      if (lane == 0)
         for (int k = 2 * np; k < W; ++k) F[warp * W + k] = 0ull;
-        vline[warp] = l;
+      __syncwarp();
+      // the colours of the previous block's lines that this line conflicts with (the planes
+      // may or may not hold them yet)
+      if ((cprev >> lane) & 1u) {
+        const int c = col[prv][lane];
+        atomicOr(&F[warp * W + (c >> 6)], 1ull << (c & 63));
+      }
+      if (lane == 0) {
+        vline[cur][warp] = l;
         conf[warp] = A.conf[s + warp];
       }
     }
+    __threadfence_block();  // this step's plane updates land before the next step reads
     __syncthreads();
     // warp 0: the greedy choice, line by line, on a window of 64 colours from base, the lowest
     // colour free for some line of the block (colours below it are full or taken for every
@@ -212,7 +274,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
       int mine = -1;
       bool fail = false;
       auto write_back = [&]() {
-        col[lane] = mine;
+        col[cur][lane] = mine;
         if (cl < 64 * W) {
           csize[cl] = n_lo;
           if (n_lo >= cap) atomicOr(&full_s[cl >> 6], 1ull << (cl & 63));
@@ -233,7 +295,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
             for (int k = 0; k < W && cc < 0; ++k) {
               unsigned long long t = F[i * W + k] | full_s[k];
               for (unsigned b = my_conf; b; b &= b - 1u) {
-                const int q = col[__ffs(b) - 1];
+                const int q = col[cur][__ffs(b) - 1];
                 if ((q >> 6) == k) t |= 1ull << (q & 63);
               }
               if (~t) cc = 64 * k + __ffsll(static_cast<long long>(~t)) - 1;
@@ -256,6 +318,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
                  __ballot_sync(0xffffffffu, n_lo >= cap);
       }
       write_back();
+      if (lane < m && !fail) A.colour[s + lane] = static_cast<int16_t>(mine);
       int top = mine;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) top = max(top, __shfl_xor_sync(0xffffffffu, top, o));
@@ -266,30 +329,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
     }
     __syncthreads();
     if (s_fail) break;
-    // record the colours and set them in the bins and lines
-    if (warp < m) {
-      const int c = col[warp], l = vline[warp];
-      const unsigned long long bit = 1ull << (c & 63);
-      const int wk = c >> 6;
-      const int nb = A.nb, dv = 32 / nb, db = 32 - dv * nb;
-      for (int v = lane / nb, b = lane - (lane / nb) * nb; v < nt;) {  // lanes over (view, bin)
-        const int32_t p = pk[warp * nt + v];
-        if ((static_cast<unsigned>(p) >> b) & 1u)
-          atomicOr(A.bin_used + (static_cast<size_t>(v) * A.n_r + (p >> 16) + b) * W + wk, bit);
-        v += dv;
-        b += db;
-        if (b >= nb) {
-          b -= nb;
-          ++v;
-        }
-      }
-      if (lane == 0) {
-        atomicOr(A.line_used + static_cast<size_t>(l) * W + wk, bit);
-        A.colour[s + warp] = static_cast<int16_t>(c);
-      }
-    }
-    __threadfence_block();
-    __syncthreads();
+    mp = m;
   }
   if (s_fail) {
     if (tid == 0) {
@@ -343,7 +383,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
 }  // namespace
 
 size_t colour_smem_bytes(int n_theta, int words) {
-  return sizeof(int32_t) * kBlock * n_theta + sizeof(unsigned long long) * kBlock * words +
+  return sizeof(int32_t) * 2 * kBlock * n_theta + sizeof(unsigned long long) * kBlock * words +
          sizeof(int) * 64 * words;
 }
 
@@ -360,7 +400,7 @@ int launch_colour_schedule(const ColourArgs& a, void* stream) {
   cudaMemsetAsync(a.bin_used, 0, bins * sizeof(unsigned long long), s);
   cudaMemsetAsync(a.line_used, 0, lines * sizeof(unsigned long long), s);
   if (a.n > 0) {
-    const size_t csm = sizeof(int32_t) * kBlock * a.n_theta;
+    const size_t csm = sizeof(int32_t) * 2 * kBlock * a.n_theta;
     static const int lim = dyn_smem_limit(colour_conflicts_kernel);
     if (csm > static_cast<size_t>(lim)) return -7;
     cudaError_t e = cudaFuncSetAttribute(colour_conflicts_kernel,

@@ -179,7 +179,7 @@ int Engine::bf_prepare_schedule() {
         (static_cast<uint32_t>(static_cast<uint16_t>(acol_lo_[i])) << 16) | acol_mask_[i]);
   if (cudaMalloc(&d_packed_, packed.size() * sizeof(int32_t)) != cudaSuccess ||
       cudaMalloc(&d_vis_, nl * sizeof(int32_t)) != cudaSuccess ||
-      cudaMalloc(&d_conf_, nl * sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(&d_conf_, 2 * nl * sizeof(unsigned)) != cudaSuccess ||
       cudaMalloc(&d_colour_, nl * sizeof(int16_t)) != cudaSuccess ||
       cudaMalloc(&d_bin_used_, static_cast<size_t>(g.n_theta) * g.n_r * kColourWords * 8) !=
           cudaSuccess ||
@@ -265,6 +265,7 @@ int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
     ca.vis = d_vis_;
     ca.n = static_cast<int>(vis_host_.size());
     ca.conf = d_conf_;
+    ca.conf_prev = d_conf_ + static_cast<size_t>(g.n_z) * g.n_x;
     ca.colour = d_colour_;
     ca.bin_used = d_bin_used_;
     ca.line_used = d_line_used_;

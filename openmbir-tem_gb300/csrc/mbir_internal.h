@@ -156,6 +156,7 @@ struct ColourArgs {
   const int32_t* vis;             // [n] the call's lines (lineok and active), ascending
   int n;
   unsigned* conf;                 // [n] scratch: conflict words of each block of 32 lines
+  unsigned* conf_prev;            // [n] scratch: conflict words against the previous block
   int16_t* colour;                // [n_z*n_x] scratch: colour of each of the call's lines
   unsigned long long* bin_used;   // [n_theta][n_r][words] scratch, cleared by the launcher
   unsigned long long* line_used;  // [n_z*n_x][words] scratch, cleared by the launcher
