@@ -8,17 +8,18 @@
 // within a colour), the colour offsets and the counts, all in device memory, so the sweep that
 // follows reads them without a host round trip.
 //
-// Lines are coloured 32 at a time (a block).  First, one CTA per block computes the block's
+// Lines are coloured 31 at a time (a block: warp 0 colours one block while the other 31 warps
+// read for the next, one line each).  First, one CTA per block computes the block's
 // conflict words from the lines' footprints (bit j of conf[i]: line j < i of the block
-// conflicts with line i; bit j of conf_prev[i]: line j of the previous block does); this needs
-// no colours, so every block runs in parallel.  Then one CTA of 1024 threads walks the blocks in
-// order.  Each step ORs the colours of the previous block into the bit planes of its bins and
-// lines (global memory, L2-resident) while every warp reads the planes of its line's bins and
-// neighbours: they hold every block before the previous one, and the previous block's colours
-// that a line must see (those of lines it conflicts with) come from conf_prev, so the planes
-// being updated meanwhile change nothing.  Warp 0 then assigns the 32 colours in order, which
-// is the sequential greedy choice because each line also sees the colours of the earlier lines
-// of its block that it conflicts with.
+// conflicts with line i; conf_p1[i], conf_p2[i]: line j of the block before, of the one before
+// that); this needs no colours, so every block runs in parallel.  Then one CTA of 1024 threads
+// walks the blocks in order.  While warp 0 assigns the colours of block b in order (the
+// sequential greedy choice, because each line also sees the colours of the earlier lines of its
+// block that it conflicts with), warps 1-31 OR the colours of block b-1 into the bit planes of
+// its bins and lines (global memory, L2-resident) and read, for block b+1, the planes of each
+// line's bins and neighbours.  Those hold every block before b-1; the colours of blocks b-1 and
+// b that a line must see (those of the lines it conflicts with) are added from conf_p2 and
+// conf_p1 once block b is coloured, so the planes being updated meanwhile change nothing.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -29,7 +30,12 @@ namespace mbir {
 namespace {
 
 constexpr int kThreads = 1024;
-constexpr int kBlock = 32;  // lines coloured per step
+constexpr int kBlock = 31;  // lines coloured per step
+
+// int32 footprints of 3 blocks, rounded up to 16 bytes so that what follows stays aligned
+__host__ __device__ constexpr size_t footprint_ints(int n_theta) {
+  return (static_cast<size_t>(3 * kBlock) * n_theta + 3) & ~static_cast<size_t>(3);
+}
 
 __device__ __forceinline__ bool bins_overlap(int32_t pi, int32_t pj) {
   const unsigned mi = static_cast<unsigned>(pi) & 0xffffu, mj = static_cast<unsigned>(pj) & 0xffffu;
@@ -64,21 +70,21 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* warp_sums, int* 
   return warp_sums[warp] + incl - v;
 }
 
-// conflict words of block blockIdx.x of the call's lines: within the block and against the
-// previous block
+// conflict words of block blockIdx.x of the call's lines: within the block and against the two
+// blocks before it
 __global__ void __launch_bounds__(kThreads) colour_conflicts_kernel(ColourArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nt = A.n_theta, nx = A.n_x;
-  int32_t* pk = reinterpret_cast<int32_t*>(smem);  // [2 kBlock][nt]: this block, previous block
-  __shared__ int vz[2 * kBlock], vx[2 * kBlock];
+  int32_t* pk = reinterpret_cast<int32_t*>(smem);  // [3 kBlock][nt]: this block, b-1, b-2
+  __shared__ int vz[3 * kBlock], vx[3 * kBlock];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int s = blockIdx.x * kBlock;
+  const int bk = blockIdx.x, s = bk * kBlock;
   const int m = min(kBlock, A.n - s);
-  const int mp = blockIdx.x > 0 ? kBlock : 0;
   if (m <= 0) return;
-  for (int r = warp; r < 2 * kBlock; r += kThreads / 32) {
-    if (r < kBlock ? r >= m : r - kBlock >= mp) continue;
-    const int l = A.vis[r < kBlock ? s + r : s - kBlock + (r - kBlock)];
+  for (int r = warp; r < 3 * kBlock; r += kThreads / 32) {
+    const int d = r / kBlock, j = r - d * kBlock;  // block bk - d, line j
+    if (bk < d || (d == 0 && j >= m)) continue;
+    const int l = A.vis[(bk - d) * kBlock + j];
     const int32_t* pl = A.packed + static_cast<size_t>(l) * nt;
     for (int v = lane; v < nt; v += 32) pk[r * nt + v] = pl[v];
     if (lane == 0) {
@@ -89,36 +95,127 @@ __global__ void __launch_bounds__(kThreads) colour_conflicts_kernel(ColourArgs A
   __syncthreads();
   if (warp < m) {
     const int i = warp, j = lane;
-    bool c = false;
-    if (j < i) {
-      c = abs(vz[i] - vz[j]) <= 1 && abs(vx[i] - vx[j]) <= 1;
-      for (int v = 0; v < nt && !c; ++v) c = bins_overlap(pk[i * nt + v], pk[j * nt + v]);
+    unsigned words[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      bool c = false;
+      if (d == 0 ? j < i : (bk >= d && j < kBlock)) {
+        const int q = d * kBlock + j;
+        c = abs(vz[i] - vz[q]) <= 1 && abs(vx[i] - vx[q]) <= 1;
+        for (int v = 0; v < nt && !c; ++v) c = bins_overlap(pk[i * nt + v], pk[q * nt + v]);
+      }
+      words[d] = __ballot_sync(0xffffffffu, c);
     }
-    bool cp = false;
-    if (j < mp) {
-      const int q = kBlock + j;
-      cp = abs(vz[i] - vz[q]) <= 1 && abs(vx[i] - vx[q]) <= 1;
-      for (int v = 0; v < nt && !cp; ++v) cp = bins_overlap(pk[i * nt + v], pk[q * nt + v]);
-    }
-    const unsigned b = __ballot_sync(0xffffffffu, c), bp = __ballot_sync(0xffffffffu, cp);
     if (lane == 0) {
-      A.conf[s + i] = b;
-      A.conf_prev[s + i] = bp;
+      A.conf[s + i] = words[0];
+      A.conf_p1[s + i] = words[1];
+      A.conf_p2[s + i] = words[2];
     }
   }
+}
+
+// One warp: line l's footprints into pw and the colours taken at its bins and neighbour lines
+// (words below uw, read from the bit planes when planes is set) into Fl[0..W).  Each lane
+// group reads one word pair, its lanes over (view, bin), so that consecutive lanes read
+// neighbouring bins and a load touches few cache lines; four loads in flight per lane.
+__device__ __forceinline__ void load_line(const ColourArgs& A, int W, int uw, int l, int32_t* pw,
+                                          unsigned long long* Fl, bool planes) {
+  const int lane = threadIdx.x & 31;
+  const int nt = A.n_theta, nx = A.n_x, nb = A.nb;
+  const int32_t* pl = A.packed + static_cast<size_t>(l) * nt;
+  for (int v = lane; v < nt; v += 32) pw[v] = pl[v];
+  __syncwarp();
+  if (!planes) {
+    if (lane < W) Fl[lane] = 0ull;
+    return;
+  }
+  const int z = l / nx, x = l - z * nx;
+  const int np = uw <= 2 ? 1 : uw <= 4 ? 2 : 4;  // word pairs read (W is 2, 4 or 8)
+  const int gs = 32 / np;                        // lanes per word pair
+  const int kk = lane / gs, sub = lane - kk * gs;
+  const int dv = gs / nb, db = gs - dv * nb;
+  unsigned long long fx = 0ull, fy = 0ull;
+  int v = sub / nb, b = sub - (sub / nb) * nb;
+  while (v < nt) {
+    ulonglong2 q[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      q[u] = make_ulonglong2(0ull, 0ull);
+      if (v < nt) {
+        const int32_t p = pw[v];
+        if ((static_cast<unsigned>(p) >> b) & 1u) {
+          const size_t row = (static_cast<size_t>(v) * A.n_r + (p >> 16) + b) * W;
+          q[u] = __ldcg(reinterpret_cast<const ulonglong2*>(A.bin_used + row) + kk);
+        }
+      }
+      v += dv;
+      b += db;
+      if (b >= nb) {
+        b -= nb;
+        ++v;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      fx |= q[u].x;
+      fy |= q[u].y;
+    }
+  }
+  for (int q = sub; q < 9; q += gs) {
+    const int zz = z + q / 3 - 1, xx = x + q % 3 - 1;
+    if (zz >= 0 && zz < A.n_z && xx >= 0 && xx < nx) {
+      const size_t row = (static_cast<size_t>(zz) * nx + xx) * W;
+      const ulonglong2 u = __ldcg(reinterpret_cast<const ulonglong2*>(A.line_used + row) + kk);
+      fx |= u.x;
+      fy |= u.y;
+    }
+  }
+  for (int o = gs >> 1; o > 0; o >>= 1) {
+    fx |= __shfl_xor_sync(0xffffffffu, fx, o);
+    fy |= __shfl_xor_sync(0xffffffffu, fy, o);
+  }
+  if (sub == 0) {
+    Fl[2 * kk] = fx;
+    Fl[2 * kk + 1] = fy;
+  }
+  if (lane == 0)  // words from 2 np on hold no colours of these planes
+    for (int k = 2 * np; k < W; ++k) Fl[k] = 0ull;
+}
+
+// One warp: colour c of line l (footprints pw) ORed into the bit planes of its bins and line,
+// lanes over (view, bin); not waited for.
+__device__ __forceinline__ void set_line(const ColourArgs& A, int W, const int32_t* pw, int l,
+                                         int c) {
+  const int lane = threadIdx.x & 31;
+  const int nt = A.n_theta, nb = A.nb;
+  const unsigned long long bit = 1ull << (c & 63);
+  const int wk = c >> 6;
+  const int dv = 32 / nb, db = 32 - dv * nb;
+  for (int v = lane / nb, b = lane - (lane / nb) * nb; v < nt;) {
+    const int32_t p = pw[v];
+    if ((static_cast<unsigned>(p) >> b) & 1u)
+      atomicOr(A.bin_used + (static_cast<size_t>(v) * A.n_r + (p >> 16) + b) * W + wk, bit);
+    v += dv;
+    b += db;
+    if (b >= nb) {
+      b -= nb;
+      ++v;
+    }
+  }
+  if (lane == 0) atomicOr(A.line_used + static_cast<size_t>(l) * W + wk, bit);
 }
 
 __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int W = A.words;
-  const int nt = A.n_theta, nx = A.n_x, nl = A.n_z * A.n_x;
-  int32_t* pk = reinterpret_cast<int32_t*>(smem);  // [2][kBlock][nt] footprints, by block parity
-  // [kBlock][W] colours taken for each line of the block
-  unsigned long long* F = reinterpret_cast<unsigned long long*>(pk + 2 * kBlock * nt);
-  int* csize = reinterpret_cast<int*>(F + kBlock * W);  // [64 W] class sizes
-  __shared__ unsigned conf[kBlock];
-  __shared__ int col[2][kBlock];  // colours, by block parity
-  __shared__ int vline[2][kBlock];
+  const int nt = A.n_theta;
+  int32_t* pk = reinterpret_cast<int32_t*>(smem);  // [3][kBlock][nt] footprints, block index % 3
+  // [2][kBlock][W] colours taken for each line of a block, by block parity
+  unsigned long long* F = reinterpret_cast<unsigned long long*>(pk + footprint_ints(nt));
+  int* csize = reinterpret_cast<int*>(F + 2 * kBlock * W);  // [64 W] class sizes
+  __shared__ unsigned conf[2][32];  // in-block conflict words, by block parity
+  __shared__ int col[3][32];        // colours (a lane each), block index % 3
+  __shared__ int vline[3][32];
   __shared__ int warp_sums[32];
   __shared__ unsigned long long full_s[8];
   __shared__ int s_total, s_ncol, s_fail;
@@ -130,114 +227,26 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
     s_ncol = 0;
     s_fail = 0;
   }
-  (void)nl;
   const int n = A.n;  // the call's lines, ascending, in A.vis
   __syncthreads();
 
-  // phase 1: colour kBlock lines per step
-  int mp = 0;  // lines of the previous block
-  for (int s = 0; s < n; s += kBlock) {
-    const int m = min(kBlock, n - s);
-    const int cur = (s / kBlock) & 1, prv = cur ^ 1;
-    const int uw = min(s_ncol / 64 + 1, W);  // words holding colours so far
-    const int nb = A.nb;
-    // the previous block's colours into the planes of its bins and lines, not waited for here;
-    // lanes over (view, bin)
-    if (warp < mp) {
-      const int c = col[prv][warp];
-      const unsigned long long bit = 1ull << (c & 63);
-      const int wk = c >> 6;
-      const int32_t* pw = pk + (prv * kBlock + warp) * nt;
-      const int dv = 32 / nb, db = 32 - dv * nb;
-      for (int v = lane / nb, b = lane - (lane / nb) * nb; v < nt;) {
-        const int32_t p = pw[v];
-        if ((static_cast<unsigned>(p) >> b) & 1u)
-          atomicOr(A.bin_used + (static_cast<size_t>(v) * A.n_r + (p >> 16) + b) * W + wk, bit);
-        v += dv;
-        b += db;
-        if (b >= nb) {
-          b -= nb;
-          ++v;
-        }
-      }
-      if (lane == 0) atomicOr(A.line_used + static_cast<size_t>(vline[prv][warp]) * W + wk, bit);
+  // phase 1: colour kBlock lines per step; block 0's lines need no planes (nothing coloured)
+  const int nblk = (n + kBlock - 1) / kBlock;
+  int ncol_w = 0;  // warp 0: colours so far, published in s_ncol between steps
+  if (warp < min(kBlock, n)) {
+    load_line(A, W, 1, A.vis[warp], pk + warp * nt, F + warp * W, false);
+    if (lane == 0) {
+      vline[0][warp] = A.vis[warp];
+      conf[0][warp] = A.conf[warp];
     }
-    if (warp < m) {
-      const int l = A.vis[s + warp];
-      const unsigned cprev = A.conf_prev[s + warp];
-      const int z = l / nx, x = l - z * nx;
-      // footprints once, then every word pair in use of each touched bin and neighbour line:
-      // each lane group reads one word pair, its lanes over (view, bin), so that consecutive
-      // lanes read neighbouring bins and a load touches few cache lines; eight loads in flight
-      int32_t* pw = pk + (cur * kBlock + warp) * nt;
-      const int32_t* pl = A.packed + static_cast<size_t>(l) * nt;
-      for (int v = lane; v < nt; v += 32) pw[v] = pl[v];
-      __syncwarp();
-      const int np = uw <= 2 ? 1 : uw <= 4 ? 2 : 4;  // word pairs read (W is 2, 4 or 8)
-      const int gs = 32 / np;                        // lanes per word pair
-      const int kk = lane / gs, sub = lane - kk * gs;
-      const int dv = gs / nb, db = gs - dv * nb;
-      unsigned long long fx = 0ull, fy = 0ull;
-      int v = sub / nb, b = sub - (sub / nb) * nb;
-      while (v < nt) {
-        ulonglong2 q[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          q[u] = make_ulonglong2(0ull, 0ull);
-          if (v < nt) {
-            const int32_t p = pw[v];
-            if ((static_cast<unsigned>(p) >> b) & 1u) {
-              const size_t row = (static_cast<size_t>(v) * A.n_r + (p >> 16) + b) * W;
-              q[u] = __ldcg(reinterpret_cast<const ulonglong2*>(A.bin_used + row) + kk);
-            }
-          }
-          v += dv;
-          b += db;
-          if (b >= nb) {
-            b -= nb;
-            ++v;
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          fx |= q[u].x;
-          fy |= q[u].y;
-        }
-      }
-      for (int q = sub; q < 9; q += gs) {
-        const int zz = z + q / 3 - 1, xx = x + q % 3 - 1;
-        if (zz >= 0 && zz < A.n_z && xx >= 0 && xx < nx) {
-          const size_t row = (static_cast<size_t>(zz) * nx + xx) * W;
-          const ulonglong2 u = __ldcg(reinterpret_cast<const ulonglong2*>(A.line_used + row) + kk);
-          fx |= u.x;
-          fy |= u.y;
-        }
-      }
-      for (int o = gs >> 1; o > 0; o >>= 1) {
-        fx |= __shfl_xor_sync(0xffffffffu, fx, o);
-        fy |= __shfl_xor_sync(0xffffffffu, fy, o);
-      }
-      if (sub == 0) {
-        F[warp * W + 2 * kk] = fx;
-        F[warp * W + 2 * kk + 1] = fy;
-      }
-      // words from 2 np on hold no colours yet
-      if (lane == 0)
-        for (int k = 2 * np; k < W; ++k) F[warp * W + k] = 0ull;
-      __syncwarp();
-      // the colours of the previous block's lines that this line conflicts with (the planes
-      // may or may not hold them yet)
-      if ((cprev >> lane) & 1u) {
-        const int c = col[prv][lane];
-        atomicOr(&F[warp * W + (c >> 6)], 1ull << (c & 63));
-      }
-      if (lane == 0) {
-        vline[cur][warp] = l;
-        conf[warp] = A.conf[s + warp];
-      }
-    }
-    __threadfence_block();  // this step's plane updates land before the next step reads
-    __syncthreads();
+  }
+  __syncthreads();
+  for (int bk = 0; bk < nblk; ++bk) {
+    const int s = bk * kBlock, m = min(kBlock, n - s);
+    const int mp = bk > 0 ? kBlock : 0;                                 // lines of block bk-1
+    const int mn = bk + 1 < nblk ? min(kBlock, n - s - kBlock) : 0;  // lines of block bk+1
+    const int cur = bk % 3, nxt = (bk + 1) % 3, prv = (bk + 2) % 3;
+    const int fc = bk & 1, fn = fc ^ 1;
     // warp 0: the greedy choice, line by line, on a window of 64 colours from base, the lowest
     // colour free for some line of the block (colours below it are full or taken for every
     // line, and stay so).  Every lane keeps in
@@ -246,10 +255,11 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
     // with no free colour in the window takes the first free colour found from the shared
     // copies (written back for it); classes beyond the window are counted in shared memory.
     if (warp == 0) {
+      const unsigned long long* Fb = F + fc * kBlock * W;
       int base = 64 * W;
       if (lane < m)
         for (int k = 0; k < W; ++k) {
-          const unsigned long long t = F[lane * W + k] | full_s[k];
+          const unsigned long long t = Fb[lane * W + k] | full_s[k];
           if (~t) {
             base = 64 * k + __ffsll(static_cast<long long>(~t)) - 1;
             break;
@@ -262,7 +272,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
         const unsigned long long lo = k0 < W ? v[k0] : 0ull, hi = k0 + 1 < W ? v[k0 + 1] : 0ull;
         return sh ? (lo >> sh) | (hi << (64 - sh)) : lo;
       };
-      unsigned long long acc = lane < m ? window(F + lane * W) : 0ull;
+      unsigned long long acc = lane < m ? window(Fb + lane * W) : 0ull;
       // colours from max_colours on count as full, so a free window colour is a valid one
       const int lim = A.max_colours - base;
       unsigned long long fullw =
@@ -270,7 +280,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
       const int cap = A.class_cap > 0 ? A.class_cap : 0x7fffffff;
       const int cl = base + lane, ch = base + 32 + lane;  // this lane's two window classes
       int n_lo = cl < 64 * W ? csize[cl] : 0, n_hi = ch < 64 * W ? csize[ch] : 0;
-      const unsigned my_conf = lane < m ? conf[lane] : 0u;
+      const unsigned my_conf = lane < m ? conf[fc][lane] : 0u;
       int mine = -1;
       bool fail = false;
       auto write_back = [&]() {
@@ -293,7 +303,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
           int cc = -1;
           if (lane == i)
             for (int k = 0; k < W && cc < 0; ++k) {
-              unsigned long long t = F[i * W + k] | full_s[k];
+              unsigned long long t = Fb[i * W + k] | full_s[k];
               for (unsigned b = my_conf; b; b &= b - 1u) {
                 const int q = col[cur][__ffs(b) - 1];
                 if ((q >> 6) == k) t |= 1ull << (q & 63);
@@ -322,14 +332,40 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
       int top = mine;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) top = max(top, __shfl_xor_sync(0xffffffffu, top, o));
-      if (lane == 0) {
-        if (fail) s_fail = 1;
-        s_ncol = max(s_ncol, top + 1);
+      ncol_w = max(ncol_w, top + 1);
+      if (lane == 0 && fail) s_fail = 1;
+    } else {
+      // warps 1-31: block bk-1's colours into the planes, then block bk+1's colour sets
+      const int uw = min(s_ncol / 64 + 1, W);  // words holding colours of blocks before bk
+      for (int j = warp - 1; j < mp; j += kThreads / 32 - 1)
+        set_line(A, W, pk + (prv * kBlock + j) * nt, vline[prv][j], col[prv][j]);
+      for (int j = warp - 1; j < mn; j += kThreads / 32 - 1) {
+        const int l = A.vis[s + kBlock + j];
+        load_line(A, W, uw, l, pk + (nxt * kBlock + j) * nt, F + (fn * kBlock + j) * W, true);
+        if (lane == 0) {
+          vline[nxt][j] = l;
+          conf[fn][j] = A.conf[s + kBlock + j];
+        }
       }
     }
+    __threadfence_block();  // this step's plane updates land before the next step reads
     __syncthreads();
     if (s_fail) break;
-    mp = m;
+    // the colours of blocks bk-1 and bk that the lines of block bk+1 conflict with
+    if (warp < mn) {
+      const unsigned c1 = A.conf_p1[s + kBlock + warp], c2 = A.conf_p2[s + kBlock + warp];
+      unsigned long long* Fl = F + (fn * kBlock + warp) * W;
+      if ((c1 >> lane) & 1u) {
+        const int c = col[cur][lane];
+        atomicOr(&Fl[c >> 6], 1ull << (c & 63));
+      }
+      if ((c2 >> lane) & 1u) {
+        const int c = col[prv][lane];
+        atomicOr(&Fl[c >> 6], 1ull << (c & 63));
+      }
+    }
+    if (tid == 0) s_ncol = ncol_w;
+    __syncthreads();
   }
   if (s_fail) {
     if (tid == 0) {
@@ -383,8 +419,16 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
 }  // namespace
 
 size_t colour_smem_bytes(int n_theta, int words) {
-  return sizeof(int32_t) * 2 * kBlock * n_theta + sizeof(unsigned long long) * kBlock * words +
+  return sizeof(int32_t) * footprint_ints(n_theta) +
+         sizeof(unsigned long long) * 2 * kBlock * words +
          sizeof(int) * 64 * words;
+}
+
+bool colour_schedule_fits(int n_theta, int words) {
+  static const int lim_c = dyn_smem_limit(colour_conflicts_kernel);
+  static const int lim_k = dyn_smem_limit(colour_kernel);
+  return sizeof(int32_t) * 3 * kBlock * n_theta <= static_cast<size_t>(lim_c) &&
+         colour_smem_bytes(n_theta, words) <= static_cast<size_t>(lim_k);
 }
 
 int launch_colour_schedule(const ColourArgs& a, void* stream) {
@@ -400,7 +444,7 @@ int launch_colour_schedule(const ColourArgs& a, void* stream) {
   cudaMemsetAsync(a.bin_used, 0, bins * sizeof(unsigned long long), s);
   cudaMemsetAsync(a.line_used, 0, lines * sizeof(unsigned long long), s);
   if (a.n > 0) {
-    const size_t csm = sizeof(int32_t) * 2 * kBlock * a.n_theta;
+    const size_t csm = sizeof(int32_t) * 3 * kBlock * a.n_theta;
     static const int lim = dyn_smem_limit(colour_conflicts_kernel);
     if (csm > static_cast<size_t>(lim)) return -7;
     cudaError_t e = cudaFuncSetAttribute(colour_conflicts_kernel,

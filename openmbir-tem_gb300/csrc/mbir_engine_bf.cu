@@ -172,6 +172,7 @@ int Engine::bf_prepare_schedule() {
   acol_mask_.assign(nl * g.n_theta, 0);
   acol_bins(host.data(), static_cast<int>(nl), g.n_theta, nb_, acol_lo_.data(), acol_mask_.data());
   if (p_.call_schedule != 0) return MBIR_OK;
+  if (!colour_schedule_fits(g.n_theta, kColourWords)) return MBIR_OK;  // host colouring instead
   // device colour schedule: packed bins and scratch
   std::vector<int32_t> packed(nl * g.n_theta);
   for (size_t i = 0; i < packed.size(); ++i)
@@ -179,7 +180,7 @@ int Engine::bf_prepare_schedule() {
         (static_cast<uint32_t>(static_cast<uint16_t>(acol_lo_[i])) << 16) | acol_mask_[i]);
   if (cudaMalloc(&d_packed_, packed.size() * sizeof(int32_t)) != cudaSuccess ||
       cudaMalloc(&d_vis_, nl * sizeof(int32_t)) != cudaSuccess ||
-      cudaMalloc(&d_conf_, 2 * nl * sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(&d_conf_, 3 * nl * sizeof(unsigned)) != cudaSuccess ||
       cudaMalloc(&d_colour_, nl * sizeof(int16_t)) != cudaSuccess ||
       cudaMalloc(&d_bin_used_, static_cast<size_t>(g.n_theta) * g.n_r * kColourWords * 8) !=
           cudaSuccess ||
@@ -265,7 +266,8 @@ int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
     ca.vis = d_vis_;
     ca.n = static_cast<int>(vis_host_.size());
     ca.conf = d_conf_;
-    ca.conf_prev = d_conf_ + static_cast<size_t>(g.n_z) * g.n_x;
+    ca.conf_p1 = d_conf_ + static_cast<size_t>(g.n_z) * g.n_x;
+    ca.conf_p2 = d_conf_ + 2 * static_cast<size_t>(g.n_z) * g.n_x;
     ca.colour = d_colour_;
     ca.bin_used = d_bin_used_;
     ca.line_used = d_line_used_;

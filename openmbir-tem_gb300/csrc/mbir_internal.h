@@ -156,7 +156,8 @@ struct ColourArgs {
   const int32_t* vis;             // [n] the call's lines (lineok and active), ascending
   int n;
   unsigned* conf;                 // [n] scratch: conflict words of each block of 32 lines
-  unsigned* conf_prev;            // [n] scratch: conflict words against the previous block
+  unsigned* conf_p1;              // [n] scratch: conflict words against the block before
+  unsigned* conf_p2;              // [n] scratch: against the block before that
   int16_t* colour;                // [n_z*n_x] scratch: colour of each of the call's lines
   unsigned long long* bin_used;   // [n_theta][n_r][words] scratch, cleared by the launcher
   unsigned long long* line_used;  // [n_z*n_x][words] scratch, cleared by the launcher
@@ -167,6 +168,7 @@ struct ColourArgs {
 };
 int launch_colour_schedule(const ColourArgs& a, void* stream);
 size_t colour_smem_bytes(int n_theta, int words);
+bool colour_schedule_fits(int n_theta, int words);  // shared memory of both kernels
 
 // Batched sweep: per-series sweep arguments and a queue of (series, slice y) items.
 struct BatchArgs {
