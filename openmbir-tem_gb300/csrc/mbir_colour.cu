@@ -114,21 +114,14 @@ __global__ void __launch_bounds__(kThreads) colour_conflicts_kernel(ColourArgs A
   }
 }
 
-// One warp: line l's footprints into pw and the colours taken at its bins and neighbour lines
-// (words below uw, read from the bit planes when planes is set) into Fl[0..W).  Each lane
-// group reads one word pair, its lanes over (view, bin), so that consecutive lanes read
-// neighbouring bins and a load touches few cache lines; four loads in flight per lane.
-__device__ __forceinline__ void load_line(const ColourArgs& A, int W, int uw, int l, int32_t* pw,
-                                          unsigned long long* Fl, bool planes) {
+// One warp: the colours taken at the bins (footprints pw) and neighbour lines of line l, words
+// below uw, read from the bit planes into Fl[0..W).  Each lane group reads one word pair, its
+// lanes over (view, bin), so that consecutive lanes read neighbouring bins and a load touches
+// few cache lines; four loads in flight per lane.
+__device__ __forceinline__ void load_planes(const ColourArgs& A, int W, int uw, int l,
+                                            const int32_t* pw, unsigned long long* Fl) {
   const int lane = threadIdx.x & 31;
   const int nt = A.n_theta, nx = A.n_x, nb = A.nb;
-  const int32_t* pl = A.packed + static_cast<size_t>(l) * nt;
-  for (int v = lane; v < nt; v += 32) pw[v] = pl[v];
-  __syncwarp();
-  if (!planes) {
-    if (lane < W) Fl[lane] = 0ull;
-    return;
-  }
   const int z = l / nx, x = l - z * nx;
   const int np = uw <= 2 ? 1 : uw <= 4 ? 2 : 4;  // word pairs read (W is 2, 4 or 8)
   const int gs = 32 / np;                        // lanes per word pair
@@ -231,15 +224,21 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
   __syncthreads();
 
   // phase 1: colour kBlock lines per step; block 0's lines need no planes (nothing coloured)
+  static_assert(kThreads / 32 - 1 == kBlock, "one reading warp per line of a block");
   const int nblk = (n + kBlock - 1) / kBlock;
   int ncol_w = 0;  // warp 0: colours so far, published in s_ncol between steps
   if (warp < min(kBlock, n)) {
-    load_line(A, W, 1, A.vis[warp], pk + warp * nt, F + warp * W, false);
+    const int l = A.vis[warp];
+    const int32_t* pl = A.packed + static_cast<size_t>(l) * nt;
+    for (int v = lane; v < nt; v += 32) pk[warp * nt + v] = pl[v];
+    if (lane < W) F[warp * W + lane] = 0ull;
     if (lane == 0) {
-      vline[0][warp] = A.vis[warp];
+      vline[0][warp] = l;
       conf[0][warp] = A.conf[warp];
     }
   }
+  // reading warps: the line of block 1 (read a step ahead from here on)
+  int l_ahead = warp >= 1 && kBlock + warp - 1 < n ? A.vis[kBlock + warp - 1] : 0;
   __syncthreads();
   for (int bk = 0; bk < nblk; ++bk) {
     const int s = bk * kBlock, m = min(kBlock, n - s);
@@ -335,16 +334,32 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
       ncol_w = max(ncol_w, top + 1);
       if (lane == 0 && fail) s_fail = 1;
     } else {
-      // warps 1-31: block bk-1's colours into the planes, then block bk+1's colour sets
+      // warps 1-31, one line j each: the footprints of block bk+1's line (its line read a step
+      // ahead) requested first, block bk-1's colours into the planes meanwhile, then block
+      // bk+1's colour sets
+      const int j = warp - 1;
       const int uw = min(s_ncol / 64 + 1, W);  // words holding colours of blocks before bk
-      for (int j = warp - 1; j < mp; j += kThreads / 32 - 1)
-        set_line(A, W, pk + (prv * kBlock + j) * nt, vline[prv][j], col[prv][j]);
-      for (int j = warp - 1; j < mn; j += kThreads / 32 - 1) {
-        const int l = A.vis[s + kBlock + j];
-        load_line(A, W, uw, l, pk + (nxt * kBlock + j) * nt, F + (fn * kBlock + j) * W, true);
+      const int l = l_ahead;
+      const int32_t* pl = A.packed + static_cast<size_t>(l) * nt;
+      int32_t f0 = 0, f1 = 0;
+      unsigned cw = 0u;
+      if (j < mn) {
+        if (lane < nt) f0 = pl[lane];
+        if (lane + 32 < nt) f1 = pl[lane + 32];
+        cw = A.conf[s + kBlock + j];
+      }
+      l_ahead = s + 2 * kBlock + j < n ? A.vis[s + 2 * kBlock + j] : 0;
+      if (j < mp) set_line(A, W, pk + (prv * kBlock + j) * nt, vline[prv][j], col[prv][j]);
+      if (j < mn) {
+        int32_t* pw = pk + (nxt * kBlock + j) * nt;
+        if (lane < nt) pw[lane] = f0;
+        if (lane + 32 < nt) pw[lane + 32] = f1;
+        for (int v = lane + 64; v < nt; v += 32) pw[v] = pl[v];
+        __syncwarp();
+        load_planes(A, W, uw, l, pw, F + (fn * kBlock + j) * W);
         if (lane == 0) {
           vline[nxt][j] = l;
-          conf[fn][j] = A.conf[s + kBlock + j];
+          conf[fn][j] = cw;
         }
       }
     }
