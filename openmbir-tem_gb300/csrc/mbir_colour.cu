@@ -127,6 +127,17 @@ __device__ __forceinline__ void load_planes(const ColourArgs& A, int W, int uw, 
   const int gs = 32 / np;                        // lanes per word pair
   const int kk = lane / gs, sub = lane - kk * gs;
   const int dv = gs / nb, db = gs - dv * nb;
+  // the neighbour lines first, in flight with the first bin loads
+  ulonglong2 un = make_ulonglong2(0ull, 0ull);
+  for (int q = sub; q < 9; q += gs) {
+    const int zz = z + q / 3 - 1, xx = x + q % 3 - 1;
+    if (zz >= 0 && zz < A.n_z && xx >= 0 && xx < nx) {
+      const size_t row = (static_cast<size_t>(zz) * nx + xx) * W;
+      const ulonglong2 u = __ldcg(reinterpret_cast<const ulonglong2*>(A.line_used + row) + kk);
+      un.x |= u.x;
+      un.y |= u.y;
+    }
+  }
   unsigned long long fx = 0ull, fy = 0ull;
   int v = sub / nb, b = sub - (sub / nb) * nb;
   while (v < nt) {
@@ -154,15 +165,8 @@ __device__ __forceinline__ void load_planes(const ColourArgs& A, int W, int uw, 
       fy |= q[u].y;
     }
   }
-  for (int q = sub; q < 9; q += gs) {
-    const int zz = z + q / 3 - 1, xx = x + q % 3 - 1;
-    if (zz >= 0 && zz < A.n_z && xx >= 0 && xx < nx) {
-      const size_t row = (static_cast<size_t>(zz) * nx + xx) * W;
-      const ulonglong2 u = __ldcg(reinterpret_cast<const ulonglong2*>(A.line_used + row) + kk);
-      fx |= u.x;
-      fy |= u.y;
-    }
-  }
+  fx |= un.x;
+  fy |= un.y;
   for (int o = gs >> 1; o > 0; o >>= 1) {
     fx |= __shfl_xor_sync(0xffffffffu, fx, o);
     fy |= __shfl_xor_sync(0xffffffffu, fy, o);
@@ -207,6 +211,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
   unsigned long long* F = reinterpret_cast<unsigned long long*>(pk + footprint_ints(nt));
   int* csize = reinterpret_cast<int*>(F + 2 * kBlock * W);  // [64 W] class sizes
   __shared__ unsigned conf[2][32];  // in-block conflict words, by block parity
+  __shared__ unsigned cprev[2][32];  // the next block's words against blocks b and b-1
   __shared__ int col[3][32];        // colours (a lane each), block index % 3
   __shared__ int vline[3][32];
   __shared__ int warp_sums[32];
@@ -342,11 +347,13 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
       const int l = l_ahead;
       const int32_t* pl = A.packed + static_cast<size_t>(l) * nt;
       int32_t f0 = 0, f1 = 0;
-      unsigned cw = 0u;
+      unsigned cw = 0u, cw1 = 0u, cw2 = 0u;
       if (j < mn) {
         if (lane < nt) f0 = pl[lane];
         if (lane + 32 < nt) f1 = pl[lane + 32];
         cw = A.conf[s + kBlock + j];
+        cw1 = A.conf_p1[s + kBlock + j];
+        cw2 = A.conf_p2[s + kBlock + j];
       }
       l_ahead = s + 2 * kBlock + j < n ? A.vis[s + 2 * kBlock + j] : 0;
       if (j < mp) set_line(A, W, pk + (prv * kBlock + j) * nt, vline[prv][j], col[prv][j]);
@@ -360,6 +367,8 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
         if (lane == 0) {
           vline[nxt][j] = l;
           conf[fn][j] = cw;
+          cprev[0][j] = cw1;
+          cprev[1][j] = cw2;
         }
       }
     }
@@ -368,7 +377,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
     if (s_fail) break;
     // the colours of blocks bk-1 and bk that the lines of block bk+1 conflict with
     if (warp < mn) {
-      const unsigned c1 = A.conf_p1[s + kBlock + warp], c2 = A.conf_p2[s + kBlock + warp];
+      const unsigned c1 = cprev[0][warp], c2 = cprev[1][warp];
       unsigned long long* Fl = F + (fn * kBlock + warp) * W;
       if ((c1 >> lane) & 1u) {
         const int c = col[cur][lane];
