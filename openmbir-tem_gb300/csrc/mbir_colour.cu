@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(kThreads) colour_conflicts_kernel(ColourArgs A
 // One warp: the colours taken at the bins (footprints pw) and neighbour lines of line l, words
 // below uw, read from the bit planes into Fl[0..W).  Each lane group reads one word pair, its
 // lanes over (view, bin), so that consecutive lanes read neighbouring bins and a load touches
-// few cache lines; four loads in flight per lane.
+// few cache lines; six loads in flight per lane.
 __device__ __forceinline__ void load_planes(const ColourArgs& A, int W, int uw, int l,
                                             const int32_t* pw, unsigned long long* Fl) {
   const int lane = threadIdx.x & 31;
@@ -141,9 +141,9 @@ __device__ __forceinline__ void load_planes(const ColourArgs& A, int W, int uw, 
   unsigned long long fx = 0ull, fy = 0ull;
   int v = sub / nb, b = sub - (sub / nb) * nb;
   while (v < nt) {
-    ulonglong2 q[4];
+    ulonglong2 q[6];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 6; ++u) {
       q[u] = make_ulonglong2(0ull, 0ull);
       if (v < nt) {
         const int32_t p = pw[v];
@@ -160,7 +160,7 @@ __device__ __forceinline__ void load_planes(const ColourArgs& A, int W, int uw, 
       }
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 6; ++u) {
       fx |= q[u].x;
       fy |= q[u].y;
     }
