@@ -204,3 +204,30 @@ def test_bf_device_colour_schedule_matches_host(lib_built, oracle_mod):
         assert sg[3] == so[3] and sg[2] == so[2], (k, sg, so)
         assert rel(e.volume(), o.volume()) <= 1e-5, (k, rel(e.volume(), o.volume()))
         assert rel(e.error_sinogram(), o.error()) <= 1e-5, k
+
+
+@pytest.mark.parametrize("n_r", [32, 48])
+def test_bf_device_colour_schedule_short_calls(lib_built, n_r):
+    """Calls of two and three 31-line blocks of the device colouring (~50 and ~75 lines: the
+    first and last steps of its pipeline, a partial last block): the device schedule equals the
+    host definition."""
+    mbir = lib_built
+    y, ang, th = bf_case(n_r=n_r, n_t=4)
+    p = bf_params(mbir, th, call_schedule=0, bragg_threshold=5.0e10)
+    e = mbir.Engine(p)
+    e.set_sinogram(y, ang)
+    e.prepare()
+    lo, mask, ok = e.footprint_bins()
+    nz, nx = ok.shape
+    sizes = []
+    for k in range(6):
+        e.sweep(0, k)
+        lines, lofs = e.call_schedule()
+        sizes.append(len(lines))
+        act = np.zeros(nz * nx, np.uint8)
+        act[lines] = 1
+        hl, ho = mbir.colour_schedule(ok, lo, mask, 3, y.shape[1], act.reshape(nz, nx),
+                                      class_cap=32)
+        np.testing.assert_array_equal(lines, hl)
+        np.testing.assert_array_equal(lofs, ho)
+    assert 31 < min(sizes) and max(sizes) < 3 * 31, sizes
