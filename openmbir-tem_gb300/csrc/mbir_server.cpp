@@ -183,8 +183,8 @@ void Server::loop() {
         for (Request* r : cur) broken.emplace_back(r, batch_->last_error());
       } else {
         // per request, side by side: gain/offset, variance, cost and the stop test
-        // (verdict 0: continue, 1: finished, 2: failed)
-        std::vector<int> verdict(cur.size(), 0);
+        // (outcome 0: continue, 1: finished, 2: failed)
+        std::vector<int> outcome(cur.size(), 0);
         parallel_for(static_cast<int>(cur.size()), device_, [&](int k) {
           Request* r = cur[k];
           Engine* e = r->engine.get();
@@ -193,7 +193,7 @@ void Server::loop() {
           if (r->params.joint_estimation) erc = e->joint_estimation();
           if (!erc && (bf ? r->params.noise_estimation : r->params.noise_model))
             erc = e->update_weights();
-          if (erc) return verdict[k] = 2;
+          if (erc) return outcome[k] = 2;
           r->outer_done++;
           // a bright-field call updates 1/20 of the voxel lines (NHICD): the cost is compared
           // once per equivalent iteration of 20 calls
@@ -201,18 +201,18 @@ void Server::loop() {
           bool conv = false;
           if (r->outer_done % period == 0 || r->outer_done >= r->max_outer) {
             double c = 0;
-            if (e->compute_cost(nullptr, &c)) return verdict[k] = 2;
+            if (e->compute_cost(nullptr, &c)) return outcome[k] = 2;
             conv = r->outer_done > period && std::fabs(c - r->cost) <= r->tol * std::fabs(c);
             r->prev_cost = r->cost;
             r->cost = c;
           }
-          if (conv || r->outer_done >= r->max_outer) verdict[k] = 1;
+          if (conv || r->outer_done >= r->max_outer) outcome[k] = 1;
           return 0;
         });
         for (size_t k = 0; k < cur.size(); k++) {
-          if (verdict[k] == 2)
+          if (outcome[k] == 2)
             broken.emplace_back(cur[k], cur[k]->engine->last_error());
-          else if (verdict[k] == 1)
+          else if (outcome[k] == 1)
             finished.push_back(cur[k]);
         }
       }
