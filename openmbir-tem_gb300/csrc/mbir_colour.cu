@@ -22,9 +22,11 @@
 // conf_p1 once block b is coloured, so the planes being updated meanwhile change nothing.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "mbir_internal.h"
+#include "mbir_schedule.h"
 
 namespace mbir {
 namespace {
@@ -440,7 +442,26 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
   }
 }
 
+// packed[i] = packed_footprint of table entry i (wf floats each), i < n
+__global__ void pack_footprints_kernel(const float* __restrict__ table, size_t n, int wf, int nb,
+                                       int32_t* __restrict__ packed) {
+  const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+  for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    packed[i] = packed_footprint(table + i * wf, nb);
+}
+
 }  // namespace
+
+int launch_pack_footprints(const float4* table, size_t n, int nb, int32_t* packed, void* stream) {
+  if (nb < 1 || nb > 16) return -7;
+  if (n == 0) return 0;
+  constexpr int kPackThreads = 256;
+  const size_t blocks = std::min<size_t>((n + kPackThreads - 1) / kPackThreads, 152 * 16);
+  pack_footprints_kernel<<<static_cast<unsigned>(blocks), kPackThreads, 0,
+                           static_cast<cudaStream_t>(stream)>>>(
+      reinterpret_cast<const float*>(table), n, 4 * acol_width(nb), nb, packed);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
 
 size_t colour_smem_bytes(int n_theta, int words) {
   return sizeof(int32_t) * footprint_ints(n_theta) +

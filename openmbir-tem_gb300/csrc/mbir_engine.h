@@ -131,6 +131,7 @@ class Engine {
   int bf_run();
   int bf_roi_sum(int kind, double* out);
   int bf_prepare_schedule();                      // A-column table for level-scheduled calls
+  int host_footprint_bins();                      // acol_lo_, acol_mask_ (once, on demand)
   int bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a);  // the call's levels
   void bf_schedule_readback();                    // queue the device schedule's copy to host
   void bf_schedule_settle();                      // after the stream synchronised

@@ -142,9 +142,10 @@ int Engine::bf_upload() {
 }
 
 // Level-scheduled calls (FP32, parallel order, NHICD): the A-column table of every voxel line
-// (built once on the device by the sweep's own arithmetic) and, on the host, each entry's first
-// bin and nonzero mask, from which every call's dependency levels are computed.  Without room
-// for the table the calls walk the rows.
+// (built once on the device by the sweep's own arithmetic) and each entry's first bin and
+// nonzero mask: packed on the device for the device colouring, unpacked on the host
+// (host_footprint_bins) for the host schedules.  Without room for the table the calls walk the
+// rows.
 int Engine::bf_prepare_schedule() {
   if (fp64_ || !p_.nhicd || p_.order_mode != MBIR_ORDER_PARALLEL || p_.call_schedule == 1)
     return MBIR_OK;
@@ -165,20 +166,14 @@ int Engine::bf_prepare_schedule() {
                       d_lineok_};
   int rc = launch_acol_f32(dg_, tab, nb_, d_acol_, s);
   if (rc) return cuda_check(rc, "A-column table");
-  std::vector<float> host(n4 * 4);
-  cudaMemcpyAsync(host.data(), d_acol_, n4 * sizeof(float4), cudaMemcpyDeviceToHost, s);
-  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "A-column table");
-  acol_lo_.assign(nl * g.n_theta, 0);
-  acol_mask_.assign(nl * g.n_theta, 0);
-  acol_bins(host.data(), static_cast<int>(nl), g.n_theta, nb_, acol_lo_.data(), acol_mask_.data());
-  if (p_.call_schedule != 0) return MBIR_OK;
-  if (!colour_schedule_fits(g.n_theta, kColourWords)) return MBIR_OK;  // host colouring instead
+  acol_lo_.clear();
+  acol_mask_.clear();
+  // host schedules: the footprint bins on the host now
+  if (p_.call_schedule != 0 || !colour_schedule_fits(g.n_theta, kColourWords))
+    return host_footprint_bins();
   // device colour schedule: packed bins and scratch
-  std::vector<int32_t> packed(nl * g.n_theta);
-  for (size_t i = 0; i < packed.size(); ++i)
-    packed[i] = static_cast<int32_t>(
-        (static_cast<uint32_t>(static_cast<uint16_t>(acol_lo_[i])) << 16) | acol_mask_[i]);
-  if (cudaMalloc(&d_packed_, packed.size() * sizeof(int32_t)) != cudaSuccess ||
+  const size_t n_entries = nl * g.n_theta;
+  if (cudaMalloc(&d_packed_, n_entries * sizeof(int32_t)) != cudaSuccess ||
       cudaMalloc(&d_vis_, nl * sizeof(int32_t)) != cudaSuccess ||
       cudaMalloc(&d_conf_, 3 * nl * sizeof(unsigned)) != cudaSuccess ||
       cudaMalloc(&d_colour_, nl * sizeof(int16_t)) != cudaSuccess ||
@@ -200,13 +195,30 @@ int Engine::bf_prepare_schedule() {
     dfree_any(d_hc_lines_);
     dfree_any(d_hc_lofs_);
     dfree_any(d_hc_count_);
-    return MBIR_OK;  // host colouring instead
+    return host_footprint_bins();  // host colouring instead
   }
   hc_valid_.assign(kNumHomogeneous, 0);
   hc_start_.assign(kNumHomogeneous, 0);
-  cudaMemcpyAsync(d_packed_, packed.data(), packed.size() * sizeof(int32_t),
-                  cudaMemcpyHostToDevice, s);
+  if ((rc = launch_pack_footprints(d_acol_, n_entries, nb_, d_packed_, s)))
+    return cuda_check(rc, "packed bins");
   if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "packed bins");
+  return MBIR_OK;
+}
+
+// The A-column table's first bins and nonzero masks on the host (acol_lo_, acol_mask_), read
+// back from the device table once; used by the host schedules and mbir_get_footprint_bins.
+int Engine::host_footprint_bins() {
+  if (!acol_lo_.empty() || d_acol_ == nullptr) return MBIR_OK;
+  const Geometry& g = g_;
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const size_t nl = static_cast<size_t>(g.n_z) * g.n_x;
+  const size_t n4 = nl * g.n_theta * acol_width(nb_);
+  std::vector<float> host(n4 * 4);
+  cudaMemcpyAsync(host.data(), d_acol_, n4 * sizeof(float4), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "A-column table");
+  acol_lo_.assign(nl * g.n_theta, 0);
+  acol_mask_.assign(nl * g.n_theta, 0);
+  acol_bins(host.data(), static_cast<int>(nl), g.n_theta, nb_, acol_lo_.data(), acol_mask_.data());
   return MBIR_OK;
 }
 
@@ -289,6 +301,7 @@ int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
     if (cur_hslot_ >= 0) hc_valid_[cur_hslot_] = 1;
     return MBIR_OK;
   }
+  if (int rc = host_footprint_bins()) return rc;
   const auto t0 = std::chrono::steady_clock::now();
   LevelScheduleIn in{g.n_z, g.n_x, g.n_theta, g.n_r, nb_, stride_, rows.data(),
                      tab_.line_nonempty.data(), active_host_.data(), acol_lo_.data(),
@@ -714,6 +727,8 @@ int Engine::get_call_schedule(int32_t* lines, int32_t cap, int32_t* lofs, int32_
 
 int Engine::get_footprint_bins(int16_t* lo, uint16_t* mask, uint8_t* lineok) const {
   if (state_ < 2) return MBIR_ESTATE;
+  int rc = const_cast<Engine*>(this)->host_footprint_bins();
+  if (rc) return rc;
   if (acol_lo_.empty()) return MBIR_ENOTSUP;
   if (lo) std::copy(acol_lo_.begin(), acol_lo_.end(), lo);
   if (mask) std::copy(acol_mask_.begin(), acol_mask_.end(), mask);

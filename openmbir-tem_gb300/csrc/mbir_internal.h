@@ -169,6 +169,9 @@ struct ColourArgs {
 int launch_colour_schedule(const ColourArgs& a, void* stream);
 size_t colour_smem_bytes(int n_theta, int words);
 bool colour_schedule_fits(int n_theta, int words);  // shared memory of both kernels
+// packed[i] = (first bin << 16) | nonzero mask of A-column table entry i (packed_footprint), for
+// the n = lines x views entries of the table
+int launch_pack_footprints(const float4* table, size_t n, int nb, int32_t* packed, void* stream);
 
 // Batched sweep: per-series sweep arguments and a queue of (series, slice y) items.
 struct BatchArgs {

@@ -215,15 +215,11 @@ int colour_schedule(const LevelScheduleIn& in, int max_colours, int class_cap,
 void acol_bins(const float* table, int n_lines, int n_theta, int nb, int16_t* lo,
                uint16_t* mask) {
   const int wf = ((nb + 1 + 3) / 4) * 4;
+  static_assert(sizeof(int32_t) == sizeof(float), "int32 and float differ in size");
   for (size_t i = 0; i < static_cast<size_t>(n_lines) * n_theta; ++i) {
     const float* e = table + i * wf;
-    int32_t j;
-    static_assert(sizeof(j) == sizeof(float), "int32 and float differ in size");
-    std::memcpy(&j, e, sizeof(j));
-    unsigned bits = 0;
-    for (int b = 0; b < nb; ++b)
-      if (e[1 + b] > 0.f) bits |= 1u << b;
-    lo[i] = static_cast<int16_t>(bits ? j : 0);
+    const unsigned bits = footprint_mask(e, nb);
+    lo[i] = footprint_lo(e, bits);
     mask[i] = static_cast<uint16_t>(bits);
   }
 }

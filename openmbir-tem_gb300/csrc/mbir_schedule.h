@@ -1,7 +1,14 @@
 // mbir_schedule.h -- level schedule of a sparse ICD call (see mbir_schedule.cpp).
 #pragma once
 #include <cstdint>
+#include <cstring>
 #include <vector>
+
+#if defined(__CUDACC__)
+#define MBIR_HD __host__ __device__
+#else
+#define MBIR_HD
+#endif
 
 namespace mbir {
 
@@ -39,5 +46,26 @@ int colour_schedule(const LevelScheduleIn& in, int max_colours, int class_cap,
 
 // First bin and nonzero mask per (line, view) from the FP32 A-column table.
 void acol_bins(const float* table, int n_lines, int n_theta, int nb, int16_t* lo, uint16_t* mask);
+
+// One A-column table entry (e[0]: the first bin's int32 bits, e[1..nb]: the values): bit b of
+// the mask when value b is positive, and the first bin (0 when no value is).  The host bins
+// above and the device colouring's packed bins (packed_footprint) both come from these.
+inline MBIR_HD unsigned footprint_mask(const float* e, int nb) {
+  unsigned bits = 0;
+  for (int b = 0; b < nb; ++b)
+    if (e[1 + b] > 0.f) bits |= 1u << b;
+  return bits;
+}
+inline MBIR_HD int16_t footprint_lo(const float* e, unsigned bits) {
+  int32_t j;
+  memcpy(&j, e, sizeof(j));
+  return static_cast<int16_t>(bits ? j : 0);
+}
+// (first bin << 16) | mask, the first bin as its 16-bit pattern
+inline MBIR_HD int32_t packed_footprint(const float* e, int nb) {
+  const unsigned bits = footprint_mask(e, nb);
+  return static_cast<int32_t>(
+      (static_cast<uint32_t>(static_cast<uint16_t>(footprint_lo(e, bits))) << 16) | bits);
+}
 
 }  // namespace mbir
