@@ -387,35 +387,39 @@ int Engine::build_tables() {
       return fail(MBIR_ENOTSUP, "voxel slices y and y+2 share detector rows");
   // empty A-columns (the reference zeroes those lines, HAADF_ReconstructionEngine.cpp:614-625)
   tab_.line_nonempty.assign(static_cast<size_t>(g.n_z) * g.n_x, 0);
-  footprint_entries_ = 0;
-  for (int z = 0; z < g.n_z; z++)
-    for (int x = 0; x < g.n_x; x++) {
-      const double xc = g.x0 + ((double)x + 0.5) * g.delta_xz;
-      const double zc = g.z0 + ((double)z + 0.5) * g.delta_xz;
-      int64_t nnz = 0;
-      for (int i = 0; i < nt; i++) {
-        const double r = xc * tab_.cosv[i] - zc * tab_.sinv[i];
-        const double rmin = r - g.delta_xz, rmax = r + g.delta_xz;
-        if (rmax < g.R0 || rmin > g.RMax) continue;
-        int imin = static_cast<int>(std::floor((rmin - g.R0) / g.delta_r));
-        int imax = static_cast<int>(std::floor((rmax - g.R0) / g.delta_r));
-        if (imax >= g.n_r) imax = g.n_r - 1;
-        if (imin < 0) imin = 0;
-        for (int j = imin; j <= imax; j++) {
-          const double dr = std::fabs(r - (g.R0 + ((double)j + 0.5) * g.delta_r));
-          const int idr = static_cast<int>(std::floor(dr / g.offset_r));
-          if (idr < bins_) {
-            const double w1 = dr - idr * g.offset_r, w2 = (idr + 1) * g.offset_r - dr;
-            const int ii = idr + 1 < bins_ ? idr + 1 : bins_ - 1;
-            const double f1 = (w2 / g.offset_r) * tab_.H[static_cast<size_t>(i) * bins_ + idr] +
-                              (w1 / g.offset_r) * tab_.H[static_cast<size_t>(i) * bins_ + ii];
-            if (f1 > 0) nnz++;
+  std::vector<int64_t> row_entries(g.n_z, 0);  // summed in row order below
+  host_parallel(g.n_z, [&](int z_begin, int z_end) {
+    for (int z = z_begin; z < z_end; z++)
+      for (int x = 0; x < g.n_x; x++) {
+        const double xc = g.x0 + ((double)x + 0.5) * g.delta_xz;
+        const double zc = g.z0 + ((double)z + 0.5) * g.delta_xz;
+        int64_t nnz = 0;
+        for (int i = 0; i < nt; i++) {
+          const double r = xc * tab_.cosv[i] - zc * tab_.sinv[i];
+          const double rmin = r - g.delta_xz, rmax = r + g.delta_xz;
+          if (rmax < g.R0 || rmin > g.RMax) continue;
+          int imin = static_cast<int>(std::floor((rmin - g.R0) / g.delta_r));
+          int imax = static_cast<int>(std::floor((rmax - g.R0) / g.delta_r));
+          if (imax >= g.n_r) imax = g.n_r - 1;
+          if (imin < 0) imin = 0;
+          for (int j = imin; j <= imax; j++) {
+            const double dr = std::fabs(r - (g.R0 + ((double)j + 0.5) * g.delta_r));
+            const int idr = static_cast<int>(std::floor(dr / g.offset_r));
+            if (idr < bins_) {
+              const double w1 = dr - idr * g.offset_r, w2 = (idr + 1) * g.offset_r - dr;
+              const int ii = idr + 1 < bins_ ? idr + 1 : bins_ - 1;
+              const double f1 = (w2 / g.offset_r) * tab_.H[static_cast<size_t>(i) * bins_ + idr] +
+                                (w1 / g.offset_r) * tab_.H[static_cast<size_t>(i) * bins_ + ii];
+              if (f1 > 0) nnz++;
+            }
           }
         }
+        tab_.line_nonempty[static_cast<size_t>(z) * g.n_x + x] = nnz > 0 ? 1 : 0;
+        row_entries[z] += nnz;
       }
-      tab_.line_nonempty[static_cast<size_t>(z) * g.n_x + x] = nnz > 0 ? 1 : 0;
-      footprint_entries_ += nnz;
-    }
+  });
+  footprint_entries_ = 0;
+  for (int z = 0; z < g.n_z; z++) footprint_entries_ += row_entries[z];
   return MBIR_OK;
 }
 
@@ -427,31 +431,37 @@ int Engine::compute_stride() {
   const double d = g.delta_xz / g.delta_r, eps = 1e-4;
   int S = 2;
   for (; S < g.n_x; ++S) {
-    bool conflict = false;
-    for (int v = 0; v < g.n_theta && !conflict; ++v) {
-      const double bxv = g.delta_xz * tab_.cosv[v] / g.delta_r;
-      const double bzv = g.delta_xz * tab_.sinv[v] / g.delta_r;
-      const double u0 = ((g.x0 + 0.5 * g.delta_xz) * tab_.cosv[v] -
-                         (g.z0 + 0.5 * g.delta_xz) * tab_.sinv[v] - g.R0) /
-                        g.delta_r;
-      for (int z = 0; z < g.n_z && !conflict; ++z) {
-        for (int x = 0; x + S < g.n_x; ++x) {
-          const double ua = u0 + x * bxv - z * bzv, ub = ua + S * bxv;
-          double alo = std::floor(ua - d - eps), ahi = std::floor(ua + d + eps);
-          double blo = std::floor(ub - d - eps), bhi = std::floor(ub + d + eps);
-          alo = std::max(alo, 0.0);
-          blo = std::max(blo, 0.0);
-          ahi = std::min(ahi, (double)g.n_r - 1);
-          bhi = std::min(bhi, (double)g.n_r - 1);
-          if (alo > ahi || blo > bhi) continue;
-          if (!(ahi < blo || bhi < alo)) {
-            conflict = true;
-            break;
+    // any conflict at this stride, searched over rows in parallel (a yes/no answer)
+    std::atomic<bool> found{false};
+    host_parallel(g.n_z, [&](int z_begin, int z_end) {
+      bool conflict = false;
+      for (int v = 0; v < g.n_theta && !conflict; ++v) {
+        const double bxv = g.delta_xz * tab_.cosv[v] / g.delta_r;
+        const double bzv = g.delta_xz * tab_.sinv[v] / g.delta_r;
+        const double u0 = ((g.x0 + 0.5 * g.delta_xz) * tab_.cosv[v] -
+                           (g.z0 + 0.5 * g.delta_xz) * tab_.sinv[v] - g.R0) /
+                          g.delta_r;
+        if (found.load(std::memory_order_relaxed)) break;
+        for (int z = z_begin; z < z_end && !conflict; ++z) {
+          for (int x = 0; x + S < g.n_x; ++x) {
+            const double ua = u0 + x * bxv - z * bzv, ub = ua + S * bxv;
+            double alo = std::floor(ua - d - eps), ahi = std::floor(ua + d + eps);
+            double blo = std::floor(ub - d - eps), bhi = std::floor(ub + d + eps);
+            alo = std::max(alo, 0.0);
+            blo = std::max(blo, 0.0);
+            ahi = std::min(ahi, (double)g.n_r - 1);
+            bhi = std::min(bhi, (double)g.n_r - 1);
+            if (alo > ahi || blo > bhi) continue;
+            if (!(ahi < blo || bhi < alo)) {
+              conflict = true;
+              break;
+            }
           }
         }
       }
-    }
-    if (!conflict) break;
+      if (conflict) found.store(true);
+    });
+    if (!found.load()) break;
   }
   stride_ = std::max(2, std::min(S, std::max(g.n_x, 2)));
   return MBIR_OK;

@@ -3,9 +3,11 @@
 // stay in HBM from prepare() to destruction.
 #pragma once
 
+#include <algorithm>
 #include <atomic>
 #include <cstdint>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/mbir_gb300.h"
@@ -305,6 +307,36 @@ class Engine {
 // GenRandList's permutation (Common/VoxelUpdateList.cpp:157-215) drawn from mt19937 through
 // boost's uniform_int(0, n-1): element i of a list goes to position out[i].
 void rand_list_perm(uint32_t seed, int n, std::vector<int32_t>& out);
+
+// Host set-up loops: fn(begin, end) over [0, n) in contiguous chunks on up to 16 host threads
+// (the caller's included).  One region runs threaded at a time per process; a region that starts
+// while another runs (engines prepared side by side) runs on its caller's thread.  fn must
+// write only its own range's outputs, so results do not depend on the split.
+inline std::atomic<int>& host_parallel_busy() {
+  static std::atomic<int> busy{0};
+  return busy;
+}
+template <typename F>
+void host_parallel(int n, F fn) {
+  if (n <= 0) return;
+  const int hw = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+  const int nt = std::min(n, std::min(hw, 16));
+  int idle = 0;
+  if (nt <= 1 || !host_parallel_busy().compare_exchange_strong(idle, 1)) {
+    fn(0, n);
+    return;
+  }
+  const int chunk = (n + nt - 1) / nt;
+  std::vector<std::thread> pool;
+  pool.reserve(nt - 1);
+  for (int t = 1; t < nt; ++t) {
+    const int b = t * chunk, e = std::min(n, b + chunk);
+    if (b < e) pool.emplace_back(fn, b, e);
+  }
+  fn(0, std::min(n, chunk));
+  for (auto& th : pool) th.join();
+  host_parallel_busy().store(0);
+}
 
 // MRC I/O (mrc_io.cpp)
 struct MrcVolume {

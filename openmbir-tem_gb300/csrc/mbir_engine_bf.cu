@@ -11,6 +11,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <memory>
 
 #include "mbir_engine.h"
 
@@ -67,23 +68,25 @@ int Engine::bf_prepare_host() {
   const Geometry& g = g_;
   const size_t nh = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;
   ylog_.resize(nh);
-  for (int th = 0; th < g.n_theta; th++)
-    for (int r = 0; r < g.n_r; r++) {
-      const size_t b = (static_cast<size_t>(th) * g.n_r + r) * g.n_t;
-      bool stopped = false;
-      for (int t = 0; t < g.n_t; t++) {
-        double v = static_cast<double>(counts_[b + t]);
-        if (!stopped) {
-          v += p_.bf_offset;
-          if (v < 0) {
-            stopped = true;
-          } else {
-            v = -std::log(v / 1.0);
+  host_parallel(g.n_theta, [&](int th_begin, int th_end) {
+    for (int th = th_begin; th < th_end; th++)
+      for (int r = 0; r < g.n_r; r++) {
+        const size_t b = (static_cast<size_t>(th) * g.n_r + r) * g.n_t;
+        bool stopped = false;
+        for (int t = 0; t < g.n_t; t++) {
+          double v = static_cast<double>(counts_[b + t]);
+          if (!stopped) {
+            v += p_.bf_offset;
+            if (v < 0) {
+              stopped = true;
+            } else {
+              v = -std::log(v / 1.0);
+            }
           }
+          ylog_[b + t] = v;
         }
-        ylog_[b + t] = v;
       }
-    }
+  });
   // GenRegularList + GenRandList (execute :555-559): position perm[i] holds line i
   const int nl = g.n_z * g.n_x;
   std::vector<int32_t> perm;
@@ -118,16 +121,19 @@ int Engine::bf_upload() {
   const Geometry& g = g_;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
   const size_t nh = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;
-  std::vector<double> w(nh);
-  for (int th = 0; th < g.n_theta; th++)
-    for (int r = 0; r < g.n_r; r++)
-      for (int t = 0; t < g.n_t; t++) {
-        const size_t i = (static_cast<size_t>(th) * g.n_r + r) * g.n_t + t;
-        double v = 1.0 / std::exp(ylog_[i]);
-        if (p_.noise_estimation) v /= alpha_[th];
-        w[i] = v;
-      }
-  cudaMemcpyAsync(d_stage64_, w.data(), sizeof(double) * nh, cudaMemcpyHostToDevice, s);
+  // every entry is written below, by the threads (so they also take the first-touch faults)
+  std::unique_ptr<double[]> w(new double[nh]);
+  host_parallel(g.n_theta, [&](int th_begin, int th_end) {
+    for (int th = th_begin; th < th_end; th++)
+      for (int r = 0; r < g.n_r; r++)
+        for (int t = 0; t < g.n_t; t++) {
+          const size_t i = (static_cast<size_t>(th) * g.n_r + r) * g.n_t + t;
+          double v = 1.0 / std::exp(ylog_[i]);
+          if (p_.noise_estimation) v /= alpha_[th];
+          w[i] = v;
+        }
+  });
+  cudaMemcpyAsync(d_stage64_, w.get(), sizeof(double) * nh, cudaMemcpyHostToDevice, s);
   int rc = launch_layout_from_double(d_stage64_, d_w_, g.n_theta, g.n_r, n_rp_, g.n_t, fp64_, s);
   if (rc) return cuda_check(rc, "weights upload");
   cudaMemsetAsync(d_sel_, 1, static_cast<size_t>(g.n_t) * g.n_theta * n_sp_, s);
