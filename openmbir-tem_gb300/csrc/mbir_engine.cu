@@ -316,20 +316,22 @@ int Engine::build_tables() {
   }
   tab_.H.assign(static_cast<size_t>(nt) * bins_, 0.0);
   const double bw = g.delta_r, r0 = -bw / 2, step = bw / BR, tc = PR / (2 * g.delta_xz);
-  for (int k = 0; k < nt; k++)
-    for (int i = 0; i < bins_; i++) {
-      const double rmin = i * g.offset_r - g.delta_xz;
-      double s = 0;
-      for (int pp = 0; pp < BR; pp++) {
-        const double r = r0 + pp * step;
-        if (r < rmin) continue;
-        int pi = static_cast<int>(std::floor((r - rmin) * tc));
-        if (pi < 0) pi = 0;
-        if (pi >= PR) pi = PR - 1;
-        s += profile[static_cast<size_t>(k) * PR + pi] * beam[pp];
+  host_parallel(nt, [&](int k_begin, int k_end) {
+    for (int k = k_begin; k < k_end; k++)
+      for (int i = 0; i < bins_; i++) {
+        const double rmin = i * g.offset_r - g.delta_xz;
+        double s = 0;
+        for (int pp = 0; pp < BR; pp++) {
+          const double r = r0 + pp * step;
+          if (r < rmin) continue;
+          int pi = static_cast<int>(std::floor((r - rmin) * tc));
+          if (pi < 0) pi = 0;
+          if (pi >= PR) pi = PR - 1;
+          s += profile[static_cast<size_t>(k) * PR + pi] * beam[pp];
+        }
+        tab_.H[static_cast<size_t>(k) * bins_ + i] = s;
       }
-      tab_.H[static_cast<size_t>(k) * bins_ + i] = s;
-    }
+  });
   // H_t (HAADF_ForwardModel.cpp:408-451)
   tab_.Ht.assign(bins_, 0.0);
   for (int i = 0; i < bins_; i++) {
