@@ -7,7 +7,9 @@
 #include <atomic>
 #include <cstdint>
 #include <string>
+#include <memory>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "../../include/mbir_gb300.h"
@@ -15,6 +17,28 @@
 #include "mbir_schedule.h"
 
 namespace mbir {
+
+// Allocator whose value-less construct leaves elements uninitialised: vector::resize without
+// zeroing, for host buffers whose every element is written before it is read (the writing
+// threads then take the first-touch page faults side by side).
+template <typename T>
+struct UninitAlloc : std::allocator<T> {
+  template <typename U>
+  struct rebind {
+    using other = UninitAlloc<U>;
+  };
+  UninitAlloc() = default;
+  template <typename U>
+  UninitAlloc(const UninitAlloc<U>&) noexcept {}
+  template <typename U>
+  void construct(U* p) noexcept {
+    ::new (static_cast<void*>(p)) U;
+  }
+  template <typename U, typename... A>
+  void construct(U* p, A&&... a) {
+    ::new (static_cast<void*>(p)) U(std::forward<A>(a)...);
+  }
+};
 
 // Geometry of one resolution level, FP64, as the reference derives it
 // (InitialReconstructionInitializer.cpp:98-167, MRCSinogramInitializer.cpp:302-305).
@@ -258,7 +282,7 @@ class Engine {
   double* d_bfout_ = nullptr;               // reduction results
   double* d_alpha_ = nullptr;               // [n_theta] variance per view
   double* d_stage64_ = nullptr;             // FP64 host-layout staging
-  std::vector<double> ylog_;                // -log(counts + bf_offset), [theta][r][t]
+  std::vector<double, UninitAlloc<double>> ylog_;  // -log(counts + bf_offset), [theta][r][t]
   std::vector<int32_t> bf_master_;          // random permutation of all lines
   std::vector<int32_t> call_lines_;         // lines of the last sweep/call
   std::vector<uint8_t> active_host_;
