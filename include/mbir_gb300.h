@@ -48,6 +48,10 @@ extern "C" {
 #define MBIR_ORDER_PARALLEL 0  /* red/black y-slices x conflict-free voxel sets (GPU order) */
 #define MBIR_ORDER_REFERENCE 1 /* the reference's single-task random line order, y sequential */
 
+#define MBIR_SEED_PER_CALL 0   /* reference order: each NHICD call's list drawn from seed + 1 + call */
+#define MBIR_SEED_FIXED 1      /* reference order: every list drawn from `seed`, as the reference
+                                  draws them when its millisecond clock seed does not change */
+
 #define MBIR_PRECISION_FP32 0  /* volume, error sinogram and footprints in FP32 (reductions FP64) */
 #define MBIR_PRECISION_FP64 1  /* everything in FP64, the reference's Real_t */
 
@@ -125,6 +129,13 @@ typedef struct mbir_params {
                                  bits).  mbir_get_call_lines returns the visit order of 0 and 2.
                                  The colouring runs on the device; the schedules of the 20
                                  homogeneous sub-lists are built once and reused. */
+  int32_t seed_mode;          /* MBIR_SEED_PER_CALL / MBIR_SEED_FIXED (reference order, BF) */
+  int32_t float_params;       /* 1: round the parameters the reference's pipeline keeps in float
+                                 members (thickness, target gain, stop threshold, sigma_x,
+                                 diffuseness with q = diffuseness + 1 in float, default offset,
+                                 variance and initial value, Bragg T / delta / offset, the BF
+                                 offset -log(dosage + bf_offset)), so results equal the
+                                 reference's command-line runs; 0: use the values as given */
 } mbir_params;
 
 typedef struct mbir_status {

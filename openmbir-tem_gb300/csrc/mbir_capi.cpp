@@ -103,6 +103,35 @@ void mbir_params_default(mbir_params* p, int32_t modality) {
   }
 }
 
+namespace {
+// The reference's multi-resolution pipeline keeps these parameters in float members
+// (HAADF_MultiResolutionReconstruction.h:76-89, BFMultiResolutionReconstruction.h:76-107) and
+// evaluates p = diffuseness + 1 in float (HAADF_MultiResolutionReconstruction.cpp:333); the BF
+// command line stores -log(dosage + bf_offset) in such a member (BFReconstructionArgsParser.cpp:
+// 272-274).  float_params = 1 applies the same roundings, so that results equal the reference
+// run from its command line (the rounding is idempotent; the BF offset is rounded where the
+// engine computes it, Engine::bf_default_offset).
+mbir_params with_float_params(const mbir_params& in) {
+  mbir_params p = in;
+  if (!p.float_params) return p;
+  auto f = [](double v) { return static_cast<double>(static_cast<float>(v)); };
+  if (p.qggmrf_q == 0.0)
+    p.qggmrf_q = static_cast<double>(static_cast<float>(p.diffuseness) + 1.0f);
+  p.diffuseness = f(p.diffuseness);
+  p.sample_thickness = f(p.sample_thickness);
+  p.target_gain = f(p.target_gain);
+  p.stop_threshold = f(p.stop_threshold);
+  p.sigma_x = f(p.sigma_x);
+  p.default_offset = f(p.default_offset);
+  p.default_variance = f(p.default_variance);
+  p.default_recon_value = f(p.default_recon_value);
+  p.bragg_threshold = f(p.bragg_threshold);
+  p.bragg_delta = f(p.bragg_delta);
+  p.bf_offset = f(p.bf_offset);
+  return p;
+}
+}  // namespace
+
 mbir_engine* mbir_create(const mbir_params* p) {
   if (!p || p->struct_size != static_cast<int32_t>(sizeof(mbir_params))) {
     g_create_error = "mbir_create: params missing or struct_size mismatch";
@@ -119,13 +148,14 @@ mbir_engine* mbir_create(const mbir_params* p) {
     return nullptr;
   }
   if (!(p->sigma_x > 0) || p->num_resolutions < 1 || p->final_resolution < 1 ||
-      !(p->qggmrf_c > 0) || !(p->qggmrf_p > 0)) {
+      !(p->qggmrf_c > 0) || !(p->qggmrf_p > 0) ||
+      (p->seed_mode != MBIR_SEED_PER_CALL && p->seed_mode != MBIR_SEED_FIXED)) {
     g_create_error = "mbir_create: invalid parameter value";
     return nullptr;
   }
   try {
     auto* e = new mbir_engine;
-    e->impl = new mbir::Engine(*p);
+    e->impl = new mbir::Engine(with_float_params(*p));
     return e;
   } catch (...) {
     g_create_error = "mbir_create: allocation failed";
@@ -263,6 +293,8 @@ int32_t mbir_run_multires(const mbir_params* p, const float* counts, const float
                           int32_t n_theta, int32_t n_r, int32_t n_t, double delta_r,
                           double delta_t, float* out, int64_t n, int32_t* dims_out) {
   if (!p || !counts || !tilts_deg) return MBIR_EINVAL;
+  const mbir_params top = with_float_params(*p);
+  p = &top;
   const int levels = p->num_resolutions > 0 ? p->num_resolutions : 1;
   std::vector<float> prev;
   int pdims[3] = {0, 0, 0};

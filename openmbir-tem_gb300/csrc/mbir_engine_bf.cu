@@ -58,7 +58,9 @@ void rand_list_perm(uint32_t seed, int n, std::vector<int32_t>& out) {
 // the BF command line passes the offset d = -log(default_dosage + bf_offset)
 // (BFReconstructionArgsParser.cpp:272-274)
 double Engine::bf_default_offset() const {
-  return -std::log(p_.default_dosage + p_.bf_offset);
+  const double d = -std::log(p_.default_dosage + p_.bf_offset);
+  // the reference's pipeline stores it in a float member (BFMultiResolutionReconstruction.h:83)
+  return p_.float_params ? static_cast<double>(static_cast<float>(d)) : d;
 }
 
 // processRawCounts (BFForwardModel.cpp:939-972): counts + bf_offset, then -log(c / BF_MAX) with
@@ -376,11 +378,19 @@ int Engine::bf_call_begin(int outer, int inner, DevBF* out) {
       if (filt[l] > thr) list.push_back(l);
   }
   if (p_.order_mode == MBIR_ORDER_REFERENCE) {
-    // the call's visit order: GenRandList of its list (one worker), seeded per call
+    // the call's visit order: the worker's GenRandList of its list (one worker,
+    // BFReconstructionEngine_Extra.cpp:691).  A non-homogeneous list was already shuffled once
+    // by GenNonHomList (:1044); the reference seeds both from its millisecond clock, which
+    // gives both the same seed, so the same permutation is applied twice.
+    const uint32_t call_seed =
+        p_.seed_mode == MBIR_SEED_FIXED ? p_.seed : p_.seed + 1u + static_cast<uint32_t>(bf_calls_);
     std::vector<int32_t> perm;
-    rand_list_perm(p_.seed + 1u + static_cast<uint32_t>(bf_calls_), static_cast<int>(list.size()),
-                   perm);
+    rand_list_perm(call_seed, static_cast<int>(list.size()), perm);
     call_lines_.assign(list.size(), 0);
+    if (p_.nhicd && bf_eff_ % 2 == 1) {
+      for (size_t i = 0; i < list.size(); i++) call_lines_[perm[i]] = list[i];
+      list = call_lines_;
+    }
     for (size_t i = 0; i < list.size(); i++) call_lines_[perm[i]] = list[i];
   } else {
     call_lines_ = list;

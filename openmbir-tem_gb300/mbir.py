@@ -25,6 +25,7 @@ ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "EDEVICE", -4: "EIO", -5: "ESTATE", -6
 HAADF, BF = 0, 1
 ORDER_PARALLEL, ORDER_REFERENCE = 0, 1
 FP32, FP64 = 0, 1
+SEED_PER_CALL, SEED_FIXED = 0, 1
 
 
 class MbirParams(C.Structure):
@@ -84,6 +85,8 @@ class MbirParams(C.Structure):
         ("nhicd", C.c_int32),
         ("lane_shape", C.c_int32),
         ("call_schedule", C.c_int32),
+        ("seed_mode", C.c_int32),
+        ("float_params", C.c_int32),
     ]
 
 

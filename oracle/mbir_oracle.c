@@ -6,8 +6,8 @@
  *
  * All paths below are relative to the reference project root (Code/MBIRLib/...).
  * Arithmetic is FP64 throughout, in the reference's loop order, so that the restatement
- * reproduces the reference to rounding.  Parity unpinned: the reference has no golden vectors
- * for this path and cannot be built from its own sources alone (mbir_oracle.h says why).
+ * reproduces the reference bit for bit: it is pinned to the reference's own programs built from
+ * their sources (mbir_oracle.h says how).
  */
 #include "mbir_oracle.h"
 
@@ -576,6 +576,7 @@ double* orc_yest(orc_ctx* c) { return c->yest; }
 double* orc_gain(orc_ctx* c) { return c->I; }
 double* orc_offset(orc_ctx* c) { return c->mu; }
 double* orc_variance(orc_ctx* c) { return c->alpha; }
+double* orc_counts(orc_ctx* c) { return c->counts; }
 const double* orc_detector_response(const orc_ctx* c) { return c->H; }
 const double* orc_ht(const orc_ctx* c) { return c->Ht; }
 const double* orc_voxel_profile(const orc_ctx* c) { return c->profile; }
@@ -1484,7 +1485,18 @@ double orc_bf_cost(const orc_ctx* c, double* parts) {
  * whose filtered update magnitude is in the top 1/20), the Bragg threshold schedule, the
  * stop rule of stopCriteria and the nuisance updates.  Each call visits its list in the order
  * of orc_rand_list_perm(seed + 1 + call) (the reference: GenRandList per worker, clock seed). */
-int orc_bf_run(orc_ctx* c, uint32_t seed, int max_calls) {
+static int bf_run_impl(orc_ctx* c, uint32_t seed, uint32_t list_seed_step, int max_calls);
+
+int orc_bf_run(orc_ctx* c, uint32_t seed, int max_calls) { return bf_run_impl(c, seed, 1u, max_calls); }
+
+/* The reference seeds every list generator from the millisecond clock
+ * (VoxelUpdateList.cpp:171-172); with the clock frozen at one value every list draw starts from
+ * the same seed, which this entry point reproduces. */
+int orc_bf_run_fixed_seed(orc_ctx* c, uint32_t seed, int max_calls) {
+  return bf_run_impl(c, seed, 0u, max_calls);
+}
+
+static int bf_run_impl(orc_ctx* c, uint32_t seed, uint32_t list_seed_step, int max_calls) {
   const int nl = c->n_z * c->n_x;
   int32_t* perm = (int32_t*)malloc(sizeof(int32_t) * (nl > 0 ? nl : 1));
   int32_t* master = (int32_t*)malloc(sizeof(int32_t) * (nl > 0 ? nl : 1));
@@ -1529,7 +1541,16 @@ int orc_bf_run(orc_ctx* c, uint32_t seed, int max_calls) {
         orc_bf_vsc(c);
         n = orc_bf_nh_lines(c, orc_bf_nh_threshold(c), list);
       }
-      orc_rand_list_perm(seed + 1u + (uint32_t)calls, n, perm);
+      /* The worker's GenRandList of the call's list (BFReconstructionEngine_Extra.cpp:691).  A
+       * non-homogeneous list was already randomised once by GenNonHomList (:1044); both draws
+       * happen within the same millisecond of the reference's clock and so use one seed. */
+      const uint32_t call_seed = list_seed_step ? seed + 1u + (uint32_t)calls : seed;
+      orc_rand_list_perm(call_seed, n, perm);
+      const int nh_call = c->p.nhicd && (eff % 2 == 1);
+      if (nh_call) {
+        for (int i = 0; i < n; i++) order[perm[i]] = list[i];
+        memcpy(list, order, sizeof(int32_t) * n);
+      }
       for (int i = 0; i < n; i++) order[perm[i]] = list[i];
       double st[4];
       orc_bf_sweep_lines(c, order, n, outer, inner, st);

@@ -8,13 +8,13 @@
  * Every function restates one piece of the reference (Code/MBIRLib/...) in plain C with
  * the reference's own FP64 arithmetic and loop order; each cites the file:line it follows.
  *
- * PARITY UNPINNED: the reference ships no golden vectors, known-answer tests or expected
- * outputs for this path (its Code/Test programs print values without assertions), and its
- * engine cannot be compiled from its own sources alone (it needs cmake-generated
- * configuration headers, Boost and TBB), so this restatement is not checked against outputs of
- * the reference itself.  It is checked against published known answers (MT19937), algebraic
- * properties of the reference algorithm (tests/test_oracle.py) and two independent FP64
- * implementations of the setup tables (this file and the engine's host code).
+ * PINNED TO THE REFERENCE: the reference's own HAADFReconstruction and BFReconstruction programs,
+ * compiled from their sources by oracle/build_ref.py (stand-in Boost/TBB headers, a frozen clock
+ * seed), produce outputs that this restatement reproduces bit for bit when it is given the
+ * parameters the reference's pipeline hands its engine (oracle/refrun.py) and the C library's
+ * pow (pinned_pow = 0): the forward projection, 20 HAADF outer iterations with gain/offset and
+ * variance estimation, and 42 bright-field NHICD calls with the Bragg schedule
+ * (tests/test_oracle_vs_ref.py against the fixtures of tests/golden/, and live runs).
  */
 #ifndef MBIR_ORACLE_H_
 #define MBIR_ORACLE_H_
@@ -76,6 +76,9 @@ double* orc_volume(orc_ctx* c);
 double* orc_error(orc_ctx* c);
 double* orc_weight(orc_ctx* c);
 double* orc_yest(orc_ctx* c);
+/* the measurements the engine works on: the input counts (BF: -log(counts + bf_offset) once
+ * prepared) */
+double* orc_counts(orc_ctx* c);
 double* orc_gain(orc_ctx* c);
 double* orc_offset(orc_ctx* c);
 double* orc_variance(orc_ctx* c);
@@ -151,6 +154,8 @@ double orc_bf_cost(const orc_ctx* c, double* parts);
 /* BFReconstructionEngine::execute loops in reference (list) order with lists drawn from
  * `seed`; runs at most max_calls updateVoxels calls (<= 0: no limit); returns the calls run */
 int orc_bf_run(orc_ctx* c, uint32_t seed, int max_calls);
+/* the same with every list drawn from `seed` (the reference with its clock seed frozen) */
+int orc_bf_run_fixed_seed(orc_ctx* c, uint32_t seed, int max_calls);
 /* y-slab sharding: one colour of the slice-order sweep over slices [y0, y1); per-view sums over
  * detector rows [t0, t1) (kind 0: [theta][6] jointEstimation sums, kind 1: [theta] sum e^2);
  * nuisance update with the jointEstimation error rebuild (variance may be null) */

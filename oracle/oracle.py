@@ -62,7 +62,7 @@ def lib():
             "orc_dims": (None, [C.c_void_p, _I, _D]),
             "orc_offsets": (None, [C.c_void_p, _D]),
             "orc_volume": (_D, [C.c_void_p]), "orc_error": (_D, [C.c_void_p]),
-            "orc_weight": (_D, [C.c_void_p]), "orc_yest": (_D, [C.c_void_p]),
+            "orc_weight": (_D, [C.c_void_p]), "orc_yest": (_D, [C.c_void_p]), "orc_counts": (_D, [C.c_void_p]),
             "orc_gain": (_D, [C.c_void_p]), "orc_offset": (_D, [C.c_void_p]),
             "orc_variance": (_D, [C.c_void_p]),
             "orc_detector_response": (_D, [C.c_void_p]), "orc_ht": (_D, [C.c_void_p]),
@@ -100,6 +100,7 @@ def lib():
             "orc_bf_update_selector": (None, [C.c_void_p]),
             "orc_bf_cost": (C.c_double, [C.c_void_p, _D]),
             "orc_bf_run": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int]),
+            "orc_bf_run_fixed_seed": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int]),
             "orc_icd_sweep_colour": (None, [C.c_void_p, _I, C.c_int, C.c_int, C.c_int, C.c_int,
                                             C.c_int, C.c_int, _D]),
             "orc_view_sums": (None, [C.c_void_p, C.c_int, C.c_int, C.c_int, _D]),
@@ -161,6 +162,16 @@ def params_from_mbir(p):
         # the BF command line turns the void dosage into the offset d = -log(dosage + bf_offset)
         # (BFReconstructionArgsParser.cpp:272-274)
         o.default_offset = -np.log(p.default_dosage + p.bf_offset) if p.use_default_offset else 0.0
+    if getattr(p, "float_params", 0):
+        # the pipeline's float members (HAADF_MultiResolutionReconstruction.h:76-89,
+        # BFMultiResolutionReconstruction.h:76-107); p = diffuseness + 1 in float (:333)
+        f32 = lambda v: float(np.float32(v))  # noqa: E731
+        if p.qggmrf_q == 0:
+            o.mrf_q = float(np.float32(np.float32(p.diffuseness) + np.float32(1.0)))
+        for k in ("length_z", "sigma_x", "target_gain", "default_offset", "default_variance",
+                  "default_recon_value", "stop_threshold", "bragg_threshold", "bragg_delta",
+                  "bf_offset"):
+            setattr(o, k, f32(getattr(o, k)))
     return o
 
 
@@ -391,6 +402,14 @@ class Oracle:
 
     def bf_run(self, seed, max_calls=0):
         return lib().orc_bf_run(self._h, seed, max_calls)
+
+    def bf_run_fixed_seed(self, seed, max_calls=0):
+        """bf_run with every list drawn from `seed` (the reference with its clock seed frozen)."""
+        return lib().orc_bf_run_fixed_seed(self._h, seed, max_calls)
+
+    def measured(self):
+        """The measurements the engine works on (BF: -log(counts + bf_offset) once prepared)."""
+        return self._view(lib().orc_counts, self.shape)
 
     def run(self, seed, n_cost=0):
         log = np.zeros(max(n_cost, 1))

@@ -1,0 +1,116 @@
+#!/usr/bin/env python3
+"""Generate the reference-output fixtures in this directory from OpenMBIR-TEM itself.
+
+Needs the reference tree (its programs are built from source by oracle/build_ref.py into
+oracle/_ref) and runs them through oracle/refrun.py on seeded synthetic inputs:
+
+* haadf_small.npz -- a reduced HAADF case (64 x 8 detector, 36 views over +-70 deg, thickness
+  16): the forward projection of a random volume (0 outer iterations from
+  --initial_recon_file; the volume's values are float32 numbers) and 5 outer iterations with
+  gain/offset and variance estimation;
+* bf_small.npz -- a reduced bright-field case (64 x 8 detector, 31 views over +-60 deg): 40
+  outer iterations with 3 inner calls (the Bragg schedule: T = 5e10 for the first calls, then
+  T = 3), NHICD lists, offset and variance estimation; and the first 6 calls of the same
+  schedule (4 outer iterations);
+* haadf_cfg0.json -- the benchmark's small HAADF configuration (128 x 32 detector, 71 views over
+  +-70 deg at 2 deg, thickness 32, volume 128 x 32 x 64): SHA-256 digests and sums of the
+  inputs and of the reference's float64 outputs after 1, 5 and 20 outer iterations.
+
+Every run uses one worker and a frozen clock seed (refrun.py explains both).  The inputs of the
+small cases are stored with their outputs; the cfg0 input is regenerated from its seed and
+checked against its stored digest.
+
+Usage: python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+for p in (os.path.join(ROOT, "oracle"), os.path.join(ROOT, "openmbir-tem_gb300"),
+          os.path.join(ROOT, "tests")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import refrun  # noqa: E402
+import synthetic  # noqa: E402
+from conftest import bf_case, small_case  # noqa: E402
+
+HAADF_SEED = 12345
+BF_SEED = 777
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a, "<f8").tobytes()).hexdigest()
+
+
+def cfg0_input():
+    y, ang, _ = synthetic.haadf_two_spheres()
+    return y, ang
+
+
+def haadf_small(tmp):
+    y, ang, th = small_case()
+    n_theta, n_r, n_t = y.shape
+    kw = dict(thickness=th, diffuseness=0.1, sigma_x=0.2, seed=HAADF_SEED)
+    rng = np.random.default_rng(11)
+    n_z = int(round(2 * th))
+    init_yxz = np.maximum(rng.normal(0.3, 0.3, (n_t, n_r, n_z)), 0.0).astype(np.float32)
+    fp = refrun.run_haadf(os.path.join(tmp, "hs_fp"), y, ang, outer=0,
+                          initial=init_yxz.astype(np.float64), **kw)
+    it5 = refrun.run_haadf(os.path.join(tmp, "hs_it5"), y, ang, outer=5, **kw)
+    np.savez_compressed(os.path.join(HERE, "haadf_small.npz"), counts=y, tilts=ang,
+                        thickness=th, init_yxz=init_yxz, fp_sinogram=fp["sinogram"],
+                        it5_object_yxz=it5["object_yxz"], it5_gain=it5["gain"],
+                        it5_offset=it5["offset"])
+
+
+def bf_small(tmp):
+    c, ang, th = bf_case()
+    out = refrun.run_bf(os.path.join(tmp, "bf40"), c, ang, th, 0.1, 0.02, outer=40, inner=3,
+                        seed=BF_SEED)
+    six = refrun.run_bf(os.path.join(tmp, "bf6"), c, ang, th, 0.1, 0.02, outer=4, inner=3,
+                        seed=BF_SEED)
+    np.savez_compressed(os.path.join(HERE, "bf_small.npz"), counts=c, tilts=ang, thickness=th,
+                        object_yxz=out["object_yxz"], gain=out["gain"], offset=out["offset"],
+                        variance=out["variance"], sinogram=out["sinogram"],
+                        c6_object_yxz=six["object_yxz"], c6_offset=six["offset"],
+                        c6_variance=six["variance"])
+
+
+def haadf_cfg0(tmp):
+    y, ang = cfg0_input()
+    rec = {"input_counts_sha256": digest(y), "input_tilts_sha256": digest(ang),
+           "shape": list(y.shape), "thickness": 32.0, "diffuseness": 0.1, "sigma_x": 0.2,
+           "seed": HAADF_SEED, "runs": {}}
+    for outer in (1, 5, 20):
+        o = refrun.run_haadf(os.path.join(tmp, f"c0_{outer}"), y, ang, 32.0, 0.1, 0.2, outer,
+                             seed=HAADF_SEED)
+        rec["runs"][str(outer)] = {
+            k: {"sha256": digest(o[k]), "sum": float(np.sum(o[k])),
+                "norm": float(np.linalg.norm(o[k]))}
+            for k in ("object_yxz", "gain", "offset", "sinogram")}
+    with open(os.path.join(HERE, "haadf_cfg0.json"), "w") as f:
+        json.dump(rec, f, indent=1, sort_keys=True)
+
+
+def main():
+    if not refrun.ensure_built():
+        print("make_golden: the reference programs are not available", file=sys.stderr)
+        return 1
+    with tempfile.TemporaryDirectory() as tmp:
+        haadf_small(tmp)
+        bf_small(tmp)
+        haadf_cfg0(tmp)
+    for f in sorted(os.listdir(HERE)):
+        print(f, os.path.getsize(os.path.join(HERE, f)))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
