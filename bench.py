@@ -91,6 +91,59 @@ def params_for(mbir, th, mod, outer=20, inner=1):
     return p
 
 
+def oracle_params_for(th, mod):
+    """The same workload parameters as params_for, for the CPU restatement alone: the reference
+    arm and the CPU baseline never load the product library."""
+    sys.path.insert(0, ORACLE)
+    import oracle
+    o = oracle.OrcParams()
+    o.delta_xz_factor = 1.0
+    o.interpolate_factor = 1.0
+    o.length_z = th
+    o.extend_object = 0
+    o.x_shrink_factor = 0.6
+    o.z_stretch = 2
+    o.response_bins = 64
+    o.profile_resolution = 1536
+    o.beam_resolution = 512
+    o.compat_double_angle = 0 if mod == "BF" else 1
+    o.sigma_x = 0.02 if mod == "BF" else 0.2
+    o.mrf_p = 2.0
+    o.mrf_q = 1.1
+    o.mrf_c = 0.01 if mod == "BF" else 0.001
+    o.mrf_alpha = 1.5
+    o.target_gain = 1.0
+    o.default_variance = 1.0
+    o.use_default_offset = 1 if mod == "BF" else 0
+    o.default_offset = -np.log(1.0e4) if mod == "BF" else 0.0
+    o.joint_estimation = 1
+    o.noise_model = 0 if mod == "BF" else 1
+    o.zero_skipping = 1
+    o.stop_threshold = 0.0
+    o.outer_iterations = 20
+    o.inner_iterations = 1
+    o.threshold_reduction_factor = 1.0
+    o.modality = 1 if mod == "BF" else 0
+    o.noise_estimation = 1 if mod == "BF" else 0
+    o.bragg_threshold = 5.0e10 if mod == "BF" else 0.0
+    o.bragg_delta = 0.5
+    o.nhicd = 1 if mod == "BF" else 0
+    return o
+
+
+def workload_config(name):
+    """The workload as both arms report it (config is the same dict on the GPU line and on the
+    reference line; measured details go elsewhere)."""
+    mod, n_r, n_t, th, mx, st, npart = WORKLOADS[name]
+    views = int(round(2 * mx / st)) + 1
+    return {"workload": name, "modality": mod, "volume_zxy": [int(round(2 * th)), n_r, n_t],
+            "views": views, "detector": [n_r, n_t],
+            "step": ("one NHICD equivalent iteration (20 updateVoxels calls)" if mod == "BF"
+                     else "one full ICD sweep"),
+            "l2": "flushed before every timed step (512 MiB write)",
+            "parallelism": "replicas"}
+
+
 class ClockSampler:
     """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -147,19 +200,17 @@ def cpu_reference_sample(name, budget_s=12.0, n_t=32, threads=None, max_calls=No
     about `budget_s` seconds of calls.  BF: NHICD calls (homogeneous and non-homogeneous lists
     alternating); HAADF: full sweeps.  Returns the cpu_baseline dict (voxel updates/s)."""
     sys.path.insert(0, ORACLE)
-    import mbir
     import oracle
     threads = threads or os.cpu_count() or 1
     y, ang, th, mod = make_data(name, n_t_override=n_t)
-    p = params_for(mbir, th, mod)
-    o = oracle.Oracle(oracle.params_from_mbir(p), y, ang)
+    o = oracle.Oracle(oracle_params_for(th, mod), y, ang)
     o.prepare()
     upd = 0.0
     calls = 0
     t0 = time.perf_counter()
     if mod == "BF":
         nl = o.nz * o.nx
-        perm = oracle.rand_list_perm(p.seed, nl)
+        perm = oracle.rand_list_perm(1, nl)
         master = np.empty(nl, np.int32)
         master[perm] = np.arange(nl, dtype=np.int32)
         n_el = nl // CALLS_PER_EQUIT
@@ -202,7 +253,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": args.workload, "note": "bounded CPU sample of the workload"},
+            "config": workload_config(args.workload),
             "cpu_baseline": res,
             "e2e": {"value": res["value"], "unit": res["unit"], "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
@@ -251,18 +302,12 @@ def uneven_series(n, seed=0, large_frac=0.0, bf_frac=0.0):
     return out
 
 
-def run_batch(args):
-    """Time to a 1e-4 relative cost tolerance for 64 uneven HAADF reconstructions: one at a time
+def batch_measure(mbir, n, seed=1, batch_threads=None, tol=1e-4, max_outer=60):
+    """Time to a relative cost tolerance for n uneven HAADF reconstructions: one at a time
     through the step-wise C ABI (sweep, gain/offset, variance, cost per outer iteration) against
     all of them advancing together in one persistent launch per sweep (mbir_batch_run)."""
     import torch
-    import build as pkg_build
-    pkg_build.build()
-    import mbir
-    torch.cuda.set_device(0)
-    n = args.series
-    data = uneven_series(n, seed=1)
-    tol, max_outer = 1e-4, 60
+    data = uneven_series(n, seed=seed)
 
     def engine(item):
         mod, y, ang, th = item
@@ -302,8 +347,8 @@ def run_batch(args):
     # all together
     engines = [engine(item) for item in data]
     with mbir.Batch(0) as b:
-        if args.batch_threads:
-            b.set_threads(args.batch_threads)
+        if batch_threads:
+            b.set_threads(batch_threads)
         for e in engines:
             b.add(e)
         torch.cuda.synchronize()
@@ -315,11 +360,8 @@ def run_batch(args):
     for e in engines:
         e.close()
     vox = sum(int(np.prod([d[1].shape[1], d[1].shape[2], 2 * d[3]])) for d in data)
-    line = {"metric": "batched time-to-tolerance speed-up vs one-at-a-time GPU path",
-            "value": seq_s / bat_s, "unit": "x", "higher_is_better": True, "n_gpus": 1,
-            "data": "synthetic",
-            "config": {"workload": "batch-64-uneven-haadf", "series": n, "voxels_total": vox,
-                       "tolerance": tol, "max_outer": max_outer},
+    return {"speedup": seq_s / bat_s, "series": n, "voxels_total": vox, "tolerance": tol,
+            "max_outer": max_outer,
             "sequential": {"wall_s": seq_s, "voxel_updates": seq_upd,
                            "voxel_updates_per_s": seq_upd / seq_s,
                            "outer_iterations": int(np.sum(seq_iters)), "phases": phase},
@@ -327,23 +369,33 @@ def run_batch(args):
                         "sweep_device_s": bat_sweep_s,
                         "voxel_updates_per_s": bat_upd / bat_s,
                         "outer_iterations": int(np.sum(iters))}}
-    print(json.dumps(line))
 
 
-def run_serve(args):
-    """Served stream: Poisson arrivals (mean 20 requests/s) of mixed HAADF/BF requests from the
-    uneven size distribution plus 5% of the 512x256x128 / 61-view shape, each to a 1e-4 relative
-    cost tolerance; p50/p99 latency and throughput, against the same requests served one at a
-    time."""
+def run_batch(args):
     import torch
     import build as pkg_build
     pkg_build.build()
     import mbir
     torch.cuda.set_device(0)
-    n = args.series
-    data = uneven_series(n, seed=2, large_frac=0.05, bf_frac=0.3)
-    rng = np.random.default_rng(3)
-    gaps = rng.exponential(1.0 / 20.0, n)
+    r = batch_measure(mbir, args.series, batch_threads=args.batch_threads)
+    line = {"metric": "batched time-to-tolerance speed-up vs one-at-a-time GPU path",
+            "value": r["speedup"], "unit": "x", "higher_is_better": True, "n_gpus": 1,
+            "data": "synthetic",
+            "config": {"workload": f"batch-{args.series}-uneven-haadf", "series": args.series,
+                       "voxels_total": r["voxels_total"], "tolerance": r["tolerance"],
+                       "max_outer": r["max_outer"]},
+            "sequential": r["sequential"], "batched": r["batched"]}
+    print(json.dumps(line))
+
+
+def serve_measure(mbir, n, rate, seed=2, one_at_a_time=True):
+    """Served stream: Poisson arrivals (mean `rate` requests/s) of mixed HAADF/BF requests from
+    the uneven size distribution plus 5% of the 512x256x128 / 61-view shape, each to a 1e-4
+    relative cost tolerance; p50/p99 latency and throughput with continuous batching, and
+    (optionally) with the same requests served one at a time."""
+    data = uneven_series(n, seed=seed, large_frac=0.05, bf_frac=0.3)
+    rng = np.random.default_rng(seed + 1)
+    gaps = rng.exponential(1.0 / rate, n)
 
     def submit_all(server):
         ids = []
@@ -364,18 +416,82 @@ def run_serve(args):
                   "mean_ms": st.mean_ms, "completed": st.completed, "failed": st.failed,
                   "peak_active": st.peak_active, "requests_per_s": st.completed / wall,
                   "voxel_updates_per_s": st.voxel_updates / wall}
-    with mbir.Server(0, 0, 1) as s:
-        wall1 = submit_all(s)
-        st = s.stats()
-        single = {"wall_s": wall1, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms,
-                  "requests_per_s": st.completed / wall1}
-    line = {"metric": "served p50/p99 request latency and throughput", "value": served["p99_ms"],
-            "unit": "ms (p99)", "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
-            "config": {"workload": "serve-poisson-20rps", "requests": n, "bf_fraction": 0.3,
-                       "large_fraction": 0.05, "tolerance": 1e-4},
-            "continuous_batching": served, "one_at_a_time": single,
-            "throughput_ratio": served["requests_per_s"] / max(single["requests_per_s"], 1e-12)}
+    out = {"requests": n, "arrival_rate_per_s": rate, "bf_fraction": 0.3,
+           "large_fraction": 0.05, "tolerance": 1e-4, "continuous_batching": served}
+    if one_at_a_time:
+        with mbir.Server(0, 0, 1) as s:
+            wall1 = submit_all(s)
+            st = s.stats()
+            out["one_at_a_time"] = {"wall_s": wall1, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms,
+                                    "requests_per_s": st.completed / wall1}
+        out["throughput_ratio"] = (served["requests_per_s"] /
+                                   max(out["one_at_a_time"]["requests_per_s"], 1e-12))
+    return out
+
+
+def run_serve(args):
+    import torch
+    import build as pkg_build
+    pkg_build.build()
+    import mbir
+    torch.cuda.set_device(0)
+    r = serve_measure(mbir, args.series, args.rate)
+    line = {"metric": "served p50/p99 request latency and throughput",
+            "value": r["continuous_batching"]["p99_ms"], "unit": "ms (p99)",
+            "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": f"serve-poisson-{args.rate:g}rps", "requests": args.series,
+                       "bf_fraction": 0.3, "large_fraction": 0.05, "tolerance": 1e-4},
+            "continuous_batching": r["continuous_batching"],
+            "one_at_a_time": r.get("one_at_a_time"), "throughput_ratio": r.get("throughput_ratio")}
     print(json.dumps(line))
+
+
+def e2e_run(mbir, args, y, ang, th, mod, device):
+    """One reconstruction through the C ABI from host buffers: create, upload, set-up and
+    projection, the calls with offset and variance updates, read-back of the volume."""
+    bf = mod == "BF"
+    n_outer = CALLS_PER_EQUIT if bf else 3
+    pe = params_for(mbir, th, mod, outer=n_outer, inner=1)
+    pe.device = device
+    if args.call_schedule is not None:
+        pe.call_schedule = args.call_schedule
+    if args.lane_shape is not None:
+        pe.lane_shape = args.lane_shape
+    t0 = time.perf_counter()
+    with mbir.Engine(pe) as e2:
+        e2.set_sinogram(y, ang)
+        e2.run()
+        host_vol = e2.volume()
+        s2 = e2.status()
+    dt = time.perf_counter() - t0
+    return {"value": s2.voxels_updated / dt, "unit": "voxel-updates/s",
+            "h2d_bytes_per_step": int(y.nbytes), "d2h_bytes_per_step": int(host_vol.nbytes),
+            "step": f"mbir_create + mbir_set_sinogram + mbir_run ({n_outer} outer iterations: "
+                    "call, offset and variance updates) + mbir_get_volume, host buffers",
+            "wall_s": dt}
+
+
+def e2e_cold(args, device):
+    """e2e_run in a fresh Python process (nothing of this process's CUDA state is reused)."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--e2e-child", "--workload", args.workload,
+           "--device", str(device)]
+    if args.call_schedule is not None:
+        cmd += ["--call-schedule", str(args.call_schedule)]
+    if args.lane_shape is not None:
+        cmd += ["--lane-shape", str(args.lane_shape)]
+    try:
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+        return json.loads(r.stdout.strip().splitlines()[-1])
+    except Exception:
+        return None
+
+
+def run_e2e_child(args):
+    import build as pkg_build
+    pkg_build.build()
+    y, ang, th, mod = make_data(args.workload, seed=0)
+    import mbir  # the library loads here, outside the timed region; the device context does not
+    print(json.dumps(e2e_run(mbir, args, y, ang, th, mod, args.device)))
 
 
 def main():
@@ -387,6 +503,11 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
                     choices=sorted(WORKLOADS) + ["batch-64", "serve-poisson"])
     ap.add_argument("--series", type=int, default=64, help="batch/serve: number of requests")
+    ap.add_argument("--rate", type=float, default=20.0, help="serve: mean arrivals per second")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="default line: skip the batched time-to-tolerance measurement")
+    ap.add_argument("--no-serve", action="store_true",
+                    help="default line: skip the served-stream measurement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--batch-threads", type=int, default=None,
@@ -395,7 +516,12 @@ def main():
                     help="voxel-group shape (1 16x4, 2 32x2, 3 32x3, 4 32x5; default autotuned)")
     ap.add_argument("--call-schedule", type=int, default=None,
                     help="BF NHICD call schedule (0 colour classes, 1 row walk, 2 levels)")
+    ap.add_argument("--e2e-child", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--device", type=int, default=0, help=argparse.SUPPRESS)
     args = ap.parse_args()
+    if args.e2e_child:
+        run_e2e_child(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return
@@ -500,18 +626,15 @@ def main():
         except Exception:
             traffic = None
 
+    cfg = workload_config(args.workload)
+    assert cfg["volume_zxy"] == [nz, nx, ny], (cfg, (nz, nx, ny))
     out = {"metric": METRIC, "value": value, "unit": "voxel-updates/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic",
-           "config": {"workload": args.workload, "modality": mod,
-                      "volume_zxy": [nz, nx, ny], "views": int(y.shape[0]),
-                      "detector": [int(y.shape[1]), int(y.shape[2])],
-                      "step": ("one NHICD equivalent iteration (20 updateVoxels calls)" if bf
-                               else "one full ICD sweep"),
-                      "order": "parallel (red/black y, conflict-free x)",
-                      "l2": "flushed before every timed step (512 MiB write)",
-                      "parallelism": f"replicas x{world}",
+           "config": cfg,
+           "details": {"order": "parallel (red/black y, conflict-free x)",
+                      "replicas": world,
                       "voxels_updated_per_step": upd / args.steps,
                       "voxels_visited_per_step": visited / args.steps,
                       "slices_in_smem": bool(st.staged), "x_stride": st.stride,
@@ -533,31 +656,28 @@ def main():
            "clocks": clk.summary()}
 
     if not args.no_e2e:
-        # end to end through the C ABI from host buffers
-        n_outer = CALLS_PER_EQUIT if bf else 3
-        pe = params_for(mbir, th, mod, outer=n_outer, inner=1)
-        pe.device = local
-        if args.call_schedule is not None:
-            pe.call_schedule = args.call_schedule
-        if args.lane_shape is not None:
-            pe.lane_shape = args.lane_shape
-        host_vol = np.empty((nz, nx, ny), np.float32)
+        # end to end through the C ABI from host buffers: cold, in a fresh process (CUDA context,
+        # module load, set-up, autotuning all inside the timed region), and warm, in this
+        # process after the timed engine (module loaded, shape tuning cached)
+        warm = e2e_run(mbir, args, y, ang, th, mod, local)
         barrier()
-        t0 = time.perf_counter()
-        with mbir.Engine(pe) as e2:
-            e2.set_sinogram(y, ang)
-            e2.run()
-            host_vol[...] = e2.volume()
-            s2 = e2.status()
-        dt = time.perf_counter() - t0
-        out["e2e"] = {"value": s2.voxels_updated / dt * world, "unit": "voxel-updates/s",
-                      "h2d_bytes_per_step": int(y.nbytes),
-                      "d2h_bytes_per_step": int(host_vol.nbytes),
-                      "step": f"mbir_set_sinogram + mbir_run ({n_outer} outer iterations: call, "
-                              "offset and variance updates) + mbir_get_volume, host buffers",
-                      "wall_s": dt}
+        cold = e2e_cold(args, local)
+        out["e2e"] = dict(cold) if cold else dict(warm)
+        out["e2e"]["value"] *= world
+        out["e2e"]["process"] = "fresh" if cold else "warm (fresh-process run failed)"
+        out["e2e_warm"] = dict(warm, value=warm["value"] * world)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_reference_sample(args.workload)
+    if rank == 0 and not args.no_batch:
+        # the metric's second part: time to a 1e-4 relative cost tolerance, batched against the
+        # plain one-reconstruction-at-a-time GPU path (16 uneven series; --workload batch-64
+        # runs the full 64)
+        out["time_to_converge"] = batch_measure(mbir, 16, batch_threads=args.batch_threads)
+    if rank == 0 and not args.no_serve:
+        # the third part: p50/p99 request latency of the served stream, at the benchmark's 20
+        # requests/s (more than one GPU serves: the queue grows) and at 2 requests/s
+        out["serving"] = {"rate_20": serve_measure(mbir, 24, 20.0, one_at_a_time=True),
+                          "rate_2": serve_measure(mbir, 12, 2.0, one_at_a_time=False)}
     if rank == 0:
         print(json.dumps(out))
     eng.close()

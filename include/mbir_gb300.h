@@ -48,9 +48,11 @@ extern "C" {
 #define MBIR_ORDER_PARALLEL 0  /* red/black y-slices x conflict-free voxel sets (GPU order) */
 #define MBIR_ORDER_REFERENCE 1 /* the reference's single-task random line order, y sequential */
 
-#define MBIR_SEED_PER_CALL 0   /* reference order: each NHICD call's list drawn from seed + 1 + call */
-#define MBIR_SEED_FIXED 1      /* reference order: every list drawn from `seed`, as the reference
-                                  draws them when its millisecond clock seed does not change */
+#define MBIR_SEED_PER_CALL 0   /* reference order: HAADF sweep k visits in the order drawn from
+                                  seed + k, BF NHICD call k's list from seed + 1 + k (the reference
+                                  reseeds from its millisecond clock each time) */
+#define MBIR_SEED_FIXED 1      /* reference order: every order and list drawn from `seed`, as the
+                                  reference draws them when its clock seed does not change */
 
 #define MBIR_PRECISION_FP32 0  /* volume, error sinogram and footprints in FP32 (reductions FP64) */
 #define MBIR_PRECISION_FP64 1  /* everything in FP64, the reference's Real_t */
@@ -79,7 +81,8 @@ typedef struct mbir_params {
   double default_variance;    /* --default_variance */
   double default_recon_value; /* --default_recon_value */
   int32_t extend_object;      /* --extend_object */
-  int32_t interpolate_initial_recon; /* --interpolate_initial_recon */
+  int32_t interpolate_initial_recon; /* --interpolate_initial_recon: mbir_set_initial_volume takes
+                                 a half-size volume and replicates each voxel 2x2x2 */
   int32_t tilt_selection;     /* --tilt_selection: 0 = a-tilt, 1 = b-tilt */
   int32_t use_subvolume;      /* --subvolume given */
   int32_t subvolume[6];       /* xmin,ymin,zmin,xmax,ymax,zmax */
@@ -96,7 +99,7 @@ typedef struct mbir_params {
   int32_t zero_skipping;      /* 1 */
   int32_t noise_model;        /* 1 */
   int32_t noise_estimation;   /* 0 (never set by the reference; zero-initialised here) */
-  int32_t estimate_prior;     /* 0 */
+  int32_t estimate_prior;     /* 0 (1 is not supported: mbir_create fails, MBIR_ENOTSUP elsewhere) */
   double threshold_reduction_factor; /* 1 */
   /* QGGMRF prior rho(d) = (|d|^P/s^P) / (c + |d|^(P-Q)/s^(P-Q)) */
   double qggmrf_p;            /* 2 */
@@ -129,7 +132,7 @@ typedef struct mbir_params {
                                  bits).  mbir_get_call_lines returns the visit order of 0 and 2.
                                  The colouring runs on the device; the schedules of the 20
                                  homogeneous sub-lists are built once and reused. */
-  int32_t seed_mode;          /* MBIR_SEED_PER_CALL / MBIR_SEED_FIXED (reference order, BF) */
+  int32_t seed_mode;          /* MBIR_SEED_PER_CALL / MBIR_SEED_FIXED (reference order) */
   int32_t float_params;       /* 1: round the parameters the reference's pipeline keeps in float
                                  members (thickness, target gain, stop threshold, sigma_x,
                                  diffuseness with q = diffuseness + 1 in float, default offset,
@@ -178,7 +181,9 @@ int32_t mbir_set_sinogram(mbir_engine* e, const float* counts, const float* tilt
  * excluded_views and tilt_selection exactly as the reference reader. */
 int32_t mbir_load_sinogram_mrc(mbir_engine* e, const char* path);
 
-/* Optional initial volume [z][x][y] (y fastest), sized as mbir_get_dims reports. */
+/* Optional initial volume [z][x][y] (y fastest), sized as mbir_get_dims reports; with
+ * interpolate_initial_recon set, (N_z/2) x (N_x/2) x (N_y/2) values, each filling its 2x2x2 block
+ * (InitialReconstructionBinReader.cpp:101-131; needs the sinogram set first). */
 int32_t mbir_set_initial_volume(mbir_engine* e, const float* vol, int64_t n);
 /* Optional initial nuisance vectors (length n_theta each; NULL keeps the default). */
 int32_t mbir_set_initial_nuisance(mbir_engine* e, const double* gains, const double* offsets,
@@ -322,9 +327,8 @@ const char* mbir_server_last_error(const mbir_server* s);
 /* Library version string */
 const char* mbir_version(void);
 
-/* Per-view sums of squared errors, sums_dev[v] = sum over r, t of error_dev[v][r][t]^2 (the sums
- * updateWeights divides by N_r N_t, HAADF_ReconstructionEngine_Extra.cpp:825-833), computed on
- * caller-owned device buffers (FP32 error sinogram in the reference's [theta][r][t] layout, FP64
+/* Per-view sums of squared errors, sums_dev[v] = sum over r, t of error_dev[v][r][t]^2 (the sums a
+ * per-view noise-variance estimate divides by N_r N_t), computed on caller-owned device buffers (FP32 error sinogram in the reference's [theta][r][t] layout, FP64
  * output of n_theta values) with no allocation: for callers whose device memory is owned by their
  * own pool, or whose path must not allocate.  No counterpart in the reference (it is this
  * library's addition).  Limits: n_theta <= 1024 (MBIR_EINVAL beyond); the scratch (128 KiB of
@@ -352,16 +356,6 @@ int32_t mbir_level_schedule(int32_t n_z, int32_t n_x, int32_t n_theta, int32_t n
                             int32_t* lines, int32_t lines_cap, int32_t* lofs, int32_t lofs_cap,
                             int32_t* n_lines, int32_t* n_levels);
 
-/* Colour schedule of one sparse ICD call (host only; what a BF NHICD call runs with
- * call_schedule = 0).  Same inputs as mbir_level_schedule without the row walk: the call's
- * lines are visited z-major (z, then x ascending) and each takes the smallest colour that no
- * earlier line sharing a touched bin at some view, or lying in its 3x3 (z, x) neighbourhood,
- * holds and that has fewer than class_cap lines (0: no cap; the engine caps classes at the
- * sweep kernel's voxel groups).  Writes the lines colour by colour (z-major within a colour)
- * and the colour offsets;
- * MBIR_EINVAL on bad input, short buffers or more than max_colours (<= 4096) colours.  Replaces
- * no reference interface (the reference draws a random visit order per call,
- * BFReconstructionEngine_Extra.cpp:576-628). */
 /* The last scheduled BF call's schedule (call_schedule 0 or 2): its lines level by level
  * (lines[cap]) and the level offsets (lofs[lofs_cap], n_levels + 1 values); *n_lines and
  * *n_levels receive the counts (0 after a row-walk call).  Any pointer may be NULL.  No
@@ -376,6 +370,16 @@ int32_t mbir_get_call_schedule(mbir_engine* e, int32_t* lines, int32_t cap, int3
 int32_t mbir_get_footprint_bins(mbir_engine* e, int16_t* lo, uint16_t* mask,
                                 uint8_t* lineok);
 
+/* Colour schedule of one sparse ICD call (host only; what a BF NHICD call runs with
+ * call_schedule = 0).  Same inputs as mbir_level_schedule without the row walk: the call's
+ * lines are visited z-major (z, then x ascending) and each takes the smallest colour that no
+ * earlier line sharing a touched bin at some view, or lying in its 3x3 (z, x) neighbourhood,
+ * holds and that has fewer than class_cap lines (0: no cap; the engine caps classes at the
+ * sweep kernel's voxel groups).  Writes the lines colour by colour (z-major within a colour)
+ * and the colour offsets;
+ * MBIR_EINVAL on bad input, short buffers or more than max_colours (<= 4096) colours.  Replaces
+ * no reference interface (the reference draws a random visit order per call,
+ * BFReconstructionEngine_Extra.cpp:576-628). */
 int32_t mbir_colour_schedule(int32_t n_z, int32_t n_x, int32_t n_theta, int32_t n_r, int32_t nb,
                              int32_t max_colours, int32_t class_cap, const uint8_t* lineok,
                              const uint8_t* active,

@@ -147,6 +147,12 @@ mbir_engine* mbir_create(const mbir_params* p) {
     g_create_error = "mbir_create: invalid bright-field parameter";
     return nullptr;
   }
+  if (p->estimate_prior) {
+    // ESTIMATE_PRIOR (HAADF_ReconstructionEngine.cpp:807-812): the sigma_x re-estimate between
+    // outer iterations is not built; refuse rather than run a different algorithm
+    g_create_error = "mbir_create: estimate_prior is not supported by this build";
+    return nullptr;
+  }
   if (!(p->sigma_x > 0) || p->num_resolutions < 1 || p->final_resolution < 1 ||
       !(p->qggmrf_c > 0) || !(p->qggmrf_p > 0) ||
       (p->seed_mode != MBIR_SEED_PER_CALL && p->seed_mode != MBIR_SEED_FIXED)) {
@@ -293,6 +299,7 @@ int32_t mbir_run_multires(const mbir_params* p, const float* counts, const float
                           int32_t n_theta, int32_t n_r, int32_t n_t, double delta_r,
                           double delta_t, float* out, int64_t n, int32_t* dims_out) {
   if (!p || !counts || !tilts_deg) return MBIR_EINVAL;
+  if (p->estimate_prior) return MBIR_ENOTSUP;
   const mbir_params top = with_float_params(*p);
   p = &top;
   const int levels = p->num_resolutions > 0 ? p->num_resolutions : 1;
@@ -434,6 +441,7 @@ int64_t mbir_server_submit(mbir_server* s, const mbir_params* p, const float* co
                            double dr, double dt, int32_t max_outer, double tol) {
   if (!s || !p || !counts || !tilts) return MBIR_EINVAL;
   if (p->struct_size != static_cast<int32_t>(sizeof(mbir_params))) return MBIR_EINVAL;
+  if (p->estimate_prior) return MBIR_ENOTSUP;
   if (p->modality != MBIR_MODALITY_HAADF && p->modality != MBIR_MODALITY_BF) return MBIR_EINVAL;
   try {
     return s->impl->submit(*p, counts, tilts, n_theta, n_r, n_t, dr, dt, max_outer, tol);

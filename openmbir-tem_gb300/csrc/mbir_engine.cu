@@ -212,7 +212,34 @@ int Engine::set_sinogram(const float* counts, const float* tilts_deg, int n_thet
 
 int Engine::set_initial_volume(const float* vol, int64_t n) {
   if (!vol || n <= 0) return fail(MBIR_EINVAL, "set_initial_volume: bad arguments");
-  init_vol_.assign(vol, vol + n);
+  if (!p_.interpolate_initial_recon) {
+    init_vol_.assign(vol, vol + n);
+    host_ready_ = false;
+    return MBIR_OK;
+  }
+  // --interpolate_initial_recon (InitialReconstructionBinReader.cpp:101-131): the given volume
+  // has half the voxels along each axis ([z][x][y] of N_z/2 x N_x/2 x N_y/2, integer halves);
+  // each value fills its 2x2x2 block and the rest of the volume starts at zero
+  if (state_ < 1) return fail(MBIR_ESTATE, "set_initial_volume: set the sinogram first");
+  if (g_.n_y == 0) {
+    int rc = build_geometry();
+    if (rc) return rc;
+  }
+  const int hz = g_.n_z / 2, hx = g_.n_x / 2, hy = g_.n_y / 2;
+  if (n != static_cast<int64_t>(hz) * hx * hy)
+    return fail(MBIR_EINVAL, "set_initial_volume: the interpolated initial volume must hold "
+                             "(N_z/2) x (N_x/2) x (N_y/2) voxels");
+  init_vol_.assign(static_cast<size_t>(g_.n_z) * g_.n_x * g_.n_y, 0.f);
+  for (int z = 0; z < hz; z++)
+    for (int x = 0; x < hx; x++)
+      for (int y = 0; y < hy; y++) {
+        const float b = vol[(static_cast<size_t>(z) * hx + x) * hy + y];
+        for (int a = 0; a < 2; a++)
+          for (int c = 0; c < 2; c++)
+            for (int r = 0; r < 2; r++)
+              init_vol_[(static_cast<size_t>(2 * z + a) * g_.n_x + 2 * x + c) * g_.n_y + 2 * y +
+                        r] = b;
+      }
   host_ready_ = false;
   return MBIR_OK;
 }
@@ -884,8 +911,14 @@ int Engine::sweep(int outer, int inner, double* stats4) {
   int rc = 0;
   cudaEventRecord(static_cast<cudaEvent_t>(ev0_), s);
   if (p_.order_mode == MBIR_ORDER_REFERENCE) {
+    // UpdateYSlice seeds its generator from the millisecond clock at every sweep
+    // (HAADF_ReconstructionEngine_UpdateVoxels.cpp:161-162): a new order per sweep (seed + sweep
+    // index), or the same order every sweep as with the clock frozen (MBIR_SEED_FIXED)
+    const uint32_t sweep_seed = p_.seed_mode == MBIR_SEED_FIXED
+                                    ? p_.seed
+                                    : p_.seed + static_cast<uint32_t>(sweeps_done_);
     std::vector<int32_t> lines;
-    reference_visit_order(p_.seed, g.n_z, g.n_x, lines);
+    reference_visit_order(sweep_seed, g.n_z, g.n_x, lines);
     call_lines_ = lines;
     cudaMemcpyAsync(d_lines_, lines.data(), sizeof(int32_t) * lines.size(), cudaMemcpyHostToDevice, s);
     if (exact_) {

@@ -115,6 +115,7 @@ class Engine {
   int set_bragg_threshold(double t);
   // y-slab sharding (mbir_shard.cu): sweeps and per-view sums restricted to slices [y0, y1)
   int set_slab(int y0, int y1);
+  int slab_rows_owned();
   int sweep_colour(int colour, int outer, int inner, double* stats4);
   int get_planes(int y, int n, float* out);
   int set_planes(int y, int n, const float* in);
@@ -350,16 +351,34 @@ void host_parallel(int n, F fn) {
     fn(0, n);
     return;
   }
+  // the busy flag is released however this returns; threads that could not be created leave
+  // their ranges to the calling thread, and the threads already started are always joined
+  struct Release {
+    ~Release() { host_parallel_busy().store(0); }
+  } release;
   const int chunk = (n + nt - 1) / nt;
   std::vector<std::thread> pool;
   pool.reserve(nt - 1);
+  int next = chunk;  // first index not handed to a thread
   for (int t = 1; t < nt; ++t) {
     const int b = t * chunk, e = std::min(n, b + chunk);
-    if (b < e) pool.emplace_back(fn, b, e);
+    if (b >= e) break;
+    try {
+      pool.emplace_back(fn, b, e);
+    } catch (...) {
+      break;  // thread limit reached: run the rest here
+    }
+    next = e;
   }
+  struct Join {
+    std::vector<std::thread>& p;
+    ~Join() {
+      for (auto& th : p)
+        if (th.joinable()) th.join();
+    }
+  } join{pool};
   fn(0, std::min(n, chunk));
-  for (auto& th : pool) th.join();
-  host_parallel_busy().store(0);
+  if (next < n) fn(next, n);
 }
 
 // MRC I/O (mrc_io.cpp)

@@ -4,9 +4,9 @@
 // Callers that cannot allocate: a host framework that owns every byte of device memory through
 // its own pool (and forbids cudaMalloc/cudaFree while it streams, since those synchronise the
 // device and fragment its pool), or a latency-bound pipeline that must not pay an allocation on
-// the path.  For them mbir_error_view_sums_noalloc computes the sums updateWeights needs
-// (HAADF_ReconstructionEngine_Extra.cpp:825-833: sum over r, t of e^2 per view) from an error
-// sinogram they already hold on the device, writing into an output buffer they own.
+// the path.  For them mbir_error_view_sums_noalloc computes, per view, the sum over r and t of
+// e^2 (the sums a per-view noise-variance update divides by N_r N_t) from an error sinogram
+// they already hold on the device, writing into an output buffer they own.
 //
 // The only scratch is the file-scope array below (kMaxViews x kChunks doubles, 128 KiB):
 // per-(view, chunk) partial sums.  Every slot read in a call is written earlier in the same
@@ -102,7 +102,17 @@ extern "C" int32_t mbir_error_view_sums_noalloc(const float* error_dev, int32_t 
   const int rc = scratch_for_current_device(&partial);
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  view_sq_partial_kernel<<<dim3(n_theta, kChunks), 256, 0, s>>>(error_dev, n_r * n_t, partial);
-  view_sq_final_kernel<<<(n_theta + 127) / 128, 128, 0, s>>>(partial, n_theta, sums_dev);
-  return cudaGetLastError() == cudaSuccess ? MBIR_OK : MBIR_EDEVICE;
+  // Each launch's own status is returned by cudaLaunchKernel; cudaGetLastError would also
+  // return (and clear) an earlier, unrelated error of the caller's and report it as ours.
+  int n_rt = n_r * n_t;
+  void* a1[] = {const_cast<float**>(&error_dev), &n_rt, &partial};
+  if (cudaLaunchKernel(reinterpret_cast<const void*>(view_sq_partial_kernel),
+                       dim3(n_theta, kChunks), dim3(256), a1, 0, s) != cudaSuccess)
+    return MBIR_EDEVICE;
+  int nt = n_theta;
+  void* a2[] = {&partial, &nt, &sums_dev};
+  if (cudaLaunchKernel(reinterpret_cast<const void*>(view_sq_final_kernel),
+                       dim3((n_theta + 127) / 128), dim3(128), a2, 0, s) != cudaSuccess)
+    return MBIR_EDEVICE;
+  return MBIR_OK;
 }

@@ -49,6 +49,13 @@ Server::~Server() {
   for (auto& kv : all_) kv.second->engine.reset();
 }
 
+const char* Server::last_error() const {
+  thread_local std::string copy;
+  std::lock_guard<std::mutex> lk(mu_);
+  copy = err_;
+  return copy.c_str();
+}
+
 size_t Server::estimate_bytes(const Request& r) const {
   const size_t rb = r.params.precision == MBIR_PRECISION_FP64 ? 8 : 4;
   const size_t n_rp = (static_cast<size_t>(r.n_r) + 3) / 4 * 4;
@@ -61,6 +68,21 @@ size_t Server::estimate_bytes(const Request& r) const {
     const size_t lines = static_cast<size_t>(r.dims[0]) * r.dims[1];
     bf = rb * sino + static_cast<size_t>(r.n_t) * r.n_theta * n_sp +
          8 * static_cast<size_t>(r.n_theta) * r.n_r * r.n_t + lines * (8 * 3 + 1);
+    if (r.params.nhicd && r.params.call_schedule != 1) {
+      // scheduled NHICD calls (Engine::bf_prepare_schedule): the A-column table of every line,
+      // [lines][n_theta][acol_width(nb)] float4 with nb = 2 * (voxel / detector size) + 1, the
+      // schedule, and the device colouring's packed bins, conflict words and colour planes
+      const int levels = std::max(1, r.params.num_resolutions);
+      const int lvl = (r.params.level < 0 || r.params.level >= levels) ? levels - 1
+                                                                       : r.params.level;
+      const int factor = (1 << (levels - 1 - lvl)) * std::max(1, r.params.final_resolution);
+      const size_t acol_w = static_cast<size_t>(2 * factor + 1 + 4) / 4;
+      const size_t entries = lines * r.n_theta;
+      const size_t words = 8;  // 64-bit colour words per bin / line (512 colours)
+      bf += entries * acol_w * 16 + (2 * lines + 1) * 4 + entries * 4 + lines * (4 + 12 + 2 + 4) +
+            static_cast<size_t>(r.n_theta) * r.n_r * words * 8 + lines * words * 8 +
+            20 * (std::min<size_t>(64 * words, lines) + 1) * 4 + 64;
+    }
   }
   return rb * (3 * sino + vox) + host_layout + bf + (1u << 20);
 }
@@ -85,6 +107,7 @@ int64_t Server::submit(const mbir_params& p, const float* counts, const float* t
   int32_t d[6];
   if (rc == 0) rc = r->engine->dims(d);
   if (rc) {
+    std::lock_guard<std::mutex> lk(mu_);
     err_ = r->engine->last_error();
     return rc;
   }

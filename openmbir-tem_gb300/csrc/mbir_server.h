@@ -59,7 +59,8 @@ class Server {
   int result(int64_t id, float* out, int64_t n, int32_t* dims);
   int release(int64_t id);
   int stats(ServerStats* st);
-  const char* last_error() const { return err_.c_str(); }
+  // a copy taken under the lock, owned by the calling thread (valid until its next call)
+  const char* last_error() const;
 
  private:
   void loop();
@@ -73,7 +74,7 @@ class Server {
   int64_t used_ = 0;
   int64_t last_admitted_id_ = 0;
   int64_t next_id_ = 1;
-  std::mutex mu_;
+  mutable std::mutex mu_;
   std::condition_variable cv_, done_cv_;
   std::deque<Request*> queue_;
   std::vector<Request*> active_;

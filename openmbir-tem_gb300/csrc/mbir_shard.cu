@@ -25,6 +25,23 @@ int Engine::set_slab(int y0, int y1) {
   if (y0 < 0 || y1 > g_.n_y || y0 >= y1) return fail(MBIR_EINVAL, "set_slab: bad slice range");
   slab_y0_ = y0;
   slab_y1_ = y1;
+  return slab_rows_owned();
+}
+
+// A slab owns its detector rows only when its edge slices share no row with the slices just
+// outside it (at delta_xy = delta_t every slice has its own row; other pixel shapes let slices
+// y and y+1 share one, and two slab engines would then update their own copies of that row).
+// Checked once the voxel-line response exists (set_slab after prepare, or the first sweep).
+int Engine::slab_rows_owned() {
+  if (slab_y1_ <= 0 || static_cast<int>(tab_.t_first.size()) != g_.n_y) return MBIR_OK;
+  auto shared = [&](int a, int b) {
+    return tab_.t_count[a] > 0 && tab_.t_count[b] > 0 &&
+           tab_.t_first[a] + tab_.t_count[a] > tab_.t_first[b];
+  };
+  if ((slab_y0_ > 0 && shared(slab_y0_ - 1, slab_y0_)) ||
+      (slab_y1_ < g_.n_y && shared(slab_y1_ - 1, slab_y1_)))
+    return fail(MBIR_ENOTSUP, "set_slab: an edge slice of the slab shares detector rows with "
+                              "the slice next to it outside the slab");
   return MBIR_OK;
 }
 
@@ -35,6 +52,7 @@ int Engine::sweep_colour(int colour, int outer, int inner, double* st4) {
   if (bf_ || p_.order_mode != MBIR_ORDER_PARALLEL)
     return fail(MBIR_ENOTSUP, "sweep_colour: HAADF parallel order only");
   if (colour != 0 && colour != 1) return fail(MBIR_EINVAL, "sweep_colour: colour is 0 or 1");
+  if (int rc = slab_rows_owned()) return rc;
   const Geometry& g = g_;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
   const int y0 = slab_y1_ > 0 ? slab_y0_ : 0, y1 = slab_y1_ > 0 ? slab_y1_ : g.n_y;

@@ -31,6 +31,23 @@ def slabs(n_y, world):
     return out
 
 
+def check_slab_rows(rows, bounds):
+    """Slabs own their detector rows only when no two neighbouring slabs' edge slices share a
+    row.  rows[y] = (first detector row, row count) of slice y's voxel-line response
+    (storeVoxelResponse, HAADF_ReconstructionEngine_Extra.cpp:329-404); at delta_xy = delta_t
+    each slice has exactly its own row, but other pixel shapes let slices y and y+1 share one.
+    Raises ValueError naming the first shared boundary (every rank sees the same rows and
+    bounds, so every rank raises before any exchange)."""
+    for (a0, a1), (b0, b1) in zip(bounds[:-1], bounds[1:]):
+        if a1 <= a0 or b1 <= b0:
+            continue
+        last, first = rows[a1 - 1], rows[b0]
+        if last[1] > 0 and first[1] > 0 and last[0] + last[1] > first[0]:
+            raise ValueError(f"slabs [{a0}, {a1}) and [{b0}, {b1}) share detector rows "
+                             f"(slice {a1 - 1} ends at row {last[0] + last[1] - 1}, slice {b0} "
+                             f"starts at row {first[0]})")
+
+
 def solve_gain_offset(sums, target_gain):
     """The Lagrange solve of jointEstimation (HAADF_ReconstructionEngine_Extra.cpp:521-598) from
     the six per-view sums [theta][6] = (y w, w, yh w, yh w y, y^2 w, yh^2 w); mean gain fixed to
@@ -122,7 +139,10 @@ def run_sharded(dist, backend, n_outer, target_gain=1.0, joint_estimation=True,
     nz, nx, n_y, n_theta, n_r, n_t = backend.dims()
     world = dist.get_world_size()
     rank = dist.get_rank()
-    y0, y1 = slabs(n_y, world)[rank]
+    bounds = slabs(n_y, world)
+    if hasattr(backend, "slice_rows"):
+        check_slab_rows(backend.slice_rows(), bounds)
+    y0, y1 = bounds[rank]
     backend.set_slab(y0, y1)
     history = []
     for outer in range(n_outer):

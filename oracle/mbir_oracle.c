@@ -1116,6 +1116,13 @@ static double prior_cost(const orc_ctx* c) {
 /* HAADF_ReconstructionEngine::execute outer/inner loops (HAADF_ReconstructionEngine.cpp:706-815)
  * with RegularRandomOrderUpdate and the ROI stop rule of updateVoxels (_UpdateVoxels.cpp:765-787). */
 int orc_run(orc_ctx* c, uint32_t seed, double* cost_log, int n_cost) {
+  return orc_run_seeded(c, seed, 0u, cost_log, n_cost);
+}
+
+/* The same with sweep k drawing its order from seed + k * seed_step: the reference reseeds from
+ * its millisecond clock at every sweep, so consecutive sweeps visit the lines in new orders
+ * (seed_step = 0: one order for every sweep, the clock frozen). */
+int orc_run_seeded(orc_ctx* c, uint32_t seed, uint32_t seed_step, double* cost_log, int n_cost) {
   int sweeps = 0;
   double stop = c->p.stop_threshold;
   int num_iter = c->p.inner_iterations;
@@ -1124,7 +1131,7 @@ int orc_run(orc_ctx* c, uint32_t seed, double* cost_log, int n_cost) {
     int status = 1;
     for (int inner = 0; inner < num_iter; inner++) {
       double st[4];
-      orc_icd_sweep_reference(c, seed, outer, inner, st);
+      orc_icd_sweep_reference(c, seed + (uint32_t)sweeps * seed_step, outer, inner, st);
       if (cost_log && sweeps < n_cost) cost_log[sweeps] = orc_cost(c, NULL);
       sweeps++;
       status = 1;

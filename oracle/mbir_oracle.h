@@ -123,6 +123,8 @@ void orc_visit_order(uint32_t seed, int n_z, int n_x, int32_t* out);
  * loops with a fixed reference-order seed per sweep.  cost_log (optional, capacity n_cost)
  * receives the cost after every sweep; returns the number of sweeps run. */
 int orc_run(orc_ctx* c, uint32_t seed, double* cost_log, int n_cost);
+/* the same with sweep k visiting in the order drawn from seed + k * seed_step */
+int orc_run_seeded(orc_ctx* c, uint32_t seed, uint32_t seed_step, double* cost_log, int n_cost);
 
 /* ---- bright field -------------------------------------------------------------------- */
 /* selector [n_theta][n_r][n_t] (1: entry selected, quadratic data term) */

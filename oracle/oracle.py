@@ -83,6 +83,7 @@ def lib():
             "orc_cost": (C.c_double, [C.c_void_p, _D]),
             "orc_visit_order": (None, [C.c_uint32, C.c_int, C.c_int, _I]),
             "orc_run": (C.c_int, [C.c_void_p, C.c_uint32, _D, C.c_int]),
+            "orc_run_seeded": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, _D, C.c_int]),
             "orc_selector": (_U8, [C.c_void_p]), "orc_filt_map": (_D, [C.c_void_p]),
             "orc_set_bragg": (None, [C.c_void_p, C.c_double]),
             "orc_get_bragg": (C.c_double, [C.c_void_p]),
@@ -411,9 +412,11 @@ class Oracle:
         """The measurements the engine works on (BF: -log(counts + bf_offset) once prepared)."""
         return self._view(lib().orc_counts, self.shape)
 
-    def run(self, seed, n_cost=0):
+    def run(self, seed, n_cost=0, seed_step=0):
+        """execute()'s loops; sweep k visits in the order of seed + k * seed_step."""
         log = np.zeros(max(n_cost, 1))
-        n = lib().orc_run(self._h, seed, log.ctypes.data_as(_D) if n_cost else None, n_cost)
+        n = lib().orc_run_seeded(self._h, seed, seed_step,
+                                 log.ctypes.data_as(_D) if n_cost else None, n_cost)
         return n, log[:min(n, n_cost)]
 
 

@@ -68,6 +68,7 @@ def haadf_params(mbir, thickness, **kw):
     p.inner_iterations = 1
     p.stop_threshold = 0.0
     p.lane_shape = 1  # fixed voxel-group shape: engines compared bit for bit must agree
+    p.seed_mode = mbir.SEED_FIXED  # reference order: one visit order for every sweep
     for k, v in kw.items():
         setattr(p, k, v)
     return p

@@ -58,6 +58,27 @@ class OracleBackend:
         if variance is not None:
             self.o.apply_nuisance(self.o.gain().copy(), self.o.offset().copy(), variance)
 
+    def slice_rows(self):
+        out = []
+        for y in range(self.o.ny):
+            t0, val = self.o.voxel_line_response(y)
+            out.append((t0, len(val)))
+        return out
+
+
+class LostRankBackend(OracleBackend):
+    """A rank whose host fails after `fail_after` sweeps: it raises between sweeps, with none
+    of its work in flight, and its process leaves the group."""
+
+    def __init__(self, o, schedule, fail_after):
+        super().__init__(o, schedule)
+        self.fail_after = fail_after
+
+    def sweep_colour(self, colour, outer, inner):
+        if colour == 0 and self.sweeps == self.fail_after:
+            raise RuntimeError("injected host failure")
+        return super().sweep_colour(colour, outer, inner)
+
 
 def _problem():
     import mbir
@@ -134,3 +155,108 @@ def test_two_cpu_ranks_match_single_process(oracle_mod, lib_built):
     np.testing.assert_allclose(g, o.gain(), rtol=1e-9)
     np.testing.assert_allclose(off, o.offset(), rtol=1e-9, atol=1e-12)
     np.testing.assert_allclose(var, o.variance(), rtol=1e-9)
+
+
+def test_check_slab_rows_finds_shared_rows():
+    import shard
+    own = [(y, 1) for y in range(8)]
+    shard.check_slab_rows(own, shard.slabs(8, 2))
+    wide = [(y, 2) for y in range(8)]  # slice y covers rows y and y+1
+    with pytest.raises(ValueError, match="share detector rows"):
+        shard.check_slab_rows(wide, shard.slabs(8, 2))
+
+
+def _rank_shared_rows(rank, world, port, q):
+    import sys
+    from datetime import timedelta
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    for d in (os.path.join(root, "openmbir-tem_gb300"), os.path.join(root, "oracle"), here):
+        sys.path.insert(0, d)
+    import torch.distributed as dist
+    import oracle
+    import shard
+    from conftest import small_case
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world, timeout=timedelta(seconds=30))
+    try:
+        import mbir
+        from conftest import haadf_params
+        y, ang, th = small_case()
+        p = haadf_params(mbir, th)
+        # rectangular pixels: delta_r = 1.5 delta_t, so a voxel slice (delta_xy = delta_r)
+        # spans one and a half detector rows and neighbouring slices share a row
+        o = oracle.Oracle(oracle.params_from_mbir(p), y, ang, 1.5, 1.0)
+        be = OracleBackend(o, None)
+        try:
+            shard.run_sharded(dist, be, 1, p.target_gain)
+            q.put((rank, "ran"))
+        except ValueError as ex:
+            q.put((rank, str(ex)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_cpu_ranks_refuse_shared_boundary_rows(oracle_mod, lib_built):
+    """Slabs whose edge slices share a detector row cannot own it: both ranks refuse before any
+    exchange (the engine's set_slab answers MBIR_ENOTSUP for the same case)."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_shared_rows, args=(r, 2, port, q)) for r in range(2)]
+    for pr in procs:
+        pr.start()
+    got = dict(q.get(timeout=300) for _ in range(2))
+    for pr in procs:
+        pr.join(timeout=60)
+        assert pr.exitcode == 0
+    assert all("share detector rows" in m for m in got.values()), got
+
+
+def _rank_lost(rank, world, port, q):
+    import sys
+    import time
+    from datetime import timedelta
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    for d in (os.path.join(root, "openmbir-tem_gb300"), os.path.join(root, "oracle"), here):
+        sys.path.insert(0, d)
+    import torch.distributed as dist
+    import shard
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world, timeout=timedelta(seconds=10))
+    e, o, p = _problem()
+    be = LostRankBackend(o, e.schedule, 1) if rank == 1 else OracleBackend(o, e.schedule)
+    t0 = time.time()
+    try:
+        shard.run_sharded(dist, be, 3, p.target_gain)
+        q.put((rank, "finished", time.time() - t0))
+    except Exception as ex:  # the survivor sees the lost peer as a failed collective
+        q.put((rank, type(ex).__name__ + ": " + str(ex)[:200], time.time() - t0))
+    q.close()
+    q.join_thread()  # the message is on its way before the process leaves
+    # no destroy_process_group: the failed rank leaves, as a crashed host would
+    os._exit(0)
+
+
+def test_lost_cpu_rank_fails_the_next_exchange(oracle_mod, lib_built):
+    """Failure detection on CPU ranks: rank 1 fails between sweeps (after its first sweep, with
+    nothing in flight) and leaves.  Rank 0 does not hang: its next exchange ends with an error
+    within the process group's timeout."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_lost, args=(r, 2, port, q)) for r in range(2)]
+    for pr in procs:
+        pr.start()
+    got = {}
+    for _ in range(2):
+        r, msg, dt = q.get(timeout=300)
+        got[r] = (msg, dt)
+    for pr in procs:
+        pr.join(timeout=60)
+    assert "injected host failure" in got[1][0]
+    assert got[0][0] != "finished", got
+    assert got[0][1] < 120, got
