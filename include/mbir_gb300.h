@@ -161,6 +161,8 @@ typedef struct mbir_status {
   double kernel_ms_total; /* device time of the parallel-order sweep kernels alone (colour
                              launches; icd_ms_total also holds list, schedule and statistics) */
   double colour_ms_total; /* device time of the colour-schedule launches (call_schedule 0) */
+  int64_t pipelined_launches; /* colour launches of scheduled BF calls run by the pipelined
+                                 kernel (next classes' loads in flight) */
 } mbir_status;
 
 typedef struct mbir_engine mbir_engine;

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -91,6 +92,8 @@ Engine::Engine(const mbir_params& p) : p_(p) {
   bf_ = p_.modality == MBIR_MODALITY_BF;
   rb_ = fp64_ ? sizeof(double) : sizeof(float);
   bins_ = p_.detector_response_bins > 0 ? p_.detector_response_bins : 64;
+  const char* pl = std::getenv("MBIR_PIPELINED_SCHED");
+  pipelined_ = !(pl != nullptr && pl[0] == '0');
 }
 
 Engine::~Engine() { release(); }
@@ -1334,6 +1337,7 @@ int Engine::status(mbir_status* st) const {
   st->sched_ms_total = sched_ms_;
   st->kernel_ms_total = kernel_ms_;
   st->colour_ms_total = colour_ms_;
+  st->pipelined_launches = pipelined_launches_;
   return MBIR_OK;
 }
 

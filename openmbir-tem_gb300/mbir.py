@@ -99,6 +99,7 @@ class MbirStatus(C.Structure):
         ("stride", C.c_int32), ("staged", C.c_int32), ("lane_shape", C.c_int32),
         ("sched_levels", C.c_int32), ("sched_ms_total", C.c_double),
         ("kernel_ms_total", C.c_double), ("colour_ms_total", C.c_double),
+        ("pipelined_launches", C.c_int64),
     ]
 
 
