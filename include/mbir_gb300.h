@@ -252,8 +252,17 @@ int32_t mbir_status_get(mbir_engine* e, mbir_status* st);
 void mbir_cancel(mbir_engine* e);
 
 /* ReconstructedVolume MRC (float32, z reversed, x cropped as the reference), ReconstructedObject.bin
- * (double, y-x-z), Final{Gain,Offset}Parameters.bin and FinalVariances.bin (double[N_theta]). */
+ * (double, y-x-z), Final{Gain,Offset}Parameters.bin and FinalVariances.bin (double[N_theta]),
+ * ReconstructedSinogram.bin ((y - e) * I + mu, double [theta][r][t]) in `dir`.  Replaces
+ * HAADF_ForwardModel::writeMRCFile / writeReconstructionFile / writeNuisanceParameters /
+ * writeSinogramFile (HAADF_ForwardModel.cpp:34-137). */
 int32_t mbir_write_outputs(mbir_engine* e, const char* dir, const char* mrc_path);
+/* The same plus the VTK legacy volume (binary structured points, big-endian float32, scalar
+ * "TomoVoxel") and the Avizo AmiraMesh volume (binary little-endian float lattice) when their
+ * paths are not NULL or empty; replaces writeVtkFile / writeAvizoFile
+ * (HAADF_ForwardModel.cpp:139-242, VTKFileWriters.hpp, AvizoUniformCoordinateWriter.cpp). */
+int32_t mbir_write_outputs_ex(mbir_engine* e, const char* dir, const char* mrc_path,
+                              const char* vtk_path, const char* avizo_path);
 
 /* Multi-resolution pipeline (HAADF_MultiResolutionReconstruction::execute,
  * HAADF_MultiResolutionReconstruction.cpp:175-485): coarse-to-fine levels with sigma_x scaling

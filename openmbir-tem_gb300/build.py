@@ -38,6 +38,9 @@ def nvcc():
 def _stale():
     if not os.path.exists(LIB):
         return True
+    if any(not os.path.exists(os.path.join(HERE, "bin", n))
+           for n in ("HAADFReconstruction", "BFReconstruction")):
+        return True
     t = os.path.getmtime(LIB)
     deps = [os.path.join(CSRC, s) for s in SOURCES + HEADERS]
     deps.append(os.path.join(ROOT, "include", "mbir_gb300.h"))
@@ -93,7 +96,31 @@ def build(force=False, verbose=False, ptxas_v=False):
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_cli(verbose)
     return LIB
+
+
+CLI_SRC = os.path.join(HERE, "cli", "mbir_reconstruct.cpp")
+BIN = os.path.join(HERE, "bin")
+CLI_PROGRAMS = {"HAADFReconstruction": 0, "BFReconstruction": 1}
+
+
+def build_cli(verbose=False):
+    """The two command-line programs (bin/HAADFReconstruction, bin/BFReconstruction) over the
+    C ABI, linked to libmbir_gb300.so next to them (rpath $ORIGIN/..)."""
+    os.makedirs(BIN, exist_ok=True)
+    for name, bf in CLI_PROGRAMS.items():
+        exe = os.path.join(BIN, name)
+        deps = [CLI_SRC, LIB, os.path.join(ROOT, "include", "mbir_gb300.h")]
+        if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(d) for d in deps):
+            continue
+        cmd = ["g++", "-std=c++17", "-O2", f"-DMBIR_CLI_BF={bf}", "-o", exe, CLI_SRC,
+               f"-L{HERE}", "-l:libmbir_gb300.so", "-Wl,-rpath,$ORIGIN/.."]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"CLI build failed for {name}:\n{r.stdout}\n{r.stderr}")
 
 
 if __name__ == "__main__":

@@ -290,6 +290,11 @@ void mbir_cancel(mbir_engine* e) {
 int32_t mbir_write_outputs(mbir_engine* e, const char* dir, const char* mrc_path) {
   return guarded(e, [&](mbir::Engine& m) { return m.write_outputs(dir, mrc_path); });
 }
+int32_t mbir_write_outputs_ex(mbir_engine* e, const char* dir, const char* mrc_path,
+                              const char* vtk_path, const char* avizo_path) {
+  return guarded(
+      e, [&](mbir::Engine& m) { return m.write_outputs(dir, mrc_path, vtk_path, avizo_path); });
+}
 
 // HAADF_MultiResolutionReconstruction::execute (HAADF_MultiResolutionReconstruction.cpp:175-485):
 // per level i: sigma_x * 2^((levels-1-i)(1-3/p)), NumIter = 1 after the first level,

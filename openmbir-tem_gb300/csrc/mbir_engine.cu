@@ -1341,7 +1341,8 @@ int Engine::status(mbir_status* st) const {
   return MBIR_OK;
 }
 
-int Engine::write_outputs(const char* dir, const char* mrc_path) {
+int Engine::write_outputs(const char* dir, const char* mrc_path, const char* vtk_path,
+                          const char* avizo_path) {
   if (state_ < 2) return fail(MBIR_ESTATE, "write_outputs: nothing reconstructed");
   const Geometry& g = g_;
   const size_t nv = static_cast<size_t>(g.n_z) * g.n_x * g.n_y;
@@ -1371,29 +1372,55 @@ int Engine::write_outputs(const char* dir, const char* mrc_path) {
     std::fwrite(vecs[i]->data(), sizeof(double), g.n_theta, f);
     std::fclose(f);
   }
-  if (mrc_path && mrc_path[0]) {
-    // computeOriginalXDims (_Extra.cpp:252-275) and the "+1" of execute() (:882-886)
-    int crop_start = 0, crop_end = g.n_x;
-    for (int j = 0; j < g.n_x; j++) {
-      const double x = g.x0 + ((double)j + 0.5) * g.delta_xz;
-      if (x >= -(g.n_r * g.delta_r) / 2 && x <= (g.n_r * g.delta_r) / 2) {
-        crop_start = j;
-        break;
+  // ReconstructedSinogram.bin: (y - e) * I + mu per entry, [theta][r][t] doubles, y the
+  // measurements the engine works on (bright field: after -log) (execute :861-875,
+  // SinogramBinWriter.cpp:115-126)
+  {
+    const size_t ns = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;
+    std::vector<float> e(ns);
+    if ((rc = get_error(e.data(), static_cast<int64_t>(ns)))) return rc;
+    FILE* f = std::fopen((d + "/ReconstructedSinogram.bin").c_str(), "wb");
+    if (!f) return fail(MBIR_EIO, "cannot write ReconstructedSinogram.bin");
+    std::vector<double> buf(static_cast<size_t>(g.n_r) * g.n_t);
+    for (int th = 0; th < g.n_theta; ++th) {
+      for (size_t k = 0; k < buf.size(); ++k) {
+        const size_t i = static_cast<size_t>(th) * buf.size() + k;
+        const double y = bf_ ? ylog_[i] : static_cast<double>(counts_[i]);
+        buf[k] = (y - static_cast<double>(e[i])) * I_[th] + mu_[th];
       }
+      std::fwrite(buf.data(), sizeof(double), buf.size(), f);
     }
-    for (int j = g.n_x - 1; j >= 0; j--) {
-      const double x = g.x0 + ((double)j + 0.5) * g.delta_xz;
-      if (x >= -(g.n_r * g.delta_r) / 2 && x <= (g.n_r * g.delta_r) / 2) {
-        crop_end = j;
-        break;
-      }
-    }
-    crop_end += 1;
-    std::string err;
-    if (mrc_write_volume(mrc_path, vol.data(), g.n_z, g.n_x, g.n_y, crop_start, crop_end,
-                         g.length_x, err))
-      return fail(MBIR_EIO, err);
+    std::fclose(f);
   }
+  // computeOriginalXDims (_Extra.cpp:252-275): the columns whose centres lie on the detector;
+  // the VTK file takes [start, end), the MRC and Avizo files [start, end] (execute :879-901)
+  int crop_start = 0, crop_end = g.n_x;
+  for (int j = 0; j < g.n_x; j++) {
+    const double x = g.x0 + ((double)j + 0.5) * g.delta_xz;
+    if (x >= -(g.n_r * g.delta_r) / 2 && x <= (g.n_r * g.delta_r) / 2) {
+      crop_start = j;
+      break;
+    }
+  }
+  for (int j = g.n_x - 1; j >= 0; j--) {
+    const double x = g.x0 + ((double)j + 0.5) * g.delta_xz;
+    if (x >= -(g.n_r * g.delta_r) / 2 && x <= (g.n_r * g.delta_r) / 2) {
+      crop_end = j;
+      break;
+    }
+  }
+  std::string err;
+  if (vtk_path && vtk_path[0] &&
+      vtk_write_volume(vtk_path, vol.data(), g.n_z, g.n_x, g.n_y, crop_start, crop_end, err))
+    return fail(MBIR_EIO, err);
+  if (mrc_path && mrc_path[0] &&
+      mrc_write_volume(mrc_path, vol.data(), g.n_z, g.n_x, g.n_y, crop_start, crop_end + 1,
+                       g.length_x, err))
+    return fail(MBIR_EIO, err);
+  if (avizo_path && avizo_path[0] &&
+      avizo_write_volume(avizo_path, vol.data(), g.n_z, g.n_x, g.n_y, crop_start, crop_end + 1,
+                         g.delta_xy, g.delta_xz, err))
+    return fail(MBIR_EIO, err);
   return MBIR_OK;
 }
 

@@ -127,7 +127,8 @@ class Engine {
   int apply_nuisance(const double* gain, const double* offset, const double* variance);
   int status(mbir_status* st) const;
   void cancel() { cancel_.store(1); }
-  int write_outputs(const char* dir, const char* mrc_path);
+  int write_outputs(const char* dir, const char* mrc_path, const char* vtk_path = nullptr,
+                    const char* avizo_path = nullptr);
 
   const char* last_error() const { return err_.c_str(); }
   int fail(int code, const std::string& msg);
@@ -396,5 +397,10 @@ int mrc_read(const std::string& path, const int* vmin, const int* vmax, MrcVolum
              bool header_only, std::string& err);
 int mrc_write_volume(const std::string& path, const float* zxy, int n_z, int n_x, int n_y,
                      int x_start, int x_end, double length_x, std::string& err);
+int vtk_write_volume(const std::string& path, const float* zxy, int n_z, int n_x, int n_y,
+                     int x_start, int x_end, std::string& err);
+int avizo_write_volume(const std::string& path, const float* zxy, int n_z, int n_x, int n_y,
+                       int x_start, int x_end, double delta_xy, double delta_xz,
+                       std::string& err);
 
 }  // namespace mbir

@@ -2,9 +2,11 @@
 // reference's MRCReader / MRCWriter (Code/MBIRLib/IOFilters/MRCReader.cpp:99-368,
 // MRCWriter.cpp:90-290; header layout MRCHeader.h:46-212).  Fields are read and written at
 // their fixed byte offsets, little-endian, so no struct packing is assumed.
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -224,6 +226,102 @@ int mrc_write_volume(const std::string& path, const float* zxy, int n_z, int n_x
   std::fwrite(&dmin, 4, 1, f);
   std::fwrite(&dmax, 4, 1, f);
   std::fwrite(&mean, 4, 1, f);
+  std::fclose(f);
+  return MBIR_OK;
+}
+
+// VTK legacy structured points, binary (VTKFileWriters.hpp:288-321 as writeVtkFile uses it,
+// HAADF_ForwardModel.cpp:139-178): header lines, then the voxels as big-endian float32, z from
+// the last slice down, y, x over [x_start, x_end).
+int vtk_write_volume(const std::string& path, const float* zxy, int n_z, int n_x, int n_y,
+                     int x_start, int x_end, std::string& err) {
+  if (x_start < 0) x_start = 0;
+  if (x_end > n_x) x_end = n_x;
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) {
+    err = "cannot open '" + path + "' for writing";
+    return MBIR_EIO;
+  }
+  const int nx = x_end - x_start;
+  std::fprintf(f, "# vtk DataFile Version 2.0\n");
+  std::fprintf(f, "data set from OpenMBIR\n");
+  std::fprintf(f, "BINARY\n");
+  std::fprintf(f, "DATASET STRUCTURED_POINTS\n");
+  std::fprintf(f, "DIMENSIONS %d %d %d\n", nx, n_y, n_z);
+  std::fprintf(f, "ORIGIN 0.0 0.0 0.0\n");
+  std::fprintf(f, "SPACING %f %f %f\n", 1.0, 1.0, 1.0);
+  std::fprintf(f, "POINT_DATA %d\n\n", nx * n_y * n_z);
+  std::fprintf(f, "SCALARS %s float 1\n", "TomoVoxel");
+  std::fprintf(f, "LOOKUP_TABLE default\n");
+  std::vector<unsigned char> row(static_cast<size_t>(nx) * 4);
+  for (int z = n_z - 1; z >= 0; z--)
+    for (int y = 0; y < n_y; ++y) {
+      for (int x = x_start; x < x_end; ++x) {
+        uint32_t u;
+        const float d = zxy[(static_cast<size_t>(z) * n_x + x) * n_y + y];
+        std::memcpy(&u, &d, 4);
+        unsigned char* o = row.data() + 4 * static_cast<size_t>(x - x_start);
+        o[0] = static_cast<unsigned char>(u >> 24);
+        o[1] = static_cast<unsigned char>(u >> 16);
+        o[2] = static_cast<unsigned char>(u >> 8);
+        o[3] = static_cast<unsigned char>(u);
+      }
+      std::fwrite(row.data(), 1, row.size(), f);
+    }
+  std::fclose(f);
+  return MBIR_OK;
+}
+
+// AmiraMesh binary (AvizoUniformCoordinateWriter.cpp:110-196): text header with the lattice
+// size, bounding box (voxel sizes delta_xy, delta_xy, delta_xz as float) and a float lattice,
+// then "@1" and the voxels as little-endian float32, z from the last slice down, y, x.
+int avizo_write_volume(const std::string& path, const float* zxy, int n_z, int n_x, int n_y,
+                       int x_start, int x_end, double delta_xy, double delta_xz,
+                       std::string& err) {
+  if (x_start < 0) x_start = 0;
+  if (x_end > n_x) x_end = n_x;
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) {
+    err = "cannot open '" + path + "' for writing";
+    return MBIR_EIO;
+  }
+  const size_t x = static_cast<size_t>(x_end - x_start), y = n_y, z = n_z;
+  const float res[3] = {static_cast<float>(delta_xy), static_cast<float>(delta_xy),
+                        static_cast<float>(delta_xz)};
+  std::ostringstream ss;
+  ss << "# AmiraMesh BINARY-LITTLE-ENDIAN 2.1\n\n";
+  ss << "# Dimensions in x-, y-, and z-direction\n";
+  ss << "define Lattice " << x << " " << y << " " << z << "\n\n";
+  ss << "Parameters {\n";
+  ss << "     OpenMBIRParams {\n";
+  ss << "         Author \"OpenMBIR\",\n";
+  ss << "         DateTime \"\"\n";
+  ss << "     }\n";
+  ss << "     Units {\n";
+  ss << "         Coordinates \"microns\"\n";
+  ss << "     }\n";
+  ss << "     Content \"" << x << "x" << y << "x" << z << " int, uniform coordinates\",\n";
+  const float o = 0.0f;
+  ss << "     # Bounding Box is xmin xmax ymin ymax zmin zmax\n";
+  ss << "     BoundingBox " << o << " " << o + (res[0] * x);
+  ss << " " << o << " " << o + (res[1] * y);
+  ss << " " << o << " " << o + (res[2] * z);
+  ss << ",\n";
+  ss << "     CoordType \"uniform\"\n";
+  ss << "}\n\n";
+  ss << "Lattice { float TomoVoxels } = @1\n\n";
+  ss << "# Data section follows\n";
+  ss << "@1\n";
+  const std::string h = ss.str();
+  std::fwrite(h.data(), 1, h.size(), f);
+  std::vector<float> slice(x * y);
+  for (int zz = n_z - 1; zz >= 0; zz--) {
+    size_t idx = 0;
+    for (int yy = 0; yy < n_y; ++yy)
+      for (int xx = x_start; xx < x_end; ++xx)
+        slice[idx++] = zxy[(static_cast<size_t>(zz) * n_x + xx) * n_y + yy];
+    std::fwrite(slice.data(), sizeof(float), slice.size(), f);
+  }
   std::fclose(f);
   return MBIR_OK;
 }

@@ -12,6 +12,8 @@ oracle/_ref) and runs them through oracle/refrun.py on seeded synthetic inputs:
   outer iterations with 3 inner calls (the Bragg schedule: T = 5e10 for the first calls, then
   T = 3), NHICD lists, offset and variance estimation; and the first 6 calls of the same
   schedule (4 outer iterations);
+* output_headers.json -- the headers of the reference's MRC, VTK and Avizo volume files for the
+  reduced HAADF case (everything but the voxel values);
 * haadf_cfg0.json -- the benchmark's small HAADF configuration (128 x 32 detector, 71 views over
   +-70 deg at 2 deg, thickness 32, volume 128 x 32 x 64): SHA-256 digests and sums of the
   inputs and of the reference's float64 outputs after 1, 5 and 20 outer iterations.
@@ -52,6 +54,30 @@ def digest(a):
 def cfg0_input():
     y, ang, _ = synthetic.haadf_two_spheres()
     return y, ang
+
+
+def output_headers(tmp):
+    """The headers of the reference's volume files (MRC with its FEI extended header, VTK, Avizo)
+    for the reduced HAADF case, 1 outer iteration: everything but the voxel values."""
+    y, ang, th = small_case()
+    refrun.run_haadf(os.path.join(tmp, "hdr"), y, ang, th, 0.1, 0.2, 1, seed=HAADF_SEED)
+    out = os.path.join(tmp, "hdr", "out")
+    with open(os.path.join(out, "recon.mrc"), "rb") as f:
+        mrc = f.read(1024)
+        n_ext = int.from_bytes(mrc[92:96], "little")
+        ext = f.read(n_ext)
+    with open(os.path.join(out, "recon.vtk"), "rb") as f:
+        vtk = f.read()
+    vtk_hdr = vtk[:vtk.index(b"LOOKUP_TABLE default\n") + len(b"LOOKUP_TABLE default\n")]
+    with open(os.path.join(out, "recon.am"), "rb") as f:
+        am = f.read()
+    am_hdr = am[:am.index(b"# Data section follows\n@1\n") + len(b"# Data section follows\n@1\n")]
+    rec = {"mrc_header_hex": mrc.hex(), "mrc_ext_header_hex": ext.hex(),
+           "mrc_size": os.path.getsize(os.path.join(out, "recon.mrc")),
+           "vtk_header": vtk_hdr.decode(), "vtk_size": len(vtk),
+           "am_header": am_hdr.decode(), "am_size": len(am)}
+    with open(os.path.join(HERE, "output_headers.json"), "w") as f:
+        json.dump(rec, f, indent=1, sort_keys=True)
 
 
 def haadf_small(tmp):
@@ -105,6 +131,7 @@ def main():
         return 1
     with tempfile.TemporaryDirectory() as tmp:
         haadf_small(tmp)
+        output_headers(tmp)
         bf_small(tmp)
         haadf_cfg0(tmp)
     for f in sorted(os.listdir(HERE)):
