@@ -161,8 +161,6 @@ typedef struct mbir_status {
   double kernel_ms_total; /* device time of the parallel-order sweep kernels alone (colour
                              launches; icd_ms_total also holds list, schedule and statistics) */
   double colour_ms_total; /* device time of the colour-schedule launches (call_schedule 0) */
-  int64_t pipelined_launches; /* colour launches of scheduled BF calls run by the pipelined
-                                 kernel (next classes' loads in flight) */
 } mbir_status;
 
 typedef struct mbir_engine mbir_engine;
@@ -286,6 +284,11 @@ int32_t mbir_batch_size(const mbir_batch* b);
  * slices per SM; a slice's detector rows are staged in shared memory only when two CTAs' worth
  * fits, otherwise they are used in place in HBM).  Same results either way. */
 int32_t mbir_batch_set_threads(mbir_batch* b, int32_t threads);
+/* Limit (seconds, default 10) of the device-side wait in a batched sweep: a colour-1 slice waits
+ * for its series' colour-0 slices, and a wait that runs out skips that slice; the sweep then
+ * returns MBIR_ETIMEOUT and the engines stay usable.  No counterpart in the reference (its
+ * threads join with no limit, HAADF_ReconstructionEngine_UpdateVoxels.cpp:715). */
+int32_t mbir_batch_set_wait_limit(mbir_batch* b, double seconds);
 /* one sweep of every engine (outer index drives zero skipping); stats: 4 doubles per engine */
 int32_t mbir_batch_sweep(mbir_batch* b, int32_t outer, double* stats);
 /* outer iterations (batched sweep + per-engine gain/offset, variance, cost) until each engine's

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <numeric>
 #include <string>
@@ -166,7 +167,11 @@ int Batch::sweep(const std::vector<std::pair<int, int>>& iters, double* stats) {
   cudaMemcpyAsync(d_series_, args.data(), sizeof(SweepArgs) * n, cudaMemcpyHostToDevice, s);
   // counters: one queue per shape group, then done[n], need[n]
   std::vector<int> ctr(kShapes + 2 * n, 0);
-  for (int i = 0; i < n; i++) ctr[kShapes + n + i] = need_[i];
+  // MBIR_TEST_UNMET_BATCH_WAIT=1 (failure-detection tests only): every series needs one more
+  // colour-0 slice than it has, so each colour-1 slice's bounded wait runs out
+  const char* unmet_env = std::getenv("MBIR_TEST_UNMET_BATCH_WAIT");
+  const bool unmet = unmet_env != nullptr && unmet_env[0] == '1';
+  for (int i = 0; i < n; i++) ctr[kShapes + n + i] = need_[i] + (unmet ? 1 : 0);
   cudaMemcpyAsync(d_ctr_, ctr.data(), sizeof(int) * ctr.size(), cudaMemcpyHostToDevice, s);
   cudaEventRecord(static_cast<cudaEvent_t>(ev0_), s);
   for (int g = 0; g < kShapes; g++) {
@@ -178,6 +183,7 @@ int Batch::sweep(const std::vector<std::pair<int, int>>& iters, double* stats) {
     b.queue = d_ctr_ + g;
     b.done = d_ctr_ + kShapes;
     b.need = d_ctr_ + kShapes + n;
+    b.wait_ns = wait_ns_;
     rc = launch_batch_sweep(b, nb, g, threads_, smem, grid_, s);
     if (rc) return fail(MBIR_EDEVICE, std::string("batch sweep launch: ") +
                                           cudaGetErrorString(cudaGetLastError()));

@@ -58,6 +58,13 @@ class Batch {
   void set_grid(int g) { grid_ = g; }
   // threads per CTA of the persistent sweep: 512 (one CTA per SM) or 256 (two per SM; a slice is
   // staged in shared memory only when two CTAs' worth fits)
+  // limit of the device-side wait of a colour-1 slice for its series' colour-0 slices; a wait
+  // that runs out skips the slice and the sweep returns MBIR_ETIMEOUT
+  int set_wait_limit(double seconds) {
+    if (!(seconds > 0) || seconds > 600) return MBIR_EINVAL;
+    wait_ns_ = static_cast<unsigned long long>(seconds * 1e9);
+    return MBIR_OK;
+  }
   int set_threads(int t) {
     if (t != 256 && t != 512) return MBIR_EINVAL;
     threads_ = t;
@@ -86,6 +93,7 @@ class Batch {
   void* ev1_ = nullptr;
   int grid_ = 0;
   int threads_ = 512;
+  unsigned long long wait_ns_ = 10000000000ull;  // colour-1 wait limit (10 s)
   // launch groups: voxel-group shape (4) x modality (HAADF, bright field), one launch each
   static constexpr int kShapes = 8;
   int group_off_[kShapes] = {0};

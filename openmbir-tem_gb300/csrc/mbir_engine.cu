@@ -92,8 +92,6 @@ Engine::Engine(const mbir_params& p) : p_(p) {
   bf_ = p_.modality == MBIR_MODALITY_BF;
   rb_ = fp64_ ? sizeof(double) : sizeof(float);
   bins_ = p_.detector_response_bins > 0 ? p_.detector_response_bins : 64;
-  const char* pl = std::getenv("MBIR_PIPELINED_SCHED");
-  pipelined_ = !(pl != nullptr && pl[0] == '0');
 }
 
 Engine::~Engine() { release(); }
@@ -678,11 +676,13 @@ int Engine::check_device_error() {
   if (cudaMemcpyAsync(&h, d_err_, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return cuda_check(MBIR_EDEVICE, "device error check");
+  if (h == 0) return 0;
+  // reported once: the work a timed-out wait guarded was skipped, the state stays consistent
+  cudaMemsetAsync(d_err_, 0, sizeof(int), s);
   if (h & 4)
     return fail(MBIR_ENOTSUP,
                 "call schedule: the call needs more than 512 colours (use call_schedule 2)");
-  if (h) return fail(MBIR_ETIMEOUT, "a bounded device wait timed out");
-  return 0;
+  return fail(MBIR_ETIMEOUT, "a bounded device wait timed out");
 }
 
 int Engine::build_host() {
@@ -1337,7 +1337,6 @@ int Engine::status(mbir_status* st) const {
   st->sched_ms_total = sched_ms_;
   st->kernel_ms_total = kernel_ms_;
   st->colour_ms_total = colour_ms_;
-  st->pipelined_launches = pipelined_launches_;
   return MBIR_OK;
 }
 

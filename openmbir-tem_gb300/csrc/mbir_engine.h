@@ -116,10 +116,7 @@ class Engine {
   // y-slab sharding (mbir_shard.cu): sweeps and per-view sums restricted to slices [y0, y1)
   int set_slab(int y0, int y1);
   int slab_rows_owned();
-  // scheduled BF calls run the pipelined kernel (mbir_sweep_f32_sched.cu) where it applies;
-  // MBIR_PIPELINED_SCHED=0 in the environment keeps the plain scheduled sweep
-  bool pipelined_ = true;
-  int64_t pipelined_launches_ = 0;
+
   int sweep_colour(int colour, int outer, int inner, double* stats4);
   int get_planes(int y, int n, float* out);
   int set_planes(int y, int n, const float* in);

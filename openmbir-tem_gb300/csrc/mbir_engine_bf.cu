@@ -263,7 +263,6 @@ int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
     a.sched_count = out_count;
     a.n_levels = 0;
     a.acol = d_acol_;
-    a.sched_capped = 1;  // classes capped at the voxel groups
     if (!build) return MBIR_OK;
     ColourArgs ca{};
     ca.n_z = g.n_z;
@@ -318,7 +317,6 @@ int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
   int levels = -2;
   if (p_.call_schedule == 0)
     levels = colour_schedule(in, kMaxColours, groups, sched_work_, sched_lines_, sched_lofs_);
-  a.sched_capped = levels >= 0 ? 1 : 0;
   if (levels == -2) levels = level_schedule(in, sched_work_, sched_lines_, sched_lofs_);
   if (levels < 0) return fail(MBIR_EINVAL, "call schedule: invalid row order");
   call_lines_ = sched_lines_;
@@ -548,15 +546,7 @@ int Engine::bf_call(int outer, int inner, double* st4) {
       a.stats = d_stats_ + (colour ? static_cast<size_t>(n0) * kStatSlots : 0);
       if (a.n_slices <= 0) continue;
       const size_t smem = a.sched_lines != nullptr ? smem_sched_bytes_ : smem_bytes_;
-      // scheduled calls with one detector row per slice, staged slices and classes no larger
-      // than the voxel groups run the pipelined kernel (same results, loads ahead)
-      rc = -7;
-      if (pipelined_ && a.sched_lines != nullptr && a.sched_capped && stage_ && t_rows_ == 1 &&
-          shape_ == 1)
-        rc = launch_sweep_sched(a, nb_, s);
-      if (rc == 0) pipelined_launches_++;
-      if (rc == -7) rc = launch_sweep(a, nb_, smem, s);
-      if (rc) return cuda_check(rc, "BF call launch");
+      if ((rc = launch_sweep(a, nb_, smem, s))) return cuda_check(rc, "BF call launch");
     }
     cudaEventRecord(static_cast<cudaEvent_t>(ev3_), s);
     kernel_timed_ = true;

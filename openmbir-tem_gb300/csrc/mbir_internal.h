@@ -113,7 +113,6 @@ struct SweepArgs {
   const int* sched_count;  // device [2] (lines, levels) written by the colour kernel, or nullptr
                            // (then n_levels holds the level count)
   const float4* acol;      // [n_z*n_x][n_theta][acol_width(NB)] A-column table (FP32)
-  int sched_capped;        // 1: no level holds more lines than the kernel has voxel groups
 };
 
 // A-column table entry of one voxel line at one view: the first bin (int bits) and the NB
@@ -182,6 +181,7 @@ struct BatchArgs {
   int* queue;                // item counter (zeroed before the launch)
   int* done;                 // [n_series] finished colour-0 slices (zeroed before the launch)
   const int* need;           // [n_series] number of colour-0 slices
+  unsigned long long wait_ns;  // limit of a colour-1 slice's wait for its colour-0 slices
 };
 
 struct RefOrderArgs {
@@ -263,10 +263,6 @@ int launch_exact_view_sums(const ExactArgs& a, int kind, const double* y, const 
 
 // launchers (mbir_kernels.cu); fp64 selects Real = double for the void* arrays
 int launch_sweep(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
-// A scheduled FP32 bright-field call with the next classes' loads in flight
-// (mbir_sweep_f32_sched.cu); -7 when the configuration needs the plain sweep kernel.
-int launch_sweep_sched(const SweepArgs& a, int nb, void* stream);
-size_t sched_sweep_smem(int n_theta, int n_lines, int n_rs, int n_sp);
 int launch_ref_order(const RefOrderArgs& a, int nb, void* stream);
 // sched: the layout of a scheduled bright-field call (smaller: no response table or row lists)
 size_t sweep_smem_bytes(int n_theta, int n_x, int n_rs, int t_rows, int bins, int fp64,

@@ -1238,7 +1238,7 @@ __global__ void __launch_bounds__(kWarps * 32, 1) batch_sweep_kernel(BatchArgs B
           int done;
           asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(done) : "l"(B.done + s) : "memory");
           if (done >= B.need[s]) break;
-          if (global_ns() - t0 > kWaitNs * 5) {
+          if (global_ns() - t0 > B.wait_ns) {
             ok = 0;
             atomicOr(B.series[s].err, 2);
             break;

@@ -99,7 +99,6 @@ class MbirStatus(C.Structure):
         ("stride", C.c_int32), ("staged", C.c_int32), ("lane_shape", C.c_int32),
         ("sched_levels", C.c_int32), ("sched_ms_total", C.c_double),
         ("kernel_ms_total", C.c_double), ("colour_ms_total", C.c_double),
-        ("pipelined_launches", C.c_int64),
     ]
 
 
@@ -162,12 +161,15 @@ SIGNATURES = {
     "mbir_status_get": (C.c_int32, [C.c_void_p, C.POINTER(MbirStatus)]),
     "mbir_cancel": (None, [C.c_void_p]),
     "mbir_write_outputs": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_char_p]),
+    "mbir_write_outputs_ex": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p,
+                                          C.c_char_p]),
     "mbir_batch_create": (C.c_void_p, [C.c_int32]),
     "mbir_batch_destroy": (None, [C.c_void_p]),
     "mbir_batch_add": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "mbir_batch_remove": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "mbir_batch_size": (C.c_int32, [C.c_void_p]),
     "mbir_batch_set_threads": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "mbir_batch_set_wait_limit": (C.c_int32, [C.c_void_p, C.c_double]),
     "mbir_batch_sweep": (C.c_int32, [C.c_void_p, C.c_int32, _D]),
     "mbir_batch_run": (C.c_int32, [C.c_void_p, C.c_int32, C.c_double, _I, _D]),
     "mbir_batch_last_ms": (C.c_double, [C.c_void_p]),
@@ -560,6 +562,10 @@ class Batch:
     def set_threads(self, threads):
         """CTA size of the persistent batched sweep: 512 or 256 (two slices per SM)."""
         self._check(lib().mbir_batch_set_threads(self._h, int(threads)))
+
+    def set_wait_limit(self, seconds):
+        """Limit of the device-side wait of a colour-1 slice (mbir_batch_set_wait_limit)."""
+        self._check(lib().mbir_batch_set_wait_limit(self._h, float(seconds)))
 
 
 class Server:

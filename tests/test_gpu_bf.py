@@ -232,32 +232,3 @@ def test_bf_device_colour_schedule_short_calls(lib_built, n_r):
         np.testing.assert_array_equal(lofs, ho)
     assert 31 < min(sizes) and max(sizes) < 3 * 31, sizes
 
-
-def test_bf_pipelined_schedule_kernel_bitwise(lib_built, oracle_mod, monkeypatch):
-    """Scheduled NHICD calls run by the pipelined kernel (the next classes' A-column, weights,
-    neighbours and values in flight; same-slice neighbours patched from the class before) give
-    the plain scheduled kernel's bits: a run with the Bragg schedule (T = 3 after the first
-    inner calls), offset and variance updates, homogeneous and non-homogeneous lists."""
-    mbir = lib_built
-    y, ang, th = bf_case()
-    out = []
-    for env in ("1", "0"):
-        monkeypatch.setenv("MBIR_PIPELINED_SCHED", env)
-        p = bf_params(mbir, th, outer_iterations=5, inner_iterations=4, call_schedule=0, seed=11)
-        e = mbir.Engine(p)
-        e.set_sinogram(y, ang)
-        e.run()
-        st = e.status()
-        sel, w, mag, _, _ = e.bf_state()
-        out.append((e.volume(), e.error_sinogram(), sel, mag, e.nuisance(), st))
-        e.close()
-    (v0, e0, s0, m0, n0, st0), (v1, e1, s1, m1, n1, st1) = out
-    assert st0.pipelined_launches > 0 and st1.pipelined_launches == 0
-    assert st0.sweeps_done == st1.sweeps_done
-    assert st0.voxels_updated == st1.voxels_updated
-    assert st0.voxels_visited == st1.voxels_visited
-    assert np.array_equal(v0, v1), rel(v0, v1)
-    assert np.array_equal(e0, e1), rel(e0, e1)
-    assert np.array_equal(s0, s1) and np.array_equal(m0, m1)
-    for a, b in zip(n0, n1):
-        np.testing.assert_array_equal(a, b)
