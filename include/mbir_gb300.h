@@ -338,6 +338,19 @@ int32_t mbir_server_release(mbir_server* s, int64_t id);
 int32_t mbir_server_get_stats(mbir_server* s, mbir_server_stats* st);
 const char* mbir_server_last_error(const mbir_server* s);
 
+/* Estimate of sigma_x from an MRC tilt series (host only), as SigmaXEstimation::execute
+ * (GenericFilters/SigmaXEstimation.cpp:137-234) computes it for the reference's GUIs: per view the
+ * mean absolute deviation of the counts in the region x_range x y_range (bright field, with
+ * use_bf_offset: of log(counts + bf_offset)), divided by target_gain, times cos(tilt) /
+ * sample_thickness, summed over the tilts and divided by the view count.  The region follows the
+ * reference's reader (columns x_range[0]..x_range[1] and rows y_range[0]..y_range[1] read
+ * inclusively, the first (x1-x0)(y1-y0) values used); a NULL range or negative bounds mean
+ * 0..nx (0..ny).  tilts_deg: n_tilts angles, or n_tilts = 0 for the FEI header's a-tilts. */
+int32_t mbir_estimate_sigma_x(const char* mrc_path, double sample_thickness, double target_gain,
+                              int32_t use_bf_offset, double bf_offset, const float* tilts_deg,
+                              int32_t n_tilts, const int32_t* x_range, const int32_t* y_range,
+                              double* sigma_x);
+
 /* Library version string */
 const char* mbir_version(void);
 

@@ -290,6 +290,28 @@ void mbir_cancel(mbir_engine* e) {
 int32_t mbir_write_outputs(mbir_engine* e, const char* dir, const char* mrc_path) {
   return guarded(e, [&](mbir::Engine& m) { return m.write_outputs(dir, mrc_path); });
 }
+int32_t mbir_estimate_sigma_x(const char* mrc_path, double sample_thickness, double target_gain,
+                              int32_t use_bf_offset, double bf_offset, const float* tilts_deg,
+                              int32_t n_tilts, const int32_t* x_range, const int32_t* y_range,
+                              double* sigma_x) {
+  if (!mrc_path || !sigma_x || (n_tilts > 0 && !tilts_deg) || n_tilts < 0) return MBIR_EINVAL;
+  try {
+    std::vector<float> tilts(tilts_deg, tilts_deg + n_tilts);
+    if (n_tilts == 0) {  // the a-tilts of the FEI extended header
+      mbir::MrcVolume hdr;
+      std::string err;
+      if (mbir::mrc_read(mrc_path, nullptr, nullptr, hdr, true, err)) return MBIR_EIO;
+      tilts = hdr.a_tilt;
+    }
+    std::string err;
+    return mbir::estimate_sigma_x(mrc_path, sample_thickness, target_gain, use_bf_offset != 0,
+                                  bf_offset, tilts.data(), static_cast<int>(tilts.size()),
+                                  x_range, y_range, sigma_x, err);
+  } catch (...) {
+    return MBIR_ENOMEM;
+  }
+}
+
 int32_t mbir_write_outputs_ex(mbir_engine* e, const char* dir, const char* mrc_path,
                               const char* vtk_path, const char* avizo_path) {
   return guarded(

@@ -394,6 +394,9 @@ int mrc_read(const std::string& path, const int* vmin, const int* vmax, MrcVolum
              bool header_only, std::string& err);
 int mrc_write_volume(const std::string& path, const float* zxy, int n_z, int n_x, int n_y,
                      int x_start, int x_end, double length_x, std::string& err);
+int estimate_sigma_x(const std::string& path, double thickness, double target_gain,
+                     bool use_bf_offset, double bf_offset, const float* tilts, int n_tilts,
+                     const int* xd, const int* yd, double* out, std::string& err);
 int vtk_write_volume(const std::string& path, const float* zxy, int n_z, int n_x, int n_y,
                      int x_start, int x_end, std::string& err);
 int avizo_write_volume(const std::string& path, const float* zxy, int n_z, int n_x, int n_y,

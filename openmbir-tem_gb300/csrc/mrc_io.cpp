@@ -2,6 +2,8 @@
 // reference's MRCReader / MRCWriter (Code/MBIRLib/IOFilters/MRCReader.cpp:99-368,
 // MRCWriter.cpp:90-290; header layout MRCHeader.h:46-212).  Fields are read and written at
 // their fixed byte offsets, little-endian, so no struct packing is assumed.
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -26,6 +28,11 @@ int32_t rd_i32(const unsigned char* b, int off) {
 float rd_f32(const unsigned char* b, int off) {
   float v;
   std::memcpy(&v, b + off, 4);
+  return v;
+}
+uint16_t rd_u16(const unsigned char* b) {
+  uint16_t v;
+  std::memcpy(&v, b, 2);
   return v;
 }
 void wr_i32(unsigned char* b, int off, int32_t v) { std::memcpy(b + off, &v, 4); }
@@ -227,6 +234,123 @@ int mrc_write_volume(const std::string& path, const float* zxy, int n_z, int n_x
   std::fwrite(&dmax, 4, 1, f);
   std::fwrite(&mean, 4, 1, f);
   std::fclose(f);
+  return MBIR_OK;
+}
+
+// SigmaXEstimation::execute (GenericFilters/SigmaXEstimation.cpp:137-234): per view, the mean
+// absolute deviation of the counts in a detector region (bright field: of log(counts +
+// bf_offset), values <= 0 skipped in the sums but counted), divided by the target gain, times
+// cos(tilt) / thickness, summed over the tilts and divided by the view count.  The region is read
+// as the reference reads it, one reader per view (MRCReader.cpp:205-368): rows y0..y1 and columns
+// x0..x1 inclusive, each run taken from the file at nx*ny*z + nx*y + x0 into one buffer of
+// (x1-x0+1)(y1-y0+1) values, and the first (x1-x0)(y1-y0) values of the buffer used.  A run that
+// starts at or past the end of the file reads nothing, one that crosses it keeps the bytes before
+// it; either way that view's reading stops there and the estimate goes on with the next view
+// (MRCReader::read returns success whatever its partial reads did).  The reference leaves the
+// unread tail of its malloc'd buffer uninitialised; here it is zero.  That tail reaches the used
+// values only when a default region (x1 = nx, y1 = ny) meets ny > nx + 1 on the last view.
+// Unset bounds (< 0) are 0 and nx (ny).
+int estimate_sigma_x(const std::string& path, double thickness, double target_gain,
+                     bool use_bf_offset, double bf_offset, const float* tilts, int n_tilts,
+                     const int* xd, const int* yd, double* out, std::string& err) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) {
+    err = "cannot open MRC file '" + path + "'";
+    return MBIR_EIO;
+  }
+  unsigned char h[kHeaderBytes];
+  if (std::fread(h, 1, kHeaderBytes, f) != kHeaderBytes) {
+    std::fclose(f);
+    err = "MRC header truncated";
+    return MBIR_EIO;
+  }
+  const int nx = rd_i32(h, 0), ny = rd_i32(h, 4), nz = rd_i32(h, 8), mode = rd_i32(h, 12);
+  const int32_t next = rd_i32(h, 92);
+  size_t ts = 0;
+  switch (mode) {
+    case 0: ts = 1; break;
+    case 1: ts = 2; break;
+    case 2: ts = 4; break;
+    case 6: ts = 2; break;
+    default: ts = 0;
+  }
+  if (nx <= 0 || ny <= 0 || nz <= 0 || next < 0 || ts == 0) {
+    std::fclose(f);
+    err = "MRC header: invalid dimensions or unsupported mode";
+    return MBIR_EINVAL;
+  }
+  std::fseek(f, 0, SEEK_END);
+  const long long file_bytes = std::ftell(f);
+  const long long data_start = kHeaderBytes + static_cast<long long>(next);
+  int x0 = xd ? xd[0] : -1, x1 = xd ? xd[1] : -1, y0 = yd ? yd[0] : -1, y1 = yd ? yd[1] : -1;
+  if (x0 < 0) x0 = 0;
+  if (x1 < 0) x1 = nx;
+  if (y0 < 0) y0 = 0;
+  if (y1 < 0) y1 = ny;
+  const int32_t count = (x1 - x0) * (y1 - y0);
+  const long long run = x1 - x0 + 1, rows = y1 - y0 + 1;
+  std::vector<double> sum2s(static_cast<size_t>(nz), 0.0);
+  const size_t n_values = (run > 0 && rows > 0) ? static_cast<size_t>(run * rows) : 0;
+  std::vector<unsigned char> raw(n_values * ts);
+  std::vector<double> buf(n_values);
+  for (int z = 0; z < nz; ++z) {
+    std::fill(raw.begin(), raw.end(), 0);
+    size_t at = 0;  // bytes of the buffer filled so far
+    for (int y = y0; y <= y1 && run > 0; ++y) {
+      const long long off = data_start + (static_cast<long long>(nx) * ny * z +
+                                          static_cast<long long>(nx) * y + x0) *
+                                             static_cast<long long>(ts);
+      const long long want = run * static_cast<long long>(ts);
+      if (off < data_start || off >= file_bytes) break;  // peek() at the end of the file
+      const long long got = std::min(want, file_bytes - off);
+      std::fseek(f, static_cast<long>(off), SEEK_SET);
+      if (std::fread(raw.data() + at, 1, static_cast<size_t>(got), f) !=
+          static_cast<size_t>(got)) {
+        std::fclose(f);
+        err = "MRC read failed";
+        return MBIR_EIO;
+      }
+      at += static_cast<size_t>(want);
+      if (got != want) break;  // gcount() short of the run: the partial read stops the view
+    }
+    for (size_t i = 0; i < n_values; ++i) {
+      const unsigned char* q = raw.data() + i * ts;
+      double v = 0;
+      if (mode == 0) v = q[0];
+      if (mode == 1) v = static_cast<int16_t>(rd_u16(q));
+      if (mode == 2) v = rd_f32(q, 0);
+      if (mode == 6) v = rd_u16(q);
+      buf[i] = v;
+    }
+    if (count <= 0 || static_cast<size_t>(count) > buf.size()) continue;
+    double dev = 0, mean = 0;
+    if (use_bf_offset) {  // calcBFAvgDeviation (:84-105)
+      for (int32_t i = 0; i < count; i++) {
+        const double t = buf[i] + bf_offset;
+        if (t > 0) mean += std::log(t);
+      }
+      mean /= count;
+      for (int32_t i = 0; i < count; i++) {
+        const double t = buf[i] + bf_offset;
+        if (t > 0) dev += std::fabs(std::log(t) - mean);
+      }
+    } else {  // calcAvgDeviation (:66-80)
+      for (int32_t i = 0; i < count; i++) mean += buf[i];
+      mean /= count;
+      for (int32_t i = 0; i < count; i++) dev += std::fabs(buf[i] - mean);
+    }
+    dev /= count;
+    sum2s[z] = dev;
+  }
+  std::fclose(f);
+  double sum1 = 0.0;
+  const float deg_to_rad = 0.017453292519943f;
+  for (int i = 0; i < n_tilts && i < nz; ++i) {
+    sum2s[i] /= target_gain;
+    const double cosine = std::cos(tilts[i] * deg_to_rad);  // float cosine, as the reference
+    sum1 += (sum2s[i] * cosine) / (thickness);
+  }
+  *out = sum1 / nz;
   return MBIR_OK;
 }
 

@@ -161,6 +161,8 @@ SIGNATURES = {
     "mbir_status_get": (C.c_int32, [C.c_void_p, C.POINTER(MbirStatus)]),
     "mbir_cancel": (None, [C.c_void_p]),
     "mbir_write_outputs": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_char_p]),
+    "mbir_estimate_sigma_x": (C.c_int32, [C.c_char_p, C.c_double, C.c_double, C.c_int32,
+                                          C.c_double, _F, C.c_int32, _I, _I, _D]),
     "mbir_write_outputs_ex": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p,
                                           C.c_char_p]),
     "mbir_batch_create": (C.c_void_p, [C.c_int32]),
@@ -651,3 +653,23 @@ def run_multires(params, counts, tilts_deg, delta_r=1.0, delta_t=1.0):
     if rc != MBIR_OK:
         raise MbirError(rc, "multires")
     return out
+
+
+def estimate_sigma_x(mrc_path, sample_thickness, target_gain=1.0, bf_offset=None, tilts=None,
+                     x_range=None, y_range=None):
+    """sigma_x estimate of an MRC tilt series (mbir_estimate_sigma_x); bf_offset not None uses
+    the bright-field log form."""
+    t = None if tilts is None else np.ascontiguousarray(tilts, np.float32)
+    xr = None if x_range is None else np.ascontiguousarray(x_range, np.int32)
+    yr = None if y_range is None else np.ascontiguousarray(y_range, np.int32)
+    out = C.c_double()
+    rc = lib().mbir_estimate_sigma_x(str(mrc_path).encode(), float(sample_thickness),
+                                     float(target_gain), 0 if bf_offset is None else 1,
+                                     0.0 if bf_offset is None else float(bf_offset),
+                                     None if t is None else _fp(t), 0 if t is None else len(t),
+                                     None if xr is None else xr.ctypes.data_as(_I),
+                                     None if yr is None else yr.ctypes.data_as(_I),
+                                     C.byref(out))
+    if rc != MBIR_OK:
+        raise MbirError(rc, "mbir_estimate_sigma_x failed")
+    return out.value

@@ -12,7 +12,9 @@ Only two things stand in for the reference's build system and its external libra
 * oracle/ref_shim/ref_runtime.cpp -- a fixed-seed switch for the reference's clock seeds and a
   zeroing operator new (the engines leave some parameter fields unset).
 
-The objects and the two programs go to oracle/_ref/ (git-ignored).  They are the parity pin of
+A third program, SigmaXEstimate (oracle/ref_shim/ref_sigmax_main.cpp, a main of this recipe),
+drives the reference's SigmaXEstimation filter the way its GUIs do.  The objects and the
+programs go to oracle/_ref/ (git-ignored).  They are the parity pin of
 the CPU restatement oracle/mbir_oracle.c: tests/test_oracle_vs_ref.py runs both on the same
 inputs and compares their outputs, and tests/golden/make_golden.py stores small outputs of the
 programs as fixtures so that the pin also holds where the reference tree is absent.
@@ -91,6 +93,8 @@ PROGRAMS = {
     "HAADFReconstruction": ["main.cpp", "HAADFReconstructionArgsParser.cpp"],
     "BFReconstruction": ["main.cpp", "BFReconstructionArgsParser.cpp"],
 }
+# harnesses of this recipe (oracle/ref_shim) over reference classes the programs do not reach
+HARNESSES = {"SigmaXEstimate": "ref_sigmax_main.cpp"}
 
 # -O2 as the reference's release build; no FMA contraction so that its FP64 arithmetic rounds
 # operation by operation (as the oracle's does) on hosts whose default ISA has FMA.
@@ -122,8 +126,7 @@ def build(reference=DEFAULT_REFERENCE, jobs=None, quiet=False):
             print(f"build_ref: reference tree not found under {reference}", file=sys.stderr)
         return False
     os.makedirs(os.path.join(OUT, "obj"), exist_ok=True)
-    includes = [SHIM, code, os.path.join(code, "MBIRLib"), os.path.join(code, "MXA"),
-                os.path.join(code, "tclap") if False else code]
+    includes = [SHIM, code, os.path.join(code, "MBIRLib"), os.path.join(code, "MXA")]
     units = []
     for rel in MBIRLIB_SOURCES:
         extra = []
@@ -133,6 +136,8 @@ def build(reference=DEFAULT_REFERENCE, jobs=None, quiet=False):
     for rel in MXA_SOURCES:
         units.append((os.path.join(code, "MXA", rel), "MXA__" + _obj_name(rel), []))
     units.append((os.path.join(SHIM, "ref_runtime.cpp"), "shim__ref_runtime.o", []))
+    for prog, src in HARNESSES.items():
+        units.append((os.path.join(SHIM, src), prog + "__" + _obj_name(src), []))
     for prog, files in PROGRAMS.items():
         for f in files:
             rel = os.path.join("Applications", prog, f)
@@ -153,7 +158,7 @@ def build(reference=DEFAULT_REFERENCE, jobs=None, quiet=False):
         print("build_ref: compile errors\n" + "\n".join(errors), file=sys.stderr)
         return False
     lib_objs = [o for n, o in objs.items() if n.startswith(("MBIRLib__", "MXA__", "shim__"))]
-    for prog in PROGRAMS:
+    for prog in list(PROGRAMS) + list(HARNESSES):
         exe = os.path.join(OUT, prog)
         pobjs = [o for n, o in objs.items() if n.startswith(prog + "__")]
         newest = max(os.path.getmtime(o) for o in lib_objs + pobjs)
@@ -165,7 +170,7 @@ def build(reference=DEFAULT_REFERENCE, jobs=None, quiet=False):
             print(f"build_ref: link of {prog} failed\n{r.stderr[-4000:]}", file=sys.stderr)
             return False
     if not quiet:
-        print(f"build_ref: {', '.join(PROGRAMS)} in {OUT}")
+        print(f"build_ref: {', '.join(list(PROGRAMS) + list(HARNESSES))} in {OUT}")
     return True
 
 
