@@ -203,8 +203,15 @@ int Batch::sweep(const std::vector<std::pair<int, int>>& iters, double* stats) {
   last_ms_ = ms;
   total_ms_ += ms;
   sweeps_++;
+  // every engine's error word is read (and cleared) before the first failure is reported, so
+  // that no stale word fails the next sweep
+  int first_bad = -1, first_rc = MBIR_OK;
   for (int i = 0; i < n; i++)
-    if ((rc = eng_[i]->check_errors())) return fail(rc, eng_[i]->last_error());
+    if ((rc = eng_[i]->check_errors()) && first_bad < 0) {
+      first_bad = i;
+      first_rc = rc;
+    }
+  if (first_bad >= 0) return fail(first_rc, eng_[first_bad]->last_error());
   const std::vector<int> fin = parallel_for(n, device_, [&](int i) {
     const int outer = iters.empty() ? 0 : iters[i].first;
     const int inner = iters.empty() ? 0 : iters[i].second;

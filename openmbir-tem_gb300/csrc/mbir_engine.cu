@@ -146,6 +146,8 @@ void Engine::release() {
   dfree(d_colour_);
   dfree(d_bin_used_);
   dfree(d_line_used_);
+  dfree(d_cfsets_);
+  dfree(d_cflags_);
   dfree(d_sched_count_);
   dfree(d_hc_lines_);
   dfree(d_hc_lofs_);
@@ -1506,7 +1508,11 @@ int Engine::autotune_shape() {
   int best = shape_;
   float best_ms = 0;
   int rc = MBIR_OK;
-  for (int sh : cands) {
+  // two rounds over the candidates, the best time of each kept: the first launch of a kernel
+  // instantiation also loads its module, which must not count against the shape tried first
+  std::vector<int> trials;
+  for (int rep = 0; rep < 2; rep++) trials.insert(trials.end(), cands.begin(), cands.end());
+  for (int sh : trials) {
     a.shape = sh;
     cudaEventRecord(static_cast<cudaEvent_t>(ev0_), s);
     for (int colour = 0; colour < 2 && rc == MBIR_OK; colour++) {

@@ -313,6 +313,8 @@ class Engine {
   int16_t* d_colour_ = nullptr;             // [n_z*n_x] scratch
   unsigned long long* d_bin_used_ = nullptr;   // [n_theta][n_r][kColourWords]
   unsigned long long* d_line_used_ = nullptr;  // [n_z*n_x][kColourWords]
+  unsigned long long* d_cfsets_ = nullptr;  // [ceil(n_z*n_x/31)*31][kColourWords] (multi-CTA)
+  int* d_cflags_ = nullptr;                 // [3*ceil(n_z*n_x/31) + 1] (multi-CTA)
   int32_t* d_sched_count_ = nullptr;        // [2] lines, colours
   bool sched_on_device_ = false;            // the last call's schedule was built on the device
   bool readback_pending_ = false;

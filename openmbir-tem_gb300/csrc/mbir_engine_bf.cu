@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 
@@ -183,7 +184,7 @@ int Engine::bf_prepare_schedule() {
   const size_t n_entries = nl * g.n_theta;
   if (cudaMalloc(&d_packed_, n_entries * sizeof(int32_t)) != cudaSuccess ||
       cudaMalloc(&d_vis_, nl * sizeof(int32_t)) != cudaSuccess ||
-      cudaMalloc(&d_conf_, 3 * nl * sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(&d_conf_, 5 * nl * sizeof(unsigned)) != cudaSuccess ||
       cudaMalloc(&d_colour_, nl * sizeof(int16_t)) != cudaSuccess ||
       cudaMalloc(&d_bin_used_, static_cast<size_t>(g.n_theta) * g.n_r * kColourWords * 8) !=
           cudaSuccess ||
@@ -204,6 +205,14 @@ int Engine::bf_prepare_schedule() {
     dfree_any(d_hc_lofs_);
     dfree_any(d_hc_count_);
     return host_footprint_bins();  // host colouring instead
+  }
+  // scratch of the multi-CTA colouring (without it the one-CTA form runs)
+  const size_t nblk = (nl + 30) / 31;
+  if (cudaMalloc(&d_cfsets_, nblk * 31 * kColourWords * 8) != cudaSuccess ||
+      cudaMalloc(&d_cflags_, (3 * nblk + 1) * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    dfree_any(d_cfsets_);
+    dfree_any(d_cflags_);
   }
   hc_valid_.assign(kNumHomogeneous, 0);
   hc_start_.assign(kNumHomogeneous, 0);
@@ -288,6 +297,8 @@ int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
     ca.conf = d_conf_;
     ca.conf_p1 = d_conf_ + static_cast<size_t>(g.n_z) * g.n_x;
     ca.conf_p2 = d_conf_ + 2 * static_cast<size_t>(g.n_z) * g.n_x;
+    ca.conf_p3 = d_conf_ + 3 * static_cast<size_t>(g.n_z) * g.n_x;
+    ca.conf_p4 = d_conf_ + 4 * static_cast<size_t>(g.n_z) * g.n_x;
     ca.colour = d_colour_;
     ca.bin_used = d_bin_used_;
     ca.line_used = d_line_used_;
@@ -295,6 +306,21 @@ int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
     ca.lofs = out_lofs;
     ca.count = out_count;
     ca.err = d_err_;
+    // MBIR_COLOUR_SEQUENTIAL=1: every block of the colouring line by line (same schedule; for
+    // checking the parallel form)
+    const char* seq = std::getenv("MBIR_COLOUR_SEQUENTIAL");
+    ca.sequential = (seq != nullptr && seq[0] == '1') ? 1 : 0;
+    if (d_cfsets_ != nullptr && d_cflags_ != nullptr) {
+      // MBIR_COLOUR_HELPERS: helper CTAs of the multi-CTA colouring (default 8, 0: one CTA)
+      const char* hv = std::getenv("MBIR_COLOUR_HELPERS");
+      const int helpers = hv ? std::max(0, std::min(64, std::atoi(hv))) : 8;
+      const size_t nblk = (static_cast<size_t>(g.n_z) * g.n_x + 30) / 31;
+      ca.fsets = d_cfsets_;
+      ca.flags = d_cflags_;
+      ca.abort_flag = d_cflags_ + 3 * nblk;
+      ca.wait_ns = 2000000000ull;
+      ca.helpers = helpers;
+    }
     cudaEventRecord(static_cast<cudaEvent_t>(ev4_), s);
     const int crc = launch_colour_schedule(ca, s);
     cudaEventRecord(static_cast<cudaEvent_t>(ev5_), s);

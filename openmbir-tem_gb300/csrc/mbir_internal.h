@@ -158,13 +158,23 @@ struct ColourArgs {
   unsigned* conf;                 // [n] scratch: conflict words of each block of 32 lines
   unsigned* conf_p1;              // [n] scratch: conflict words against the block before
   unsigned* conf_p2;              // [n] scratch: against the block before that
+  unsigned* conf_p3;              // [n] scratch: against the block before that one
+  unsigned* conf_p4;              // [n] scratch: against the fourth block back
   int16_t* colour;                // [n_z*n_x] scratch: colour of each of the call's lines
   unsigned long long* bin_used;   // [n_theta][n_r][words] scratch, cleared by the launcher
   unsigned long long* line_used;  // [n_z*n_x][words] scratch, cleared by the launcher
   int32_t* lines;                 // [n_z*n_x] out: lines colour by colour
   int32_t* lofs;                  // [max_colours + 1] out: colour offsets
   int32_t* count;                 // [2] out: lines, colours
-  int* err;                       // value 4 is ORed in when max_colours do not suffice
+  int* err;                       // value 4 is ORed in when max_colours do not suffice, 2 when
+                                  // a wait of the multi-CTA form ran out of time
+  // multi-CTA form (used when fsets and flags are set and the device launches cooperatively)
+  unsigned long long* fsets;      // [ceil(n/31)*31][words] scratch: taken-colour sets per line
+  int* flags;                     // [3*ceil(n/31)] scratch: ready, coloured, written per block
+  int* abort_flag;                // [1] scratch
+  unsigned long long wait_ns;     // limit of each wait on a flag
+  int helpers;                    // helper CTAs (0: the one-CTA form)
+  int sequential;                 // 1: every block line by line (the parallel form's check)
 };
 int launch_colour_schedule(const ColourArgs& a, void* stream);
 size_t colour_smem_bytes(int n_theta, int words);

@@ -70,10 +70,15 @@ def test_cli_haadf_reconstruction_files(cli_built, tmp_path):
     y, ang, th = small_case()
     refrun.write_mrc(str(tmp_path / "in.mrc"), y, ang)
     out = tmp_path / "out"
+    # the whole series as the subvolume, as the run that wrote the header fixture had it (without
+    # the flag the reference hands its engine six zeros, a 63 x 3 detector window of one view)
+    n_theta, n_r, n_t = y.shape
+    sv = (0, 0, 0, n_r - 1, n_t - 1, n_theta - 1)
     r = run("HAADFReconstruction", "-s", str(tmp_path / "in.mrc"), "--outputfile",
-            str(out / "recon.mrc"), "--thickness", "16", "--diffuseness", "0.1", "--sigma_x",
-            "0.2", "--num_resolutions", "1", "--outer_iterations", "1", "--inner_iterations",
-            "1", "--stop_threshold", "0", "--target_gain", "1")
+            str(out / "recon.mrc"), "--subvolume", ",".join(str(v) for v in sv), "--thickness",
+            "16", "--diffuseness", "0.1", "--sigma_x", "0.2", "--num_resolutions", "1",
+            "--outer_iterations", "1", "--inner_iterations", "1", "--stop_threshold", "0",
+            "--target_gain", "1")
     assert r.returncode == 0, r.stdout + r.stderr
     with open(os.path.join(HERE, "golden", "output_headers.json")) as f:
         ref = json.load(f)
@@ -103,6 +108,8 @@ def test_cli_haadf_reconstruction_files(cli_built, tmp_path):
     p.target_gain = 1.0
     p.float_params = 1
     p.use_subvolume = 1
+    for i, v in enumerate(sv):
+        p.subvolume[i] = v
     with mbir.Engine(p) as e:
         e.load_mrc(str(tmp_path / "in.mrc"))
         e.run()

@@ -232,3 +232,32 @@ def test_bf_device_colour_schedule_short_calls(lib_built, n_r):
         np.testing.assert_array_equal(lofs, ho)
     assert 31 < min(sizes) and max(sizes) < 3 * 31, sizes
 
+
+@pytest.mark.parametrize("helpers,sequential", [("8", "0"), ("0", "0"), ("8", "1")])
+def test_bf_device_colour_schedule_long_calls(lib_built, monkeypatch, helpers, sequential):
+    """Calls of well over twenty 31-line blocks, so that the helper CTAs of the multi-CTA device
+    colouring run ahead of the colouring CTA and each take several blocks: homogeneous and
+    non-homogeneous calls give the host definition's schedule exactly, with helpers and without,
+    and with the blocks' parallel greedy form and line by line."""
+    mbir = lib_built
+    monkeypatch.setenv("MBIR_COLOUR_HELPERS", helpers)
+    monkeypatch.setenv("MBIR_COLOUR_SEQUENTIAL", sequential)
+    y, ang, th = bf_case(n_r=512, n_t=4, thickness=64.0, n_particles=24)
+    p = bf_params(mbir, th, call_schedule=0, bragg_threshold=5.0e10)
+    with mbir.Engine(p) as e:
+        e.set_sinogram(y, ang)
+        e.prepare()
+        lo, mask, ok = e.footprint_bins()
+        nz, nx = ok.shape
+        sizes = []
+        for k in range(4):
+            e.sweep(0, k)
+            lines, lofs = e.call_schedule()
+            sizes.append(len(lines))
+            act = np.zeros(nz * nx, np.uint8)
+            act[lines] = 1
+            hl, ho = mbir.colour_schedule(ok, lo, mask, 3, y.shape[1], act.reshape(nz, nx),
+                                          class_cap=32)
+            np.testing.assert_array_equal(lines, hl)
+            np.testing.assert_array_equal(lofs, ho)
+    assert min(sizes) > 20 * 31, sizes
