@@ -371,6 +371,96 @@ def batch_measure(mbir, n, seed=1, batch_threads=None, tol=1e-4, max_outer=60):
                         "outer_iterations": int(np.sum(iters))}}
 
 
+PRECISION_WORKLOAD = "precision-1024x512x256-121v"
+
+
+def run_precision(args):
+    """The precision study: the bright-field workload family at 1024 x 512 detector, 121 views
+    over +-60 deg at 1 deg, volume 1024 x 512 x 256 (x, y, z), the particles-on-slab phantom at
+    4x the areal particle density of the 512 x 256 workload.  Seeded synthetic data: the
+    voxelised phantom projected by the engine's own FP32 projector, then Poisson counts at 1e4
+    electrons with +-3% per-view dose drift.  The FP32 engine and the FP64 engine run the same
+    20 NHICD calls (one equivalent iteration) with offset and variance updates from the same
+    start, in the same visit order (the row walk, which the FP32 engine runs as dependency
+    levels); the line reports each result's error of the FP32 run against the FP64 run after
+    the first call (one call from the same state: the arithmetic alone) and after the 20 calls
+    (where the non-homogeneous lines chosen from the update magnitudes can differ as well)."""
+    import torch
+    torch.cuda.set_device(0)
+    import build as pkg_build
+    pkg_build.build()
+    import mbir
+    import synthetic
+    n_r, n_t, th, mx, st = 1024, 512, 128.0, 60.0, 1.0
+    ang = synthetic.tilt_angles(mx, st).astype(np.float32)
+    n_part = 4 * 200 * (n_r * n_t) // (512 * 256)
+    t0 = time.perf_counter()
+    ph = params_for(mbir, th, "HAADF", outer=1)
+    with mbir.Engine(ph) as e:
+        e.set_sinogram(np.ones((len(ang), n_r, n_t), np.float32), ang)
+        nz, nx, ny = e.dims()[:3]
+        vol = synthetic.particles_on_slab_volume(nx, ny, nz, th, n_part, seed=0)
+        e.set_initial_volume(vol)
+        e.prepare()
+        proj = e.projection()
+    del vol
+    counts, _ = synthetic.bf_counts(proj, seed=1)
+    del proj
+    gen_s = time.perf_counter() - t0
+    out = {}
+    for calls in (1, CALLS_PER_EQUIT):
+        for name, prec in (("fp32", mbir.FP32), ("fp64", mbir.FP64)):
+            p = params_for(mbir, th, "BF", outer=calls, inner=1)
+            p.precision = prec
+            # the FP32 calls in the dependency levels of the row walk: the FP64 engine's own
+            # visit order, so that the errors are those of the arithmetic alone
+            p.call_schedule = 2
+            with mbir.Engine(p) as e:
+                e.set_sinogram(counts, ang)
+                t = time.perf_counter()
+                e.run()
+                wall = time.perf_counter() - t
+                s_ = e.status()
+                g, off, var = e.nuisance()
+                out[(calls, name)] = {
+                    "volume": e.volume().astype(np.float64), "cost": e.cost()[0], "offset": off,
+                    "variance": var, "wall_s": wall, "icd_ms": s_.icd_ms_total,
+                    "calls": s_.sweeps_done, "staged": s_.staged,
+                    "updated": int(s_.voxels_updated), "dims": [int(v) for v in e.dims()[:3]]}
+
+    def rel(x, y):
+        return float(np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300))
+
+    def errors(calls):
+        a, b = out[(calls, "fp32")], out[(calls, "fp64")]
+        return {"volume_rel_l2": rel(a["volume"], b["volume"]),
+                "volume_max_abs": float(np.abs(a["volume"] - b["volume"]).max()),
+                "volume_max": float(np.abs(b["volume"]).max()),
+                "cost_rel": abs(a["cost"] - b["cost"]) / abs(b["cost"]),
+                "offset_max_rel": float(np.max(np.abs(a["offset"] - b["offset"]) /
+                                               np.abs(b["offset"]))),
+                "variance_rel": float(np.max(np.abs(a["variance"] - b["variance"]) /
+                                             np.abs(b["variance"]))),
+                "voxels_updated": [a["updated"], b["updated"]]}
+
+    a, b = out[(CALLS_PER_EQUIT, "fp32")], out[(CALLS_PER_EQUIT, "fp64")]
+    line = {"metric": "FP32 vs FP64 error per result", "workload": PRECISION_WORKLOAD,
+            "data": "synthetic (voxelised particles-on-slab phantom, engine projector, Poisson "
+                    "counts)", "n_gpus": 1,
+            "config": {"workload": PRECISION_WORKLOAD, "detector": [n_r, n_t], "views": len(ang),
+                       "volume_zxy": a["dims"], "particles": n_part,
+                       "order": "row walk (FP32 as its dependency levels), both precisions",
+                       "slices_in_smem": bool(a["staged"])},
+            "after_1_call": errors(1),
+            "after_20_calls": errors(CALLS_PER_EQUIT),
+            "fp32": {"wall_s": a["wall_s"], "icd_ms": a["icd_ms"], "calls": a["calls"],
+                     "cost": a["cost"]},
+            "fp64": {"wall_s": b["wall_s"], "icd_ms": b["icd_ms"], "calls": b["calls"],
+                     "cost": b["cost"]},
+            "data_generation_s": gen_s}
+    print(json.dumps(line))
+
+
 def run_batch(args):
     import torch
     import build as pkg_build
@@ -501,7 +591,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
-                    choices=sorted(WORKLOADS) + ["batch-64", "serve-poisson"])
+                    choices=sorted(WORKLOADS) + ["batch-64", "serve-poisson",
+                                                 PRECISION_WORKLOAD])
     ap.add_argument("--series", type=int, default=64, help="batch/serve: number of requests")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: mean arrivals per second")
     ap.add_argument("--no-batch", action="store_true",
@@ -530,6 +621,9 @@ def main():
         return
     if args.workload == "serve-poisson":
         run_serve(args)
+        return
+    if args.workload == PRECISION_WORKLOAD:
+        run_precision(args)
         return
 
     import torch

@@ -150,7 +150,7 @@ __device__ __forceinline__ void load_planes(const ColourArgs& A, int W, int uw, 
   const int lane = threadIdx.x & 31;
   const int nt = A.n_theta, nx = A.n_x, nb = A.nb;
   const int z = l / nx, x = l - z * nx;
-  const int np = uw <= 2 ? 1 : uw <= 4 ? 2 : 4;  // word pairs read (W is 2, 4 or 8)
+  const int np = uw <= 2 ? 1 : uw <= 4 ? 2 : uw <= 8 ? 4 : 8;  // word pairs read (W 2..16)
   const int gs = 32 / np;                        // lanes per word pair
   const int kk = lane / gs, sub = lane - kk * gs;
   const int dv = gs / nb, db = gs - dv * nb;
@@ -370,12 +370,12 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
   __shared__ int choice[32];                  // warp 0: the current choices of a block's lines
   __shared__ int vline[3][32];
   __shared__ int warp_sums[32];
-  __shared__ unsigned long long full_s[8];
+  __shared__ unsigned long long full_s[16];
   __shared__ int s_total, s_ncol[2], s_fail;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   for (int c = tid; c < 64 * W; c += kThreads) csize[c] = 0;
-  if (tid < 8) full_s[tid] = 0ull;
+  if (tid < 16) full_s[tid] = 0ull;
   if (tid == 0) {
     s_ncol[0] = 0;
     s_fail = 0;
@@ -782,7 +782,8 @@ bool colour_schedule_fits(int n_theta, int words) {
 }
 
 int launch_colour_schedule(const ColourArgs& a, void* stream) {
-  if ((a.words != 2 && a.words != 4 && a.words != 8) || a.max_colours > 64 * a.words ||
+  if ((a.words != 2 && a.words != 4 && a.words != 8 && a.words != 16) ||
+      a.max_colours > 64 * a.words ||
       a.class_cap < 1 || a.class_cap > 32 || a.nb > 16)
     return -7;
   // an error left pending by an earlier call on this thread is reported as such

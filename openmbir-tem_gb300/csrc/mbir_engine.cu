@@ -683,7 +683,8 @@ int Engine::check_device_error() {
   cudaMemsetAsync(d_err_, 0, sizeof(int), s);
   if (h & 4)
     return fail(MBIR_ENOTSUP,
-                "call schedule: the call needs more than 512 colours (use call_schedule 2)");
+                "call schedule: the call needs more colours than the device colouring holds "
+                "(use call_schedule 2)");
   return fail(MBIR_ETIMEOUT, "a bounded device wait timed out");
 }
 

@@ -311,15 +311,17 @@ class Engine {
   unsigned* d_conf_ = nullptr;              // [n_z*n_x] conflict words
   std::vector<int32_t> vis_host_;
   int16_t* d_colour_ = nullptr;             // [n_z*n_x] scratch
-  unsigned long long* d_bin_used_ = nullptr;   // [n_theta][n_r][kColourWords]
-  unsigned long long* d_line_used_ = nullptr;  // [n_z*n_x][kColourWords]
-  unsigned long long* d_cfsets_ = nullptr;  // [ceil(n_z*n_x/31)*31][kColourWords] (multi-CTA)
+  unsigned long long* d_bin_used_ = nullptr;   // [n_theta][n_r][cwords_]
+  unsigned long long* d_line_used_ = nullptr;  // [n_z*n_x][cwords_]
+  unsigned long long* d_cfsets_ = nullptr;  // [ceil(n_z*n_x/31)*31][cwords_] (multi-CTA)
   int* d_cflags_ = nullptr;                 // [3*ceil(n_z*n_x/31) + 1] (multi-CTA)
   int32_t* d_sched_count_ = nullptr;        // [2] lines, colours
   bool sched_on_device_ = false;            // the last call's schedule was built on the device
   bool readback_pending_ = false;
   int32_t sched_count_host_[2] = {0, 0};
-  static constexpr int kColourWords = 8;    // up to 512 colours
+  // colour words per bin / line of the device colouring (64 colours each): 8 while a call's
+  // lines (1/20 of the lines) fit 4096, 16 (1024 colours) above that
+  int cwords_ = 16;
   // colour schedules of the homogeneous sub-lists, which repeat every 20 calls: built once
   int cur_hslot_ = -1;                      // sub-list of the current call, -1: not homogeneous
   int32_t* d_hc_lines_ = nullptr;           // [n_z*n_x] slot k at its sub-list's offset

@@ -178,7 +178,9 @@ int Engine::bf_prepare_schedule() {
   acol_lo_.clear();
   acol_mask_.clear();
   // host schedules: the footprint bins on the host now
-  if (p_.call_schedule != 0 || !colour_schedule_fits(g.n_theta, kColourWords))
+  const size_t per_call = nl / kNumHomogeneous + nl % kNumHomogeneous;
+  cwords_ = per_call <= 4096 ? 8 : 16;
+  if (p_.call_schedule != 0 || !colour_schedule_fits(g.n_theta, cwords_))
     return host_footprint_bins();
   // device colour schedule: packed bins and scratch
   const size_t n_entries = nl * g.n_theta;
@@ -186,9 +188,9 @@ int Engine::bf_prepare_schedule() {
       cudaMalloc(&d_vis_, nl * sizeof(int32_t)) != cudaSuccess ||
       cudaMalloc(&d_conf_, 5 * nl * sizeof(unsigned)) != cudaSuccess ||
       cudaMalloc(&d_colour_, nl * sizeof(int16_t)) != cudaSuccess ||
-      cudaMalloc(&d_bin_used_, static_cast<size_t>(g.n_theta) * g.n_r * kColourWords * 8) !=
+      cudaMalloc(&d_bin_used_, static_cast<size_t>(g.n_theta) * g.n_r * cwords_ * 8) !=
           cudaSuccess ||
-      cudaMalloc(&d_line_used_, nl * kColourWords * 8) != cudaSuccess ||
+      cudaMalloc(&d_line_used_, nl * cwords_ * 8) != cudaSuccess ||
       cudaMalloc(&d_sched_count_, 2 * sizeof(int32_t)) != cudaSuccess ||
       cudaMalloc(&d_hc_lines_, nl * sizeof(int32_t)) != cudaSuccess ||
       cudaMalloc(&d_hc_lofs_, kNumHomogeneous * lofs_cap() * sizeof(int32_t)) != cudaSuccess ||
@@ -208,7 +210,7 @@ int Engine::bf_prepare_schedule() {
   }
   // scratch of the multi-CTA colouring (without it the one-CTA form runs)
   const size_t nblk = (nl + 30) / 31;
-  if (cudaMalloc(&d_cfsets_, nblk * 31 * kColourWords * 8) != cudaSuccess ||
+  if (cudaMalloc(&d_cfsets_, nblk * 31 * cwords_ * 8) != cudaSuccess ||
       cudaMalloc(&d_cflags_, (3 * nblk + 1) * sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
     dfree_any(d_cfsets_);
@@ -245,7 +247,7 @@ int Engine::host_footprint_bins() {
 // (call_lines_) becomes the schedule's line order.  Leaves `a` walking the rows when the engine
 // has no A-column table.
 int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
-  constexpr int kMaxColours = 64 * kColourWords;
+  const int kMaxColours = 64 * cwords_;
   if (d_acol_ == nullptr) return MBIR_OK;
   const Geometry& g = g_;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
@@ -279,8 +281,8 @@ int Engine::bf_schedule(const std::vector<int32_t>& rows, SweepArgs& a) {
     ca.n_theta = g.n_theta;
     ca.n_r = g.n_r;
     ca.nb = nb_;
-    ca.words = kColourWords;
-    ca.max_colours = 64 * kColourWords;
+    ca.words = cwords_;
+    ca.max_colours = 64 * cwords_;
     ca.class_cap = groups;
     ca.packed = d_packed_;
     ca.lineok = d_lineok_;
@@ -462,7 +464,7 @@ void Engine::bf_schedule_readback() {
 
 // colours <= lines, so a call's colour offsets fit in min(max colours, lines) + 1 values
 size_t Engine::lofs_cap() const {
-  return std::min<size_t>(64 * kColourWords, static_cast<size_t>(g_.n_z) * g_.n_x) + 1;
+  return std::min<size_t>(64 * cwords_, static_cast<size_t>(g_.n_z) * g_.n_x) + 1;
 }
 
 void Engine::bf_schedule_settle() {

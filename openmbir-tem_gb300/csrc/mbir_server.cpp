@@ -78,9 +78,11 @@ size_t Server::estimate_bytes(const Request& r) const {
       const int factor = (1 << (levels - 1 - lvl)) * std::max(1, r.params.final_resolution);
       const size_t acol_w = static_cast<size_t>(2 * factor + 1 + 4) / 4;
       const size_t entries = lines * r.n_theta;
-      const size_t words = 8;  // 64-bit colour words per bin / line (512 colours)
-      bf += entries * acol_w * 16 + (2 * lines + 1) * 4 + entries * 4 + lines * (4 + 12 + 2 + 4) +
+      const size_t words = 16;  // 64-bit colour words per bin / line (1024 colours)
+      const size_t blocks = (lines + 30) / 31;  // 31-line blocks of the multi-CTA colouring
+      bf += entries * acol_w * 16 + (2 * lines + 1) * 4 + entries * 4 + lines * (4 + 20 + 2 + 4) +
             static_cast<size_t>(r.n_theta) * r.n_r * words * 8 + lines * words * 8 +
+            blocks * 31 * words * 8 + (3 * blocks + 1) * 4 +
             20 * (std::min<size_t>(64 * words, lines) + 1) * 4 + 64;
     }
   }

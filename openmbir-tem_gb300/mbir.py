@@ -203,7 +203,7 @@ SIGNATURES = {
 }
 
 
-def colour_schedule(lineok, lo, mask, nb, n_r, active=None, max_colours=512, class_cap=0):
+def colour_schedule(lineok, lo, mask, nb, n_r, active=None, max_colours=1024, class_cap=0):
     """Colour schedule of a sparse ICD call (mbir_colour_schedule): returns (lines, lofs)."""
     lineok = np.ascontiguousarray(lineok, np.uint8)
     n_z, n_x = lineok.shape

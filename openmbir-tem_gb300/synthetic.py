@@ -132,6 +132,32 @@ def bf_particles_on_slab(n_r=512, n_t=256, thickness=64.0, max_deg=60.0, step_de
     return counts, ang.astype(np.float32)
 
 
+def particles_on_slab_volume(n_x, n_y, n_z, thickness, n_particles, slab=(-0.75, -0.5),
+                             slab_value=0.1, seed=0):
+    """The particles-on-slab phantom of particles_on_slab voxelised on the engine's grid (1 nm
+    voxels; the volume is 2 x thickness along z, centred): float32 [z][x][y].  Each voxel whose
+    centre lies inside an ellipsoid takes the ellipsoid's value (summed where they overlap)."""
+    lz = 2 * thickness
+    vol = np.zeros((n_z, n_x, n_y), np.float32)
+    zc = -n_z / 2 + np.arange(n_z) + 0.5
+    xc = -n_x / 2 + np.arange(n_x) + 0.5
+    yc = -n_y / 2 + np.arange(n_y) + 0.5
+    z0, z1 = slab[0] * lz / 2, slab[1] * lz / 2
+    vol[(zc >= z0) & (zc < z1)] = slab_value
+    shapes = random_ellipsoids(n_particles, n_x, n_y, lz, seed=seed, z_range=(z1, lz / 2))
+    for cx, cy, cz, ax, ay, az, val in shapes:
+        iz = np.nonzero(np.abs(zc - cz) <= az)[0]
+        ix = np.nonzero(np.abs(xc - cx) <= ax)[0]
+        iy = np.nonzero(np.abs(yc - cy) <= ay)[0]
+        if len(iz) == 0 or len(ix) == 0 or len(iy) == 0:
+            continue
+        Z, X, Y = np.ix_(zc[iz], xc[ix], yc[iy])
+        m = ((X - cx) / ax) ** 2 + ((Y - cy) / ay) ** 2 + ((Z - cz) / az) ** 2 <= 1.0
+        sub = vol[iz[0]:iz[-1] + 1, ix[0]:ix[-1] + 1, iy[0]:iy[-1] + 1]
+        sub[m] += np.float32(val)
+    return vol
+
+
 def random_ellipsoids(n, extent_x, extent_y, extent_z, seed=0, axes=(3.0, 15.0),
                       values=(0.5, 2.0), z_range=None):
     rng = np.random.default_rng(seed)
