@@ -181,6 +181,20 @@ int32_t mbir_set_sinogram(mbir_engine* e, const float* counts, const float* tilt
  * excluded_views and tilt_selection exactly as the reference reader. */
 int32_t mbir_load_sinogram_mrc(mbir_engine* e, const char* path);
 
+/* HAADF with bright-field data: a bright-field tilt series of the sinogram's size,
+ * counts[theta][r][t]; each count plus BF_OFFSET (32768) multiplies its measurement's model,
+ * and the joint estimation estimates the offsets only.  After the sinogram, before prepare.
+ * Replaces HAADF_ReconstructionEngine::setBFTomoInputs/setBFSinogram and
+ * initializeBrightFieldData (HAADF_MultiResolutionReconstruction.cpp:421-422,
+ * HAADF_ReconstructionEngine_Extra.cpp:84-176, :429, :643-668, _UpdateVoxels.cpp:354-364,
+ * :438-446).  Engines with it run alone: not in a batch, not in slabs.  MBIR_EINVAL when the
+ * sizes differ ("The two file sizes are not matched"). */
+int32_t mbir_set_bright_field(mbir_engine* e, const float* counts, int32_t n_theta, int32_t n_r,
+                              int32_t n_t);
+/* The same from an MRC file, read with the sinogram's subvolume (and, when that read fails,
+ * over the sinogram's own extent), as the reference reads its --brightfield file. */
+int32_t mbir_load_bright_field_mrc(mbir_engine* e, const char* path);
+
 /* Optional initial volume [z][x][y] (y fastest), sized as mbir_get_dims reports; with
  * interpolate_initial_recon set, (N_z/2) x (N_x/2) x (N_y/2) values, each filling its 2x2x2 block
  * (InitialReconstructionBinReader.cpp:101-131; needs the sinogram set first). */

@@ -19,7 +19,7 @@ LIB = os.path.join(HERE, "libmbir_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["mbir_sweep_f32.cu", "mbir_sweep_f32_bf.cu", "mbir_sweep_f32_hbm.cu",
            "mbir_sweep_f32_batch3.cu", "mbir_sweep_f32_batch5.cu", "mbir_sweep_f64.cu",
-           "mbir_kernels.cu",
+           "mbir_kernels.cu", "mbir_bfassist.cu",
            "mbir_exact.cu", "mbir_bf.cu", "mbir_noalloc.cu",
            "mbir_engine.cu", "mbir_engine_bf.cu", "mbir_shard.cu", "mbir_batch.cu", "mbir_server.cpp", "mrc_io.cpp",
            "mbir_schedule.cpp", "mbir_colour.cu", "mbir_capi.cpp"]

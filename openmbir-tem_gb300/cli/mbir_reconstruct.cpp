@@ -247,11 +247,10 @@ int main(int argc, char** argv) {
     usage();
     return EXIT_SUCCESS;
   }
-  if (!MBIR_CLI_BF && a.count("brightfield") && !a["brightfield"].empty()) {
-    std::printf("The bright-field normalisation of HAADF data (--brightfield) is not supported "
-                "by this build.\n");
-    return EXIT_FAILURE;
-  }
+  // HAADF with a bright-field tilt series (--brightfield): read at every level with that
+  // level's sinogram subvolume (HAADF_MultiResolutionReconstruction.cpp:189-203, :370-422)
+  const std::string bright_field =
+      (!MBIR_CLI_BF && a.count("brightfield")) ? a["brightfield"] : std::string();
 
   mbir_params p;
   mbir_params_default(&p, MBIR_CLI_BF ? MBIR_MODALITY_BF : MBIR_MODALITY_HAADF);
@@ -343,6 +342,7 @@ int main(int argc, char** argv) {
       return EXIT_FAILURE;
     }
     int rc = mbir_load_sinogram_mrc(e, sino.c_str());
+    if (rc == MBIR_OK && !bright_field.empty()) rc = mbir_load_bright_field_mrc(e, bright_field.c_str());
     int32_t d[6] = {0, 0, 0, 0, 0, 0};
     if (rc == MBIR_OK) rc = mbir_get_dims(e, d);
     if (rc == MBIR_OK && i == 0 && a.count("initial_recon_file") &&

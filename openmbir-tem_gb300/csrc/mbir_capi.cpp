@@ -190,6 +190,13 @@ int32_t mbir_set_sinogram(mbir_engine* e, const float* counts, const float* tilt
 int32_t mbir_load_sinogram_mrc(mbir_engine* e, const char* path) {
   return guarded(e, [&](mbir::Engine& m) { return m.load_mrc(path); });
 }
+int32_t mbir_set_bright_field(mbir_engine* e, const float* counts, int32_t n_theta, int32_t n_r,
+                              int32_t n_t) {
+  return guarded(e, [&](mbir::Engine& m) { return m.set_bright_field(counts, n_theta, n_r, n_t); });
+}
+int32_t mbir_load_bright_field_mrc(mbir_engine* e, const char* path) {
+  return guarded(e, [&](mbir::Engine& m) { return m.load_bright_field_mrc(path); });
+}
 int32_t mbir_set_initial_volume(mbir_engine* e, const float* vol, int64_t n) {
   return guarded(e, [&](mbir::Engine& m) { return m.set_initial_volume(vol, n); });
 }

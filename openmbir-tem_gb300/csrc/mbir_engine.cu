@@ -205,11 +205,29 @@ int Engine::set_sinogram(const float* counts, const float* tilts_deg, int n_thet
   g_.delta_r = delta_r;
   g_.delta_t = delta_t;
   counts_.assign(counts, counts + static_cast<size_t>(n_theta) * n_r * n_t);
+  bfm_.clear();
   tilts_.resize(n_theta);
   for (int i = 0; i < n_theta; i++) tilts_[i] = tilts_deg[i];
   if (state_ >= 2) release();
   state_ = 1;
   host_ready_ = false;
+  return MBIR_OK;
+}
+
+// initializeBrightFieldData (HAADF_ReconstructionEngine_Extra.cpp:84-176): a bright-field tilt
+// series of the sinogram's size; each count plus BF_OFFSET (HAADFConstants.h:49) becomes the
+// measurement's factor m.  HAADF only, before prepare.
+int Engine::set_bright_field(const float* counts, int n_theta, int n_r, int n_t) {
+  if (state_ < 1) return fail(MBIR_ESTATE, "set_bright_field: set the sinogram first");
+  if (state_ >= 2) return fail(MBIR_ESTATE, "set_bright_field: before prepare");
+  if (bf_) return fail(MBIR_EINVAL, "set_bright_field: HAADF reconstructions only");
+  if (!counts) return fail(MBIR_EINVAL, "set_bright_field: null counts");
+  if (n_theta != g_.n_theta || n_r != g_.n_r || n_t != g_.n_t)
+    return fail(MBIR_EINVAL, "set_bright_field: The two file sizes are not matched");
+  const size_t n = static_cast<size_t>(n_theta) * n_r * n_t;
+  constexpr double kBfOffset = 32768.0;  // BF_OFFSET
+  bfm_.resize(n);
+  for (size_t i = 0; i < n; i++) bfm_[i] = static_cast<double>(counts[i]) + kBfOffset;
   return MBIR_OK;
 }
 
@@ -570,7 +588,9 @@ int Engine::alloc_device() {
   n_rs_ = (n_rp_ % 32 == 0) ? n_rp_ + 4 : n_rp_;
   int max_smem = 0;
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, p_.device);
-  n_sp_ = bf_ ? (g.n_r + 15) / 16 * 16 : 0;
+  const bool bfa = bright_field_assisted();
+  // the bright-field sweep (per-entry weights and selector) serves assisted HAADF as well
+  n_sp_ = (bf_ || bfa) ? (g.n_r + 15) / 16 * 16 : 0;
   // a selector row stride of a multiple of 128 bytes would put every view's byte of a detector
   // bin into one shared-memory bank; 16 more bytes spread the views over eight banks
   if (n_sp_ > 0 && n_sp_ % 128 == 0) n_sp_ += 16;
@@ -628,6 +648,14 @@ int Engine::alloc_device() {
     rc |= dmalloc(&d_bfpart_, 4096);
     rc |= dmalloc(&d_bfout_, 16);
     rc |= dmalloc(&d_alpha_, g.n_theta);
+    rc |= dmalloc(&d_stage64_, nh);
+  }
+  if (bfa) {
+    const size_t nl = static_cast<size_t>(g.n_z) * g.n_x;
+    rc |= dmalloc_bytes(&d_w_, ns * rb_);
+    rc |= dmalloc_bytes(&d_bfm_, ns * rb_);
+    rc |= dmalloc(&d_sel_, static_cast<size_t>(g.n_t) * g.n_theta * n_sp_);
+    rc |= dmalloc(&d_active_, nl);
     rc |= dmalloc(&d_stage64_, nh);
   }
   if (rc) return fail(MBIR_ENOMEM, "device allocation failed");
@@ -772,6 +800,15 @@ int Engine::prepare() {
     if ((rc = launch_sino_to_dev(d_stage_, d_y_, g.n_theta, g.n_r, n_rp_, g.n_t, fp64_, s)))
       return cuda_check(rc, "sinogram upload");
   }
+  if (bright_field_assisted()) {
+    cudaMemcpyAsync(d_stage64_, bfm_.data(), sizeof(double) * nh, cudaMemcpyHostToDevice, s);
+    if ((rc = launch_layout_from_double(d_stage64_, d_bfm_, g.n_theta, g.n_r, n_rp_, g.n_t, fp64_,
+                                        s)))
+      return cuda_check(rc, "bright-field upload");
+    // selector always on, every line in every sweep
+    cudaMemsetAsync(d_sel_, 1, static_cast<size_t>(g.n_t) * g.n_theta * n_sp_, s);
+    cudaMemsetAsync(d_active_, 1, static_cast<size_t>(g.n_z) * g.n_x, s);
+  }
 
   // initial volume (InitialReconstructionInitializer::initializeData, :74-90)
   const size_t nv = static_cast<size_t>(g.n_z) * g.n_x * g.n_y;
@@ -861,8 +898,11 @@ int Engine::forward_project() {
   if (exact_) {
     int rc = launch_exact_project(exact_args(), static_cast<double*>(d_yest_), s);
     if (rc) return cuda_check(rc, "forward projection (exact)");
-    rc = launch_error_from_projection(d_y_, d_yest_, d_e_, d_mu_, g.n_theta, n_rp_, g.n_r, g.n_t,
-                                      fp64_, s);
+    rc = bright_field_assisted()
+             ? launch_exact_bfa_error(exact_args(), static_cast<const double*>(d_y_),
+                                      static_cast<const double*>(d_yest_), d_mu_, s)
+             : launch_error_from_projection(d_y_, d_yest_, d_e_, d_mu_, g.n_theta, n_rp_, g.n_r,
+                                            g.n_t, fp64_, s);
     if (rc) return cuda_check(rc, "error sinogram");
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "forward projection");
     return check_device_error();
@@ -889,11 +929,33 @@ int Engine::forward_project() {
     int rc = launch_sweep(a, nb_, smem_bytes_, s);
     if (rc) return cuda_check(rc, "forward projection launch");
   }
-  int rc = launch_error_from_projection(d_y_, d_yest_, d_e_, d_mu_, g.n_theta, n_rp_, g.n_r,
-                                        g.n_t, fp64_, s);
+  int rc;
+  if (bright_field_assisted()) {
+    // scaled error e / m and per-entry weights m^2 w (mbir_bfassist.cu)
+    rc = launch_bfa_error(d_y_, d_yest_, d_bfm_, d_e_, d_mu_, g.n_theta, n_rp_, g.n_r, g.n_t,
+                          fp64_, s);
+    if (!rc) rc = launch_bfa_weights(d_bfm_, d_wv_, d_w_, g.n_theta, n_rp_, g.n_r, g.n_t, fp64_, s);
+  } else {
+    rc = launch_error_from_projection(d_y_, d_yest_, d_e_, d_mu_, g.n_theta, n_rp_, g.n_r, g.n_t,
+                                      fp64_, s);
+  }
   if (rc) return cuda_check(rc, "error sinogram");
   if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "forward projection");
   return check_device_error();
+}
+
+// The bright-field sweep arguments of an assisted HAADF engine: per-entry weights m^2 w, the
+// selector always on, every line, no magnitude map
+DevBF Engine::bfa_sweep_args() const {
+  DevBF b{};
+  b.w = d_w_;
+  b.sel = d_sel_;
+  b.n_sp = n_sp_;
+  b.active = d_active_;
+  b.mag_fx = nullptr;
+  b.bragg_t = 1.0e30;
+  b.bragg_dt = 0.0;
+  return b;
 }
 
 void Engine::row_order_for_sweep(int sweep, std::vector<int32_t>& order) const {
@@ -948,6 +1010,10 @@ int Engine::sweep(int outer, int inner, double* stats4) {
     a.zero_skipping = p_.zero_skipping;
     a.fp64 = fp64_;
     a.stats = d_stat4_;
+    if (bright_field_assisted()) {
+      a.bf = 1;
+      a.bfa = bfa_sweep_args();
+    }
     if ((rc = launch_ref_order(a, nb_, s))) return cuda_check(rc, "reference-order sweep");
     }
   } else {
@@ -970,6 +1036,10 @@ int Engine::sweep(int outer, int inner, double* stats4) {
     a.n_rs = stage_ ? n_rs_ : 0;
     a.shape = shape_;
     a.err = d_err_;
+    if (bright_field_assisted()) {
+      a.bf = 1;
+      a.bfa = bfa_sweep_args();
+    }
     const int n0 = (g.n_y + 1) / 2;
     cudaEventRecord(static_cast<cudaEvent_t>(ev2_), s);
     for (int colour = 0; colour < 2; colour++) {
@@ -1027,6 +1097,7 @@ ExactArgs Engine::exact_args() {
   a.lineok = d_lineok_;
   a.x = static_cast<double*>(d_x_);
   a.e = static_cast<double*>(d_e_);
+  a.bfm = bright_field_assisted() ? static_cast<const double*>(d_bfm_) : nullptr;
   return a;
 }
 
@@ -1034,6 +1105,8 @@ int Engine::batch_args(int outer, int inner, SweepArgs* out, size_t* smem_needed
   if (state_ < 2) return fail(MBIR_ESTATE, "batch: engine not prepared");
   if (fp64_ || p_.order_mode != MBIR_ORDER_PARALLEL)
     return fail(MBIR_ENOTSUP, "batch: FP32 parallel-order engines only");
+  if (bright_field_assisted())
+    return fail(MBIR_ENOTSUP, "batch: HAADF with bright-field data runs alone");
   const Geometry& g = g_;
   std::vector<int32_t> rows;
   row_order_for_sweep(sweeps_done_, rows);
@@ -1093,6 +1166,7 @@ int Engine::batch_finish(int outer, int inner, const double* st, double ms) {
 int Engine::joint_estimation() {
   if (state_ < 2) return fail(MBIR_ESTATE, "joint_estimation: call prepare first");
   if (bf_) return bf_joint_estimation();
+  if (bright_field_assisted()) return bfa_offsets();
   const Geometry& g = g_;
   const int nt = g.n_theta;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
@@ -1142,10 +1216,13 @@ int Engine::update_weights() {
   const Geometry& g = g_;
   const int nt = g.n_theta;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const bool scaled = bright_field_assisted() && !exact_;  // e / m in d_e_
   int rc = exact_ ? launch_exact_view_sums(exact_args(), 1, static_cast<const double*>(d_y_), d_mu_,
                                            d_vsum_, s)
-                 : launch_view_sums(1, d_y_, d_e_, d_mu_, d_gain_, d_wv_, d_partial_, d_vsum_, nt,
-                                    n_rp_, g.n_r, g.n_t, n_chunk_, fp64_, s);
+           : scaled ? launch_bfa_sums(1, d_bfm_, d_e_, d_partial_, d_vsum_, nt, n_rp_, g.n_r,
+                                      g.n_t, n_chunk_, fp64_, s)
+                    : launch_view_sums(1, d_y_, d_e_, d_mu_, d_gain_, d_wv_, d_partial_, d_vsum_,
+                                       nt, n_rp_, g.n_r, g.n_t, n_chunk_, fp64_, s);
   if (rc) return cuda_check(rc, "variance sums");
   std::vector<double> vs(nt);
   cudaMemcpyAsync(vs.data(), d_vsum_, sizeof(double) * nt, cudaMemcpyDeviceToHost, s);
@@ -1154,6 +1231,46 @@ int Engine::update_weights() {
     alpha_[v] = vs[v] / (g.n_r * g.n_t);
     w_[v] = 1.0 / alpha_[v];
   }
+  if ((rc = upload_views())) return rc;
+  if (scaled) {
+    rc = launch_bfa_weights(d_bfm_, d_wv_, d_w_, nt, n_rp_, g.n_r, g.n_t, fp64_, s);
+    if (rc) return cuda_check(rc, "bright-field weights");
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "update weights");
+  }
+  return MBIR_OK;
+}
+
+// jointEstimation with bright-field data (HAADF_ReconstructionEngine_Extra.cpp:429, :643-668):
+// the offsets only, per view the weighted mean of the error taken off the error
+int Engine::bfa_offsets() {
+  const Geometry& g = g_;
+  const int nt = g.n_theta;
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  int rc;
+  if (exact_) {
+    cudaMemcpyAsync(d_mu2_, mu_.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, s);
+    if ((rc = launch_exact_bfa_offsets(exact_args(), d_mu2_, s)))
+      return cuda_check(rc, "offset estimation (exact)");
+    cudaMemcpyAsync(mu_.data(), d_mu2_, sizeof(double) * nt, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "offsets");
+    return upload_views();
+  }
+  // the weights are one value per view, so the weighted mean is sum(m e') / (N_r N_t)
+  if ((rc = launch_bfa_sums(0, d_bfm_, d_e_, d_partial_, d_vsum_, nt, n_rp_, g.n_r, g.n_t,
+                            n_chunk_, fp64_, s)))
+    return cuda_check(rc, "offset sums");
+  std::vector<double> vs(nt);
+  cudaMemcpyAsync(vs.data(), d_vsum_, sizeof(double) * nt, cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "offsets");
+  std::vector<double> step(nt);
+  for (int v = 0; v < nt; v++) {
+    step[v] = vs[v] / (static_cast<double>(g.n_r) * g.n_t);
+    mu_[v] += step[v];
+  }
+  cudaMemcpyAsync(d_mu2_, step.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, s);
+  if ((rc = launch_bfa_offset_apply(d_bfm_, d_e_, d_mu2_, nt, n_rp_, g.n_r, g.n_t, fp64_, s)))
+    return cuda_check(rc, "offset step");
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "offsets");
   return upload_views();
 }
 
@@ -1164,8 +1281,11 @@ int Engine::compute_cost(double* parts3, double* total) {
   const Geometry& g = g_;
   const int nt = g.n_theta;
   cudaStream_t s = static_cast<cudaStream_t>(stream_);
-  int rc = launch_view_sums(1, d_y_, d_e_, d_mu_, d_gain_, d_wv_, d_partial_, d_vsum_, nt, n_rp_,
-                            g.n_r, g.n_t, n_chunk_, fp64_, s);
+  int rc = (bright_field_assisted() && !exact_)
+               ? launch_bfa_sums(1, d_bfm_, d_e_, d_partial_, d_vsum_, nt, n_rp_, g.n_r, g.n_t,
+                                 n_chunk_, fp64_, s)
+               : launch_view_sums(1, d_y_, d_e_, d_mu_, d_gain_, d_wv_, d_partial_, d_vsum_, nt,
+                                  n_rp_, g.n_r, g.n_t, n_chunk_, fp64_, s);
   if (rc) return cuda_check(rc, "cost data term");
   double* prior_partial = d_partial_ + static_cast<size_t>(nt) * n_chunk_ * 6;
   rc = launch_prior_cost(d_x_, flt_, g.n_z, g.n_x, g.n_y, prior_partial, prior_blocks_, fp64_,
@@ -1278,7 +1398,12 @@ static int sino_readout(Engine* eng, const void* dsrc, float* stage, float* out,
 
 int Engine::get_error(float* out, int64_t n) {
   if (state_ < 2) return fail(MBIR_ESTATE, "get_error: call prepare first");
-  return sino_readout(this, d_e_, d_stage_, out, n, g_, n_rp_, fp64_, stream_);
+  const int rc = sino_readout(this, d_e_, d_stage_, out, n, g_, n_rp_, fp64_, stream_);
+  if (rc || !bright_field_assisted() || exact_) return rc;
+  // the parallel engines keep e / m on the device (mbir_bfassist.cu)
+  for (size_t i = 0; i < bfm_.size() && static_cast<int64_t>(i) < n; i++)
+    out[i] = static_cast<float>(static_cast<double>(out[i]) * bfm_[i]);
+  return MBIR_OK;
 }
 int Engine::get_projection(float* out, int64_t n) {
   if (state_ < 2) return fail(MBIR_ESTATE, "get_projection: call prepare first");
@@ -1438,7 +1563,7 @@ std::map<std::vector<int>, int> g_tune_cache;
 }  // namespace
 
 int Engine::autotune_shape() {
-  if (fp64_ || p_.order_mode != MBIR_ORDER_PARALLEL) return MBIR_OK;
+  if (fp64_ || p_.order_mode != MBIR_ORDER_PARALLEL || bright_field_assisted()) return MBIR_OK;
   const Geometry& g = g_;
   std::vector<int> cands;
   for (int sh = 1; sh <= 4; sh++)

@@ -84,6 +84,15 @@ class Engine {
   int set_sinogram(const float* counts, const float* tilts_deg, int n_theta, int n_r, int n_t,
                    double delta_r, double delta_t);
   int load_mrc(const char* path);
+  int read_mrc_series(const char* path, std::vector<float>& counts, std::vector<float>& tilts,
+                      int& n_theta, int& n_r, int& n_t, double& dr, bool need_tilts);
+  // HAADF with bright-field data (initializeBrightFieldData): a bright-field tilt series of the
+  // sinogram's size, [theta][r][t]; before prepare
+  int set_bright_field(const float* counts, int n_theta, int n_r, int n_t);
+  int load_bright_field_mrc(const char* path);
+  bool bright_field_assisted() const { return !bfm_.empty(); }
+  DevBF bfa_sweep_args() const;
+  int bfa_offsets();
   int set_initial_volume(const float* vol, int64_t n);
   int set_initial_nuisance(const double* g, const double* o, const double* v);
   int dims(int32_t* d) const;
@@ -190,6 +199,7 @@ class Engine {
 
   // host inputs
   std::vector<float> counts_;     // [theta][r][t]
+  std::vector<double> bfm_;       // [theta][r][t] bright-field count + BF_OFFSET (assisted HAADF)
   std::vector<double> tilts_;     // degrees
   std::vector<float> init_vol_;   // optional [z][x][y]
   std::vector<double> user_gain_, user_offset_, user_var_;
@@ -276,6 +286,7 @@ class Engine {
 
   // bright-field state
   void* d_w_ = nullptr;                     // Real [n_t][n_theta][n_rp] weights
+  void* d_bfm_ = nullptr;                   // Real [n_t][n_theta][n_rp] bright-field factor m
   uint8_t* d_sel_ = nullptr;                // [n_t][n_theta][n_sp] Bragg selector
   unsigned long long* d_magfx_ = nullptr;   // [n_z][n_x] fixed-point magnitudes of a call
   double* d_mag_ = nullptr;                 // [n_z][n_x] update-magnitude map

@@ -17,6 +17,8 @@
 // Only the elementwise parts run in parallel.  It is a parity mode, not a fast path.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "mbir_internal.h"
 
 namespace mbir {
@@ -301,7 +303,8 @@ __global__ void __launch_bounds__(32, 1) exact_icd_kernel(ExactArgs A) {
                 th1 += qc * (evv * pe * w);
               }
             } else {
-              const double pe = k0 * hv[a];
+              double pe = k0 * hv[a];
+              if (A.bfm) pe *= A.bfm[ei];  // with bright-field data (_UpdateVoxels.cpp:358-364)
               th2 += (pe * pe * A.weight[th]);
               th1 += (evv * pe * A.weight[th]);
             }
@@ -348,7 +351,10 @@ __global__ void __launch_bounds__(32, 1) exact_icd_kernel(ExactArgs A) {
           const size_t ei = static_cast<size_t>(t0 + a) * sino_plane +
                             static_cast<size_t>(th) * g.n_rp + r;
           const double k2 = (A.gain[th] * (col.val[q] * hv[a] * (nv - V)));
-          e[ei] -= k2;
+          if (A.bfm)
+            e[ei] -= (A.bfm[ei] * k2);  // with bright-field data (_UpdateVoxels.cpp:442-446)
+          else
+            e[ei] -= k2;
           if (A.bf) {  // BFForwardModel::updateErrorSinogram (BFForwardModel.cpp:921-929)
             const size_t si = static_cast<size_t>(t0 + a) * sel_plane +
                               static_cast<size_t>(th) * A.n_sp + r;
@@ -451,7 +457,57 @@ __global__ void exact_view_sums_kernel(ExactArgs A, int kind, const double* y, c
   out[th * 6 + 5] = d;
 }
 
+// calculateMeasurementWeight's error with bright-field data (_Extra.cpp:722-727):
+// e = y - m Y_Est - mu, one thread per measurement
+__global__ void exact_bfa_error_kernel(ExactArgs A, const double* y, const double* yest,
+                                       const double* mu) {
+  const DevGeom& g = A.g;
+  const size_t total = static_cast<size_t>(g.n_t) * g.n_theta * g.n_rp;
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const int r = static_cast<int>(i % g.n_rp);
+    const int v = static_cast<int>((i / g.n_rp) % g.n_theta);
+    A.e[i] = (r < g.n_r) ? y[i] - A.bfm[i] * yest[i] - mu[v] : 0.0;
+  }
+}
+
+// jointEstimation with bright-field data, offsets only (_Extra.cpp:643-668): per view (one
+// thread) the error's weighted mean over r then t, taken off the error and added to mu
+__global__ void exact_bfa_offsets_kernel(ExactArgs A, double* mu) {
+  const DevGeom& g = A.g;
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= g.n_theta) return;
+  const size_t plane = static_cast<size_t>(g.n_theta) * g.n_rp;
+  const double w = A.weight[v];
+  double num_sum = 0, den_sum = 0;
+  for (int r = 0; r < g.n_r; r++)
+    for (int t = 0; t < g.n_t; t++) {
+      const size_t i = static_cast<size_t>(t) * plane + static_cast<size_t>(v) * g.n_rp + r;
+      num_sum += (A.e[i] * w);
+      den_sum += w;
+    }
+  const double a = num_sum / den_sum;
+  for (int r = 0; r < g.n_r; r++)
+    for (int t = 0; t < g.n_t; t++)
+      A.e[static_cast<size_t>(t) * plane + static_cast<size_t>(v) * g.n_rp + r] -= a;
+  mu[v] += a;
+}
+
 }  // namespace
+
+int launch_exact_bfa_error(const ExactArgs& a, const double* y, const double* yest,
+                           const double* mu, void* stream) {
+  const size_t n = static_cast<size_t>(a.g.n_t) * a.g.n_theta * a.g.n_rp;
+  const int grid = static_cast<int>(std::min<size_t>((n + 255) / 256, 152 * 16));
+  exact_bfa_error_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(a, y, yest, mu);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+int launch_exact_bfa_offsets(const ExactArgs& a, double* mu, void* stream) {
+  exact_bfa_offsets_kernel<<<(a.g.n_theta + 63) / 64, 64, 0, static_cast<cudaStream_t>(stream)>>>(
+      a, mu);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
 
 int launch_exact_icd(const ExactArgs& a, void* stream) {
   exact_icd_kernel<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(a);

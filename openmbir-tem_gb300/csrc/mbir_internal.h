@@ -237,7 +237,24 @@ struct ExactArgs {
   int n_sp;
   double bragg_t, bragg_delta;
   double* mag;           // [n_z][n_x] per-line sum |dx| (reset for each line of the call)
+  // HAADF with bright-field data: bright-field count + BF_OFFSET per entry, [n_t][n_theta][n_rp]
+  // (nullptr without)
+  const double* bfm;
 };
+
+// HAADF with bright-field data (mbir_bfassist.cu; the reference-exact forms in mbir_exact.cu).
+// Arrays share the [t][theta][r_pad] layout; m = bright-field count + BF_OFFSET.
+int launch_bfa_error(const void* y, const void* yest, const void* m, void* e, const double* mu,
+                     int n_theta, int n_rp, int n_r, int n_t, int fp64, void* stream);
+int launch_bfa_weights(const void* m, const double* wv, void* w, int n_theta, int n_rp, int n_r,
+                       int n_t, int fp64, void* stream);
+int launch_bfa_sums(int kind, const void* m, const void* e, double* partial, double* out,
+                    int n_theta, int n_rp, int n_r, int n_t, int n_chunk, int fp64, void* stream);
+int launch_bfa_offset_apply(const void* m, void* e, const double* step, int n_theta, int n_rp,
+                            int n_r, int n_t, int fp64, void* stream);
+int launch_exact_bfa_error(const ExactArgs& a, const double* y, const double* yest,
+                           const double* mu, void* stream);
+int launch_exact_bfa_offsets(const ExactArgs& a, double* mu, void* stream);
 
 // Bright-field sinogram-wide passes (mbir_bf.cu).  Arrays share the [t][theta][row] layout.
 struct BfSino {

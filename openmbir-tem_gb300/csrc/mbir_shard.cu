@@ -14,6 +14,8 @@ namespace mbir {
 
 int Engine::set_slab(int y0, int y1) {
   if (state_ < 1) return fail(MBIR_ESTATE, "set_slab: no sinogram");
+  if (bright_field_assisted() && !(y0 == 0 && y1 == 0))
+    return fail(MBIR_ENOTSUP, "set_slab: HAADF with bright-field data runs unsharded");
   if (g_.n_y == 0) {
     int rc = build_geometry();
     if (rc) return rc;

@@ -452,7 +452,12 @@ int avizo_write_volume(const std::string& path, const float* zxy, int n_z, int n
 
 // MRCSinogramInitializer::execute (MRCSinogramInitializer.cpp:79-339) plus the tilt read of
 // the CLI (HAADFReconstructionArgsParser.cpp:296-322).
-int Engine::load_mrc(const char* path) {
+// The tilt series of an MRC file as MRCSinogramInitializer reads it (MRCSinogramInitializer.cpp:
+// 113-300): the subvolume made symmetric about the centre of rotation and its y range a multiple
+// of 3 x the interpolation factor, excluded views dropped; counts [theta][r][t].
+int Engine::read_mrc_series(const char* path, std::vector<float>& counts,
+                            std::vector<float>& tilts, int& n_theta_out, int& n_r_out,
+                            int& n_t_out, double& dr_out, bool need_tilts) {
   if (!path) return fail(MBIR_EINVAL, "load_mrc: null path");
   MrcVolume hdr;
   std::string err;
@@ -462,7 +467,7 @@ int Engine::load_mrc(const char* path) {
     return fail(MBIR_EINVAL,
                 "The data type of the MRC file was not either 1 (signed 16 Bit Ints), 2 (32 bit "
                 "floats) or 6 (unsigned 16 Bit Ints)");
-  if (!hdr.has_fei) return fail(MBIR_EINVAL, "MRC file carries no FEI tilt angles");
+  if (need_tilts && !hdr.has_fei) return fail(MBIR_EINVAL, "MRC file carries no FEI tilt angles");
   int vmin[3] = {0, 0, 0}, vmax[3] = {hdr.nx - 1, hdr.ny - 1, hdr.nz - 1};
   if (p_.use_subvolume) {
     const int levels = p_.num_resolutions > 0 ? p_.num_resolutions : 1;
@@ -523,20 +528,58 @@ int Engine::load_mrc(const char* path) {
   rc = mrc_read(path, vmin, vmax, vol, false, err);
   if (rc) return fail(rc, err);
   const int n_theta = static_cast<int>(good.size());
-  std::vector<float> counts(static_cast<size_t>(n_theta) * n_r * n_t);
-  std::vector<float> tilts(n_theta);
+  counts.assign(static_cast<size_t>(n_theta) * n_r * n_t, 0.f);
+  tilts.assign(n_theta, 0.f);
   const std::vector<float>& src_tilts = p_.tilt_selection == 0 ? hdr.a_tilt : hdr.b_tilt;
   for (int z = 0; z < n_theta; z++) {
     const int dz = good[z] - vmin[2];
     // the reference indexes the tilt list by the kept-view position, not the file section
     // (MRCSinogramInitializer.cpp:271)
-    tilts[z] = src_tilts[z];
+    if (z < static_cast<int>(src_tilts.size())) tilts[z] = src_tilts[z];
     for (int y = 0; y < n_t; y++)
       for (int x = 0; x < n_r; x++)
         counts[(static_cast<size_t>(z) * n_r + x) * n_t + y] =
             vol.data[static_cast<size_t>(dz) * n_r * n_t + static_cast<size_t>(y) * n_r + x];
   }
+  n_theta_out = n_theta;
+  n_r_out = n_r;
+  n_t_out = n_t;
+  dr_out = dr;
+  return MBIR_OK;
+}
+
+int Engine::load_mrc(const char* path) {
+  std::vector<float> counts, tilts;
+  int n_theta = 0, n_r = 0, n_t = 0;
+  double dr = 1.0;
+  const int rc = read_mrc_series(path, counts, tilts, n_theta, n_r, n_t, dr, true);
+  if (rc) return rc;
   return set_sinogram(counts.data(), tilts.data(), n_theta, n_r, n_t, dr, dr);
+}
+
+// The bright-field file of an HAADF reconstruction (initializeBrightFieldData,
+// HAADF_ReconstructionEngine_Extra.cpp:84-149): read with the HAADF series' subvolume; when
+// that read fails, once more over the HAADF sinogram's own extent; the sizes must then match.
+int Engine::load_bright_field_mrc(const char* path) {
+  if (state_ < 1) return fail(MBIR_ESTATE, "load_bright_field_mrc: set the sinogram first");
+  std::vector<float> counts, tilts;
+  int n_theta = 0, n_r = 0, n_t = 0;
+  double dr = 1.0;
+  int rc = read_mrc_series(path, counts, tilts, n_theta, n_r, n_t, dr, false);
+  if (rc && rc != MBIR_EIO) {
+    const mbir_params saved = p_;
+    p_.use_subvolume = 1;
+    p_.subvolume[0] = 0;
+    p_.subvolume[1] = 0;
+    p_.subvolume[2] = 0;
+    p_.subvolume[3] = g_.n_r - 1;
+    p_.subvolume[4] = g_.n_t - 1;
+    p_.subvolume[5] = g_.n_theta - 1;
+    rc = read_mrc_series(path, counts, tilts, n_theta, n_r, n_t, dr, false);
+    p_ = saved;
+  }
+  if (rc) return rc;
+  return set_bright_field(counts.data(), n_theta, n_r, n_t);
 }
 
 }  // namespace mbir

@@ -128,6 +128,8 @@ SIGNATURES = {
     "mbir_set_sinogram": (C.c_int32, [C.c_void_p, _F, _F, C.c_int32, C.c_int32, C.c_int32,
                                       C.c_double, C.c_double]),
     "mbir_load_sinogram_mrc": (C.c_int32, [C.c_void_p, C.c_char_p]),
+    "mbir_set_bright_field": (C.c_int32, [C.c_void_p, _F, C.c_int32, C.c_int32, C.c_int32]),
+    "mbir_load_bright_field_mrc": (C.c_int32, [C.c_void_p, C.c_char_p]),
     "mbir_set_initial_volume": (C.c_int32, [C.c_void_p, _F, C.c_int64]),
     "mbir_set_initial_nuisance": (C.c_int32, [C.c_void_p, _D, _D, _D]),
     "mbir_get_dims": (C.c_int32, [C.c_void_p, _I]),
@@ -329,6 +331,16 @@ class Engine:
 
     def load_mrc(self, path):
         return self._check(lib().mbir_load_sinogram_mrc(self._h, str(path).encode()))
+
+    def set_bright_field(self, counts):
+        """HAADF with bright-field data: counts[theta][r][t] of the sinogram's size."""
+        c = np.ascontiguousarray(counts, np.float32)
+        n_theta, n_r, n_t = c.shape
+        return self._check(lib().mbir_set_bright_field(self._h, c.ctypes.data_as(_F), n_theta,
+                                                        n_r, n_t))
+
+    def load_bright_field_mrc(self, path):
+        return self._check(lib().mbir_load_bright_field_mrc(self._h, str(path).encode()))
 
     def dims(self):
         d = np.zeros(6, np.int32)

@@ -72,6 +72,9 @@ struct orc_ctx {
   double* filt_map;    /* VSC-filtered mag map [n_z][n_x] */
   double bragg_t;      /* current Bragg threshold T */
   int counts_logged;   /* processRawCounts applied */
+  /* HAADF with bright-field data: the bright-field counts + BF_OFFSET [n_theta][n_r][n_t]
+   * (NULL without) */
+  double* bfm;
 };
 
 /* ---------------------------------------------------------------------------------------
@@ -545,9 +548,21 @@ void orc_destroy(orc_ctx* c) {
                   c->col_start,  c->col_count, c->col_index, c->col_val,     c->counts,
                   c->x,          c->e,        c->w,          c->yest,        c->I,
                   c->mu,         c->alpha,    c->init_gain,  c->init_offset, c->init_var,
-                  c->mask,       c->mag_map,  c->filt_map,   c->sel};
+                  c->mask,       c->mag_map,  c->filt_map,   c->sel,       c->bfm};
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) free(ptrs[i]);
   free(c);
+}
+
+/* initializeBrightFieldData (HAADF_ReconstructionEngine_Extra.cpp:84-176): the bright-field
+ * tilt series of the same size, BF_OFFSET (HAADFConstants.h:49) added to every count; from
+ * then on the forward model carries BF_Flag.  bf_counts: [n_theta][n_r][n_t]. */
+void orc_set_bf_assist(orc_ctx* c, const double* bf_counts) {
+  size_t ns = (size_t)c->n_theta * c->n_r * c->n_t;
+  free(c->bfm);
+  c->bfm = NULL;
+  if (!bf_counts) return;
+  c->bfm = (double*)malloc(sizeof(double) * ns);
+  for (size_t i = 0; i < ns; i++) c->bfm[i] = bf_counts[i] + 32768.0;
 }
 
 void orc_dims(const orc_ctx* c, int32_t* dims, double* geo) {
@@ -717,7 +732,11 @@ void orc_measurement_weight(orc_ctx* c) {
     if (c->p.noise_model) c->alpha[th] = c->init_var[th];
     for (int r = 0; r < c->n_r; r++)
       for (int t = 0; t < c->n_t; t++) {
-        S3(c, e, th, r, t) = S3(c, counts, th, r, t) - S3(c, yest, th, r, t) - c->mu[th];
+        if (c->bfm) /* :722-727 */
+          S3(c, e, th, r, t) =
+              S3(c, counts, th, r, t) - S3(c, bfm, th, r, t) * S3(c, yest, th, r, t) - c->mu[th];
+        else
+          S3(c, e, th, r, t) = S3(c, counts, th, r, t) - S3(c, yest, th, r, t) - c->mu[th];
         double w = 1.0;
         if (c->p.noise_model) w /= c->alpha[th];
         S3(c, w, th, r, t) = w;
@@ -765,6 +784,7 @@ static void update_voxel(orc_ctx* c, int jn, int kn, int i, int outer, int inner
     for (int a = 0; a < tc; a++) {
       size_t ei = ((size_t)th * c->n_r + r) * c->n_t + (t0 + a);
       double pe = k0 * hv[a];
+      if (c->bfm) pe *= c->bfm[ei]; /* :358-364 */
       th2 += (pe * pe * c->w[ei]);
       th1 += (c->e[ei] * pe * c->w[ei]);
     }
@@ -795,7 +815,10 @@ static void update_voxel(orc_ctx* c, int jn, int kn, int i, int outer, int inner
     for (int a = 0; a < tc; a++) {
       size_t ei = ((size_t)th * c->n_r + r) * c->n_t + (t0 + a);
       double k2 = (c->I[th] * (c->col_val[base + q] * hv[a] * (nv - V)));
-      c->e[ei] -= k2;
+      if (c->bfm)
+        c->e[ei] -= (c->bfm[ei] * k2); /* :442-446 */
+      else
+        c->e[ei] -= k2;
     }
   }
 }
@@ -967,6 +990,23 @@ void orc_icd_sweep_slices(orc_ctx* c, const int32_t* row_order, int stride, int 
 
 /* jointEstimation, gain+offset branch (HAADF_ReconstructionEngine_Extra.cpp:419-636). */
 int orc_joint_estimation(orc_ctx* c) {
+  if (c->bfm) {
+    /* with bright-field data only the offsets are estimated (:429, :643-668): per view the
+     * weighted mean of the error, taken off the error and added to the offset */
+    for (int th = 0; th < c->n_theta; th++) {
+      double num_sum = 0, den_sum = 0;
+      for (int r = 0; r < c->n_r; r++)
+        for (int t = 0; t < c->n_t; t++) {
+          num_sum += (S3(c, e, th, r, t) * S3(c, w, th, r, t));
+          den_sum += S3(c, w, th, r, t);
+        }
+      double a = num_sum / den_sum;
+      for (int r = 0; r < c->n_r; r++)
+        for (int t = 0; t < c->n_t; t++) S3(c, e, th, r, t) -= a;
+      c->mu[th] += a;
+    }
+    return 0;
+  }
   int nt = c->n_theta;
   double* Qk = (double*)calloc((size_t)nt * 3, sizeof(double));
   double* bk = (double*)calloc((size_t)nt * 2, sizeof(double));

@@ -112,6 +112,9 @@ void orc_icd_sweep_lines(orc_ctx* c, const int32_t* lines, int n_lines, int oute
                          double* stats);
 
 int orc_joint_estimation(orc_ctx* c);
+/* HAADF with bright-field data (initializeBrightFieldData): counts [n_theta][n_r][n_t], NULL to
+ * clear; call before orc_init_nuisance / orc_measurement_weight */
+void orc_set_bf_assist(orc_ctx* c, const double* bf_counts);
 void orc_update_weights(orc_ctx* c);
 /* parts[0] = data term, parts[1] = prior term, parts[2] = noise term; returns the sum */
 double orc_cost(const orc_ctx* c, double* parts);

@@ -79,6 +79,7 @@ def lib():
             "orc_icd_sweep_slices": (None, [C.c_void_p, _I, C.c_int, C.c_int, C.c_int, _D]),
             "orc_icd_sweep_lines": (None, [C.c_void_p, _I, C.c_int, C.c_int, C.c_int, _D]),
             "orc_joint_estimation": (C.c_int, [C.c_void_p]),
+            "orc_set_bf_assist": (None, [C.c_void_p, _D]),
             "orc_update_weights": (None, [C.c_void_p]),
             "orc_cost": (C.c_double, [C.c_void_p, _D]),
             "orc_visit_order": (None, [C.c_uint32, C.c_int, C.c_int, _I]),
@@ -254,6 +255,16 @@ class Oracle:
 
     def init_nuisance(self):
         return lib().orc_init_nuisance(self._h)
+
+    def set_bf_assist(self, bf_counts):
+        """HAADF with bright-field data: counts [theta][r][t] of the same size (None clears);
+        before prepare."""
+        if bf_counts is None:
+            lib().orc_set_bf_assist(self._h, None)
+            return
+        b = np.ascontiguousarray(bf_counts, np.float64)
+        assert b.shape == tuple(self.shape), (b.shape, self.shape)
+        lib().orc_set_bf_assist(self._h, b.ctypes.data_as(_D))
 
     def prepare(self, vol=None):
         """volume init, nuisance init, forward projection, weights (execute() up to :691)."""

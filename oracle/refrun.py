@@ -143,9 +143,10 @@ def _run(exe, args, workdir, seed, threads, timeout):
 
 def run_haadf(workdir, counts, tilts, thickness, diffuseness, sigma_x, outer, inner=1,
               stop=0.0, target_gain=1.0, seed=12345, threads=1, initial=None, levels=1,
-              subvolume=None, extra=(), timeout=1800):
+              subvolume=None, extra=(), timeout=1800, brightfield=None):
     """Run HAADFReconstruction on counts[theta][r][t]; returns the finest level's outputs.
-    `initial`: starting volume [y][x][z] (the --initial_recon_file layout)."""
+    `initial`: starting volume [y][x][z] (the --initial_recon_file layout); `brightfield`:
+    bright-field counts of the same size (--brightfield)."""
     if os.path.exists(workdir):
         shutil.rmtree(workdir)
     os.makedirs(workdir)
@@ -161,6 +162,9 @@ def run_haadf(workdir, counts, tilts, thickness, diffuseness, sigma_x, outer, in
     if initial is not None:
         np.ascontiguousarray(initial, "<f8").tofile(os.path.join(workdir, "init.bin"))
         args += ["--initial_recon_file", os.path.join(workdir, "init.bin")]
+    if brightfield is not None:
+        write_mrc(os.path.join(workdir, "bf.mrc"), brightfield, tilts)
+        args += ["--brightfield", os.path.join(workdir, "bf.mrc")]
     _run(HAADF_EXE, args, workdir, seed, threads, timeout)
     return read_outputs(os.path.join(workdir, "out", "1x"), n_theta, n_r, n_t)
 

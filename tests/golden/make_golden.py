@@ -14,6 +14,9 @@ oracle/_ref) and runs them through oracle/refrun.py on seeded synthetic inputs:
   schedule (4 outer iterations);
 * output_headers.json -- the headers of the reference's MRC, VTK and Avizo volume files for the
   reduced HAADF case (everything but the voxel values);
+* haadf_bf_assist_small.npz -- the reduced HAADF case with a bright-field tilt series of the
+  same size (--brightfield; the bright-field counts seen through one of the case's spheres):
+  5 outer iterations;
 * haadf_cfg0.json -- the benchmark's small HAADF configuration (128 x 32 detector, 71 views over
   +-70 deg at 2 deg, thickness 32, volume 128 x 32 x 64): SHA-256 digests and sums of the
   inputs and of the reference's float64 outputs after 1, 5 and 20 outer iterations.
@@ -96,6 +99,26 @@ def haadf_small(tmp):
                         it5_offset=it5["offset"])
 
 
+def haadf_bf_assist_small(tmp):
+    """The reduced HAADF case with a bright-field tilt series of the same size (--brightfield):
+    5 outer iterations."""
+    y, ang, th = small_case()
+    bf = bright_field_series(y.shape, ang)
+    out = refrun.run_haadf(os.path.join(tmp, "hbf"), y, ang, th, 0.1, 0.2, 5, seed=HAADF_SEED,
+                           brightfield=bf)
+    np.savez_compressed(os.path.join(HERE, "haadf_bf_assist_small.npz"), counts=y, bf_counts=bf,
+                        tilts=ang, thickness=th, it5_object_yxz=out["object_yxz"],
+                        it5_gain=out["gain"], it5_offset=out["offset"])
+
+
+def bright_field_series(shape, ang, seed=5):
+    """Bright-field counts seen through the first sphere of the reduced HAADF case."""
+    rng = np.random.default_rng(seed)
+    proj = synthetic.ellipsoid_projection(ang, shape[1], shape[2],
+                                          [(-12.0, 0.0, 0.0, 10.0, 10.0, 10.0, 1.0)])
+    return np.maximum(rng.poisson(1.0e4 * np.exp(-0.02 * proj)), 1).astype(np.float32)
+
+
 def bf_small(tmp):
     c, ang, th = bf_case()
     out = refrun.run_bf(os.path.join(tmp, "bf40"), c, ang, th, 0.1, 0.02, outer=40, inner=3,
@@ -134,6 +157,7 @@ def main():
         output_headers(tmp)
         bf_small(tmp)
         haadf_cfg0(tmp)
+        haadf_bf_assist_small(tmp)
     for f in sorted(os.listdir(HERE)):
         print(f, os.path.getsize(os.path.join(HERE, f)))
     return 0

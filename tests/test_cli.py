@@ -142,3 +142,45 @@ def test_cli_bf_two_levels(cli_built, tmp_path):
     coarse = np.fromfile(out / "2x" / "ReconstructedObject.bin", "<f8")
     assert fine.size == 8 * coarse.size
     assert np.all(np.isfinite(fine)) and fine.max() > 0
+
+
+@pytest.mark.gpu
+def test_cli_haadf_with_bright_field(cli_built, tmp_path):
+    """--brightfield: the bright-field tilt series read with the sinogram's subvolume; the same
+    volume as the library run with the same files."""
+    import mbir
+    import refrun
+    g = dict(np.load(os.path.join(HERE, "golden", "haadf_bf_assist_small.npz")))
+    y, bf, ang = g["counts"], g["bf_counts"], g["tilts"]
+    refrun.write_mrc(str(tmp_path / "in.mrc"), y, ang)
+    refrun.write_mrc(str(tmp_path / "bf.mrc"), bf, ang)
+    n_theta, n_r, n_t = y.shape
+    sv = (0, 0, 0, n_r - 1, n_t - 1, n_theta - 1)
+    out = tmp_path / "out"
+    r = run("HAADFReconstruction", "-s", str(tmp_path / "in.mrc"), "--brightfield",
+            str(tmp_path / "bf.mrc"), "--outputfile", str(out / "recon.mrc"), "--subvolume",
+            ",".join(str(v) for v in sv), "--thickness", "16", "--diffuseness", "0.1",
+            "--sigma_x", "0.2", "--num_resolutions", "1", "--outer_iterations", "2",
+            "--inner_iterations", "1", "--stop_threshold", "0", "--target_gain", "1")
+    assert r.returncode == 0, r.stdout + r.stderr
+    p = mbir.default_params()
+    p.sample_thickness = 16.0
+    p.diffuseness = 0.1
+    p.sigma_x = 0.2
+    p.num_resolutions = 1
+    p.outer_iterations = 2
+    p.inner_iterations = 1
+    p.stop_threshold = 0.0
+    p.target_gain = 1.0
+    p.float_params = 1
+    p.use_subvolume = 1
+    for i, v in enumerate(sv):
+        p.subvolume[i] = v
+    with mbir.Engine(p) as e:
+        e.load_mrc(str(tmp_path / "in.mrc"))
+        e.load_bright_field_mrc(str(tmp_path / "bf.mrc"))
+        e.run()
+        vol = e.volume()
+        nz, nx, ny = e.dims()[:3]
+    obj = np.fromfile(out / "1x" / "ReconstructedObject.bin", "<f8").reshape(ny, nx, nz)
+    np.testing.assert_array_equal(np.transpose(obj, (2, 1, 0)), vol.astype(np.float64))

@@ -10,6 +10,9 @@ the MRC header (float 1e-9 m * 1e9).  Tolerances:
   HAADF reference order, 5 outer iterations with gain,
     offset and variance estimation (FP64 exact mode)      ||dx|| / ||x||      <= 1e-4
     gains, offsets                                       max relative        <= 1e-6
+  HAADF with a bright-field tilt series, 5 outer iterations
+    (FP64 exact mode)                                     ||dx|| / ||x||      <= 1e-4
+    offsets                                              max relative        <= 1e-6
   bright field, first 6 NHICD calls of the Bragg schedule
     with offset/variance updates (FP64 exact mode)        ||dx|| / ||x||      <= 1e-6
     offsets, variance                                    max relative        <= 1e-9
@@ -124,3 +127,20 @@ def test_reference_order_bf_six_calls(lib_built):
     _, off, var = e.nuisance()
     np.testing.assert_allclose(off, g["c6_offset"], rtol=1e-9)
     np.testing.assert_allclose(var, g["c6_variance"], rtol=1e-9)
+
+
+def test_reference_order_haadf_with_bright_field(lib_built):
+    """HAADF with a bright-field tilt series (the reference's --brightfield run), reference-exact
+    FP64 mode, 5 outer iterations."""
+    mbir = lib_built
+    g = load("haadf_bf_assist_small.npz")
+    e = haadf_engine(mbir, g, 5, order_mode=1, precision=mbir.FP64, seed=12345,
+                     seed_mode=mbir.SEED_FIXED)
+    e.set_bright_field(g["bf_counts"])
+    e.run()
+    nz, nx, ny = e.dims()[:3]
+    ref = np.transpose(g["it5_object_yxz"].reshape(ny, nx, nz), (2, 1, 0))
+    assert rel(e.volume(), ref) <= 1e-4, rel(e.volume(), ref)
+    gain, off, _ = e.nuisance()
+    np.testing.assert_array_equal(gain, g["it5_gain"])  # not estimated with bright-field data
+    np.testing.assert_allclose(off, g["it5_offset"], rtol=1e-6)

@@ -9,8 +9,9 @@ pow as the reference uses, reproduces them bit for bit:
 * HAADF forward projection of a fixed volume (A matrix, detector response, voxel-line
   response, initial offsets);
 * HAADF after 5 outer iterations (ICD sweeps in the reference's visit order, jointEstimation,
-  updateWeights), and the benchmark's small HAADF configuration after 1, 5 and 20 outer
-  iterations (SHA-256 of the float64 outputs);
+  updateWeights), the same with a bright-field tilt series (--brightfield), and the benchmark's
+  small HAADF configuration after 1, 5 and 20 outer iterations (SHA-256 of the float64
+  outputs);
 * bright field after 42 NHICD calls (Bragg schedule, homogeneous and non-homogeneous lists,
   offset, variance and selector updates).
 
@@ -66,6 +67,20 @@ def test_haadf_five_outer_iterations_bitwise(oracle_mod):
     assert orc.run(12345)[0] == 5
     ny, nx, nz = orc.ny, orc.nx, orc.nz
     ref = np.transpose(g["it5_object_yxz"].reshape(ny, nx, nz), (2, 1, 0))
+    np.testing.assert_array_equal(orc.volume(), ref)
+    np.testing.assert_array_equal(orc.gain(), g["it5_gain"])
+    np.testing.assert_array_equal(orc.offset(), g["it5_offset"])
+
+
+def test_haadf_with_bright_field_five_outer_iterations_bitwise(oracle_mod):
+    """HAADF with a bright-field tilt series (--brightfield): the factor bright field +
+    BF_OFFSET in the error, theta1/theta2 and the scatter, offset-only estimation."""
+    g = load("haadf_bf_assist_small.npz")
+    orc = haadf_oracle(oracle_mod, g["counts"], g["tilts"], float(g["thickness"]), 5)
+    orc.set_bf_assist(g["bf_counts"])
+    orc.prepare()
+    assert orc.run(12345)[0] == 5
+    ref = np.transpose(g["it5_object_yxz"].reshape(orc.ny, orc.nx, orc.nz), (2, 1, 0))
     np.testing.assert_array_equal(orc.volume(), ref)
     np.testing.assert_array_equal(orc.gain(), g["it5_gain"])
     np.testing.assert_array_equal(orc.offset(), g["it5_offset"])
