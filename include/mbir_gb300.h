@@ -199,6 +199,9 @@ int32_t mbir_load_bright_field_mrc(mbir_engine* e, const char* path);
  * interpolate_initial_recon set, (N_z/2) x (N_x/2) x (N_y/2) values, each filling its 2x2x2 block
  * (InitialReconstructionBinReader.cpp:101-131; needs the sinogram set first). */
 int32_t mbir_set_initial_volume(mbir_engine* e, const float* vol, int64_t n);
+/* The same as doubles: the reference hands resolution levels the doubles of
+ * ReconstructedObject.bin, and an FP64 engine starts from them exactly. */
+int32_t mbir_set_initial_volume_f64(mbir_engine* e, const double* vol, int64_t n);
 /* Optional initial nuisance vectors (length n_theta each; NULL keeps the default). */
 int32_t mbir_set_initial_nuisance(mbir_engine* e, const double* gains, const double* offsets,
                                   const double* variances);
@@ -218,7 +221,10 @@ int32_t mbir_compute_cost(mbir_engine* e, double* parts3, double* total);
 int32_t mbir_forward_project(mbir_engine* e);
 
 /* Read-outs (host buffers owned by the caller) */
-int32_t mbir_get_volume(mbir_engine* e, float* out, int64_t n);          /* [z][x][y] */
+int32_t mbir_get_volume(mbir_engine* e, float* out, int64_t n);
+/* The volume as doubles, [z][x][y] (an FP64 engine's values exactly; the values written to
+ * ReconstructedObject.bin). */
+int32_t mbir_get_volume_f64(mbir_engine* e, double* out, int64_t n);          /* [z][x][y] */
 int32_t mbir_get_error_sinogram(mbir_engine* e, float* out, int64_t n);  /* [theta][r][t] */
 int32_t mbir_get_projection(mbir_engine* e, float* out, int64_t n);      /* last forward projection [theta][r][t] */
 int32_t mbir_get_nuisance(mbir_engine* e, double* gains, double* offsets, double* variances);

@@ -208,19 +208,18 @@ bool make_dirs(const std::string& d) {
 
 // --initial_recon_file: doubles in y-x-z order (InitialReconstructionBinReader.cpp:101-155),
 // returned as [z][x][y] floats of the given size
-bool read_object_bin(const std::string& path, int n_z, int n_x, int n_y, std::vector<float>& out) {
+bool read_object_bin(const std::string& path, int n_z, int n_x, int n_y, std::vector<double>& out) {
   FILE* f = std::fopen(path.c_str(), "rb");
   if (!f) return false;
   std::vector<double> buf(static_cast<size_t>(n_z) * n_x * n_y);
   const size_t got = std::fread(buf.data(), sizeof(double), buf.size(), f);
   std::fclose(f);
   if (got != buf.size()) return false;
-  out.assign(buf.size(), 0.f);
+  out.assign(buf.size(), 0.0);
   size_t k = 0;
   for (int y = 0; y < n_y; ++y)
     for (int x = 0; x < n_x; ++x)
-      for (int z = 0; z < n_z; ++z)
-        out[(static_cast<size_t>(z) * n_x + x) * n_y + y] = static_cast<float>(buf[k++]);
+      for (int z = 0; z < n_z; ++z) out[(static_cast<size_t>(z) * n_x + x) * n_y + y] = buf[k++];
   return true;
 }
 
@@ -311,7 +310,7 @@ int main(int argc, char** argv) {
   // p = diffuseness + 1 in float, as the pipeline computes it
   const double pq = static_cast<double>(static_cast<float>(p.diffuseness) + 1.0f);
   const auto t0 = std::chrono::steady_clock::now();
-  std::vector<float> prev;
+  std::vector<double> prev;
   int prev_dims[3] = {0, 0, 0};
   std::vector<double> g, o, v;
   std::vector<std::string> temp_files;
@@ -348,16 +347,16 @@ int main(int argc, char** argv) {
     if (rc == MBIR_OK && i == 0 && a.count("initial_recon_file") &&
         !a["initial_recon_file"].empty()) {
       const int f = q.interpolate_initial_recon ? 2 : 1;
-      std::vector<float> init;
+      std::vector<double> init;
       if (!read_object_bin(a["initial_recon_file"], d[0] / f, d[1] / f, d[2] / f, init)) {
         std::printf("Error opening Input file '%s'\n", a["initial_recon_file"].c_str());
         mbir_destroy(e);
         return EXIT_FAILURE;
       }
-      rc = mbir_set_initial_volume(e, init.data(), static_cast<int64_t>(init.size()));
+      rc = mbir_set_initial_volume_f64(e, init.data(), static_cast<int64_t>(init.size()));
     }
     if (rc == MBIR_OK && i > 0) {
-      rc = mbir_set_initial_volume(e, prev.data(), static_cast<int64_t>(prev.size()));
+      rc = mbir_set_initial_volume_f64(e, prev.data(), static_cast<int64_t>(prev.size()));
       if (rc == MBIR_OK) rc = mbir_set_initial_nuisance(e, g.data(), o.data(), v.data());
     }
     std::printf("%dx: reconstructing %d x %d x %d voxels (z, x, y) from %d views\n", interp >> i,
@@ -376,11 +375,11 @@ int main(int argc, char** argv) {
         temp_files.push_back(level_dir + "/" + n);
     }
     if (rc == MBIR_OK) {
-      prev.assign(static_cast<size_t>(d[0]) * d[1] * d[2], 0.f);
+      prev.assign(static_cast<size_t>(d[0]) * d[1] * d[2], 0.0);
       g.assign(d[3], 0.0);
       o.assign(d[3], 0.0);
       v.assign(d[3], 0.0);
-      rc = mbir_get_volume(e, prev.data(), static_cast<int64_t>(prev.size()));
+      rc = mbir_get_volume_f64(e, prev.data(), static_cast<int64_t>(prev.size()));
       if (rc == MBIR_OK) rc = mbir_get_nuisance(e, g.data(), o.data(), v.data());
       prev_dims[0] = d[0];
       prev_dims[1] = d[1];

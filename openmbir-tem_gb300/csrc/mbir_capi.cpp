@@ -200,6 +200,12 @@ int32_t mbir_load_bright_field_mrc(mbir_engine* e, const char* path) {
 int32_t mbir_set_initial_volume(mbir_engine* e, const float* vol, int64_t n) {
   return guarded(e, [&](mbir::Engine& m) { return m.set_initial_volume(vol, n); });
 }
+int32_t mbir_set_initial_volume_f64(mbir_engine* e, const double* vol, int64_t n) {
+  return guarded(e, [&](mbir::Engine& m) { return m.set_initial_volume_f64(vol, n); });
+}
+int32_t mbir_get_volume_f64(mbir_engine* e, double* out, int64_t n) {
+  return guarded(e, [&](mbir::Engine& m) { return m.get_volume_f64(out, n); });
+}
 int32_t mbir_set_initial_nuisance(mbir_engine* e, const double* g, const double* o,
                                   const double* v) {
   return guarded(e, [&](mbir::Engine& m) { return m.set_initial_nuisance(g, o, v); });
@@ -337,7 +343,7 @@ int32_t mbir_run_multires(const mbir_params* p, const float* counts, const float
   const mbir_params top = with_float_params(*p);
   p = &top;
   const int levels = p->num_resolutions > 0 ? p->num_resolutions : 1;
-  std::vector<float> prev;
+  std::vector<double> prev;
   int pdims[3] = {0, 0, 0};
   std::vector<double> g(n_theta), o(n_theta), v(n_theta);
   bool have_nuis = false;
@@ -357,23 +363,25 @@ int32_t mbir_run_multires(const mbir_params* p, const float* counts, const float
       if ((rc = eng.dims(d))) return rc;
       if (have_nuis && (rc = eng.set_initial_nuisance(g.data(), o.data(), v.data()))) return rc;
       if (i > 0) {
-        // 2x voxel replication of the previous level (InterpFlag = 1)
-        std::vector<float> up(static_cast<size_t>(d[0]) * d[1] * d[2], 0.f);
+        // 2x voxel replication of the previous level (InterpFlag = 1), in FP64 as the
+        // reference reads ReconstructedObject.bin
+        std::vector<double> up(static_cast<size_t>(d[0]) * d[1] * d[2], 0.0);
         const int ze = d[0] / 2, xe = d[1] / 2, ye = d[2] / 2;
         for (int y = 0; y < ye && y < pdims[2]; y++)
           for (int x = 0; x < xe && x < pdims[1]; x++)
             for (int z = 0; z < ze && z < pdims[0]; z++) {
-              const float b = prev[(static_cast<size_t>(z) * pdims[1] + x) * pdims[2] + y];
+              const double b = prev[(static_cast<size_t>(z) * pdims[1] + x) * pdims[2] + y];
               for (int a = 0; a < 2; a++)
                 for (int c = 0; c < 2; c++)
                   for (int r = 0; r < 2; r++)
                     up[(static_cast<size_t>(2 * z + a) * d[1] + 2 * x + c) * d[2] + 2 * y + r] = b;
             }
-        if ((rc = eng.set_initial_volume(up.data(), static_cast<int64_t>(up.size())))) return rc;
+        if ((rc = eng.set_initial_volume_f64(up.data(), static_cast<int64_t>(up.size()))))
+          return rc;
       }
       if ((rc = eng.run())) return rc;
-      prev.assign(static_cast<size_t>(d[0]) * d[1] * d[2], 0.f);
-      if ((rc = eng.get_volume(prev.data(), static_cast<int64_t>(prev.size())))) return rc;
+      prev.assign(static_cast<size_t>(d[0]) * d[1] * d[2], 0.0);
+      if ((rc = eng.get_volume_f64(prev.data(), static_cast<int64_t>(prev.size())))) return rc;
       pdims[0] = d[0];
       pdims[1] = d[1];
       pdims[2] = d[2];
@@ -391,7 +399,7 @@ int32_t mbir_run_multires(const mbir_params* p, const float* counts, const float
   }
   if (out) {
     if (n < static_cast<int64_t>(nv)) return MBIR_EINVAL;
-    std::memcpy(out, prev.data(), nv * sizeof(float));
+    for (size_t i = 0; i < nv; i++) out[i] = static_cast<float>(prev[i]);
   }
   return MBIR_OK;
 }

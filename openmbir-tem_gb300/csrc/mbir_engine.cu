@@ -231,7 +231,10 @@ int Engine::set_bright_field(const float* counts, int n_theta, int n_r, int n_t)
   return MBIR_OK;
 }
 
-int Engine::set_initial_volume(const float* vol, int64_t n) {
+// --initial_recon_file (InitialReconstructionBinReader.cpp:73-135): the starting volume, as
+// doubles (the reference hands levels the doubles of ReconstructedObject.bin)
+template <typename T>
+int Engine::set_initial_volume_t(const T* vol, int64_t n) {
   if (!vol || n <= 0) return fail(MBIR_EINVAL, "set_initial_volume: bad arguments");
   if (!p_.interpolate_initial_recon) {
     init_vol_.assign(vol, vol + n);
@@ -250,11 +253,11 @@ int Engine::set_initial_volume(const float* vol, int64_t n) {
   if (n != static_cast<int64_t>(hz) * hx * hy)
     return fail(MBIR_EINVAL, "set_initial_volume: the interpolated initial volume must hold "
                              "(N_z/2) x (N_x/2) x (N_y/2) voxels");
-  init_vol_.assign(static_cast<size_t>(g_.n_z) * g_.n_x * g_.n_y, 0.f);
+  init_vol_.assign(static_cast<size_t>(g_.n_z) * g_.n_x * g_.n_y, 0.0);
   for (int z = 0; z < hz; z++)
     for (int x = 0; x < hx; x++)
       for (int y = 0; y < hy; y++) {
-        const float b = vol[(static_cast<size_t>(z) * hx + x) * hy + y];
+        const double b = vol[(static_cast<size_t>(z) * hx + x) * hy + y];
         for (int a = 0; a < 2; a++)
           for (int c = 0; c < 2; c++)
             for (int r = 0; r < 2; r++)
@@ -263,6 +266,13 @@ int Engine::set_initial_volume(const float* vol, int64_t n) {
       }
   host_ready_ = false;
   return MBIR_OK;
+}
+
+int Engine::set_initial_volume(const float* vol, int64_t n) {
+  return set_initial_volume_t(vol, n);
+}
+int Engine::set_initial_volume_f64(const double* vol, int64_t n) {
+  return set_initial_volume_t(vol, n);
 }
 
 int Engine::set_initial_nuisance(const double* g, const double* o, const double* v) {
@@ -812,21 +822,39 @@ int Engine::prepare() {
 
   // initial volume (InitialReconstructionInitializer::initializeData, :74-90)
   const size_t nv = static_cast<size_t>(g.n_z) * g.n_x * g.n_y;
-  std::vector<float> vol(nv);
+  std::vector<double> vol(nv);
   if (!init_vol_.empty()) {
     if (init_vol_.size() != nv) return fail(MBIR_EINVAL, "initial volume size does not match");
     vol = init_vol_;
   } else {
-    std::fill(vol.begin(), vol.end(), static_cast<float>(p_.default_recon_value));
+    std::fill(vol.begin(), vol.end(), fp64_ ? p_.default_recon_value
+                                            : static_cast<double>(static_cast<float>(
+                                                  p_.default_recon_value)));
   }
   for (int z = 0; z < g.n_z; z++)
     for (int x = 0; x < g.n_x; x++)
       if (!tab_.line_nonempty[static_cast<size_t>(z) * g.n_x + x])
-        for (int y = 0; y < g.n_y; y++) vol[(static_cast<size_t>(z) * g.n_x + x) * g.n_y + y] = 0.f;
-  cudaMemcpyAsync(d_stage_, vol.data(), sizeof(float) * nv, cudaMemcpyHostToDevice, s);
-  if ((rc = launch_vol_to_dev(d_stage_, d_x_, g.n_z, g.n_x, g.n_y, fp64_, s)))
-    return cuda_check(rc, "volume upload");
-  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "prepare sync");
+        for (int y = 0; y < g.n_y; y++) vol[(static_cast<size_t>(z) * g.n_x + x) * g.n_y + y] = 0.0;
+  if (fp64_) {
+    // the doubles as given (an FP64 engine starts exactly where the reference starts)
+    double* tmp = nullptr;
+    if (cudaMalloc(&tmp, sizeof(double) * nv) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(MBIR_ENOMEM, "volume upload: device allocation failed");
+    }
+    cudaMemcpyAsync(tmp, vol.data(), sizeof(double) * nv, cudaMemcpyHostToDevice, s);
+    rc = launch_vol64_to_dev(tmp, d_x_, g.n_z, g.n_x, g.n_y, fp64_, s);
+    const bool ok = cudaStreamSynchronize(s) == cudaSuccess;
+    cudaFree(tmp);
+    if (rc) return cuda_check(rc, "volume upload");
+    if (!ok) return cuda_check(MBIR_EDEVICE, "prepare sync");
+  } else {
+    std::vector<float> vf(vol.begin(), vol.end());
+    cudaMemcpyAsync(d_stage_, vf.data(), sizeof(float) * nv, cudaMemcpyHostToDevice, s);
+    if ((rc = launch_vol_to_dev(d_stage_, d_x_, g.n_z, g.n_x, g.n_y, fp64_, s)))
+      return cuda_check(rc, "volume upload");
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "prepare sync");
+  }
 
   // device geometry + prior constants
   dg_.n_theta = g.n_theta;
@@ -1385,6 +1413,27 @@ int Engine::get_volume(float* out, int64_t n) {
   return cudaStreamSynchronize(s) == cudaSuccess ? 0 : cuda_check(MBIR_EDEVICE, "volume read-out");
 }
 
+// The volume as doubles, [z][x][y] (an FP64 engine's values exactly)
+int Engine::get_volume_f64(double* out, int64_t n) {
+  if (state_ < 2) return fail(MBIR_ESTATE, "get_volume: nothing reconstructed");
+  const Geometry& g = g_;
+  const size_t nv = static_cast<size_t>(g.n_z) * g.n_x * g.n_y;
+  if (!out || n < static_cast<int64_t>(nv)) return fail(MBIR_EINVAL, "get_volume: buffer too small");
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  std::vector<unsigned char> raw(nv * rb_);
+  cudaMemcpyAsync(raw.data(), d_x_, raw.size(), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "volume read-out");
+  for (int y = 0; y < g.n_y; y++)
+    for (int z = 0; z < g.n_z; z++)
+      for (int x = 0; x < g.n_x; x++) {
+        const size_t i = (static_cast<size_t>(y) * g.n_z + z) * g.n_x + x;
+        const double v = fp64_ ? reinterpret_cast<const double*>(raw.data())[i]
+                               : static_cast<double>(reinterpret_cast<const float*>(raw.data())[i]);
+        out[(static_cast<size_t>(z) * g.n_x + x) * g.n_y + y] = v;
+      }
+  return MBIR_OK;
+}
+
 static int sino_readout(Engine* eng, const void* dsrc, float* stage, float* out, int64_t n,
                         const Geometry& g, int n_rp, int fp64, void* stream) {
   const size_t nh = static_cast<size_t>(g.n_theta) * g.n_r * g.n_t;
@@ -1477,15 +1526,18 @@ int Engine::write_outputs(const char* dir, const char* mrc_path, const char* vtk
   int rc = get_volume(vol.data(), static_cast<int64_t>(nv));
   if (rc) return rc;
   std::string d = dir ? dir : ".";
-  // ReconstructedObject.bin: doubles in y-x-z order (RawGeometryWriter.cpp:83-91)
+  // ReconstructedObject.bin: doubles in y-x-z order (RawGeometryWriter.cpp:83-91), an FP64
+  // engine's values exactly
   {
+    std::vector<double> v64(nv);
+    if ((rc = get_volume_f64(v64.data(), static_cast<int64_t>(nv)))) return rc;
     FILE* f = std::fopen((d + "/ReconstructedObject.bin").c_str(), "wb");
     if (!f) return fail(MBIR_EIO, "cannot write ReconstructedObject.bin");
     std::vector<double> buf;
     buf.reserve(nv);
     for (int y = 0; y < g.n_y; ++y)
       for (int x = 0; x < g.n_x; ++x)
-        for (int z = 0; z < g.n_z; z++) buf.push_back(vol[(static_cast<size_t>(z) * g.n_x + x) * g.n_y + y]);
+        for (int z = 0; z < g.n_z; z++) buf.push_back(v64[(static_cast<size_t>(z) * g.n_x + x) * g.n_y + y]);
     std::fwrite(buf.data(), sizeof(double), buf.size(), f);
     std::fclose(f);
   }

@@ -84,6 +84,10 @@ class Engine {
   int set_sinogram(const float* counts, const float* tilts_deg, int n_theta, int n_r, int n_t,
                    double delta_r, double delta_t);
   int load_mrc(const char* path);
+  int set_initial_volume_f64(const double* vol, int64_t n);
+  template <typename T>
+  int set_initial_volume_t(const T* vol, int64_t n);
+  int get_volume_f64(double* out, int64_t n);
   int read_mrc_series(const char* path, std::vector<float>& counts, std::vector<float>& tilts,
                       int& n_theta, int& n_r, int& n_t, double& dr, bool need_tilts);
   // HAADF with bright-field data (initializeBrightFieldData): a bright-field tilt series of the
@@ -201,7 +205,7 @@ class Engine {
   std::vector<float> counts_;     // [theta][r][t]
   std::vector<double> bfm_;       // [theta][r][t] bright-field count + BF_OFFSET (assisted HAADF)
   std::vector<double> tilts_;     // degrees
-  std::vector<float> init_vol_;   // optional [z][x][y]
+  std::vector<double> init_vol_;  // optional [z][x][y]
   std::vector<double> user_gain_, user_offset_, user_var_;
 
   Geometry g_;

@@ -320,6 +320,9 @@ int launch_sino_to_host(const void* dev_layout, float* host_layout, int n_theta,
                         int n_rp, int n_t, int fp64, void* stream);
 int launch_vol_to_dev(const float* zxy, void* yzx, int n_z, int n_x, int n_y, int fp64,
                       void* stream);
+// the same from an FP64 volume in device memory ([z][x][y] doubles)
+int launch_vol64_to_dev(const double* zxy, void* yzx, int n_z, int n_x, int n_y, int fp64,
+                        void* stream);
 int launch_vol_to_host(const void* yzx, float* zxy, int n_z, int n_x, int n_y, int fp64,
                        void* stream);
 int launch_error_from_projection(const void* y, const void* yest, void* e, const double* mu,

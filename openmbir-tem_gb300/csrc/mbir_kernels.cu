@@ -156,6 +156,19 @@ __global__ void vol_to_dev_kernel(const float* __restrict__ zxy, Real* __restric
   }
 }
 template <typename Real>
+__global__ void vol64_to_dev_kernel(const double* __restrict__ zxy, Real* __restrict__ yzx,
+                                    int n_z, int n_x, int n_y) {
+  const size_t total = static_cast<size_t>(n_z) * n_x * n_y;
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const int x = static_cast<int>(i % n_x);
+    const size_t rest = i / n_x;
+    const int z = static_cast<int>(rest % n_z);
+    const int y = static_cast<int>(rest / n_z);
+    yzx[i] = static_cast<Real>(zxy[(static_cast<size_t>(z) * n_x + x) * n_y + y]);
+  }
+}
+template <typename Real>
 __global__ void vol_to_host_kernel(const Real* __restrict__ yzx, float* __restrict__ zxy, int n_z,
                                    int n_x, int n_y) {
   const size_t total = static_cast<size_t>(n_z) * n_x * n_y;
@@ -408,6 +421,17 @@ int launch_vol_to_dev(const float* zxy, void* yzx, int n_z, int n_x, int n_y, in
     vol_to_dev_kernel<double><<<grid_for(n, 256), 256, 0, s>>>(zxy, RP<double>(yzx), n_z, n_x, n_y);
   else
     vol_to_dev_kernel<float><<<grid_for(n, 256), 256, 0, s>>>(zxy, RP<float>(yzx), n_z, n_x, n_y);
+  return ok_or(cudaGetLastError());
+}
+int launch_vol64_to_dev(const double* zxy, void* yzx, int n_z, int n_x, int n_y, int fp64,
+                        void* stream) {
+  const size_t n = static_cast<size_t>(n_z) * n_x * n_y;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (fp64)
+    vol64_to_dev_kernel<double><<<grid_for(n, 256), 256, 0, s>>>(zxy, RP<double>(yzx), n_z, n_x,
+                                                                  n_y);
+  else
+    vol64_to_dev_kernel<float><<<grid_for(n, 256), 256, 0, s>>>(zxy, RP<float>(yzx), n_z, n_x, n_y);
   return ok_or(cudaGetLastError());
 }
 int launch_vol_to_host(const void* yzx, float* zxy, int n_z, int n_x, int n_y, int fp64,

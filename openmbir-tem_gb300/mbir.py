@@ -128,6 +128,8 @@ SIGNATURES = {
     "mbir_set_sinogram": (C.c_int32, [C.c_void_p, _F, _F, C.c_int32, C.c_int32, C.c_int32,
                                       C.c_double, C.c_double]),
     "mbir_load_sinogram_mrc": (C.c_int32, [C.c_void_p, C.c_char_p]),
+    "mbir_set_initial_volume_f64": (C.c_int32, [C.c_void_p, _D, C.c_int64]),
+    "mbir_get_volume_f64": (C.c_int32, [C.c_void_p, _D, C.c_int64]),
     "mbir_set_bright_field": (C.c_int32, [C.c_void_p, _F, C.c_int32, C.c_int32, C.c_int32]),
     "mbir_load_bright_field_mrc": (C.c_int32, [C.c_void_p, C.c_char_p]),
     "mbir_set_initial_volume": (C.c_int32, [C.c_void_p, _F, C.c_int64]),
@@ -348,6 +350,11 @@ class Engine:
         return tuple(int(v) for v in d)
 
     def set_initial_volume(self, vol):
+        """[z][x][y]; float64 arrays go through the FP64 entry point (exact for FP64 engines)."""
+        if np.asarray(vol).dtype == np.float64:
+            v = np.ascontiguousarray(vol, dtype=np.float64)
+            return self._check(lib().mbir_set_initial_volume_f64(self._h, v.ctypes.data_as(_D),
+                                                                 v.size))
         vol = np.ascontiguousarray(vol, dtype=np.float32)
         return self._check(lib().mbir_set_initial_volume(self._h, _fp(vol), vol.size))
 
@@ -387,6 +394,13 @@ class Engine:
         nz, nx, ny = self.dims()[:3]
         out = np.empty((nz, nx, ny), np.float32)
         self._check(lib().mbir_get_volume(self._h, _fp(out), out.size))
+        return out
+
+    def volume64(self):
+        """The volume as doubles (an FP64 engine's values exactly)."""
+        nz, nx, ny = self.dims()[:3]
+        out = np.empty((nz, nx, ny), np.float64)
+        self._check(lib().mbir_get_volume_f64(self._h, out.ctypes.data_as(_D), out.size))
         return out
 
     def _sino(self, fn):

@@ -17,6 +17,9 @@ oracle/_ref) and runs them through oracle/refrun.py on seeded synthetic inputs:
 * haadf_bf_assist_small.npz -- the reduced HAADF case with a bright-field tilt series of the
   same size (--brightfield; the bright-field counts seen through one of the case's spheres):
   5 outer iterations;
+* bf_multires_small.npz -- the reduced bright-field case with 12 detector rows over two
+  resolution levels (coarse 2x, then 1x), 2 outer iterations with 2 inner calls at the coarse
+  level;
 * haadf_cfg0.json -- the benchmark's small HAADF configuration (128 x 32 detector, 71 views over
   +-70 deg at 2 deg, thickness 32, volume 128 x 32 x 64): SHA-256 digests and sums of the
   inputs and of the reference's float64 outputs after 1, 5 and 20 outer iterations.
@@ -111,6 +114,19 @@ def haadf_bf_assist_small(tmp):
                         it5_gain=out["gain"], it5_offset=out["offset"])
 
 
+def bf_multires_small(tmp):
+    """The reduced bright-field case (12 detector rows) over two resolution levels (coarse 2x,
+    then 1x), 2 outer iterations with 2 inner calls at the coarse level.  (The reference's HAADF
+    program stops at its second level: it reads a FinalVariances.bin that its first level does
+    not write.)"""
+    c, ang, th = bf_case(n_t=12)
+    out = refrun.run_bf(os.path.join(tmp, "bmr"), c, ang, th, 0.1, 0.02, outer=2, inner=2,
+                        seed=BF_SEED, levels=2)
+    np.savez_compressed(os.path.join(HERE, "bf_multires_small.npz"), counts=c, tilts=ang,
+                        thickness=th, object_yxz=out["object_yxz"], offset=out["offset"],
+                        variance=out["variance"])
+
+
 def bright_field_series(shape, ang, seed=5):
     """Bright-field counts seen through the first sphere of the reduced HAADF case."""
     rng = np.random.default_rng(seed)
@@ -158,6 +174,7 @@ def main():
         bf_small(tmp)
         haadf_cfg0(tmp)
         haadf_bf_assist_small(tmp)
+        bf_multires_small(tmp)
     for f in sorted(os.listdir(HERE)):
         print(f, os.path.getsize(os.path.join(HERE, f)))
     return 0

@@ -13,6 +13,8 @@ the MRC header (float 1e-9 m * 1e9).  Tolerances:
   HAADF with a bright-field tilt series, 5 outer iterations
     (FP64 exact mode)                                     ||dx|| / ||x||      <= 1e-4
     offsets                                              max relative        <= 1e-6
+  bright field over two resolution levels (coarse 2x then
+    1x, hand-off of volume, offsets and variances)          ||dx|| / ||x||      <= 1e-4
   bright field, first 6 NHICD calls of the Bragg schedule
     with offset/variance updates (FP64 exact mode)        ||dx|| / ||x||      <= 1e-6
     offsets, variance                                    max relative        <= 1e-9
@@ -144,3 +146,32 @@ def test_reference_order_haadf_with_bright_field(lib_built):
     gain, off, _ = e.nuisance()
     np.testing.assert_array_equal(gain, g["it5_gain"])  # not estimated with bright-field data
     np.testing.assert_allclose(off, g["it5_offset"], rtol=1e-6)
+
+
+def test_bf_two_resolution_levels(lib_built):
+    """The reference's two-level bright-field run (coarse 2x, then 1x: sigma_x scaled per level,
+    the coarse volume replicated 2x2x2 and the offsets and variances handed on), reference-exact
+    FP64 mode through mbir_run_multires."""
+    mbir = lib_built
+    g = load("bf_multires_small.npz")
+    p = mbir.default_params(mbir.BF)
+    p.sample_thickness = float(g["thickness"])
+    p.diffuseness = 0.1
+    p.sigma_x = 0.02
+    p.num_resolutions = 2
+    p.outer_iterations = 2
+    p.inner_iterations = 2
+    p.stop_threshold = 0.0
+    p.use_default_offset = 1
+    p.default_dosage = 1.0e4
+    p.bragg_threshold = 3.0
+    p.extend_object = 1
+    p.float_params = 1
+    p.order_mode = 1
+    p.precision = mbir.FP64
+    p.seed = 777
+    p.seed_mode = mbir.SEED_FIXED
+    vol = mbir.run_multires(p, g["counts"], g["tilts"], refrun.REF_DELTA, refrun.REF_DELTA)
+    nz, nx, ny = vol.shape
+    ref = np.transpose(g["object_yxz"].reshape(ny, nx, nz), (2, 1, 0))
+    assert rel(vol, ref) <= 1e-4, rel(vol, ref)
