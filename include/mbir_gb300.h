@@ -122,8 +122,10 @@ typedef struct mbir_params {
                                  build, BFConstants.h), 0 = every voxel line in each call */
   int32_t lane_shape;         /* FP32 voxel-group shape: 0 = autotuned at prepare; 1 = 16 lanes x
                                  4 views (<= 64 views), 2 = 32 x 2 (<= 64), 3 = 32 x 3 (<= 96),
-                                 4 = 32 x 5 (<= 160).  Results depend on the shape in the last bits
-                                 (summation order); fix it for bit-reproducible runs. */
+                                 4 = 32 x 5 (<= 160), 5 = 32 x 8 (161-256 views; slices in HBM,
+                                 taken by default there).  Results depend on the shape in the last
+                                 bits (summation order); fix it for bit-reproducible runs.  Above
+                                 160 views: parallel order only, no batch. */
   int32_t call_schedule;      /* BF NHICD calls (FP32, parallel order): 0 = colour the call's
                                  conflict graph and run the colour classes in turn (one barrier
                                  per class; the visit order is colour by colour), 1 = walk the

@@ -18,6 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmbir_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["mbir_sweep_f32.cu", "mbir_sweep_f32_bf.cu", "mbir_sweep_f32_hbm.cu",
+           "mbir_sweep_f32_hbm_bf.cu",
            "mbir_sweep_f32_batch3.cu", "mbir_sweep_f32_batch5.cu", "mbir_sweep_f64.cu",
            "mbir_kernels.cu", "mbir_bfassist.cu",
            "mbir_exact.cu", "mbir_bf.cu", "mbir_noalloc.cu",

@@ -196,7 +196,7 @@ int Engine::set_sinogram(const float* counts, const float* tilts_deg, int n_thet
       !(delta_t > 0))
     return fail(MBIR_EINVAL, "set_sinogram: bad arguments");
   if (n_theta > 32 * kMaxViewsPerLane)
-    return fail(MBIR_ENOTSUP, "set_sinogram: more than 160 views");
+    return fail(MBIR_ENOTSUP, "set_sinogram: more than 256 views");
   if (n_r > 65535 || n_t > 65535) return fail(MBIR_EINVAL, "set_sinogram: detector too large");
   g_ = Geometry();
   g_.n_theta = n_theta;
@@ -606,7 +606,9 @@ int Engine::alloc_device() {
   if (n_sp_ > 0 && n_sp_ % 128 == 0) n_sp_ += 16;
   smem_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, n_rs_, t_rows_, bins_, fp64_, n_sp_);
   smem_sched_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, n_rs_, t_rows_, bins_, fp64_, n_sp_, true);
-  stage_ = smem_bytes_ <= static_cast<size_t>(max_smem) && p_.slice_staging == 0;
+  // above 160 views the sweeps keep the slices in HBM (32 lanes x 8 views)
+  stage_ = smem_bytes_ <= static_cast<size_t>(max_smem) && p_.slice_staging == 0 &&
+           g.n_theta <= kMaxViewsShaped;
   if (!stage_) {
     smem_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, 0, t_rows_, bins_, fp64_, 0);
     smem_sched_bytes_ = sweep_smem_bytes(g.n_theta, g.n_x, 0, t_rows_, bins_, fp64_, 0, true);
@@ -745,6 +747,8 @@ int Engine::build_host() {
 int Engine::prepare() {
   if (state_ < 1) return fail(MBIR_ESTATE, "prepare: no sinogram");
   if (state_ >= 2) release();
+  if (p_.order_mode == MBIR_ORDER_REFERENCE && g_.n_theta > kMaxViewsShaped)
+    return fail(MBIR_ENOTSUP, "prepare: the reference-order modes take at most 160 views");
   int rc;
   if ((rc = build_host())) return rc;
   if ((rc = alloc_device())) return rc;
@@ -900,7 +904,9 @@ int Engine::prepare() {
   sweeps_done_ = 0;
   // voxel-group shape: the requested one when it covers the views, else the default
   shape_ = 0;
-  if (p_.lane_shape >= 1 && p_.lane_shape <= 4 && g.n_theta <= shape_max_views(p_.lane_shape))
+  if (((p_.lane_shape >= 1 && p_.lane_shape <= 4) ||
+       (p_.lane_shape == 5 && g.n_theta > kMaxViewsShaped)) &&
+      g.n_theta <= shape_max_views(p_.lane_shape))
     shape_ = p_.lane_shape;
   if (shape_ == 0) {
     const int d = lane_shape(g.n_theta);
@@ -1135,6 +1141,8 @@ int Engine::batch_args(int outer, int inner, SweepArgs* out, size_t* smem_needed
     return fail(MBIR_ENOTSUP, "batch: FP32 parallel-order engines only");
   if (bright_field_assisted())
     return fail(MBIR_ENOTSUP, "batch: HAADF with bright-field data runs alone");
+  if (g_.n_theta > kMaxViewsShaped)
+    return fail(MBIR_ENOTSUP, "batch: series of at most 160 views");
   const Geometry& g = g_;
   std::vector<int32_t> rows;
   row_order_for_sweep(sweeps_done_, rows);

@@ -15,15 +15,22 @@
 
 namespace mbir {
 
-constexpr int kMaxViewsPerLane = 5;   // n_theta <= 160
+constexpr int kMaxViewsPerLane = 8;   // n_theta <= 256 (parallel sweeps)
+// Above this many views the parallel sweeps work on the slices in HBM with 32 lanes x 8 views;
+// the reference-order kernels, the reference-exact mode and the batch take at most this many
+constexpr int kMaxViewsShaped = 160;
 
 // Voxel-group shape of the FP32 sweep kernels for n_theta views: 0 = 16 lanes x 4 views per
-// lane (two voxels per warp), 1 = 32 lanes x 3 views, 2 = 32 lanes x 5 views.
-inline int lane_shape(int n_theta) { return n_theta <= 64 ? 0 : (n_theta <= 96 ? 1 : 2); }
-// Explicit shapes of the public parameter: 1 = 16x4, 2 = 32x2, 3 = 32x3, 4 = 32x5; the largest
-// view count each covers
+// lane (two voxels per warp), 1 = 32 lanes x 3 views, 2 = 32 lanes x 5 views, 3 = 32 lanes x 8
+// views.
+inline int lane_shape(int n_theta) {
+  return n_theta <= 64 ? 0 : (n_theta <= 96 ? 1 : (n_theta <= kMaxViewsShaped ? 2 : 3));
+}
+// Explicit shapes of the public parameter: 1 = 16x4, 2 = 32x2, 3 = 32x3, 4 = 32x5, 5 = 32x8
+// (slices in HBM); the largest view count each covers
 inline int shape_max_views(int shape) {
-  return shape == 1 ? 64 : shape == 2 ? 64 : shape == 3 ? 96 : shape == 4 ? 160 : 0;
+  return shape == 1 ? 64 : shape == 2 ? 64 : shape == 3 ? 96 : shape == 4 ? 160
+                                                                          : shape == 5 ? 256 : 0;
 }
 constexpr int kWarps = 16;            // warps per ICD block
 constexpr int kMaxTRows = 4;          // t rows a voxel slice may touch
@@ -298,6 +305,7 @@ int launch_sweep_f32_smem(const SweepArgs& a, int nb, size_t smem_bytes, void* s
 int launch_sweep_f32_smem_haadf(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_sweep_f32_smem_bf(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 int launch_sweep_f32_hbm(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
+int launch_sweep_f32_hbm_bf(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);
 // A-column table [n_z*n_x][n_theta][acol_width(nb)] of the FP32 sweep (level-scheduled calls)
 int launch_acol_f32(const DevGeom& g, const DevTables& tab, int nb, float4* out, void* stream);
 int launch_sweep_f64(const SweepArgs& a, int nb, size_t smem_bytes, void* stream);

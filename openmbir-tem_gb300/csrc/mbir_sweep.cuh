@@ -1485,8 +1485,18 @@ template <bool STAGE, bool BF>
 int launch_sweep_f32_pick(const SweepArgs& a, int nb, size_t smem, cudaStream_t s) {
   // explicit shape (1..4) when it covers the views, else the default for the view count
   int shape = a.shape;
-  if (shape < 1 || shape > 4 || a.g.n_theta > shape_max_views(shape))
+  if (shape < 1 || shape > 5 || a.g.n_theta > shape_max_views(shape))
     shape = 1 + (lane_shape(a.g.n_theta) == 0 ? 0 : lane_shape(a.g.n_theta) + 1);
+  if constexpr (!STAGE) {  // more than 160 views: 32 lanes x 8 views, slices in HBM
+    if (shape == 5) {
+      if (nb == 3) return launch_sweep_t<float, 3, 32, 8, STAGE, BF>(a, smem, s);
+      if (nb == 5) return launch_sweep_t<float, 5, 32, 8, STAGE, BF>(a, smem, s);
+      if (nb == 9) return launch_sweep_t<float, 9, 32, 8, STAGE, BF>(a, smem, s);
+      return -7;
+    }
+  } else {
+    if (shape == 5) return -7;
+  }
   if (nb == 9) return launch_sweep_t<float, 9, 32, 5, STAGE, BF>(a, smem, s);
   if (nb == 3) {
     if (shape == 1) return launch_sweep_t<float, 3, 16, 4, STAGE, BF>(a, smem, s);

@@ -8,6 +8,13 @@ int launch_sweep_f64(const SweepArgs& a, int nb, size_t smem, void* stream) {
   using namespace sweep;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const bool st = a.smem_rows != 0;
+  if (a.g.n_theta > kMaxViewsShaped) {  // 32 lanes x 8 views, slices in HBM
+    if (st) return -7;
+    if (nb == 3) return launch_sweep_m<double, 3, 32, 8, false>(a, smem, s);
+    if (nb == 5) return launch_sweep_m<double, 5, 32, 8, false>(a, smem, s);
+    if (nb == 9) return launch_sweep_m<double, 9, 32, 8, false>(a, smem, s);
+    return -7;
+  }
   if (nb == 3)
     return st ? launch_sweep_m<double, 3, 32, 5, true>(a, smem, s)
               : launch_sweep_m<double, 3, 32, 5, false>(a, smem, s);

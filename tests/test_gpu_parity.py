@@ -337,6 +337,42 @@ def test_many_views_in_shared_memory(lib_built, oracle_mod):
     assert rel(e.volume(), o.volume()) <= 1e-5
 
 
+@pytest.mark.parametrize("precision,tol", [(0, 1e-5), (1, 1e-7)])
+def test_more_than_160_views(lib_built, oracle_mod, precision, tol):
+    """241 views over +-60 deg at 0.5 deg: a parallel sweep with 32 lanes x 8 views on the slices
+    in HBM, FP32 and FP64, against the oracle in the same order from the same state (the FP64
+    volume is read out in float32), then a sweep that lowers the cost; the reference-order
+    modes refuse the series."""
+    import synthetic
+    mbir = lib_built
+    ang = synthetic.tilt_angles(60.0, 0.5)
+    assert len(ang) == 241
+    proj = synthetic.ellipsoid_projection(ang, 64, 4, [(0, 0, 0, 14, 14, 8, 1.0)])
+    y, _ = synthetic.haadf_measurements(proj, seed=7)
+    case = (y, ang.astype(np.float32), 16.0)
+    e, o, p, y = pair(mbir, oracle_mod, case=case, precision=precision)
+    e.prepare()
+    st = e.status()
+    assert st.staged == 0 and (precision == 1 or st.lane_shape == 5)
+    o.prepare()
+    assert rel(e.error_sinogram(), o.error()) <= 1e-5
+    rows, stride = e.schedule(0)
+    sg = e.sweep(0, 0)
+    so = o.sweep_slices(rows, stride, 0, 0)
+    assert sg[3] == so[3] and sg[2] == so[2], (sg, so)
+    assert rel(e.volume(), o.volume()) <= tol, rel(e.volume(), o.volume())
+    assert rel(e.error_sinogram(), o.error()) <= 1e-5
+    c0 = e.cost()[0]
+    e.sweep(0, 1)
+    assert e.cost()[0] <= c0
+    e.close()
+    r = mbir.Engine(haadf_params(mbir, 16.0, order_mode=1))
+    r.set_sinogram(*case[:2])
+    with pytest.raises(mbir.MbirError):
+        r.prepare()
+    r.close()
+
+
 def test_reference_exact_mode_bitwise(lib_built, oracle_mod):
     """The reference-exact mode performs the oracle's operations in the oracle's order (powers
     by the pinned method on both sides), so after 3 outer iterations with gain/offset and
