@@ -283,6 +283,10 @@ int32_t mbir_write_outputs(mbir_engine* e, const char* dir, const char* mrc_path
  * (HAADF_ForwardModel.cpp:139-242, VTKFileWriters.hpp, AvizoUniformCoordinateWriter.cpp). */
 int32_t mbir_write_outputs_ex(mbir_engine* e, const char* dir, const char* mrc_path,
                               const char* vtk_path, const char* avizo_path);
+/* HAADF: during mbir_run, after every inner iteration, the volume as the MRC file
+ * <dir>/<outer>_<inner>_ReconstructedVolume.rec, the intermediate image the reference writes to
+ * its temporary directory (HAADF_ReconstructionEngine.cpp:757-763); NULL or "" turns it off. */
+int32_t mbir_set_intermediate_dir(mbir_engine* e, const char* dir);
 
 /* Multi-resolution pipeline (HAADF_MultiResolutionReconstruction::execute,
  * HAADF_MultiResolutionReconstruction.cpp:175-485): coarse-to-fine levels with sigma_x scaling

@@ -361,6 +361,8 @@ int main(int argc, char** argv) {
     }
     std::printf("%dx: reconstructing %d x %d x %d voxels (z, x, y) from %d views\n", interp >> i,
                 d[0], d[1], d[2], d[3]);
+    // the HAADF program's intermediate images, <outer>_<inner>_ReconstructedVolume.rec
+    if (rc == MBIR_OK && !MBIR_CLI_BF) rc = mbir_set_intermediate_dir(e, level_dir.c_str());
     if (rc == MBIR_OK) rc = mbir_run(e);
     if (rc == MBIR_OK) {
       const bool last = i == levels - 1;
@@ -373,6 +375,15 @@ int main(int argc, char** argv) {
                             "FinalOffsetParameters.bin", "FinalVariances.bin",
                             "ReconstructedSinogram.bin"})
         temp_files.push_back(level_dir + "/" + n);
+      for (int o = 0; o < q.outer_iterations; ++o)
+        for (int k = 0; k < std::max(1, q.inner_iterations); ++k) {
+          const std::string rec = level_dir + "/" + std::to_string(o) + "_" + std::to_string(k) +
+                                  "_ReconstructedVolume.rec";
+          if (FILE* f = std::fopen(rec.c_str(), "rb")) {
+            std::fclose(f);
+            temp_files.push_back(rec);
+          }
+        }
     }
     if (rc == MBIR_OK) {
       prev.assign(static_cast<size_t>(d[0]) * d[1] * d[2], 0.0);

@@ -1371,6 +1371,11 @@ int Engine::run() {
     for (int inner = 0; inner < num_iter; inner++) {
       double st[4];
       if ((rc = sweep(outer, inner, st))) return rc;
+      // the intermediate image of every inner iteration (HAADF_ReconstructionEngine.cpp:757-763)
+      if (!interm_dir_.empty() &&
+          (rc = write_volume_mrc(interm_dir_ + "/" + std::to_string(outer) + "_" +
+                                 std::to_string(inner) + "_ReconstructedVolume.rec")))
+        return rc;
       if (p_.cost_every_sweep && (rc = compute_cost(nullptr, nullptr))) return rc;
       status = 1;
       if (st[1] > 0 && (st[0] / st[1]) < stop) {
@@ -1525,6 +1530,46 @@ int Engine::status(mbir_status* st) const {
   return MBIR_OK;
 }
 
+int Engine::set_intermediate_dir(const char* dir) {
+  interm_dir_ = dir ? dir : "";
+  return MBIR_OK;
+}
+
+// computeOriginalXDims (_Extra.cpp:252-275): the columns whose centres lie on the detector
+static void original_x_dims(const Geometry& g, int& crop_start, int& crop_end) {
+  crop_start = 0;
+  crop_end = g.n_x;
+  for (int j = 0; j < g.n_x; j++) {
+    const double x = g.x0 + ((double)j + 0.5) * g.delta_xz;
+    if (x >= -(g.n_r * g.delta_r) / 2 && x <= (g.n_r * g.delta_r) / 2) {
+      crop_start = j;
+      break;
+    }
+  }
+  for (int j = g.n_x - 1; j >= 0; j--) {
+    const double x = g.x0 + ((double)j + 0.5) * g.delta_xz;
+    if (x >= -(g.n_r * g.delta_r) / 2 && x <= (g.n_r * g.delta_r) / 2) {
+      crop_end = j;
+      break;
+    }
+  }
+}
+
+// writeMRCFile(path, cropStart, cropEnd) of the current volume (HAADF_ForwardModel.cpp:176-245)
+int Engine::write_volume_mrc(const std::string& path) {
+  const Geometry& g = g_;
+  std::vector<float> vol(static_cast<size_t>(g.n_z) * g.n_x * g.n_y);
+  int rc = get_volume(vol.data(), static_cast<int64_t>(vol.size()));
+  if (rc) return rc;
+  int crop_start = 0, crop_end = g.n_x;
+  original_x_dims(g, crop_start, crop_end);
+  std::string err;
+  if (mrc_write_volume(path, vol.data(), g.n_z, g.n_x, g.n_y, crop_start, crop_end + 1,
+                       g.length_x, err))
+    return fail(MBIR_EIO, err);
+  return MBIR_OK;
+}
+
 int Engine::write_outputs(const char* dir, const char* mrc_path, const char* vtk_path,
                           const char* avizo_path) {
   if (state_ < 2) return fail(MBIR_ESTATE, "write_outputs: nothing reconstructed");
@@ -1579,23 +1624,10 @@ int Engine::write_outputs(const char* dir, const char* mrc_path, const char* vtk
     }
     std::fclose(f);
   }
-  // computeOriginalXDims (_Extra.cpp:252-275): the columns whose centres lie on the detector;
-  // the VTK file takes [start, end), the MRC and Avizo files [start, end] (execute :879-901)
+  // the VTK file takes [start, end) of the original x dims, the MRC and Avizo files
+  // [start, end] (execute :879-901)
   int crop_start = 0, crop_end = g.n_x;
-  for (int j = 0; j < g.n_x; j++) {
-    const double x = g.x0 + ((double)j + 0.5) * g.delta_xz;
-    if (x >= -(g.n_r * g.delta_r) / 2 && x <= (g.n_r * g.delta_r) / 2) {
-      crop_start = j;
-      break;
-    }
-  }
-  for (int j = g.n_x - 1; j >= 0; j--) {
-    const double x = g.x0 + ((double)j + 0.5) * g.delta_xz;
-    if (x >= -(g.n_r * g.delta_r) / 2 && x <= (g.n_r * g.delta_r) / 2) {
-      crop_end = j;
-      break;
-    }
-  }
+  original_x_dims(g, crop_start, crop_end);
   std::string err;
   if (vtk_path && vtk_path[0] &&
       vtk_write_volume(vtk_path, vol.data(), g.n_z, g.n_x, g.n_y, crop_start, crop_end, err))

@@ -85,6 +85,9 @@ class Engine {
                    double delta_r, double delta_t);
   int load_mrc(const char* path);
   int set_initial_volume_f64(const double* vol, int64_t n);
+  // HAADF: after every inner iteration the volume as <dir>/<outer>_<inner>_ReconstructedVolume.rec
+  int set_intermediate_dir(const char* dir);
+  int write_volume_mrc(const std::string& path);
   template <typename T>
   int set_initial_volume_t(const T* vol, int64_t n);
   int get_volume_f64(double* out, int64_t n);
@@ -204,6 +207,7 @@ class Engine {
   // host inputs
   std::vector<float> counts_;     // [theta][r][t]
   std::vector<double> bfm_;       // [theta][r][t] bright-field count + BF_OFFSET (assisted HAADF)
+  std::string interm_dir_;        // per-iteration MRC volumes (empty: none)
   std::vector<double> tilts_;     // degrees
   std::vector<double> init_vol_;  // optional [z][x][y]
   std::vector<double> user_gain_, user_offset_, user_var_;

@@ -132,6 +132,7 @@ SIGNATURES = {
     "mbir_get_volume_f64": (C.c_int32, [C.c_void_p, _D, C.c_int64]),
     "mbir_set_bright_field": (C.c_int32, [C.c_void_p, _F, C.c_int32, C.c_int32, C.c_int32]),
     "mbir_load_bright_field_mrc": (C.c_int32, [C.c_void_p, C.c_char_p]),
+    "mbir_set_intermediate_dir": (C.c_int32, [C.c_void_p, C.c_char_p]),
     "mbir_set_initial_volume": (C.c_int32, [C.c_void_p, _F, C.c_int64]),
     "mbir_set_initial_nuisance": (C.c_int32, [C.c_void_p, _D, _D, _D]),
     "mbir_get_dims": (C.c_int32, [C.c_void_p, _I]),
@@ -340,6 +341,11 @@ class Engine:
         n_theta, n_r, n_t = c.shape
         return self._check(lib().mbir_set_bright_field(self._h, c.ctypes.data_as(_F), n_theta,
                                                         n_r, n_t))
+
+    def set_intermediate_dir(self, directory):
+        """HAADF: <dir>/<outer>_<inner>_ReconstructedVolume.rec after every inner iteration."""
+        d = b"" if directory is None else str(directory).encode()
+        return self._check(lib().mbir_set_intermediate_dir(self._h, d))
 
     def load_bright_field_mrc(self, path):
         return self._check(lib().mbir_load_bright_field_mrc(self._h, str(path).encode()))

@@ -94,8 +94,12 @@ def test_cli_haadf_reconstruction_files(cli_built, tmp_path):
     am = (out / "recon.am").read_bytes()
     assert len(am) == ref["am_size"] and am.startswith(ref["am_header"].encode())
     for name in ("ReconstructedObject.bin", "FinalGainParameters.bin",
-                 "FinalOffsetParameters.bin", "FinalVariances.bin", "ReconstructedSinogram.bin"):
+                 "FinalOffsetParameters.bin", "FinalVariances.bin", "ReconstructedSinogram.bin",
+                 "0_0_ReconstructedVolume.rec"):
         assert (out / "1x" / name).exists(), name
+    # the intermediate image of the one outer iteration is the final volume in the same format
+    rec = (out / "1x" / "0_0_ReconstructedVolume.rec").read_bytes()
+    assert len(rec) == len(mrc) and rec[1024:] == mrc[1024:]
     # the same run through the library: the command line maps its flags onto these parameters
     p = mbir.default_params()
     p.sample_thickness = 16.0
