@@ -10,14 +10,15 @@
 //
 // Lines are coloured 31 at a time (a block).  First, one CTA per block computes the block's
 // conflict words from the lines' footprints (bit j of conf[i]: line j < i of the block
-// conflicts with line i; conf_p1..conf_p3[i]: line j of the block before, of the one before
-// that, and so on, kBack = 3 blocks back); this needs no colours, so every block runs in
+// conflicts with line i; conf_p1..conf_p4[i]: line j of the block before, of the one before
+// that, and so on, kBack = 4 blocks back); this needs no colours, so every block runs in
 // parallel.  Then one CTA of 1024 threads walks the blocks in order, one CTA barrier per block:
 // warp 0 colours block b while warps 1-31 bring in, one line each, block b+1's taken-colour sets
 // F (the colours of the conflicting lines of the blocks up to b+1-kBack-1, read from bit planes
-// per detector bin and per line in global memory) and conflict words.  Warp 0 adds the colours of
-// the conflicting lines of the kBack blocks before b (from the conflict words) and of the earlier
-// lines of block b itself, so the sets need only hold the older blocks.
+// per detector bin and per line in global memory) and conflict words, add the colours of the
+// conflicting lines of blocks b+2-kBack..b-1 (conflict words), and, once warp 0 has chosen block
+// b's colours (a named barrier it arrives at), those of block b.  Warp 0 adds only the colours
+// of the earlier lines of the block it colours.
 //
 // Warp 0's choice is the sequential greedy's, found in parallel: each lane (line) takes the
 // first colour free of its set, of the full classes and of the current choices of the earlier
@@ -319,36 +320,47 @@ __device__ void colour_helper(const ColourArgs& A, unsigned char* smem) {
   }
 }
 
-// One warp, line j of the next block: the colours of its conflicting lines in the blocks before
-// the previous one (conflict words b[d], colours c[d] a lane each, d < kBack - 1) ORed into its
-// set Fl, one word per lane after a warp reduction per word.
-static_assert(kBack == 4, "add_older's callers list the blocks bk-1..bk-3");
+// One warp, line j of the next block: the colours of its conflicting lines in N earlier blocks
+// (conflict words b[d], colours c[d] a lane each) ORed into its set Fl, one warp reduction per
+// colour word that holds one of them (the colours of a few neighbouring blocks share one or two).
+template <int N>
 __device__ __forceinline__ void add_older(unsigned long long* Fl, int W, const unsigned* b,
                                           const int* const* c) {
   const int lane = threadIdx.x & 31;
-  int q[kBack - 1];
+  int q[N];
 #pragma unroll
-  for (int d = 0; d < kBack - 1; ++d) q[d] = ((b[d] >> lane) & 1u) ? c[d][lane] : -1;
-  unsigned keep_lo = 0u, keep_hi = 0u;
-  for (int w = 0; w < W; ++w) {
+  for (int d = 0; d < N; ++d) q[d] = ((b[d] >> lane) & 1u) ? c[d][lane] : -1;
+  for (;;) {
+    int fw = 0x7fffffff;  // this lane's lowest word still to add
+#pragma unroll
+    for (int d = 0; d < N; ++d)
+      if (q[d] >= 0) fw = min(fw, q[d] >> 6);
+    const unsigned pend = __ballot_sync(0xffffffffu, fw != 0x7fffffff);
+    if (!pend) break;
+    const int w = __shfl_sync(0xffffffffu, fw, __ffs(pend) - 1);
     unsigned lo = 0u, hi = 0u;
 #pragma unroll
-    for (int d = 0; d < kBack - 1; ++d)
+    for (int d = 0; d < N; ++d)
       if (q[d] >= 0 && (q[d] >> 6) == w) {
         const int r = q[d] & 63;
         if (r < 32) lo |= 1u << r; else hi |= 1u << (r - 32);
+        q[d] = -1;
       }
     lo = __reduce_or_sync(0xffffffffu, lo);
     hi = __reduce_or_sync(0xffffffffu, hi);
-    if (lane == w) {
-      keep_lo = lo;
-      keep_hi = hi;
-    }
+    if (lane == 0 && w < W) Fl[w] |= (static_cast<unsigned long long>(hi) << 32) | lo;
   }
   __syncwarp();
-  if (lane < W && (keep_lo | keep_hi))
-    Fl[lane] |= (static_cast<unsigned long long>(keep_hi) << 32) | keep_lo;
-  __syncwarp();
+}
+
+// Named barrier 1 of the colouring CTA, once a step: warp 0 arrives when it has chosen the
+// step's colours (in shared memory), the reading warps wait there before adding them to the
+// next block's sets.  A hardware barrier that every warp reaches once per step, no spin.
+__device__ __forceinline__ void colours_chosen_arrive() {
+  asm volatile("bar.arrive 1, %0;" ::"n"(kThreads) : "memory");
+}
+__device__ __forceinline__ void colours_chosen_wait() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kThreads) : "memory");
 }
 
 template <bool PIPE>
@@ -365,7 +377,6 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
   unsigned long long* F = reinterpret_cast<unsigned long long*>(pk + footprint_ints(nt));
   int* csize = reinterpret_cast<int*>(F + 2 * kBlock * W);  // [64 W] class sizes
   __shared__ unsigned conf[2][32];            // in-block conflict words, by block parity
-  __shared__ unsigned cprev[2][32];           // words against block b-1, by parity
   __shared__ int col[kRing][32];              // colours (a lane each), block index % kRing
   __shared__ int choice[32];                  // warp 0: the current choices of a block's lines
   __shared__ int vline[3][32];
@@ -395,7 +406,6 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
     if (lane == 0) {
       vline[0][warp] = l;
       conf[0][warp] = A.conf[warp];
-      cprev[0][warp] = 0u;
     }
   }
   auto publish = [&](int b) {
@@ -425,9 +435,8 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
     if (warp == 1 && bk > 0) publish(bk - 1);
     if (warp == 0) {
       // The greedy choice of block bk.  Line i's taken colours: its set F (colours of the
-      // conflicting lines of the blocks before bk-kBack, from the planes), the colours of its
-      // conflicting lines in blocks bk-kBack..bk-1 (conflict words) and in block bk before it,
-      // and the full classes.  Fast form on a 128-colour window from base (the lowest colour
+      // conflicting lines of the blocks before bk, built by the reading warps in step bk-1),
+      // those of its conflicting lines in block bk before it, and the full classes.  Fast form on a 128-colour window from base (the lowest colour
       // free for some line; lower colours are taken or full for every line): every lane takes
       // the first free colour given the current choices of the earlier lines it conflicts
       // with, repeated until no choice changes -- line i's choice is final once lines 0..i-1
@@ -439,7 +448,6 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
       const int cap = A.class_cap > 0 ? A.class_cap : 0x7fffffff;
       const bool act = lane < m;
       const unsigned my_conf = act ? conf[fc][lane] : 0u;
-      const unsigned my_prev = act ? cprev[fc][lane] : 0u;  // block bk-1 (older ones are in F)
       int base = 64 * W;
       if (act)
         for (int k = 0; k < W; ++k) {
@@ -465,10 +473,14 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
       const int lim = A.max_colours - base;
       f0 |= u0 | (lim >= 64 ? 0ull : lim <= 0 ? ~0ull : ~0ull << lim);
       f1 |= u1 | (lim >= 128 ? 0ull : lim <= 64 ? ~0ull : ~0ull << (lim - 64));
-      auto add = [&](unsigned long long& w0, unsigned long long& w1, int c) {
-        const int r = c - base;
-        if (r >= 0 && r < 64) w0 |= 1ull << r;
-        if (r >= 64 && r < 128) w1 |= 1ull << (r - 64);
+      // colour c as its bit in the window's two words (none outside the window)
+      auto bit0 = [&](int c) {
+        const unsigned r = static_cast<unsigned>(c - base);
+        return r < 64u ? 1ull << r : 0ull;
+      };
+      auto bit1 = [&](int c) {
+        const unsigned r = static_cast<unsigned>(c - base) - 64u;
+        return r < 64u ? 1ull << r : 0ull;
       };
       // the colours of the lanes of bits b in table t, four loads in flight at a time (a bit
       // taken twice adds its colour twice, which changes nothing)
@@ -484,14 +496,10 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
           const int k3 = b ? __ffs(b) - 1 : k0;
           b &= b - 1u;
           const int c0 = t[k0], c1 = t[k1], c2 = t[k2], c3 = t[k3];
-          add(w0, w1, c0);
-          add(w0, w1, c1);
-          add(w0, w1, c2);
-          add(w0, w1, c3);
+          w0 |= (bit0(c0) | bit0(c1)) | (bit0(c2) | bit0(c3));
+          w1 |= (bit1(c0) | bit1(c1)) | (bit1(c2) | bit1(c3));
         }
       };
-      const int* cprv = col[(bk + kRing - 1) & (kRing - 1)];  // block bk-1
-      add_bits(f0, f1, my_prev, cprv);
       auto first_free = [](unsigned long long w0, unsigned long long w1) {
         return ~w0 ? __ffsll(static_cast<long long>(~w0)) - 1
                    : (~w1 ? 63 + __ffsll(static_cast<long long>(~w1)) : -1);
@@ -539,15 +547,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
         col[ccur][lane] = mine;
         __syncwarp();
       } else {
-        // sequential form: the conflicting lines' colours of block bk-1 into each line's set
-        // first (its own row), then line by line on a 64-colour window
-        unsigned long long* Fw = F + fc * kBlock * W;
-        if (act)
-          for (unsigned b = my_prev; b; b &= b - 1u) {
-            const int q = cprv[__ffs(b) - 1];
-            Fw[lane * W + (q >> 6)] |= 1ull << (q & 63);
-          }
-        __syncwarp();
+        // sequential form: line by line on a 64-colour window
         int sbase = 64 * W;
         if (act)
           for (int k = 0; k < W; ++k) {
@@ -625,29 +625,37 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
         if (PIPE && fail) atomicExch(A.abort_flag, 1);
         s_ncol[fn] = ncol_w;
       }
+      __syncwarp();
+      colours_chosen_arrive();  // block bk's colours are in col: the reading warps add them
     } else if (PIPE) {
       // warps 1-31, one line j each: block bk+1's taken-colour sets, from its helper
       const int j = warp - 1;
+      unsigned long long* Fl = F + (fn * kBlock + j) * W;
+      unsigned b1 = 0u;  // conflicts with block bk, added once warp 0 has chosen its colours
       if (j < mn) {
         const int ok = lane == 0 ? wait_flag(A, A.flags + bk + 1) : 0;
         if (__shfl_sync(0xffffffffu, ok, 0) == 0) {
           if (lane == 0) atomicOr(&s_fail, 2);
         } else {
           const int q = s + kBlock + j;
-          unsigned long long* Fl = F + (fn * kBlock + j) * W;
           if (lane < W) Fl[lane] = __ldcg(A.fsets + static_cast<size_t>(q) * W + lane);
           const unsigned bo[kBack - 1] = {A.conf_p2[q], A.conf_p3[q], A.conf_p4[q]};
           const int* co[kBack - 1] = {col[(bk + kRing - 1) & (kRing - 1)],
                                       col[(bk + kRing - 2) & (kRing - 1)],
                                       col[(bk + kRing - 3) & (kRing - 1)]};
           __syncwarp();
-          add_older(Fl, W, bo, co);
+          add_older<kBack - 1>(Fl, W, bo, co);
           if (lane == 0) {
             vline[nxt][j] = A.vis[q];
             conf[fn][j] = A.conf[q];
-            cprev[fn][j] = A.conf_p1[q];
           }
+          b1 = A.conf_p1[q];
         }
+      }
+      colours_chosen_wait();
+      if (b1) {
+        const int* co[1] = {col[ccur]};
+        add_older<1>(Fl, W, &b1, co);
       }
     } else {
       // warps 1-31, one line j each: the footprints of block bk+1's line (its line read a step
@@ -684,12 +692,16 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
         const int* co[kBack - 1] = {col[(bk + kRing - 1) & (kRing - 1)],
                                     col[(bk + kRing - 2) & (kRing - 1)],
                                     col[(bk + kRing - 3) & (kRing - 1)]};
-        add_older(F + (fn * kBlock + j) * W, W, bo, co);
+        add_older<kBack - 1>(F + (fn * kBlock + j) * W, W, bo, co);
         if (lane == 0) {
           vline[nxt][j] = l;
           conf[fn][j] = cw;
-          cprev[fn][j] = cw1;
         }
+      }
+      colours_chosen_wait();  // cw1: conflicts with block bk (zero without a line j)
+      if (cw1) {
+        const int* co[1] = {col[ccur]};
+        add_older<1>(F + (fn * kBlock + j) * W, W, &cw1, co);
       }
     }
     __threadfence_block();  // this step's plane updates land before the next step reads

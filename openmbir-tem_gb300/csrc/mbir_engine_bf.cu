@@ -565,15 +565,25 @@ int Engine::bf_call(int outer, int inner, double* st4) {
     a.smem_rows = stage_ ? 1 : 0;
     a.n_rs = stage_ ? n_rs_ : 0;
     a.err = d_err_;
+    a.shape = shape_;
     if ((rc = bf_schedule(rows, a))) return rc;
     const int n0 = (g.n_y + 1) / 2;
+    size_t smem = a.sched_lines != nullptr ? smem_sched_bytes_ : smem_bytes_;
+    if (a.sched_lines != nullptr) {
+      // room for the schedule itself (offsets and lines) after the layout, when it fits: the
+      // class steps then read it from shared memory
+      const size_t limit = static_cast<size_t>(smem_optin_limit()) - 2048;
+      const size_t nl = static_cast<size_t>(g.n_z) * g.n_x;
+      const size_t lines = p_.nhicd ? nl / kNumHomogeneous + kNumHomogeneous : nl;
+      const size_t room = (lofs_cap() + 1 + lines) * sizeof(int);
+      if (smem + room <= limit) smem += room;
+    }
     cudaEventRecord(static_cast<cudaEvent_t>(ev2_), s);
     for (int colour = 0; colour < 2; colour++) {
       a.colour = colour;
       a.n_slices = (g.n_y - colour + 1) / 2;
       a.stats = d_stats_ + (colour ? static_cast<size_t>(n0) * kStatSlots : 0);
       if (a.n_slices <= 0) continue;
-      const size_t smem = a.sched_lines != nullptr ? smem_sched_bytes_ : smem_bytes_;
       if ((rc = launch_sweep(a, nb_, smem, s))) return cuda_check(rc, "BF call launch");
     }
     cudaEventRecord(static_cast<cudaEvent_t>(ev3_), s);

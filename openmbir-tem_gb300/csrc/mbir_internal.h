@@ -32,6 +32,13 @@ inline int shape_max_views(int shape) {
   return shape == 1 ? 64 : shape == 2 ? 64 : shape == 3 ? 96 : shape == 4 ? 160
                                                                           : shape == 5 ? 256 : 0;
 }
+// The shape an FP32 sweep launch uses: the explicit one when it covers the views, else the
+// default for the view count
+inline int resolved_shape(int shape, int n_theta) {
+  if (shape < 1 || shape > 5 || n_theta > shape_max_views(shape))
+    shape = 1 + (lane_shape(n_theta) == 0 ? 0 : lane_shape(n_theta) + 1);
+  return shape;
+}
 constexpr int kWarps = 16;            // warps per ICD block
 constexpr int kMaxTRows = 4;          // t rows a voxel slice may touch
 constexpr int kStatSlots = 4;         // sum|dx| (ROI), sum|x| (ROI), zero-skipped, updated

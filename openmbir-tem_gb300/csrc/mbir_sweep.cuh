@@ -105,6 +105,11 @@ __device__ __forceinline__ void bulk_commit() {
 __device__ __forceinline__ void bulk_wait_all() {
   asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
+__device__ __forceinline__ uint32_t dynamic_smem_bytes() {
+  uint32_t v;
+  asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(v));
+  return v;
+}
 
 // ---- reductions within aligned groups of G lanes (all 32 lanes take part) -----------------
 template <int G, typename T>
@@ -942,12 +947,18 @@ __device__ __forceinline__ bool run_slice(const SweepArgs& A, int y, unsigned ch
       c.acol = A.acol;
       const int n_levels = A.sched_count != nullptr ? __ldg(A.sched_count + 1) : A.n_levels;
       const int n_sl = __ldg(A.sched_lofs + n_levels);
-      // the schedule (offsets, lines as z << 16 | x) in the row walk's shared-memory lists,
-      // which this path does not use, when it fits
+      // the schedule (offsets, lines as z << 16 | x) in shared memory when it fits: after the
+      // layout (the launch's room for it), or else in the row walk's lists, which this path
+      // does not use
+      const size_t sched_ints = static_cast<size_t>(n_levels) + 1 + n_sl;
+      const size_t dyn = dynamic_smem_bytes();
       int* s_lofs = nullptr;
       int* s_zx = nullptr;
-      if (static_cast<size_t>(n_levels) + 1 + n_sl <= (L.es - L.list) / sizeof(int)) {
+      if (L.total + sched_ints * sizeof(int) <= dyn)
+        s_lofs = reinterpret_cast<int*>(smem + L.total);
+      else if (sched_ints <= (L.es - L.list) / sizeof(int))
         s_lofs = reinterpret_cast<int*>(smem + L.list);
+      if (s_lofs != nullptr) {
         s_zx = s_lofs + n_levels + 1;
         for (int i = tid; i <= n_levels; i += nthreads) s_lofs[i] = __ldg(A.sched_lofs + i);
         for (int i = tid; i < n_sl; i += nthreads) {
@@ -1484,9 +1495,7 @@ int launch_ref_t(const RefOrderArgs& a, cudaStream_t s) {
 template <bool STAGE, bool BF>
 int launch_sweep_f32_pick(const SweepArgs& a, int nb, size_t smem, cudaStream_t s) {
   // explicit shape (1..4) when it covers the views, else the default for the view count
-  int shape = a.shape;
-  if (shape < 1 || shape > 5 || a.g.n_theta > shape_max_views(shape))
-    shape = 1 + (lane_shape(a.g.n_theta) == 0 ? 0 : lane_shape(a.g.n_theta) + 1);
+  const int shape = resolved_shape(a.shape, a.g.n_theta);
   if constexpr (!STAGE) {  // more than 160 views: 32 lanes x 8 views, slices in HBM
     if (shape == 5) {
       if (nb == 3) return launch_sweep_t<float, 3, 32, 8, STAGE, BF>(a, smem, s);
