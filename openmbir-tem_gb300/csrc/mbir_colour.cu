@@ -353,6 +353,23 @@ __device__ __forceinline__ void add_older(unsigned long long* Fl, int W, const u
   __syncwarp();
 }
 
+// One warp, line j of the next block, its set Fl complete: the lowest colour free of the set
+// and of the full classes (64 W: none) into *lowest.
+__device__ __forceinline__ void note_lowest_free(const unsigned long long* Fl, int W,
+                                                 const unsigned long long* full, int* lowest) {
+  const int lane = threadIdx.x & 31;
+  const unsigned long long t = lane < W ? (Fl[lane] | full[lane]) : ~0ull;
+  const unsigned words = __ballot_sync(0xffffffffu, ~t != 0ull);
+  if (lane == 0) {
+    int first = 64 * W;
+    if (words) {
+      const int k = __ffs(words) - 1;
+      first = 64 * k + __ffsll(static_cast<long long>(~(Fl[k] | full[k]))) - 1;
+    }
+    *lowest = first;
+  }
+}
+
 // Named barrier 1 of the colouring CTA, once a step: warp 0 arrives when it has chosen the
 // step's colours (in shared memory), the reading warps wait there before adding them to the
 // next block's sets.  A hardware barrier that every warp reaches once per step, no spin.
@@ -383,13 +400,16 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
   __shared__ int warp_sums[32];
   __shared__ unsigned long long full_s[16];
   __shared__ int s_total, s_ncol[2], s_fail;
+  __shared__ int s_first[2][32];  // each line's lowest free colour, by block parity
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   for (int c = tid; c < 64 * W; c += kThreads) csize[c] = 0;
+  if (tid < 32) s_first[0][tid] = 0;  // block 0: nothing coloured yet
   if (tid < 16) full_s[tid] = 0ull;
   if (tid == 0) {
     s_ncol[0] = 0;
     s_fail = 0;
+
   }
   const int n = A.n;  // the call's lines, ascending, in A.vis
   __syncthreads();
@@ -448,15 +468,8 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
       const int cap = A.class_cap > 0 ? A.class_cap : 0x7fffffff;
       const bool act = lane < m;
       const unsigned my_conf = act ? conf[fc][lane] : 0u;
-      int base = 64 * W;
-      if (act)
-        for (int k = 0; k < W; ++k) {
-          const unsigned long long t = Fb[lane * W + k] | full_s[k];
-          if (~t) {
-            base = 64 * k + __ffsll(static_cast<long long>(~t)) - 1;
-            break;
-          }
-        }
+      // each line's lowest free colour was noted by its reading warp as its set was completed
+      int base = act ? s_first[fc][lane] : 64 * W;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) base = min(base, __shfl_xor_sync(0xffffffffu, base, o));
       const int k0 = base >> 6, sh = base & 63;
@@ -632,6 +645,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
       const int j = warp - 1;
       unsigned long long* Fl = F + (fn * kBlock + j) * W;
       unsigned b1 = 0u;  // conflicts with block bk, added once warp 0 has chosen its colours
+      bool have = false;
       if (j < mn) {
         const int ok = lane == 0 ? wait_flag(A, A.flags + bk + 1) : 0;
         if (__shfl_sync(0xffffffffu, ok, 0) == 0) {
@@ -650,6 +664,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
             conf[fn][j] = A.conf[q];
           }
           b1 = A.conf_p1[q];
+          have = true;
         }
       }
       colours_chosen_wait();
@@ -657,6 +672,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
         const int* co[1] = {col[ccur]};
         add_older<1>(Fl, W, &b1, co);
       }
+      if (have) note_lowest_free(Fl, W, full_s, &s_first[fn][j]);
     } else {
       // warps 1-31, one line j each: the footprints of block bk+1's line (its line read a step
       // ahead) requested first, block bk-1's colours into the planes meanwhile, then block
@@ -703,6 +719,7 @@ __global__ void __launch_bounds__(kThreads, 1) colour_kernel(ColourArgs A) {
         const int* co[1] = {col[ccur]};
         add_older<1>(F + (fn * kBlock + j) * W, W, &cw1, co);
       }
+      if (j < mn) note_lowest_free(F + (fn * kBlock + j) * W, W, full_s, &s_first[fn][j]);
     }
     __threadfence_block();  // this step's plane updates land before the next step reads
     __syncthreads();

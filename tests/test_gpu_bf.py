@@ -146,17 +146,17 @@ def test_bf_calls_decrease_cost(lib_built, oracle_mod):
     assert all(b <= a for a, b in zip(costs, costs[1:])), costs
 
 
-@pytest.mark.parametrize("staging", [0, 1])
-def test_bf_level_schedule_bitwise_row_walk(lib_built, oracle_mod, staging):
+@pytest.mark.parametrize("staging,shape", [(0, 1), (1, 1), (1, 2)])
+def test_bf_level_schedule_bitwise_row_walk(lib_built, oracle_mod, staging, shape):
     """Level-scheduled NHICD calls give the row walk's bits: a run with the Bragg schedule,
     offset and variance updates and homogeneous and non-homogeneous lists, slices staged in
-    shared memory or used in place in HBM."""
+    shared memory or used in place in HBM; 16-lane and 32-lane voxel groups."""
     mbir = lib_built
     y, ang, th = bf_case()
     out = []
     for sched in (2, 1):
         p = bf_params(mbir, th, outer_iterations=3, inner_iterations=4, call_schedule=sched,
-                      slice_staging=staging, seed=7)
+                      slice_staging=staging, seed=7, lane_shape=shape)
         e = mbir.Engine(p)
         e.set_sinogram(y, ang)
         e.run()
