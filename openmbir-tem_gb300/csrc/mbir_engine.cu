@@ -917,6 +917,8 @@ int Engine::prepare() {
   if (bf_ && (rc = bf_upload())) return rc;
   if (bf_ && (rc = bf_prepare_schedule())) return rc;
   if (p_.lane_shape == 0 && (rc = autotune_shape())) return rc;
+  // everything prepare queued has run: another thread may hand the engine to a batch stream
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "prepare sync");
   return MBIR_OK;
 }
 

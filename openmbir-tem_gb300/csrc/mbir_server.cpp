@@ -1,13 +1,14 @@
 // mbir_server.cpp -- continuous-batching reconstruction server.
 //
-// Requests (a tilt series + parameters) are queued by submit(); one worker thread owns the GPU.
-// Between batched sweeps it admits queued requests in arrival order while their estimated
-// device footprint fits the memory budget and a slot is free (each admitted request is
-// prepared: upload, tables, forward projection, and stays resident), runs one outer iteration
-// for every active request (one persistent batched ICD sweep, then per-request gain/offset,
-// variance and FP64 cost), and retires requests whose relative cost change fell below their
-// tolerance (or that reached max_outer), copying their volume to host memory and freeing the
-// device memory for the next arrivals.  Latency = completion - submission.
+// Requests (a tilt series + parameters) are queued by submit().  A preparer thread admits
+// queued requests in arrival order while their estimated device footprint fits the memory
+// budget and a slot is free, and prepares each (upload, tables, forward projection, on the
+// request's own engine stream, so this overlaps the batched sweeps).  The worker thread adds
+// prepared requests to the batch between steps, runs one outer iteration for every active
+// request (one persistent batched ICD sweep, then per-request gain/offset, variance and FP64
+// cost), and retires requests whose relative cost change fell below their tolerance (or that
+// reached max_outer), copying their volume to host memory and freeing the device memory for
+// the next arrivals.  Latency = completion - submission.
 #include "mbir_server.h"
 
 #include <cuda_runtime.h>
@@ -36,6 +37,7 @@ Server::Server(int device, int64_t mem_budget, int max_active)
       budget_ = int64_t(8) << 30;
   }
   worker_ = std::thread([this] { loop(); });
+  preparer_ = std::thread([this] { prepare_loop(); });
 }
 
 Server::~Server() {
@@ -44,6 +46,7 @@ Server::~Server() {
     stop_ = true;
   }
   cv_.notify_all();
+  if (preparer_.joinable()) preparer_.join();
   if (worker_.joinable()) worker_.join();
   batch_.reset();
   for (auto& kv : all_) kv.second->engine.reset();
@@ -133,8 +136,8 @@ int64_t Server::submit(const mbir_params& p, const float* counts, const float* t
 }
 
 int Server::admit_locked(std::vector<Request*>& admitted) {
-  while (!queue_.empty() &&
-         static_cast<int>(active_.size() + admitted.size()) < max_active_) {
+  while (!queue_.empty() && static_cast<int>(active_.size() + prepared_.size() + preparing_ +
+                                             admitted.size()) < max_active_) {
     Request* r = queue_.front();
     if (used_ + static_cast<int64_t>(r->bytes) > budget_) break;  // arrival order: no overtaking
     queue_.pop_front();
@@ -144,8 +147,9 @@ int Server::admit_locked(std::vector<Request*>& admitted) {
     if (r->id < last_admitted_id_) stats_.admitted_out_of_order++;
     last_admitted_id_ = r->id;
     stats_.peak_bytes = std::max(stats_.peak_bytes, used_);
-    stats_.peak_active = std::max(stats_.peak_active,
-                                  static_cast<int32_t>(active_.size() + admitted.size()));
+    stats_.peak_active = std::max(
+        stats_.peak_active, static_cast<int32_t>(active_.size() + prepared_.size() + preparing_ +
+                                                 admitted.size()));
   }
   return 0;
 }
@@ -163,6 +167,43 @@ void Server::retire(Request* r, int code, const std::string& msg) {
     stats_.failed++;
   }
   done_cv_.notify_all();
+  cv_.notify_all();  // memory and a slot are free for the preparer
+}
+
+void Server::prepare_loop() {
+  cudaSetDevice(device_);
+  std::unique_lock<std::mutex> lk(mu_);
+  for (;;) {
+    std::vector<Request*> admitted;
+    cv_.wait(lk, [&] {
+      if (stop_) return true;
+      admit_locked(admitted);
+      return !admitted.empty();
+    });
+    if (stop_) {
+      for (Request* r : admitted) retire(r, MBIR_ESTATE, "server stopped");
+      break;
+    }
+    preparing_ += static_cast<int>(admitted.size());
+    lk.unlock();
+    std::vector<int> rcs(admitted.size());
+    std::vector<std::string> msgs(admitted.size());
+    for (size_t k = 0; k < admitted.size(); k++) {
+      Request* r = admitted[k];
+      r->t_admit = now_s();
+      rcs[k] = r->engine->prepare();
+      if (rcs[k]) msgs[k] = r->engine->last_error();
+    }
+    lk.lock();
+    preparing_ -= static_cast<int>(admitted.size());
+    for (size_t k = 0; k < admitted.size(); k++) {
+      if (rcs[k])
+        retire(admitted[k], MBIR_EDEVICE, msgs[k]);
+      else
+        prepared_.push_back(admitted[k]);
+    }
+    cv_.notify_all();
+  }
 }
 
 void Server::loop() {
@@ -170,20 +211,17 @@ void Server::loop() {
   batch_ = std::make_unique<Batch>(device_);
   std::unique_lock<std::mutex> lk(mu_);
   for (;;) {
-    cv_.wait(lk, [&] { return stop_ || !queue_.empty() || !active_.empty(); });
+    cv_.wait(lk, [&] { return stop_ || !prepared_.empty() || !active_.empty(); });
     if (stop_) break;
-    std::vector<Request*> admitted;
-    admit_locked(admitted);
+    std::vector<Request*> joining;
+    joining.swap(prepared_);
     lk.unlock();
     const double t_busy0 = now_s();
     std::vector<std::pair<Request*, std::string>> failed;
     std::vector<Request*> ok;
-    for (Request* r : admitted) {
-      r->t_admit = now_s();
-      int rc = r->engine->prepare();
-      if (rc == 0) rc = batch_->add(r->engine.get());
-      if (rc)
-        failed.emplace_back(r, r->engine->last_error());
+    for (Request* r : joining) {
+      if (batch_->add(r->engine.get()))
+        failed.emplace_back(r, batch_->last_error());
       else
         ok.push_back(r);
     }

@@ -23,7 +23,7 @@ struct Request {
   int max_outer = 20;
   double tol = 1e-4;
   // lifecycle
-  int state = 0;            // 0 queued, 1 active, 2 done, <0 error code
+  int state = 0;            // 0 queued or being prepared, 1 active, 2 done, <0 error code
   double t_submit = 0, t_admit = 0, t_done = 0;  // seconds (steady clock)
   int outer_done = 0;
   double cost = 0, prev_cost = 0;
@@ -64,6 +64,7 @@ class Server {
 
  private:
   void loop();
+  void prepare_loop();
   size_t estimate_bytes(const Request& r) const;
   int admit_locked(std::vector<Request*>& admitted);
   void retire(Request* r, int code, const std::string& msg);
@@ -78,10 +79,12 @@ class Server {
   std::condition_variable cv_, done_cv_;
   std::deque<Request*> queue_;
   std::vector<Request*> active_;
+  std::vector<Request*> prepared_;  // prepared, joining the batch at the worker's next step
+  int preparing_ = 0;               // admitted, being prepared
   std::map<int64_t, std::unique_ptr<Request>> all_;
   std::vector<double> latencies_ms_;
   bool stop_ = false;
-  std::thread worker_;
+  std::thread worker_, preparer_;
   std::unique_ptr<Batch> batch_;
   std::string err_;
   ServerStats stats_;
