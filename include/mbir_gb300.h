@@ -250,7 +250,7 @@ int32_t mbir_set_bragg_threshold(mbir_engine* e, double t);
 /* y-slab sharding of one reconstruction over several engines (one per GPU), driven by a host
  * that exchanges boundary planes and sums per-view statistics between them.  Replaces the
  * y-range task split of updateVoxels (HAADF_ReconstructionEngine_UpdateVoxels.cpp:666-723)
- * across devices instead of threads.  HAADF, parallel order.
+ * across devices instead of threads.  Parallel order (bright field below).
  *   mbir_set_slab: later colour sweeps and view sums cover slices [y0, y1) only (0, 0 = all)
  *   mbir_sweep_colour: one colour (0 even, 1 odd slices) of the parallel sweep; the row order of
  *     sweep k serves both colours and the sweep counts after colour 1
@@ -268,6 +268,30 @@ int32_t mbir_set_planes(mbir_engine* e, int32_t y, int32_t n, const float* in);
 int32_t mbir_view_sums(mbir_engine* e, int32_t kind, double* out);
 int32_t mbir_apply_nuisance(mbir_engine* e, const double* gain, const double* offset,
                             const double* variance);
+/* Bright-field slabs (BFReconstructionEngine_Extra.cpp:624-752, the y-range task split of a
+ * call, with the tasks' magnitude maps reduced afterwards, :719-752): one NHICD call is
+ *   mbir_bf_call_begin: the call's lines (next homogeneous sub-list, or the non-homogeneous
+ *     list from the magnitude map), schedule and row order; then mbir_sweep_colour (0, 1) with
+ *     the halo exchange after each colour
+ *   mbir_bf_call_magnitudes: the call's update magnitude per line [z][x] over the slab's slices
+ *     (sum |dx| in fixed point, 2^-32 units), for the host to add over slabs
+ *   mbir_bf_call_end: the magnitude map takes the summed magnitudes (null: the slab's own) and
+ *     the call is counted
+ * and after an outer iteration
+ *   mbir_bf_slab_sums: kind 2 = the offset step's numerator and denominator per view [theta][2]
+ *     (jointEstimation, BFForwardModel.cpp:390-441); kind 3 = the variance sums over selected
+ *     and rejected entries [2] (updateWeights, :447-511; scales the slab's weights by the
+ *     current variance first, so once per update), over the slab's detector rows
+ *   mbir_bf_slab_apply: the same kind's sums added over slabs: offset steps or the common
+ *     variance, then the Bragg selector (updateSelector, :517-531)
+ *   mbir_roi_sums: the stop rule's ROI sums (_Extra.cpp:1200-1248): [0] of the magnitude map,
+ *     [1] of the slab's volume (to add over slabs) */
+int32_t mbir_bf_call_begin(mbir_engine* e, int32_t outer, int32_t inner);
+int32_t mbir_bf_call_magnitudes(mbir_engine* e, uint64_t* out);
+int32_t mbir_bf_call_end(mbir_engine* e, const uint64_t* magnitudes);
+int32_t mbir_bf_slab_sums(mbir_engine* e, int32_t kind, double* out);
+int32_t mbir_bf_slab_apply(mbir_engine* e, int32_t kind, const double* sums);
+int32_t mbir_roi_sums(mbir_engine* e, double* out2);
 int32_t mbir_status_get(mbir_engine* e, mbir_status* st);
 void mbir_cancel(mbir_engine* e);
 

@@ -297,6 +297,29 @@ int32_t mbir_apply_nuisance(mbir_engine* e, const double* gain, const double* of
                             const double* variance) {
   return guarded(e, [&](mbir::Engine& m) { return m.apply_nuisance(gain, offset, variance); });
 }
+int32_t mbir_bf_call_begin(mbir_engine* e, int32_t outer, int32_t inner) {
+  return guarded(e, [&](mbir::Engine& m) { return m.bf_slab_begin(outer, inner); });
+}
+int32_t mbir_bf_call_magnitudes(mbir_engine* e, uint64_t* out) {
+  static_assert(sizeof(uint64_t) == sizeof(unsigned long long), "64-bit magnitudes");
+  return guarded(e, [&](mbir::Engine& m) {
+    return m.bf_slab_magnitudes(reinterpret_cast<unsigned long long*>(out));
+  });
+}
+int32_t mbir_bf_call_end(mbir_engine* e, const uint64_t* magnitudes) {
+  return guarded(e, [&](mbir::Engine& m) {
+    return m.bf_slab_end(reinterpret_cast<const unsigned long long*>(magnitudes));
+  });
+}
+int32_t mbir_bf_slab_sums(mbir_engine* e, int32_t kind, double* out) {
+  return guarded(e, [&](mbir::Engine& m) { return m.bf_slab_sums(kind, out); });
+}
+int32_t mbir_bf_slab_apply(mbir_engine* e, int32_t kind, const double* sums) {
+  return guarded(e, [&](mbir::Engine& m) { return m.bf_slab_apply(kind, sums); });
+}
+int32_t mbir_roi_sums(mbir_engine* e, double* out2) {
+  return guarded(e, [&](mbir::Engine& m) { return m.roi_sums(out2); });
+}
 int32_t mbir_status_get(mbir_engine* e, mbir_status* st) {
   return guarded(e, [&](mbir::Engine& m) { return m.status(st); });
 }

@@ -138,6 +138,15 @@ class Engine {
   int set_planes(int y, int n, const float* in);
   int view_sums(int kind, double* out);
   int apply_nuisance(const double* gain, const double* offset, const double* variance);
+  // bright-field slabs: an NHICD call as bf_slab_begin, sweep_colour (0, 1), bf_slab_end, the
+  // call's per-line update magnitudes and the offset and variance sums summed over slabs by
+  // the host
+  int bf_slab_begin(int outer, int inner);
+  int bf_slab_magnitudes(unsigned long long* out);  // the call's, fixed point, this slab's part
+  int bf_slab_end(const unsigned long long* mag);   // summed over slabs (null: this slab's)
+  int bf_slab_sums(int kind, double* out);   // 2: offset sums [theta][2]; 3: variance sums [2]
+  int bf_slab_apply(int kind, const double* sums);
+  int roi_sums(double* out2);  // ROI magnitude-map sum; ROI volume sum over the slab
   int status(mbir_status* st) const;
   void cancel() { cancel_.store(1); }
   int write_outputs(const char* dir, const char* mrc_path, const char* vtk_path = nullptr,
@@ -181,6 +190,9 @@ class Engine {
   void bf_schedule_readback();                    // queue the device schedule's copy to host
   void bf_schedule_settle();                      // after the stream synchronised
   BfSino bf_sino() const;
+  BfSino bf_sino_rows(int t0, int t1) const;      // detector rows [t0, t1) only
+  void slab_rows(int* t0, int* t1) const;         // detector rows of the slab's slices
+  int bf_parallel_args(int iter_nonzero, const DevBF& bfa, SweepArgs* a, size_t* smem);
   double bf_default_offset() const;
 
   int autotune_shape();  // pick the fastest voxel-group shape on a snapshot of the state
@@ -310,6 +322,9 @@ class Engine {
   std::vector<uint8_t> active_host_;
   uint32_t bf_listsel_ = 0, bf_eff_ = 0;
   int slab_y0_ = 0, slab_y1_ = 0;           // 0, 0: the whole volume
+  bool slab_call_open_ = false;             // a bright-field slab call between begin and end
+  SweepArgs slab_args_{};
+  size_t slab_smem_ = 0;
   int bf_calls_ = 0;
   double bragg_t_ = 0;
 

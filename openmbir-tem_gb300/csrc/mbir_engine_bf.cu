@@ -544,40 +544,10 @@ int Engine::bf_call(int outer, int inner, double* st4) {
       if ((rc = launch_ref_order(a, nb_, s))) return cuda_check(rc, "BF call (reference order)");
     }
   } else {
-    std::vector<int32_t> rows;
-    row_order_for_sweep(sweeps_done_, rows);
-    cudaMemcpyAsync(d_rows_, rows.data(), sizeof(int) * g.n_z, cudaMemcpyHostToDevice, s);
     SweepArgs a{};
-    a.g = dg_;
-    a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_,
-                      d_lineok_};
-    a.flt = flt_;
-    a.x = d_x_;
-    a.e = d_e_;
-    a.row_order = d_rows_;
-    a.stride = stride_;
-    a.mode = kModeICD;
-    a.fp64 = fp64_;
-    a.bf = 1;
-    a.bfa = bfa;
-    a.iter_nonzero = iter_nonzero;
-    a.zero_skipping = p_.zero_skipping;
-    a.smem_rows = stage_ ? 1 : 0;
-    a.n_rs = stage_ ? n_rs_ : 0;
-    a.err = d_err_;
-    a.shape = shape_;
-    if ((rc = bf_schedule(rows, a))) return rc;
+    size_t smem = 0;
+    if ((rc = bf_parallel_args(iter_nonzero, bfa, &a, &smem))) return rc;
     const int n0 = (g.n_y + 1) / 2;
-    size_t smem = a.sched_lines != nullptr ? smem_sched_bytes_ : smem_bytes_;
-    if (a.sched_lines != nullptr) {
-      // room for the schedule itself (offsets and lines) after the layout, when it fits: the
-      // class steps then read it from shared memory
-      const size_t limit = static_cast<size_t>(smem_optin_limit()) - 2048;
-      const size_t nl = static_cast<size_t>(g.n_z) * g.n_x;
-      const size_t lines = p_.nhicd ? nl / kNumHomogeneous + kNumHomogeneous : nl;
-      const size_t room = (lofs_cap() + 1 + lines) * sizeof(int);
-      if (smem + room <= limit) smem += room;
-    }
     cudaEventRecord(static_cast<cudaEvent_t>(ev2_), s);
     for (int colour = 0; colour < 2; colour++) {
       a.colour = colour;
@@ -610,6 +580,51 @@ int Engine::bf_call(int outer, int inner, double* st4) {
   inner_ = inner;
   if (st4)
     for (int i = 0; i < 4; i++) st4[i] = st[i];
+  return MBIR_OK;
+}
+
+// The launch arguments of a parallel-order call (the call's lines already chosen): row order
+// of this sweep, the call's schedule (device colouring or dependency levels, or none for the
+// row walk) and the launch's shared memory.
+int Engine::bf_parallel_args(int iter_nonzero, const DevBF& bfa, SweepArgs* out, size_t* smem_out) {
+  const Geometry& g = g_;
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  int rc;
+  std::vector<int32_t> rows;
+  row_order_for_sweep(sweeps_done_, rows);
+  cudaMemcpyAsync(d_rows_, rows.data(), sizeof(int) * g.n_z, cudaMemcpyHostToDevice, s);
+  SweepArgs& a = *out;
+  a = SweepArgs{};
+  a.g = dg_;
+  a.tab = DevTables{d_H_, d_bx_, d_bxd_, d_u0_, d_bz_, d_gw_, d_tfirst_, d_tcount_, d_hval_,
+                    d_lineok_};
+  a.flt = flt_;
+  a.x = d_x_;
+  a.e = d_e_;
+  a.row_order = d_rows_;
+  a.stride = stride_;
+  a.mode = kModeICD;
+  a.fp64 = fp64_;
+  a.bf = 1;
+  a.bfa = bfa;
+  a.iter_nonzero = iter_nonzero;
+  a.zero_skipping = p_.zero_skipping;
+  a.smem_rows = stage_ ? 1 : 0;
+  a.n_rs = stage_ ? n_rs_ : 0;
+  a.err = d_err_;
+  a.shape = shape_;
+  if ((rc = bf_schedule(rows, a))) return rc;
+  size_t smem = a.sched_lines != nullptr ? smem_sched_bytes_ : smem_bytes_;
+  if (a.sched_lines != nullptr) {
+    // room for the schedule itself (offsets and lines) after the layout, when it fits: the
+    // class steps then read it from shared memory
+    const size_t limit = static_cast<size_t>(smem_optin_limit()) - 2048;
+    const size_t nl = static_cast<size_t>(g.n_z) * g.n_x;
+    const size_t lines = p_.nhicd ? nl / kNumHomogeneous + kNumHomogeneous : nl;
+    const size_t room = (lofs_cap() + 1 + lines) * sizeof(int);
+    if (smem + room <= limit) smem += room;
+  }
+  *smem_out = smem;
   return MBIR_OK;
 }
 

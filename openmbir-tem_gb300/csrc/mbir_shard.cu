@@ -4,8 +4,12 @@
 // owns a contiguous block of the error sinogram: ICD needs no sinogram exchange between slabs.
 // The prior couples neighbouring slices, so after each colour phase a slab's boundary planes
 // go to its neighbours (host-mediated: get_planes / set_planes), and the per-view sums of the
-// gain/offset and variance estimates are summed over slabs before the host solves them.  Each
+// gain/offset and variance estimates are summed over slabs before the host solves them.  Bright
+// field the same way, one NHICD call at a time: the call's lines come from the magnitude map,
+// which the host keeps identical on every slab by summing each call's per-line magnitudes over
+// the slabs; the offset and variance sums and the stop rule's volume sum are summed too.  Each
 // engine holds the whole problem; only its slab is updated and summed.
+#include <algorithm>
 #include <vector>
 
 #include "mbir_engine.h"
@@ -48,11 +52,14 @@ int Engine::slab_rows_owned() {
 }
 
 // One colour of a parallel-order sweep over the slab's slices of that colour.  Both colours of
-// sweep k use the row order of sweep k; the sweep is counted after colour 1.
+// sweep k use the row order of sweep k; the sweep is counted after colour 1.  Bright field: one
+// colour of the call opened by bf_slab_begin (its lines, schedule and row order).
 int Engine::sweep_colour(int colour, int outer, int inner, double* st4) {
   if (state_ < 2) return fail(MBIR_ESTATE, "sweep_colour: call prepare first");
-  if (bf_ || p_.order_mode != MBIR_ORDER_PARALLEL)
-    return fail(MBIR_ENOTSUP, "sweep_colour: HAADF parallel order only");
+  if (p_.order_mode != MBIR_ORDER_PARALLEL || exact_)
+    return fail(MBIR_ENOTSUP, "sweep_colour: parallel order only");
+  if (bf_ && !slab_call_open_)
+    return fail(MBIR_ESTATE, "sweep_colour: open a bright-field call first (bf_call_begin)");
   if (colour != 0 && colour != 1) return fail(MBIR_EINVAL, "sweep_colour: colour is 0 or 1");
   if (int rc = slab_rows_owned()) return rc;
   const Geometry& g = g_;
@@ -60,7 +67,7 @@ int Engine::sweep_colour(int colour, int outer, int inner, double* st4) {
   const int y0 = slab_y1_ > 0 ? slab_y0_ : 0, y1 = slab_y1_ > 0 ? slab_y1_ : g.n_y;
   const int first = y0 + ((y0 & 1) != colour ? 1 : 0);
   const int n = first < y1 ? (y1 - first + 1) / 2 : 0;
-  if (colour == 0) {
+  if (colour == 0 && !bf_) {
     std::vector<int32_t> rows;
     row_order_for_sweep(sweeps_done_, rows);
     cudaMemcpyAsync(d_rows_, rows.data(), sizeof(int) * g.n_z, cudaMemcpyHostToDevice, s);
@@ -81,6 +88,11 @@ int Engine::sweep_colour(int colour, int outer, int inner, double* st4) {
   a.n_rs = stage_ ? n_rs_ : 0;
   a.shape = shape_;
   a.err = d_err_;
+  size_t smem = smem_bytes_;
+  if (bf_) {
+    a = slab_args_;
+    smem = slab_smem_;
+  }
   a.colour = colour;
   a.y_first = first;
   a.y_end = y1;
@@ -90,7 +102,7 @@ int Engine::sweep_colour(int colour, int outer, int inner, double* st4) {
   int rc;
   cudaEventRecord(static_cast<cudaEvent_t>(ev0_), s);
   if (n > 0) {
-    if ((rc = launch_sweep(a, nb_, smem_bytes_, s))) return cuda_check(rc, "slab sweep launch");
+    if ((rc = launch_sweep(a, nb_, smem, s))) return cuda_check(rc, "slab sweep launch");
     if ((rc = launch_reduce_stats(d_stats_, n, kStatSlots, d_stat4_, s)))
       return cuda_check(rc, "stats reduce");
     cudaMemcpyAsync(st, d_stat4_, sizeof(st), cudaMemcpyDeviceToHost, s);
@@ -103,7 +115,7 @@ int Engine::sweep_colour(int colour, int outer, int inner, double* st4) {
   icd_ms_ += ms;
   visited_ += static_cast<int64_t>(st[2] + st[3]);
   updated_ += static_cast<int64_t>(st[3]);
-  if (colour == 1) {
+  if (colour == 1 && !bf_) {  // a bright-field call counts at bf_slab_end
     sweeps_done_++;
     outer_ = outer;
     inner_ = inner;
@@ -187,6 +199,174 @@ int Engine::apply_nuisance(const double* gain, const double* offset, const doubl
     }
   }
   return upload_views();
+}
+
+// Detector rows [t0, t1) of the slab's slices (of every slice without a slab); t0 >= t1: none.
+void Engine::slab_rows(int* t0, int* t1) const {
+  const Geometry& g = g_;
+  const int y0 = slab_y1_ > 0 ? slab_y0_ : 0, y1 = slab_y1_ > 0 ? slab_y1_ : g.n_y;
+  *t0 = g.n_t;
+  *t1 = 0;
+  for (int y = y0; y < y1; y++)
+    if (tab_.t_count[y] > 0) {
+      *t0 = std::min(*t0, tab_.t_first[y]);
+      *t1 = std::max(*t1, tab_.t_first[y] + tab_.t_count[y]);
+    }
+}
+
+// The bright-field sinogram arrays from detector row t0 on, t1 - t0 rows ([t][theta][r] layout:
+// a row range is one contiguous block of each array).
+BfSino Engine::bf_sino_rows(int t0, int t1) const {
+  BfSino b = bf_sino();
+  const size_t plane = static_cast<size_t>(g_.n_theta) * n_rp_;
+  b.e = static_cast<char*>(b.e) + static_cast<size_t>(t0) * plane * rb_;
+  b.w = static_cast<char*>(b.w) + static_cast<size_t>(t0) * plane * rb_;
+  b.sel += static_cast<size_t>(t0) * g_.n_theta * n_sp_;
+  b.n_t = t1 - t0;
+  return b;
+}
+
+// Opens an NHICD call on the slab (BFReconstructionEngine.cpp:610-646): the call's lines (the
+// next homogeneous sub-list, or the non-homogeneous list from the magnitude map, which every
+// slab holds summed over all slabs), its schedule and row order.  The slab's colours follow
+// with sweep_colour; bf_slab_end closes the call.
+int Engine::bf_slab_begin(int outer, int inner) {
+  if (state_ < 2) return fail(MBIR_ESTATE, "bf_call_begin: call prepare first");
+  if (!bf_) return fail(MBIR_EINVAL, "bf_call_begin: not a bright-field engine");
+  if (p_.order_mode != MBIR_ORDER_PARALLEL || exact_)
+    return fail(MBIR_ENOTSUP, "bf_call_begin: parallel order only");
+  if (slab_call_open_) return fail(MBIR_ESTATE, "bf_call_begin: a call is open");
+  if (int rc = slab_rows_owned()) return rc;
+  DevBF bfa{};
+  int rc = bf_call_begin(outer, inner, &bfa);
+  if (rc) return rc;
+  const int iter_nonzero = (inner > 0 || outer > 0) ? 1 : 0;
+  if ((rc = bf_parallel_args(iter_nonzero, bfa, &slab_args_, &slab_smem_))) return rc;
+  slab_call_open_ = true;
+  outer_ = outer;
+  inner_ = inner;
+  return MBIR_OK;
+}
+
+// The open call's update magnitude per line (sum |dx| over this slab's slices, fixed point
+// 2^-32), after both colours.
+int Engine::bf_slab_magnitudes(unsigned long long* out) {
+  if (!slab_call_open_) return fail(MBIR_ESTATE, "bf_call_magnitudes: no open call");
+  if (!out) return fail(MBIR_EINVAL, "bf_call_magnitudes: null output");
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const size_t nl = static_cast<size_t>(g_.n_z) * g_.n_x;
+  cudaMemcpyAsync(out, d_magfx_, sizeof(unsigned long long) * nl, cudaMemcpyDeviceToHost, s);
+  return cudaStreamSynchronize(s) == cudaSuccess ? MBIR_OK
+                                                 : cuda_check(MBIR_EDEVICE, "call magnitudes");
+}
+
+// Closes the call: the magnitude map takes the call's magnitudes (mag: summed over all slabs,
+// so every slab holds the same map; null: this slab's own), and the call is counted.
+int Engine::bf_slab_end(const unsigned long long* mag) {
+  if (!slab_call_open_) return fail(MBIR_ESTATE, "bf_call_end: no open call");
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const size_t nl = static_cast<size_t>(g_.n_z) * g_.n_x;
+  if (mag)
+    cudaMemcpyAsync(d_magfx_, mag, sizeof(unsigned long long) * nl, cudaMemcpyHostToDevice, s);
+  slab_call_open_ = false;
+  int rc = bf_call_end();
+  if (rc) return rc;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "call end");
+  bf_schedule_settle();
+  if ((rc = check_device_error())) return rc;
+  sweeps_done_++;
+  return MBIR_OK;
+}
+
+// Partial sums over the slab's detector rows, for the host to sum over slabs.  kind 2: the
+// offset step's numerator and denominator per view (jointEstimation, BFForwardModel.cpp:
+// 390-441), [theta][2]; kind 3: the variance sums over selected and rejected entries
+// (updateWeights, :447-511), [2], after scaling the slab's weights by the current variance as
+// updateWeights does (once per update, then bf_slab_apply(3)).
+int Engine::bf_slab_sums(int kind, double* out) {
+  if (state_ < 2) return fail(MBIR_ESTATE, "bf_slab_sums: call prepare first");
+  if (!bf_ || exact_) return fail(MBIR_ENOTSUP, "bf_slab_sums: bright field, parallel order");
+  if (kind != 2 && kind != 3) return fail(MBIR_EINVAL, "bf_slab_sums: kind is 2 or 3");
+  if (!out) return fail(MBIR_EINVAL, "bf_slab_sums: null output");
+  const int nt = g_.n_theta, K = kind == 2 ? 2 * nt : 2;
+  int t0, t1;
+  slab_rows(&t0, &t1);
+  if (t0 >= t1) {
+    for (int i = 0; i < K; i++) out[i] = 0.0;
+    return MBIR_OK;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const BfSino b = bf_sino_rows(t0, t1);
+  int rc;
+  if (kind == 2) {
+    rc = launch_bf_offset_sums(b, 0, bragg_t_, p_.bragg_delta, d_partial_, n_chunk_, d_vsum_, s);
+    if (rc) return cuda_check(rc, "offset sums");
+    cudaMemcpyAsync(out, d_vsum_, sizeof(double) * K, cudaMemcpyDeviceToHost, s);
+  } else {
+    cudaMemcpyAsync(d_alpha_, alpha_.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, s);
+    rc = launch_bf_variance_sums(b, 0, d_alpha_, d_bfpart_, d_bfout_, s);
+    if (rc) return cuda_check(rc, "variance sums");
+    cudaMemcpyAsync(out, d_bfout_, sizeof(double) * K, cudaMemcpyDeviceToHost, s);
+  }
+  return cudaStreamSynchronize(s) == cudaSuccess ? MBIR_OK : cuda_check(MBIR_EDEVICE, "slab sums");
+}
+
+// Applies the sums of bf_slab_sums added over all slabs to the slab's rows: kind 2, the offset
+// step num / den per view (e -= step, mu += step); kind 3, the common variance (weights divided
+// by it); then the Bragg selector (updateSelector, BFForwardModel.cpp:517-531).
+int Engine::bf_slab_apply(int kind, const double* sums) {
+  if (state_ < 2) return fail(MBIR_ESTATE, "bf_slab_apply: call prepare first");
+  if (!bf_ || exact_) return fail(MBIR_ENOTSUP, "bf_slab_apply: bright field, parallel order");
+  if (kind != 2 && kind != 3) return fail(MBIR_EINVAL, "bf_slab_apply: kind is 2 or 3");
+  if (!sums) return fail(MBIR_EINVAL, "bf_slab_apply: null sums");
+  const Geometry& g = g_;
+  const int nt = g.n_theta;
+  int t0, t1;
+  slab_rows(&t0, &t1);
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  const BfSino b = bf_sino_rows(t0, std::max(t0, t1));
+  int rc;
+  if (kind == 2) {
+    std::vector<double> step(nt);
+    for (int v = 0; v < nt; v++) {
+      step[v] = sums[v * 2 + 0] / sums[v * 2 + 1];
+      mu_[v] += step[v];
+    }
+    if (b.n_t > 0) {
+      cudaMemcpyAsync(d_mu2_, step.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, s);
+      if ((rc = launch_bf_offset_apply(b, d_mu2_, s))) return cuda_check(rc, "offset apply");
+    }
+  } else {
+    const double upd = (sums[0] + (p_.bragg_delta * bragg_t_) * sums[1]) /
+                       (g.n_theta * g.n_r * g.n_t);
+    for (int v = 0; v < nt; v++) alpha_[v] = upd;
+    if (b.n_t > 0 && (rc = launch_bf_scale_weights(b, upd, s))) return cuda_check(rc, "weights");
+    cudaMemcpyAsync(d_alpha_, alpha_.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, s);
+  }
+  if (b.n_t > 0 && (rc = launch_bf_selector(b, bragg_t_, s))) return cuda_check(rc, "selector");
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "slab apply");
+  return kind == 2 ? upload_views() : MBIR_OK;
+}
+
+// The stop rule's two ROI sums (stopCriteria / roiVolumeSum, BFReconstructionEngine_Extra.cpp:
+// 1200-1248): [0] over the magnitude map (the same on every slab), [1] over the volume of the
+// slab's slices (summed over slabs by the host).
+int Engine::roi_sums(double* out2) {
+  if (state_ < 2) return fail(MBIR_ESTATE, "roi_sums: call prepare first");
+  if (!bf_) return fail(MBIR_EINVAL, "roi_sums: bright field only");
+  if (!out2) return fail(MBIR_EINVAL, "roi_sums: null output");
+  int rc = bf_roi_sum(0, &out2[0]);
+  if (rc) return rc;
+  const int y0 = slab_y1_ > 0 ? slab_y0_ : 0, y1 = slab_y1_ > 0 ? slab_y1_ : g_.n_y;
+  DevGeom gs = dg_;
+  gs.n_y = y1 - y0;
+  const size_t plane = static_cast<size_t>(g_.n_z) * g_.n_x;
+  const void* xs = static_cast<const char*>(d_x_) + static_cast<size_t>(y0) * plane * rb_;
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  rc = launch_roi_sum(gs, exact_ ? 1 : 0, 1, d_mag_, xs, fp64_, d_bfpart_, d_bfout_, s);
+  if (rc) return cuda_check(rc, "ROI sum");
+  cudaMemcpyAsync(&out2[1], d_bfout_, sizeof(double), cudaMemcpyDeviceToHost, s);
+  return cudaStreamSynchronize(s) == cudaSuccess ? MBIR_OK : cuda_check(MBIR_EDEVICE, "ROI sums");
 }
 
 }  // namespace mbir

@@ -162,6 +162,12 @@ SIGNATURES = {
     "mbir_get_planes": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, _F]),
     "mbir_set_planes": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, _F]),
     "mbir_view_sums": (C.c_int32, [C.c_void_p, C.c_int32, _D]),
+    "mbir_bf_call_begin": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32]),
+    "mbir_bf_call_magnitudes": (C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    "mbir_bf_call_end": (C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    "mbir_bf_slab_sums": (C.c_int32, [C.c_void_p, C.c_int32, _D]),
+    "mbir_bf_slab_apply": (C.c_int32, [C.c_void_p, C.c_int32, _D]),
+    "mbir_roi_sums": (C.c_int32, [C.c_void_p, _D]),
     "mbir_apply_nuisance": (C.c_int32, [C.c_void_p, _D, _D, _D]),
     "mbir_status_get": (C.c_int32, [C.c_void_p, C.POINTER(MbirStatus)]),
     "mbir_cancel": (None, [C.c_void_p]),
@@ -510,6 +516,45 @@ class Engine:
         nt = self.dims()[3]
         out = np.zeros(nt * (6 if kind == 0 else 1))
         self._check(lib().mbir_view_sums(self._h, kind, out.ctypes.data_as(_D)))
+        return out
+
+    def bf_call_begin(self, outer=0, inner=0):
+        """Bright-field slabs: open one NHICD call (its lines, schedule and row order); the
+        slab's colours follow with sweep_colour, and bf_call_end closes it."""
+        self._check(lib().mbir_bf_call_begin(self._h, outer, inner))
+
+    def bf_call_magnitudes(self):
+        """The open call's update magnitude per line [z][x] over the slab's slices (uint64,
+        fixed point 2^-32), to add over slabs."""
+        nz, nx = self.dims()[:2]
+        out = np.zeros(nz * nx, np.uint64)
+        self._check(lib().mbir_bf_call_magnitudes(
+            self._h, out.ctypes.data_as(C.POINTER(C.c_uint64))))
+        return out
+
+    def bf_call_end(self, magnitudes=None):
+        """Close the call; the magnitude map takes `magnitudes` (summed over slabs; None: the
+        slab's own)."""
+        m = None if magnitudes is None else np.ascontiguousarray(magnitudes, np.uint64)
+        self._check(lib().mbir_bf_call_end(
+            self._h, m.ctypes.data_as(C.POINTER(C.c_uint64)) if m is not None else None))
+
+    def bf_slab_sums(self, kind):
+        """kind 2: offset-step numerator and denominator per view [theta][2]; kind 3: the two
+        variance sums (scales the slab's weights first: once per update)."""
+        nt = self.dims()[3]
+        out = np.zeros(2 * nt if kind == 2 else 2)
+        self._check(lib().mbir_bf_slab_sums(self._h, kind, out.ctypes.data_as(_D)))
+        return out
+
+    def bf_slab_apply(self, kind, sums):
+        s = np.ascontiguousarray(sums, np.float64)
+        self._check(lib().mbir_bf_slab_apply(self._h, kind, s.ctypes.data_as(_D)))
+
+    def roi_sums(self):
+        """The stop rule's ROI sums: magnitude map, and the slab's volume."""
+        out = np.zeros(2)
+        self._check(lib().mbir_roi_sums(self._h, out.ctypes.data_as(_D)))
         return out
 
     def apply_nuisance(self, gain=None, offset=None, variance=None):

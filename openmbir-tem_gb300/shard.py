@@ -15,6 +15,12 @@ Communication goes through torch.distributed on host tensors (gloo): planes and 
 (one N_z x N_x plane per neighbour, 6 N_theta doubles) and are exchanged between kernel launches,
 so no kernel ever waits on another rank.
 
+Bright field (`run_sharded_bf`) shards the same way one NHICD call at a time, as the reference
+splits a call's y range over worker tasks and adds their magnitude maps afterwards
+(BFReconstructionEngine_Extra.cpp:624-752): each call's per-line update magnitudes are added
+over ranks, so every rank derives the same non-homogeneous lists; the offset and variance sums
+and the stop rule's volume sum are added over ranks too.
+
 Backends: `EngineBackend` (the engine's C ABI, one GPU per rank) and, for tests on CPU ranks,
 any object with the same methods (tests use the FP64 oracle).
 """
@@ -99,6 +105,24 @@ class EngineBackend:
     def apply_nuisance(self, gain=None, offset=None, variance=None):
         self.e.apply_nuisance(gain, offset, variance)
 
+    def bf_call_begin(self, outer, inner):
+        self.e.bf_call_begin(outer, inner)
+
+    def bf_call_magnitudes(self):
+        return self.e.bf_call_magnitudes()
+
+    def bf_call_end(self, magnitudes):
+        self.e.bf_call_end(magnitudes)
+
+    def bf_slab_sums(self, kind):
+        return self.e.bf_slab_sums(kind)
+
+    def bf_slab_apply(self, kind, sums):
+        self.e.bf_slab_apply(kind, sums)
+
+    def roi_sums(self):
+        return self.e.roi_sums()
+
 
 def _exchange(dist, backend, y0, y1, n_y, nz, nx):
     """Every rank publishes its first and last plane; ranks take their neighbours' planes."""
@@ -157,6 +181,63 @@ def run_sharded(dist, backend, n_outer, target_gain=1.0, joint_estimation=True,
         if noise_model:
             var = _allreduce(dist, backend.view_sums(1)) / (n_r * n_t)
             backend.apply_nuisance(None, None, var)
+    return (y0, y1), history
+
+
+def _allreduce_int(dist, arr):
+    import torch
+    t = torch.from_numpy(np.ascontiguousarray(arr).astype(np.int64))
+    dist.all_reduce(t)
+    return t.numpy().astype(np.uint64)
+
+
+# NHICD list counts (MBIR::Constants k_NumHomogeniousIter / k_NumNonHomogeniousIter)
+NUM_NON_HOMOGENEOUS = 20
+
+
+def run_sharded_bf(dist, backend, n_outer, stop_threshold=0.0, reduction_factor=1.0,
+                   joint_estimation=True, noise_estimation=True, nhicd=True):
+    """A bright-field reconstruction on this rank's slab with one NHICD call per outer
+    iteration (BFReconstructionEngine::execute with one inner iteration, so the Bragg threshold
+    keeps its requested value, BFReconstructionEngine.cpp:595-858): per call both colours with
+    the halo exchange after each, the call's magnitudes added over ranks, the stop rule on the
+    ROI sums (stopCriteria, _Extra.cpp:1217-1273), then the offset and variance updates from
+    sums over all ranks.  Returns the rank's (y0, y1) and the summed statistics per call."""
+    nz, nx, n_y = backend.dims()[:3]
+    world = dist.get_world_size()
+    rank = dist.get_rank()
+    bounds = slabs(n_y, world)
+    if hasattr(backend, "slice_rows"):
+        check_slab_rows(backend.slice_rows(), bounds)
+    y0, y1 = bounds[rank]
+    backend.set_slab(y0, y1)
+    history = []
+    prev_mag, stop, calls = 0.0, stop_threshold, 0
+    for outer in range(n_outer):
+        eff = calls
+        backend.bf_call_begin(outer, 0)
+        st = np.zeros(4)
+        for colour in (0, 1):
+            st += backend.sweep_colour(colour, outer, 0)
+            _exchange(dist, backend, y0, y1, n_y, nz, nx)
+        backend.bf_call_end(_allreduce_int(dist, backend.bf_call_magnitudes()))
+        calls += 1
+        history.append(_allreduce(dist, st))
+        roi = backend.roi_sums()
+        status = 1
+        check = (eff % NUM_NON_HOMOGENEOUS == 0) if nhicd else True
+        if check and eff > 0 and prev_mag > 0 and abs(roi[0]) / abs(prev_mag) < stop:
+            stop *= reduction_factor
+            status = 0
+        if not nhicd or eff % NUM_NON_HOMOGENEOUS == 0:
+            prev_mag = float(_allreduce(dist, roi[1:2])[0])
+        if status == 0 and outer >= 1:
+            break
+        if n_outer > 1:
+            if joint_estimation:
+                backend.bf_slab_apply(2, _allreduce(dist, backend.bf_slab_sums(2)))
+            if noise_estimation:
+                backend.bf_slab_apply(3, _allreduce(dist, backend.bf_slab_sums(3)))
     return (y0, y1), history
 
 

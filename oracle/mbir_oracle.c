@@ -1492,6 +1492,119 @@ void orc_bf_update_selector(orc_ctx* c) {
   for (size_t i = 0; i < ns; i++) c->sel[i] = (c->e[i] * c->e[i] * c->w[i] < T * T) ? 1 : 0;
 }
 
+/* ---- bright-field slabs: the y-range task split of updateVoxels
+ * (BFReconstructionEngine_Extra.cpp:624-752) with the tasks' magnitude maps and the estimates'
+ * sums added over slabs by the caller.  Rows [t0, t1) are the slab's detector rows. */
+
+/* the call's lines restart their magnitudes (BFUpdateYSlice.cpp:171) */
+void orc_bf_reset_mag(orc_ctx* c, const unsigned char* active) {
+  size_t nl = (size_t)c->n_z * c->n_x;
+  for (size_t l = 0; l < nl; l++)
+    if (active[l]) c->mag_map[l] = 0;
+}
+
+/* one colour of orc_bf_sweep_slices over slices [y0, y1) (magnitudes accumulate) */
+void orc_bf_sweep_colour(orc_ctx* c, const unsigned char* active, const int32_t* row_order,
+                         int stride, int colour, int y0, int y1, int outer, int inner,
+                         double* stats) {
+  stats[0] = stats[1] = stats[2] = stats[3] = 0;
+  for (int i = y0; i < y1; i++) {
+    if ((i & 1) != colour) continue;
+    for (int rr = 0; rr < c->n_z; rr++) {
+      int z = row_order[rr];
+      for (int k = 0; k < stride; k++)
+        for (int x = k; x < c->n_x; x += stride) {
+          int l = z * c->n_x + x;
+          if (active[l] && c->col_count[l] > 0)
+            bf_update_voxel(c, z, x, i, outer, inner, stats, c->mag_map);
+        }
+    }
+  }
+}
+
+/* orc_bf_joint_estimation's per-view numerator and denominator over rows [t0, t1), [theta][2] */
+void orc_bf_offset_sums(const orc_ctx* c, int t0, int t1, double* out) {
+  const double T = c->bragg_t, dl = c->p.bragg_delta;
+  for (int th = 0; th < c->n_theta; th++) {
+    double num = 0, den = 0;
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = t0; t < t1; t++) {
+        double ev = S3(c, e, th, r, t), w = S3(c, w, th, r, t);
+        if (S3(c, sel, th, r, t) == 1) {
+          num += (ev * w);
+          den += w;
+        } else {
+          num += (T * dl * ev / fabs(ev)) * sqrt(w);
+          den += ((T * dl * sqrt(w)) / fabs(ev));
+        }
+      }
+    out[th * 2] = num;
+    out[th * 2 + 1] = den;
+  }
+}
+
+static void bf_selector_rows(orc_ctx* c, int t0, int t1) {
+  const double T = c->bragg_t;
+  for (int th = 0; th < c->n_theta; th++)
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = t0; t < t1; t++) {
+        double ev = S3(c, e, th, r, t);
+        S3(c, sel, th, r, t) = (ev * ev * S3(c, w, th, r, t) < T * T) ? 1 : 0;
+      }
+}
+
+/* the offset steps from sums added over slabs: e -= num/den on rows [t0, t1), mu += num/den,
+ * then the selector of those rows */
+void orc_bf_apply_offsets(orc_ctx* c, const double* sums, int t0, int t1) {
+  for (int th = 0; th < c->n_theta; th++) {
+    double a = sums[th * 2] / sums[th * 2 + 1];
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = t0; t < t1; t++) S3(c, e, th, r, t) -= a;
+    c->mu[th] += a;
+  }
+  bf_selector_rows(c, t0, t1);
+}
+
+/* orc_bf_update_weights' two sums over rows [t0, t1), after w *= alpha on those rows */
+void orc_bf_variance_sums(orc_ctx* c, int t0, int t1, double* out2) {
+  for (int th = 0; th < c->n_theta; th++)
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = t0; t < t1; t++) S3(c, w, th, r, t) *= c->alpha[th];
+  double sum1 = 0, sum2 = 0;
+  for (int th = 0; th < c->n_theta; th++)
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = t0; t < t1; t++) {
+        double ev = S3(c, e, th, r, t), w = S3(c, w, th, r, t);
+        if (S3(c, sel, th, r, t) == 1)
+          sum1 += (ev * ev * w);
+        else
+          sum2 += fabs(ev) * sqrt(c->alpha[th] * w);
+      }
+  out2[0] = sum1;
+  out2[1] = sum2;
+}
+
+/* the common variance from sums added over slabs; w /= it on rows [t0, t1), then their selector */
+void orc_bf_apply_variance(orc_ctx* c, const double* sums, int t0, int t1) {
+  const double T = c->bragg_t, dl = c->p.bragg_delta;
+  double upd = (sums[0] + (dl * T) * sums[1]) / (c->n_theta * c->n_r * c->n_t);
+  for (int th = 0; th < c->n_theta; th++) c->alpha[th] = upd;
+  for (int th = 0; th < c->n_theta; th++)
+    for (int r = 0; r < c->n_r; r++)
+      for (int t = t0; t < t1; t++) S3(c, w, th, r, t) /= c->alpha[th];
+  bf_selector_rows(c, t0, t1);
+}
+
+/* orc_roi_volume_sum over slices [y0, y1) */
+double orc_roi_volume_sum_range(const orc_ctx* c, int y0, int y1) {
+  double sum = 0;
+  for (int j = 0; j < c->n_z; j++)
+    for (int k = 0; k < c->n_x; k++)
+      if (c->mask[(size_t)j * c->n_x + k] == 1)
+        for (int i = y0; i < y1; i++) sum += X3(c, j, k, i);
+  return sum;
+}
+
 /* BFReconstructionEngine::computeCost (BFReconstructionEngine.cpp:1084-1097) =
  * BFForwardModel::forwardCost (BFForwardModel.cpp:812-846) + QGGMRF::PriorModelCost.
  * parts: [0] data, [1] prior, [2] noise. */

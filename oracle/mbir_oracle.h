@@ -167,6 +167,16 @@ int orc_bf_run_fixed_seed(orc_ctx* c, uint32_t seed, int max_calls);
 void orc_icd_sweep_colour(orc_ctx* c, const int32_t* row_order, int stride, int colour, int y0,
                           int y1, int outer, int inner, double* stats);
 void orc_view_sums(const orc_ctx* c, int kind, int t0, int t1, double* out);
+/* bright-field slabs (rows [t0, t1), slices [y0, y1)) */
+void orc_bf_reset_mag(orc_ctx* c, const unsigned char* active);
+void orc_bf_sweep_colour(orc_ctx* c, const unsigned char* active, const int32_t* row_order,
+                         int stride, int colour, int y0, int y1, int outer, int inner,
+                         double* stats);
+void orc_bf_offset_sums(const orc_ctx* c, int t0, int t1, double* out);
+void orc_bf_apply_offsets(orc_ctx* c, const double* sums, int t0, int t1);
+void orc_bf_variance_sums(orc_ctx* c, int t0, int t1, double* out2);
+void orc_bf_apply_variance(orc_ctx* c, const double* sums, int t0, int t1);
+double orc_roi_volume_sum_range(const orc_ctx* c, int y0, int y1);
 void orc_apply_nuisance(orc_ctx* c, const double* gain, const double* offset,
                         const double* variance);
 /* one call with the reference's worker split over y (timing of the reference CPU path) */

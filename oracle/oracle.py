@@ -106,6 +106,14 @@ def lib():
             "orc_icd_sweep_colour": (None, [C.c_void_p, _I, C.c_int, C.c_int, C.c_int, C.c_int,
                                             C.c_int, C.c_int, _D]),
             "orc_view_sums": (None, [C.c_void_p, C.c_int, C.c_int, C.c_int, _D]),
+            "orc_bf_reset_mag": (None, [C.c_void_p, _U8]),
+            "orc_bf_sweep_colour": (None, [C.c_void_p, _U8, _I, C.c_int, C.c_int, C.c_int,
+                                           C.c_int, C.c_int, C.c_int, _D]),
+            "orc_bf_offset_sums": (None, [C.c_void_p, C.c_int, C.c_int, _D]),
+            "orc_bf_apply_offsets": (None, [C.c_void_p, _D, C.c_int, C.c_int]),
+            "orc_bf_variance_sums": (None, [C.c_void_p, C.c_int, C.c_int, _D]),
+            "orc_bf_apply_variance": (None, [C.c_void_p, _D, C.c_int, C.c_int]),
+            "orc_roi_volume_sum_range": (C.c_double, [C.c_void_p, C.c_int, C.c_int]),
             "orc_apply_nuisance": (None, [C.c_void_p, _D, _D, _D]),
             "orc_bf_sweep_lines_mt": (None, [C.c_void_p, _I, C.c_int, C.c_int, C.c_int, C.c_int,
                                              _D]),
@@ -365,6 +373,39 @@ class Oracle:
         lib().orc_bf_sweep_slices(self._h, active.ctypes.data_as(_U8), rows.ctypes.data_as(_I),
                                   stride, outer, inner, st.ctypes.data_as(_D))
         return st
+
+    def bf_reset_mag(self, active):
+        a = np.ascontiguousarray(active, np.uint8)
+        lib().orc_bf_reset_mag(self._h, a.ctypes.data_as(_U8))
+
+    def bf_sweep_colour(self, active, row_order, stride, colour, y0, y1, outer=0, inner=0):
+        active = np.ascontiguousarray(active, np.uint8)
+        rows = np.ascontiguousarray(row_order, np.int32)
+        st = np.zeros(4)
+        lib().orc_bf_sweep_colour(self._h, active.ctypes.data_as(_U8), rows.ctypes.data_as(_I),
+                                  stride, colour, y0, y1, outer, inner, st.ctypes.data_as(_D))
+        return st
+
+    def bf_offset_sums(self, t0, t1):
+        out = np.zeros(2 * self.shape[0])
+        lib().orc_bf_offset_sums(self._h, t0, t1, out.ctypes.data_as(_D))
+        return out
+
+    def bf_apply_offsets(self, sums, t0, t1):
+        s = np.ascontiguousarray(sums, np.float64)
+        lib().orc_bf_apply_offsets(self._h, s.ctypes.data_as(_D), t0, t1)
+
+    def bf_variance_sums(self, t0, t1):
+        out = np.zeros(2)
+        lib().orc_bf_variance_sums(self._h, t0, t1, out.ctypes.data_as(_D))
+        return out
+
+    def bf_apply_variance(self, sums, t0, t1):
+        s = np.ascontiguousarray(sums, np.float64)
+        lib().orc_bf_apply_variance(self._h, s.ctypes.data_as(_D), t0, t1)
+
+    def roi_volume_sum_range(self, y0, y1):
+        return lib().orc_roi_volume_sum_range(self._h, y0, y1)
 
     def bf_sweep_slices_order(self, lines, outer=0, inner=0):
         """The slice-parallel call with every slice visiting `lines` in the given order."""

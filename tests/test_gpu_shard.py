@@ -8,7 +8,7 @@ import socket
 import numpy as np
 import pytest
 
-from conftest import haadf_params, small_case
+from conftest import bf_case, bf_params, haadf_params, small_case
 
 pytestmark = pytest.mark.gpu
 
@@ -30,7 +30,7 @@ def _rank(rank, world, port, q):
     import torch.distributed as dist
     import mbir
     import shard
-    from conftest import haadf_params, small_case
+    from conftest import bf_case, bf_params, haadf_params, small_case
     dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
                             world_size=world)
     try:
@@ -75,3 +75,69 @@ def test_two_ranks_match_one_engine(lib_built):
     assert r <= 1e-4, r
     np.testing.assert_allclose(g, g1, rtol=1e-5)
     np.testing.assert_allclose(var, var1, rtol=1e-4)
+
+
+BF_OUTER = 24  # more than one equivalent iteration of NHICD calls (20)
+
+
+def _rank_bf(rank, world, port, q):
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    for d in (os.path.join(root, "openmbir-tem_gb300"), os.path.join(root, "oracle"), here):
+        sys.path.insert(0, d)
+    import torch.distributed as dist
+    import mbir
+    import shard
+    from conftest import bf_case, bf_params
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world)
+    try:
+        y, ang, th = bf_case()
+        with mbir.Engine(bf_params(mbir, th, outer_iterations=BF_OUTER)) as e:
+            e.set_sinogram(y, ang)
+            e.prepare()
+            be = shard.EngineBackend(e)
+            (y0, y1), hist = shard.run_sharded_bf(dist, be, BF_OUTER)
+            vol = shard.gather_volume(dist, be, y0, y1)
+            if rank == 0:
+                _, _, mag, _, _ = e.bf_state()
+                q.put((vol, e.nuisance(), mag, np.array(hist)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_ranks_bright_field_match_one_engine(lib_built):
+    """Bright-field NHICD calls on two slabs (homogeneous and non-homogeneous lists, device
+    colour schedules, offset and variance updates): the first call updates the same voxels as
+    one engine, and the run ends where one engine's run ends (the cross-slab sums differ only in
+    their order)."""
+    import multiprocessing as mp
+    mbir = lib_built
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_bf, args=(r, 2, port, q)) for r in range(2)]
+    for pr in procs:
+        pr.start()
+    vol, (g, off, var), mag, hist = q.get(timeout=300)
+    for pr in procs:
+        pr.join(timeout=120)
+        assert pr.exitcode == 0
+    y, ang, th = bf_case()
+    with mbir.Engine(bf_params(mbir, th, outer_iterations=BF_OUTER)) as e:
+        e.set_sinogram(y, ang)
+        e.prepare()
+        first = e.sweep(0, 0)
+        np.testing.assert_array_equal(hist[0][2:], first[2:])
+    with mbir.Engine(bf_params(mbir, th, outer_iterations=BF_OUTER)) as e:
+        e.set_sinogram(y, ang)
+        e.run()
+        ref = e.volume()
+        _, off1, var1 = e.nuisance()
+        _, _, mag1, _, _ = e.bf_state()
+    r = float(np.linalg.norm(vol.astype(np.float64) - ref) / np.linalg.norm(ref))
+    assert r <= 1e-4, r
+    np.testing.assert_allclose(off, off1, rtol=1e-5)
+    np.testing.assert_allclose(var, var1, rtol=1e-4)
+    assert float(np.linalg.norm(mag - mag1) / np.linalg.norm(mag1)) <= 1e-3

@@ -120,6 +120,105 @@ def _rank(rank, world, port, q):
         dist.destroy_process_group()
 
 
+class OracleBFBackend(OracleBackend):
+    """Bright-field oracle ranks: every call takes all lines (no NHICD lists) in the engine's
+    row order; the slab's rows are its slices' rows (delta_xy = delta_t)."""
+
+    def bf_call_begin(self, outer, inner):
+        self.active = np.ones(self.o.nz * self.o.nx, np.uint8)
+        self.rows, self.stride = self.schedule(self.sweeps)
+        self.o.bf_reset_mag(self.active)
+
+    def sweep_colour(self, colour, outer, inner):
+        return self.o.bf_sweep_colour(self.active, self.rows, self.stride, colour, self.y0,
+                                      self.y1, outer, inner)
+
+    def bf_call_magnitudes(self):
+        return np.where(self.active.reshape(self.o.nz, self.o.nx) != 0, self.o.mag_map(), 0.0)
+
+    def bf_call_end(self, magnitudes):
+        act = self.active.reshape(self.o.nz, self.o.nx) != 0
+        self.o.mag_map()[act] = np.asarray(magnitudes).reshape(self.o.nz, self.o.nx)[act]
+        self.sweeps += 1
+
+    def roi_sums(self):
+        return np.array([self.o.roi_mag_sum(), self.o.roi_volume_sum_range(self.y0, self.y1)])
+
+    def bf_slab_sums(self, kind):
+        if kind == 2:
+            return self.o.bf_offset_sums(self.y0, self.y1)
+        return self.o.bf_variance_sums(self.y0, self.y1)
+
+    def bf_slab_apply(self, kind, sums):
+        if kind == 2:
+            self.o.bf_apply_offsets(sums, self.y0, self.y1)
+        else:
+            self.o.bf_apply_variance(sums, self.y0, self.y1)
+
+
+def _rank_bf(rank, world, port, q):
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    for d in (os.path.join(root, "openmbir-tem_gb300"), os.path.join(root, "oracle"), here):
+        sys.path.insert(0, d)
+    import torch
+    import torch.distributed as dist
+    import mbir
+    import oracle
+    import shard
+    from conftest import bf_case, bf_params
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world)
+    try:
+        y, ang, th = bf_case(n_r=48, n_t=6)
+        p = bf_params(mbir, th, nhicd=0)
+        e = mbir.Engine(p)  # host-only use: geometry and schedule
+        e.set_sinogram(y, ang)
+        o = oracle.Oracle(oracle.params_from_mbir(p), y, ang)
+        o.prepare()
+        be = OracleBFBackend(o, e.schedule)
+        (y0, y1), hist = shard.run_sharded_bf(dist, be, 3, nhicd=False)
+        vol = np.zeros((o.nz, o.nx, o.ny))
+        vol[:, :, y0:y1] = o.volume()[:, :, y0:y1]
+        t = torch.from_numpy(vol)
+        dist.all_reduce(t)
+        if rank == 0:
+            q.put((t.numpy(), o.offset().copy(), o.variance().copy(), o.mag_map().copy(),
+                   np.array(hist)))
+    finally:
+        dist.destroy_process_group()
+
+
+def _run_ranks(target, world):
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=target, args=(r, world, port, q)) for r in range(world)]
+    for pr in procs:
+        pr.start()
+    out = q.get(timeout=300)
+    for pr in procs:
+        pr.join(timeout=60)
+        assert pr.exitcode == 0
+    return out
+
+
+def test_two_cpu_ranks_bright_field_match_one_rank(oracle_mod, lib_built):
+    """Bright-field slabs on two CPU ranks (FP64 oracle): per call both colours with halo
+    exchange, the call's magnitude map added over ranks, offset and variance updates from sums
+    over ranks; the same as one rank holding the whole volume (1e-9: only the order of the
+    cross-rank sums differs)."""
+    vol2, off2, var2, mag2, hist2 = _run_ranks(_rank_bf, 2)
+    vol1, off1, var1, mag1, hist1 = _run_ranks(_rank_bf, 1)
+    np.testing.assert_array_equal(hist2[0][2:], hist1[0][2:])  # same updates in the first call
+    assert np.linalg.norm(vol2 - vol1) / np.linalg.norm(vol1) <= 1e-9
+    np.testing.assert_allclose(off2, off1, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(var2, var1, rtol=1e-9)
+    np.testing.assert_allclose(mag2, mag1, rtol=1e-9, atol=1e-15)
+
+
 def test_slabs_partition():
     import shard
     for n_y, world in ((8, 2), (9, 2), (7, 3), (2, 4)):
