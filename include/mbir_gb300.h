@@ -280,8 +280,9 @@ int32_t mbir_apply_nuisance(mbir_engine* e, const double* gain, const double* of
  * and after an outer iteration
  *   mbir_bf_slab_sums: kind 2 = the offset step's numerator and denominator per view [theta][2]
  *     (jointEstimation, BFForwardModel.cpp:390-441); kind 3 = the variance sums over selected
- *     and rejected entries [2] (updateWeights, :447-511; scales the slab's weights by the
- *     current variance first, so once per update), over the slab's detector rows
+ *     and rejected entries and the number of entries [3] (updateWeights, :447-511; scales the
+ *     slab's weights by the current variance first, so once per update), over the slab's
+ *     detector rows
  *   mbir_bf_slab_apply: the same kind's sums added over slabs: offset steps or the common
  *     variance, then the Bragg selector (updateSelector, :517-531)
  *   mbir_roi_sums: the stop rule's ROI sums (_Extra.cpp:1200-1248): [0] of the magnitude map,

@@ -281,14 +281,15 @@ int Engine::bf_slab_end(const unsigned long long* mag) {
 // Partial sums over the slab's detector rows, for the host to sum over slabs.  kind 2: the
 // offset step's numerator and denominator per view (jointEstimation, BFForwardModel.cpp:
 // 390-441), [theta][2]; kind 3: the variance sums over selected and rejected entries
-// (updateWeights, :447-511), [2], after scaling the slab's weights by the current variance as
-// updateWeights does (once per update, then bf_slab_apply(3)).
+// (updateWeights, :447-511) and the number of entries they cover, [3], after scaling the slab's
+// weights by the current variance as updateWeights does (once per update, then
+// bf_slab_apply(3)).
 int Engine::bf_slab_sums(int kind, double* out) {
   if (state_ < 2) return fail(MBIR_ESTATE, "bf_slab_sums: call prepare first");
   if (!bf_ || exact_) return fail(MBIR_ENOTSUP, "bf_slab_sums: bright field, parallel order");
   if (kind != 2 && kind != 3) return fail(MBIR_EINVAL, "bf_slab_sums: kind is 2 or 3");
   if (!out) return fail(MBIR_EINVAL, "bf_slab_sums: null output");
-  const int nt = g_.n_theta, K = kind == 2 ? 2 * nt : 2;
+  const int nt = g_.n_theta, K = kind == 2 ? 2 * nt : 3;
   int t0, t1;
   slab_rows(&t0, &t1);
   if (t0 >= t1) {
@@ -306,14 +307,16 @@ int Engine::bf_slab_sums(int kind, double* out) {
     cudaMemcpyAsync(d_alpha_, alpha_.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, s);
     rc = launch_bf_variance_sums(b, 0, d_alpha_, d_bfpart_, d_bfout_, s);
     if (rc) return cuda_check(rc, "variance sums");
-    cudaMemcpyAsync(out, d_bfout_, sizeof(double) * K, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(out, d_bfout_, sizeof(double) * 2, cudaMemcpyDeviceToHost, s);
+    out[2] = static_cast<double>(nt) * g_.n_r * (t1 - t0);
   }
   return cudaStreamSynchronize(s) == cudaSuccess ? MBIR_OK : cuda_check(MBIR_EDEVICE, "slab sums");
 }
 
 // Applies the sums of bf_slab_sums added over all slabs to the slab's rows: kind 2, the offset
-// step num / den per view (e -= step, mu += step); kind 3, the common variance (weights divided
-// by it); then the Bragg selector (updateSelector, BFForwardModel.cpp:517-531).
+// step num / den per view (e -= step, mu += step); kind 3, the common variance (the two sums
+// over the entries they cover; weights divided by it); then the Bragg selector
+// (updateSelector, BFForwardModel.cpp:517-531).
 int Engine::bf_slab_apply(int kind, const double* sums) {
   if (state_ < 2) return fail(MBIR_ESTATE, "bf_slab_apply: call prepare first");
   if (!bf_ || exact_) return fail(MBIR_ENOTSUP, "bf_slab_apply: bright field, parallel order");
@@ -337,8 +340,7 @@ int Engine::bf_slab_apply(int kind, const double* sums) {
       if ((rc = launch_bf_offset_apply(b, d_mu2_, s))) return cuda_check(rc, "offset apply");
     }
   } else {
-    const double upd = (sums[0] + (p_.bragg_delta * bragg_t_) * sums[1]) /
-                       (g.n_theta * g.n_r * g.n_t);
+    const double upd = (sums[0] + (p_.bragg_delta * bragg_t_) * sums[1]) / sums[2];
     for (int v = 0; v < nt; v++) alpha_[v] = upd;
     if (b.n_t > 0 && (rc = launch_bf_scale_weights(b, upd, s))) return cuda_check(rc, "weights");
     cudaMemcpyAsync(d_alpha_, alpha_.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, s);

@@ -541,9 +541,10 @@ class Engine:
 
     def bf_slab_sums(self, kind):
         """kind 2: offset-step numerator and denominator per view [theta][2]; kind 3: the two
-        variance sums (scales the slab's weights first: once per update)."""
+        variance sums and the number of entries they cover (scales the slab's weights first:
+        once per update)."""
         nt = self.dims()[3]
-        out = np.zeros(2 * nt if kind == 2 else 2)
+        out = np.zeros(2 * nt if kind == 2 else 3)
         self._check(lib().mbir_bf_slab_sums(self._h, kind, out.ctypes.data_as(_D)))
         return out
 

@@ -21,8 +21,10 @@ splits a call's y range over worker tasks and adds their magnitude maps afterwar
 over ranks, so every rank derives the same non-homogeneous lists; the offset and variance sums
 and the stop rule's volume sum are added over ranks too.
 
-Backends: `EngineBackend` (the engine's C ABI, one GPU per rank) and, for tests on CPU ranks,
-any object with the same methods (tests use the FP64 oracle).
+Backends: `EngineBackend` (the engine's C ABI, one GPU per rank; the engine holds the whole
+problem), `OwnedSlabBackend` (the engine holds only the rank's slab, one halo plane on each side
+and their detector rows: the device memory of one slab) and, for tests on CPU ranks, any object
+with the same methods (tests use the FP64 oracle).
 """
 import numpy as np
 
@@ -98,6 +100,88 @@ class EngineBackend:
 
     def set_planes(self, y, planes):
         self.e.set_planes(y, planes)
+
+    def view_sums(self, kind):
+        return self.e.view_sums(kind)
+
+    def apply_nuisance(self, gain=None, offset=None, variance=None):
+        self.e.apply_nuisance(gain, offset, variance)
+
+    def bf_call_begin(self, outer, inner):
+        self.e.bf_call_begin(outer, inner)
+
+    def bf_call_magnitudes(self):
+        return self.e.bf_call_magnitudes()
+
+    def bf_call_end(self, magnitudes):
+        self.e.bf_call_end(magnitudes)
+
+    def bf_slab_sums(self, kind):
+        return self.e.bf_slab_sums(kind)
+
+    def bf_slab_apply(self, kind, sums):
+        self.e.bf_slab_apply(kind, sums)
+
+    def roi_sums(self):
+        return self.e.roi_sums()
+
+
+def owned_slab(n_y, world, rank):
+    """This rank's slab [y0, y1) and the slices [base, top) its engine holds: the slab plus one
+    halo plane on each side, the lower end rounded down to an even slice so that the engine's
+    local slice parity is the global one (the red/black colours keep their meaning)."""
+    y0, y1 = slabs(n_y, world)[rank]
+    base = max(0, y0 - 1)
+    base -= base & 1
+    return (y0, y1), base, min(n_y, y1 + 1)
+
+
+class OwnedSlabBackend:
+    """A rank's engine built on its own slices only (`owned_slab`): the tilt series' detector
+    rows of slices [base, top) as its sinogram, the initial nuisance estimated from the whole
+    series (so that every rank starts where one engine would), and the drivers' global slice
+    indices mapped to the engine's.  Make it with `make`."""
+
+    def __init__(self, engine, dims, base):
+        self.e = engine
+        self.dims_g = tuple(dims)
+        self.base = base
+
+    @classmethod
+    def make(cls, mbir, params, counts, tilts, world, rank, rows_per_slice=1, delta_r=1.0,
+             delta_t=1.0):
+        """counts [theta][r][t] of the whole series; rows_per_slice = delta_xy / delta_t."""
+        import numpy as _np
+        with mbir.Engine(params) as full:  # host only: geometry and the initial nuisance
+            full.set_sinogram(counts, tilts, delta_r, delta_t)
+            dims = full.dims()
+            gain, offset, var = full.nuisance()
+        (y0, y1), base, top = owned_slab(dims[2], world, rank)
+        f = rows_per_slice
+        sub = _np.ascontiguousarray(counts[:, :, f * base:f * top])
+        e = mbir.Engine(params)
+        e.set_sinogram(sub, tilts, delta_r, delta_t)
+        e.set_initial_nuisance(gain, offset, var)
+        e.prepare()
+        return cls(e, dims, base)
+
+    def close(self):
+        self.e.close()
+
+    def dims(self):
+        return self.dims_g
+
+    def set_slab(self, y0, y1):
+        self.e.set_slab(y0 - self.base, y1 - self.base)
+
+    def sweep_colour(self, colour, outer, inner):
+        return self.e.sweep_colour(colour, outer, inner)
+
+    def get_planes(self, y, n):
+        return self.e.get_planes(y - self.base, n)
+
+    def set_planes(self, y, planes):
+        self.e.set_planes(y - self.base, planes)
 
     def view_sums(self, kind):
         return self.e.view_sums(kind)

@@ -1565,8 +1565,9 @@ void orc_bf_apply_offsets(orc_ctx* c, const double* sums, int t0, int t1) {
   bf_selector_rows(c, t0, t1);
 }
 
-/* orc_bf_update_weights' two sums over rows [t0, t1), after w *= alpha on those rows */
-void orc_bf_variance_sums(orc_ctx* c, int t0, int t1, double* out2) {
+/* orc_bf_update_weights' two sums over rows [t0, t1), after w *= alpha on those rows, and the
+ * number of entries they cover */
+void orc_bf_variance_sums(orc_ctx* c, int t0, int t1, double* out3) {
   for (int th = 0; th < c->n_theta; th++)
     for (int r = 0; r < c->n_r; r++)
       for (int t = t0; t < t1; t++) S3(c, w, th, r, t) *= c->alpha[th];
@@ -1580,14 +1581,16 @@ void orc_bf_variance_sums(orc_ctx* c, int t0, int t1, double* out2) {
         else
           sum2 += fabs(ev) * sqrt(c->alpha[th] * w);
       }
-  out2[0] = sum1;
-  out2[1] = sum2;
+  out3[0] = sum1;
+  out3[1] = sum2;
+  out3[2] = (double)c->n_theta * c->n_r * (t1 - t0);
 }
 
-/* the common variance from sums added over slabs; w /= it on rows [t0, t1), then their selector */
+/* the common variance from sums added over slabs (the two sums over the entries they cover);
+ * w /= it on rows [t0, t1), then their selector */
 void orc_bf_apply_variance(orc_ctx* c, const double* sums, int t0, int t1) {
   const double T = c->bragg_t, dl = c->p.bragg_delta;
-  double upd = (sums[0] + (dl * T) * sums[1]) / (c->n_theta * c->n_r * c->n_t);
+  double upd = (sums[0] + (dl * T) * sums[1]) / sums[2];
   for (int th = 0; th < c->n_theta; th++) c->alpha[th] = upd;
   for (int th = 0; th < c->n_theta; th++)
     for (int r = 0; r < c->n_r; r++)

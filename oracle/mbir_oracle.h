@@ -174,7 +174,7 @@ void orc_bf_sweep_colour(orc_ctx* c, const unsigned char* active, const int32_t*
                          double* stats);
 void orc_bf_offset_sums(const orc_ctx* c, int t0, int t1, double* out);
 void orc_bf_apply_offsets(orc_ctx* c, const double* sums, int t0, int t1);
-void orc_bf_variance_sums(orc_ctx* c, int t0, int t1, double* out2);
+void orc_bf_variance_sums(orc_ctx* c, int t0, int t1, double* out3);
 void orc_bf_apply_variance(orc_ctx* c, const double* sums, int t0, int t1);
 double orc_roi_volume_sum_range(const orc_ctx* c, int y0, int y1);
 void orc_apply_nuisance(orc_ctx* c, const double* gain, const double* offset,

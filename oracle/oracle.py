@@ -396,7 +396,7 @@ class Oracle:
         lib().orc_bf_apply_offsets(self._h, s.ctypes.data_as(_D), t0, t1)
 
     def bf_variance_sums(self, t0, t1):
-        out = np.zeros(2)
+        out = np.zeros(3)
         lib().orc_bf_variance_sums(self._h, t0, t1, out.ctypes.data_as(_D))
         return out
 

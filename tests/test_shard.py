@@ -120,6 +120,91 @@ def _rank(rank, world, port, q):
         dist.destroy_process_group()
 
 
+class OracleOwnedBackend(OracleBackend):
+    """An oracle rank that holds only its slab's slices, one halo plane on each side and their
+    detector rows (shard.owned_slab), with the drivers' global slice indices mapped to its own."""
+
+    def __init__(self, o, schedule, dims, base):
+        super().__init__(o, schedule)
+        self.dims_g = tuple(dims)
+        self.base = base
+
+    def dims(self):
+        return self.dims_g
+
+    def set_slab(self, y0, y1):
+        super().set_slab(y0 - self.base, y1 - self.base)
+
+    def get_planes(self, y, n):
+        return super().get_planes(y - self.base, n)
+
+    def set_planes(self, y, planes):
+        super().set_planes(y - self.base, planes)
+
+
+def _owned_problem(world, rank):
+    import mbir
+    import oracle
+    import shard
+    from conftest import haadf_params, small_case
+    y, ang, th = small_case(n_t=16)
+    p = haadf_params(mbir, th)
+    e = mbir.Engine(p)  # host-only use: geometry, schedule, the initial nuisance of the series
+    e.set_sinogram(y, ang)
+    dims = e.dims()
+    nuis = e.nuisance()
+    (y0, y1), base, top = shard.owned_slab(dims[2], world, rank)
+    o = oracle.Oracle(oracle.params_from_mbir(p), np.ascontiguousarray(y[:, :, base:top]), ang)
+    o.prepare()
+    o.apply_nuisance(*nuis)
+    return e, o, p, dims, base, nuis
+
+
+def _rank_owned(rank, world, port, q):
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    for d in (os.path.join(root, "openmbir-tem_gb300"), os.path.join(root, "oracle"), here):
+        sys.path.insert(0, d)
+    import torch
+    import torch.distributed as dist
+    import shard
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world)
+    try:
+        e, o, p, dims, base, _ = _owned_problem(world, rank)
+        be = OracleOwnedBackend(o, e.schedule, dims, base)
+        (y0, y1), hist = shard.run_sharded(dist, be, 3, p.target_gain)
+        vol = np.zeros((dims[0], dims[1], dims[2]))
+        vol[:, :, y0:y1] = o.volume()[:, :, y0 - base:y1 - base]
+        t = torch.from_numpy(vol)
+        dist.all_reduce(t)
+        if rank == 0:
+            q.put((t.numpy(), o.gain().copy(), o.offset().copy(), o.variance().copy(),
+                   np.array(hist)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_owned_slabs_two_cpu_ranks_match_single_process(oracle_mod, lib_built):
+    """Ranks that hold only their slab, one halo plane each side and those slices' detector
+    rows (16 slices over two ranks: 9 and 10 slices held) give one process's result."""
+    vol, g, off, var, hist = _run_ranks(_rank_owned, 2)
+    e, o, p, dims, base, nuis = _owned_problem(1, 0)
+    assert base == 0 and o.ny == dims[2]
+    for k in range(3):
+        rows, stride = e.schedule(k)
+        st = o.sweep_slices(rows, stride, k, 0)
+        np.testing.assert_allclose(hist[k][2:], st[2:])
+        o.joint_estimation()
+        o.update_weights()
+    ref = o.volume()
+    assert np.linalg.norm(vol - ref) / np.linalg.norm(ref) <= 1e-9
+    np.testing.assert_allclose(g, o.gain(), rtol=1e-9)
+    np.testing.assert_allclose(off, o.offset(), rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(var, o.variance(), rtol=1e-9)
+
+
 class OracleBFBackend(OracleBackend):
     """Bright-field oracle ranks: every call takes all lines (no NHICD lists) in the engine's
     row order; the slab's rows are its slices' rows (delta_xy = delta_t)."""
