@@ -406,9 +406,10 @@ int32_t mbir_estimate_sigma_x(const char* mrc_path, double sample_thickness, dou
 const char* mbir_version(void);
 
 /* Per-view sums of squared errors, sums_dev[v] = sum over r, t of error_dev[v][r][t]^2 (the sums a
- * per-view noise-variance estimate divides by N_r N_t), computed on caller-owned device buffers (FP32 error sinogram in the reference's [theta][r][t] layout, FP64
- * output of n_theta values) with no allocation: for callers whose device memory is owned by their
- * own pool, or whose path must not allocate.  No counterpart in the reference (it is this
+ * per-view noise-variance estimate divides by N_r N_t), computed on caller-owned device buffers
+ * (FP32 error sinogram in the reference's [theta][r][t] layout, FP64 output of n_theta values)
+ * with no allocation: for callers whose device memory is owned by their own pool, or whose path
+ * must not allocate.  No counterpart in the reference (it is this
  * library's addition).  Limits: n_theta <= 1024 (MBIR_EINVAL beyond); the scratch (128 KiB of
  * per-view partial sums, fully rewritten by every call) lives in one static device array per
  * device, so calls that overlap in time race and must be serialised by the caller.  The first call
