@@ -355,6 +355,7 @@ def batch_measure(mbir, n, seed=1, batch_threads=None, tol=1e-4, max_outer=60):
         t0 = time.perf_counter()
         iters, _ = b.run(max_outer, tol)
         bat_s = time.perf_counter() - t0
+        bat_threads = b.threads()
         bat_sweep_s = b.total_ms() / 1e3
         bat_upd = sum(e.status().voxels_updated for e in engines)
     for e in engines:
@@ -367,6 +368,7 @@ def batch_measure(mbir, n, seed=1, batch_threads=None, tol=1e-4, max_outer=60):
                            "outer_iterations": int(np.sum(seq_iters)), "phases": phase},
             "batched": {"wall_s": bat_s, "voxel_updates": bat_upd,
                         "sweep_device_s": bat_sweep_s,
+                        "threads_per_cta": bat_threads,
                         "voxel_updates_per_s": bat_upd / bat_s,
                         "outer_iterations": int(np.sum(iters))}}
 

@@ -331,10 +331,13 @@ void mbir_batch_destroy(mbir_batch* b);
 int32_t mbir_batch_add(mbir_batch* b, mbir_engine* e);
 int32_t mbir_batch_remove(mbir_batch* b, mbir_engine* e);
 int32_t mbir_batch_size(const mbir_batch* b);
-/* threads per CTA of the persistent batched sweep: 512 (default; one slice per SM) or 256 (two
- * slices per SM; a slice's detector rows are staged in shared memory only when two CTAs' worth
- * fits, otherwise they are used in place in HBM).  Same results either way. */
+/* threads per CTA of the persistent batched sweep (the slice-group shape): 512 (one slice per
+ * SM), 256 (two slices per SM; a slice's detector rows are staged in shared memory only when
+ * two CTAs' worth fits, otherwise they are used in place in HBM) or 0 (default: tuned online,
+ * the second to fifth sweeps running 512, 256, 256, 512 and the one with the lower device time
+ * per updated voxel kept).  Same results either way.  get: the value in use (0 while tuning). */
 int32_t mbir_batch_set_threads(mbir_batch* b, int32_t threads);
+int32_t mbir_batch_get_threads(mbir_batch* b);
 /* Limit (seconds, default 10) of the device-side wait in a batched sweep: a colour-1 slice waits
  * for its series' colour-0 slices, and a wait that runs out skips that slice; the sweep then
  * returns MBIR_ETIMEOUT and the engines stay usable.  No counterpart in the reference (its

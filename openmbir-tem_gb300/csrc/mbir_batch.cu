@@ -128,7 +128,14 @@ int Batch::sweep(const std::vector<std::pair<int, int>>& iters, double* stats) {
   cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device_);
   // staged slices must leave room for the kernel's static shared memory (and, with 256-thread
   // CTAs, for a second CTA on the SM)
-  const bool two = threads_ == 256;
+  // online tuning: the batch's first sweep (every voxel updated) runs at 512 threads and is not
+  // measured; the next four run 512, 256, 256, 512 (a drift in the cost per voxel as the
+  // reconstructions converge cancels)
+  const bool tuning = threads_ == 0 && tuned_ == 0;
+  const int trial = tune_sweeps_ - 1;
+  const int threads = threads_ ? threads_
+                               : (tuned_ ? tuned_ : (trial == 1 || trial == 2 ? 256 : 512));
+  const bool two = threads == 256;
   const size_t stage_cap = two ? static_cast<size_t>(std::min(max_optin, per_sm / 2 - 1024)) - 2048
                                : static_cast<size_t>(max_optin) - 2048;
   // per-engine set-up (row order, bright-field list, active mask, level schedule) side by side
@@ -184,7 +191,7 @@ int Batch::sweep(const std::vector<std::pair<int, int>>& iters, double* stats) {
     b.done = d_ctr_ + kShapes;
     b.need = d_ctr_ + kShapes + n;
     b.wait_ns = wait_ns_;
-    rc = launch_batch_sweep(b, nb, g, threads_, smem, grid_, s);
+    rc = launch_batch_sweep(b, nb, g, threads, smem, grid_, s);
     if (rc) return fail(MBIR_EDEVICE, std::string("batch sweep launch: ") +
                                           cudaGetErrorString(cudaGetLastError()));
   }
@@ -221,6 +228,22 @@ int Batch::sweep(const std::vector<std::pair<int, int>>& iters, double* stats) {
     if (fin[i]) return fail(fin[i], eng_[i]->last_error());
     if (stats)
       for (int k = 0; k < kStatSlots; k++) stats[kStatSlots * i + k] = st[kStatSlots * i + k];
+  }
+  if (tuning) {
+    // device time per updated voxel of each slice-group shape
+    if (trial >= 0) {
+      double vox = 0.0;
+      for (int i = 0; i < n; i++) vox += st[kStatSlots * i + 3];
+      const int k = two ? 1 : 0;
+      tune_ms_[k] += ms;
+      tune_vox_[k] += vox;
+    }
+    if (++tune_sweeps_ >= 5) {
+      tuned_ = (tune_vox_[0] > 0 && tune_vox_[1] > 0 &&
+                tune_ms_[1] / tune_vox_[1] < tune_ms_[0] / tune_vox_[0])
+                   ? 256
+                   : 512;
+    }
   }
   return MBIR_OK;
 }

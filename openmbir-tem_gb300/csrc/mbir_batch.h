@@ -56,8 +56,6 @@ class Batch {
   double total_ms() const { return total_ms_; }
   int sweeps() const { return sweeps_; }
   void set_grid(int g) { grid_ = g; }
-  // threads per CTA of the persistent sweep: 512 (one CTA per SM) or 256 (two per SM; a slice is
-  // staged in shared memory only when two CTAs' worth fits)
   // limit of the device-side wait of a colour-1 slice for its series' colour-0 slices; a wait
   // that runs out skips the slice and the sweep returns MBIR_ETIMEOUT
   int set_wait_limit(double seconds) {
@@ -65,11 +63,20 @@ class Batch {
     wait_ns_ = static_cast<unsigned long long>(seconds * 1e9);
     return MBIR_OK;
   }
+  // slice-group shape of the persistent sweep: 512 threads per CTA (one CTA per SM), 256 (two
+  // per SM; a slice is staged in shared memory only when two CTAs' worth fits), or 0 (default):
+  // tuned online over the second to fifth sweeps (512, 256, 256, 512), the one with the lower
+  // device time per updated voxel kept.  Results do not depend on it.
   int set_threads(int t) {
-    if (t != 256 && t != 512) return MBIR_EINVAL;
+    if (t != 0 && t != 256 && t != 512) return MBIR_EINVAL;
     threads_ = t;
+    tuned_ = 0;
+    tune_sweeps_ = 0;
+    tune_ms_[0] = tune_ms_[1] = tune_vox_[0] = tune_vox_[1] = 0.0;
     return MBIR_OK;
   }
+  // threads per CTA in use: the fixed or tuned value, 0 while the tuning sweeps run
+  int threads() const { return threads_ ? threads_ : tuned_; }
   const char* last_error() const { return err_.c_str(); }
   int fail(int code, const std::string& m);
 
@@ -92,7 +99,10 @@ class Batch {
   void* ev0_ = nullptr;
   void* ev1_ = nullptr;
   int grid_ = 0;
-  int threads_ = 512;
+  int threads_ = 0;                            // 0: tuned online
+  int tuned_ = 0;                              // the tuning's choice once made
+  int tune_sweeps_ = 0;
+  double tune_ms_[2] = {0.0, 0.0}, tune_vox_[2] = {0.0, 0.0};  // [512, 256]
   unsigned long long wait_ns_ = 10000000000ull;  // colour-1 wait limit (10 s)
   // launch groups: voxel-group shape (4) x modality (HAADF, bright field), one launch each
   static constexpr int kShapes = 8;

@@ -462,6 +462,7 @@ int32_t mbir_batch_size(const mbir_batch* b) {
 int32_t mbir_batch_set_threads(mbir_batch* b, int32_t threads) {
   return b ? b->impl->set_threads(threads) : MBIR_EINVAL;
 }
+int32_t mbir_batch_get_threads(mbir_batch* b) { return b ? b->impl->threads() : MBIR_EINVAL; }
 int32_t mbir_batch_set_wait_limit(mbir_batch* b, double seconds) {
   return b ? b->impl->set_wait_limit(seconds) : MBIR_EINVAL;
 }

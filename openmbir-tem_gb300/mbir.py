@@ -182,6 +182,7 @@ SIGNATURES = {
     "mbir_batch_remove": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "mbir_batch_size": (C.c_int32, [C.c_void_p]),
     "mbir_batch_set_threads": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "mbir_batch_get_threads": (C.c_int32, [C.c_void_p]),
     "mbir_batch_set_wait_limit": (C.c_int32, [C.c_void_p, C.c_double]),
     "mbir_batch_sweep": (C.c_int32, [C.c_void_p, C.c_int32, _D]),
     "mbir_batch_run": (C.c_int32, [C.c_void_p, C.c_int32, C.c_double, _I, _D]),
@@ -640,8 +641,13 @@ class Batch:
         return lib().mbir_batch_total_ms(self._h)
 
     def set_threads(self, threads):
-        """CTA size of the persistent batched sweep: 512 or 256 (two slices per SM)."""
+        """CTA size of the persistent batched sweep: 512, 256 (two slices per SM) or 0 (tuned
+        online over the second to fifth sweeps, the default)."""
         self._check(lib().mbir_batch_set_threads(self._h, int(threads)))
+
+    def threads(self):
+        """The CTA size in use (0 while the online tuning runs)."""
+        return int(lib().mbir_batch_get_threads(self._h))
 
     def set_wait_limit(self, seconds):
         """Limit of the device-side wait of a colour-1 slice (mbir_batch_set_wait_limit)."""

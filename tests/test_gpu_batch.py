@@ -56,6 +56,27 @@ def test_batched_sweeps_match_single(lib_built):
         assert rel(eb.error_sinogram(), ea.error_sinogram()) <= 1e-5
 
 
+def test_batch_slice_group_tuning(lib_built):
+    """The batch tunes its CTA size online over its second to fifth sweeps (512, 256, 256, 512
+    threads) and keeps one; the results are those of a fixed CTA size, bit for bit."""
+    mbir = lib_built
+    tuned, fixed = make_engines(mbir), make_engines(mbir)
+    with mbir.Batch(0) as bt, mbir.Batch(0) as bx:
+        for e in tuned:
+            bt.add(e)
+        for e in fixed:
+            bx.add(e)
+        bx.set_threads(512)
+        seen = []
+        for k in range(7):
+            seen.append(bt.threads())
+            np.testing.assert_array_equal(bt.sweep(outer=k), bx.sweep(outer=k))
+        assert seen[:5] == [0] * 5 and seen[5] in (256, 512) and seen[6] == seen[5], seen
+    for a, b in zip(tuned, fixed):
+        np.testing.assert_array_equal(a.volume(), b.volume())
+        np.testing.assert_array_equal(a.error_sinogram(), b.error_sinogram())
+
+
 def test_batch_run_to_tolerance(lib_built):
     mbir = lib_built
     engines = make_engines(mbir)
