@@ -275,6 +275,63 @@ def _rank_bf(rank, world, port, q):
         dist.destroy_process_group()
 
 
+class OracleOwnedBFBackend(OracleBFBackend):
+    """A bright-field oracle rank holding only its slab, halo planes and their detector rows."""
+
+    def __init__(self, o, schedule, dims, base):
+        super().__init__(o, schedule)
+        self.dims_g = tuple(dims)
+        self.base = base
+
+    def dims(self):
+        return self.dims_g
+
+    def set_slab(self, y0, y1):
+        super().set_slab(y0 - self.base, y1 - self.base)
+
+    def get_planes(self, y, n):
+        return super().get_planes(y - self.base, n)
+
+    def set_planes(self, y, planes):
+        super().set_planes(y - self.base, planes)
+
+
+def _rank_owned_bf(rank, world, port, q):
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    for d in (os.path.join(root, "openmbir-tem_gb300"), os.path.join(root, "oracle"), here):
+        sys.path.insert(0, d)
+    import torch
+    import torch.distributed as dist
+    import mbir
+    import oracle
+    import shard
+    from conftest import bf_case, bf_params
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world)
+    try:
+        y, ang, th = bf_case(n_r=48, n_t=12)
+        p = bf_params(mbir, th, nhicd=0)
+        e = mbir.Engine(p)  # host-only use: geometry and schedule
+        e.set_sinogram(y, ang)
+        dims = e.dims()
+        (y0, y1), base, top = shard.owned_slab(dims[2], world, rank)
+        o = oracle.Oracle(oracle.params_from_mbir(p), np.ascontiguousarray(y[:, :, base:top]),
+                          ang)
+        o.prepare()
+        be = OracleOwnedBFBackend(o, e.schedule, dims, base)
+        (y0, y1), hist = shard.run_sharded_bf(dist, be, 3, nhicd=False)
+        vol = np.zeros(dims[:3])
+        vol[:, :, y0:y1] = o.volume()[:, :, y0 - base:y1 - base]
+        t = torch.from_numpy(vol)
+        dist.all_reduce(t)
+        if rank == 0:
+            q.put((t.numpy(), o.offset().copy(), o.variance().copy(), np.array(hist)))
+    finally:
+        dist.destroy_process_group()
+
+
 def _run_ranks(target, world):
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
@@ -288,6 +345,19 @@ def _run_ranks(target, world):
         pr.join(timeout=60)
         assert pr.exitcode == 0
     return out
+
+
+def test_owned_slabs_bright_field_two_cpu_ranks_match_one_rank(oracle_mod, lib_built):
+    """Bright-field ranks holding only their slab, halo planes and rows (12 slices over two
+    ranks: 7 and 8 held) give the result of one rank holding the whole series; the variance
+    sums carry the number of entries they cover, so the sub-problems' own row counts do not
+    enter the variance."""
+    vol2, off2, var2, hist2 = _run_ranks(_rank_owned_bf, 2)
+    vol1, off1, var1, hist1 = _run_ranks(_rank_owned_bf, 1)
+    np.testing.assert_array_equal(hist2[0][2:], hist1[0][2:])
+    assert np.linalg.norm(vol2 - vol1) / np.linalg.norm(vol1) <= 1e-9
+    np.testing.assert_allclose(off2, off1, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(var2, var1, rtol=1e-9)
 
 
 def test_two_cpu_ranks_bright_field_match_one_rank(oracle_mod, lib_built):
