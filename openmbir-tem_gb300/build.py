@@ -107,14 +107,17 @@ CLI_PROGRAMS = {"HAADFReconstruction": 0, "BFReconstruction": 1}
 
 def build_cli(verbose=False):
     """The two command-line programs (bin/HAADFReconstruction, bin/BFReconstruction) over the
-    C ABI, linked to libmbir_gb300.so next to them (rpath $ORIGIN/..)."""
+    C++ pipeline classes of include/mbir_gb300.hpp, linked to libmbir_gb300.so next to them
+    (rpath $ORIGIN/..)."""
     os.makedirs(BIN, exist_ok=True)
     for name, bf in CLI_PROGRAMS.items():
         exe = os.path.join(BIN, name)
-        deps = [CLI_SRC, LIB, os.path.join(ROOT, "include", "mbir_gb300.h")]
+        deps = [CLI_SRC, LIB, os.path.join(ROOT, "include", "mbir_gb300.h"),
+                os.path.join(ROOT, "include", "mbir_gb300.hpp")]
         if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(d) for d in deps):
             continue
-        cmd = ["g++", "-std=c++17", "-O2", f"-DMBIR_CLI_BF={bf}", "-o", exe, CLI_SRC,
+        cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-pthread", f"-DMBIR_CLI_BF={bf}", "-o", exe,
+               CLI_SRC,
                f"-L{HERE}", "-l:libmbir_gb300.so", "-Wl,-rpath,$ORIGIN/.."]
         if verbose:
             print(" ".join(cmd), flush=True)

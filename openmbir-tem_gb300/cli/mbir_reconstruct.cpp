@@ -4,23 +4,18 @@
 // Built twice (MBIR_CLI_BF = 0 / 1) into openmbir-tem_gb300/bin/.  Each program accepts the flag
 // set of the reference program of the same name (Code/Applications/HAADFReconstruction/
 // HAADFReconstructionArgsParser.cpp:143-211, Code/Applications/BFReconstruction/
-// BFReconstructionArgsParser.cpp:145-226) and runs the multi-resolution pipeline the way
-// HAADF_MultiResolutionReconstruction::execute / BFMultiResolutionReconstruction::execute do
-// (HAADF_MultiResolutionReconstruction.cpp:175-485): per level i of L, voxels of
-// 2^(L-1-i) * final_resolution detector pixels, sigma_x * 2^((L-1-i)(1-3/p)), one inner iteration
-// after the first level, the stop threshold doubled from level 2, the previous level's volume
-// replicated 2x2x2 and its gains, offsets and variances handed on.  Each level writes its files
-// (ReconstructedObject.bin, Final*Parameters.bin, FinalVariances.bin, ReconstructedSinogram.bin)
-// to <output dir>/<factor>x/; the last one also writes the MRC output file and, beside it, the
-// .vtk and .am volumes.  Parameters that the reference's pipeline keeps in float members are
-// rounded the same way (mbir_params.float_params).  The bright-field program always extends the
-// object (the reference's pipeline default, which its command line never changes).
+// BFReconstructionArgsParser.cpp:145-226) and runs the multi-resolution pipeline through
+// mbir_gb300::HAADF_MultiResolutionReconstruction / BFMultiResolutionReconstruction
+// (include/mbir_gb300.hpp), the classes that replace the reference's pipeline classes: per level
+// the voxel size, sigma_x, iteration and stop-threshold rules of
+// HAADF_MultiResolutionReconstruction.cpp:175-485, the previous level's volume replicated 2x2x2
+// and its nuisance handed on, each level's files in <output dir>/<factor>x/ and the MRC, .vtk
+// and .am volumes from the last level.  The pipeline's messages are printed one per line.  The
+// bright-field program always extends the object (the reference's pipeline default, which its
+// command line never changes).
 //
 // Exit status: 0 on success, 1 on a parse or reconstruction error (the reference returns
 // EXIT_FAILURE for both).
-#include <sys/stat.h>
-#include <sys/types.h>
-
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -31,7 +26,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/mbir_gb300.h"
+#include "../../include/mbir_gb300.hpp"
 
 #ifndef MBIR_CLI_BF
 #define MBIR_CLI_BF 0
@@ -182,47 +177,6 @@ bool parse_ints(const std::string& s, std::vector<int>& v) {
   return true;
 }
 
-std::string parent_path(const std::string& f) {
-  const size_t k = f.find_last_of('/');
-  return k == std::string::npos ? "." : (k == 0 ? "/" : f.substr(0, k));
-}
-std::string stem(const std::string& f) {
-  const size_t k = f.find_last_of('/');
-  std::string b = k == std::string::npos ? f : f.substr(k + 1);
-  const size_t d = b.find_last_of('.');
-  return d == std::string::npos ? b : b.substr(0, d);
-}
-bool make_dirs(const std::string& d) {
-  std::string acc;
-  for (size_t i = 0; i <= d.size(); ++i) {
-    if (i == d.size() || d[i] == '/') {
-      if (!acc.empty()) {
-        struct stat st;
-        if (stat(acc.c_str(), &st) != 0 && mkdir(acc.c_str(), 0755) != 0) return false;
-      }
-    }
-    if (i < d.size()) acc.push_back(d[i]);
-  }
-  return true;
-}
-
-// --initial_recon_file: doubles in y-x-z order (InitialReconstructionBinReader.cpp:101-155),
-// returned as [z][x][y] floats of the given size
-bool read_object_bin(const std::string& path, int n_z, int n_x, int n_y, std::vector<double>& out) {
-  FILE* f = std::fopen(path.c_str(), "rb");
-  if (!f) return false;
-  std::vector<double> buf(static_cast<size_t>(n_z) * n_x * n_y);
-  const size_t got = std::fread(buf.data(), sizeof(double), buf.size(), f);
-  std::fclose(f);
-  if (got != buf.size()) return false;
-  out.assign(buf.size(), 0.0);
-  size_t k = 0;
-  for (int y = 0; y < n_y; ++y)
-    for (int x = 0; x < n_x; ++x)
-      for (int z = 0; z < n_z; ++z) out[(static_cast<size_t>(z) * n_x + x) * n_y + y] = buf[k++];
-  return true;
-}
-
 double num(const std::map<std::string, std::string>& a, const char* k) {
   return std::strtod(a.at(k).c_str(), nullptr);
 }
@@ -251,35 +205,40 @@ int main(int argc, char** argv) {
   const std::string bright_field =
       (!MBIR_CLI_BF && a.count("brightfield")) ? a["brightfield"] : std::string();
 
-  mbir_params p;
-  mbir_params_default(&p, MBIR_CLI_BF ? MBIR_MODALITY_BF : MBIR_MODALITY_HAADF);
-  p.float_params = 1;
-  p.sample_thickness = num(a, "thickness");
-  p.tilt_selection = inum(a, "tilt_selection");
-  p.diffuseness = num(a, "diffuseness");
-  p.final_resolution = inum(a, "final_resolution");
-  p.sigma_x = num(a, "sigma_x");
-  p.stop_threshold = num(a, "stop_threshold");
-  p.num_resolutions = inum(a, "num_resolutions");
-  p.target_gain = num(a, "target_gain");
-  p.outer_iterations = inum(a, "outer_iterations");
-  p.inner_iterations = inum(a, "inner_iterations");
-  p.default_variance = num(a, "default_variance");
-  p.default_recon_value = num(a, "default_recon_value");
-  if (MBIR_CLI_BF) {
-    p.bragg_threshold = num(a, "bragg_T");
-    p.bragg_delta = num(a, "bragg_delta");
-    p.bf_offset = num(a, "bf_offset");
-    p.default_dosage = num(a, "default_dosage");
-    p.use_default_offset = a.count("use_default_dosage") ? 1 : 0;
-    p.extend_object = 1;
-  } else {
-    p.default_offset = num(a, "default_offset");
-    p.use_default_offset = a.count("use_default_offset") ? 1 : 0;
-    p.extend_object = a.count("extend_object") ? 1 : 0;
-  }
-  // the reference always hands the engine a subvolume (six zeros when the flag is absent)
-  p.use_subvolume = 1;
+#if MBIR_CLI_BF
+  mbir_gb300::BFMultiResolutionReconstruction m;
+#else
+  mbir_gb300::HAADF_MultiResolutionReconstruction m;
+#endif
+  m.setInputFile(a["sinofile"]);
+  m.setOutputFile(a["outputfile"]);
+  if (!bright_field.empty()) m.setBrightFieldFile(bright_field);
+  if (a.count("initial_recon_file")) m.setInitialReconstructionFile(a["initial_recon_file"]);
+  m.setDeleteTempFiles(a.count("delete_tmp_files") > 0);
+  m.setSampleThickness(num(a, "thickness"));
+  m.setTiltSelection(inum(a, "tilt_selection"));
+  m.setMRFShapeParameter(num(a, "diffuseness"));
+  m.setFinalResolution(inum(a, "final_resolution"));
+  m.setSigmaX(num(a, "sigma_x"));
+  m.setStopThreshold(num(a, "stop_threshold"));
+  m.setNumberResolutions(inum(a, "num_resolutions"));
+  m.setTargetGain(num(a, "target_gain"));
+  m.setInterpolateInitialReconstruction(a.count("interpolate_initial_recon") > 0);
+  m.setOuterIterations(inum(a, "outer_iterations"));
+  m.setInnerIterations(inum(a, "inner_iterations"));
+  m.setDefaultVariance(num(a, "default_variance"));
+  m.setInitialReconstructionValue(num(a, "default_recon_value"));
+#if MBIR_CLI_BF
+  m.setBraggThreshold(num(a, "bragg_T"));
+  m.setBraggDelta(num(a, "bragg_delta"));
+  m.setBfOffset(num(a, "bf_offset"));
+  m.setDefaultDosage(num(a, "default_dosage"));
+  m.setUseDefaultDosage(a.count("use_default_dosage") > 0);
+#else
+  m.setDefaultOffsetValue(num(a, "default_offset"));
+  m.setUseDefaultOffset(a.count("use_default_offset") > 0);
+  m.setExtendObject(a.count("extend_object") > 0);
+#endif
   if (a.count("subvolume")) {
     std::vector<int> sv;
     if (!parse_ints(a["subvolume"], sv) || sv.size() != 6) {
@@ -287,132 +246,23 @@ int main(int argc, char** argv) {
                   "64,128,256,80,150,280\nError Parsing the arguments.\n");
       return EXIT_FAILURE;
     }
-    for (int i = 0; i < 6; ++i) p.subvolume[i] = sv[i];
+    m.setSubvolume(sv);
   }
   if (a.count("exclude_views")) {
     std::vector<int> ev;
-    if (!parse_ints(a["exclude_views"], ev) || ev.size() > 256) {
+    if (!parse_ints(a["exclude_views"], ev) || !m.setViewMasks(ev)) {
       std::printf("Error Parsing the Tilt Mask Values. They should be entered as 4,7,12,34,67\n"
                   "Error Parsing the arguments.\n");
       return EXIT_FAILURE;
     }
-    p.n_excluded_views = static_cast<int32_t>(ev.size());
-    for (size_t i = 0; i < ev.size(); ++i) p.excluded_views[i] = ev[i];
   }
-  const std::string sino = a["sinofile"], output = a["outputfile"];
-  const std::string out_dir = parent_path(output);
-  if (!make_dirs(out_dir)) {
-    std::printf("Error creating the output directory '%s'\n   Exiting Now.\n", out_dir.c_str());
-    return EXIT_FAILURE;
-  }
-  const int levels = p.num_resolutions > 0 ? p.num_resolutions : 1;
-  const int interp = (1 << (levels - 1)) * std::max(1, p.final_resolution);
-  // p = diffuseness + 1 in float, as the pipeline computes it
-  const double pq = static_cast<double>(static_cast<float>(p.diffuseness) + 1.0f);
+  m.setMessageHandler([](const std::string& msg) { std::printf("%s\n", msg.c_str()); });
   const auto t0 = std::chrono::steady_clock::now();
-  std::vector<double> prev;
-  int prev_dims[3] = {0, 0, 0};
-  std::vector<double> g, o, v;
-  std::vector<std::string> temp_files;
-  for (int i = 0; i < levels; ++i) {
-    mbir_params q = p;
-    q.level = i;
-    q.qggmrf_q = pq;
-    q.sigma_x = std::pow(2.0, (levels - 1 - i) * (1 - 3 / pq)) *
-                static_cast<double>(static_cast<float>(p.sigma_x));
-    if (i > 0) {
-      q.inner_iterations = 1;
-      // later levels take the nuisance and the volume from the level before
-      q.default_recon_value = 0.0;
-      q.default_variance = 1.0;
-      q.use_default_offset = 0;
-      q.default_offset = 0.0;
-    }
-    if (i >= 2) q.stop_threshold = static_cast<float>(p.stop_threshold) * 2.0f;
-    q.interpolate_initial_recon = i == 0 ? (a.count("interpolate_initial_recon") ? 1 : 0) : 1;
-    const std::string level_dir = out_dir + "/" + std::to_string(interp >> i) + "x";
-    if (!make_dirs(level_dir)) {
-      std::printf("Could not create path: %s\n", level_dir.c_str());
-      return EXIT_FAILURE;
-    }
-    mbir_engine* e = mbir_create(&q);
-    if (!e) {
-      std::printf("Error Reconstructing the Data\n");
-      return EXIT_FAILURE;
-    }
-    int rc = mbir_load_sinogram_mrc(e, sino.c_str());
-    if (rc == MBIR_OK && !bright_field.empty()) rc = mbir_load_bright_field_mrc(e, bright_field.c_str());
-    int32_t d[6] = {0, 0, 0, 0, 0, 0};
-    if (rc == MBIR_OK) rc = mbir_get_dims(e, d);
-    if (rc == MBIR_OK && i == 0 && a.count("initial_recon_file") &&
-        !a["initial_recon_file"].empty()) {
-      const int f = q.interpolate_initial_recon ? 2 : 1;
-      std::vector<double> init;
-      if (!read_object_bin(a["initial_recon_file"], d[0] / f, d[1] / f, d[2] / f, init)) {
-        std::printf("Error opening Input file '%s'\n", a["initial_recon_file"].c_str());
-        mbir_destroy(e);
-        return EXIT_FAILURE;
-      }
-      rc = mbir_set_initial_volume_f64(e, init.data(), static_cast<int64_t>(init.size()));
-    }
-    if (rc == MBIR_OK && i > 0) {
-      rc = mbir_set_initial_volume_f64(e, prev.data(), static_cast<int64_t>(prev.size()));
-      if (rc == MBIR_OK) rc = mbir_set_initial_nuisance(e, g.data(), o.data(), v.data());
-    }
-    std::printf("%dx: reconstructing %d x %d x %d voxels (z, x, y) from %d views\n", interp >> i,
-                d[0], d[1], d[2], d[3]);
-    // the HAADF program's intermediate images, <outer>_<inner>_ReconstructedVolume.rec
-    if (rc == MBIR_OK && !MBIR_CLI_BF) rc = mbir_set_intermediate_dir(e, level_dir.c_str());
-    if (rc == MBIR_OK) rc = mbir_run(e);
-    if (rc == MBIR_OK) {
-      const bool last = i == levels - 1;
-      const std::string vtk = out_dir + "/" + stem(output) + ".vtk";
-      const std::string am = out_dir + "/" + stem(output) + ".am";
-      rc = last ? mbir_write_outputs_ex(e, level_dir.c_str(), output.c_str(), vtk.c_str(),
-                                        am.c_str())
-                : mbir_write_outputs(e, level_dir.c_str(), nullptr);
-      for (const char* n : {"ReconstructedObject.bin", "FinalGainParameters.bin",
-                            "FinalOffsetParameters.bin", "FinalVariances.bin",
-                            "ReconstructedSinogram.bin"})
-        temp_files.push_back(level_dir + "/" + n);
-      for (int o = 0; o < q.outer_iterations; ++o)
-        for (int k = 0; k < std::max(1, q.inner_iterations); ++k) {
-          const std::string rec = level_dir + "/" + std::to_string(o) + "_" + std::to_string(k) +
-                                  "_ReconstructedVolume.rec";
-          if (FILE* f = std::fopen(rec.c_str(), "rb")) {
-            std::fclose(f);
-            temp_files.push_back(rec);
-          }
-        }
-    }
-    if (rc == MBIR_OK) {
-      prev.assign(static_cast<size_t>(d[0]) * d[1] * d[2], 0.0);
-      g.assign(d[3], 0.0);
-      o.assign(d[3], 0.0);
-      v.assign(d[3], 0.0);
-      rc = mbir_get_volume_f64(e, prev.data(), static_cast<int64_t>(prev.size()));
-      if (rc == MBIR_OK) rc = mbir_get_nuisance(e, g.data(), o.data(), v.data());
-      prev_dims[0] = d[0];
-      prev_dims[1] = d[1];
-      prev_dims[2] = d[2];
-    }
-    if (rc != MBIR_OK) {
-      std::printf("%s\nError Reconstructing the Data\n", mbir_last_error(e));
-      mbir_destroy(e);
-      return EXIT_FAILURE;
-    }
-    mbir_status st;
-    mbir_status_get(e, &st);
-    std::printf("%dx: %d ICD calls, %lld voxel updates, ICD device time %.1f ms\n", interp >> i,
-                st.sweeps_done, static_cast<long long>(st.voxels_updated), st.icd_ms_total);
-    mbir_destroy(e);
-  }
-  if (a.count("delete_tmp_files"))
-    for (const std::string& f : temp_files) std::remove(f.c_str());
+  if (m.execute() != MBIR_OK) return EXIT_FAILURE;
   const double s =
       std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  std::printf("Final Dimensions of Object:\n  Nx = %d\n  Ny = %d\n  Nz = %d\n", prev_dims[1],
-              prev_dims[2], prev_dims[0]);
+  const int32_t* d = m.getDims();
+  std::printf("Final Dimensions of Object:\n  Nx = %d\n  Ny = %d\n  Nz = %d\n", d[1], d[2], d[0]);
   std::printf("Total Running Time: %.3f s\nCompleted MBIR Reconstruction Run\n", s);
   return EXIT_SUCCESS;
 }
