@@ -192,7 +192,11 @@ void Server::prepare_loop() {
       Request* r = admitted[k];
       r->t_admit = now_s();
       rcs[k] = r->engine->prepare();
-      if (rcs[k]) msgs[k] = r->engine->last_error();
+      if (rcs[k]) {
+        // the request's device memory goes back now: the budget already counts it as free
+        msgs[k] = r->engine->last_error();
+        r->engine.reset();
+      }
     }
     lk.lock();
     preparing_ -= static_cast<int>(admitted.size());
@@ -220,10 +224,12 @@ void Server::loop() {
     std::vector<std::pair<Request*, std::string>> failed;
     std::vector<Request*> ok;
     for (Request* r : joining) {
-      if (batch_->add(r->engine.get()))
+      if (batch_->add(r->engine.get())) {
         failed.emplace_back(r, batch_->last_error());
-      else
+        r->engine.reset();  // not in the batch: free its device memory outside the lock
+      } else {
         ok.push_back(r);
+      }
     }
     lk.lock();
     for (auto& f : failed) retire(f.first, MBIR_EDEVICE, f.second);
@@ -279,9 +285,15 @@ void Server::loop() {
             finished.push_back(cur[k]);
         }
       }
-      for (Request* r : finished) {
+      for (auto it = finished.begin(); it != finished.end();) {
+        Request* r = *it;
         r->result.resize(static_cast<size_t>(r->dims[0]) * r->dims[1] * r->dims[2]);
-        r->engine->get_volume(r->result.data(), static_cast<int64_t>(r->result.size()));
+        if (r->engine->get_volume(r->result.data(), static_cast<int64_t>(r->result.size()))) {
+          broken.emplace_back(r, r->engine->last_error());
+          it = finished.erase(it);
+        } else {
+          ++it;
+        }
       }
     }
     lk.lock();
