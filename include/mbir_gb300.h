@@ -313,6 +313,24 @@ int32_t mbir_write_outputs_ex(mbir_engine* e, const char* dir, const char* mrc_p
  * its temporary directory (HAADF_ReconstructionEngine.cpp:757-763); NULL or "" turns it off. */
 int32_t mbir_set_intermediate_dir(mbir_engine* e, const char* dir);
 
+/* Observer of an engine's messages, in place of the reference's Observable::notify(msg,
+ * progress, aspect) (Code/MBIRLib/Common/Observable.h:65-101); the aspect numbers follow its
+ * ObserverAspect order.  The engine sends "Calculating A Matrix...." (0, progress message) and
+ * "Starting Forward Projection" (10, progress value and message) from prepare, the path of each
+ * intermediate image (0, intermediate image), "Reconstruction Complete" (100, progress value
+ * and message) at the end of mbir_run, and the text of every error it returns (100, error
+ * message; the same text as mbir_last_error).  fn runs on the thread of the entry point that
+ * sends the message, must not throw, and must not call the same engine except mbir_cancel,
+ * mbir_status_get and mbir_last_error.  fn = NULL removes the observer. */
+#define MBIR_UPDATE_PROGRESS_VALUE 0
+#define MBIR_UPDATE_PROGRESS_MESSAGE 1
+#define MBIR_UPDATE_WARNING_MESSAGE 2
+#define MBIR_UPDATE_ERROR_MESSAGE 3
+#define MBIR_UPDATE_PROGRESS_VALUE_AND_MESSAGE 4
+#define MBIR_UPDATE_INTERMEDIATE_IMAGE 5
+typedef void (*mbir_observer_fn)(const char* msg, int32_t progress, int32_t aspect, void* user);
+int32_t mbir_set_observer(mbir_engine* e, mbir_observer_fn fn, void* user);
+
 /* Multi-resolution pipeline (HAADF_MultiResolutionReconstruction::execute,
  * HAADF_MultiResolutionReconstruction.cpp:175-485): coarse-to-fine levels with sigma_x scaling
  * and 2x voxel replication hand-off; writes the final volume to out ([z][x][y], n floats). */

@@ -44,6 +44,8 @@
 namespace mbir_gb300 {
 
 using MessageHandler = std::function<void(const std::string&)>;
+/* an engine's messages: text, progress (0-100) and MBIR_UPDATE_* aspect (mbir_set_observer) */
+using Observer = std::function<void(const std::string& msg, int progress, int aspect)>;
 
 namespace detail {
 
@@ -156,6 +158,9 @@ class ReconstructionEngine {
   }
   /* HAADF: write <dir>/<outer>_<inner>_ReconstructedVolume.rec after every inner iteration */
   void setIntermediateDir(const std::string& dir) { inter_dir_ = dir; }
+  /* the engine's progress, intermediate-image and error messages (the reference's observers);
+   * takes effect at the next load */
+  void setObserver(Observer o) { observer_ = std::move(o); }
 
   void setCancel(bool v) {
     cancel_.store(v);
@@ -176,6 +181,7 @@ class ReconstructionEngine {
       std::lock_guard<std::mutex> lk(mu_);
       e_ = e;
     }
+    if (observer_) mbir_set_observer(e_, &ReconstructionEngine::forward_message, this);
     int rc;
     if (!sino_file_.empty())
       rc = mbir_load_sinogram_mrc(e_, sino_file_.c_str());
@@ -251,6 +257,13 @@ class ReconstructionEngine {
   mbir_engine* handle() { return e_; }
 
  private:
+  static void forward_message(const char* msg, int32_t progress, int32_t aspect, void* self) {
+    try {
+      static_cast<ReconstructionEngine*>(self)->observer_(msg ? msg : "", progress, aspect);
+    } catch (...) {
+      // an observer's exception must not cross the C ABI
+    }
+  }
   int ok() {
     err_ = MBIR_OK;
     msg_.clear();
@@ -277,6 +290,7 @@ class ReconstructionEngine {
   double delta_r_ = 1.0, delta_t_ = 1.0;
   std::vector<double> init_, init_g_, init_o_, init_v_;
   int32_t dims_[6] = {0, 0, 0, 0, 0, 0};
+  Observer observer_;
   mbir_engine* e_ = nullptr;
   bool loaded_ = false;
   std::mutex mu_;  // guards e_ against a concurrent setCancel
@@ -367,6 +381,8 @@ class MultiResolutionReconstruction {
   mbir_params& params() { return p_; }
 
   void setMessageHandler(MessageHandler h) { notify_ = std::move(h); }
+  /* the running level's engine messages (ReconstructionEngine::setObserver) */
+  void setObserver(Observer o) { observer_ = std::move(o); }
   void setCancel(bool v) {
     cancel_.store(v);
     std::lock_guard<std::mutex> lk(mu_);
@@ -411,6 +427,7 @@ class MultiResolutionReconstruction {
       if (!detail::make_dirs(level_dir)) return fail(MBIR_EIO, "Could not create path: " + level_dir);
       auto eng = std::make_shared<ReconstructionEngine>(q.modality);
       eng->setParams(q);
+      if (observer_) eng->setObserver(observer_);
       eng->setSinogramFile(input_);
       if (!bf && !bright_field_.empty()) eng->setBrightFieldFile(bright_field_);
       {
@@ -510,6 +527,7 @@ class MultiResolutionReconstruction {
   std::string input_, output_, temp_dir_, bright_field_, initial_file_;
   bool delete_temp_ = false, interpolate_ = false;
   MessageHandler notify_;
+  Observer observer_;
   std::mutex mu_;  // guards current_ against a concurrent setCancel
   std::shared_ptr<ReconstructionEngine> current_;
   std::atomic<bool> cancel_{false};

@@ -197,6 +197,9 @@ int32_t mbir_set_bright_field(mbir_engine* e, const float* counts, int32_t n_the
 int32_t mbir_set_intermediate_dir(mbir_engine* e, const char* dir) {
   return guarded(e, [&](mbir::Engine& m) { return m.set_intermediate_dir(dir); });
 }
+int32_t mbir_set_observer(mbir_engine* e, mbir_observer_fn fn, void* user) {
+  return guarded(e, [&](mbir::Engine& m) { return m.set_observer(fn, user); });
+}
 int32_t mbir_load_bright_field_mrc(mbir_engine* e, const char* path) {
   return guarded(e, [&](mbir::Engine& m) { return m.load_bright_field_mrc(path); });
 }

@@ -178,7 +178,12 @@ void Engine::add_kernel_time() {
 int Engine::fail(int code, const std::string& msg) {
   err_ = msg;
   if (p_.verbose) std::fprintf(stderr, "mbir: %s\n", msg.c_str());
+  notify(err_, 100, MBIR_UPDATE_ERROR_MESSAGE);
   return code;
+}
+
+void Engine::notify(const std::string& msg, int progress, int aspect) const {
+  if (observer_) observer_(msg.c_str(), progress, aspect, observer_user_);
 }
 
 int Engine::cuda_check(int code, const char* what) {
@@ -749,6 +754,7 @@ int Engine::prepare() {
   if (state_ >= 2) release();
   if (p_.order_mode == MBIR_ORDER_REFERENCE && g_.n_theta > kMaxViewsShaped)
     return fail(MBIR_ENOTSUP, "prepare: the reference-order modes take at most 160 views");
+  notify("Calculating A Matrix....", 0, MBIR_UPDATE_PROGRESS_MESSAGE);
   int rc;
   if ((rc = build_host())) return rc;
   if ((rc = alloc_device())) return rc;
@@ -913,6 +919,7 @@ int Engine::prepare() {
     shape_ = d == 0 ? 1 : d + 2;
   }
   // forward projection + error sinogram (HAADF_ReconstructionEngine.cpp:636-691)
+  notify("Starting Forward Projection", 10, MBIR_UPDATE_PROGRESS_VALUE_AND_MESSAGE);
   if ((rc = forward_project())) return rc;
   if (bf_ && (rc = bf_upload())) return rc;
   if (bf_ && (rc = bf_prepare_schedule())) return rc;
@@ -1363,6 +1370,7 @@ int Engine::run() {
     if ((rc = bf_run())) return rc;
     state_ = 4;
     total_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    notify("Reconstruction Complete", 100, MBIR_UPDATE_PROGRESS_VALUE_AND_MESSAGE);
     return MBIR_OK;
   }
   double stop = p_.stop_threshold;
@@ -1374,10 +1382,12 @@ int Engine::run() {
       double st[4];
       if ((rc = sweep(outer, inner, st))) return rc;
       // the intermediate image of every inner iteration (HAADF_ReconstructionEngine.cpp:757-763)
-      if (!interm_dir_.empty() &&
-          (rc = write_volume_mrc(interm_dir_ + "/" + std::to_string(outer) + "_" +
-                                 std::to_string(inner) + "_ReconstructedVolume.rec")))
-        return rc;
+      if (!interm_dir_.empty()) {
+        const std::string image = interm_dir_ + "/" + std::to_string(outer) + "_" +
+                                  std::to_string(inner) + "_ReconstructedVolume.rec";
+        if ((rc = write_volume_mrc(image))) return rc;
+        notify(image, 0, MBIR_UPDATE_INTERMEDIATE_IMAGE);
+      }
       if (p_.cost_every_sweep && (rc = compute_cost(nullptr, nullptr))) return rc;
       status = 1;
       if (st[1] > 0 && (st[0] / st[1]) < stop) {
@@ -1397,6 +1407,7 @@ int Engine::run() {
   }
   state_ = 4;
   total_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  notify("Reconstruction Complete", 100, MBIR_UPDATE_PROGRESS_VALUE_AND_MESSAGE);
   return MBIR_OK;
 }
 
@@ -1534,6 +1545,12 @@ int Engine::status(mbir_status* st) const {
 
 int Engine::set_intermediate_dir(const char* dir) {
   interm_dir_ = dir ? dir : "";
+  return MBIR_OK;
+}
+
+int Engine::set_observer(mbir_observer_fn fn, void* user) {
+  observer_ = fn;
+  observer_user_ = fn ? user : nullptr;
   return MBIR_OK;
 }
 

@@ -87,6 +87,8 @@ class Engine {
   int set_initial_volume_f64(const double* vol, int64_t n);
   // HAADF: after every inner iteration the volume as <dir>/<outer>_<inner>_ReconstructedVolume.rec
   int set_intermediate_dir(const char* dir);
+  int set_observer(mbir_observer_fn fn, void* user);
+  void notify(const std::string& msg, int progress, int aspect) const;
   int write_volume_mrc(const std::string& path);
   template <typename T>
   int set_initial_volume_t(const T* vol, int64_t n);
@@ -220,6 +222,8 @@ class Engine {
   std::vector<float> counts_;     // [theta][r][t]
   std::vector<double> bfm_;       // [theta][r][t] bright-field count + BF_OFFSET (assisted HAADF)
   std::string interm_dir_;        // per-iteration MRC volumes (empty: none)
+  mbir_observer_fn observer_ = nullptr;  // progress and error messages (null: none)
+  void* observer_user_ = nullptr;
   std::vector<double> tilts_;     // degrees
   std::vector<double> init_vol_;  // optional [z][x][y]
   std::vector<double> user_gain_, user_offset_, user_var_;

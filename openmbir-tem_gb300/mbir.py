@@ -26,6 +26,10 @@ HAADF, BF = 0, 1
 ORDER_PARALLEL, ORDER_REFERENCE = 0, 1
 FP32, FP64 = 0, 1
 SEED_PER_CALL, SEED_FIXED = 0, 1
+# observer aspects (mbir_set_observer), the reference's ObserverAspect order
+(UPDATE_PROGRESS_VALUE, UPDATE_PROGRESS_MESSAGE, UPDATE_WARNING_MESSAGE, UPDATE_ERROR_MESSAGE,
+ UPDATE_PROGRESS_VALUE_AND_MESSAGE, UPDATE_INTERMEDIATE_IMAGE) = range(6)
+OBSERVER = C.CFUNCTYPE(None, C.c_char_p, C.c_int32, C.c_int32, C.c_void_p)
 
 
 class MbirParams(C.Structure):
@@ -133,6 +137,7 @@ SIGNATURES = {
     "mbir_set_bright_field": (C.c_int32, [C.c_void_p, _F, C.c_int32, C.c_int32, C.c_int32]),
     "mbir_load_bright_field_mrc": (C.c_int32, [C.c_void_p, C.c_char_p]),
     "mbir_set_intermediate_dir": (C.c_int32, [C.c_void_p, C.c_char_p]),
+    "mbir_set_observer": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "mbir_set_initial_volume": (C.c_int32, [C.c_void_p, _F, C.c_int64]),
     "mbir_set_initial_nuisance": (C.c_int32, [C.c_void_p, _D, _D, _D]),
     "mbir_get_dims": (C.c_int32, [C.c_void_p, _I]),
@@ -353,6 +358,20 @@ class Engine:
         """HAADF: <dir>/<outer>_<inner>_ReconstructedVolume.rec after every inner iteration."""
         d = b"" if directory is None else str(directory).encode()
         return self._check(lib().mbir_set_intermediate_dir(self._h, d))
+
+    def set_observer(self, fn):
+        """fn(msg: str, progress: int, aspect: int) receives the engine's messages (aspects
+        UPDATE_*, the reference's ObserverAspect order); None removes it."""
+        if fn is None:
+            self._observer = None
+            return self._check(lib().mbir_set_observer(self._h, None, None))
+
+        def forward(msg, progress, aspect, _user):
+            fn(msg.decode(errors="replace") if msg else "", progress, aspect)
+
+        self._observer = OBSERVER(forward)  # kept alive as long as the engine can call it
+        return self._check(lib().mbir_set_observer(self._h, C.cast(self._observer, C.c_void_p),
+                                                   None))
 
     def load_bright_field_mrc(self, path):
         return self._check(lib().mbir_load_bright_field_mrc(self._h, str(path).encode()))

@@ -7,7 +7,7 @@
 //   compat_classes run <counts.f32> <tilts.f32> n_theta n_r n_t thickness <out.f32>
 //       a HAADF reconstruction through HAADF_ReconstructionEngine from arrays, executed twice
 //       on the same object; writes the first volume ([z][x][y] float32) and says whether the
-//       second equals it
+//       second equals it and how many "Reconstruction Complete" messages the observer saw
 //   compat_classes cancel <counts.f32> <tilts.f32> n_theta n_r n_t thickness
 //       setCancel(true) from another thread once the first sweep is done
 #include <chrono>
@@ -91,6 +91,12 @@ int run(char** argv, bool cancel) {
   small_case_params(e.params(), thickness);
   e.setSinogram(counts.data(), tilts.data(), n_theta, n_r, n_t, 1.0, 1.0);
   if (!cancel) {
+    int complete = 0;
+    e.setObserver([&](const std::string& m, int progress, int aspect) {
+      if (m == "Reconstruction Complete" && progress == 100 &&
+          aspect == MBIR_UPDATE_PROGRESS_VALUE_AND_MESSAGE)
+        ++complete;
+    });
     const int rc = e.execute();
     std::printf("execute %d\n", rc);
     std::vector<float> vol, vol2;
@@ -102,6 +108,7 @@ int run(char** argv, bool cancel) {
     std::printf("execute_again %d\n", e.execute());
     if (e.getVolume(vol2) != MBIR_OK) return 1;
     std::printf("same_volume %d\n", vol == vol2 ? 1 : 0);
+    std::printf("complete %d\n", complete);
     FILE* f = std::fopen(argv[8], "wb");
     if (!f) return 1;
     std::fwrite(vol.data(), sizeof(float), vol.size(), f);

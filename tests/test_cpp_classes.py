@@ -6,8 +6,9 @@ CPU: the header compiles and links against the library; error conditions without
 engine with no sinogram, results read before a load, an output directory that cannot be made, a
 cancel set before execute() gives the reference's -999).  GPU: an engine run from arrays gives
 the same volume, bit for bit, as the C ABI run with the same parameters, twice on the same
-object; setCancel(true) from another thread ends a long run with -999.  The pipeline classes'
-GPU runs are the command-line programs' tests (tests/test_cli.py), which are built on them.
+object, with the observer seeing each run complete; setCancel(true) from another thread ends a
+long run with -999.  The pipeline classes' GPU runs are the command-line programs' tests
+(tests/test_cli.py), which are built on them.
 """
 import os
 import subprocess
@@ -75,6 +76,7 @@ def test_engine_class_matches_c_abi(compat_exe, tmp_path):
     assert out["execute"] == [0] and out["execute_again"] == [0]
     assert out["nuisance"] == [0, shape[0]]
     assert out["same_volume"] == [1]
+    assert out["complete"] == [2]  # the observer, registered at each load
     p = haadf_params(mbir, th)
     with mbir.Engine(p) as e:
         e.set_sinogram(y, ang)
