@@ -313,6 +313,22 @@ int32_t mbir_write_outputs_ex(mbir_engine* e, const char* dir, const char* mrc_p
  * its temporary directory (HAADF_ReconstructionEngine.cpp:757-763); NULL or "" turns it off. */
 int32_t mbir_set_intermediate_dir(mbir_engine* e, const char* dir);
 
+/* Checkpoint and exact resume of a HAADF run (without bright-field data).  mbir_write_checkpoint
+ * (after mbir_run or between step-wise phases) writes to `dir` the reference's level hand-off
+ * files ReconstructedObject.bin, Final{Gain,Offset}Parameters.bin and FinalVariances.bin
+ * (HAADF_MultiResolutionReconstruction.cpp:212-222 reads them back; InitialReconstructionBinReader.cpp:
+ * 73-168) plus ReconstructedSinogram.bin and Checkpoint.bin (the outer iterations mbir_run has
+ * completed, the sweeps done, the stop threshold after its reductions and the error sinogram).
+ * mbir_read_checkpoint, on an engine created with the same parameters and given the same series
+ * (after mbir_set_sinogram / mbir_load_sinogram_mrc), makes every later prepare start from that
+ * state, and mbir_run continues at the checkpoint's outer iteration up to outer_iterations: a
+ * run of N outer iterations and a run of K, checkpointed and resumed to N, give the same bits.
+ * MBIR_EINVAL when the checkpoint comes from another configuration or series, MBIR_EIO when a
+ * file is missing or short, MBIR_ENOTSUP for bright field.  The reference resumes only from a
+ * volume (--initial_recon_file, HAADFReconstructionArgsParser.cpp:189-190). */
+int32_t mbir_write_checkpoint(mbir_engine* e, const char* dir);
+int32_t mbir_read_checkpoint(mbir_engine* e, const char* dir);
+
 /* Observer of an engine's messages, in place of the reference's Observable::notify(msg,
  * progress, aspect) (Code/MBIRLib/Common/Observable.h:65-101); the aspect numbers follow its
  * ObserverAspect order.  The engine sends "Calculating A Matrix...." (0, progress message) and

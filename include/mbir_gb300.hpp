@@ -161,6 +161,12 @@ class ReconstructionEngine {
   /* the engine's progress, intermediate-image and error messages (the reference's observers);
    * takes effect at the next load */
   void setObserver(Observer o) { observer_ = std::move(o); }
+  /* HAADF: resume from a checkpoint directory (mbir_read_checkpoint) at every load; an initial
+   * volume or nuisance set here as well would replace the checkpoint's.  "" turns it off. */
+  void setResumeCheckpoint(const std::string& dir) {
+    resume_dir_ = dir;
+    loaded_ = false;
+  }
 
   void setCancel(bool v) {
     cancel_.store(v);
@@ -194,6 +200,7 @@ class ReconstructionEngine {
       rc = mbir_load_bright_field_mrc(e_, bf_file_.c_str());
     else if (rc == MBIR_OK && !bf_counts_.empty())
       rc = mbir_set_bright_field(e_, bf_counts_.data(), bf_dims_[0], bf_dims_[1], bf_dims_[2]);
+    if (rc == MBIR_OK && !resume_dir_.empty()) rc = mbir_read_checkpoint(e_, resume_dir_.c_str());
     if (rc == MBIR_OK) rc = mbir_get_dims(e_, dims_);
     if (rc != MBIR_OK) return fail(rc, mbir_last_error(e_));
     loaded_ = true;
@@ -246,6 +253,11 @@ class ReconstructionEngine {
     if (!e_) return not_loaded();
     return check(mbir_status_get(e_, &st));
   }
+  /* HAADF: the run's state in dir, for setResumeCheckpoint (mbir_write_checkpoint) */
+  int writeCheckpoint(const std::string& dir) {
+    if (!e_) return not_loaded();
+    return check(mbir_write_checkpoint(e_, dir.c_str()));
+  }
   /* the reference's output files in dir, and the MRC / VTK / Avizo volumes where a path is set */
   int writeOutputs(const std::string& dir, const std::string& mrc = std::string(),
                    const std::string& vtk = std::string(), const std::string& am = std::string()) {
@@ -284,7 +296,7 @@ class ReconstructionEngine {
   }
 
   mbir_params p_{};
-  std::string sino_file_, bf_file_, inter_dir_;
+  std::string sino_file_, bf_file_, inter_dir_, resume_dir_;
   std::vector<float> counts_, tilts_, bf_counts_;
   int32_t n_theta_ = 0, n_r_ = 0, n_t_ = 0, bf_dims_[3] = {0, 0, 0};
   double delta_r_ = 1.0, delta_t_ = 1.0;

@@ -200,6 +200,12 @@ int32_t mbir_set_intermediate_dir(mbir_engine* e, const char* dir) {
 int32_t mbir_set_observer(mbir_engine* e, mbir_observer_fn fn, void* user) {
   return guarded(e, [&](mbir::Engine& m) { return m.set_observer(fn, user); });
 }
+int32_t mbir_write_checkpoint(mbir_engine* e, const char* dir) {
+  return guarded(e, [&](mbir::Engine& m) { return m.write_checkpoint(dir); });
+}
+int32_t mbir_read_checkpoint(mbir_engine* e, const char* dir) {
+  return guarded(e, [&](mbir::Engine& m) { return m.read_checkpoint(dir); });
+}
 int32_t mbir_load_bright_field_mrc(mbir_engine* e, const char* path) {
   return guarded(e, [&](mbir::Engine& m) { return m.load_bright_field_mrc(path); });
 }

@@ -905,9 +905,21 @@ int Engine::prepare() {
   flt_.sig_pq = std::pow(p_.sigma_x, p_.qggmrf_p - p_.qggmrf_q);
   flt_.inv_sig_pq = 1.0 / flt_.sig_pq;
 
+  if (resume_ && bright_field_assisted())
+    return fail(MBIR_ENOTSUP, "checkpoint: HAADF without bright-field data only");
+  if (resume_) {
+    // the checkpoint's gains, offsets and variances exactly (no renormalisation); w = 1/alpha
+    // holds for HAADF with and without the noise model
+    I_ = resume_gain_;
+    mu_ = resume_offset_;
+    alpha_ = resume_var_;
+    for (int k = 0; k < g.n_theta; k++) w_[k] = 1.0 / alpha_[k];
+  }
   if ((rc = upload_views())) return rc;
   state_ = 2;
   sweeps_done_ = 0;
+  outer_next_ = resume_ ? resume_outer_ : 0;
+  stop_now_ = resume_ ? resume_stop_ : p_.stop_threshold;
   // voxel-group shape: the requested one when it covers the views, else the default
   shape_ = 0;
   if (((p_.lane_shape >= 1 && p_.lane_shape <= 4) ||
@@ -921,6 +933,15 @@ int Engine::prepare() {
   // forward projection + error sinogram (HAADF_ReconstructionEngine.cpp:636-691)
   notify("Starting Forward Projection", 10, MBIR_UPDATE_PROGRESS_VALUE_AND_MESSAGE);
   if ((rc = forward_project())) return rc;
+  if (resume_) {
+    // the checkpoint's error sinogram in place of the one the projection rebuilt (that one
+    // differs in the last bits from the sweeps' running updates)
+    const size_t bytes = static_cast<size_t>(g.n_t) * g.n_theta * n_rp_ * rb_;
+    if (resume_e_.size() != bytes)
+      return fail(MBIR_EINVAL, "checkpoint: error sinogram size does not match this engine");
+    cudaMemcpyAsync(d_e_, resume_e_.data(), bytes, cudaMemcpyHostToDevice, s);
+    sweeps_done_ = resume_sweeps_;
+  }
   if (bf_ && (rc = bf_upload())) return rc;
   if (bf_ && (rc = bf_prepare_schedule())) return rc;
   if (p_.lane_shape == 0 && (rc = autotune_shape())) return rc;
@@ -1373,10 +1394,10 @@ int Engine::run() {
     notify("Reconstruction Complete", 100, MBIR_UPDATE_PROGRESS_VALUE_AND_MESSAGE);
     return MBIR_OK;
   }
-  double stop = p_.stop_threshold;
-  int num_iter = p_.inner_iterations;
-  for (int outer = 0; outer < p_.outer_iterations; outer++) {
-    if (outer != 0) num_iter = 1;
+  // a resumed run continues at the checkpoint's outer iteration and stop threshold
+  double stop = stop_now_;
+  for (int outer = outer_next_; outer < p_.outer_iterations; outer++) {
+    const int num_iter = outer == 0 ? p_.inner_iterations : 1;
     int status = 1;
     for (int inner = 0; inner < num_iter; inner++) {
       double st[4];
@@ -1398,12 +1419,10 @@ int Engine::run() {
     }
     if (cancel_.load()) return fail(MBIR_ECANCELLED, "cancelled");
     if (p_.joint_estimation && (rc = joint_estimation())) return rc;
-    if (p_.noise_model) {
-      if ((rc = update_weights())) return rc;
-      if (status == 0 && outer >= 1) break;
-    } else if (status == 0 && outer >= 1) {
-      break;
-    }
+    if (p_.noise_model && (rc = update_weights())) return rc;
+    outer_next_ = outer + 1;
+    stop_now_ = stop;
+    if (status == 0 && outer >= 1) break;
   }
   state_ = 4;
   total_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -1551,6 +1570,126 @@ int Engine::set_intermediate_dir(const char* dir) {
 int Engine::set_observer(mbir_observer_fn fn, void* user) {
   observer_ = fn;
   observer_user_ = fn ? user : nullptr;
+  return MBIR_OK;
+}
+
+namespace {
+// Checkpoint.bin: this header, then the error sinogram's bytes in the engine's device layout
+// ([t][theta][r padded to n_rp], FP32 or FP64)
+struct CheckpointHeader {
+  char magic[8];
+  int32_t v[16];  // kCk* fields below
+  double stop;
+  uint64_t e_bytes;
+};
+constexpr char kCheckpointMagic[8] = {'M', 'B', 'I', 'R', 'C', 'K', 'P', '1'};
+enum {
+  kCkModality, kCkPrecision, kCkExact, kCkOrder, kCkNz, kCkNx, kCkNy, kCkNtheta, kCkNr, kCkNt,
+  kCkNrp, kCkElem, kCkOuterNext, kCkSweeps, kCkFields
+};
+
+bool read_doubles(const std::string& path, std::vector<double>& out, size_t n) {
+  out.assign(n, 0.0);
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return false;
+  const size_t got = std::fread(out.data(), sizeof(double), n, f);
+  const bool at_end = std::fgetc(f) == EOF;
+  std::fclose(f);
+  return got == n && at_end;
+}
+}  // namespace
+
+// Writes the run's state to dir: ReconstructedObject.bin, Final{Gain,Offset}Parameters.bin,
+// FinalVariances.bin (the reference's level hand-off files, read back the way
+// HAADF_MultiResolutionReconstruction.cpp:212-222 reads them) and Checkpoint.bin (outer
+// iterations done, sweeps done, stop threshold, error sinogram).
+int Engine::write_checkpoint(const char* dir) {
+  if (state_ < 2) return fail(MBIR_ESTATE, "write_checkpoint: call prepare first");
+  if (bf_ || bright_field_assisted())
+    return fail(MBIR_ENOTSUP, "write_checkpoint: HAADF without bright-field data only");
+  int rc = write_outputs(dir, nullptr);
+  if (rc) return rc;
+  const Geometry& g = g_;
+  const size_t bytes = static_cast<size_t>(g.n_t) * g.n_theta * n_rp_ * rb_;
+  std::vector<unsigned char> e(bytes);
+  cudaStream_t s = static_cast<cudaStream_t>(stream_);
+  cudaMemcpyAsync(e.data(), d_e_, bytes, cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_check(MBIR_EDEVICE, "checkpoint read-out");
+  CheckpointHeader h{};
+  std::memcpy(h.magic, kCheckpointMagic, sizeof h.magic);
+  const int32_t fields[kCkFields] = {
+      bf_ ? MBIR_MODALITY_BF : MBIR_MODALITY_HAADF, fp64_ ? 1 : 0, exact_ ? 1 : 0,
+      p_.order_mode, g.n_z, g.n_x, g.n_y, g.n_theta, g.n_r, g.n_t, n_rp_,
+      static_cast<int32_t>(rb_), outer_next_, sweeps_done_};
+  std::memcpy(h.v, fields, sizeof fields);
+  h.stop = stop_now_;
+  h.e_bytes = bytes;
+  const std::string path = std::string(dir ? dir : ".") + "/Checkpoint.bin";
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) return fail(MBIR_EIO, "cannot write " + path);
+  const bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 &&
+                  std::fwrite(e.data(), 1, bytes, f) == bytes;
+  if (std::fclose(f) != 0 || !ok) return fail(MBIR_EIO, "cannot write " + path);
+  return MBIR_OK;
+}
+
+// Reads a checkpoint written by an engine of the same configuration and series; every later
+// prepare starts from it (volume, gains, offsets, variances, error sinogram, sweep count) and
+// mbir_run continues at its outer iteration.
+int Engine::read_checkpoint(const char* dir) {
+  if (state_ < 1) return fail(MBIR_ESTATE, "read_checkpoint: set the sinogram first");
+  if (bf_ || bright_field_assisted())
+    return fail(MBIR_ENOTSUP, "read_checkpoint: HAADF without bright-field data only");
+  int rc;
+  if (g_.n_y == 0 && (rc = build_geometry())) return rc;
+  const Geometry& g = g_;
+  const std::string d = dir ? dir : ".";
+  const std::string path = d + "/Checkpoint.bin";
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return fail(MBIR_EIO, "cannot read " + path);
+  CheckpointHeader h{};
+  const bool got = std::fread(&h, sizeof h, 1, f) == 1;
+  int32_t v[kCkFields];
+  std::memcpy(v, h.v, sizeof v);
+  const int32_t want[kCkNrp] = {
+      MBIR_MODALITY_HAADF, fp64_ ? 1 : 0, exact_ ? 1 : 0, p_.order_mode, g.n_z, g.n_x, g.n_y,
+      g.n_theta, g.n_r, g.n_t};
+  if (!got || std::memcmp(h.magic, kCheckpointMagic, sizeof h.magic) != 0) {
+    std::fclose(f);
+    return fail(MBIR_EIO, path + " is not a checkpoint");
+  }
+  if (std::memcmp(v, want, sizeof want) != 0 || v[kCkElem] != static_cast<int32_t>(rb_) ||
+      v[kCkOuterNext] < 0 || v[kCkSweeps] < 0 || h.e_bytes > (uint64_t(1) << 40)) {
+    std::fclose(f);
+    return fail(MBIR_EINVAL, "checkpoint: written by an engine of another configuration or series");
+  }
+  std::vector<unsigned char> e(static_cast<size_t>(h.e_bytes));
+  const bool got_e = std::fread(e.data(), 1, e.size(), f) == e.size();
+  std::fclose(f);
+  if (!got_e) return fail(MBIR_EIO, path + " is truncated");
+  const size_t nv = static_cast<size_t>(g.n_z) * g.n_x * g.n_y;
+  std::vector<double> yxz, gain, offset, var;
+  if (!read_doubles(d + "/ReconstructedObject.bin", yxz, nv) ||
+      !read_doubles(d + "/FinalGainParameters.bin", gain, g.n_theta) ||
+      !read_doubles(d + "/FinalOffsetParameters.bin", offset, g.n_theta) ||
+      !read_doubles(d + "/FinalVariances.bin", var, g.n_theta))
+    return fail(MBIR_EIO, "checkpoint: a .bin file is missing or of the wrong size in " + d);
+  // ReconstructedObject.bin is y-x-z; the engine's initial volume [z][x][y], taken as it is
+  // (no 2x2x2 interpolation)
+  init_vol_.assign(nv, 0.0);
+  size_t k = 0;
+  for (int y = 0; y < g.n_y; ++y)
+    for (int x = 0; x < g.n_x; ++x)
+      for (int z = 0; z < g.n_z; ++z) init_vol_[(static_cast<size_t>(z) * g.n_x + x) * g.n_y + y] = yxz[k++];
+  resume_e_ = std::move(e);
+  resume_gain_ = std::move(gain);
+  resume_offset_ = std::move(offset);
+  resume_var_ = std::move(var);
+  resume_outer_ = v[kCkOuterNext];
+  resume_sweeps_ = v[kCkSweeps];
+  resume_stop_ = h.stop;
+  resume_ = true;
+  host_ready_ = false;
   return MBIR_OK;
 }
 

@@ -88,6 +88,9 @@ class Engine {
   // HAADF: after every inner iteration the volume as <dir>/<outer>_<inner>_ReconstructedVolume.rec
   int set_intermediate_dir(const char* dir);
   int set_observer(mbir_observer_fn fn, void* user);
+  // checkpoint of a HAADF run and its exact resume (the reference's .bin files + Checkpoint.bin)
+  int write_checkpoint(const char* dir);
+  int read_checkpoint(const char* dir);
   void notify(const std::string& msg, int progress, int aspect) const;
   int write_volume_mrc(const std::string& path);
   template <typename T>
@@ -223,6 +226,14 @@ class Engine {
   std::vector<double> bfm_;       // [theta][r][t] bright-field count + BF_OFFSET (assisted HAADF)
   std::string interm_dir_;        // per-iteration MRC volumes (empty: none)
   mbir_observer_fn observer_ = nullptr;  // progress and error messages (null: none)
+  // checkpoints: where the run stands, and the state read_checkpoint hands to every prepare
+  int outer_next_ = 0;    // outer iterations mbir_run has completed
+  double stop_now_ = 0;   // the stop threshold after its reductions
+  bool resume_ = false;
+  int resume_outer_ = 0, resume_sweeps_ = 0;
+  double resume_stop_ = 0;
+  std::vector<unsigned char> resume_e_;  // the error sinogram in its device layout
+  std::vector<double> resume_gain_, resume_offset_, resume_var_;
   void* observer_user_ = nullptr;
   std::vector<double> tilts_;     // degrees
   std::vector<double> init_vol_;  // optional [z][x][y]

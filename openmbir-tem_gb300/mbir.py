@@ -138,6 +138,8 @@ SIGNATURES = {
     "mbir_load_bright_field_mrc": (C.c_int32, [C.c_void_p, C.c_char_p]),
     "mbir_set_intermediate_dir": (C.c_int32, [C.c_void_p, C.c_char_p]),
     "mbir_set_observer": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mbir_write_checkpoint": (C.c_int32, [C.c_void_p, C.c_char_p]),
+    "mbir_read_checkpoint": (C.c_int32, [C.c_void_p, C.c_char_p]),
     "mbir_set_initial_volume": (C.c_int32, [C.c_void_p, _F, C.c_int64]),
     "mbir_set_initial_nuisance": (C.c_int32, [C.c_void_p, _D, _D, _D]),
     "mbir_get_dims": (C.c_int32, [C.c_void_p, _I]),
@@ -372,6 +374,15 @@ class Engine:
         self._observer = OBSERVER(forward)  # kept alive as long as the engine can call it
         return self._check(lib().mbir_set_observer(self._h, C.cast(self._observer, C.c_void_p),
                                                    None))
+
+    def write_checkpoint(self, directory):
+        """HAADF: the run's state in `directory` (the reference's .bin files + Checkpoint.bin)."""
+        return self._check(lib().mbir_write_checkpoint(self._h, str(directory).encode()))
+
+    def read_checkpoint(self, directory):
+        """HAADF: start every later prepare from a checkpoint of the same configuration and
+        series; run() continues at its outer iteration."""
+        return self._check(lib().mbir_read_checkpoint(self._h, str(directory).encode()))
 
     def load_bright_field_mrc(self, path):
         return self._check(lib().mbir_load_bright_field_mrc(self._h, str(path).encode()))
