@@ -335,7 +335,11 @@ int32_t mbir_read_checkpoint(mbir_engine* e, const char* dir);
  * "Starting Forward Projection" (10, progress value and message) from prepare, the path of each
  * intermediate image (0, intermediate image), "Reconstruction Complete" (100, progress value
  * and message) at the end of mbir_run, and the text of every error it returns (100, error
- * message; the same text as mbir_last_error).  fn runs on the thread of the entry point that
+ * message; the same text as mbir_last_error).  mbir_run also sends after every outer iteration
+ * one line of metrics as a JSON object (progress = the share of outer_iterations done, progress
+ * message): {"outer", "sweeps" (ICD calls so far), "rel_update" (the last sweep's
+ * sum|dx| / sum|x| over the ROI), "cost" (the last FP64 cost, null when none was computed),
+ * "voxels_updated", "icd_ms" (both so far)}.  fn runs on the thread of the entry point that
  * sends the message, must not throw, and must not call the same engine except mbir_cancel,
  * mbir_status_get and mbir_last_error.  fn = NULL removes the observer. */
 #define MBIR_UPDATE_PROGRESS_VALUE 0

@@ -186,6 +186,22 @@ void Engine::notify(const std::string& msg, int progress, int aspect) const {
   if (observer_) observer_(msg.c_str(), progress, aspect, observer_user_);
 }
 
+// The run's metrics after outer iteration `outer`, as one JSON object: sweeps (ICD calls) so
+// far, the last sweep's sum|dx| / sum|x| over the ROI, the last FP64 cost (null when none was
+// computed), voxel updates and ICD device time so far
+void Engine::notify_iteration(int outer) const {
+  if (!observer_) return;
+  char cost[40] = "null";
+  if (std::isfinite(last_cost_)) std::snprintf(cost, sizeof cost, "%.17g", last_cost_);
+  char buf[320];
+  std::snprintf(buf, sizeof buf,
+                "{\"outer\": %d, \"sweeps\": %d, \"rel_update\": %.9g, \"cost\": %s, "
+                "\"voxels_updated\": %lld, \"icd_ms\": %.3f}",
+                outer, sweeps_done_, last_rel_, cost, static_cast<long long>(updated_), icd_ms_);
+  const int n = std::max(1, p_.outer_iterations);
+  notify(buf, std::min(100, 100 * (outer + 1) / n), MBIR_UPDATE_PROGRESS_MESSAGE);
+}
+
 int Engine::cuda_check(int code, const char* what) {
   if (code == 0) return 0;
   cudaError_t e = cudaGetLastError();
@@ -1422,6 +1438,7 @@ int Engine::run() {
     if (p_.noise_model && (rc = update_weights())) return rc;
     outer_next_ = outer + 1;
     stop_now_ = stop;
+    notify_iteration(outer);
     if (status == 0 && outer >= 1) break;
   }
   state_ = 4;

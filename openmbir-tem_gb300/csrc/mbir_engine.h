@@ -92,6 +92,7 @@ class Engine {
   int write_checkpoint(const char* dir);
   int read_checkpoint(const char* dir);
   void notify(const std::string& msg, int progress, int aspect) const;
+  void notify_iteration(int outer) const;  // one JSON line per completed outer iteration
   int write_volume_mrc(const std::string& path);
   template <typename T>
   int set_initial_volume_t(const T* vol, int64_t n);

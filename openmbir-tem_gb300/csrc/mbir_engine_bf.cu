@@ -767,11 +767,15 @@ int Engine::bf_run() {
         bragg_t_ = temp_t;
       }
     }
-    if (status == 0 && outer >= 1) break;
+    if (status == 0 && outer >= 1) {
+      notify_iteration(outer);
+      break;
+    }
     if (p_.outer_iterations > 1) {
       if (p_.joint_estimation && (rc = bf_joint_estimation())) return rc;
       if (p_.noise_estimation && (rc = bf_update_weights())) return rc;
     }
+    notify_iteration(outer);
   }
   return MBIR_OK;
 }
