@@ -460,9 +460,10 @@ class MultiResolutionReconstruction {
         eng->setInitialVolume(prev);
         eng->setInitialNuisance(g, o, v);
       }
-      message(std::to_string(interp >> i) + "x: reconstructing " + std::to_string(d[0]) + " x " +
-              std::to_string(d[1]) + " x " + std::to_string(d[2]) + " voxels (z, x, y) from " +
-              std::to_string(d[3]) + " views");
+      if (rc == MBIR_OK)
+        message(std::to_string(interp >> i) + "x: reconstructing " + std::to_string(d[0]) +
+                " x " + std::to_string(d[1]) + " x " + std::to_string(d[2]) +
+                " voxels (z, x, y) from " + std::to_string(d[3]) + " views");
       // the HAADF program's intermediate images, <outer>_<inner>_ReconstructedVolume.rec
       if (rc == MBIR_OK && !bf) eng->setIntermediateDir(level_dir);
       if (rc == MBIR_OK) rc = eng->execute();
