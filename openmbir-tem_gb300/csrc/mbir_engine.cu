@@ -1675,8 +1675,11 @@ int Engine::read_checkpoint(const char* dir) {
     std::fclose(f);
     return fail(MBIR_EIO, path + " is not a checkpoint");
   }
+  // the error sinogram's size follows from the series: rows padded as alloc_device pads them
+  const int32_t n_rp = (g.n_r + 3) / 4 * 4;
+  const uint64_t e_bytes = static_cast<uint64_t>(g.n_t) * g.n_theta * n_rp * rb_;
   if (std::memcmp(v, want, sizeof want) != 0 || v[kCkElem] != static_cast<int32_t>(rb_) ||
-      v[kCkOuterNext] < 0 || v[kCkSweeps] < 0 || h.e_bytes > (uint64_t(1) << 40)) {
+      v[kCkNrp] != n_rp || v[kCkOuterNext] < 0 || v[kCkSweeps] < 0 || h.e_bytes != e_bytes) {
     std::fclose(f);
     return fail(MBIR_EINVAL, "checkpoint: written by an engine of another configuration or series");
   }
