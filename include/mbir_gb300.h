@@ -339,9 +339,10 @@ int32_t mbir_read_checkpoint(mbir_engine* e, const char* dir);
  * one line of metrics as a JSON object (progress = the share of outer_iterations done, progress
  * message): {"outer", "sweeps" (ICD calls so far), "rel_update" (the last sweep's
  * sum|dx| / sum|x| over the ROI), "cost" (the last FP64 cost, null when none was computed),
- * "voxels_updated", "icd_ms" (both so far)}.  fn runs on the thread of the entry point that
- * sends the message, must not throw, and must not call the same engine except mbir_cancel,
- * mbir_status_get and mbir_last_error.  fn = NULL removes the observer. */
+ * "voxels_updated", "icd_ms" (both so far)}.  fn runs on the thread that does the engine's
+ * work: the caller's, or for an engine in a batch or a server, one of their threads.  It must not
+ * throw, and must not call the same engine except mbir_cancel, mbir_status_get and
+ * mbir_last_error.  fn = NULL removes the observer. */
 #define MBIR_UPDATE_PROGRESS_VALUE 0
 #define MBIR_UPDATE_PROGRESS_MESSAGE 1
 #define MBIR_UPDATE_WARNING_MESSAGE 2
