@@ -413,29 +413,13 @@ class MultiResolutionReconstruction {
       return fail(MBIR_EIO, "Error creating the output directory '" + out_dir +
                                 "'\n   Exiting Now.");
     const bool bf = p_.modality == MBIR_MODALITY_BF;
-    const int levels = p_.num_resolutions > 0 ? p_.num_resolutions : 1;
-    const int interp = (1 << (levels - 1)) * std::max(1, p_.final_resolution);
-    const double pq = static_cast<double>(static_cast<float>(p_.diffuseness) + 1.0f);
+    const int levels = numberOfLevels();
     std::vector<double> prev, g, o, v;
     std::vector<std::string> temp_files;
     for (int i = 0; i < levels; ++i) {
       if (cancel_.load()) return fail(MBIR_ECANCELLED, "cancelled");
-      mbir_params q = p_;
-      q.level = i;
-      q.qggmrf_q = pq;
-      q.sigma_x = std::pow(2.0, (levels - 1 - i) * (1 - 3 / pq)) *
-                  static_cast<double>(static_cast<float>(p_.sigma_x));
-      if (i > 0) {
-        q.inner_iterations = 1;
-        // later levels take the nuisance and the volume from the level before
-        q.default_recon_value = 0.0;
-        q.default_variance = 1.0;
-        q.use_default_offset = 0;
-        q.default_offset = 0.0;
-      }
-      if (i >= 2) q.stop_threshold = static_cast<float>(p_.stop_threshold) * 2.0f;
-      q.interpolate_initial_recon = i == 0 ? (interpolate_ ? 1 : 0) : 1;
-      const std::string level_dir = out_dir + "/" + std::to_string(interp >> i) + "x";
+      const mbir_params q = levelParams(i);
+      const std::string level_dir = out_dir + "/" + std::to_string(levelFactor(i)) + "x";
       if (!detail::make_dirs(level_dir)) return fail(MBIR_EIO, "Could not create path: " + level_dir);
       auto eng = std::make_shared<ReconstructionEngine>(q.modality);
       eng->setParams(q);
@@ -461,7 +445,7 @@ class MultiResolutionReconstruction {
         eng->setInitialNuisance(g, o, v);
       }
       if (rc == MBIR_OK)
-        message(std::to_string(interp >> i) + "x: reconstructing " + std::to_string(d[0]) +
+        message(std::to_string(levelFactor(i)) + "x: reconstructing " + std::to_string(d[0]) +
                 " x " + std::to_string(d[1]) + " x " + std::to_string(d[2]) +
                 " voxels (z, x, y) from " + std::to_string(d[3]) + " views");
       // the HAADF program's intermediate images, <outer>_<inner>_ReconstructedVolume.rec
@@ -490,7 +474,7 @@ class MultiResolutionReconstruction {
       for (int k = 0; k < 3; ++k) dims_[k] = d[k];
       mbir_status st{};
       eng->getStatus(st);
-      message(std::to_string(interp >> i) + "x: " + std::to_string(st.sweeps_done) +
+      message(std::to_string(levelFactor(i)) + "x: " + std::to_string(st.sweeps_done) +
               " ICD calls, " + std::to_string(static_cast<long long>(st.voxels_updated)) +
               " voxel updates, ICD device time " + fixed1(st.icd_ms_total) + " ms");
     }
@@ -505,6 +489,35 @@ class MultiResolutionReconstruction {
     offsets_ = std::move(o);
     variances_ = std::move(v);
     return MBIR_OK;
+  }
+
+  /* the levels execute() runs, and the parameters of level i (0 = coarsest): the settings
+   * above with the per-level rules of HAADF_MultiResolutionReconstruction.cpp:318-357 */
+  int numberOfLevels() const { return p_.num_resolutions > 0 ? p_.num_resolutions : 1; }
+  /* voxel size of level i in detector pixels, the name of its directory (<factor>x) */
+  int levelFactor(int i) const {
+    return ((1 << (numberOfLevels() - 1)) * std::max(1, p_.final_resolution)) >> i;
+  }
+  mbir_params levelParams(int i) const {
+    const int levels = numberOfLevels();
+    // p = diffuseness + 1 in float, as the pipeline computes it
+    const double pq = static_cast<double>(static_cast<float>(p_.diffuseness) + 1.0f);
+    mbir_params q = p_;
+    q.level = i;
+    q.qggmrf_q = pq;
+    q.sigma_x = std::pow(2.0, (levels - 1 - i) * (1 - 3 / pq)) *
+                static_cast<double>(static_cast<float>(p_.sigma_x));
+    if (i > 0) {
+      q.inner_iterations = 1;
+      // later levels take the nuisance and the volume from the level before
+      q.default_recon_value = 0.0;
+      q.default_variance = 1.0;
+      q.use_default_offset = 0;
+      q.default_offset = 0.0;
+    }
+    if (i >= 2) q.stop_threshold = static_cast<float>(p_.stop_threshold) * 2.0f;
+    q.interpolate_initial_recon = i == 0 ? (interpolate_ ? 1 : 0) : 1;
+    return q;
   }
 
   /* after execute(): N_z, N_x, N_y of the final level, its volume [z][x][y] and nuisance */

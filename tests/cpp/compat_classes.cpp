@@ -10,6 +10,8 @@
 //       second equals it and how many "Reconstruction Complete" messages the observer saw
 //   compat_classes cancel <counts.f32> <tilts.f32> n_theta n_r n_t thickness
 //       setCancel(true) from another thread once the first sweep is done
+//   compat_classes levels
+//       the per-level parameters of a three-level pipeline
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -78,6 +80,31 @@ int errors(const std::string& dir) {
   return 0;
 }
 
+int levels() {
+  mbir_gb300::HAADF_MultiResolutionReconstruction m;
+  m.setNumberResolutions(3);
+  m.setFinalResolution(2);
+  m.setSigmaX(0.3);
+  m.setMRFShapeParameter(0.2);
+  m.setStopThreshold(0.005);
+  m.setInnerIterations(10);
+  m.setOuterIterations(7);
+  m.setDefaultVariance(2.0);
+  m.setInitialReconstructionValue(0.5);
+  m.setDefaultOffsetValue(0.1);
+  m.setUseDefaultOffset(true);
+  m.setInterpolateInitialReconstruction(false);
+  for (int i = 0; i < m.numberOfLevels(); ++i) {
+    const mbir_params q = m.levelParams(i);
+    std::printf("level%d %d %d %d %d %d %d %d\n", i, q.level, m.levelFactor(i), q.inner_iterations,
+                q.outer_iterations, q.use_default_offset, q.interpolate_initial_recon,
+                q.float_params);
+    std::printf("level%d_f %.17g %.17g %.17g %.17g %.17g %.17g\n", i, q.sigma_x, q.qggmrf_q,
+                q.stop_threshold, q.default_recon_value, q.default_variance, q.default_offset);
+  }
+  return 0;
+}
+
 int run(char** argv, bool cancel) {
   const int n_theta = std::atoi(argv[4]), n_r = std::atoi(argv[5]), n_t = std::atoi(argv[6]);
   const double thickness = std::atof(argv[7]);
@@ -140,8 +167,9 @@ int run(char** argv, bool cancel) {
 
 int main(int argc, char** argv) {
   if (argc >= 3 && std::strcmp(argv[1], "errors") == 0) return errors(argv[2]);
+  if (argc >= 2 && std::strcmp(argv[1], "levels") == 0) return levels();
   if (argc >= 9 && std::strcmp(argv[1], "run") == 0) return run(argv, false);
   if (argc >= 8 && std::strcmp(argv[1], "cancel") == 0) return run(argv, true);
-  std::fprintf(stderr, "usage: compat_classes errors|run|cancel ...\n");
+  std::fprintf(stderr, "usage: compat_classes errors|levels|run|cancel ...\n");
   return 2;
 }

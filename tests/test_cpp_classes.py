@@ -4,7 +4,7 @@ the test program tests/cpp/compat_classes.cpp.
 
 CPU: the header compiles and links against the library; error conditions without a GPU (an
 engine with no sinogram, results read before a load, an output directory that cannot be made, a
-cancel set before execute() gives the reference's -999).  GPU: an engine run from arrays gives
+cancel set before execute() gives the reference's -999); the pipeline's per-level parameters.  GPU: an engine run from arrays gives
 the same volume, bit for bit, as the C ABI run with the same parameters, twice on the same
 object, with the observer seeing each run complete; setCancel(true) from another thread ends a
 long run with -999.  The pipeline classes' GPU runs are the command-line programs' tests
@@ -41,7 +41,7 @@ def run(exe, *args):
     out = {}
     for line in r.stdout.splitlines():
         k, *v = line.split()
-        out[k] = [int(x) for x in v]
+        out[k] = [float(x) if k.endswith("_f") else int(x) for x in v]
     return r, out
 
 
@@ -54,6 +54,29 @@ def test_classes_error_paths(compat_exe, tmp_path):
     assert rc in (MBIR_EDEVICE, MBIR_ESTATE) and cond == rc and has_msg == 1
     assert out["output_dir"] == [MBIR_EIO, MBIR_EIO, 1]
     assert out["cancel_before"] == [MBIR_ECANCELLED, 1]
+
+
+def test_pipeline_level_parameters(compat_exe):
+    """The per-level rules of HAADF_MultiResolutionReconstruction.cpp:318-357 for three levels:
+    voxels of 2^(L-1-i) * final_resolution pixels, p = diffuseness + 1 in float, sigma_x scaled
+    by 2^((L-1-i)(1-3/p)), the inner iterations and the default volume, variance and offset on
+    the first level only, the stop threshold doubled (in float) from the third level, the
+    previous level's volume interpolated from the second level."""
+    r, out = run(compat_exe, "levels")
+    assert r.returncode == 0, r.stdout + r.stderr
+    L = 3
+    f32 = np.float32
+    p = float(f32(0.2) + f32(1.0))
+    for i in range(L):
+        level, factor, inner, outer, use_off, interp, float_params = out[f"level{i}"]
+        assert (level, factor, outer, float_params) == (i, 2 ** (L - 1 - i) * 2, 7, 1)
+        assert inner == (10 if i == 0 else 1)
+        assert use_off == (1 if i == 0 else 0) and interp == (0 if i == 0 else 1)
+        sigma, q, stop, recon, var, off = out[f"level{i}_f"]
+        assert q == p
+        assert sigma == 2.0 ** ((L - 1 - i) * (1 - 3 / p)) * float(f32(0.3))
+        assert stop == (float(f32(0.005) * f32(2.0)) if i >= 2 else 0.005)
+        assert (recon, var, off) == ((0.5, 2.0, 0.1) if i == 0 else (0.0, 1.0, 0.0))
 
 
 def small_inputs(tmp_path):
