@@ -20,6 +20,13 @@ oracle/_ref) and runs them through oracle/refrun.py on seeded synthetic inputs:
 * bf_multires_small.npz -- the reduced bright-field case with 12 detector rows over two
   resolution levels (coarse 2x, then 1x), 2 outer iterations with 2 inner calls at the coarse
   level;
+* shepp_logan.npz -- the reference's own input fixture (Resources/InputFiles/
+  ScheppLoganSinogram128NoiselessLimitedAngle.bin, 87 views over +-70 deg at 1 deg steps near
+  the ends and 2 deg in the middle, as ParamsWithROIAndViewSelectShepLogan.txt lists them; 128
+  x 3 detector) reconstructed with thickness 32 from the fixture's offsets (0, the default
+  offset; the offset the reference estimates from this noiseless sinogram's view means leaves
+  an all-zero first sweep and NaN gains), 3 outer iterations with gain/offset and variance
+  estimation;
 * haadf_cfg0.json -- the benchmark's small HAADF configuration (128 x 32 detector, 71 views over
   +-70 deg at 2 deg, thickness 32, volume 128 x 32 x 64): SHA-256 digests and sums of the
   inputs and of the reference's float64 outputs after 1, 5 and 20 outer iterations.
@@ -28,7 +35,7 @@ Every run uses one worker and a frozen clock seed (refrun.py explains both).  Th
 small cases are stored with their outputs; the cfg0 input is regenerated from its seed and
 checked against its stored digest.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [fixture ...]   (default: all; names without suffix)
 """
 import hashlib
 import json
@@ -102,6 +109,30 @@ def haadf_small(tmp):
                         it5_offset=it5["offset"])
 
 
+def shepp_logan_input(reference=refrun.DEFAULT_REFERENCE):
+    """The reference's Shepp-Logan sinogram (float64 [theta][r][t], 87 x 128 x 3) as float32
+    counts, and its tilt angles (the parameter file lists each angle followed by its selection
+    flag, all 1)."""
+    d = os.path.join(reference, "Resources", "InputFiles")
+    sino = np.fromfile(os.path.join(d, "ScheppLoganSinogram128NoiselessLimitedAngle.bin"), "<f8")
+    with open(os.path.join(d, "ParamsWithROIAndViewSelectShepLogan.txt")) as f:
+        text = f.read()
+    body = text.split("SinoAngles", 1)[1].split("Geom", 1)[0].split()
+    angles = np.array([float(a) for a in body[0::2]], np.float32)
+    assert angles.size == 87 and all(v == "1" for v in body[1::2])
+    return sino.reshape(87, 128, 3).astype(np.float32), angles
+
+
+def shepp_logan(tmp):
+    y, ang = shepp_logan_input()
+    th = 32.0
+    out = refrun.run_haadf(os.path.join(tmp, "sl"), y, ang, th, 0.1, 0.2, 3, seed=HAADF_SEED,
+                           extra=("--use_default_offset", "--default_offset", "0"))
+    np.savez_compressed(os.path.join(HERE, "shepp_logan.npz"), counts=y, tilts=ang,
+                        thickness=th, it3_object_yxz=out["object_yxz"], it3_gain=out["gain"],
+                        it3_offset=out["offset"])
+
+
 def haadf_bf_assist_small(tmp):
     """The reduced HAADF case with a bright-field tilt series of the same size (--brightfield):
     5 outer iterations."""
@@ -168,13 +199,13 @@ def main():
     if not refrun.ensure_built():
         print("make_golden: the reference programs are not available", file=sys.stderr)
         return 1
+    makers = [haadf_small, output_headers, bf_small, haadf_cfg0, haadf_bf_assist_small,
+              bf_multires_small, shepp_logan]
+    wanted = set(sys.argv[1:])
     with tempfile.TemporaryDirectory() as tmp:
-        haadf_small(tmp)
-        output_headers(tmp)
-        bf_small(tmp)
-        haadf_cfg0(tmp)
-        haadf_bf_assist_small(tmp)
-        bf_multires_small(tmp)
+        for make in makers:
+            if not wanted or make.__name__ in wanted:
+                make(tmp)
     for f in sorted(os.listdir(HERE)):
         print(f, os.path.getsize(os.path.join(HERE, f)))
     return 0

@@ -13,7 +13,9 @@ pow as the reference uses, reproduces them bit for bit:
   small HAADF configuration after 1, 5 and 20 outer iterations (SHA-256 of the float64
   outputs);
 * bright field after 42 NHICD calls (Bragg schedule, homogeneous and non-homogeneous lists,
-  offset, variance and selector updates).
+  offset, variance and selector updates);
+* HAADF after 3 outer iterations on the reference's own input fixture, the noiseless
+  limited-angle Shepp-Logan sinogram (87 views with 1 and 2 degree steps, 128 x 3 detector).
 
 Where the reference tree is present the programs are also run live, on other seeds and
 schedules, and compared the same way.
@@ -70,6 +72,23 @@ def test_haadf_five_outer_iterations_bitwise(oracle_mod):
     np.testing.assert_array_equal(orc.volume(), ref)
     np.testing.assert_array_equal(orc.gain(), g["it5_gain"])
     np.testing.assert_array_equal(orc.offset(), g["it5_offset"])
+
+
+def test_haadf_shepp_logan_fixture_bitwise(oracle_mod):
+    """The reference's Resources/InputFiles Shepp-Logan sinogram and tilt list (non-uniform
+    steps), from its fixture offsets of 0: volume, gains and offsets after 3 outer iterations."""
+    g = load("shepp_logan.npz")
+    o = refrun.haadf_params(float(g["thickness"]), 0.1, 0.2, 3, use_default_offset=True,
+                            default_offset=0.0)
+    orc = oracle_mod.Oracle(o, g["counts"], g["tilts"], refrun.REF_DELTA, refrun.REF_DELTA)
+    orc.prepare()
+    assert orc.run(12345)[0] == 3
+    ny, nx, nz = orc.ny, orc.nx, orc.nz
+    assert (ny, nx, nz) == (3, 128, 64)
+    ref = np.transpose(g["it3_object_yxz"].reshape(ny, nx, nz), (2, 1, 0))
+    np.testing.assert_array_equal(orc.volume(), ref)
+    np.testing.assert_array_equal(orc.gain(), g["it3_gain"])
+    np.testing.assert_array_equal(orc.offset(), g["it3_offset"])
 
 
 def test_haadf_with_bright_field_five_outer_iterations_bitwise(oracle_mod):
