@@ -314,11 +314,12 @@ int32_t mbir_write_outputs_ex(mbir_engine* e, const char* dir, const char* mrc_p
 int32_t mbir_set_intermediate_dir(mbir_engine* e, const char* dir);
 
 /* Checkpoint and exact resume of a HAADF run (without bright-field data).  mbir_write_checkpoint
- * (after mbir_run or between step-wise phases) writes to `dir` the reference's level hand-off
- * files ReconstructedObject.bin, Final{Gain,Offset}Parameters.bin and FinalVariances.bin
- * (HAADF_MultiResolutionReconstruction.cpp:212-222 reads them back; InitialReconstructionBinReader.cpp:
- * 73-168) plus ReconstructedSinogram.bin and Checkpoint.bin (the outer iterations mbir_run has
- * completed, the sweeps done, the stop threshold after its reductions and the error sinogram).
+ * (after mbir_run or between step-wise phases) writes to `dir` (an existing directory) the
+ * reference's level hand-off files ReconstructedObject.bin, Final{Gain,Offset}Parameters.bin and
+ * FinalVariances.bin (HAADF_MultiResolutionReconstruction.cpp:212-222 reads them back;
+ * InitialReconstructionBinReader.cpp:73-168) plus ReconstructedSinogram.bin and Checkpoint.bin
+ * (the outer iterations mbir_run has completed, the sweeps done, the stop threshold after its
+ * reductions and the error sinogram).
  * mbir_read_checkpoint, on an engine created with the same parameters and given the same series
  * (after mbir_set_sinogram / mbir_load_sinogram_mrc), makes every later prepare start from that
  * state, and mbir_run continues at the checkpoint's outer iteration up to outer_iterations: a
